@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""Benchmark: ray segments per second of the GB300 path-trace hot path.
+
+Workload (the triangle+analytic configuration): 1920x1080, 1 spp x 64
+accumulated frames, max depth 8; 200 displaced geodesic icospheres (9,680 tris
+each) on a 512x512 quad-grid ground (2,460,288 triangles), 1,024 analytic
+spheres, 2048x1024 log-normal env map with a 0.5 deg sun disc of 1e4 (extracted
+as an HDRI light), 256 materials.  Seeded synthetic data of those shapes.
+
+One step = the 64-frame accumulation (reset on the first frame).  `value` =
+(extension + shadow segments) / device time of the K timed steps, inputs
+resident in HBM.  `e2e` = the same through pt_gpu_render_to_host: per-frame
+push data in from the host and the RGBA32F accumulation buffer copied back to
+pinned host memory inside the timed region.  The scene buffers (~250 MB) stay
+resident across steps, as they do across frames in the reference engine.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "demont-engine_gb300")
+METRIC = "Mrays/s (ray segments: extension + shadow)"
+W_FULL, H_FULL, FRAMES = 1920, 1080, 64
+
+
+def load_pkg():
+    spec = importlib.util.spec_from_file_location("demont_gb300", os.path.join(PKG, "__init__.py"),
+                                                  submodule_search_locations=[PKG])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["demont_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms (read-only)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def extend_traffic_per_ray():
+    """DRAM bytes per extension segment of k_extend from the committed ncu
+    summary (profiles/k_extend_c1.md, line `dram_bytes_per_extension_segment: X`)."""
+    p = os.path.join(ROOT, "profiles", "k_extend_c1.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_extension_segment:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def algorithmic_bytes(pt, orc, scene, head, prm):
+    """B_seg = 32 (ray) + 16 (hit) + 32 N_node + 52 N_tri + 112 N_prim per extension
+    segment, N from the oracle walking the reference binary BVH on a crop of frame 0."""
+    _, c = orc.render(scene.packed(), head, prm, W_FULL, H_FULL, 1, crop=(704, 396, 1216, 684))
+    n = max(c.ext_rays, 1)
+    nn, nt, npr = c.ext_nodes / n, c.ext_tris / n, c.ext_prims / n
+    return 32 + 16 + 32 * nn + 52 * nt + 112 * npr, {"nodes": nn, "tris": nt, "prims": npr,
+                                                       "sample_segments": int(c.ext_rays)}
+
+
+def cpu_baseline(pt, orc, scene, head, prm, budget_s=12.0):
+    """fp32 oracle (the reference-semantics CPU port) on whole frames of the
+    same workload, all host threads, about `budget_s` seconds."""
+    cores = os.cpu_count() or 1
+    acc = np.zeros((H_FULL, W_FULL, 4), np.float32)
+    segs, t_used, rows = 0, 0.0, 0
+    y = 0
+    band = 72
+    while t_used < budget_s and y < H_FULL:
+        t0 = time.perf_counter()
+        _, c = orc.render(scene.packed(), head, prm, W_FULL, H_FULL, 1, accum=acc,
+                          crop=(0, y, W_FULL, min(H_FULL, y + band)), threads=cores)
+        t_used += time.perf_counter() - t0
+        segs += c.ext_rays + c.shadow_rays
+        rows += min(H_FULL, y + band) - y
+        y += band
+    return {"value": segs / t_used / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+            "sample": f"frame 0 of the workload, rows 0..{rows} of 1080 (1920 wide), 1 spp, "
+                      f"{segs} segments in {t_used:.1f} s"}
+
+
+def run_reference(args):
+    """The reference's CPU implementation of this path is its Slang shader
+    (not runnable: no Slang/Vulkan/Metal here) and a reduced Software preview
+    tracer that needs Embree + glm (absent); the timed reference arm is
+    therefore the oracle's fp32 restatement of the shader on the host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, ROOT)
+    pt = load_pkg()
+    import oracle as orc
+    orc.load()
+    scene = pt.Scene().synth(1, seed=0)
+    head, prm = scene.push(W_FULL, H_FULL, 0, 1)
+    cores = os.cpu_count() or 1
+    band = 120
+    acc = np.zeros((H_FULL, W_FULL, 4), np.float32)
+
+    def step(i):
+        y = (i * band) % H_FULL
+        t0 = time.perf_counter()
+        _, c = orc.render(scene.packed(), head, prm, W_FULL, H_FULL, 1, accum=acc,
+                          crop=(0, y, W_FULL, y + band), threads=cores)
+        return time.perf_counter() - t0, c.ext_rays + c.shadow_rays
+
+    for i in range(args.warmup):
+        step(i)
+    tt, ss = 0.0, 0
+    for i in range(args.steps):
+        t, s = step(args.warmup + i)
+        tt += t
+        ss += s
+    v = ss / tt / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "triangles+analytic 1920x1080 1spp x64 frames depth 8 (2,460,288 tris, "
+                                   "1024 spheres, 2048x1024 env)", "step": f"1920x{band} band of one frame"},
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": f"1920x{band} bands of frame 0, {ss} segments over {args.steps} steps"},
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=FRAMES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, world, local = dist_env()
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+    sys.path.insert(0, ROOT)
+    pt = load_pkg()
+    scene = pt.Scene().synth(1, seed=0)
+    dev = pt.Device(local)
+    dev.upload(scene)
+    dev.set_target(W_FULL, H_FULL)
+    # replicas: each rank renders its own disjoint frame range of the same workload
+    head, prm = scene.push(W_FULL, H_FULL, frame_index=rank * 1_000_000, reset=1)
+
+    def barrier():
+        if pg:
+            import torch
+            torch.cuda.synchronize()
+            pg.barrier()
+
+    dev.set_profiling(True)
+    for _ in range(args.warmup):
+        dev.render(head, prm, args.frames)
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_dev, segs, ext, ext_ms, ext_launch, launches = 0.0, 0, 0, 0.0, 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dev.render(head, prm, args.frames)
+        st = dev.stats()
+        t_dev += st.gpu_ms / 1e3
+        segs += st.extension_rays + st.shadow_rays
+        ext += st.extension_rays
+        ext_ms += st.extend_ms
+        ext_launch += st.extend_launches
+        launches += st.waves * (2 + head.spp) + 4 * st.extend_launches
+    t_wall = time.perf_counter() - t0
+    barrier()
+    clk = clocks.stop()
+
+    # end to end through the C-ABI with host buffers (pinned when torch can pin)
+    dev.set_profiling(False)
+    try:
+        import torch
+        host = torch.empty((H_FULL, W_FULL, 4), dtype=torch.float32, pin_memory=True).numpy()
+    except Exception:
+        host = np.empty((H_FULL, W_FULL, 4), np.float32)
+    dev.render_to_host(head, prm, args.frames, host)
+    barrier()
+    t1 = time.perf_counter()
+    e2e_segs = 0
+    for _ in range(args.steps):
+        dev.render_to_host(head, prm, args.frames, host)
+        st = dev.stats()
+        e2e_segs += st.extension_rays + st.shadow_rays
+    t_e2e = time.perf_counter() - t1
+    barrier()
+
+    if pg:
+        import torch
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        ss = torch.tensor([segs, e2e_segs], dtype=torch.float64, device="cuda")
+        pg.all_reduce(ss, op=pg.ReduceOp.SUM)
+        t_dev, t_e2e = tt.tolist()
+        segs, e2e_segs = ss.tolist()
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return 0
+
+    import oracle as orc
+    orc.load()
+    bseg, nbar = algorithmic_bytes(pt, orc, scene, head, prm)
+    peak, peak_kind = measured_peak()
+    ext_s = ext_ms / 1e3
+    achieved = (ext * bseg / ext_s / 1e9) if ext_s > 0 else None
+    tpr = extend_traffic_per_ray()
+    per_launch_rays = ext / max(ext_launch, 1)
+    roofline = {"bound": "hbm", "kernel": "k_extend (closest hit)", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                "traffic": (tpr * per_launch_rays) if tpr else None,
+                "algorithmic_bytes_per_launch": bseg * per_launch_rays,
+                "avg_launch_ms": ext_ms / max(ext_launch, 1), "launches": ext_launch,
+                "B_seg": bseg, "N_per_segment": nbar, "peak_kind": peak_kind}
+    line = {"metric": METRIC, "value": segs / t_dev / 1e6, "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+            "wall_ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "triangles+analytic 1920x1080 1spp x64 frames depth 8 (2,460,288 tris, "
+                                   "1024 spheres, 2048x1024 env)", "frames_per_step": args.frames,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "no flush: per-wave path state (~6 GB) and scene (~250 MB) exceed the 129 MB L2"},
+            "e2e": {"value": e2e_segs / t_e2e / 1e6, "unit": "Mrays/s",
+                    "h2d_bytes_per_step": args.frames * (ctypes.sizeof(pt.PtPushHead) + ctypes.sizeof(pt.PtPathParams)),
+                    "d2h_bytes_per_step": W_FULL * H_FULL * 16},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "clocks": clk}
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pt, orc, scene, head, prm)
+    print(json.dumps(line), flush=True)
+    dev.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

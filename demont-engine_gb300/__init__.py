@@ -1,0 +1,381 @@
+"""Python mirror of the GB300 path-trace C-ABI (include/pt_gpu.h, include/pt_scene.h).
+
+The product is the shared library ``_build/libdemont_pt.so`` (CUDA kernels for
+sm_103a + the C++ host scene builder).  This module only binds it with ctypes
+and wraps buffers as numpy arrays; it never computes anything itself, and it
+raises when the library is missing instead of falling back to anything.
+
+The directory name contains a hyphen, so it is loaded by path::
+
+    import importlib.util, sys
+    spec = importlib.util.spec_from_file_location(
+        "demont_gb300", "demont-engine_gb300/__init__.py",
+        submodule_search_locations=["demont-engine_gb300"])
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdemont_pt.so")
+
+PT_OK = 0
+ERRORS = {-1: "PT_ERR_INVALID", -2: "PT_ERR_CUDA", -3: "PT_ERR_OOM", -4: "PT_ERR_STATE",
+          -5: "PT_ERR_KERNEL", -6: "PT_ERR_UNSUPPORTED"}
+HIT_MISS = 0xFFFFFFFF
+HIT_TRI = 1 << 30
+
+u32 = ctypes.c_uint32
+f32 = ctypes.c_float
+P = ctypes.POINTER
+
+
+class PtPushHead(ctypes.Structure):
+    _fields_ = [("pos_fovtan", f32 * 4), ("fwd_aspect", f32 * 4), ("right_xyz", f32 * 4),
+                ("up_xyz", f32 * 4), ("frame_index", u32), ("reset_accum", u32),
+                ("max_bounces", u32), ("tlas_present", u32), ("prim_count", u32), ("spp", u32),
+                ("denoiser_enabled", u32), ("env_map_present", u32), ("halton_jitter", f32 * 2),
+                ("env_intensity", f32), ("env_total_luminance", f32)]
+
+
+class PtPathParams(ctypes.Structure):
+    _fields_ = [("refract_budget", f32), ("firefly_clamp", f32), ("mis_enabled", u32),
+                ("accum_ema_alpha", f32), ("bvh_params", u32 * 4), ("light_count", u32),
+                ("light_tree_enabled", u32), ("light_tree_node_count", u32), ("rr_start", u32),
+                ("sun_and_mode", f32 * 4), ("reserved", u32 * 4)]
+
+
+class PtBvhNode(ctypes.Structure):
+    _fields_ = [("aabb_min", f32 * 3), ("left_first", u32), ("aabb_max", f32 * 3), ("count", u32)]
+
+
+class PtStats(ctypes.Structure):
+    _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
+                ("paths", ctypes.c_uint64), ("frames", u32), ("waves", u32), ("gpu_ms", ctypes.c_double),
+                ("extend_ms", ctypes.c_double), ("shadow_ms", ctypes.c_double),
+                ("extend_launches", u32), ("shadow_launches", u32)]
+
+
+class PtPackedScene(ctypes.Structure):
+    _fields_ = [("prims", P(f32)), ("prim_count", u32), ("linear_prim_count", u32),
+                ("bvh_nodes", P(PtBvhNode)), ("bvh_node_count", u32),
+                ("positions", P(f32)), ("vertex_count", u32), ("indices", P(u32)), ("tri_count", u32),
+                ("tri_nodes", P(PtBvhNode)), ("tri_node_count", u32), ("tri_perm", P(u32)),
+                ("tri_perm_count", u32), ("tri_mat_ids", P(u32)), ("materials", P(f32)),
+                ("material_count", u32), ("lights", P(f32)), ("light_count", u32),
+                ("env_rgba", P(f32)), ("env_w", u32), ("env_h", u32), ("env_marginal", P(f32)),
+                ("env_conditional", P(f32)), ("env_total_luminance", ctypes.c_double),
+                ("hdri_count", u32), ("hdri_dir_pmf", P(f32)), ("hdri_col", P(f32)),
+                ("env_present", u32)]
+
+
+# every entry point include/*.h declares, with its ctypes signature
+SIGNATURES = {
+    # pt_gpu.h
+    "pt_gpu_create": (ctypes.c_int, [P(ctypes.c_void_p), ctypes.c_int]),
+    "pt_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pt_gpu_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "pt_gpu_version": (ctypes.c_char_p, []),
+    "pt_gpu_upload_prims": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32, P(PtBvhNode), u32]),
+    "pt_gpu_upload_mesh": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, P(u32), u32, P(PtBvhNode), u32,
+                                          P(u32), u32, P(u32)]),
+    "pt_gpu_upload_materials": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
+    "pt_gpu_upload_lights": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
+    "pt_gpu_upload_env": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32, P(f32), P(f32), P(f32),
+                                         P(f32), u32]),
+    "pt_gpu_set_target": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
+    "pt_gpu_read_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
+    "pt_gpu_write_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
+    "pt_gpu_accum_device_ptr": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p)]),
+    "pt_gpu_render": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32]),
+    "pt_gpu_render_to_host": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32,
+                                             P(f32)]),
+    "pt_gpu_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtStats)]),
+    "pt_gpu_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pt_gpu_set_wave_frames": (ctypes.c_int, [ctypes.c_void_p, u32]),
+    "pt_gpu_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    # pt_scene.h
+    "pt_scene_create": (ctypes.c_int, [P(ctypes.c_void_p)]),
+    "pt_scene_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pt_scene_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "pt_scene_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "pt_scene_prim_sphere": (ctypes.c_int, [ctypes.c_void_p, u32, f32, f32, f32, f32, ctypes.c_int, f32,
+                                            f32, f32, f32, f32]),
+    "pt_scene_prim_plane": (ctypes.c_int, [ctypes.c_void_p, u32, f32, f32, f32, f32, ctypes.c_int, f32,
+                                           f32, f32, f32, f32]),
+    "pt_scene_prim_set_emission": (ctypes.c_int, [ctypes.c_void_p, u32, f32, f32, f32]),
+    "pt_scene_prim_set_orient": (ctypes.c_int, [ctypes.c_void_p, u32, f32, f32, f32, f32]),
+    "pt_scene_light_quad": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 14),
+    "pt_scene_light_point": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 6),
+    "pt_scene_light_sphere": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 7),
+    "pt_scene_light_spot": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 11),
+    "pt_scene_set_mesh": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, P(u32), u32, P(u32)]),
+    "pt_scene_set_materials": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
+    "pt_scene_set_env": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32]),
+    "pt_scene_set_camera": (ctypes.c_int, [ctypes.c_void_p, f32, f32, f32, f32, f32, f32]),
+    "pt_scene_set_cvar": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double]),
+    "pt_scene_get_cvar": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, P(ctypes.c_double)]),
+    "pt_scene_pack": (ctypes.c_int, [ctypes.c_void_p]),
+    "pt_scene_packed": (ctypes.c_int, [ctypes.c_void_p, P(PtPackedScene)]),
+    "pt_scene_fill_push": (ctypes.c_int, [ctypes.c_void_p, u32, u32, u32, u32, P(PtPushHead),
+                                          P(PtPathParams)]),
+    "pt_scene_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pt_scene_synth": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double]),
+    "pt_build_analytic_bvh": (ctypes.c_int, [P(f32), u32, P(PtBvhNode), P(u32), P(u32)]),
+    "pt_build_triangle_bvh": (ctypes.c_int, [P(f32), u32, P(u32), u32, P(PtBvhNode), P(u32), P(u32),
+                                             P(u32)]),
+    "pt_build_env_cdf": (ctypes.c_int, [P(f32), u32, u32, P(ctypes.c_uint8), P(f32), P(f32),
+                                        P(ctypes.c_double)]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the product library; raises FileNotFoundError when it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} not found: build it with `python demont-engine_gb300/build.py` "
+            "(there is no fallback path)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class PtError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def fptr(a):
+    return a.ctypes.data_as(P(f32)) if a is not None else None
+
+
+def uptr(a):
+    return a.ctypes.data_as(P(u32)) if a is not None else None
+
+
+def nptr(a):
+    return a.ctypes.data_as(P(PtBvhNode)) if a is not None else None
+
+
+def nodes_to_array(nodes_ptr, n):
+    """PtBvhNode* -> structured numpy copy (n, 8) of uint32 words."""
+    if n == 0:
+        return np.zeros((0, 8), np.uint32)
+    buf = (ctypes.c_uint32 * (8 * n)).from_address(ctypes.addressof(nodes_ptr.contents))
+    return np.frombuffer(buf, dtype=np.uint32).reshape(n, 8).copy()
+
+
+class Scene:
+    """Host scene builder (pt_scene_*): the reference's scene commands, cvars,
+    packing rules and the seeded synthetic configs."""
+
+    def __init__(self):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        self._check(self.lib.pt_scene_create(ctypes.byref(h)), h)
+        self.h = h
+
+    def _check(self, rc, h=None):
+        if rc != PT_OK:
+            msg = self.lib.pt_scene_last_error(h if h is not None else self.h)
+            raise PtError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synth(self, config_id: int, seed: int = 0, scale: float = 1.0):
+        self._check(self.lib.pt_scene_synth(self.h, config_id, seed, scale))
+        return self
+
+    def set_cvar(self, name: str, value: float):
+        self._check(self.lib.pt_scene_set_cvar(self.h, name.encode(), float(value)))
+
+    def get_cvar(self, name: str) -> float:
+        v = ctypes.c_double()
+        self._check(self.lib.pt_scene_get_cvar(self.h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def sphere(self, id, x, y, z, r, mat, rgb, rough=0.0, ior=1.5):
+        self._check(self.lib.pt_scene_prim_sphere(self.h, id, x, y, z, r, mat, *rgb, rough, ior))
+
+    def plane(self, id, n, d, mat, rgb, rough=0.0, ior=1.0):
+        self._check(self.lib.pt_scene_prim_plane(self.h, id, *n, d, mat, *rgb, rough, ior))
+
+    def emission(self, id, rgb):
+        self._check(self.lib.pt_scene_prim_set_emission(self.h, id, *rgb))
+
+    def orient(self, id, q):
+        self._check(self.lib.pt_scene_prim_set_orient(self.h, id, *q))
+
+    def light_quad(self, id, pos, n, u, u_half, v_half, rgb):
+        self._check(self.lib.pt_scene_light_quad(self.h, id, *pos, *n, *u, u_half, v_half, *rgb))
+
+    def light_point(self, id, pos, rgb):
+        self._check(self.lib.pt_scene_light_point(self.h, id, *pos, *rgb))
+
+    def light_sphere(self, id, pos, radius, rgb):
+        self._check(self.lib.pt_scene_light_sphere(self.h, id, *pos, radius, *rgb))
+
+    def light_spot(self, id, pos, d, outer_deg, inner_deg, rgb):
+        self._check(self.lib.pt_scene_light_spot(self.h, id, *pos, *d, outer_deg, inner_deg, *rgb))
+
+    def mesh(self, positions, indices, mat_ids=None):
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        mid = None if mat_ids is None else np.ascontiguousarray(mat_ids, np.uint32)
+        self._keep_mesh = (pos, idx, mid)
+        self._check(self.lib.pt_scene_set_mesh(self.h, fptr(pos), pos.size // 3, uptr(idx),
+                                               idx.size // 3, uptr(mid)))
+
+    def materials(self, mats12):
+        m = np.ascontiguousarray(mats12, np.float32).reshape(-1)
+        self._check(self.lib.pt_scene_set_materials(self.h, fptr(m), m.size // 12))
+
+    def env(self, rgb):
+        """rgb: (H, W, 3) float32 lat-long image, or None for no env map."""
+        if rgb is None:
+            self._check(self.lib.pt_scene_set_env(self.h, None, 0, 0))
+            return
+        a = np.ascontiguousarray(rgb, np.float32)
+        H, W = a.shape[:2]
+        self._check(self.lib.pt_scene_set_env(self.h, fptr(a), W, H))
+
+    def camera(self, pos, yaw, pitch, fov_deg):
+        self._check(self.lib.pt_scene_set_camera(self.h, *pos, yaw, pitch, fov_deg))
+
+    def packed(self) -> PtPackedScene:
+        ps = PtPackedScene()
+        self._check(self.lib.pt_scene_packed(self.h, ctypes.byref(ps)))
+        return ps
+
+    def push(self, width, height, frame_index=0, reset=1):
+        head, prm = PtPushHead(), PtPathParams()
+        self._check(self.lib.pt_scene_fill_push(self.h, width, height, frame_index, reset,
+                                                ctypes.byref(head), ctypes.byref(prm)))
+        return head, prm
+
+    def arrays(self) -> dict:
+        """numpy copies of the packed buffers (for tests and inspection)."""
+        p = self.packed()
+
+        def f(ptr, n):
+            return np.ctypeslib.as_array(ptr, shape=(n,)).copy() if n else np.zeros(0, np.float32)
+
+        def u(ptr, n):
+            return np.ctypeslib.as_array(ptr, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+
+        out = dict(prims=f(p.prims, p.prim_count * 28).reshape(-1, 28),
+                   linear=p.linear_prim_count,
+                   bvh=nodes_to_array(p.bvh_nodes, p.bvh_node_count),
+                   positions=f(p.positions, p.vertex_count * 3).reshape(-1, 3),
+                   indices=u(p.indices, p.tri_count * 3).reshape(-1, 3),
+                   tri_bvh=nodes_to_array(p.tri_nodes, p.tri_node_count),
+                   tri_perm=u(p.tri_perm, p.tri_perm_count),
+                   lights=f(p.lights, p.light_count * 20).reshape(-1, 20),
+                   env_total=p.env_total_luminance, hdri_count=p.hdri_count)
+        if p.env_present:
+            out["env_marginal"] = f(p.env_marginal, p.env_h)
+            out["env_conditional"] = f(p.env_conditional, p.env_w * p.env_h).reshape(p.env_h, p.env_w)
+            out["hdri_dir_pmf"] = f(p.hdri_dir_pmf, 32).reshape(8, 4)
+            out["hdri_col"] = f(p.hdri_col, 32).reshape(8, 4)
+        return out
+
+
+class Device:
+    """One CUDA device context (pt_gpu_*)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.pt_gpu_create(ctypes.byref(h), device)
+        self.h = h
+        if rc != PT_OK:
+            msg = self.lib.pt_gpu_last_error(h) if h else b"create failed"
+            if h:
+                self.lib.pt_gpu_destroy(h)
+            self.h = None
+            raise PtError(rc, msg.decode())
+        self.W = self.H = 0
+
+    def _check(self, rc):
+        if rc != PT_OK:
+            raise PtError(rc, self.lib.pt_gpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pt_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, scene: Scene):
+        self._check(self.lib.pt_scene_upload(scene.h, self.h))
+
+    def set_target(self, width, height):
+        self._check(self.lib.pt_gpu_set_target(self.h, width, height))
+        self.W, self.H = width, height
+
+    def render(self, head, prm, frames=1):
+        self._check(self.lib.pt_gpu_render(self.h, ctypes.byref(head), ctypes.byref(prm), frames))
+
+    def render_to_host(self, head, prm, frames, out):
+        self._check(self.lib.pt_gpu_render_to_host(self.h, ctypes.byref(head), ctypes.byref(prm),
+                                                   frames, fptr(out)))
+        return out
+
+    def read_accum(self, out=None):
+        if out is None:
+            out = np.empty((self.H, self.W, 4), np.float32)
+        self._check(self.lib.pt_gpu_read_accum(self.h, fptr(out)))
+        return out
+
+    def write_accum(self, a):
+        a = np.ascontiguousarray(a, np.float32)
+        self._check(self.lib.pt_gpu_write_accum(self.h, fptr(a)))
+
+    def stats(self) -> PtStats:
+        s = PtStats()
+        self._check(self.lib.pt_gpu_get_stats(self.h, ctypes.byref(s)))
+        return s
+
+    def set_profiling(self, on=True):
+        self._check(self.lib.pt_gpu_set_profiling(self.h, 1 if on else 0))
+
+    def set_wave_frames(self, n):
+        self._check(self.lib.pt_gpu_set_wave_frames(self.h, n))
+
+    def trace(self, ro4, rd4):
+        ro4 = np.ascontiguousarray(ro4, np.float32)
+        rd4 = np.ascontiguousarray(rd4, np.float32)
+        n = ro4.shape[0]
+        hit = np.empty(n, np.uint32)
+        t = np.empty(n, np.float32)
+        self._check(self.lib.pt_gpu_trace_closest(self.h, ro4.ctypes.data, rd4.ctypes.data, n,
+                                                  hit.ctypes.data, t.ctypes.data, 0))
+        return hit, t

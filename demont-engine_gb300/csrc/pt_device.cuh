@@ -1,0 +1,450 @@
+// Device-side math, traversal and sampling for the path-trace wavefront.
+//
+// Semantics follow shaders/PathTrace.slang and shaders/PathTraceMath.slang
+// (citations inline).  Built with -fmad=false and IEEE division/sqrt, so
+// every expression rounds exactly as written; sin/cos/atan2/acos are the
+// polynomial versions below (not libdevice), which makes the whole render
+// reproducible bit for bit by a CPU restatement that evaluates the same
+// expressions.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ptd {
+
+// ---------------------------------------------------------------------------
+// small vector type
+// ---------------------------------------------------------------------------
+struct V3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 v3(float4 a) { return V3{a.x, a.y, a.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ V3 operator/(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float length(V3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ V3 normalize(V3 a) {
+    const float inv = 1.0f / sqrtf(dot(a, a));
+    return a * inv;
+}
+__device__ __forceinline__ bool any_pos(V3 a) { return a.x > 0.0f || a.y > 0.0f || a.z > 0.0f; }
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return a + t * (b - a); }
+__device__ __forceinline__ V3 lerp3(V3 a, V3 b, float t) { return a + t * (b - a); }
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+// HLSL reflect(i, n) = i - 2 dot(n, i) n; refract per the HLSL/GLSL definition.
+__device__ __forceinline__ V3 reflect(V3 i, V3 n) { return i - (2.0f * dot(n, i)) * n; }
+__device__ __forceinline__ V3 refract(V3 i, V3 n, float eta) {
+    const float c = dot(n, i);
+    const float k = 1.0f - (eta * eta) * (1.0f - c * c);
+    if (k < 0.0f) return {0.0f, 0.0f, 0.0f};
+    return eta * i - (eta * c + sqrtf(k)) * n;
+}
+__device__ __forceinline__ float4 f4(V3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// ---------------------------------------------------------------------------
+// Polynomial transcendentals.  sin/cos: Cody-Waite reduction by pi/2 (3-part
+// constant), Taylor series of sin to r^9 and cos to r^10 on |r| <= pi/4.
+// atan: Taylor series to w^17 on |w| <= tan(pi/8), atan(z) = pi/4 +
+// atan((z-1)/(z+1)) above; acos(x) = atan2(sqrt((1-x)(1+x)), x).
+// ---------------------------------------------------------------------------
+constexpr float kPio2Hi = 0x1.92p+0f;
+constexpr float kPio2Mid = 0x1.fb54p-12f;
+constexpr float kPio2Lo = 0x1.10b462p-30f;
+constexpr float kTwoOverPi = 0x1.45f306p-1f;
+constexpr float kPiF = 0x1.921fb6p+1f;
+constexpr float kPio2F = 0x1.921fb6p+0f;
+constexpr float kPio4F = 0x1.921fb6p-1f;
+constexpr float kTanPi8 = 0x1.a8279ap-2f;
+constexpr float kS1 = float(-1.0 / 6.0), kS2 = float(1.0 / 120.0), kS3 = float(-1.0 / 5040.0),
+                kS4 = float(1.0 / 362880.0);
+constexpr float kC1 = -0.5f, kC2 = float(1.0 / 24.0), kC3 = float(-1.0 / 720.0),
+                kC4 = float(1.0 / 40320.0), kC5 = float(-1.0 / 3628800.0);
+constexpr float kA1 = float(-1.0 / 3.0), kA2 = float(1.0 / 5.0), kA3 = float(-1.0 / 7.0),
+                kA4 = float(1.0 / 9.0), kA5 = float(-1.0 / 11.0), kA6 = float(1.0 / 13.0),
+                kA7 = float(-1.0 / 15.0), kA8 = float(1.0 / 17.0);
+
+__device__ __forceinline__ float poly_sin(float r) {
+    const float r2 = r * r;
+    float p = kS4;
+    p = p * r2 + kS3;
+    p = p * r2 + kS2;
+    p = p * r2 + kS1;
+    return r + (r * r2) * p;
+}
+__device__ __forceinline__ float poly_cos(float r) {
+    const float r2 = r * r;
+    float q = kC5;
+    q = q * r2 + kC4;
+    q = q * r2 + kC3;
+    q = q * r2 + kC2;
+    q = q * r2 + kC1;
+    return 1.0f + r2 * q;
+}
+__device__ __forceinline__ float reduce_pio2(float x, int& quadrant) {
+    const float k = rintf(x * kTwoOverPi);
+    float r = x - k * kPio2Hi;
+    r = r - k * kPio2Mid;
+    r = r - k * kPio2Lo;
+    quadrant = int(k) & 3;
+    return r;
+}
+__device__ __forceinline__ float f_sin(float x) {
+    int q;
+    const float r = reduce_pio2(x, q);
+    if (q == 0) return poly_sin(r);
+    if (q == 1) return poly_cos(r);
+    if (q == 2) return -poly_sin(r);
+    return -poly_cos(r);
+}
+__device__ __forceinline__ float f_cos(float x) {
+    int q;
+    const float r = reduce_pio2(x, q);
+    if (q == 0) return poly_cos(r);
+    if (q == 1) return -poly_sin(r);
+    if (q == 2) return -poly_cos(r);
+    return poly_sin(r);
+}
+__device__ __forceinline__ float atan_poly(float w) {
+    const float w2 = w * w;
+    float p = kA8;
+    p = p * w2 + kA7;
+    p = p * w2 + kA6;
+    p = p * w2 + kA5;
+    p = p * w2 + kA4;
+    p = p * w2 + kA3;
+    p = p * w2 + kA2;
+    p = p * w2 + kA1;
+    return w + (w * w2) * p;
+}
+__device__ __forceinline__ float atan_unit(float z) {
+    if (z > kTanPi8) return kPio4F + atan_poly((z - 1.0f) / (z + 1.0f));
+    return atan_poly(z);
+}
+__device__ __forceinline__ float f_atan2(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    if (ax == 0.0f && ay == 0.0f) return (x < 0.0f) ? kPiF : 0.0f;
+    const bool swap = ay > ax;
+    const float z = swap ? (ax / ay) : (ay / ax);
+    float a = atan_unit(z);
+    if (swap) a = kPio2F - a;
+    if (x < 0.0f) a = kPiF - a;
+    if (y < 0.0f) a = -a;
+    return a;
+}
+__device__ __forceinline__ float f_acos(float x) {
+    const float s = sqrtf((1.0f - x) * (1.0f + x));
+    return f_atan2(s, x);
+}
+
+// shader literal constants, rounded once to float
+constexpr float kPi = float(3.14159265358979);
+constexpr float kTwoPi = float(6.28318530717958);
+constexpr float kInvPi = float(1.0 / 3.14159265358979);
+constexpr float kTwoPiHemi = float(6.28318530718);
+constexpr float kInvTwoPiSky = float(1.0 / 6.28318530718);
+constexpr float kInvPiSky = float(1.0 / 3.14159265359);
+constexpr float kInvTwoPiPdf = float(1.0 / 6.28318530717958);
+constexpr float kInvPiPdf = float(1.0 / 3.14159265358979);
+
+// ---------------------------------------------------------------------------
+// PCG (shaders/PathTraceMath.slang:16-24)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t x) {
+    x = x * 747796405u + 2891336453u;
+    x = ((x >> ((x >> 28u) + 4u)) ^ x) * 277803737u;
+    return (x >> 22u) ^ x;
+}
+__device__ __forceinline__ float randf(uint32_t& seed) {
+    seed = pcg_hash(seed);
+    return float(seed & 0x00FFFFFFu) / 16777216.0f;
+}
+
+// q * v * q^-1 (shaders/PathTrace.slang:2028-2031)
+__device__ __forceinline__ V3 quat_rotate(float4 q, V3 v) {
+    const V3 u = v3(q.x, q.y, q.z);
+    return v + 2.0f * cross(u, cross(u, v) + q.w * v);
+}
+
+// ---------------------------------------------------------------------------
+// Scene in HBM
+// ---------------------------------------------------------------------------
+constexpr uint32_t kMatLambert = 0u, kMatMetal = 1u, kMatDielectric = 2u;
+constexpr uint32_t kMiss = 0xFFFFFFFFu;
+constexpr uint32_t kTriBit = 1u << 30;
+constexpr uint32_t kTraverseCap = 1u << 22;   // loop-iteration cap per query (error word if hit)
+
+struct DScene {
+    // analytic records: geo = sphere (centre at shutter 1, radius) / plane (rotated n, d)
+    const float4* prim_geo;
+    const uint32_t* prim_type;
+    const float4* prim_rec;      // 7 float4 per record, the reference packing
+    uint32_t prim_count, linear_count;
+    const float4* bvh;           // 2 float4 per node (reference 32-byte node)
+    uint32_t bvh_nodes;
+    // triangles in BVH leaf-slot order: (v0, orig id) (e1, material) (e2, 0)
+    const float4* tri;
+    uint32_t tri_slots;
+    const float4* tri_bvh;
+    uint32_t tri_nodes;
+    uint32_t tri_enabled;        // bvh_params.z != 0
+    uint32_t mesh_has_mat;
+    const float4* mats;          // 3 float4 per material
+    uint32_t mat_count;
+    const float4* lights;        // 5 float4 per light
+    uint32_t light_count;
+    const float4* env;           // W*H texels
+    const float* marg;
+    const float* cond;
+    uint32_t env_w, env_h;
+    uint32_t hdri_count;
+    float4 hdri_dir[8];
+    float4 hdri_col[8];
+    uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
+};
+
+struct HitRec {
+    float t;
+    uint32_t id;
+};
+
+// slab test (shaders/PathTrace.slang:2321-2329)
+__device__ __forceinline__ bool slab(V3 ro, V3 inv, float4 lo, float4 hi, float tmax) {
+    const float t0x = (lo.x - ro.x) * inv.x, t1x = (hi.x - ro.x) * inv.x;
+    const float t0y = (lo.y - ro.y) * inv.y, t1y = (hi.y - ro.y) * inv.y;
+    const float t0z = (lo.z - ro.z) * inv.z, t1z = (hi.z - ro.z) * inv.z;
+    const float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+    const float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    return tmx >= fmaxf(tmin, 0.0f) && tmin <= tmax;
+}
+__device__ __forceinline__ V3 safe_inv(V3 rd) {
+    const float sx = (fabsf(rd.x) > 1e-30f) ? rd.x : 1e-30f;
+    const float sy = (fabsf(rd.y) > 1e-30f) ? rd.y : 1e-30f;
+    const float sz = (fabsf(rd.z) > 1e-30f) ? rd.z : 1e-30f;
+    return v3(1.0f / sx, 1.0f / sy, 1.0f / sz);
+}
+
+// testAnalyticPrim geometry part (shaders/PathTrace.slang:2066-2161,
+// PathTraceMath.slang:194-214).  Updates best t / id on a strictly closer hit.
+__device__ __forceinline__ void test_prim(const DScene& S, uint32_t idx, V3 ro, V3 rd, HitRec& h) {
+    const float4 g = __ldg(S.prim_geo + idx);
+    const uint32_t type = __ldg(S.prim_type + idx);
+    float t;
+    if (type == 0u) {
+        const V3 oc = ro - v3(g);
+        const float b = dot(oc, rd);
+        const float k = dot(oc, oc) - g.w * g.w;
+        float hh = b * b - k;
+        if (hh < 0.0f) return;
+        hh = sqrtf(hh);
+        const float t0 = -b - hh, t1 = -b + hh;
+        t = (t0 > 1e-3f) ? t0 : t1;
+    } else if (type == 1u) {
+        const V3 n = v3(g);
+        const float denom = dot(rd, n);
+        if (fabsf(denom) < 1e-4f) return;
+        t = -(dot(ro, n) + g.w) / denom;
+    } else {
+        return;
+    }
+    if (t > 1e-3f && t < h.t) {
+        h.t = t;
+        h.id = idx;
+    }
+}
+
+// traceScene closest hit (shaders/PathTrace.slang:2331-2693): planes linearly,
+// analytic BVH (stack 32, right child popped first), then the triangle BVH
+// (stack 64) which only replaces the analytic hit when strictly closer.
+__device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, float t_init) {
+    HitRec h{t_init, kMiss};
+    const uint32_t linear = S.linear_count;
+    for (uint32_t i = 0; i < linear; ++i) test_prim(S, i, ro, rd, h);
+    uint32_t iters = 0;
+    if (S.bvh_nodes == 0u) {
+        for (uint32_t i = linear; i < S.prim_count; ++i) test_prim(S, i, ro, rd, h);
+    } else {
+        const V3 inv = safe_inv(rd);
+        uint32_t stack[32];
+        int sp = 0;
+        stack[sp++] = 0u;
+        while (sp > 0) {
+            if (++iters > kTraverseCap) { atomicOr(S.err, 1u); break; }
+            const uint32_t idx = stack[--sp];
+            const float4 lo = __ldg(S.bvh + 2u * idx), hi = __ldg(S.bvh + 2u * idx + 1u);
+            if (!slab(ro, inv, lo, hi, h.t)) continue;
+            const uint32_t lf = __float_as_uint(lo.w), cnt = __float_as_uint(hi.w);
+            if (cnt > 0u) {
+                const uint32_t base = lf + linear;
+                for (uint32_t k = 0; k < cnt; ++k) test_prim(S, base + k, ro, rd, h);
+            } else if (sp + 2 <= 32) {
+                stack[sp++] = lf;
+                stack[sp++] = lf + 1u;
+            }
+        }
+    }
+    if (S.tri_enabled != 0u && S.tri_nodes > 0u) {
+        float t_mesh = h.t;
+        uint32_t slot_hit = 0;
+        bool found = false;
+        const V3 inv = safe_inv(rd);
+        uint32_t stack[64];
+        int sp = 0;
+        stack[sp++] = 0u;
+        while (sp > 0) {
+            if (++iters > kTraverseCap) { atomicOr(S.err, 1u); break; }
+            const uint32_t idx = stack[--sp];
+            const float4 lo = __ldg(S.tri_bvh + 2u * idx), hi = __ldg(S.tri_bvh + 2u * idx + 1u);
+            if (!slab(ro, inv, lo, hi, t_mesh)) continue;
+            const uint32_t lf = __float_as_uint(lo.w), cnt = __float_as_uint(hi.w);
+            if (cnt > 0u) {
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    const uint32_t slot = lf + k;
+                    const float4 a = __ldg(S.tri + 3u * slot);
+                    const float4 b = __ldg(S.tri + 3u * slot + 1u);
+                    const float4 c = __ldg(S.tri + 3u * slot + 2u);
+                    const V3 v0 = v3(a), e1 = v3(b), e2 = v3(c);
+                    const V3 pv = cross(rd, e2);
+                    const float det = dot(e1, pv);
+                    if (fabsf(det) < 1e-8f) continue;
+                    const float inv_det = 1.0f / det;
+                    const V3 tvec = ro - v0;
+                    const float u = dot(tvec, pv) * inv_det;
+                    if (u < 0.0f || u > 1.0f) continue;
+                    const V3 qv = cross(tvec, e1);
+                    const float v = dot(rd, qv) * inv_det;
+                    if (v < 0.0f || u + v > 1.0f) continue;
+                    const float tt = dot(e2, qv) * inv_det;
+                    if (tt > 1e-3f && tt < t_mesh) {
+                        found = true;
+                        t_mesh = tt;
+                        slot_hit = slot;
+                    }
+                }
+            } else if (sp + 2 <= 64) {
+                stack[sp++] = lf;
+                stack[sp++] = lf + 1u;
+            }
+        }
+        if (found) {
+            h.t = t_mesh;
+            h.id = kTriBit | slot_hit;   // slot in leaf order; shading reads the record
+        }
+    }
+    return h;
+}
+
+// Surface attributes of a hit (the HitInfo fields testAnalyticPrim and the
+// mesh branch fill in, shaders/PathTrace.slang:2101-2146, 2639-2690).
+struct Surface {
+    V3 normal;
+    uint32_t mat;
+    V3 albedo;
+    float rough;
+    float ior;
+    V3 emission;
+};
+
+__device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, HitRec h) {
+    Surface s;
+    if (h.id & kTriBit) {
+        const uint32_t slot = h.id & ~kTriBit;
+        const float4 b = __ldg(S.tri + 3u * slot + 1u);
+        const float4 c = __ldg(S.tri + 3u * slot + 2u);
+        s.normal = normalize(cross(v3(b), v3(c)));
+        if (S.mesh_has_mat && S.mat_count > 0u) {
+            uint32_t m = __float_as_uint(b.w);
+            if (m >= S.mat_count) m = S.mat_count - 1u;
+            const float4 m0 = __ldg(S.mats + 3u * m), m1 = __ldg(S.mats + 3u * m + 1u),
+                         m2 = __ldg(S.mats + 3u * m + 2u);
+            s.albedo = v3(m0);
+            s.rough = m0.w;
+            s.emission = v3(m1);
+            s.ior = m1.w;
+            s.mat = uint32_t(m2.x);
+        } else {
+            s.mat = kMatMetal;
+            s.albedo = v3(1.00f, 0.85f, 0.45f);
+            s.rough = 0.05f;
+            s.ior = 1.0f;
+            s.emission = v3(0.0f, 0.0f, 0.0f);
+        }
+    } else {
+        const float4 g = __ldg(S.prim_geo + h.id);
+        const uint32_t type = __ldg(S.prim_type + h.id);
+        if (type == 0u) s.normal = normalize(ro + rd * h.t - v3(g));
+        else s.normal = v3(g);
+        const float4 r1 = __ldg(S.prim_rec + 7u * h.id + 1u);
+        const float4 r2 = __ldg(S.prim_rec + 7u * h.id + 2u);
+        const float4 r4 = __ldg(S.prim_rec + 7u * h.id + 4u);
+        s.mat = uint32_t(r2.y);
+        s.albedo = v3(r1);
+        s.rough = r1.w;
+        s.ior = r2.z;
+        s.emission = v3(r4);
+    }
+    return s;
+}
+
+// Schlick (shaders/PathTraceMath.slang:73-76)
+__device__ __forceinline__ float schlick(float cos_t, float r0) {
+    const float m = 1.0f - cos_t;
+    return r0 + (1.0f - r0) * m * m * m * m * m;
+}
+
+// cosine hemisphere (shaders/PathTraceMath.slang:30-42)
+__device__ __forceinline__ V3 cos_hemi(V3 n, uint32_t& seed) {
+    const float u1 = randf(seed);
+    const float u2 = randf(seed);
+    const float r = sqrtf(u1);
+    const float phi = kTwoPiHemi * u2;
+    const float x = r * f_cos(phi);
+    const float y = r * f_sin(phi);
+    const float z = sqrtf(fmaxf(0.0f, 1.0f - u1));
+    const V3 ax = (fabsf(n.x) > 0.9f) ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+    const V3 t = normalize(cross(n, ax));
+    const V3 b = cross(n, t);
+    return normalize(t * x + b * y + n * z);
+}
+
+// transmittance (shaders/PathTrace.slang:5089-5196) with clouds and water off.
+// Counts the closest-hit queries it makes in *segs.
+__device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t_max, int kmax,
+                                            uint32_t& segs) {
+    V3 t = v3(1.0f, 1.0f, 1.0f);
+    for (int i = 0; i <= kmax; ++i) {
+        ++segs;
+        const HitRec h = trace_closest(S, o, d, 1e30f);
+        if (h.id == kMiss || h.t >= t_max) return t;
+        const Surface sf = surface_at(S, o, d, h);
+        if (sf.mat != kMatDielectric) return v3(0.0f, 0.0f, 0.0f);
+        if (i == kmax) return v3(0.0f, 0.0f, 0.0f);
+        const float ndi = dot(sf.normal, d);
+        const V3 nf = (ndi < 0.0f) ? sf.normal : -sf.normal;
+        const float ia = (ndi < 0.0f) ? 1.0f : sf.ior;
+        const float ib = (ndi < 0.0f) ? sf.ior : 1.0f;
+        const float eta = ia / ib;
+        const float cos_i = fabsf(dot(nf, -d));
+        const float r0 = ((ia - ib) / (ia + ib)) * ((ia - ib) / (ia + ib));
+        const float fr = schlick(cos_i, r0);
+        const V3 refr = refract(d, nf, eta);
+        if (length(refr) < 1e-3f) return v3(0.0f, 0.0f, 0.0f);
+        t = t * ((1.0f - fr) * sf.albedo);
+        const float adv = h.t + 1e-3f;
+        o = o + d * adv;
+        d = normalize(refr);
+        t_max = fmaxf(t_max - adv, 0.0f);
+    }
+    return v3(0.0f, 0.0f, 0.0f);
+}
+
+}  // namespace ptd

@@ -1,0 +1,1210 @@
+// GB300 path-trace hot path: wavefront integrator + C-ABI (include/pt_gpu.h).
+//
+// One frame of the reference kernel (shaders/PathTrace.slang:5450-7930) is a
+// per-pixel loop over spp samples, each a loop over bounces.  Here the same
+// work runs as a wavefront over a "wave" = F frames x all pixels:
+//
+//   init     per path slot: seed = pcgHash(x*1973 + y*9277 + frame*26699)
+//   for s < spp (samples share the pixel's seed stream, so they run in order):
+//     camera   primary rays for every slot (consumes the jitter draws)
+//     for b < max_bounces:
+//       extend   closest hit for the live queue
+//       shade    miss / emission / NEE sampling / BSDF / Russian roulette in
+//                the reference's RNG order; NEE shadow rays go to a queue with
+//                their pending contribution; survivors go to the next queue
+//       shadow   transmittance for every queued shadow ray
+//       resolve  adds the visible NEE terms in the reference's order, and the
+//                sample radiance of paths that ended this bounce
+//   accumulate  running mean over the wave's frames, in frame order
+//
+// All float math is compiled with -fmad=false and follows the shader's
+// operation order, so the result equals a scalar restatement bit for bit.
+
+#include "pt_gpu.h"
+#include "pt_device.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace ptd;
+
+namespace {
+
+constexpr uint32_t kEnded = 4u, kSkipSky = 1u, kPrevLambert = 2u;
+constexpr int kThreads = 256;
+
+struct DFrame {
+    V3 cam_pos;
+    float tanf;
+    V3 fwd;
+    float aspect;
+    V3 right;
+    V3 up;
+    uint32_t W, H, npix, nframes, frame_index0, spp, maxb, denoiser;
+    float jx, jy;
+    uint32_t env_present;
+    float env_intensity, env_total;
+    int kmax;
+    float firefly;
+    uint32_t mis, rr_start, light_count;
+};
+
+struct DPaths {
+    float4* ray_o;
+    float4* ray_d;
+    float4* thr;      // w: cosine pdf of the last Lambert bounce (MIS)
+    float4* rad;
+    float4* fsum;
+    uint32_t* seed;
+    uint32_t* state;
+    float* hit_t;
+    uint32_t* hit_id;
+    uint32_t* shmask;  // bits 0-2: shadow slot issued; bits 4-6: clamp as indirect
+    float4* sh_o;      // 3 per path: origin, w = t_max
+    float4* sh_d;      // direction, w = first scalar factor
+    float4* sh_pre;    // throughput * emitter radiance, w = second scalar factor
+    float4* sh_brdf;   // brdf, w = pdf
+    float4* sh_tr;     // transmittance result
+    uint32_t* q[2];
+    uint32_t* sq;
+    uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue
+    unsigned long long* stat;   // [0] extension rays, [1] shadow segments
+};
+
+// ---------------------------------------------------------------------------
+// sampling helpers that need the frame constants
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V3 clamp_ind(V3 c, float w) {
+    if (w <= 0.0f) return c;
+    const float m = fmaxf(c.x, fmaxf(c.y, c.z));
+    return (m > w) ? c * (w / m) : c;
+}
+
+__device__ __forceinline__ V3 env_texel(const DScene& S, uint32_t u, uint32_t v) {
+    return v3(__ldg(S.env + (size_t(v) * S.env_w + u)));
+}
+
+// skyColor, env-map branch (shaders/PathTrace.slang:3401-3431)
+__device__ V3 sky_color(const DScene& S, const DFrame& F, V3 rd) {
+    const int32_t w = int32_t(S.env_w), hh = int32_t(S.env_h);
+    const float u = f_atan2(rd.z, rd.x) * kInvTwoPiSky + 0.5f;
+    const float v = f_acos(clampf(rd.y, -1.0f, 1.0f)) * kInvPiSky;
+    const float fx = u * float(w) - 0.5f, fy = v * float(hh) - 0.5f;
+    const int32_t ix = int32_t(floorf(fx)), iy = int32_t(floorf(fy));
+    const float tx = fx - float(ix), ty = fy - float(iy);
+    const int32_t x0 = (ix % w + w) % w, x1 = (x0 + 1) % w;
+    const int32_t y0 = min(max(iy, 0), hh - 1), y1 = min(max(iy + 1, 0), hh - 1);
+    const V3 c00 = env_texel(S, x0, y0), c10 = env_texel(S, x1, y0);
+    const V3 c01 = env_texel(S, x0, y1), c11 = env_texel(S, x1, y1);
+    const V3 sky = lerp3(lerp3(c00, c10, tx), lerp3(c01, c11, tx), ty);
+    return sky * F.env_intensity;
+}
+
+__device__ __forceinline__ uint32_t cdf_search(const float* cdf, uint32_t count, float u) {
+    uint32_t lo = 0, hi = count;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid) < u) lo = mid + 1;
+        else hi = mid;
+    }
+    return min(lo, count - 1u);
+}
+
+__device__ __forceinline__ float env_denom(const DFrame& F) { return 2.0f * kPi * kPi * F.env_total; }
+
+// sampleEnvMap (shaders/PathTrace.slang:3638-3670)
+__device__ void sample_env(const DScene& S, const DFrame& F, float xu, float xv, V3& dir, V3& color,
+                           float& pdf) {
+    dir = v3(0.0f, 1.0f, 0.0f);
+    color = v3(0.0f, 0.0f, 0.0f);
+    pdf = 0.0f;
+    if (F.env_present == 0u || !(F.env_total > 0.0f)) return;
+    const uint32_t w = S.env_w, hh = S.env_h;
+    const uint32_t vi = cdf_search(S.marg, hh, xv);
+    const uint32_t ui = cdf_search(S.cond + size_t(vi) * w, w, xu);
+    const float u = (float(ui) + 0.5f) / float(w);
+    const float v = (float(vi) + 0.5f) / float(hh);
+    const float theta = v * kPi;
+    const float phi = u * kTwoPi - kPi;
+    const float st = f_sin(theta);
+    dir = v3(st * f_cos(phi), f_cos(theta), st * f_sin(phi));
+    const V3 raw = env_texel(S, ui, vi);
+    color = raw * F.env_intensity;
+    const float lum = 0.2126f * raw.x + 0.7152f * raw.y + 0.0722f * raw.z;
+    if (st > 1e-6f) pdf = (lum * float(w * hh)) / env_denom(F);
+}
+
+__device__ __forceinline__ void dir_to_texel(const DScene& S, V3 d, float& st, uint32_t& ui,
+                                             uint32_t& vi) {
+    const float ct = clampf(d.y, -1.0f, 1.0f);
+    const float th = f_acos(ct);
+    st = f_sin(th);
+    const float ph = f_atan2(d.z, d.x);
+    const float u = (ph + kPi) * kInvTwoPiPdf;
+    const float v = th * kInvPiPdf;
+    ui = min(uint32_t(u * float(S.env_w)), S.env_w - 1u);
+    vi = min(uint32_t(v * float(S.env_h)), S.env_h - 1u);
+}
+
+// isExtractedClusterDir (shaders/PathTrace.slang:3679-3696)
+__device__ bool is_cluster_dir(const DScene& S, const DFrame& F, V3 d) {
+    if (F.env_present == 0u || S.hdri_count == 0u) return false;
+    float st;
+    uint32_t ui, vi;
+    dir_to_texel(S, d, st, ui, vi);
+    if (st < 1e-6f) return false;
+    const size_t base = size_t(vi) * S.env_w;
+    const float cc = __ldg(S.cond + base + ui);
+    const float cp = (ui > 0u) ? __ldg(S.cond + base + ui - 1u) : 0.0f;
+    return cc <= cp;
+}
+
+// pdfEnvMapDir (shaders/PathTrace.slang:3710-3727)
+__device__ float pdf_env_dir(const DScene& S, const DFrame& F, V3 d) {
+    if (F.env_present == 0u || !(F.env_total > 0.0f)) return 0.0f;
+    float st;
+    uint32_t ui, vi;
+    dir_to_texel(S, d, st, ui, vi);
+    if (st < 1e-6f) return 0.0f;
+    const V3 raw = env_texel(S, ui, vi);
+    const float lum = 0.2126f * raw.x + 0.7152f * raw.y + 0.0722f * raw.z;
+    return (lum * float(S.env_w * S.env_h)) / env_denom(F);
+}
+
+__device__ __forceinline__ float mis_balance(float a, float b) { return a / fmaxf(a + b, 1e-12f); }
+
+// sampleAnalyticLight, uniform pick (shaders/PathTrace.slang:4035-4179)
+__device__ void sample_light(const DScene& S, const DFrame& F, V3 hp, uint32_t& seed, V3& dir, V3& Le,
+                             float& pdf, float& dist) {
+    dir = v3(0.0f, 1.0f, 0.0f);
+    Le = v3(0.0f, 0.0f, 0.0f);
+    pdf = 0.0f;
+    dist = 1e30f;
+    const uint32_t n = F.light_count;
+    if (n == 0u) return;
+    const float u_pick = randf(seed);
+    const uint32_t pick = min(uint32_t(u_pick * float(n)), n - 1u);
+    const float pick_pdf = 1.0f / float(n);
+    const float4* L = S.lights + 5u * pick;
+    const float4 l0 = __ldg(L), l1 = __ldg(L + 1), l2 = __ldg(L + 2), l3 = __ldg(L + 3),
+                 l4 = __ldg(L + 4);
+    const uint32_t type = uint32_t(l1.w + 0.5f);
+    const V3 pos = v3(l0), inten = v3(l1);
+    if (type == 0u || type == 1u) {
+        const V3 tl = pos - hp;
+        const float d2 = fmaxf(dot(tl, tl), 1e-12f);
+        const float d = sqrtf(d2);
+        if (type == 0u) {
+            dir = tl / d;
+            Le = inten / d2;
+        } else {
+            const V3 tld = tl / d;
+            const V3 axis = normalize(quat_rotate(l4, v3(l2)));
+            const float cos_dir = dot(-tld, axis);
+            const float cin = l3.x, cout = l2.w;
+            float fall = 0.0f;
+            if (cos_dir >= cin) fall = 1.0f;
+            else if (cos_dir > cout) fall = (cos_dir - cout) / fmaxf(cin - cout, 1e-6f);
+            dir = tld;
+            Le = inten * (fall / d2);
+        }
+        pdf = pick_pdf;
+        dist = d;
+        return;
+    }
+    if (type == 2u) {
+        const float x0 = randf(seed);
+        const float x1 = randf(seed);
+        const float z = 1.0f - 2.0f * x0;
+        const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+        const float phi = kTwoPi * x1;
+        const V3 nl = v3(r * f_cos(phi), r * f_sin(phi), z);
+        const V3 lp = pos + nl * l0.w;
+        const V3 tl = lp - hp;
+        const float d2 = fmaxf(dot(tl, tl), 1e-12f);
+        const float d = sqrtf(d2);
+        const V3 wi = tl / d;
+        const float cl = fmaxf(0.0f, dot(nl, -wi));
+        if (cl <= 0.0f) return;
+        const float area = 4.0f * kPi * l0.w * l0.w;
+        const float pdf_sa = d2 / fmaxf(area * cl, 1e-12f);
+        dir = wi;
+        Le = inten;
+        pdf = pick_pdf * pdf_sa;
+        dist = d;
+        return;
+    }
+    if (type == 3u) {
+        const float xa = randf(seed) * 2.0f - 1.0f;
+        const float xb = randf(seed) * 2.0f - 1.0f;
+        const V3 uvec = quat_rotate(l4, v3(l3));
+        const float ulen = length(uvec);
+        if (ulen < 1e-6f) return;
+        const V3 nq = normalize(quat_rotate(l4, v3(l2)));
+        const V3 vax = normalize(cross(nq, uvec));
+        const V3 lp = pos + uvec * xa + vax * (l3.w * xb);
+        const V3 tl = lp - hp;
+        const float d2 = fmaxf(dot(tl, tl), 1e-12f);
+        const float d = sqrtf(d2);
+        const V3 wi = tl / d;
+        const float cl = dot(nq, -wi);
+        if (cl <= 0.0f) return;
+        const float area = 4.0f * ulen * l3.w;
+        const float pdf_sa = d2 / fmaxf(area * cl, 1e-12f);
+        dir = wi;
+        Le = inten;
+        pdf = pick_pdf * pdf_sa;
+        dist = d;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void warp_add(unsigned long long* dst, uint32_t v) {
+    unsigned long long x = v;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(dst, x);
+}
+
+__device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool pred) {
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, pred);
+    const int lane = threadIdx.x & 31;
+    const int leader = mask ? __ffs(mask) - 1 : 0;
+    uint32_t base = 0;
+    if (lane == leader && mask) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// prim geometry at upload: sphere centre = lerp(prev, curr, shutter 1), plane
+// normal rotated by the orientation quaternion (shaders/PathTrace.slang:2096, 2120).
+__global__ void k_prep_prims(const float4* rec, uint32_t n, float4* geo, uint32_t* type) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v0 = rec[7u * i], v2 = rec[7u * i + 2u], v3r = rec[7u * i + 3u], v5 = rec[7u * i + 5u];
+    const uint32_t t = uint32_t(v2.x);
+    float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (t == 0u) {
+        const V3 c = lerp3(v3(v3r), v3(v0), 1.0f);
+        g = f4(c, v0.w);
+    } else if (t == 1u) {
+        g = f4(quat_rotate(v5, v3(v0)), v0.w);
+    }
+    geo[i] = g;
+    type[i] = t;
+}
+
+// triangle records in BVH leaf-slot order: (v0, orig id) (v1 - v0, material) (v2 - v0, 0)
+__global__ void k_prep_tris(const float* pos, const uint32_t* idx, const uint32_t* perm,
+                            const uint32_t* mat, uint32_t slots, float4* tri) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= slots) return;
+    const uint32_t t = perm[j];
+    const uint32_t i0 = idx[3u * t], i1 = idx[3u * t + 1u], i2 = idx[3u * t + 2u];
+    const V3 v0 = v3(pos[3u * i0], pos[3u * i0 + 1u], pos[3u * i0 + 2u]);
+    const V3 v1 = v3(pos[3u * i1], pos[3u * i1 + 1u], pos[3u * i1 + 2u]);
+    const V3 v2 = v3(pos[3u * i2], pos[3u * i2 + 1u], pos[3u * i2 + 2u]);
+    const uint32_t m = mat ? mat[t] : 0u;
+    tri[3u * j] = f4(v0, __uint_as_float(t));
+    tri[3u * j + 1u] = f4(v1 - v0, __uint_as_float(m));
+    tri[3u * j + 2u] = f4(v2 - v0, 0.0f);
+}
+
+__global__ void k_init_wave(DFrame F, DPaths P, uint32_t npaths, uint32_t frame0) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npaths) return;
+    const uint32_t f = p / F.npix, pix = p - f * F.npix;
+    const uint32_t x = pix % F.W, y = pix / F.W;
+    P.seed[p] = pcg_hash(x * 1973u + y * 9277u + (frame0 + f) * 26699u);
+    P.fsum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// primary rays (shaders/PathTrace.slang:5722-5778)
+__global__ void k_camera(DFrame F, DPaths P, uint32_t npaths, uint32_t s) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) P.cnt[0] = npaths;
+    if (p >= npaths) return;
+    const uint32_t f = p / F.npix, pix = p - f * F.npix;
+    const uint32_t x = pix % F.W, y = pix / F.W;
+    uint32_t seed = P.seed[p];
+    float jx, jy;
+    if (F.denoiser != 0u && s == 0u) {
+        jx = F.jx;
+        jy = F.jy;
+    } else {
+        const float a = randf(seed);
+        const float b = randf(seed);
+        jx = a - 0.5f;
+        jy = b - 0.5f;
+    }
+    const float ux = ((float(x) + 0.5f + jx) / float(F.W)) * 2.0f - 1.0f;
+    float uy = ((float(y) + 0.5f + jy) / float(F.H)) * 2.0f - 1.0f;
+    uy = -uy;
+    const V3 rd = normalize(F.fwd + F.right * (ux * F.aspect * F.tanf) + F.up * (uy * F.tanf));
+    P.seed[p] = seed;
+    P.ray_o[p] = f4(F.cam_pos, 0.0f);
+    P.ray_d[p] = f4(rd, 0.0f);
+    P.thr[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    P.rad[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    P.state[p] = 0u;
+    P.q[0][p] = p;
+}
+
+__global__ void __launch_bounds__(kThreads) k_extend(DScene S, DPaths P, int qsel) {
+    const uint32_t n = P.cnt[qsel];
+    const uint32_t* q = P.q[qsel];
+    uint32_t done = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = q[i];
+        const float4 o = P.ray_o[p], d = P.ray_d[p];
+        const HitRec h = trace_closest(S, v3(o), v3(d), 1e30f);
+        P.hit_t[p] = h.t;
+        P.hit_id[p] = h.id;
+        ++done;
+    }
+    warp_add(P.stat + 0, done);
+}
+
+__device__ __forceinline__ void issue_shadow(const DPaths& P, uint32_t p, int k, V3 o, V3 d, float tmax,
+                                             V3 pre, float s2, V3 brdf, float s1, float pdf,
+                                             bool clamp, uint32_t& mask) {
+    const uint32_t e = 3u * p + uint32_t(k);
+    P.sh_o[e] = f4(o, tmax);
+    P.sh_d[e] = f4(d, s1);
+    P.sh_pre[e] = f4(pre, s2);
+    P.sh_brdf[e] = f4(brdf, pdf);
+    mask |= (1u << k) | (clamp ? (16u << k) : 0u);
+}
+
+// one bounce of the loop body (shaders/PathTrace.slang:5921-6914)
+__global__ void __launch_bounds__(kThreads) k_shade(DScene S, DFrame F, DPaths P, int qsel, uint32_t b) {
+    const uint32_t n = P.cnt[qsel];
+    const uint32_t* q = P.q[qsel];
+    uint32_t* qn = P.q[qsel ^ 1];
+    const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
+    for (uint32_t it = 0; it < n_iter; ++it) {
+        const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        bool cont = false;
+        uint32_t shadow_mask = 0;
+        uint32_t p = 0;
+        if (i < n) {
+            p = q[i];
+            const float4 o4 = P.ray_o[p], d4 = P.ray_d[p], t4 = P.thr[p], r4 = P.rad[p];
+            V3 ro = v3(o4), rd = v3(d4), thr = v3(t4), rad = v3(r4);
+            float prev_pdf = t4.w;
+            uint32_t st = P.state[p];
+            uint32_t seed = P.seed[p];
+            const HitRec h{P.hit_t[p], P.hit_id[p]};
+            bool ended = false;
+            if (h.id == kMiss) {
+                if (F.mis != 0u && (st & kPrevLambert)) {
+                    if (!is_cluster_dir(S, F, rd)) {
+                        const float pe = pdf_env_dir(S, F, rd);
+                        const float wb = mis_balance(prev_pdf, pe);
+                        rad = rad + clamp_ind(thr * sky_color(S, F, rd) * wb, F.firefly);
+                    }
+                } else if (!(st & kSkipSky)) {
+                    if (b == 0u) rad = rad + thr * sky_color(S, F, rd);
+                    else rad = rad + clamp_ind(thr * sky_color(S, F, rd), F.firefly);
+                }
+                ended = true;
+            } else {
+                const Surface sf = surface_at(S, ro, rd, h);
+                const V3 hp = ro + rd * h.t;
+                const float ndi = dot(sf.normal, rd);
+                const V3 nf = (ndi < 0.0f) ? sf.normal : -sf.normal;
+                if (any_pos(sf.emission)) {
+                    if (b == 0u) rad = rad + thr * sf.emission;
+                    else rad = rad + clamp_ind(thr * sf.emission, F.firefly);
+                }
+                if (sf.mat == kMatLambert) {
+                    const V3 so = hp + nf * 1e-3f;
+                    if (F.light_count > 0u) {
+                        V3 ldir, Le;
+                        float lpdf, ldist;
+                        sample_light(S, F, hp, seed, ldir, Le, lpdf, ldist);
+                        const float ndl = dot(nf, ldir);
+                        if (lpdf > 0.0f && ndl > 0.0f) {
+                            const float tmax = fmaxf(ldist - 1e-3f, 0.0f);
+                            issue_shadow(P, p, 0, so, ldir, tmax, thr * Le, 1.0f, sf.albedo / kPi, ndl,
+                                         lpdf, b != 0u, shadow_mask);
+                        }
+                    }
+                    if (F.env_present) {
+                        const float xu = randf(seed);
+                        const float xv = randf(seed);
+                        V3 edir, ecol;
+                        float epdf;
+                        sample_env(S, F, xu, xv, edir, ecol, epdf);
+                        const float ndl = dot(nf, edir);
+                        if (epdf > 0.0f && ndl > 0.0f) {
+                            const float pdf_brdf = ndl * kInvPi;
+                            const bool fire = (F.mis != 0u) && ((b + 1u) < F.maxb);
+                            const float wl = fire ? mis_balance(epdf, pdf_brdf) : 1.0f;
+                            issue_shadow(P, p, 1, so, edir, 1e30f, thr * ecol, wl, sf.albedo / kPi, ndl,
+                                         epdf, true, shadow_mask);
+                        }
+                        if (S.hdri_count > 0u) {
+                            const float u = randf(seed);
+                            float acc = 0.0f;
+                            uint32_t sel = 0;
+                            for (uint32_t k = 0; k < 8u; ++k) {
+                                if (k >= S.hdri_count) break;
+                                acc += S.hdri_dir[k].w;
+                                if (u <= acc) { sel = k; break; }
+                                sel = k;
+                            }
+                            const V3 hdir = v3(S.hdri_dir[sel]);
+                            const V3 hcol = v3(S.hdri_col[sel]) * F.env_intensity;
+                            const float hpdf = fmaxf(S.hdri_dir[sel].w, 1e-6f);
+                            const float ndl2 = dot(nf, hdir);
+                            if (ndl2 > 0.0f && hpdf > 0.0f)
+                                issue_shadow(P, p, 2, so, hdir, 1e30f, thr * hcol, 1.0f, sf.albedo / kPi,
+                                             ndl2, hpdf, b != 0u, shadow_mask);
+                        }
+                        st = (F.mis == 0u) ? (st | kSkipSky) : (st & ~kSkipSky);
+                    }
+                    thr = thr * sf.albedo;
+                    ro = hp + nf * 1e-3f;
+                    rd = cos_hemi(nf, seed);
+                    if (F.mis != 0u && F.env_present) {
+                        prev_pdf = fmaxf(0.0f, dot(nf, rd)) * kInvPi;
+                        st |= kPrevLambert;
+                    } else {
+                        st &= ~kPrevLambert;
+                    }
+                } else if (sf.mat == kMatMetal) {
+                    V3 r = reflect(rd, nf);
+                    r = normalize(r + sf.rough * (cos_hemi(nf, seed) - nf));
+                    thr = thr * sf.albedo;
+                    ro = hp + nf * 1e-3f;
+                    rd = r;
+                    st &= ~(kSkipSky | kPrevLambert);
+                } else if (sf.mat == kMatDielectric) {
+                    const float ia = (ndi < 0.0f) ? 1.0f : sf.ior;
+                    const float ib = (ndi < 0.0f) ? sf.ior : 1.0f;
+                    const float eta = ia / ib;
+                    const float cos_i = fabsf(dot(nf, -rd));
+                    float r0 = (ia - ib) / (ia + ib);
+                    r0 = r0 * r0;
+                    const float fr = schlick(cos_i, r0);
+                    const V3 refl = reflect(rd, nf);
+                    const V3 refr = refract(rd, nf, eta);
+                    const bool tir = length(refr) < 1e-3f;
+                    if (tir || randf(seed) < fr) {
+                        rd = refl;
+                        ro = hp + nf * 1e-3f;
+                        st &= ~(kSkipSky | kPrevLambert);
+                    } else {
+                        rd = normalize(refr);
+                        ro = hp - nf * 1e-3f;
+                    }
+                }
+                if (b >= F.rr_start) {
+                    float pr = fmaxf(thr.x, fmaxf(thr.y, thr.z));
+                    pr = clampf(pr, 0.05f, 1.0f);
+                    if (randf(seed) > pr) ended = true;
+                    else thr = thr / pr;
+                }
+                if (b + 1u >= F.maxb) ended = true;
+            }
+            if (ended) st |= kEnded;
+            P.ray_o[p] = f4(ro, 0.0f);
+            P.ray_d[p] = f4(rd, 0.0f);
+            P.thr[p] = f4(thr, prev_pdf);
+            P.rad[p] = f4(rad, 0.0f);
+            P.state[p] = st;
+            P.seed[p] = seed;
+            P.shmask[p] = shadow_mask;
+            cont = !ended;
+        }
+        // compaction: survivors to the next queue, shadow rays to the shadow queue
+        const uint32_t slot = warp_push(P.cnt + (qsel ^ 1), cont);
+        if (cont) qn[slot] = p;
+        for (int k = 0; k < 3; ++k) {
+            const bool has = (shadow_mask >> k) & 1u;
+            const uint32_t ss = warp_push(P.cnt + 2, has);
+            if (has) P.sq[ss] = 3u * p + uint32_t(k);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_shadow(DScene S, DPaths P, int kmax) {
+    const uint32_t n = P.cnt[2];
+    uint32_t segs = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t e = P.sq[i];
+        const float4 o = P.sh_o[e], d = P.sh_d[e];
+        const V3 tr = transmittance(S, v3(o), v3(d), o.w, kmax, segs);
+        P.sh_tr[e] = f4(tr, 0.0f);
+    }
+    warp_add(P.stat + 1, segs);
+}
+
+// NEE terms in the reference order (light, env, HDRI), then the sample's
+// radiance for paths that ended (shaders/PathTrace.slang:6341-6520, 7701).
+__global__ void k_resolve(DFrame F, DPaths P, int qsel) {
+    const uint32_t n = P.cnt[qsel];
+    const uint32_t* q = P.q[qsel];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = q[i];
+        const uint32_t mask = P.shmask[p];
+        const uint32_t st = P.state[p];
+        if (mask == 0u && !(st & kEnded)) continue;
+        float4 r4 = P.rad[p];
+        V3 rad = v3(r4);
+        for (int k = 0; k < 3; ++k) {
+            if (!((mask >> k) & 1u)) continue;
+            const uint32_t e = 3u * p + uint32_t(k);
+            const V3 tr = v3(P.sh_tr[e]);
+            if (!any_pos(tr)) continue;
+            const float4 pre = P.sh_pre[e], br = P.sh_brdf[e];
+            const float s1 = P.sh_d[e].w;
+            const V3 c = v3(pre) * tr * v3(br) * s1 * pre.w / br.w;
+            rad = rad + (((mask >> (4 + k)) & 1u) ? clamp_ind(c, F.firefly) : c);
+        }
+        if (mask) P.rad[p] = f4(rad, 0.0f);
+        if (st & kEnded) {
+            const float4 fs = P.fsum[p];
+            P.fsum[p] = make_float4(fs.x + rad.x, fs.y + rad.y, fs.z + rad.z, 0.0f);
+        }
+    }
+}
+
+// running mean / EMA (shaders/PathTrace.slang:7707-7781)
+__device__ __forceinline__ float clean(float v) { return (isnan(v) || isinf(v)) ? 0.0f : fmaxf(v, 0.0f); }
+
+__global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes, bool reset_first,
+                             float ema_in) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= F.npix) return;
+    float4 a = accum[pix];
+    const float nspp = float(F.spp == 0u ? 1u : F.spp);
+    const float ema = clampf(ema_in, 0.0f, 0.999f);
+    for (uint32_t f = 0; f < nframes; ++f) {
+        const float4 s = P.fsum[size_t(f) * F.npix + pix];
+        V3 fr = v3(s) / nspp;
+        fr = v3(clean(fr.x), clean(fr.y), clean(fr.z));
+        if (f == 0 && reset_first) a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (isnan(a.x) || isinf(a.x) || isnan(a.y) || isinf(a.y) || isnan(a.z) || isinf(a.z) ||
+            isnan(a.w) || isinf(a.w))
+            a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const V3 pr = v3(a);
+        float n_new;
+        V3 avg;
+        if (a.w < 0.5f || ema <= 0.0f) {
+            n_new = a.w + 1.0f;
+            avg = (pr * a.w + fr) / n_new;
+        } else {
+            avg = pr * ema + fr * (1.0f - ema);
+            n_new = fminf(a.w + 1.0f, 1.0f / fmaxf(1.0f - ema, 1e-3f));
+        }
+        a = f4(avg, n_new);
+    }
+    accum[pix] = a;
+}
+
+__global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint32_t n, uint32_t* hit,
+                              float* t) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 o = ro[i], d = rd[i];
+    const float tinit = (d.w > 0.0f) ? d.w : 1e30f;
+    const HitRec h = trace_closest(S, v3(o), v3(d), tinit);
+    uint32_t id = h.id;
+    if (id != kMiss && (id & kTriBit)) {
+        const float4 a = S.tri[3u * (id & ~kTriBit)];
+        id = kTriBit | __float_as_uint(a.w);
+    }
+    hit[i] = id;
+    t[i] = (h.id == kMiss) ? 0.0f : h.t;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <class T> struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace
+
+struct pt_gpu_ctx {
+    int device = 0;
+    int sm_count = 152;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // scene
+    DBuf<float4> prim_rec, prim_geo, bvh, tri, tri_bvh, mats, lights, env;
+    DBuf<uint32_t> prim_type;
+    DBuf<float> marg, cond;
+    uint32_t prim_count = 0, linear_count = 0, bvh_nodes = 0, tri_slots = 0, tri_nodes = 0, tri_count = 0;
+    uint32_t mat_count = 0, light_count = 0, env_w = 0, env_h = 0, hdri_count = 0;
+    bool mesh_has_mat = false;
+    float hdri_dir[32] = {0}, hdri_col[32] = {0};
+    DBuf<uint32_t> err_word;
+    // target
+    uint32_t W = 0, H = 0;
+    DBuf<float4> accum;
+    // wave buffers
+    size_t cap = 0;
+    DBuf<float4> ray_o, ray_d, thr, rad, fsum, sh_o, sh_d, sh_pre, sh_brdf, sh_tr;
+    DBuf<uint32_t> seed, state, hit_id, shmask, q0, q1, sq, cnt;
+    DBuf<float> hit_t;
+    DBuf<unsigned long long> stat;
+    uint32_t wave_frames_override = 0;
+    PtStats stats{};
+    bool profile = false;
+    std::vector<cudaEvent_t> ev_pool;
+};
+
+namespace {
+
+int set_err(pt_gpu_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e__ = (call);                                                         \
+        if (e__ != cudaSuccess)                                                           \
+            return set_err(ctx, PT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+    } while (0)
+
+template <class T> void dfree(DBuf<T>& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+}
+
+template <class T> int dalloc(pt_gpu_ctx* ctx, DBuf<T>& b, size_t n) {
+    if (b.n >= n && b.p) return PT_OK;
+    dfree(b);
+    if (n == 0) return PT_OK;
+    cudaError_t e = cudaMalloc(&b.p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return set_err(ctx, PT_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b.n = n;
+    return PT_OK;
+}
+
+template <class T> int dupload(pt_gpu_ctx* ctx, DBuf<T>& b, const void* src, size_t n) {
+    int rc = dalloc(ctx, b, n);
+    if (rc) return rc;
+    if (n) CK(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return PT_OK;
+}
+
+// BVH sanity: children after their parent (so traversal terminates), leaf ranges
+// inside the prim range.  Malformed input is rejected before any kernel reads it.
+bool check_bvh(const PtBvhNode* nodes, uint32_t n_nodes, uint32_t n_leaf_items, std::string& why) {
+    for (uint32_t i = 0; i < n_nodes; ++i) {
+        const PtBvhNode& nd = nodes[i];
+        if (nd.count > 0u) {
+            if (uint64_t(nd.left_first) + nd.count > n_leaf_items) {
+                why = "leaf range out of bounds at node " + std::to_string(i);
+                return false;
+            }
+        } else if (nd.left_first <= i || uint64_t(nd.left_first) + 1 >= n_nodes) {
+            why = "bad child index at node " + std::to_string(i);
+            return false;
+        }
+    }
+    return true;
+}
+
+DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
+    DScene S{};
+    S.prim_geo = c->prim_geo.p;
+    S.prim_type = c->prim_type.p;
+    S.prim_rec = c->prim_rec.p;
+    S.prim_count = c->prim_count;
+    S.linear_count = c->linear_count;
+    S.bvh = c->bvh.p;
+    S.bvh_nodes = c->bvh_nodes;
+    S.tri = c->tri.p;
+    S.tri_slots = c->tri_slots;
+    S.tri_bvh = c->tri_bvh.p;
+    S.tri_nodes = c->tri_nodes;
+    S.tri_enabled = (c->tri_nodes > 0u) ? 1u : 0u;
+    S.mesh_has_mat = c->mesh_has_mat ? 1u : 0u;
+    S.mats = c->mats.p;
+    S.mat_count = c->mat_count;
+    S.lights = c->lights.p;
+    S.light_count = c->light_count;
+    S.env = c->env.p;
+    S.marg = c->marg.p;
+    S.cond = c->cond.p;
+    S.env_w = c->env_w;
+    S.env_h = c->env_h;
+    S.hdri_count = c->hdri_count;
+    for (int i = 0; i < 8; ++i) {
+        S.hdri_dir[i] = make_float4(c->hdri_dir[4 * i], c->hdri_dir[4 * i + 1], c->hdri_dir[4 * i + 2],
+                                    c->hdri_dir[4 * i + 3]);
+        S.hdri_col[i] = make_float4(c->hdri_col[4 * i], c->hdri_col[4 * i + 1], c->hdri_col[4 * i + 2],
+                                    c->hdri_col[4 * i + 3]);
+    }
+    S.err = c->err_word.p;
+    if (prm) {
+        // the push tail decides what the kernel walks (bvh_params), as in the reference
+        S.linear_count = prm->bvh_params[0];
+        S.bvh_nodes = prm->bvh_params[1];
+        S.tri_enabled = (prm->bvh_params[2] != 0u) ? 1u : 0u;
+        S.tri_nodes = prm->bvh_params[3];
+        S.light_count = prm->light_count;
+    }
+    return S;
+}
+
+int grid_for(pt_gpu_ctx* c, size_t work, int per_sm) {
+    const size_t need = (work + kThreads - 1) / kThreads;
+    const size_t cap = size_t(c->sm_count) * per_sm;
+    return int(std::max<size_t>(1, std::min(need, cap)));
+}
+
+int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
+    if (ctx->cap >= npaths) return PT_OK;
+    int rc = 0;
+    rc |= dalloc(ctx, ctx->ray_o, npaths);
+    rc |= dalloc(ctx, ctx->ray_d, npaths);
+    rc |= dalloc(ctx, ctx->thr, npaths);
+    rc |= dalloc(ctx, ctx->rad, npaths);
+    rc |= dalloc(ctx, ctx->fsum, npaths);
+    rc |= dalloc(ctx, ctx->seed, npaths);
+    rc |= dalloc(ctx, ctx->state, npaths);
+    rc |= dalloc(ctx, ctx->hit_t, npaths);
+    rc |= dalloc(ctx, ctx->hit_id, npaths);
+    rc |= dalloc(ctx, ctx->shmask, npaths);
+    rc |= dalloc(ctx, ctx->q0, npaths);
+    rc |= dalloc(ctx, ctx->q1, npaths);
+    rc |= dalloc(ctx, ctx->sq, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_o, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_d, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_pre, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_brdf, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_tr, 3 * npaths);
+    if (rc) return PT_ERR_OOM;
+    ctx->cap = npaths;
+    return PT_OK;
+}
+
+cudaEvent_t pool_event(pt_gpu_ctx* c, size_t i) {
+    while (c->ev_pool.size() <= i) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c->ev_pool.push_back(e);
+    }
+    return c->ev_pool[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pt_gpu_version(void) { return "demont-gb300 sm_103a wavefront v1"; }
+
+int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
+    if (!out) return PT_ERR_INVALID;
+    *out = nullptr;
+    auto* ctx = new pt_gpu_ctx();
+    ctx->device = device_ordinal;
+    cudaError_t e = cudaSetDevice(device_ordinal);
+    if (e != cudaSuccess) {
+        *out = ctx;
+        return set_err(ctx, PT_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    }
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device_ordinal);
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ctx->ev0));
+    CK(cudaEventCreate(&ctx->ev1));
+    int rc = dalloc(ctx, ctx->err_word, 1);
+    if (rc) { *out = ctx; return rc; }
+    rc = dalloc(ctx, ctx->cnt, 4);
+    if (rc) { *out = ctx; return rc; }
+    rc = dalloc(ctx, ctx->stat, 4);
+    if (rc) { *out = ctx; return rc; }
+    CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *out = ctx;
+    return PT_OK;
+}
+
+int pt_gpu_destroy(pt_gpu_ctx* ctx) {
+    if (!ctx) return PT_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto* b : {&ctx->prim_rec, &ctx->prim_geo, &ctx->bvh, &ctx->tri, &ctx->tri_bvh, &ctx->mats,
+                    &ctx->lights, &ctx->env, &ctx->accum, &ctx->ray_o, &ctx->ray_d, &ctx->thr,
+                    &ctx->rad, &ctx->fsum, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
+                    &ctx->sh_tr})
+        dfree(*b);
+    for (auto* b : {&ctx->prim_type, &ctx->seed, &ctx->state, &ctx->hit_id, &ctx->shmask, &ctx->q0,
+                    &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word})
+        dfree(*b);
+    dfree(ctx->marg);
+    dfree(ctx->cond);
+    dfree(ctx->hit_t);
+    dfree(ctx->stat);
+    for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PT_OK;
+}
+
+const char* pt_gpu_last_error(const pt_gpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int pt_gpu_upload_prims(pt_gpu_ctx* ctx, const float* recs28, uint32_t n, uint32_t linear_count,
+                        const PtBvhNode* nodes, uint32_t n_nodes) {
+    if (!ctx) return PT_ERR_INVALID;
+    if ((n && !recs28) || (n_nodes && !nodes) || linear_count > n)
+        return set_err(ctx, PT_ERR_INVALID, "upload_prims: bad arguments");
+    std::string why;
+    if (n_nodes && !check_bvh(nodes, n_nodes, n - linear_count, why))
+        return set_err(ctx, PT_ERR_INVALID, "upload_prims: " + why);
+    int rc = dupload(ctx, ctx->prim_rec, recs28, size_t(n) * 7);
+    if (rc) return rc;
+    if ((rc = dalloc(ctx, ctx->prim_geo, n)) || (rc = dalloc(ctx, ctx->prim_type, n))) return rc;
+    if (n) {
+        k_prep_prims<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->prim_rec.p, n, ctx->prim_geo.p,
+                                                               ctx->prim_type.p);
+        CK(cudaGetLastError());
+    }
+    if ((rc = dupload(ctx, ctx->bvh, nodes, size_t(n_nodes) * 2))) return rc;
+    ctx->prim_count = n;
+    ctx->linear_count = linear_count;
+    ctx->bvh_nodes = n_nodes;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv, const uint32_t* indices,
+                       uint32_t nt, const PtBvhNode* nodes, uint32_t n_nodes, const uint32_t* perm,
+                       uint32_t n_perm, const uint32_t* mat_ids) {
+    if (!ctx) return PT_ERR_INVALID;
+    if ((nv && !positions) || (nt && !indices) || (n_nodes && !nodes) || (n_perm && !perm))
+        return set_err(ctx, PT_ERR_INVALID, "upload_mesh: null buffer");
+    std::string why;
+    if (n_nodes && !check_bvh(nodes, n_nodes, n_perm, why))
+        return set_err(ctx, PT_ERR_INVALID, "upload_mesh: " + why);
+    for (uint32_t j = 0; j < n_perm; ++j) {
+        const uint32_t t = perm[j];
+        if (t >= nt) return set_err(ctx, PT_ERR_INVALID, "upload_mesh: permuted id out of range");
+        if (indices[3u * t] >= nv || indices[3u * t + 1] >= nv || indices[3u * t + 2] >= nv)
+            return set_err(ctx, PT_ERR_INVALID, "upload_mesh: vertex index out of range");
+    }
+    DBuf<float> dpos;
+    DBuf<uint32_t> didx, dperm, dmat;
+    int rc = 0;
+    if ((rc = dupload(ctx, dpos, positions, size_t(nv) * 3)) ||
+        (rc = dupload(ctx, didx, indices, size_t(nt) * 3)) ||
+        (rc = dupload(ctx, dperm, perm, n_perm)) ||
+        (rc = dupload(ctx, dmat, mat_ids, mat_ids ? nt : 0)) ||
+        (rc = dalloc(ctx, ctx->tri, size_t(n_perm) * 3))) {
+        dfree(dpos); dfree(didx); dfree(dperm); dfree(dmat);
+        return rc;
+    }
+    if (n_perm) {
+        k_prep_tris<<<(n_perm + 255) / 256, 256, 0, ctx->stream>>>(dpos.p, didx.p, dperm.p, dmat.p,
+                                                                   n_perm, ctx->tri.p);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dfree(dpos); dfree(didx); dfree(dperm); dfree(dmat);
+    if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("prep_tris: ") + cudaGetErrorString(e));
+    if ((rc = dupload(ctx, ctx->tri_bvh, nodes, size_t(n_nodes) * 2))) return rc;
+    ctx->tri_slots = n_perm;
+    ctx->tri_nodes = n_nodes;
+    ctx->tri_count = nt;
+    ctx->mesh_has_mat = (mat_ids != nullptr);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_upload_materials(pt_gpu_ctx* ctx, const float* mats12, uint32_t n) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (n && !mats12) return set_err(ctx, PT_ERR_INVALID, "upload_materials: null buffer");
+    int rc = dupload(ctx, ctx->mats, mats12, size_t(n) * 3);
+    if (rc) return rc;
+    ctx->mat_count = n;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_upload_lights(pt_gpu_ctx* ctx, const float* recs20, uint32_t n) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (n && !recs20) return set_err(ctx, PT_ERR_INVALID, "upload_lights: null buffer");
+    int rc = dupload(ctx, ctx->lights, recs20, size_t(n) * 5);
+    if (rc) return rc;
+    ctx->light_count = n;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H, const float* marginal,
+                      const float* conditional, const float* hdri_dir_pmf, const float* hdri_col,
+                      uint32_t n_hdri) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (n_hdri > 8) return set_err(ctx, PT_ERR_INVALID, "upload_env: at most 8 HDRI lights");
+    if ((W || H) && (!rgba || !marginal || !conditional || W == 0 || H == 0))
+        return set_err(ctx, PT_ERR_INVALID, "upload_env: bad image");
+    if (n_hdri && (!hdri_dir_pmf || !hdri_col)) return set_err(ctx, PT_ERR_INVALID, "upload_env: null HDRI lights");
+    int rc = 0;
+    if ((rc = dupload(ctx, ctx->env, rgba, size_t(W) * H)) || (rc = dupload(ctx, ctx->marg, marginal, H)) ||
+        (rc = dupload(ctx, ctx->cond, conditional, size_t(W) * H)))
+        return rc;
+    ctx->env_w = W;
+    ctx->env_h = H;
+    ctx->hdri_count = n_hdri;
+    std::memset(ctx->hdri_dir, 0, sizeof(ctx->hdri_dir));
+    std::memset(ctx->hdri_col, 0, sizeof(ctx->hdri_col));
+    if (n_hdri) {
+        std::memcpy(ctx->hdri_dir, hdri_dir_pmf, size_t(n_hdri) * 16);
+        std::memcpy(ctx->hdri_col, hdri_col, size_t(n_hdri) * 16);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_set_target(pt_gpu_ctx* ctx, uint32_t width, uint32_t height) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (width == 0 || height == 0 || uint64_t(width) * height > (1ull << 28))
+        return set_err(ctx, PT_ERR_INVALID, "set_target: bad size");
+    int rc = dalloc(ctx, ctx->accum, size_t(width) * height);
+    if (rc) return rc;
+    ctx->W = width;
+    ctx->H = height;
+    CK(cudaMemsetAsync(ctx->accum.p, 0, size_t(width) * height * 16, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_read_accum(pt_gpu_ctx* ctx, float* host_rgba) {
+    if (!ctx || !host_rgba) return PT_ERR_INVALID;
+    if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "read_accum: no target");
+    CK(cudaMemcpyAsync(host_rgba, ctx->accum.p, size_t(ctx->W) * ctx->H * 16, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_write_accum(pt_gpu_ctx* ctx, const float* host_rgba) {
+    if (!ctx || !host_rgba) return PT_ERR_INVALID;
+    if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "write_accum: no target");
+    CK(cudaMemcpyAsync(ctx->accum.p, host_rgba, size_t(ctx->W) * ctx->H * 16, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_accum_device_ptr(pt_gpu_ctx* ctx, void** dptr) {
+    if (!ctx || !dptr) return PT_ERR_INVALID;
+    if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "accum_device_ptr: no target");
+    *dptr = ctx->accum.p;
+    return PT_OK;
+}
+
+int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->wave_frames_override = frames_per_wave;
+    return PT_OK;
+}
+
+int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm, uint32_t frames) {
+    if (!ctx || !head || !prm) return PT_ERR_INVALID;
+    if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "render: no target (pt_gpu_set_target)");
+    if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: tlas_present (hardware RT) has no CUDA path");
+    if (prm->light_tree_enabled) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: light tree not built");
+    if (!head->env_map_present)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, "render: procedural sky modes (no env map) not built");
+    if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
+        (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))
+        return set_err(ctx, PT_ERR_INVALID, "render: prim_count / bvh_params disagree with the uploaded prims");
+    if (prm->bvh_params[1] == 0u && ctx->bvh_nodes == 0u && ctx->linear_count > ctx->prim_count)
+        return set_err(ctx, PT_ERR_INVALID, "render: bad linear count");
+    if (prm->bvh_params[2] != 0u && prm->bvh_params[3] != 0u && prm->bvh_params[3] != ctx->tri_nodes)
+        return set_err(ctx, PT_ERR_INVALID, "render: bvh_params.w disagrees with the uploaded mesh BVH");
+    if (prm->light_count > ctx->light_count)
+        return set_err(ctx, PT_ERR_INVALID, "render: light_count exceeds the uploaded lights");
+    if (ctx->env_w == 0 || ctx->env_h == 0) return set_err(ctx, PT_ERR_STATE, "render: env map not uploaded");
+    if (frames == 0) return PT_OK;
+
+    DFrame F{};
+    F.cam_pos = v3(head->pos_fovtan[0], head->pos_fovtan[1], head->pos_fovtan[2]);
+    F.tanf = head->pos_fovtan[3];
+    F.fwd = v3(head->fwd_aspect[0], head->fwd_aspect[1], head->fwd_aspect[2]);
+    F.aspect = head->fwd_aspect[3];
+    F.right = v3(head->right_xyz[0], head->right_xyz[1], head->right_xyz[2]);
+    F.up = v3(head->up_xyz[0], head->up_xyz[1], head->up_xyz[2]);
+    F.W = ctx->W;
+    F.H = ctx->H;
+    F.npix = ctx->W * ctx->H;
+    F.spp = head->spp == 0u ? 1u : head->spp;
+    F.maxb = head->max_bounces;
+    F.denoiser = head->denoiser_enabled;
+    F.jx = head->halton_jitter[0];
+    F.jy = head->halton_jitter[1];
+    F.env_present = head->env_map_present;
+    F.env_intensity = head->env_intensity;
+    F.env_total = head->env_total_luminance;
+    F.kmax = int(prm->refract_budget);
+    F.firefly = prm->firefly_clamp;
+    F.mis = prm->mis_enabled;
+    F.rr_start = prm->rr_start;
+    F.light_count = prm->light_count;
+    const DScene S = make_scene(ctx, prm);
+
+    uint32_t fpw = ctx->wave_frames_override;
+    if (fpw == 0) fpw = std::max<uint32_t>(1, uint32_t((16u << 20) / std::max<uint32_t>(F.npix, 1)));
+    fpw = std::min(fpw, frames);
+    int rc = ensure_wave(ctx, size_t(fpw) * F.npix);
+    if (rc) return rc;
+
+    DPaths P{};
+    P.ray_o = ctx->ray_o.p; P.ray_d = ctx->ray_d.p; P.thr = ctx->thr.p; P.rad = ctx->rad.p;
+    P.fsum = ctx->fsum.p; P.seed = ctx->seed.p; P.state = ctx->state.p; P.hit_t = ctx->hit_t.p;
+    P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
+    P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
+    P.q[0] = ctx->q0.p; P.q[1] = ctx->q1.p; P.sq = ctx->sq.p; P.cnt = ctx->cnt.p; P.stat = ctx->stat.p;
+
+    CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
+    ctx->stats = PtStats{};
+    size_t ev_i = 0;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
+        const uint32_t nf = std::min(fpw, frames - f0);
+        const uint32_t npaths = nf * F.npix;
+        F.nframes = nf;
+        F.frame_index0 = head->frame_index + f0;
+        const int gp = (npaths + 255) / 256;
+        k_init_wave<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, head->frame_index + f0);
+        for (uint32_t s = 0; s < F.spp; ++s) {
+            k_camera<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, s);
+            for (uint32_t b = 0; b < F.maxb; ++b) {
+                const int qs = int(b & 1u);
+                CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
+                CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
+                const int ge = grid_for(ctx, npaths, 8);
+                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
+                k_extend<<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
+                k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
+                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
+                k_shadow<<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
+                k_resolve<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, qs);
+                ctx->stats.extend_launches++;
+                ctx->stats.shadow_launches++;
+            }
+        }
+        k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf,
+                                                                   f0 == 0 && head->reset_accum != 0u, prm->accum_ema_alpha);
+        ctx->stats.waves++;
+        ctx->stats.paths += uint64_t(npaths) * F.spp;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.gpu_ms = ms;
+    ctx->stats.frames = frames;
+    if (ctx->profile) {
+        double ext = 0, sh = 0;
+        for (size_t i = 0; i + 3 < ev_i; i += 4) {
+            float a = 0, c = 0;
+            cudaEventElapsedTime(&a, ctx->ev_pool[i], ctx->ev_pool[i + 1]);
+            cudaEventElapsedTime(&c, ctx->ev_pool[i + 2], ctx->ev_pool[i + 3]);
+            ext += a;
+            sh += c;
+        }
+        ctx->stats.extend_ms = ext;
+        ctx->stats.shadow_ms = sh;
+    }
+    unsigned long long st[4];
+    uint32_t errw = 0;
+    CK(cudaMemcpy(st, ctx->stat.p, sizeof(st), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
+    ctx->stats.extension_rays = st[0];
+    ctx->stats.shadow_rays = st[1];
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "render: traversal iteration cap reached (malformed BVH?)");
+    return PT_OK;
+}
+
+int pt_gpu_render_to_host(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
+                          uint32_t frames, float* host_rgba) {
+    int rc = pt_gpu_render(ctx, head, params, frames);
+    if (rc) return rc;
+    return pt_gpu_read_accum(ctx, host_rgba);
+}
+
+int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out) {
+    if (!ctx || !out) return PT_ERR_INVALID;
+    *out = ctx->stats;
+    return PT_OK;
+}
+
+int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->profile = on != 0;
+    return PT_OK;
+}
+
+int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d, uint32_t n,
+                         uint32_t* hit_id, float* t, int on_device) {
+    if (!ctx || (n && (!ray_o || !ray_d || !hit_id || !t))) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    PtPathParams prm{};
+    prm.bvh_params[0] = ctx->linear_count;
+    prm.bvh_params[1] = ctx->bvh_nodes;
+    prm.bvh_params[2] = ctx->tri_count;
+    prm.bvh_params[3] = ctx->tri_nodes;
+    prm.light_count = ctx->light_count;
+    const DScene S = make_scene(ctx, &prm);
+    CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
+    const float4 *dro, *drd;
+    uint32_t* dh;
+    float* dt;
+    DBuf<float4> bo, bd;
+    DBuf<uint32_t> bh;
+    DBuf<float> bt;
+    if (on_device) {
+        dro = reinterpret_cast<const float4*>(ray_o);
+        drd = reinterpret_cast<const float4*>(ray_d);
+        dh = hit_id;
+        dt = t;
+    } else {
+        int rc = 0;
+        if ((rc = dupload(ctx, bo, ray_o, n)) || (rc = dupload(ctx, bd, ray_d, n)) || (rc = dalloc(ctx, bh, n)) ||
+            (rc = dalloc(ctx, bt, n))) {
+            dfree(bo); dfree(bd); dfree(bh); dfree(bt);
+            return rc;
+        }
+        dro = bo.p; drd = bd.p; dh = bh.p; dt = bt.p;
+    }
+    k_trace_probe<<<(n + 127) / 128, 128, 0, ctx->stream>>>(S, dro, drd, n, dh, dt);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && !on_device) {
+        e = cudaMemcpyAsync(hit_id, dh, size_t(n) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(t, dt, size_t(n) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dfree(bo); dfree(bd); dfree(bh); dfree(bt);
+    if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("trace_closest: ") + cudaGetErrorString(e));
+    uint32_t errw = 0;
+    CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "trace_closest: traversal iteration cap reached");
+    return PT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1242 @@
+// Host-side scene builder: the reference engine's scene API and upload
+// packing rules, restated in C++ so the GPU path is a drop-in for the
+// reference's `pathtrace` dispatch.  See include/pt_scene.h for the API.
+//
+// Compiled with -ffp-contract=off: every float expression here must round
+// exactly as written so that BVH boxes, centroids and packed records are
+// bit-identical to what the reference builds from the same inputs.
+
+#include "pt_scene.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <numbers>
+#include <numeric>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Binary centroid-median BVH builders.
+//
+// Same algorithm as the reference (src/renderer/AnalyticBvh.cpp:369-486,
+// src/renderer/TriangleBvh.cpp:33-169): top-down, split the range at
+// count/2 after std::nth_element on the widest centroid axis, leaf <= 4,
+// left child then right child appended, left child index in left_first.
+// std::nth_element is the C++ standard library's selection routine; calling
+// it on the same keys in the same order reproduces the reference's
+// permutation exactly, so the trees are bit-identical.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kMaxLeafSize = 4;
+
+inline void aabb_reset(float (&mn)[3], float (&mx)[3]) {
+    const float inf = std::numeric_limits<float>::infinity();
+    mn[0] = mn[1] = mn[2] = inf;
+    mx[0] = mx[1] = mx[2] = -inf;
+}
+
+struct SphereItem {      // one finite analytic prim: center + bounding radius
+    float center[3];
+    float radius;
+    uint32_t prim_id;
+    float centroid[3];
+};
+
+struct TriItem {
+    float aabb_min[3];
+    float aabb_max[3];
+    float centroid[3];
+    uint32_t prim_id;
+};
+
+template <typename Item, typename BoxFn>
+uint32_t build_recursive(std::vector<Item>& work, std::vector<PtBvhNode>& nodes,
+                         uint32_t node_idx, uint32_t first, uint32_t count, BoxFn include_box) {
+    float bn[3], bx[3];
+    aabb_reset(bn, bx);
+    for (uint32_t i = 0; i < count; ++i) include_box(bn, bx, work[first + i]);
+    for (int a = 0; a < 3; ++a) {
+        nodes[node_idx].aabb_min[a] = bn[a];
+        nodes[node_idx].aabb_max[a] = bx[a];
+    }
+    if (count <= kMaxLeafSize) {
+        nodes[node_idx].left_first = first;
+        nodes[node_idx].count = count;
+        return 1;
+    }
+    float cmn[3], cmx[3];
+    aabb_reset(cmn, cmx);
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* c = work[first + i].centroid;
+        for (int a = 0; a < 3; ++a) {
+            if (c[a] < cmn[a]) cmn[a] = c[a];
+            if (c[a] > cmx[a]) cmx[a] = c[a];
+        }
+    }
+    int axis = 0;
+    float widest = cmx[0] - cmn[0];
+    for (int a = 1; a < 3; ++a) {
+        const float w = cmx[a] - cmn[a];
+        if (w > widest) { widest = w; axis = a; }
+    }
+    if (widest > 0.0f) {
+        Item* begin = work.data() + first;
+        std::nth_element(begin, begin + count / 2, begin + count,
+                         [axis](const Item& a, const Item& b) {
+                             return a.centroid[axis] < b.centroid[axis];
+                         });
+    }
+    const uint32_t left_count = count / 2;
+    const uint32_t right_count = count - left_count;
+    const uint32_t left_idx = static_cast<uint32_t>(nodes.size());
+    nodes[node_idx].left_first = left_idx;
+    nodes[node_idx].count = 0;
+    nodes.push_back(PtBvhNode{});
+    nodes.push_back(PtBvhNode{});
+    uint32_t emitted = 1;
+    emitted += build_recursive(work, nodes, left_idx, first, left_count, include_box);
+    emitted += build_recursive(work, nodes, left_idx + 1, first + left_count, right_count, include_box);
+    return emitted;
+}
+
+void build_sphere_bvh(const std::vector<SphereItem>& in, std::vector<PtBvhNode>& nodes,
+                      std::vector<uint32_t>& perm) {
+    nodes.clear();
+    perm.clear();
+    if (in.empty()) return;
+    std::vector<SphereItem> work = in;
+    for (auto& w : work) {
+        w.centroid[0] = w.center[0];
+        w.centroid[1] = w.center[1];
+        w.centroid[2] = w.center[2];
+    }
+    nodes.reserve(2 * work.size());
+    nodes.push_back(PtBvhNode{});
+    build_recursive(work, nodes, 0, 0, static_cast<uint32_t>(work.size()),
+                    [](float (&mn)[3], float (&mx)[3], const SphereItem& w) {
+                        for (int i = 0; i < 3; ++i) {
+                            if (w.center[i] - w.radius < mn[i]) mn[i] = w.center[i] - w.radius;
+                            if (w.center[i] + w.radius > mx[i]) mx[i] = w.center[i] + w.radius;
+                        }
+                    });
+    perm.reserve(work.size());
+    for (const auto& w : work) perm.push_back(w.prim_id);
+}
+
+void build_tri_bvh(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t n_index,
+                   std::vector<PtBvhNode>& nodes, std::vector<uint32_t>& perm) {
+    nodes.clear();
+    perm.clear();
+    if (n_index == 0 || (n_index % 3u) != 0u) return;
+    const uint32_t nt = n_index / 3u;
+    std::vector<TriItem> work;
+    work.reserve(nt);
+    for (uint32_t t = 0; t < nt; ++t) {
+        const uint32_t i0 = idx[3u * t + 0u], i1 = idx[3u * t + 1u], i2 = idx[3u * t + 2u];
+        if (i0 >= nv || i1 >= nv || i2 >= nv) continue;   // reference skips bad triangles
+        const float* v0 = pos + 3u * i0;
+        const float* v1 = pos + 3u * i1;
+        const float* v2 = pos + 3u * i2;
+        TriItem w{};
+        for (int a = 0; a < 3; ++a) {
+            w.aabb_min[a] = std::min(v0[a], std::min(v1[a], v2[a]));
+            w.aabb_max[a] = std::max(v0[a], std::max(v1[a], v2[a]));
+            w.centroid[a] = (v0[a] + v1[a] + v2[a]) * (1.0f / 3.0f);
+        }
+        w.prim_id = t;
+        work.push_back(w);
+    }
+    if (work.empty()) return;
+    nodes.reserve(2 * work.size());
+    nodes.push_back(PtBvhNode{});
+    build_recursive(work, nodes, 0, 0, static_cast<uint32_t>(work.size()),
+                    [](float (&mn)[3], float (&mx)[3], const TriItem& w) {
+                        for (int i = 0; i < 3; ++i) {
+                            if (w.aabb_min[i] < mn[i]) mn[i] = w.aabb_min[i];
+                            if (w.aabb_max[i] > mx[i]) mx[i] = w.aabb_max[i];
+                        }
+                    });
+    perm.reserve(work.size());
+    for (const auto& w : work) perm.push_back(w.prim_id);
+}
+
+// ---------------------------------------------------------------------------
+// Env map: luminance-CDF builder (src/renderer/HdrImage.cpp:169-219).
+// Row conditional = prefix of lum*sin(theta) in double, normalised per row;
+// marginal = prefix of row sums normalised by the total, last entry forced
+// to 1 when the total is positive.
+// ---------------------------------------------------------------------------
+double env_cdf(const float* rgb, uint32_t W, uint32_t H, const uint8_t* mask,
+               float* marginal, float* conditional) {
+    for (uint32_t v = 0; v < H; ++v) marginal[v] = 0.0f;
+    double total = 0.0;
+    for (uint32_t v = 0; v < H; ++v) {
+        const double sin_theta = std::sin(std::numbers::pi * (double(v) + 0.5) / double(H));
+        double row_sum = 0.0;
+        for (uint32_t u = 0; u < W; ++u) {
+            const size_t pi = size_t(v) * W + u;
+            const float r = rgb[pi * 3 + 0], g = rgb[pi * 3 + 1], b = rgb[pi * 3 + 2];
+            const float lum_raw = 0.2126f * r + 0.7152f * g + 0.0722f * b;
+            const float lum = (mask && mask[pi]) ? 0.0f : lum_raw;
+            row_sum += double(lum) * sin_theta;
+            conditional[pi] = float(row_sum);
+        }
+        const double norm = (row_sum > 0.0) ? (1.0 / row_sum) : 0.0;
+        for (uint32_t u = 0; u < W; ++u) {
+            const size_t pi = size_t(v) * W + u;
+            conditional[pi] = float(double(conditional[pi]) * norm);
+        }
+        marginal[v] = float(row_sum);
+        total += row_sum;
+    }
+    const double norm = (total > 0.0) ? (1.0 / total) : 0.0;
+    double prefix = 0.0;
+    for (uint32_t v = 0; v < H; ++v) {
+        prefix += marginal[v];
+        marginal[v] = float(prefix * norm);
+    }
+    if (H > 0 && total > 0.0) marginal[H - 1] = 1.0f;
+    return total;
+}
+
+struct HdriLight {
+    float dir[3];
+    float irradiance[3];
+    float luminance;
+    float pmf;
+};
+
+// HDRI bright-cluster extraction (src/engine/Engine.cpp:4371-4545): mark the
+// top `top_frac` luminance pixels (threshold >= 5% of peak and >= 0.5), flood
+// fill 4-connected clusters (u wraps), keep the <= 8 brightest clusters with
+// >= 3 pixels as directional lights with a luminance pmf, and leave only the
+// kept clusters masked out of the CDF.
+void extract_hdri(const float* rgb, uint32_t W, uint32_t H, double top_frac,
+                  std::vector<uint8_t>& light_mask, std::vector<HdriLight>& lights) {
+    const size_t N = size_t(W) * H;
+    light_mask.assign(N, 0u);
+    lights.clear();
+    std::vector<float> lums(N);
+    float peak = 0.0f;
+    for (size_t pi = 0; pi < N; ++pi) {
+        const float lum = 0.2126f * rgb[pi * 3 + 0] + 0.7152f * rgb[pi * 3 + 1] +
+                          0.0722f * rgb[pi * 3 + 2];
+        lums[pi] = lum;
+        if (lum > peak) peak = lum;
+    }
+    constexpr float kMinPeakLum = 0.5f;
+    if (peak > kMinPeakLum) {
+        if (top_frac < 1e-6) top_frac = 1e-6;
+        if (top_frac > 0.5) top_frac = 0.5;
+        const size_t k_idx = N - std::max<size_t>(1, size_t(double(N) * top_frac));
+        std::vector<float> sorted = lums;
+        std::nth_element(sorted.begin(), sorted.begin() + k_idx, sorted.end());
+        float thresh = sorted[k_idx];
+        if (thresh < 0.05f * peak) thresh = 0.05f * peak;
+        if (thresh < kMinPeakLum) thresh = kMinPeakLum;
+        for (size_t pi = 0; pi < N; ++pi)
+            if (lums[pi] >= thresh) light_mask[pi] = 1u;
+    }
+
+    const double kTwoPiSq = 2.0 * std::numbers::pi * std::numbers::pi;
+    const double dOmega_unit = kTwoPiSq / double(N);
+    struct Acc {
+        double cdir[3] = {0, 0, 0};
+        double cw = 0.0;
+        double flux[3] = {0, 0, 0};
+        double lum = 0.0;
+        uint32_t pixels = 0;
+    };
+    std::vector<Acc> clusters;
+    std::vector<uint32_t> cid_of(N, 0u);
+    std::vector<std::pair<uint32_t, uint32_t>> stack;
+    for (uint32_t v0 = 0; v0 < H; ++v0) {
+        for (uint32_t u0 = 0; u0 < W; ++u0) {
+            const size_t p0 = size_t(v0) * W + u0;
+            if (!light_mask[p0] || cid_of[p0] != 0u) continue;
+            const uint32_t cid = uint32_t(clusters.size()) + 1u;
+            clusters.emplace_back();
+            stack.clear();
+            stack.emplace_back(u0, v0);
+            cid_of[p0] = cid;
+            while (!stack.empty()) {
+                auto [u, v] = stack.back();
+                stack.pop_back();
+                Acc& acc = clusters[cid - 1];
+                const size_t pi = size_t(v) * W + u;
+                const double theta = std::numbers::pi * (double(v) + 0.5) / double(H);
+                const double sint = std::sin(theta), cost = std::cos(theta);
+                const double dOmega = dOmega_unit * sint;
+                const double phi = 2.0 * std::numbers::pi * (double(u) + 0.5) / double(W) -
+                                   std::numbers::pi;
+                const float r = rgb[pi * 3 + 0], g = rgb[pi * 3 + 1], b = rgb[pi * 3 + 2];
+                const double lum = 0.2126 * r + 0.7152 * g + 0.0722 * b;
+                const double wdir = lum * dOmega;
+                acc.cdir[0] += (sint * std::cos(phi)) * wdir;
+                acc.cdir[1] += cost * wdir;
+                acc.cdir[2] += (sint * std::sin(phi)) * wdir;
+                acc.cw += wdir;
+                acc.flux[0] += double(r) * dOmega;
+                acc.flux[1] += double(g) * dOmega;
+                acc.flux[2] += double(b) * dOmega;
+                acc.lum += lum * dOmega;
+                acc.pixels += 1u;
+                const uint32_t um = (u == 0u) ? (W - 1u) : (u - 1u);
+                const uint32_t up = (u + 1u >= W) ? 0u : (u + 1u);
+                auto try_push = [&](uint32_t uu, uint32_t vv) {
+                    const size_t pp = size_t(vv) * W + uu;
+                    if (light_mask[pp] && cid_of[pp] == 0u) {
+                        cid_of[pp] = cid;
+                        stack.emplace_back(uu, vv);
+                    }
+                };
+                try_push(um, v);
+                try_push(up, v);
+                if (v > 0) try_push(u, v - 1u);
+                if (v + 1u < H) try_push(u, v + 1u);
+            }
+        }
+    }
+    std::vector<uint32_t> order(clusters.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(),
+              [&](uint32_t a, uint32_t b) { return clusters[a].lum > clusters[b].lum; });
+    std::vector<uint8_t> keep(clusters.size() + 1u, 0u);
+    double total_lum = 0.0;
+    for (uint32_t i : order) {
+        if (lights.size() >= 8) break;
+        const Acc& c = clusters[i];
+        if (c.pixels < 3u || c.cw <= 0.0) continue;
+        keep[i + 1u] = 1u;
+        HdriLight L{};
+        // normalize in double as v * (1 / sqrt(dot(v, v)))
+        const double d2 = (c.cdir[0] * c.cdir[0] + c.cdir[1] * c.cdir[1]) + c.cdir[2] * c.cdir[2];
+        const double inv = 1.0 / std::sqrt(d2);
+        for (int a = 0; a < 3; ++a) {
+            L.dir[a] = float(c.cdir[a] * inv);
+            L.irradiance[a] = float(c.flux[a]);
+        }
+        L.luminance = float(c.lum);
+        total_lum += c.lum;
+        lights.push_back(L);
+    }
+    if (total_lum > 0.0) {
+        const float inv_total = float(1.0 / total_lum);
+        for (auto& L : lights) L.pmf = L.luminance * inv_total;
+    }
+    for (size_t pi = 0; pi < N; ++pi) {
+        const uint32_t c = cid_of[pi];
+        if (c != 0u && !keep[c]) light_mask[pi] = 0u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PCG32 (O'Neill 2014, pcg32_random_r / pcg32_srandom_r) for the synthetic
+// scene generators.
+// ---------------------------------------------------------------------------
+struct Pcg32 {
+    uint64_t state = 0, inc = 1;
+    Pcg32(uint64_t initstate, uint64_t initseq) {
+        inc = (initseq << 1u) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+    uint32_t next() {
+        const uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        const uint32_t xorshifted = uint32_t(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = uint32_t(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((0u - rot) & 31u));
+    }
+    float unit() { return float(next() >> 8) * (1.0f / 16777216.0f); }
+    float range(float lo, float hi) { return lo + (hi - lo) * unit(); }
+    double gauss() {   // Box-Muller, double precision
+        double u1 = (double(next() >> 8) + 0.5) * (1.0 / 16777216.0);
+        double u2 = double(next() >> 8) * (1.0 / 16777216.0);
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * std::numbers::pi * u2);
+    }
+};
+
+// Integer lattice hash for value noise (Wang-style mix), in [0, 1).
+inline float lattice(int32_t x, int32_t y, int32_t z, uint32_t seed) {
+    uint32_t h = uint32_t(x) * 0x8da6b343u ^ uint32_t(y) * 0xd8163841u ^ uint32_t(z) * 0xcb1ab31fu ^ seed;
+    h ^= h >> 16; h *= 0x7feb352du; h ^= h >> 15; h *= 0x846ca68bu; h ^= h >> 16;
+    return float(h >> 8) * (1.0f / 16777216.0f);
+}
+
+float value_noise(float px, float py, float pz, uint32_t seed) {
+    const float fx = std::floor(px), fy = std::floor(py), fz = std::floor(pz);
+    const int32_t ix = int32_t(fx), iy = int32_t(fy), iz = int32_t(fz);
+    auto fade = [](float t) { return t * t * (3.0f - 2.0f * t); };
+    const float tx = fade(px - fx), ty = fade(py - fy), tz = fade(pz - fz);
+    float c[2][2][2];
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            for (int d = 0; d < 2; ++d) c[a][b][d] = lattice(ix + a, iy + b, iz + d, seed);
+    auto lerp = [](float a, float b, float t) { return a + t * (b - a); };
+    const float x00 = lerp(c[0][0][0], c[1][0][0], tx), x10 = lerp(c[0][1][0], c[1][1][0], tx);
+    const float x01 = lerp(c[0][0][1], c[1][0][1], tx), x11 = lerp(c[0][1][1], c[1][1][1], tx);
+    return lerp(lerp(x00, x10, ty), lerp(x01, x11, ty), tz);
+}
+
+// ---------------------------------------------------------------------------
+// Scene state
+// ---------------------------------------------------------------------------
+struct Prim {
+    uint8_t type = 0;       // 0 sphere, 1 plane
+    uint8_t material = 0;
+    float pos[3] = {0, 0, 0};
+    float radius_or_d = 0.5f;
+    float albedo[3] = {1, 1, 1};
+    float roughness = 0.0f;
+    float ior = 1.5f;
+    float prev[3] = {0, 0, 0};
+    float emission[3] = {0, 0, 0};
+    float orient[4] = {0, 0, 0, 1};
+    uint32_t tex[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+};
+
+struct Light {
+    uint32_t type = 0;      // 0 point, 1 spot, 2 sphere, 3 quad
+    float pos[3] = {0, 0, 0};
+    float radius = 0.0f;
+    float intensity[3] = {1, 1, 1};
+    float dir[3] = {0, -1, 0};
+    float cos_outer = 0.0f;
+    float cos_inner = 0.0f;
+    float u_vec[3] = {0, 0, 0};
+    float v_half = 0.0f;
+    float orient[4] = {0, 0, 0, 1};
+};
+
+struct CVar {
+    const char* name;
+    double value;
+};
+
+}  // namespace
+
+struct pt_scene {
+    std::string err;
+    std::map<uint32_t, Prim> prims;
+    std::map<uint32_t, Light> lights;
+    std::vector<float> mesh_pos;
+    std::vector<uint32_t> mesh_idx;
+    std::vector<uint32_t> mesh_mat;
+    bool mesh_has_mat = false;
+    std::vector<float> materials;
+    std::vector<float> env_rgb;
+    uint32_t env_w = 0, env_h = 0;
+    bool env_present = false;
+    float cam_pos[3] = {0.0f, 1.5f, 4.0f};
+    float cam_yaw = 0.0f, cam_pitch = -0.20f, cam_fov = 60.0f;
+    std::vector<CVar> cvars = {
+        {"r_max_bounces", 8},        {"r_spp", 1},
+        {"r_mis", 1},                {"r_firefly_clamp", 10},
+        {"r_caustics", 1},           {"r_refract_bounces", 4},
+        {"r_env_intensity", 1},      {"r_accum_ema_alpha", 0},
+        {"r_analytic_bvh_threshold", 16},
+        {"r_hdri_extract_percentile", 0.005},
+        {"r_light_tree", 0},         {"r_rr_start", 2},
+        {"r_denoiser", 0},
+    };
+
+    // packed state
+    bool dirty_prims = true, dirty_mesh = true, dirty_lights = true, dirty_env = true;
+    std::vector<float> packed_prims;
+    uint32_t linear_count = 0;
+    std::vector<PtBvhNode> bvh;
+    std::vector<PtBvhNode> tri_bvh;
+    std::vector<uint32_t> tri_perm;
+    std::vector<float> packed_lights;
+    std::vector<float> env_rgba, env_marg, env_cond;
+    double env_total = 0.0;
+    std::vector<HdriLight> hdri;
+    float hdri_dir[32] = {0};
+    float hdri_col[32] = {0};
+
+    double cvar(const char* n) const {
+        for (const auto& c : cvars)
+            if (std::strcmp(c.name, n) == 0) return c.value;
+        return 0.0;
+    }
+};
+
+namespace {
+
+int fail(pt_scene* s, const std::string& m) {
+    if (s) s->err = m;
+    return PT_ERR_INVALID;
+}
+
+void pack_prims(pt_scene* s) {
+    struct Ref { const Prim* p; uint32_t id; };
+    std::vector<Ref> inf, fin;
+    for (const auto& [id, p] : s->prims) {
+        if (p.type == 1u) inf.push_back({&p, id});
+        else fin.push_back({&p, id});
+    }
+    uint32_t threshold = 16u;
+    {
+        const double t = s->cvar("r_analytic_bvh_threshold");
+        if (t > 0) threshold = uint32_t(t);
+    }
+    std::vector<uint32_t> order(fin.size());
+    std::iota(order.begin(), order.end(), 0u);
+    s->bvh.clear();
+    if (!fin.empty() && uint32_t(fin.size()) >= threshold) {
+        std::vector<SphereItem> items(fin.size());
+        for (uint32_t i = 0; i < fin.size(); ++i) {
+            const Prim& p = *fin[i].p;
+            items[i] = SphereItem{{p.pos[0], p.pos[1], p.pos[2]}, p.radius_or_d, i, {0, 0, 0}};
+        }
+        build_sphere_bvh(items, s->bvh, order);
+    }
+    s->linear_count = uint32_t(inf.size());
+    const size_t count = s->prims.size();
+    s->packed_prims.assign(count * 28, 0.0f);
+    auto pack = [&](size_t out, const Prim& p, uint32_t id) {
+        float* o = s->packed_prims.data() + out * 28;
+        o[0] = p.pos[0]; o[1] = p.pos[1]; o[2] = p.pos[2]; o[3] = p.radius_or_d;
+        o[4] = p.albedo[0]; o[5] = p.albedo[1]; o[6] = p.albedo[2]; o[7] = p.roughness;
+        o[8] = float(p.type); o[9] = float(p.material); o[10] = p.ior;
+        std::memcpy(&o[11], &id, 4);
+        o[12] = p.prev[0]; o[13] = p.prev[1]; o[14] = p.prev[2]; o[15] = 0.0f;
+        o[16] = p.emission[0]; o[17] = p.emission[1]; o[18] = p.emission[2]; o[19] = 0.0f;
+        o[20] = p.orient[0]; o[21] = p.orient[1]; o[22] = p.orient[2]; o[23] = p.orient[3];
+        std::memcpy(&o[24], p.tex, 16);
+    };
+    for (size_t i = 0; i < inf.size(); ++i) pack(i, *inf[i].p, inf[i].id);
+    for (size_t i = 0; i < order.size(); ++i) pack(s->linear_count + i, *fin[order[i]].p, fin[order[i]].id);
+    s->dirty_prims = false;
+}
+
+void pack_mesh(pt_scene* s) {
+    build_tri_bvh(s->mesh_pos.data(), uint32_t(s->mesh_pos.size() / 3), s->mesh_idx.data(),
+                  uint32_t(s->mesh_idx.size()), s->tri_bvh, s->tri_perm);
+    s->dirty_mesh = false;
+}
+
+void pack_lights(pt_scene* s) {
+    s->packed_lights.assign(s->lights.size() * 20, 0.0f);
+    size_t i = 0;
+    for (const auto& [id, L] : s->lights) {
+        float* o = s->packed_lights.data() + i * 20;
+        o[0] = L.pos[0]; o[1] = L.pos[1]; o[2] = L.pos[2]; o[3] = L.radius;
+        o[4] = L.intensity[0]; o[5] = L.intensity[1]; o[6] = L.intensity[2]; o[7] = float(L.type);
+        o[8] = L.dir[0]; o[9] = L.dir[1]; o[10] = L.dir[2]; o[11] = L.cos_outer;
+        o[12] = (L.type == 1u) ? L.cos_inner : L.u_vec[0];
+        o[13] = L.u_vec[1]; o[14] = L.u_vec[2]; o[15] = L.v_half;
+        o[16] = L.orient[0]; o[17] = L.orient[1]; o[18] = L.orient[2]; o[19] = L.orient[3];
+        ++i;
+    }
+    s->dirty_lights = false;
+}
+
+void pack_env(pt_scene* s) {
+    s->env_rgba.clear();
+    s->env_marg.clear();
+    s->env_cond.clear();
+    s->hdri.clear();
+    s->env_total = 0.0;
+    std::memset(s->hdri_dir, 0, sizeof(s->hdri_dir));
+    std::memset(s->hdri_col, 0, sizeof(s->hdri_col));
+    if (s->env_present) {
+        const uint32_t W = s->env_w, H = s->env_h;
+        std::vector<uint8_t> mask;
+        extract_hdri(s->env_rgb.data(), W, H, s->cvar("r_hdri_extract_percentile"), mask, s->hdri);
+        s->env_marg.resize(H);
+        s->env_cond.resize(size_t(W) * H);
+        s->env_total = env_cdf(s->env_rgb.data(), W, H, mask.data(), s->env_marg.data(),
+                               s->env_cond.data());
+        s->env_rgba.resize(size_t(W) * H * 4);
+        for (size_t pi = 0; pi < size_t(W) * H; ++pi) {
+            s->env_rgba[pi * 4 + 0] = s->env_rgb[pi * 3 + 0];
+            s->env_rgba[pi * 4 + 1] = s->env_rgb[pi * 3 + 1];
+            s->env_rgba[pi * 4 + 2] = s->env_rgb[pi * 3 + 2];
+            s->env_rgba[pi * 4 + 3] = 1.0f;
+        }
+        for (size_t i = 0; i < s->hdri.size(); ++i) {
+            const HdriLight& L = s->hdri[i];
+            s->hdri_dir[i * 4 + 0] = L.dir[0]; s->hdri_dir[i * 4 + 1] = L.dir[1];
+            s->hdri_dir[i * 4 + 2] = L.dir[2]; s->hdri_dir[i * 4 + 3] = L.pmf;
+            s->hdri_col[i * 4 + 0] = L.irradiance[0]; s->hdri_col[i * 4 + 1] = L.irradiance[1];
+            s->hdri_col[i * 4 + 2] = L.irradiance[2]; s->hdri_col[i * 4 + 3] = 0.0f;
+        }
+    }
+    s->dirty_env = false;
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic scenes
+// ---------------------------------------------------------------------------
+struct MatDraw { int type; float albedo[3]; float rough; float ior; };
+
+MatDraw draw_material(Pcg32& rng) {
+    MatDraw m{};
+    const uint32_t k = std::min<uint32_t>(uint32_t(rng.unit() * 3.0f), 2u);
+    m.type = int(k);
+    m.rough = 0.0f;
+    m.ior = 1.5f;
+    if (k == 0) {
+        for (int a = 0; a < 3; ++a) m.albedo[a] = rng.range(0.05f, 0.95f);
+    } else if (k == 1) {
+        for (int a = 0; a < 3; ++a) m.albedo[a] = rng.range(0.5f, 1.0f);
+        m.rough = rng.range(0.0f, 0.3f);
+    } else {
+        m.albedo[0] = m.albedo[1] = m.albedo[2] = 1.0f;
+        m.ior = rng.range(1.3f, 1.7f);
+    }
+    return m;
+}
+
+void add_box(std::vector<float>& pos, std::vector<uint32_t>& idx, std::vector<uint32_t>& mat,
+             const float c[3], const float h[3], uint32_t mat_id) {
+    const uint32_t base = uint32_t(pos.size() / 3);
+    for (int k = 0; k < 8; ++k) {
+        pos.push_back(c[0] + ((k & 1) ? h[0] : -h[0]));
+        pos.push_back(c[1] + ((k & 2) ? h[1] : -h[1]));
+        pos.push_back(c[2] + ((k & 4) ? h[2] : -h[2]));
+    }
+    static const uint32_t faces[12][3] = {
+        {0, 2, 1}, {1, 2, 3}, {4, 5, 6}, {5, 7, 6},   // -z, +z
+        {0, 1, 4}, {1, 5, 4}, {2, 6, 3}, {3, 6, 7},   // -y, +y
+        {0, 4, 2}, {2, 4, 6}, {1, 3, 5}, {3, 7, 5},   // -x, +x
+    };
+    for (const auto& f : faces) {
+        idx.push_back(base + f[0]);
+        idx.push_back(base + f[1]);
+        idx.push_back(base + f[2]);
+        mat.push_back(mat_id);
+    }
+}
+
+// Geodesic icosphere of frequency nu with shared vertices (10 nu^2 + 2 of them,
+// 20 nu^2 triangles), radially displaced by 3-octave value noise.
+void add_icosphere(std::vector<float>& pos, std::vector<uint32_t>& idx, std::vector<uint32_t>& mat,
+                   const float c[3], float radius, uint32_t nu, float amp, uint32_t noise_seed,
+                   uint32_t mat_id) {
+    const double t = (1.0 + std::sqrt(5.0)) / 2.0;
+    const double V[12][3] = {{-1, t, 0}, {1, t, 0}, {-1, -t, 0}, {1, -t, 0},
+                             {0, -1, t}, {0, 1, t}, {0, -1, -t}, {0, 1, -t},
+                             {t, 0, -1}, {t, 0, 1}, {-t, 0, -1}, {-t, 0, 1}};
+    static const int F[20][3] = {{0, 11, 5}, {0, 5, 1}, {0, 1, 7}, {0, 7, 10}, {0, 10, 11},
+                                 {1, 5, 9}, {5, 11, 4}, {11, 10, 2}, {10, 7, 6}, {7, 1, 8},
+                                 {3, 9, 4}, {3, 4, 2}, {3, 2, 6}, {3, 6, 8}, {3, 8, 9},
+                                 {4, 9, 5}, {2, 4, 11}, {6, 2, 10}, {8, 6, 7}, {9, 8, 1}};
+    const uint32_t base = uint32_t(pos.size() / 3);
+    std::vector<std::array<double, 3>> dirs;
+    auto emit = [&](double x, double y, double z) {
+        const double l = std::sqrt(x * x + y * y + z * z);
+        dirs.push_back({x / l, y / l, z / l});
+        return uint32_t(dirs.size() - 1);
+    };
+    for (int i = 0; i < 12; ++i) emit(V[i][0], V[i][1], V[i][2]);
+    std::map<std::pair<int, int>, uint32_t> edge_start;   // (lo, hi) -> first interior point
+    auto edge_point = [&](int a, int b, uint32_t k) -> uint32_t {   // point k of nu along a->b
+        if (k == 0) return uint32_t(a);
+        if (k == nu) return uint32_t(b);
+        const int lo = std::min(a, b), hi = std::max(a, b);
+        auto it = edge_start.find({lo, hi});
+        if (it == edge_start.end()) {
+            const uint32_t first = uint32_t(dirs.size());
+            for (uint32_t j = 1; j < nu; ++j) {
+                const double w = double(j) / double(nu);
+                emit(V[lo][0] * (1 - w) + V[hi][0] * w, V[lo][1] * (1 - w) + V[hi][1] * w,
+                     V[lo][2] * (1 - w) + V[hi][2] * w);
+            }
+            it = edge_start.emplace(std::make_pair(lo, hi), first).first;
+        }
+        const uint32_t j = (a == lo) ? k : nu - k;
+        return it->second + (j - 1);
+    };
+    for (const auto& f : F) {
+        const int A = f[0], B = f[1], C = f[2];
+        // grid point (i, j): i steps along A->B, j along A->C, i + j <= nu
+        std::vector<uint32_t> grid((nu + 1) * (nu + 1), 0u);
+        for (uint32_t i = 0; i <= nu; ++i) {
+            for (uint32_t j = 0; i + j <= nu; ++j) {
+                uint32_t id;
+                if (j == 0) id = edge_point(A, B, i);
+                else if (i == 0) id = edge_point(A, C, j);
+                else if (i + j == nu) id = edge_point(B, C, j);
+                else {
+                    const double wa = double(nu - i - j) / nu, wb = double(i) / nu, wc = double(j) / nu;
+                    id = emit(V[A][0] * wa + V[B][0] * wb + V[C][0] * wc,
+                              V[A][1] * wa + V[B][1] * wb + V[C][1] * wc,
+                              V[A][2] * wa + V[B][2] * wb + V[C][2] * wc);
+                }
+                grid[i * (nu + 1) + j] = id;
+            }
+        }
+        for (uint32_t i = 0; i < nu; ++i) {
+            for (uint32_t j = 0; i + j < nu; ++j) {
+                const uint32_t p00 = grid[i * (nu + 1) + j], p10 = grid[(i + 1) * (nu + 1) + j],
+                               p01 = grid[i * (nu + 1) + j + 1];
+                idx.push_back(base + p00); idx.push_back(base + p10); idx.push_back(base + p01);
+                mat.push_back(mat_id);
+                if (i + j + 1 < nu) {
+                    const uint32_t p11 = grid[(i + 1) * (nu + 1) + j + 1];
+                    idx.push_back(base + p10); idx.push_back(base + p11); idx.push_back(base + p01);
+                    mat.push_back(mat_id);
+                }
+            }
+        }
+    }
+    for (const auto& d : dirs) {
+        const float px = float(d[0]) * 2.0f, py = float(d[1]) * 2.0f, pz = float(d[2]) * 2.0f;
+        const float n = (value_noise(px, py, pz, noise_seed) +
+                         0.5f * value_noise(2 * px, 2 * py, 2 * pz, noise_seed + 1) +
+                         0.25f * value_noise(4 * px, 4 * py, 4 * pz, noise_seed + 2)) / 1.75f;
+        const float r = radius * (1.0f + amp * (2.0f * n - 1.0f));
+        pos.push_back(c[0] + float(d[0]) * r);
+        pos.push_back(c[1] + float(d[1]) * r);
+        pos.push_back(c[2] + float(d[2]) * r);
+    }
+}
+
+void push_material(std::vector<float>& mats, const MatDraw& m) {
+    const float rec[12] = {m.albedo[0], m.albedo[1], m.albedo[2], m.rough, 0, 0, 0, m.ior,
+                           float(m.type), 0, 0, 0};
+    mats.insert(mats.end(), rec, rec + 12);
+}
+
+void set_cv(pt_scene* s, const char* n, double v) { pt_scene_set_cvar(s, n, v); }
+
+void synth_c0(pt_scene* s, uint64_t seed, double scale) {
+    Pcg32 rng(0x5EEDull + 0ull, seed);
+    const uint32_t n_spheres = std::max<uint32_t>(1, uint32_t(std::lround(64 * scale)));
+    for (uint32_t i = 0; i < n_spheres; ++i) {
+        const float cx = rng.range(-10, 10), cy = rng.range(-10, 10), cz = rng.range(-10, 10);
+        const float r = float(0.2 * std::pow(10.0, double(rng.unit())));
+        const MatDraw m = draw_material(rng);
+        pt_scene_prim_sphere(s, 1 + i, cx, cy, cz, r, m.type, m.albedo[0], m.albedo[1], m.albedo[2],
+                             m.rough, m.ior);
+    }
+    std::vector<float> pos, mats;
+    std::vector<uint32_t> idx, mid;
+    for (uint32_t b = 0; b < 4; ++b) {
+        const float h[3] = {rng.range(0.5f, 3.0f), rng.range(0.5f, 3.0f), rng.range(0.5f, 3.0f)};
+        const float c[3] = {rng.range(-10, 10), rng.range(-10, 10), rng.range(-10, 10)};
+        push_material(mats, draw_material(rng));
+        add_box(pos, idx, mid, c, h, b);
+    }
+    pt_scene_set_materials(s, mats.data(), uint32_t(mats.size() / 12));
+    pt_scene_set_mesh(s, pos.data(), uint32_t(pos.size() / 3), idx.data(), uint32_t(idx.size() / 3),
+                      mid.data());
+    pt_scene_light_quad(s, 1, 0, 12, 0, 0, -1, 0, 1, 0, 0, 0.5f, 0.5f, 15, 15, 15);
+    std::vector<float> black(8 * 4 * 3, 0.0f);
+    pt_scene_set_env(s, black.data(), 8, 4);
+    pt_scene_set_camera(s, 0, 0, 28, 0, 0, 45);
+    set_cv(s, "r_max_bounces", 8);
+    set_cv(s, "r_spp", 16);
+    set_cv(s, "r_rr_start", 3);
+    set_cv(s, "r_mis", 1);
+    set_cv(s, "r_caustics", 1);
+    set_cv(s, "r_refract_bounces", 4);
+    set_cv(s, "r_firefly_clamp", 10);
+    set_cv(s, "r_light_tree", 0);
+}
+
+void synth_c1(pt_scene* s, uint64_t seed, double scale) {
+    Pcg32 rng(0x5EEDull + 1ull, seed);
+    const double lin = std::sqrt(scale);
+    const uint32_t n_ico = std::max<uint32_t>(1, uint32_t(std::lround(200 * scale)));
+    const uint32_t nu = std::max<uint32_t>(2, uint32_t(std::lround(22 * lin)));
+    const uint32_t grid = std::max<uint32_t>(2, uint32_t(std::lround(512 * lin)));
+    const uint32_t n_sph = std::max<uint32_t>(1, uint32_t(std::lround(1024 * scale)));
+    uint32_t envw = std::max<uint32_t>(16, uint32_t(std::lround(2048 * lin)));
+    envw &= ~1u;
+    const uint32_t envh = envw / 2;
+
+    std::vector<float> mats;
+    push_material(mats, MatDraw{0, {0.5f, 0.5f, 0.5f}, 0.0f, 1.5f});   // ground
+    for (uint32_t i = 1; i < 256; ++i) push_material(mats, draw_material(rng));
+
+    std::vector<float> pos;
+    std::vector<uint32_t> idx, mid;
+    // ground: grid x grid quads over [-120, 120]^2 at y = 0
+    const float L = 120.0f;
+    for (uint32_t j = 0; j <= grid; ++j)
+        for (uint32_t i = 0; i <= grid; ++i) {
+            pos.push_back(-L + 2.0f * L * float(i) / float(grid));
+            pos.push_back(0.0f);
+            pos.push_back(-L + 2.0f * L * float(j) / float(grid));
+        }
+    for (uint32_t j = 0; j < grid; ++j)
+        for (uint32_t i = 0; i < grid; ++i) {
+            const uint32_t a = j * (grid + 1) + i, b = a + 1, c = a + grid + 1, d = c + 1;
+            idx.insert(idx.end(), {a, c, b, b, c, d});
+            mid.push_back(0);
+            mid.push_back(0);
+        }
+    for (uint32_t k = 0; k < n_ico; ++k) {
+        const float r = rng.range(1.5f, 4.0f);
+        const float c[3] = {rng.range(-100, 100), r, rng.range(-100, 100)};
+        add_icosphere(pos, idx, mid, c, r, nu, 0.1f, 1000u + 7u * k, 1u + (k % 255u));
+    }
+    pt_scene_set_materials(s, mats.data(), uint32_t(mats.size() / 12));
+    pt_scene_set_mesh(s, pos.data(), uint32_t(pos.size() / 3), idx.data(), uint32_t(idx.size() / 3),
+                      mid.data());
+    for (uint32_t i = 0; i < n_sph; ++i) {
+        const float r = float(0.3 * std::pow(5.0, double(rng.unit())));
+        const float cx = rng.range(-110, 110), cz = rng.range(-110, 110);
+        const MatDraw m = draw_material(rng);
+        pt_scene_prim_sphere(s, 1 + i, cx, r, cz, r, m.type, m.albedo[0], m.albedo[1], m.albedo[2],
+                             m.rough, m.ior);
+    }
+    // env: log-normal radiance per texel (mu 0, sigma 1.5) + 0.5 deg sun disc of 1e4
+    std::vector<float> rgb(size_t(envw) * envh * 3);
+    const double sun_el = 40.0 * std::numbers::pi / 180.0, sun_az = 30.0 * std::numbers::pi / 180.0;
+    const double sd[3] = {std::cos(sun_el) * std::cos(sun_az), std::sin(sun_el),
+                          std::cos(sun_el) * std::sin(sun_az)};
+    const double cos_disc = std::cos(0.25 * std::numbers::pi / 180.0);
+    for (uint32_t v = 0; v < envh; ++v) {
+        const double theta = std::numbers::pi * (v + 0.5) / envh;
+        for (uint32_t u = 0; u < envw; ++u) {
+            const double phi = 2.0 * std::numbers::pi * (u + 0.5) / envw - std::numbers::pi;
+            const double d[3] = {std::sin(theta) * std::cos(phi), std::cos(theta),
+                                 std::sin(theta) * std::sin(phi)};
+            float L0 = float(std::exp(1.5 * rng.gauss()));
+            if (d[0] * sd[0] + d[1] * sd[1] + d[2] * sd[2] >= cos_disc) L0 = 1e4f;
+            const size_t pi = size_t(v) * envw + u;
+            rgb[pi * 3 + 0] = L0;
+            rgb[pi * 3 + 1] = L0;
+            rgb[pi * 3 + 2] = L0;
+        }
+    }
+    pt_scene_set_env(s, rgb.data(), envw, envh);
+    pt_scene_set_camera(s, 0.0f, 30.0f, 150.0f, 0.0f, -0.197f, 45.0f);
+    set_cv(s, "r_max_bounces", 8);
+    set_cv(s, "r_spp", 1);
+    set_cv(s, "r_rr_start", 2);
+    set_cv(s, "r_mis", 1);
+    set_cv(s, "r_caustics", 1);
+    set_cv(s, "r_refract_bounces", 4);
+    set_cv(s, "r_firefly_clamp", 10);
+    set_cv(s, "r_light_tree", 0);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+int pt_scene_create(pt_scene** out) {
+    if (!out) return PT_ERR_INVALID;
+    *out = new pt_scene();
+    return PT_OK;
+}
+
+int pt_scene_destroy(pt_scene* s) {
+    delete s;
+    return PT_OK;
+}
+
+const char* pt_scene_last_error(const pt_scene* s) { return s ? s->err.c_str() : "null scene"; }
+
+int pt_scene_clear(pt_scene* s) {
+    if (!s) return PT_ERR_INVALID;
+    auto cv = s->cvars;
+    *s = pt_scene();
+    s->cvars = cv;
+    return PT_OK;
+}
+
+int pt_scene_prim_sphere(pt_scene* s, uint32_t id, float x, float y, float z, float radius,
+                         int material, float r, float g, float b, float roughness, float ior) {
+    if (!s) return PT_ERR_INVALID;
+    if (material < 0 || material > 2) return fail(s, "prim_sphere: unknown material");
+    if (!(radius > 0.0f)) return fail(s, "prim_sphere: radius must be > 0");
+    Prim p{};
+    p.type = 0;
+    p.material = uint8_t(material);
+    p.pos[0] = x; p.pos[1] = y; p.pos[2] = z;
+    p.prev[0] = x; p.prev[1] = y; p.prev[2] = z;
+    p.radius_or_d = radius;
+    p.albedo[0] = r; p.albedo[1] = g; p.albedo[2] = b;
+    p.roughness = roughness;
+    p.ior = ior;
+    s->prims[id] = p;
+    s->dirty_prims = true;
+    return PT_OK;
+}
+
+int pt_scene_prim_plane(pt_scene* s, uint32_t id, float nx, float ny, float nz, float d,
+                        int material, float r, float g, float b, float roughness, float ior) {
+    if (!s) return PT_ERR_INVALID;
+    if (material < 0 || material > 2) return fail(s, "prim_plane: unknown material");
+    const float len = std::sqrt(nx * nx + ny * ny + nz * nz);
+    if (!(len > 0.0f)) return fail(s, "prim_plane: zero normal");
+    nx /= len; ny /= len; nz /= len;
+    Prim p{};
+    p.type = 1;
+    p.material = uint8_t(material);
+    p.pos[0] = nx; p.pos[1] = ny; p.pos[2] = nz;
+    p.prev[0] = nx; p.prev[1] = ny; p.prev[2] = nz;
+    p.radius_or_d = d;
+    p.albedo[0] = r; p.albedo[1] = g; p.albedo[2] = b;
+    p.roughness = roughness;
+    p.ior = ior;
+    s->prims[id] = p;
+    s->dirty_prims = true;
+    return PT_OK;
+}
+
+int pt_scene_prim_set_emission(pt_scene* s, uint32_t id, float r, float g, float b) {
+    if (!s) return PT_ERR_INVALID;
+    auto it = s->prims.find(id);
+    if (it == s->prims.end()) return fail(s, "prim_set_emission: unknown id");
+    it->second.emission[0] = r; it->second.emission[1] = g; it->second.emission[2] = b;
+    s->dirty_prims = true;
+    return PT_OK;
+}
+
+int pt_scene_prim_set_orient(pt_scene* s, uint32_t id, float qx, float qy, float qz, float qw) {
+    if (!s) return PT_ERR_INVALID;
+    auto it = s->prims.find(id);
+    if (it == s->prims.end()) return fail(s, "prim_set_rotation: unknown id");
+    it->second.orient[0] = qx; it->second.orient[1] = qy;
+    it->second.orient[2] = qz; it->second.orient[3] = qw;
+    s->dirty_prims = true;
+    return PT_OK;
+}
+
+int pt_scene_light_quad(pt_scene* s, uint32_t id, float x, float y, float z, float nx, float ny,
+                        float nz, float ux, float uy, float uz, float u_half, float v_half,
+                        float r, float g, float b) {
+    if (!s) return PT_ERR_INVALID;
+    const float nlen = std::sqrt(nx * nx + ny * ny + nz * nz);
+    if (nlen < 1e-6f) return fail(s, "light_quad: normal magnitude is zero");
+    nx /= nlen; ny /= nlen; nz /= nlen;
+    const float ndu = nx * ux + ny * uy + nz * uz;
+    float uxo = ux - nx * ndu, uyo = uy - ny * ndu, uzo = uz - nz * ndu;
+    const float ulen = std::sqrt(uxo * uxo + uyo * uyo + uzo * uzo);
+    if (ulen < 1e-6f) return fail(s, "light_quad: u-axis collinear with normal");
+    uxo /= ulen; uyo /= ulen; uzo /= ulen;
+    if (u_half <= 0.0f || v_half <= 0.0f) return fail(s, "light_quad: u_half and v_half must be > 0");
+    Light L{};
+    L.type = 3;
+    L.pos[0] = x; L.pos[1] = y; L.pos[2] = z;
+    L.dir[0] = nx; L.dir[1] = ny; L.dir[2] = nz;
+    L.u_vec[0] = uxo * u_half; L.u_vec[1] = uyo * u_half; L.u_vec[2] = uzo * u_half;
+    L.v_half = v_half;
+    L.intensity[0] = r; L.intensity[1] = g; L.intensity[2] = b;
+    s->lights[id] = L;
+    s->dirty_lights = true;
+    return PT_OK;
+}
+
+int pt_scene_light_point(pt_scene* s, uint32_t id, float x, float y, float z, float r, float g,
+                         float b) {
+    if (!s) return PT_ERR_INVALID;
+    Light L{};
+    L.type = 0;
+    L.pos[0] = x; L.pos[1] = y; L.pos[2] = z;
+    L.intensity[0] = r; L.intensity[1] = g; L.intensity[2] = b;
+    s->lights[id] = L;
+    s->dirty_lights = true;
+    return PT_OK;
+}
+
+int pt_scene_light_sphere(pt_scene* s, uint32_t id, float x, float y, float z, float radius,
+                          float r, float g, float b) {
+    if (!s) return PT_ERR_INVALID;
+    if (!(radius > 0.0f)) return fail(s, "light_sphere: radius must be > 0");
+    Light L{};
+    L.type = 2;
+    L.pos[0] = x; L.pos[1] = y; L.pos[2] = z;
+    L.radius = radius;
+    L.intensity[0] = r; L.intensity[1] = g; L.intensity[2] = b;
+    s->lights[id] = L;
+    s->dirty_lights = true;
+    return PT_OK;
+}
+
+int pt_scene_light_spot(pt_scene* s, uint32_t id, float x, float y, float z, float dx, float dy,
+                        float dz, float outer_deg, float inner_deg, float r, float g, float b) {
+    if (!s) return PT_ERR_INVALID;
+    const float dlen = std::sqrt(dx * dx + dy * dy + dz * dz);
+    if (dlen < 1e-6f) return fail(s, "light_spot: direction magnitude is zero");
+    dx /= dlen; dy /= dlen; dz /= dlen;
+    const float deg2rad = std::numbers::pi_v<float> / 180.0f;
+    Light L{};
+    L.type = 1;
+    L.pos[0] = x; L.pos[1] = y; L.pos[2] = z;
+    L.dir[0] = dx; L.dir[1] = dy; L.dir[2] = dz;
+    L.intensity[0] = r; L.intensity[1] = g; L.intensity[2] = b;
+    L.cos_outer = std::cos(outer_deg * deg2rad);
+    L.cos_inner = std::cos(inner_deg * deg2rad);
+    s->lights[id] = L;
+    s->dirty_lights = true;
+    return PT_OK;
+}
+
+int pt_scene_set_mesh(pt_scene* s, const float* positions, uint32_t nv, const uint32_t* indices,
+                      uint32_t nt, const uint32_t* mat_ids) {
+    if (!s) return PT_ERR_INVALID;
+    if ((nv && !positions) || (nt && !indices)) return fail(s, "set_mesh: null buffer");
+    s->mesh_pos.assign(positions, positions + size_t(nv) * 3);
+    s->mesh_idx.assign(indices, indices + size_t(nt) * 3);
+    s->mesh_has_mat = (mat_ids != nullptr);
+    if (mat_ids) s->mesh_mat.assign(mat_ids, mat_ids + nt);
+    else s->mesh_mat.clear();
+    s->dirty_mesh = true;
+    return PT_OK;
+}
+
+int pt_scene_set_materials(pt_scene* s, const float* mats12, uint32_t n) {
+    if (!s) return PT_ERR_INVALID;
+    if (n && !mats12) return fail(s, "set_materials: null buffer");
+    s->materials.assign(mats12, mats12 + size_t(n) * 12);
+    return PT_OK;
+}
+
+int pt_scene_set_env(pt_scene* s, const float* rgb, uint32_t W, uint32_t H) {
+    if (!s) return PT_ERR_INVALID;
+    if (W == 0 || H == 0) {
+        s->env_present = false;
+        s->env_rgb.clear();
+        s->env_w = s->env_h = 0;
+    } else {
+        if (!rgb) return fail(s, "set_env: null image");
+        s->env_rgb.assign(rgb, rgb + size_t(W) * H * 3);
+        s->env_w = W;
+        s->env_h = H;
+        s->env_present = true;
+    }
+    s->dirty_env = true;
+    return PT_OK;
+}
+
+int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float pitch,
+                        float fov_deg) {
+    if (!s) return PT_ERR_INVALID;
+    s->cam_pos[0] = x; s->cam_pos[1] = y; s->cam_pos[2] = z;
+    s->cam_yaw = yaw;
+    const float lim = 85.0f * 0.01745329251994329576923690768489f;
+    s->cam_pitch = std::min(std::max(pitch, -lim), lim);
+    s->cam_fov = fov_deg;
+    return PT_OK;
+}
+
+int pt_scene_set_cvar(pt_scene* s, const char* name, double value) {
+    if (!s || !name) return PT_ERR_INVALID;
+    for (auto& c : s->cvars) {
+        if (std::strcmp(c.name, name) == 0) {
+            if (c.value != value) {
+                c.value = value;
+                if (std::strcmp(name, "r_analytic_bvh_threshold") == 0) s->dirty_prims = true;
+                if (std::strcmp(name, "r_hdri_extract_percentile") == 0) s->dirty_env = true;
+            }
+            return PT_OK;
+        }
+    }
+    return fail(s, std::string("unknown cvar ") + name);
+}
+
+int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value) {
+    if (!s || !name || !value) return PT_ERR_INVALID;
+    for (const auto& c : s->cvars) {
+        if (std::strcmp(c.name, name) == 0) {
+            *value = c.value;
+            return PT_OK;
+        }
+    }
+    return PT_ERR_INVALID;
+}
+
+int pt_scene_pack(pt_scene* s) {
+    if (!s) return PT_ERR_INVALID;
+    if (s->dirty_prims) pack_prims(s);
+    if (s->dirty_mesh) pack_mesh(s);
+    if (s->dirty_lights) pack_lights(s);
+    if (s->dirty_env) pack_env(s);
+    return PT_OK;
+}
+
+int pt_scene_packed(pt_scene* s, PtPackedScene* o) {
+    if (!s || !o) return PT_ERR_INVALID;
+    pt_scene_pack(s);
+    std::memset(o, 0, sizeof(*o));
+    o->prims = s->packed_prims.data();
+    o->prim_count = uint32_t(s->prims.size());
+    o->linear_prim_count = s->linear_count;
+    o->bvh_nodes = s->bvh.data();
+    o->bvh_node_count = uint32_t(s->bvh.size());
+    o->positions = s->mesh_pos.data();
+    o->vertex_count = uint32_t(s->mesh_pos.size() / 3);
+    o->indices = s->mesh_idx.data();
+    o->tri_count = uint32_t(s->mesh_idx.size() / 3);
+    o->tri_nodes = s->tri_bvh.data();
+    o->tri_node_count = uint32_t(s->tri_bvh.size());
+    o->tri_perm = s->tri_perm.data();
+    o->tri_perm_count = uint32_t(s->tri_perm.size());
+    o->tri_mat_ids = s->mesh_has_mat ? s->mesh_mat.data() : nullptr;
+    o->materials = s->materials.data();
+    o->material_count = uint32_t(s->materials.size() / 12);
+    o->lights = s->packed_lights.data();
+    o->light_count = uint32_t(s->lights.size());
+    o->env_present = s->env_present ? 1u : 0u;
+    o->env_rgba = s->env_rgba.data();
+    o->env_w = s->env_w;
+    o->env_h = s->env_h;
+    o->env_marginal = s->env_marg.data();
+    o->env_conditional = s->env_cond.data();
+    o->env_total_luminance = s->env_total;
+    o->hdri_count = uint32_t(s->hdri.size());
+    o->hdri_dir_pmf = s->hdri_dir;
+    o->hdri_col = s->hdri_col;
+    return PT_OK;
+}
+
+int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t frame_index,
+                       uint32_t reset_accum, PtPushHead* head, PtPathParams* params) {
+    if (!s || !head || !params || width == 0 || height == 0) return PT_ERR_INVALID;
+    pt_scene_pack(s);
+    std::memset(head, 0, sizeof(*head));
+    std::memset(params, 0, sizeof(*params));
+    // Camera basis (src/renderer/Camera.h:18-30): glm float math,
+    // normalize(v) = v * inversesqrt(dot(v, v)).
+    const float cp = std::cos(s->cam_pitch);
+    const float fwd[3] = {std::sin(s->cam_yaw) * cp, std::sin(s->cam_pitch),
+                          -std::cos(s->cam_yaw) * cp};
+    auto normalize = [](float v[3]) {
+        const float inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+        v[0] *= inv; v[1] *= inv; v[2] *= inv;
+    };
+    // right = normalize(cross(fwd, (0,1,0)))
+    float right[3] = {fwd[1] * 0.0f - fwd[2] * 1.0f, fwd[2] * 0.0f - fwd[0] * 0.0f,
+                      fwd[0] * 1.0f - fwd[1] * 0.0f};
+    normalize(right);
+    float up[3] = {right[1] * fwd[2] - right[2] * fwd[1], right[2] * fwd[0] - right[0] * fwd[2],
+                   right[0] * fwd[1] - right[1] * fwd[0]};
+    normalize(up);
+    const float fov_tan = std::tan(s->cam_fov * 0.01745329251994329576923690768489f * 0.5f);
+    head->pos_fovtan[0] = s->cam_pos[0]; head->pos_fovtan[1] = s->cam_pos[1];
+    head->pos_fovtan[2] = s->cam_pos[2]; head->pos_fovtan[3] = fov_tan;
+    head->fwd_aspect[0] = fwd[0]; head->fwd_aspect[1] = fwd[1]; head->fwd_aspect[2] = fwd[2];
+    head->fwd_aspect[3] = float(width) / float(height);
+    head->right_xyz[0] = right[0]; head->right_xyz[1] = right[1]; head->right_xyz[2] = right[2];
+    head->up_xyz[0] = up[0]; head->up_xyz[1] = up[1]; head->up_xyz[2] = up[2];
+    head->frame_index = frame_index;
+    head->reset_accum = reset_accum ? 1u : 0u;
+    head->max_bounces = uint32_t(std::max(0.0, s->cvar("r_max_bounces")));
+    head->tlas_present = 0;
+    head->prim_count = uint32_t(s->prims.size());
+    {
+        int n = int(s->cvar("r_spp"));
+        if (n < 1) n = 1;
+        if (n > 32) n = 32;
+        head->spp = uint32_t(n);
+    }
+    head->denoiser_enabled = s->cvar("r_denoiser") != 0.0 ? 1u : 0u;
+    head->env_map_present = s->env_present ? 1u : 0u;
+    head->env_intensity = float(s->cvar("r_env_intensity"));
+    head->env_total_luminance = float(s->env_total);
+
+    const bool caustics = s->cvar("r_caustics") != 0.0;
+    int rb = int(s->cvar("r_refract_bounces"));
+    rb = std::min(std::max(rb, 0), 16);
+    params->refract_budget = caustics ? float(rb) : 0.0f;
+    float ff = float(s->cvar("r_firefly_clamp"));
+    params->firefly_clamp = ff < 0.0f ? 0.0f : ff;
+    params->mis_enabled = s->cvar("r_mis") != 0.0 ? 1u : 0u;
+    float ema = float(s->cvar("r_accum_ema_alpha"));
+    params->accum_ema_alpha = std::min(std::max(ema, 0.0f), 0.999f);
+    params->bvh_params[0] = s->linear_count;
+    params->bvh_params[1] = uint32_t(s->bvh.size());
+    const bool mesh = !s->tri_bvh.empty();
+    params->bvh_params[2] = mesh ? uint32_t(s->mesh_idx.size() / 3) : 0u;
+    params->bvh_params[3] = mesh ? uint32_t(s->tri_bvh.size()) : 0u;
+    params->light_count = uint32_t(s->lights.size());
+    params->light_tree_enabled = 0;
+    params->light_tree_node_count = 0;
+    params->rr_start = uint32_t(std::max(0.0, s->cvar("r_rr_start")));
+    params->sun_and_mode[0] = 0.0f;
+    params->sun_and_mode[1] = 1.0f;
+    params->sun_and_mode[2] = 0.0f;
+    params->sun_and_mode[3] = 0.0f;
+    return PT_OK;
+}
+
+int pt_scene_synth(pt_scene* s, int config_id, uint64_t seed, double scale) {
+    if (!s) return PT_ERR_INVALID;
+    if (!(scale > 0.0) || scale > 1.0) return fail(s, "synth: scale must be in (0, 1]");
+    pt_scene_clear(s);
+    if (config_id == 0) synth_c0(s, seed, scale);
+    else if (config_id == 1) synth_c1(s, seed, scale);
+    else return fail(s, "synth: unknown config id");
+    return pt_scene_pack(s);
+}
+
+int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx) {
+    if (!s || !ctx) return PT_ERR_INVALID;
+    PtPackedScene p;
+    pt_scene_packed(s, &p);
+    int rc = pt_gpu_upload_prims(ctx, p.prims, p.prim_count, p.linear_prim_count, p.bvh_nodes,
+                                 p.bvh_node_count);
+    if (rc) return rc;
+    rc = pt_gpu_upload_materials(ctx, p.materials, p.material_count);
+    if (rc) return rc;
+    rc = pt_gpu_upload_mesh(ctx, p.positions, p.vertex_count, p.indices, p.tri_count, p.tri_nodes,
+                            p.tri_node_count, p.tri_perm, p.tri_perm_count, p.tri_mat_ids);
+    if (rc) return rc;
+    rc = pt_gpu_upload_lights(ctx, p.lights, p.light_count);
+    if (rc) return rc;
+    if (p.env_present)
+        rc = pt_gpu_upload_env(ctx, p.env_rgba, p.env_w, p.env_h, p.env_marginal, p.env_conditional,
+                               p.hdri_dir_pmf, p.hdri_col, p.hdri_count);
+    else
+        rc = pt_gpu_upload_env(ctx, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, 0);
+    return rc;
+}
+
+int pt_build_analytic_bvh(const float* cr, uint32_t n, PtBvhNode* nodes_out, uint32_t* n_nodes,
+                          uint32_t* perm_out) {
+    if ((n && (!cr || !nodes_out || !perm_out)) || !n_nodes) return PT_ERR_INVALID;
+    std::vector<SphereItem> items(n);
+    for (uint32_t i = 0; i < n; ++i)
+        items[i] = SphereItem{{cr[4 * i], cr[4 * i + 1], cr[4 * i + 2]}, cr[4 * i + 3], i, {0, 0, 0}};
+    std::vector<PtBvhNode> nodes;
+    std::vector<uint32_t> perm;
+    build_sphere_bvh(items, nodes, perm);
+    std::copy(nodes.begin(), nodes.end(), nodes_out);
+    std::copy(perm.begin(), perm.end(), perm_out);
+    *n_nodes = uint32_t(nodes.size());
+    return PT_OK;
+}
+
+int pt_build_triangle_bvh(const float* positions, uint32_t nv, const uint32_t* indices,
+                          uint32_t n_index, PtBvhNode* nodes_out, uint32_t* n_nodes,
+                          uint32_t* perm_out, uint32_t* n_perm) {
+    if (!n_nodes || !n_perm) return PT_ERR_INVALID;
+    std::vector<PtBvhNode> nodes;
+    std::vector<uint32_t> perm;
+    build_tri_bvh(positions, nv, indices, n_index, nodes, perm);
+    if (!nodes.empty() && (!nodes_out || !perm_out)) return PT_ERR_INVALID;
+    std::copy(nodes.begin(), nodes.end(), nodes_out);
+    std::copy(perm.begin(), perm.end(), perm_out);
+    *n_nodes = uint32_t(nodes.size());
+    *n_perm = uint32_t(perm.size());
+    return PT_OK;
+}
+
+int pt_build_env_cdf(const float* rgb, uint32_t W, uint32_t H, const uint8_t* mask,
+                     float* marginal, float* conditional, double* total) {
+    if (!rgb || !marginal || !conditional || !total) return PT_ERR_INVALID;
+    *total = env_cdf(rgb, W, H, mask, marginal, conditional);
+    return PT_OK;
+}
+
+}  // extern "C"

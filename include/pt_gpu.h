@@ -1,0 +1,195 @@
+/*
+ * pt_gpu.h -- C-ABI of the GB300 path-trace hot path (device side).
+ *
+ * This library replaces the reference's per-frame `pathtrace` compute
+ * dispatch: the RHI plugin call sequence
+ *   Device::CreateBuffer/WriteBuffer/CreateTexture/WriteTexture
+ *   CommandBuffer::BindComputePipeline("pathtrace") / BindBuffer /
+ *   PushConstants / Dispatch / Submit / ReadbackTexture
+ * (reference: src/rhi/Device.h:34-91, src/rhi/CommandBuffer.h:15-44,
+ *  src/rhi_software/SoftwareDevice.cpp:105-120, src/engine/Engine.cpp:6867-6900,
+ *  9580-9582) with a handful of plain C entry points.  All buffers use the
+ * reference's own layouts byte for byte, so an engine that already packs
+ * them for the reference can hand the same bytes over unchanged.
+ *
+ * Conventions
+ *   - Every call returns an int status: PT_OK (0) or a negative PT_ERR_*.
+ *     pt_gpu_last_error(ctx) returns a message for the last failure.
+ *   - A context owns one CUDA device's buffers; it is single-threaded per
+ *     caller (the reference records and submits from one engine thread).
+ *   - Host pointers are plain host memory unless a parameter says "device".
+ *   - No torch or CUDA types appear in any signature.
+ */
+#ifndef PT_GPU_H
+#define PT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_OK               0
+#define PT_ERR_INVALID     -1  /* bad argument (null pointer, size, layout) */
+#define PT_ERR_CUDA        -2  /* a CUDA runtime call failed */
+#define PT_ERR_OOM         -3  /* device allocation failed */
+#define PT_ERR_STATE       -4  /* call made in the wrong state (e.g. no target) */
+#define PT_ERR_KERNEL      -5  /* a kernel set its error word (overflow, bad index) */
+#define PT_ERR_UNSUPPORTED -6  /* feature not built */
+
+typedef struct pt_gpu_ctx pt_gpu_ctx;
+
+/* The 112-byte push-constant head.  Same fields, order and meaning as the
+ * reference's PtPush head (src/rhi_software/SoftwareTracer.cpp:38-56,
+ * shaders/PathTrace.slang:643-658, filled at src/engine/Engine.cpp:7821-7931). */
+typedef struct PtPushHead {
+    float    pos_fovtan[4];   /* camera position xyz, tan(fovY/2) */
+    float    fwd_aspect[4];   /* forward xyz, width/height */
+    float    right_xyz[4];
+    float    up_xyz[4];
+    uint32_t frame_index;     /* seeds the per-pixel PCG stream */
+    uint32_t reset_accum;     /* 1: start a new running mean */
+    uint32_t max_bounces;
+    uint32_t tlas_present;    /* must be 0: the hardware-RT branch has no CUDA counterpart */
+    uint32_t prim_count;
+    uint32_t spp;             /* samples per pixel per frame (0 is treated as 1) */
+    uint32_t denoiser_enabled;/* only its RNG effect is honoured: sample 0 uses halton_jitter */
+    uint32_t env_map_present;
+    float    halton_jitter[2];
+    float    env_intensity;
+    float    env_total_luminance;
+} PtPushHead;
+
+/* The push-constant tail fields the in-scope path reads
+ * (shaders/PathTrace.slang:660-1218; engine fill src/engine/Engine.cpp:8640-8676,
+ *  7869-7905).  Fields of features outside this library (clouds, water, SDF,
+ *  ReSTIR, spectral, DOF, motion blur, denoiser G-buffers) are absent and
+ *  behave as the reference does when those features are off. */
+typedef struct PtPathParams {
+    float    refract_budget;        /* w2j_row1.w: max dielectric hops of a shadow ray (0 = opaque) */
+    float    firefly_clamp;         /* w2j_row2.w: clampIndirect ceiling (<= 0 disables) */
+    uint32_t mis_enabled;           /* r_mis */
+    float    accum_ema_alpha;       /* accum_params.x (r_accum_ema_alpha) */
+    uint32_t bvh_params[4];         /* linear_prim_count, analytic BVH node count,
+                                       triangle count (0 = no mesh), triangle BVH node count */
+    uint32_t light_count;
+    uint32_t light_tree_enabled;    /* must be 0 (uniform pick); the tree is not built here */
+    uint32_t light_tree_node_count;
+    uint32_t rr_start;              /* Russian roulette starts at bounce b >= rr_start; reference: 2 */
+    float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 2 procedural, 3 Hosek) */
+    uint32_t reserved[4];
+} PtPathParams;
+
+/* 32-byte BVH node, identical to the reference's BvhNode / TriBvhNode
+ * (src/renderer/AnalyticBvh.h:195-201, src/renderer/TriangleBvh.h:325-331). */
+typedef struct PtBvhNode {
+    float    aabb_min[3];
+    uint32_t left_first;      /* internal: left child index (right = +1); leaf: first prim */
+    float    aabb_max[3];
+    uint32_t count;           /* 0 = internal, >0 = leaf prim count */
+} PtBvhNode;
+
+/* Per-frame counters of the last pt_gpu_render call. */
+typedef struct PtStats {
+    uint64_t extension_rays;  /* closest-hit segments traced (camera + bounce rays) */
+    uint64_t shadow_rays;     /* transmittance segments traced (incl. refraction hops) */
+    uint64_t paths;           /* camera paths started */
+    uint32_t frames;
+    uint32_t waves;
+    double   gpu_ms;          /* device time of the render, CUDA events */
+    double   extend_ms;       /* device time inside the closest-hit kernel */
+    double   shadow_ms;       /* device time inside the transmittance kernel */
+    uint32_t extend_launches;
+    uint32_t shadow_launches;
+} PtStats;
+
+/* ---- lifecycle (replaces Device::Create(BackendType), src/rhi/Device.cpp:20-48) ---- */
+int         pt_gpu_create(pt_gpu_ctx** out_ctx, int device_ordinal);
+int         pt_gpu_destroy(pt_gpu_ctx* ctx);
+const char* pt_gpu_last_error(const pt_gpu_ctx* ctx);
+/* Library build tag, e.g. "demont-gb300 sm_103a". */
+const char* pt_gpu_version(void);
+
+/* ---- scene upload (replaces the buffer writes of Engine::EnsurePrimitivesUploaded,
+ *      src/engine/Engine.cpp:4743-5070, bound at slots 5 and 18) ----
+ * recs28: n records of 28 floats (7 float4) in the reference packing
+ *         (v0 pos|normal,radius|d  v1 albedo,rough  v2 type,mat,ior,asuint(id)
+ *          v3 prev_pos  v4 emission  v5 orient quat  v6 texture tiles).
+ * linear_count: the first linear_count records are tested linearly (planes).
+ * nodes/n_nodes: the analytic BVH over records [linear_count, n); n_nodes 0 =
+ *         linear scan of all records (reference bvh_params.y == 0). */
+int pt_gpu_upload_prims(pt_gpu_ctx* ctx, const float* recs28, uint32_t n,
+                        uint32_t linear_count, const PtBvhNode* nodes, uint32_t n_nodes);
+
+/* ---- mesh upload (replaces Engine::RebuildMeshResources, src/engine/Engine.cpp:3752-3911,
+ *      slots 3, 4, 19, 20) ----
+ * positions: float[3*nv]; indices: uint32[3*nt]; nodes/perm: the triangle BVH
+ * and its permuted triangle ids (src/renderer/TriangleBvh.h).
+ * mat_ids (nullable, extension): per-triangle index into the material table of
+ * pt_gpu_upload_materials; NULL = the reference's gold metal for every triangle. */
+int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv,
+                       const uint32_t* indices, uint32_t nt,
+                       const PtBvhNode* nodes, uint32_t n_nodes,
+                       const uint32_t* perm, uint32_t n_perm,
+                       const uint32_t* mat_ids);
+
+/* ---- mesh material table (extension; the reference meshes are all gold metal,
+ *      shaders/PathTrace.slang:2655-2658) ----
+ * mats: n records of 12 floats: albedo rgb, roughness, emission rgb, ior,
+ *       material type (0 Lambert, 1 metal, 2 dielectric) as float, 3 pad. */
+int pt_gpu_upload_materials(pt_gpu_ctx* ctx, const float* mats12, uint32_t n);
+
+/* ---- analytic lights (replaces Engine::EnsureLightsUploaded, src/engine/Engine.cpp:5235-5330,
+ *      slot 27): n records of 20 floats (5 float4) in the reference packing. ---- */
+int pt_gpu_upload_lights(pt_gpu_ctx* ctx, const float* recs20, uint32_t n);
+
+/* ---- environment (replaces Engine::ReloadEnvMap's uploads, src/engine/Engine.cpp:4329-4600,
+ *      slots 9, 10, 11 and the push fields hdri_lights_*) ----
+ * rgba: float[4*W*H] texels; marginal: float[H]; conditional: float[W*H]
+ * (as built by BuildEnvCdf, src/renderer/HdrImage.cpp:169-219);
+ * hdri_dir_pmf / hdri_col: n_hdri (<= 8) float4 each (dir xyz + pmf, flux rgb). */
+int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H,
+                      const float* marginal, const float* conditional,
+                      const float* hdri_dir_pmf, const float* hdri_col, uint32_t n_hdri);
+
+/* ---- render target: the reference's accum_hdr RGBA32F texture, .a = frame count ---- */
+int pt_gpu_set_target(pt_gpu_ctx* ctx, uint32_t width, uint32_t height);
+int pt_gpu_read_accum(pt_gpu_ctx* ctx, float* host_rgba);          /* ReadbackTexture */
+int pt_gpu_write_accum(pt_gpu_ctx* ctx, const float* host_rgba);   /* resume from a saved state */
+int pt_gpu_accum_device_ptr(pt_gpu_ctx* ctx, void** device_ptr);  /* zero-copy view, device memory */
+
+/* ---- per-frame dispatch (replaces Dispatch of "pathtrace"; shaders/PathTrace.slang:5450-7930) ----
+ * Renders `frames` consecutive frames: frame f uses frame_index = head->frame_index + f
+ * and reset_accum only for f == 0 (each later frame continues the running mean),
+ * exactly as `frames` back-to-back reference dispatches would.  Frames are
+ * batched into device waves; results do not depend on the batching. */
+int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
+                  uint32_t frames);
+/* Same as pt_gpu_render, then copies the accumulation buffer to host_rgba
+ * (W*H*4 floats).  This is the end-to-end call a host engine makes. */
+int pt_gpu_render_to_host(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
+                          uint32_t frames, float* host_rgba);
+int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out);
+/* on != 0: record CUDA events around every closest-hit and transmittance
+ * launch so PtStats.extend_ms / shadow_ms report their device time. */
+int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on);
+
+/* Max number of frames batched into one device wave (default: chosen from the
+ * frame size so a wave holds about 16 M paths). 0 restores the default. */
+int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave);
+
+/* ---- parity probe: traceScene for arbitrary rays (shaders/PathTrace.slang:2331-2693) ----
+ * ray_o: n float4 (origin xyz, w unused); ray_d: n float4 (direction xyz,
+ * w = initial closest distance; <= 0 means the reference's 1e30).
+ * hit_id out: 0xFFFFFFFF = miss; (0 << 30 | slot) = analytic record `slot` of the
+ * uploaded buffer; (1u << 30 | tri) = original triangle index.  t out: hit distance.
+ * on_device != 0: all four pointers are device pointers. */
+int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d,
+                         uint32_t n, uint32_t* hit_id, float* t, int on_device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_GPU_H */

@@ -1,0 +1,159 @@
+/*
+ * pt_scene.h -- C-ABI of the host-side scene builder that feeds pt_gpu.h.
+ *
+ * It keeps the reference's scene API and packing rules so the GPU path is a
+ * drop-in for the reference engine's upload step:
+ *   - analytic prims keyed by user id in id order (the reference's
+ *     std::map<uint32_t, AnalyticPrim>, src/engine/Engine.h:836), planes
+ *     first, finite prims permuted into BVH leaf order, 28 floats per prim
+ *     (src/engine/Engine.cpp:4743-5003);
+ *   - the binary centroid-median BVHs (src/renderer/AnalyticBvh.cpp:369-486,
+ *     src/renderer/TriangleBvh.cpp:33-169), bit-identical trees;
+ *   - analytic lights, 20 floats per light (src/engine/Engine.cpp:5235-5330,
+ *     commands light_point/spot/sphere/quad at :20308-20420);
+ *   - env map: HDRI bright-cluster extraction + env CDF
+ *     (src/engine/Engine.cpp:4329-4580, src/renderer/HdrImage.cpp:169-219);
+ *   - camera basis (src/renderer/Camera.h:18-30) and the push fill
+ *     (src/engine/Engine.cpp:7821-7931, 8640-8676);
+ *   - the in-scope cvars with the reference defaults.
+ * It also holds the seeded synthetic scene generators used by the benchmark.
+ */
+#ifndef PT_SCENE_H
+#define PT_SCENE_H
+
+#include <stdint.h>
+#include "pt_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pt_scene pt_scene;
+
+/* material ids as in the reference (src/engine/Engine.h:187) */
+#define PT_MAT_LAMBERT    0
+#define PT_MAT_METAL      1
+#define PT_MAT_DIELECTRIC 2
+
+int         pt_scene_create(pt_scene** out);
+int         pt_scene_destroy(pt_scene* s);
+const char* pt_scene_last_error(const pt_scene* s);
+int         pt_scene_clear(pt_scene* s);
+
+/* prim_sphere <id> <x> <y> <z> <radius> <mat> <r> <g> <b> [roughness] [ior]
+ * (src/engine/Engine.cpp:16783-16832) */
+int pt_scene_prim_sphere(pt_scene* s, uint32_t id, float x, float y, float z, float radius,
+                         int material, float r, float g, float b, float roughness, float ior);
+/* prim_plane <id> <nx> <ny> <nz> <d> <mat> <r> <g> <b> [roughness] [ior]
+ * (src/engine/Engine.cpp:16834-16880) */
+int pt_scene_prim_plane(pt_scene* s, uint32_t id, float nx, float ny, float nz, float d,
+                        int material, float r, float g, float b, float roughness, float ior);
+/* per-prim emission (W/sr per channel) and orientation quaternion (xyzw) */
+int pt_scene_prim_set_emission(pt_scene* s, uint32_t id, float r, float g, float b);
+int pt_scene_prim_set_orient(pt_scene* s, uint32_t id, float qx, float qy, float qz, float qw);
+
+/* light_quad <id> <x y z> <nx ny nz> <ux uy uz> <u_half> <v_half> <r g b>
+ * (src/engine/Engine.cpp:20403-20450) */
+int pt_scene_light_quad(pt_scene* s, uint32_t id, float x, float y, float z,
+                        float nx, float ny, float nz, float ux, float uy, float uz,
+                        float u_half, float v_half, float r, float g, float b);
+int pt_scene_light_point(pt_scene* s, uint32_t id, float x, float y, float z,
+                         float r, float g, float b);
+int pt_scene_light_sphere(pt_scene* s, uint32_t id, float x, float y, float z, float radius,
+                          float r, float g, float b);
+int pt_scene_light_spot(pt_scene* s, uint32_t id, float x, float y, float z,
+                        float dx, float dy, float dz, float outer_deg, float inner_deg,
+                        float r, float g, float b);
+
+/* Triangle mesh in world space.  mat_ids (nullable) index the material table. */
+int pt_scene_set_mesh(pt_scene* s, const float* positions, uint32_t nv,
+                      const uint32_t* indices, uint32_t nt, const uint32_t* mat_ids);
+/* mats: n records of 12 floats (see pt_gpu_upload_materials) */
+int pt_scene_set_materials(pt_scene* s, const float* mats12, uint32_t n);
+
+/* Env map from linear RGB float[3*W*H] (rows top to bottom, the reference's
+ * LoadRadianceHdr layout).  Runs the reference's cluster extraction with
+ * r_hdri_extract_percentile and builds the masked CDF.  W = H = 0 clears it.
+ * A "black env" is an all-zero image: present, total luminance 0. */
+int pt_scene_set_env(pt_scene* s, const float* rgb, uint32_t W, uint32_t H);
+
+/* Camera (src/renderer/Camera.h): position, yaw/pitch (radians), vertical fov (deg). */
+int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float pitch,
+                        float fov_deg);
+
+/* In-scope cvars with the reference defaults (names as in src/engine/Engine.cpp):
+ * r_max_bounces 8, r_spp 1, r_mis 1, r_firefly_clamp 10, r_caustics 1,
+ * r_refract_bounces 4, r_env_intensity 1, r_accum_ema_alpha 0,
+ * r_analytic_bvh_threshold 16, r_hdri_extract_percentile 0.005, r_light_tree 0,
+ * r_rr_start 2 (extension), r_denoiser 0. Returns PT_ERR_INVALID for unknown names. */
+int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
+int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);
+
+/* Pack everything (idempotent; called by the accessors below when dirty). */
+int pt_scene_pack(pt_scene* s);
+
+/* Views of the packed buffers (valid until the next mutation). */
+typedef struct PtPackedScene {
+    const float*     prims;        /* 28 floats per record */
+    uint32_t         prim_count;
+    uint32_t         linear_prim_count;
+    const PtBvhNode* bvh_nodes;
+    uint32_t         bvh_node_count;
+    const float*     positions;
+    uint32_t         vertex_count;
+    const uint32_t*  indices;
+    uint32_t         tri_count;
+    const PtBvhNode* tri_nodes;
+    uint32_t         tri_node_count;
+    const uint32_t*  tri_perm;
+    uint32_t         tri_perm_count;
+    const uint32_t*  tri_mat_ids;   /* NULL when the mesh has no material ids */
+    const float*     materials;     /* 12 floats per material */
+    uint32_t         material_count;
+    const float*     lights;        /* 20 floats per light */
+    uint32_t         light_count;
+    const float*     env_rgba;
+    uint32_t         env_w, env_h;
+    const float*     env_marginal;
+    const float*     env_conditional;
+    double           env_total_luminance;
+    uint32_t         hdri_count;
+    const float*     hdri_dir_pmf;  /* 8 float4 */
+    const float*     hdri_col;      /* 8 float4 */
+    uint32_t         env_present;
+} PtPackedScene;
+int pt_scene_packed(pt_scene* s, PtPackedScene* out);
+
+/* Push head + tail for frame `frame_index` of a W x H target. */
+int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t frame_index,
+                       uint32_t reset_accum, PtPushHead* head, PtPathParams* params);
+
+/* Upload the packed scene into a GPU context (all pt_gpu_upload_* calls). */
+int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
+
+/* Seeded synthetic scenes (PCG32 stream, seed 0x5EED + config id):
+ *   0: 64 spheres + 4 boxes (12-tri meshes) + one 1x1 quad light (radiance 15), black env;
+ *   1: 200 displaced icospheres (nu = 22, 9680 tris each) on a 512x512 quad-grid ground,
+ *      1024 spheres, 2048x1024 log-normal env with a 0.5 deg sun disc of 1e4, 256 materials.
+ * scale (0 < scale <= 1) shrinks the triangle/sphere/env counts for fast tests
+ * (1 = the full configuration).  Sets the camera and cvars of the config. */
+int pt_scene_synth(pt_scene* s, int config_id, uint64_t seed, double scale);
+
+/* ---- reference builders, exposed for parity tests ---- */
+/* AnalyticBvh::Build over (center, radius, prim_id) records (5 x 4 bytes each).
+ * nodes_out capacity >= 2n; perm_out capacity n.  Returns node count via *n_nodes. */
+int pt_build_analytic_bvh(const float* centers_radii /* 4 floats per prim */, uint32_t n,
+                          PtBvhNode* nodes_out, uint32_t* n_nodes, uint32_t* perm_out);
+/* TriangleBvh::Build; nodes_out capacity >= 2*nt; perm_out capacity nt. */
+int pt_build_triangle_bvh(const float* positions, uint32_t nv, const uint32_t* indices,
+                          uint32_t n_index, PtBvhNode* nodes_out, uint32_t* n_nodes,
+                          uint32_t* perm_out, uint32_t* n_perm);
+/* BuildEnvCdf (mask may be NULL); returns the total in *total. */
+int pt_build_env_cdf(const float* rgb, uint32_t W, uint32_t H, const uint8_t* mask,
+                     float* marginal, float* conditional, double* total);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_SCENE_H */

@@ -1,0 +1,148 @@
+"""TEST INFRASTRUCTURE ONLY -- ctypes binding of the CPU oracle.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this package, as the checker / baseline; the product never imports it.
+
+  liboracle.so        CPU restatement of the reference path tracer (fp32 + fp64),
+                      built from oracle/pt_oracle.cpp by oracle/Makefile
+  _ref/libref_builders.so
+                      the reference's own AnalyticBvh / TriangleBvh / BuildEnvCdf
+                      compiled from the reference sources (only where the
+                      reference tree is present; never shipped)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_builders.so")
+REF_TREE = os.environ.get("PT_REFERENCE_TREE", "/root/reference")
+
+u32 = ctypes.c_uint32
+f32 = ctypes.c_float
+P = ctypes.POINTER
+
+
+class OracleCounters(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_uint64), ("nodes", ctypes.c_uint64), ("tris", ctypes.c_uint64),
+                ("prims", ctypes.c_uint64), ("ext_rays", ctypes.c_uint64),
+                ("shadow_rays", ctypes.c_uint64), ("ext_nodes", ctypes.c_uint64),
+                ("ext_tris", ctypes.c_uint64), ("ext_prims", ctypes.c_uint64)]
+
+
+def build(ref: bool | None = None):
+    """make -C oracle (and the reference builders when the reference tree exists)."""
+    targets = ["all"]
+    if ref is None:
+        ref = os.path.isdir(os.path.join(REF_TREE, "src", "renderer"))
+    if ref:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_TREE}", *targets], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build(ref=False)
+        _lib = ctypes.CDLL(LIB)
+        _lib.oracle_trace.restype = ctypes.c_int
+        _lib.oracle_render.restype = ctypes.c_int
+        for n in ("oracle_sinf", "oracle_cosf", "oracle_acosf"):
+            getattr(_lib, n).restype = f32
+            getattr(_lib, n).argtypes = [f32]
+        _lib.oracle_atan2f.restype = f32
+        _lib.oracle_atan2f.argtypes = [f32, f32]
+        _lib.oracle_pcg_hash.restype = u32
+        _lib.oracle_pcg_hash.argtypes = [u32]
+    return _lib
+
+
+def load_ref():
+    """The reference's builders compiled from source, or None where unavailable."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB):
+        _ref = ctypes.CDLL(REF_LIB)
+    return _ref
+
+
+def render(packed, head, prm, W, H, frames=1, accum=None, crop=None, fp64=False, threads=0):
+    """Render `frames` frames; returns (accum (H, W, 4) float32, OracleCounters)."""
+    lib = load()
+    if accum is None:
+        accum = np.zeros((H, W, 4), np.float32)
+    x0, y0, x1, y1 = crop if crop is not None else (0, 0, W, H)
+    c = OracleCounters()
+    rc = lib.oracle_render(ctypes.byref(packed), ctypes.byref(head), ctypes.byref(prm), u32(W), u32(H),
+                           u32(frames), accum.ctypes.data_as(P(f32)), u32(x0), u32(y0), u32(x1), u32(y1),
+                           ctypes.c_int(1 if fp64 else 0), ctypes.c_int(threads), ctypes.byref(c))
+    if rc != 0:
+        raise RuntimeError(f"oracle_render failed: {rc}")
+    return accum, c
+
+
+def trace(packed, head, prm, ro4, rd4, fp64=False):
+    lib = load()
+    ro4 = np.ascontiguousarray(ro4, np.float32)
+    rd4 = np.ascontiguousarray(rd4, np.float32)
+    n = ro4.shape[0]
+    hit = np.empty(n, np.uint32)
+    t = np.empty(n, np.float32)
+    c = OracleCounters()
+    rc = lib.oracle_trace(ctypes.byref(packed), ctypes.byref(head), ctypes.byref(prm),
+                          ro4.ctypes.data_as(P(f32)), rd4.ctypes.data_as(P(f32)), u32(n),
+                          hit.ctypes.data_as(P(u32)), t.ctypes.data_as(P(f32)),
+                          ctypes.c_int(1 if fp64 else 0), ctypes.byref(c))
+    if rc != 0:
+        raise RuntimeError(f"oracle_trace failed: {rc}")
+    return hit, t, c
+
+
+def ref_analytic_bvh(centers_radii):
+    """AnalyticBvh::Build of the reference itself: (nodes (m, 8) uint32, perm)."""
+    lib = load_ref()
+    cr = np.ascontiguousarray(centers_radii, np.float32)
+    n = cr.shape[0]
+    nodes = np.zeros((max(2 * n, 1), 8), np.uint32)
+    perm = np.zeros(max(n, 1), np.uint32)
+    m = u32()
+    lib.ref_build_analytic_bvh(cr.ctypes.data_as(P(f32)), u32(n), nodes.ctypes.data_as(ctypes.c_void_p),
+                               ctypes.byref(m), perm.ctypes.data_as(P(u32)))
+    return nodes[: m.value].copy(), perm[:n].copy()
+
+
+def ref_triangle_bvh(positions, indices):
+    lib = load_ref()
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+    idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    nt = max(idx.size // 3, 1)
+    nodes = np.zeros((2 * nt, 8), np.uint32)
+    perm = np.zeros(nt, np.uint32)
+    m, k = u32(), u32()
+    lib.ref_build_triangle_bvh(pos.ctypes.data_as(P(f32)), u32(pos.size // 3), idx.ctypes.data_as(P(u32)),
+                               u32(idx.size), nodes.ctypes.data_as(ctypes.c_void_p), ctypes.byref(m),
+                               perm.ctypes.data_as(P(u32)), ctypes.byref(k))
+    return nodes[: m.value].copy(), perm[: k.value].copy()
+
+
+def ref_env_cdf(rgb, mask=None):
+    lib = load_ref()
+    a = np.ascontiguousarray(rgb, np.float32)
+    H, W = a.shape[:2]
+    marg = np.zeros(H, np.float32)
+    cond = np.zeros(H * W, np.float32)
+    tot = ctypes.c_double()
+    mk = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib.ref_build_env_cdf(a.ctypes.data_as(P(f32)), u32(W), u32(H),
+                          None if mk is None else mk.ctypes.data_as(P(ctypes.c_uint8)),
+                          marg.ctypes.data_as(P(f32)), cond.ctypes.data_as(P(f32)), ctypes.byref(tot))
+    return marg, cond.reshape(H, W), tot.value

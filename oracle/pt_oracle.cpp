@@ -1,0 +1,925 @@
+// TEST INFRASTRUCTURE ONLY -- CPU oracle of the reference path tracer.
+//
+// Restates, function by function, the in-scope subset of
+// shaders/PathTrace.slang and shaders/PathTraceMath.slang as a scalar
+// per-pixel loop (the shader's own structure), templated on the float type.
+// Citations are to the reference's files.  Compile with -ffp-contract=off:
+// the fp32 instance must round exactly as written.
+
+#include "pt_oracle.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Polynomial transcendentals (fp32).  Not libm: both this oracle and the GPU
+// kernels evaluate these exact expressions, so their results agree bit for
+// bit.  sin/cos: Cody-Waite reduction by pi/2 with a 3-part constant, then the
+// Taylor series of sin (to r^9) and cos (to r^10) on |r| <= pi/4.
+// atan: Taylor series to w^17 on |w| <= tan(pi/8), with atan(z) =
+// pi/4 + atan((z-1)/(z+1)) above that.  acos(x) = atan2(sqrt((1-x)(1+x)), x).
+// ---------------------------------------------------------------------------
+constexpr float kPio2Hi = 0x1.92p+0f;        // 1.5703125 (8 significant bits)
+constexpr float kPio2Mid = 0x1.fb54p-12f;    // next 16 bits of pi/2
+constexpr float kPio2Lo = 0x1.10b462p-30f;   // remainder
+constexpr float kTwoOverPi = 0x1.45f306p-1f;
+constexpr float kPiF = 0x1.921fb6p+1f;
+constexpr float kPio2F = 0x1.921fb6p+0f;
+constexpr float kPio4F = 0x1.921fb6p-1f;
+constexpr float kTanPi8 = 0x1.a8279ap-2f;
+
+constexpr float kS1 = float(-1.0 / 6.0), kS2 = float(1.0 / 120.0), kS3 = float(-1.0 / 5040.0),
+                kS4 = float(1.0 / 362880.0);
+constexpr float kC1 = -0.5f, kC2 = float(1.0 / 24.0), kC3 = float(-1.0 / 720.0),
+                kC4 = float(1.0 / 40320.0), kC5 = float(-1.0 / 3628800.0);
+constexpr float kA1 = float(-1.0 / 3.0), kA2 = float(1.0 / 5.0), kA3 = float(-1.0 / 7.0),
+                kA4 = float(1.0 / 9.0), kA5 = float(-1.0 / 11.0), kA6 = float(1.0 / 13.0),
+                kA7 = float(-1.0 / 15.0), kA8 = float(1.0 / 17.0);
+
+inline float poly_sin(float r) {
+    const float r2 = r * r;
+    float p = kS4;
+    p = p * r2 + kS3;
+    p = p * r2 + kS2;
+    p = p * r2 + kS1;
+    return r + (r * r2) * p;
+}
+inline float poly_cos(float r) {
+    const float r2 = r * r;
+    float q = kC5;
+    q = q * r2 + kC4;
+    q = q * r2 + kC3;
+    q = q * r2 + kC2;
+    q = q * r2 + kC1;
+    return 1.0f + r2 * q;
+}
+inline float reduce_pio2(float x, int& quadrant) {
+    const float k = std::nearbyint(x * kTwoOverPi);
+    float r = x - k * kPio2Hi;
+    r = r - k * kPio2Mid;
+    r = r - k * kPio2Lo;
+    quadrant = int(k) & 3;
+    return r;
+}
+inline float f_sin(float x) {
+    int q;
+    const float r = reduce_pio2(x, q);
+    switch (q) {
+        case 0: return poly_sin(r);
+        case 1: return poly_cos(r);
+        case 2: return -poly_sin(r);
+        default: return -poly_cos(r);
+    }
+}
+inline float f_cos(float x) {
+    int q;
+    const float r = reduce_pio2(x, q);
+    switch (q) {
+        case 0: return poly_cos(r);
+        case 1: return -poly_sin(r);
+        case 2: return -poly_cos(r);
+        default: return poly_sin(r);
+    }
+}
+inline float atan_poly(float w) {
+    const float w2 = w * w;
+    float p = kA8;
+    p = p * w2 + kA7;
+    p = p * w2 + kA6;
+    p = p * w2 + kA5;
+    p = p * w2 + kA4;
+    p = p * w2 + kA3;
+    p = p * w2 + kA2;
+    p = p * w2 + kA1;
+    return w + (w * w2) * p;
+}
+inline float atan_unit(float z) {   // 0 <= z <= 1
+    if (z > kTanPi8) return kPio4F + atan_poly((z - 1.0f) / (z + 1.0f));
+    return atan_poly(z);
+}
+inline float f_atan2(float y, float x) {
+    const float ax = std::fabs(x), ay = std::fabs(y);
+    if (ax == 0.0f && ay == 0.0f) return (x < 0.0f) ? kPiF : 0.0f;
+    const bool swap = ay > ax;
+    const float z = swap ? (ax / ay) : (ay / ax);
+    float a = atan_unit(z);
+    if (swap) a = kPio2F - a;
+    if (x < 0.0f) a = kPiF - a;
+    if (y < 0.0f) a = -a;
+    return a;
+}
+inline float f_acos(float x) {
+    const float s = std::sqrt((1.0f - x) * (1.0f + x));
+    return f_atan2(s, x);
+}
+
+template <class R> struct M;
+template <> struct M<float> {
+    static float sin(float x) { return f_sin(x); }
+    static float cos(float x) { return f_cos(x); }
+    static float atan2(float y, float x) { return f_atan2(y, x); }
+    static float acos(float x) { return f_acos(x); }
+};
+template <> struct M<double> {
+    static double sin(double x) { return std::sin(x); }
+    static double cos(double x) { return std::cos(x); }
+    static double atan2(double y, double x) { return std::atan2(y, x); }
+    static double acos(double x) { return std::acos(x); }
+};
+
+// HLSL min/max return the non-NaN operand (IEEE minNum/maxNum).
+template <class R> inline R mn(R a, R b) { return std::fmin(a, b); }
+template <class R> inline R mx(R a, R b) { return std::fmax(a, b); }
+template <class R> inline R clampv(R v, R lo, R hi) { return mn(mx(v, lo), hi); }
+
+template <class R> struct V3 {
+    R x, y, z;
+};
+template <class R> inline V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <class R> inline V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R> inline V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R> inline V3<R> operator-(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+template <class R> inline V3<R> operator*(V3<R> a, V3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class R> inline V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R> inline V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R> inline V3<R> operator/(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R> inline V3<R> cross(V3<R> a, V3<R> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R> inline R length(V3<R> a) { return std::sqrt(dot(a, a)); }
+template <class R> inline V3<R> normalize(V3<R> a) {
+    const R inv = R(1) / std::sqrt(dot(a, a));
+    return a * inv;
+}
+template <class R> inline bool any_pos(V3<R> a) { return a.x > R(0) || a.y > R(0) || a.z > R(0); }
+template <class R> inline R lerp(R a, R b, R t) { return a + t * (b - a); }
+template <class R> inline V3<R> lerp(V3<R> a, V3<R> b, R t) { return a + t * (b - a); }
+// HLSL reflect / refract (shaders call reflect(rd, nf), refract(rd, nf, eta))
+template <class R> inline V3<R> reflect(V3<R> i, V3<R> n) { return i - (R(2) * dot(n, i)) * n; }
+template <class R> inline V3<R> refract(V3<R> i, V3<R> n, R eta) {
+    const R c = dot(n, i);
+    const R k = R(1) - (eta * eta) * (R(1) - c * c);
+    if (k < R(0)) return {R(0), R(0), R(0)};
+    return eta * i - (eta * c + std::sqrt(k)) * n;
+}
+template <class R> inline V3<R> ld3(const float* p) { return {R(p[0]), R(p[1]), R(p[2])}; }
+inline uint32_t asuint(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+// shaders/PathTraceMath.slang:16-24
+inline uint32_t pcg_hash(uint32_t x) {
+    x = x * 747796405u + 2891336453u;
+    x = ((x >> ((x >> 28u) + 4u)) ^ x) * 277803737u;
+    return (x >> 22u) ^ x;
+}
+template <class R> inline R randf(uint32_t& seed) {
+    seed = pcg_hash(seed);
+    return R(seed & 0x00FFFFFFu) / R(16777216.0);
+}
+
+// shaders/PathTrace.slang:2028-2031
+template <class R> inline V3<R> quat_rotate(const float* q, V3<R> v) {
+    const V3<R> u = ld3<R>(q);
+    return v + R(2) * cross(u, cross(u, v) + R(q[3]) * v);
+}
+
+constexpr uint32_t kMatLambert = 0, kMatMetal = 1, kMatDielectric = 2;
+constexpr uint32_t kHitMiss = 0xFFFFFFFFu;
+
+template <class R> struct Hit {
+    bool hit = false;
+    R t = R(1e30);
+    V3<R> normal{R(0), R(1), R(0)};
+    uint32_t mat = kMatLambert;
+    V3<R> albedo{R(0.5), R(0.5), R(0.5)};
+    R roughness = R(0);
+    R ior = R(1);
+    V3<R> emission{R(0), R(0), R(0)};
+    uint32_t id = kHitMiss;   // (0<<30 | record slot) or (1<<30 | triangle)
+};
+
+struct Counters {
+    uint64_t rays = 0, nodes = 0, tris = 0, prims = 0, ext = 0, shadow = 0;
+    uint64_t ext_nodes = 0, ext_tris = 0, ext_prims = 0;   // extension segments only
+    void add(const Counters& o) {
+        rays += o.rays; nodes += o.nodes; tris += o.tris; prims += o.prims;
+        ext += o.ext; shadow += o.shadow;
+        ext_nodes += o.ext_nodes; ext_tris += o.ext_tris; ext_prims += o.ext_prims;
+    }
+};
+
+template <class R> struct Tracer {
+    const PtPackedScene& S;
+    const PtPushHead& P;
+    const PtPathParams& Q;
+    uint32_t W, H;
+    Counters cnt;
+
+    // constants (literal values of the shader, rounded once to R)
+    const R kPi = R(3.14159265358979);
+    const R kTwoPi = R(6.28318530717958);
+    const R kInvPi = R(1.0 / 3.14159265358979);
+
+    Tracer(const PtPackedScene& s, const PtPushHead& p, const PtPathParams& q, uint32_t w, uint32_t h)
+        : S(s), P(p), Q(q), W(w), H(h) {}
+
+    // --- traceScene (shaders/PathTrace.slang:2066-2161, 2321-2434, 2548-2691) ---
+    void test_prim(uint32_t idx, V3<R> ro, V3<R> rd, R shutter, Hit<R>& h) {
+        cnt.prims++;
+        const float* v = S.prims + size_t(idx) * 28;
+        const uint32_t type = uint32_t(v[8]);
+        R t;
+        if (type == 0u) {   // PRIM_SPHERE, intersectSphere (PathTraceMath.slang:194-204)
+            const V3<R> c = lerp(ld3<R>(v + 12), ld3<R>(v), shutter);
+            const R rad = R(v[3]);
+            const V3<R> oc = ro - c;
+            const R b = dot(oc, rd);
+            const R k = dot(oc, oc) - rad * rad;
+            R hh = b * b - k;
+            if (hh < R(0)) return;
+            hh = std::sqrt(hh);
+            const R t0 = -b - hh, t1 = -b + hh;
+            t = (t0 > R(1e-3)) ? t0 : t1;
+            if (!(t > R(1e-3)) || !(t < h.t)) return;
+            h.hit = true;
+            h.t = t;
+            h.normal = normalize(ro + rd * t - c);
+        } else if (type == 1u) {   // PRIM_PLANE, intersectPlane (PathTraceMath.slang:209-214)
+            const V3<R> n = quat_rotate<R>(v + 20, ld3<R>(v));
+            const R denom = dot(rd, n);
+            if (std::fabs(denom) < R(1e-4)) return;
+            t = -(dot(ro, n) + R(v[3])) / denom;
+            if (!(t > R(1e-3)) || !(t < h.t)) return;
+            h.hit = true;
+            h.t = t;
+            h.normal = n;
+        } else {
+            return;
+        }
+        h.mat = uint32_t(v[9]);
+        h.albedo = ld3<R>(v + 4);
+        h.roughness = R(v[7]);
+        h.ior = R(v[10]);
+        h.emission = ld3<R>(v + 16);
+        h.id = idx;
+    }
+
+    static bool slab(V3<R> ro, V3<R> inv, const PtBvhNode& n, R tmax) {
+        const V3<R> bmin = ld3<R>(n.aabb_min), bmax = ld3<R>(n.aabb_max);
+        const V3<R> t0 = (bmin - ro) * inv, t1 = (bmax - ro) * inv;
+        const R tmin = mx(mx(mn(t0.x, t1.x), mn(t0.y, t1.y)), mn(t0.z, t1.z));
+        const R tmx = mn(mn(mx(t0.x, t1.x), mx(t0.y, t1.y)), mx(t0.z, t1.z));
+        return tmx >= mx(tmin, R(0)) && tmin <= tmax;
+    }
+
+    static V3<R> safe_inv(V3<R> rd) {
+        auto s = [](R a) { return (std::fabs(a) > R(1e-30)) ? a : R(1e-30); };
+        return {R(1) / s(rd.x), R(1) / s(rd.y), R(1) / s(rd.z)};
+    }
+
+    Hit<R> trace(V3<R> ro, V3<R> rd, R t_init = R(1e30)) {
+        cnt.rays++;
+        const R shutter = R(1);   // motion blur off
+        Hit<R> h;
+        h.t = t_init;
+        const uint32_t linear = Q.bvh_params[0];
+        const uint32_t nodes = Q.bvh_params[1];
+        const uint32_t pc = P.prim_count;
+        for (uint32_t i = 0; i < linear && i < pc; ++i) test_prim(i, ro, rd, shutter, h);
+        if (nodes == 0u) {
+            for (uint32_t i = linear; i < pc; ++i) test_prim(i, ro, rd, shutter, h);
+        } else {
+            const V3<R> inv = safe_inv(rd);
+            uint32_t stack[32];
+            int sp = 0;
+            stack[sp++] = 0u;
+            while (sp > 0) {
+                const uint32_t idx = stack[--sp];
+                const PtBvhNode& n = S.bvh_nodes[idx];
+                cnt.nodes++;
+                if (!slab(ro, inv, n, h.t)) continue;
+                if (n.count > 0u) {
+                    const uint32_t base = n.left_first + linear;
+                    for (uint32_t k = 0; k < n.count; ++k) test_prim(base + k, ro, rd, shutter, h);
+                } else if (sp + 2 <= 32) {
+                    stack[sp++] = n.left_first;
+                    stack[sp++] = n.left_first + 1u;
+                }
+            }
+        }
+        if (Q.bvh_params[2] != 0u) {
+            const uint32_t tnodes = Q.bvh_params[3];
+            R t_mesh = h.t;
+            uint32_t prim_hit = 0;
+            bool found = false;
+            if (tnodes > 0u) {
+                const V3<R> inv = safe_inv(rd);
+                uint32_t stack[64];
+                int sp = 0;
+                stack[sp++] = 0u;
+                while (sp > 0) {
+                    const uint32_t idx = stack[--sp];
+                    const PtBvhNode& n = S.tri_nodes[idx];
+                    cnt.nodes++;
+                    if (!slab(ro, inv, n, t_mesh)) continue;
+                    if (n.count > 0u) {
+                        for (uint32_t k = 0; k < n.count; ++k) {
+                            cnt.tris++;
+                            const uint32_t tri = S.tri_perm[n.left_first + k];
+                            const V3<R> v0 = ld3<R>(S.positions + 3u * S.indices[tri * 3u + 0u]);
+                            const V3<R> v1 = ld3<R>(S.positions + 3u * S.indices[tri * 3u + 1u]);
+                            const V3<R> v2 = ld3<R>(S.positions + 3u * S.indices[tri * 3u + 2u]);
+                            const V3<R> e1 = v1 - v0, e2 = v2 - v0;
+                            const V3<R> pv = cross(rd, e2);
+                            const R det = dot(e1, pv);
+                            if (std::fabs(det) < R(1e-8)) continue;
+                            const R inv_det = R(1) / det;
+                            const V3<R> tvec = ro - v0;
+                            const R u = dot(tvec, pv) * inv_det;
+                            if (u < R(0) || u > R(1)) continue;
+                            const V3<R> qv = cross(tvec, e1);
+                            const R vv = dot(rd, qv) * inv_det;
+                            if (vv < R(0) || u + vv > R(1)) continue;
+                            const R tt = dot(e2, qv) * inv_det;
+                            if (tt > R(1e-3) && tt < t_mesh) {
+                                found = true;
+                                t_mesh = tt;
+                                prim_hit = tri;
+                            }
+                        }
+                    } else if (sp + 2 <= 64) {
+                        stack[sp++] = n.left_first;
+                        stack[sp++] = n.left_first + 1u;
+                    }
+                }
+            }
+            if (found) {
+                const V3<R> v0 = ld3<R>(S.positions + 3u * S.indices[prim_hit * 3u + 0u]);
+                const V3<R> v1 = ld3<R>(S.positions + 3u * S.indices[prim_hit * 3u + 1u]);
+                const V3<R> v2 = ld3<R>(S.positions + 3u * S.indices[prim_hit * 3u + 2u]);
+                h.hit = true;
+                h.t = t_mesh;
+                h.normal = normalize(cross(v1 - v0, v2 - v0));
+                h.id = (1u << 30) | prim_hit;
+                if (S.tri_mat_ids && S.material_count > 0) {   // material table extension
+                    uint32_t m = S.tri_mat_ids[prim_hit];
+                    if (m >= S.material_count) m = S.material_count - 1;
+                    const float* mt = S.materials + size_t(m) * 12;
+                    h.mat = uint32_t(mt[8]);
+                    h.albedo = ld3<R>(mt);
+                    h.roughness = R(mt[3]);
+                    h.emission = ld3<R>(mt + 4);
+                    h.ior = R(mt[7]);
+                } else {   // MESH_ALBEDO gold metal (PathTrace.slang:1428, 2655-2658)
+                    h.mat = kMatMetal;
+                    h.albedo = {R(1.00), R(0.85), R(0.45)};
+                    h.roughness = R(0.05);
+                    h.ior = R(1);
+                    h.emission = {R(0), R(0), R(0)};
+                }
+            }
+        }
+        return h;
+    }
+
+    // --- clampIndirect (PathTrace.slang:3367-3371) ---
+    V3<R> clamp_ind(V3<R> c) const {
+        const R w = R(Q.firefly_clamp);
+        if (w <= R(0)) return c;
+        const R m = mx(c.x, mx(c.y, c.z));
+        return (m > w) ? c * (w / m) : c;
+    }
+
+    // --- env map (PathTrace.slang:3401-3431, 3619-3735) ---
+    V3<R> texel(uint32_t u, uint32_t v) const {
+        return ld3<R>(S.env_rgba + (size_t(v) * S.env_w + u) * 4);
+    }
+    V3<R> sky_color(V3<R> rd) const {
+        if (!P.env_map_present) {
+            // gradient sky (PathTrace.slang:3391-3392); sun/moon discs are not built
+            const R t = clampv(R(0.5) * (rd.y + R(1)), R(0), R(1));
+            return lerp(V3<R>{R(0.50), R(0.55), R(0.62)}, V3<R>{R(1), R(1), R(1)}, t);
+        }
+        const int32_t w = int32_t(S.env_w), hh = int32_t(S.env_h);
+        const R u = M<R>::atan2(rd.z, rd.x) * R(1.0 / 6.28318530718) + R(0.5);
+        const R v = M<R>::acos(clampv(rd.y, R(-1), R(1))) * R(1.0 / 3.14159265359);
+        const R fx = u * R(w) - R(0.5), fy = v * R(hh) - R(0.5);
+        const int32_t ix = int32_t(std::floor(fx)), iy = int32_t(std::floor(fy));
+        const R tx = fx - R(ix), ty = fy - R(iy);
+        const int32_t x0 = (ix % w + w) % w, x1 = (x0 + 1) % w;
+        const int32_t y0 = std::min(std::max(iy, 0), hh - 1), y1 = std::min(std::max(iy + 1, 0), hh - 1);
+        const V3<R> c00 = texel(x0, y0), c10 = texel(x1, y0), c01 = texel(x0, y1), c11 = texel(x1, y1);
+        const V3<R> sky = lerp(lerp(c00, c10, tx), lerp(c01, c11, tx), ty);
+        return sky * R(P.env_intensity);
+    }
+    uint32_t cdf_search(const float* cdf, uint32_t count, R u) const {
+        uint32_t lo = 0, hi = count;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (R(cdf[mid]) < u) lo = mid + 1;
+            else hi = mid;
+        }
+        return std::min(lo, count - 1);
+    }
+    R env_denom() const {   // 2.0 * pi * pi * total, left to right
+        return R(2.0) * kPi * kPi * R(P.env_total_luminance);
+    }
+    struct EnvSample { V3<R> dir; V3<R> color; R pdf; };
+    EnvSample sample_env(R xu, R xv) const {
+        EnvSample s{{R(0), R(1), R(0)}, {R(0), R(0), R(0)}, R(0)};
+        if (P.env_map_present == 0u || !(P.env_total_luminance > 0.0f)) return s;
+        const uint32_t w = S.env_w, hh = S.env_h;
+        const uint32_t vi = cdf_search(S.env_marginal, hh, xv);
+        const uint32_t ui = cdf_search(S.env_conditional + size_t(vi) * w, w, xu);
+        const R u = (R(ui) + R(0.5)) / R(w);
+        const R v = (R(vi) + R(0.5)) / R(hh);
+        const R theta = v * kPi;
+        const R phi = u * kTwoPi - kPi;
+        const R st = M<R>::sin(theta);
+        s.dir = {st * M<R>::cos(phi), M<R>::cos(theta), st * M<R>::sin(phi)};
+        const V3<R> raw = texel(ui, vi);
+        s.color = raw * R(P.env_intensity);
+        const R lum = R(0.2126) * raw.x + R(0.7152) * raw.y + R(0.0722) * raw.z;
+        if (st > R(1e-6)) s.pdf = (lum * R(w * hh)) / env_denom();
+        return s;
+    }
+    void dir_to_texel(V3<R> d, R& theta, R& st, uint32_t& ui, uint32_t& vi) const {
+        const R ct = clampv(d.y, R(-1), R(1));
+        theta = M<R>::acos(ct);
+        st = M<R>::sin(theta);
+        const R ph = M<R>::atan2(d.z, d.x);
+        const R u = (ph + kPi) * R(1.0 / 6.28318530717958);
+        const R v = theta * R(1.0 / 3.14159265358979);
+        ui = std::min(uint32_t(u * R(S.env_w)), S.env_w - 1u);
+        vi = std::min(uint32_t(v * R(S.env_h)), S.env_h - 1u);
+    }
+    bool is_cluster_dir(V3<R> d) const {
+        if (P.env_map_present == 0u || S.hdri_count == 0u) return false;
+        R th, st;
+        uint32_t ui, vi;
+        dir_to_texel(d, th, st, ui, vi);
+        if (st < R(1e-6)) return false;
+        const size_t base = size_t(vi) * S.env_w;
+        const R cc = R(S.env_conditional[base + ui]);
+        const R cp = (ui > 0u) ? R(S.env_conditional[base + ui - 1u]) : R(0);
+        return cc <= cp;
+    }
+    R pdf_env_dir(V3<R> d) const {
+        if (P.env_map_present == 0u || !(P.env_total_luminance > 0.0f)) return R(0);
+        R th, st;
+        uint32_t ui, vi;
+        dir_to_texel(d, th, st, ui, vi);
+        if (st < R(1e-6)) return R(0);
+        const V3<R> raw = texel(ui, vi);
+        const R lum = R(0.2126) * raw.x + R(0.7152) * raw.y + R(0.0722) * raw.z;
+        return (lum * R(S.env_w * S.env_h)) / env_denom();
+    }
+    static R mis_balance(R a, R b) { return a / mx(a + b, R(1e-12)); }
+
+    // --- sampleHdriLight (PathTrace.slang:3749-3768) ---
+    struct HdriSample { V3<R> dir; V3<R> color; R pdf; };
+    HdriSample sample_hdri(uint32_t& seed) const {
+        HdriSample s{{R(0), R(1), R(0)}, {R(0), R(0), R(0)}, R(0)};
+        if (S.hdri_count == 0u) return s;
+        const R u = randf<R>(seed);
+        R acc = R(0);
+        uint32_t sel = 0;
+        for (uint32_t i = 0; i < 8u; ++i) {
+            if (i >= S.hdri_count) break;
+            acc += R(S.hdri_dir_pmf[i * 4 + 3]);
+            if (u <= acc) { sel = i; break; }
+            sel = i;
+        }
+        s.dir = ld3<R>(S.hdri_dir_pmf + sel * 4);
+        s.color = ld3<R>(S.hdri_col + sel * 4) * R(P.env_intensity);
+        s.pdf = mx(R(S.hdri_dir_pmf[sel * 4 + 3]), R(1e-6));
+        return s;
+    }
+
+    // --- sampleAnalyticLight, uniform pick (PathTrace.slang:4035-4179) ---
+    struct LightSample { V3<R> dir; V3<R> Le; R pdf; R dist; };
+    LightSample sample_light(V3<R> hp, uint32_t& seed) const {
+        LightSample s{{R(0), R(1), R(0)}, {R(0), R(0), R(0)}, R(0), R(1e30)};
+        const uint32_t n = Q.light_count;
+        if (n == 0u) return s;
+        const R u_pick = randf<R>(seed);
+        const uint32_t pick = std::min(uint32_t(u_pick * R(n)), n - 1u);
+        const R pick_pdf = R(1) / R(n);
+        const float* L = S.lights + size_t(pick) * 20;
+        const uint32_t type = uint32_t(L[7] + 0.5f);
+        const V3<R> pos = ld3<R>(L);
+        const V3<R> inten = ld3<R>(L + 4);
+        if (type == 0u || type == 1u) {   // point / spot
+            const V3<R> tl = pos - hp;
+            const R d2 = mx(dot(tl, tl), R(1e-12));
+            const R d = std::sqrt(d2);
+            if (type == 0u) {
+                s.dir = tl / d;
+                s.Le = inten / d2;
+            } else {
+                const V3<R> tld = tl / d;
+                const V3<R> axis = normalize(quat_rotate<R>(L + 16, ld3<R>(L + 8)));
+                const R cos_dir = dot(-tld, axis);
+                const R cin = R(L[12]), cout = R(L[11]);
+                R fall = R(0);
+                if (cos_dir >= cin) fall = R(1);
+                else if (cos_dir > cout) fall = (cos_dir - cout) / mx(cin - cout, R(1e-6));
+                s.dir = tld;
+                s.Le = inten * (fall / d2);
+            }
+            s.pdf = pick_pdf;
+            s.dist = d;
+            return s;
+        }
+        if (type == 2u) {   // sphere: uniform area
+            const R x0 = randf<R>(seed);
+            const R x1 = randf<R>(seed);
+            const R z = R(1) - R(2) * x0;
+            const R r = std::sqrt(mx(R(0), R(1) - z * z));
+            const R phi = kTwoPi * x1;
+            const V3<R> nl{r * M<R>::cos(phi), r * M<R>::sin(phi), z};
+            const V3<R> lp = pos + nl * R(L[3]);
+            const V3<R> tl = lp - hp;
+            const R d2 = mx(dot(tl, tl), R(1e-12));
+            const R d = std::sqrt(d2);
+            const V3<R> wi = tl / d;
+            const R cl = mx(R(0), dot(nl, -wi));
+            if (cl <= R(0)) return s;
+            const R area = R(4.0) * kPi * R(L[3]) * R(L[3]);
+            const R pdf_sa = d2 / mx(area * cl, R(1e-12));
+            s.dir = wi;
+            s.Le = inten;
+            s.pdf = pick_pdf * pdf_sa;
+            s.dist = d;
+            return s;
+        }
+        if (type == 3u) {   // quad
+            const R xa = randf<R>(seed) * R(2) - R(1);
+            const R xb = randf<R>(seed) * R(2) - R(1);
+            const V3<R> uvec = quat_rotate<R>(L + 16, ld3<R>(L + 12));
+            const R ulen = length(uvec);
+            if (ulen < R(1e-6)) return s;
+            const V3<R> nq = normalize(quat_rotate<R>(L + 16, ld3<R>(L + 8)));
+            const V3<R> vax = normalize(cross(nq, uvec));
+            const V3<R> lp = pos + uvec * xa + vax * (R(L[15]) * xb);
+            const V3<R> tl = lp - hp;
+            const R d2 = mx(dot(tl, tl), R(1e-12));
+            const R d = std::sqrt(d2);
+            const V3<R> wi = tl / d;
+            const R cl = dot(nq, -wi);
+            if (cl <= R(0)) return s;
+            const R area = R(4.0) * ulen * R(L[15]);
+            const R pdf_sa = d2 / mx(area * cl, R(1e-12));
+            s.dir = wi;
+            s.Le = inten;
+            s.pdf = pick_pdf * pdf_sa;
+            s.dist = d;
+            return s;
+        }
+        return s;
+    }
+
+    // --- transmittance (PathTrace.slang:5089-5196), clouds/water off ---
+    V3<R> transmittance(V3<R> o, V3<R> d, R t_max) {
+        const int kmax = int(Q.refract_budget);
+        V3<R> t{R(1), R(1), R(1)};
+        for (int i = 0; i <= kmax; ++i) {
+            cnt.shadow++;
+            const Hit<R> h = trace(o, d);
+            if (!h.hit || h.t >= t_max) return t;
+            if (h.mat != kMatDielectric) return {R(0), R(0), R(0)};
+            if (i == kmax) return {R(0), R(0), R(0)};
+            const R ndi = dot(h.normal, d);
+            const V3<R> nf = (ndi < R(0)) ? h.normal : -h.normal;
+            const R ia = (ndi < R(0)) ? R(1) : h.ior;
+            const R ib = (ndi < R(0)) ? h.ior : R(1);
+            const R eta = ia / ib;
+            const R cos_i = std::fabs(dot(nf, -d));
+            const R r0 = ((ia - ib) / (ia + ib)) * ((ia - ib) / (ia + ib));
+            const R fr = schlick(cos_i, r0);
+            const V3<R> refr = refract(d, nf, eta);
+            if (length(refr) < R(1e-3)) return {R(0), R(0), R(0)};
+            t = t * ((R(1) - fr) * h.albedo);
+            const R adv = h.t + R(1e-3);
+            o = o + d * adv;
+            d = normalize(refr);
+            t_max = mx(t_max - adv, R(0));
+        }
+        return {R(0), R(0), R(0)};
+    }
+
+    // PathTraceMath.slang:73-76
+    static R schlick(R cos_t, R r0) {
+        const R m = R(1) - cos_t;
+        return r0 + (R(1) - r0) * m * m * m * m * m;
+    }
+    // PathTraceMath.slang:30-42
+    V3<R> cos_hemi(V3<R> n, uint32_t& seed) const {
+        const R u1 = randf<R>(seed);
+        const R u2 = randf<R>(seed);
+        const R r = std::sqrt(u1);
+        const R phi = R(6.28318530718) * u2;
+        const R x = r * M<R>::cos(phi);
+        const R y = r * M<R>::sin(phi);
+        const R z = std::sqrt(mx(R(0), R(1) - u1));
+        const V3<R> ax = (std::fabs(n.x) > R(0.9)) ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(1), R(0), R(0)};
+        const V3<R> t = normalize(cross(n, ax));
+        const V3<R> b = cross(n, t);
+        return normalize(t * x + b * y + n * z);
+    }
+
+    // --- one camera sample: the body of `for s < spp` (PathTrace.slang:5722-7705) ---
+    V3<R> sample_path(uint32_t px, uint32_t py, uint32_t s, uint32_t& seed) {
+        R jx, jy;
+        if (P.denoiser_enabled != 0u && s == 0u) {
+            jx = R(P.halton_jitter[0]);
+            jy = R(P.halton_jitter[1]);
+        } else {
+            const R a = randf<R>(seed);
+            const R b = randf<R>(seed);
+            jx = a - R(0.5);
+            jy = b - R(0.5);
+        }
+        const R ux = ((R(px) + R(0.5) + jx) / R(W)) * R(2) - R(1);
+        R uy = ((R(py) + R(0.5) + jy) / R(H)) * R(2) - R(1);
+        uy = -uy;
+        V3<R> ro = ld3<R>(P.pos_fovtan);
+        const R tanf = R(P.pos_fovtan[3]);
+        V3<R> rd = normalize(ld3<R>(P.fwd_aspect) + ld3<R>(P.right_xyz) * (ux * R(P.fwd_aspect[3]) * tanf) +
+                             ld3<R>(P.up_xyz) * (uy * tanf));
+        V3<R> thr{R(1), R(1), R(1)}, rad{R(0), R(0), R(0)};
+        bool skip_sky = false, prev_lambert = false;
+        R prev_pdf = R(0);
+        const bool env = P.env_map_present != 0u;
+        const uint32_t maxb = P.max_bounces;
+        for (uint32_t b = 0; b < maxb; ++b) {
+            cnt.ext++;
+            const uint64_t n0 = cnt.nodes, t0 = cnt.tris, p0 = cnt.prims;
+            Hit<R> h = trace(ro, rd);
+            cnt.ext_nodes += cnt.nodes - n0;
+            cnt.ext_tris += cnt.tris - t0;
+            cnt.ext_prims += cnt.prims - p0;
+            if (!h.hit) {
+                if (Q.mis_enabled != 0u && prev_lambert) {
+                    if (!is_cluster_dir(rd)) {
+                        const R pe = pdf_env_dir(rd);
+                        const R wb = mis_balance(prev_pdf, pe);
+                        // transmittance(ro, rd, 1e30) re-traces this same ray, which
+                        // just missed everything: it returns exactly (1,1,1).
+                        const V3<R> trans{R(1), R(1), R(1)};
+                        rad = rad + clamp_ind(thr * sky_color(rd) * trans * wb);
+                    }
+                } else if (!skip_sky) {
+                    if (b == 0u) rad = rad + thr * sky_color(rd);
+                    else rad = rad + clamp_ind(thr * sky_color(rd));
+                }
+                break;
+            }
+            const V3<R> hp = ro + rd * h.t;
+            const R ndi = dot(h.normal, rd);
+            const V3<R> nf = (ndi < R(0)) ? h.normal : -h.normal;
+            if (any_pos(h.emission)) {
+                if (b == 0u) rad = rad + thr * h.emission;
+                else rad = rad + clamp_ind(thr * h.emission);
+            }
+            if (h.mat == kMatLambert) {
+                if (Q.light_count > 0u) {
+                    const LightSample ls = sample_light(hp, seed);
+                    const R ndl = dot(nf, ls.dir);
+                    if (ls.pdf > R(0) && ndl > R(0)) {
+                        const R tmax = mx(ls.dist - R(1e-3), R(0));
+                        const V3<R> tr = transmittance(hp + nf * R(1e-3), ls.dir, tmax);
+                        if (any_pos(tr)) {
+                            const V3<R> brdf = h.albedo / kPi;
+                            const V3<R> c = thr * ls.Le * tr * brdf * ndl / ls.pdf;
+                            rad = rad + ((b == 0u) ? c : clamp_ind(c));
+                        }
+                    }
+                }
+                if (env) {
+                    const R xu = randf<R>(seed);
+                    const R xv = randf<R>(seed);
+                    const EnvSample es = sample_env(xu, xv);
+                    const R ndl = dot(nf, es.dir);
+                    if (es.pdf > R(0) && ndl > R(0)) {
+                        const V3<R> tr = transmittance(hp + nf * R(1e-3), es.dir, R(1e30));
+                        if (any_pos(tr)) {
+                            const V3<R> brdf = h.albedo / kPi;
+                            const R pdf_brdf = ndl * kInvPi;
+                            const bool fire = (Q.mis_enabled != 0u) && ((b + 1u) < maxb);
+                            const R wl = fire ? mis_balance(es.pdf, pdf_brdf) : R(1);
+                            rad = rad + clamp_ind(thr * es.color * tr * brdf * ndl * wl / es.pdf);
+                        }
+                    }
+                    if (S.hdri_count > 0u) {
+                        const HdriSample hl = sample_hdri(seed);
+                        const R ndl2 = dot(nf, hl.dir);
+                        if (ndl2 > R(0) && hl.pdf > R(0)) {
+                            const V3<R> ts = transmittance(hp + nf * R(1e-3), hl.dir, R(1e30));
+                            if (any_pos(ts)) {
+                                const V3<R> brdf = h.albedo / kPi;
+                                const V3<R> c = thr * hl.color * ts * brdf * ndl2 / hl.pdf;
+                                rad = rad + ((b == 0u) ? c : clamp_ind(c));
+                            }
+                        }
+                    }
+                    skip_sky = (Q.mis_enabled == 0u);
+                }
+                thr = thr * h.albedo;
+                ro = hp + nf * R(1e-3);
+                rd = cos_hemi(nf, seed);
+                if (Q.mis_enabled != 0u && env) {
+                    prev_pdf = mx(R(0), dot(nf, rd)) * kInvPi;
+                    prev_lambert = true;
+                } else {
+                    prev_lambert = false;
+                }
+            } else if (h.mat == kMatMetal) {
+                V3<R> r = reflect(rd, nf);
+                r = normalize(r + h.roughness * (cos_hemi(nf, seed) - nf));
+                thr = thr * h.albedo;
+                ro = hp + nf * R(1e-3);
+                rd = r;
+                skip_sky = false;
+                prev_lambert = false;
+            } else if (h.mat == kMatDielectric) {
+                const R ia = (ndi < R(0)) ? R(1) : h.ior;
+                const R ib = (ndi < R(0)) ? h.ior : R(1);
+                const R eta = ia / ib;
+                const R cos_i = std::fabs(dot(nf, -rd));
+                R r0 = (ia - ib) / (ia + ib);
+                r0 = r0 * r0;
+                const R fr = schlick(cos_i, r0);
+                const V3<R> refl = reflect(rd, nf);
+                const V3<R> refr = refract(rd, nf, eta);
+                const bool tir = length(refr) < R(1e-3);
+                if (tir || randf<R>(seed) < fr) {
+                    rd = refl;
+                    ro = hp + nf * R(1e-3);
+                    skip_sky = false;
+                    prev_lambert = false;
+                } else {
+                    rd = normalize(refr);
+                    ro = hp - nf * R(1e-3);
+                }
+            }
+            if (b >= Q.rr_start) {
+                R p = mx(thr.x, mx(thr.y, thr.z));
+                p = clampv(p, R(0.05), R(1));
+                if (randf<R>(seed) > p) break;
+                thr = thr / p;
+            }
+        }
+        return rad;
+    }
+
+    // frame radiance of one pixel: average of spp samples, sanitised (PathTrace.slang:7707-7734)
+    V3<R> pixel(uint32_t px, uint32_t py, uint32_t frame_index) {
+        uint32_t seed = pcg_hash(px * 1973u + py * 9277u + frame_index * 26699u);
+        const uint32_t n = (P.spp == 0u) ? 1u : P.spp;
+        V3<R> fr{R(0), R(0), R(0)};
+        for (uint32_t s = 0; s < n; ++s) fr = fr + sample_path(px, py, s, seed);
+        fr = fr / R(n);
+        auto clean = [](R v) { return (std::isnan(v) || std::isinf(v)) ? R(0) : mx(v, R(0)); };
+        return {clean(fr.x), clean(fr.y), clean(fr.z)};
+    }
+};
+
+// running mean / EMA update (PathTrace.slang:7736-7781)
+template <class R> void accumulate(R* prev4, V3<R> fr, bool reset, R ema_in) {
+    R p[4] = {prev4[0], prev4[1], prev4[2], prev4[3]};
+    if (reset) p[0] = p[1] = p[2] = p[3] = R(0);
+    bool bad = false;
+    for (int i = 0; i < 4; ++i) bad = bad || std::isnan(p[i]) || std::isinf(p[i]);
+    if (bad) p[0] = p[1] = p[2] = p[3] = R(0);
+    const R ema = clampv(ema_in, R(0), R(0.999));
+    R n_new;
+    V3<R> avg;
+    const V3<R> pr{p[0], p[1], p[2]};
+    if (p[3] < R(0.5) || ema <= R(0)) {
+        n_new = p[3] + R(1);
+        avg = (pr * p[3] + fr) / n_new;
+    } else {
+        avg = pr * ema + fr * (R(1) - ema);
+        n_new = mn(p[3] + R(1), R(1) / mx(R(1) - ema, R(1e-3)));
+    }
+    prev4[0] = avg.x; prev4[1] = avg.y; prev4[2] = avg.z; prev4[3] = n_new;
+}
+
+template <class R>
+void render(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, uint32_t W,
+            uint32_t H, uint32_t frames, float* accum, uint32_t x0, uint32_t y0, uint32_t x1,
+            uint32_t y1, int threads, Counters& total) {
+    std::vector<R> acc(size_t(W) * H * 4);
+    for (size_t i = 0; i < acc.size(); ++i) acc[i] = R(accum[i]);
+    const uint32_t rows = y1 - y0;
+    int nt = threads > 0 ? threads : int(std::thread::hardware_concurrency());
+    if (nt < 1) nt = 1;
+    std::vector<Counters> per(nt);
+    std::atomic<uint32_t> next{0};
+    auto worker = [&](int tid) {
+        Tracer<R> tr(S, P, Q, W, H);
+        for (;;) {
+            const uint32_t r = next.fetch_add(1);
+            if (r >= rows) break;
+            const uint32_t y = y0 + r;
+            for (uint32_t x = x0; x < x1; ++x) {
+                R* a = acc.data() + (size_t(y) * W + x) * 4;
+                for (uint32_t f = 0; f < frames; ++f) {
+                    const V3<R> fr = tr.pixel(x, y, P.frame_index + f);
+                    accumulate<R>(a, fr, f == 0 && P.reset_accum != 0u, R(Q.accum_ema_alpha));
+                }
+            }
+        }
+        per[tid] = tr.cnt;
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < nt; ++i) pool.emplace_back(worker, i);
+    for (auto& t : pool) t.join();
+    for (const auto& c : per) total.add(c);
+    for (uint32_t y = y0; y < y1; ++y)
+        for (uint32_t x = x0; x < x1; ++x)
+            for (int c = 0; c < 4; ++c) {
+                const size_t i = (size_t(y) * W + x) * 4 + c;
+                accum[i] = float(acc[i]);
+            }
+}
+
+template <class R>
+void trace_rays(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q,
+                const float* ro, const float* rd, uint32_t n, uint32_t* hit, float* t,
+                Counters& total) {
+    Tracer<R> tr(S, P, Q, 1, 1);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* o = ro + size_t(i) * 4;
+        const float* d = rd + size_t(i) * 4;
+        const R tinit = (d[3] > 0.0f) ? R(d[3]) : R(1e30);
+        const Hit<R> h = tr.trace(ld3<R>(o), ld3<R>(d), tinit);
+        hit[i] = h.hit ? h.id : kHitMiss;
+        t[i] = h.hit ? float(h.t) : 0.0f;
+    }
+    total.add(tr.cnt);
+}
+
+void export_counters(const Counters& c, OracleCounters* out) {
+    if (!out) return;
+    out->rays = c.rays;
+    out->nodes = c.nodes;
+    out->tris = c.tris;
+    out->prims = c.prims;
+    out->ext_rays = c.ext;
+    out->shadow_rays = c.shadow;
+    out->ext_nodes = c.ext_nodes;
+    out->ext_tris = c.ext_tris;
+    out->ext_prims = c.ext_prims;
+}
+
+}  // namespace orc
+
+extern "C" {
+
+int oracle_trace(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                 const float* ray_o, const float* ray_d, uint32_t n, uint32_t* hit_id, float* t,
+                 int fp64, OracleCounters* counters) {
+    if (!scene || !head || !params || (n && (!ray_o || !ray_d || !hit_id || !t))) return -1;
+    orc::Counters c;
+    if (fp64) orc::trace_rays<double>(*scene, *head, *params, ray_o, ray_d, n, hit_id, t, c);
+    else orc::trace_rays<float>(*scene, *head, *params, ray_o, ray_d, n, hit_id, t, c);
+    orc::export_counters(c, counters);
+    return 0;
+}
+
+int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                  uint32_t W, uint32_t H, uint32_t frames, float* accum_rgba, uint32_t x0,
+                  uint32_t y0, uint32_t x1, uint32_t y1, int fp64, int threads,
+                  OracleCounters* counters) {
+    if (!scene || !head || !params || !accum_rgba || W == 0 || H == 0) return -1;
+    if (x1 > W || y1 > H || x0 > x1 || y0 > y1) return -1;
+    // tlas (hardware RT), the light tree and the no-env-map sky branch
+    // (procedural sun/moon NEE) are not restated.
+    if (head->tlas_present || params->light_tree_enabled || !head->env_map_present) return -6;
+    orc::Counters c;
+    if (fp64)
+        orc::render<double>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
+    else
+        orc::render<float>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
+    orc::export_counters(c, counters);
+    return 0;
+}
+
+float oracle_sinf(float x) { return orc::f_sin(x); }
+float oracle_cosf(float x) { return orc::f_cos(x); }
+float oracle_atan2f(float y, float x) { return orc::f_atan2(y, x); }
+float oracle_acosf(float x) { return orc::f_acos(x); }
+uint32_t oracle_pcg_hash(uint32_t x) { return orc::pcg_hash(x); }
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+"""Regenerates tests/golden/*.npz from the reference's OWN builders
+(AnalyticBvh::Build, TriangleBvh::Build, BuildEnvCdf), compiled from the
+reference sources by `make -C oracle ref` into oracle/_ref.  Run where the
+reference tree is present:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, os.path.dirname(HERE))
+import oracle  # noqa: E402
+from conftest import XorShift32, xorshift_spheres  # noqa: E402
+
+
+def tri_soup(n, seed):
+    """Random small triangles in [-10, 10]^3 (xorshift32), plus one collinear
+    triangle and one with an out-of-range index (the builder must skip it)."""
+    rng = XorShift32(seed)
+    pos, idx = [], []
+    for t in range(n):
+        c = [rng.rangef(-10, 10) for _ in range(3)]
+        for _ in range(3):
+            pos.append([c[k] + rng.rangef(-1, 1) for k in range(3)])
+        idx.append([3 * t, 3 * t + 1, 3 * t + 2])
+    base = len(pos)
+    pos += [[0, 0, 0], [1, 1, 1], [2, 2, 2]]
+    idx.append([base, base + 1, base + 2])
+    idx.append([0, 1, 10 ** 6])
+    return np.array(pos, np.float32), np.array(idx, np.uint32)
+
+
+def main():
+    if oracle.load_ref() is None:
+        sys.exit("oracle/_ref/libref_builders.so missing: run `make -C oracle ref` first")
+    out = {}
+    for name, (n, seed) in {"s50": (50, 0xABCDEF01), "s2000": (2000, 0x12345678)}.items():
+        cr = xorshift_spheres(n, seed)
+        nodes, perm = oracle.ref_analytic_bvh(cr)
+        out[f"{name}_cr"], out[f"{name}_nodes"], out[f"{name}_perm"] = cr, nodes, perm
+    pos, idx = tri_soup(3000, 0x7A1A5EED)
+    nodes, perm = oracle.ref_triangle_bvh(pos, idx)
+    out.update(tri_pos=pos, tri_idx=idx, tri_nodes=nodes, tri_perm=perm)
+    rng = XorShift32(0xC0FFEE)
+    img = np.array([[[rng.rangef(0, 4) for _ in range(3)] for _ in range(32)] for _ in range(16)], np.float32)
+    mask = np.zeros((16, 32), np.uint8)
+    mask[3:5, 7:10] = 1
+    marg, cond, tot = oracle.ref_env_cdf(img)
+    margm, condm, totm = oracle.ref_env_cdf(img, mask)
+    out.update(env_img=img, env_mask=mask, env_marg=marg, env_cond=cond, env_total=np.float64(tot),
+               env_marg_m=margm, env_cond_m=condm, env_total_m=np.float64(totm))
+    np.savez_compressed(os.path.join(HERE, "reference_builders.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_builders.npz"))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+"""GPU path vs the fp32 oracle, through the C-ABI.  The kernels evaluate the
+shader's expressions in the same order with no FMA contraction, IEEE div/sqrt
+and the same polynomial transcendentals, so the bar is bit-exact: identical
+hit ids and t, identical accumulation buffers."""
+import numpy as np
+import pytest
+
+from conftest import xorshift_rays, xorshift_spheres
+
+pytestmark = pytest.mark.gpu
+
+
+def random_rays(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    ro = np.zeros((n, 4), np.float32)
+    ro[:, :3] = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3))
+    rd = np.zeros((n, 4), np.float32)
+    rd[:, :3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    return ro, rd
+
+
+def check_trace(pt, orc, dev, s, ro, rd):
+    dev.upload(s)
+    head, prm = s.push(8, 8)
+    g_hit, g_t = dev.trace(ro, rd)
+    o_hit, o_t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+    mism = np.flatnonzero((g_hit != o_hit) | (g_t != o_t))
+    assert mism.size == 0, f"{mism.size} of {ro.shape[0]} rays differ, first {mism[:5]}"
+    return o_hit
+
+
+@pytest.mark.parametrize("n,seed", [(50, 0xABCDEF01), (2000, 0x12345678)])
+def test_trace_xorshift_spheres(pt, orc, dev, n, seed):
+    s = pt.Scene()
+    for i, c in enumerate(xorshift_spheres(n, seed)):
+        s.sphere(i, *map(float, c[:3]), float(c[3]), 0, (0.5, 0.5, 0.5))
+    s.env(np.zeros((2, 4, 3), np.float32))
+    ro, rd = xorshift_rays(1000, 0x12345678)
+    hit = check_trace(pt, orc, dev, s, ro, rd)
+    assert (hit != 0xFFFFFFFF).sum() > 50
+
+
+def test_trace_c0_scene(pt, orc, dev):
+    s = pt.Scene().synth(0, seed=0)
+    ro, rd = random_rays(20000, -12, 12, 1)
+    hit = check_trace(pt, orc, dev, s, ro, rd)
+    assert ((hit & (1 << 30)) != 0).sum() > 100 and (hit < (1 << 30)).sum() > 100
+
+
+def test_trace_c1_scene_small(pt, orc, dev):
+    s = pt.Scene().synth(1, seed=0, scale=0.02)
+    ro, rd = random_rays(20000, -60, 60, 2)
+    ro[:, 1] = np.abs(ro[:, 1]) + 0.5
+    check_trace(pt, orc, dev, s, ro, rd)
+
+
+def test_trace_tmax_is_the_initial_distance(pt, orc, dev):
+    s = pt.Scene().synth(0, seed=0)
+    ro, rd = random_rays(5000, -12, 12, 3)
+    rd[:, 3] = 4.0
+    check_trace(pt, orc, dev, s, ro, rd)
+
+
+def render_both(pt, orc, dev, s, W, H, frames):
+    dev.upload(s)
+    dev.set_target(W, H)
+    head, prm = s.push(W, H, frame_index=11, reset=1)
+    dev.render(head, prm, frames)
+    g = dev.read_accum()
+    o, c = orc.render(s.packed(), head, prm, W, H, frames)
+    return g, o, c
+
+
+def test_render_c0_bit_exact(pt, orc, dev):
+    s = pt.Scene().synth(0, seed=3)
+    g, o, c = render_both(pt, orc, dev, s, 48, 40, 2)
+    st = dev.stats()
+    assert st.extension_rays == c.ext_rays
+    assert st.shadow_rays == c.shadow_rays
+    np.testing.assert_array_equal(g, o)
+    assert (g[..., 3] == 2).all() and g[..., :3].max() > 0
+
+
+def test_render_c1_small_bit_exact(pt, orc, dev):
+    s = pt.Scene().synth(1, seed=4, scale=0.02)
+    g, o, c = render_both(pt, orc, dev, s, 64, 36, 3)
+    assert dev.stats().shadow_rays == c.shadow_rays
+    np.testing.assert_array_equal(g, o)
+    assert g[..., :3].max() > 0
+
+
+def test_render_mis_off_and_no_clamp_bit_exact(pt, orc, dev):
+    s = pt.Scene().synth(1, seed=5, scale=0.02)
+    s.set_cvar("r_mis", 0)
+    s.set_cvar("r_firefly_clamp", 0)
+    s.set_cvar("r_caustics", 0)
+    g, o, _ = render_both(pt, orc, dev, s, 40, 30, 2)
+    np.testing.assert_array_equal(g, o)
+
+
+def test_render_lights_of_every_type_bit_exact(pt, orc, dev):
+    s = pt.Scene()
+    s.plane(1, (0, 1, 0), 0.0, 0, (0.7, 0.7, 0.7))
+    s.sphere(2, 0, 1, 0, 1, 0, (0.8, 0.3, 0.2))
+    s.sphere(3, 2.5, 0.7, 0.5, 0.7, 2, (1, 1, 1), 0, 1.5)
+    s.sphere(4, -2.5, 0.8, 0, 0.8, 1, (0.9, 0.9, 0.9), 0.1)
+    s.emission(4, (0.5, 0.2, 0.1))
+    s.light_point(1, (0, 5, 2), (20, 20, 20))
+    s.light_spot(2, (3, 4, 3), (-0.5, -1, -0.5), 40, 20, (30, 25, 20))
+    s.light_sphere(3, (-3, 4, 2), 0.5, (8, 8, 8))
+    s.light_quad(4, (0, 6, -2), (0, -1, 0), (1, 0, 0), 1.0, 0.5, (10, 10, 10))
+    s.env(np.full((8, 16, 3), 0.05, np.float32))
+    s.camera((0, 2, 8), 0.0, -0.15, 50)
+    s.set_cvar("r_spp", 4)
+    g, o, _ = render_both(pt, orc, dev, s, 40, 32, 2)
+    np.testing.assert_array_equal(g, o)
+
+
+def test_wave_batching_does_not_change_the_result(pt, dev):
+    s = pt.Scene().synth(1, seed=6, scale=0.02)
+    dev.upload(s)
+    W, H = 32, 24
+    dev.set_target(W, H)
+    head, prm = s.push(W, H, 0, 1)
+    outs = []
+    for fpw in (1, 3, 0):
+        dev.set_wave_frames(fpw)
+        dev.render(head, prm, 5)
+        outs.append(dev.read_accum())
+    dev.set_wave_frames(0)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+
+
+def test_resume_from_saved_accumulation(pt, dev):
+    """frames 0..3 in one call == frames 0..1, save, restore, frames 2..3."""
+    s = pt.Scene().synth(0, seed=7)
+    dev.upload(s)
+    W, H = 24, 24
+    dev.set_target(W, H)
+    head, prm = s.push(W, H, 0, 1)
+    dev.render(head, prm, 4)
+    ref = dev.read_accum()
+    dev.render(head, prm, 2)
+    saved = dev.read_accum()
+    dev.set_target(W, H)
+    dev.write_accum(saved)
+    head2, prm2 = s.push(W, H, 2, 0)
+    dev.render(head2, prm2, 2)
+    np.testing.assert_array_equal(dev.read_accum(), ref)
+
+
+def test_invalid_inputs_are_rejected(pt, dev):
+    import ctypes
+    lib = pt.load()
+    recs = np.zeros((4, 28), np.float32)
+    bad = (pt.PtBvhNode * 3)()
+    bad[0].count = 0
+    bad[0].left_first = 0          # child index not after its parent: would loop
+    rc = lib.pt_gpu_upload_prims(dev.h, pt.fptr(recs), 4, 0, bad, 3)
+    assert rc == -1
+    bad[0].left_first = 1
+    bad[1].count = 9               # leaf range past the records
+    bad[2].count = 1
+    assert lib.pt_gpu_upload_prims(dev.h, pt.fptr(recs), 4, 0, bad, 3) == -1
+    s = pt.Scene().synth(0)
+    dev.upload(s)
+    dev.set_target(8, 8)
+    head, prm = s.push(8, 8)
+    head.prim_count += 1
+    assert lib.pt_gpu_render(dev.h, ctypes.byref(head), ctypes.byref(prm), 1) == -1
+    head.prim_count -= 1
+    head.tlas_present = 1
+    assert lib.pt_gpu_render(dev.h, ctypes.byref(head), ctypes.byref(prm), 1) == -6
+
+
+def test_full_size_c1_frame_matches_oracle_on_crops(pt, orc, dev):
+    """1920x1080 C1 frame: finite, count 1, and three 16x16 crops identical to the oracle."""
+    s = pt.Scene().synth(1, seed=0)
+    W, H = 1920, 1080
+    dev.upload(s)
+    dev.set_target(W, H)
+    head, prm = s.push(W, H, 0, 1)
+    dev.render(head, prm, 1)
+    g = dev.read_accum()
+    assert np.isfinite(g).all() and (g[..., 3] == 1).all()
+    assert dev.stats().extension_rays >= W * H
+    acc = np.zeros((H, W, 4), np.float32)
+    for (x0, y0) in ((952, 532), (100, 900), (1700, 200)):
+        orc.render(s.packed(), head, prm, W, H, 1, accum=acc, crop=(x0, y0, x0 + 16, y0 + 16))
+        np.testing.assert_array_equal(g[y0:y0 + 16, x0:x0 + 16], acc[y0:y0 + 16, x0:x0 + 16])

@@ -1,0 +1,142 @@
+"""The oracle pinned against the reference's own contracts: PCG bit pattern
+(shaders/PathTraceMath.slang:16-24), BVH closest hit == naive scan on the
+reference test's xorshift scene/rays (tests/pt_core_analytic_bvh_test.cpp:420-469),
+the single-sphere t = 4 known answer (:339-378), triangle BVH == naive
+Moller-Trumbore, the polynomial transcendentals' accuracy, and fp32 vs fp64."""
+import numpy as np
+import pytest
+
+from conftest import xorshift_rays, xorshift_spheres
+
+
+def pcg_py(x):
+    x = (x * 747796405 + 2891336453) & 0xFFFFFFFF
+    x = (((x >> ((x >> 28) + 4)) ^ x) * 277803737) & 0xFFFFFFFF
+    return (x >> 22) ^ x
+
+
+def test_pcg_hash_bit_pattern(orc):
+    lib = orc.load()
+    for x in [0, 1, 1973, 9277 * 5 + 26699, 0xFFFFFFFF, 123456789]:
+        assert lib.oracle_pcg_hash(x) == pcg_py(x)
+
+
+def test_polynomial_transcendentals_accuracy(orc):
+    lib = orc.load()
+    xs = np.linspace(-3.3, 6.6, 4001, dtype=np.float32)
+    s = np.array([lib.oracle_sinf(float(x)) for x in xs])
+    c = np.array([lib.oracle_cosf(float(x)) for x in xs])
+    assert np.abs(s - np.sin(xs.astype(np.float64))).max() < 4e-7
+    assert np.abs(c - np.cos(xs.astype(np.float64))).max() < 4e-7
+    ys = np.linspace(-1, 1, 2001, dtype=np.float32)
+    a = np.array([lib.oracle_acosf(float(y)) for y in ys])
+    assert np.abs(a - np.arccos(ys.astype(np.float64))).max() < 1e-6
+    ang = np.linspace(-np.pi, np.pi, 3001)
+    yy, xx = np.sin(ang).astype(np.float32), np.cos(ang).astype(np.float32)
+    at = np.array([lib.oracle_atan2f(float(y), float(x)) for y, x in zip(yy, xx)])
+    assert np.abs(at - np.arctan2(yy.astype(np.float64), xx.astype(np.float64))).max() < 1e-6
+
+
+def sphere_scene(pt, cr, threshold=16):
+    s = pt.Scene()
+    s.set_cvar("r_analytic_bvh_threshold", threshold)
+    for i, c in enumerate(cr):
+        s.sphere(i, float(c[0]), float(c[1]), float(c[2]), float(c[3]), 0, (0.5, 0.5, 0.5))
+    s.env(np.zeros((2, 4, 3), np.float32))
+    return s
+
+
+def slot_to_input(a):
+    """record slot -> input index (prim ids were 0..n-1)."""
+    return a["prims"][:, 11].view(np.uint32)
+
+
+def test_bvh_trace_matches_naive_scan_reference_contract(pt, orc):
+    cr = xorshift_spheres(50, 0xABCDEF01)
+    ro, rd = xorshift_rays(1000, 0x12345678)
+    res = []
+    for thr in (16, 10 ** 6):   # BVH on / linear scan
+        s = sphere_scene(pt, cr, thr)
+        head, prm = s.push(8, 8)
+        hit, t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+        ids = np.where(hit == 0xFFFFFFFF, -1, slot_to_input(s.arrays())[np.minimum(hit, 49)].astype(np.int64))
+        res.append((ids, t))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    assert (res[0][0] >= 0).sum() > 50     # > 5 % hits, as the reference test requires
+
+
+def test_single_sphere_known_answer(pt, orc):
+    s = sphere_scene(pt, np.array([[0, 0, 5, 1]], np.float32))
+    head, prm = s.push(8, 8)
+    ro = np.zeros((2, 4), np.float32)
+    rd = np.array([[0, 0, 1, 0], [1, 0, 0, 0]], np.float32)
+    hit, t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+    assert hit[0] == 0 and t[0] == 4.0
+    assert hit[1] == 0xFFFFFFFF
+
+
+def naive_mt(pos, idx, ro, rd):
+    """Two-sided Moller-Trumbore over every triangle (numpy float32, same op order)."""
+    v0, v1, v2 = pos[idx[:, 0]], pos[idx[:, 1]], pos[idx[:, 2]]
+    e1, e2 = v1 - v0, v2 - v0
+    out_id = np.full(ro.shape[0], -1, np.int64)
+    out_t = np.zeros(ro.shape[0], np.float32)
+    for i in range(ro.shape[0]):
+        o, d = ro[i, :3], rd[i, :3]
+        pv = np.cross(d, e2).astype(np.float32)
+        det = (e1 * pv).sum(1, dtype=np.float32)
+        ok = np.abs(det) >= np.float32(1e-8)
+        inv = np.float32(1) / np.where(ok, det, np.float32(1))
+        tv = (o - v0).astype(np.float32)
+        u = (tv * pv).sum(1, dtype=np.float32) * inv
+        qv = np.cross(tv, e1).astype(np.float32)
+        v = (d * qv).sum(1, dtype=np.float32) * inv
+        tt = (e2 * qv).sum(1, dtype=np.float32) * inv
+        ok &= (u >= 0) & (u <= 1) & (v >= 0) & (u + v <= 1) & (tt > np.float32(1e-3))
+        if ok.any():
+            j = np.flatnonzero(ok)[np.argmin(tt[ok])]
+            out_id[i], out_t[i] = j, tt[j]
+    return out_id, out_t
+
+
+def test_triangle_bvh_trace_matches_naive(pt, orc):
+    rng = np.random.default_rng(3)
+    nt = 400
+    c = rng.uniform(-8, 8, (nt, 1, 3))
+    pos = (c + rng.uniform(-1.5, 1.5, (nt, 3, 3))).reshape(-1, 3).astype(np.float32)
+    idx = np.arange(nt * 3, dtype=np.uint32).reshape(-1, 3)
+    s = pt.Scene()
+    s.mesh(pos, idx)
+    s.env(np.zeros((2, 4, 3), np.float32))
+    head, prm = s.push(8, 8)
+    ro, rd = xorshift_rays(300, 0xBEEF)
+    hit, t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+    nid, nt_ = naive_mt(pos, idx, ro, rd)
+    got = np.where(hit == 0xFFFFFFFF, -1, (hit & ~np.uint32(1 << 30)).astype(np.int64))
+    agree = (got == nid)
+    assert agree.mean() >= 0.995          # exact-t ties may pick a different triangle
+    np.testing.assert_allclose(t[agree & (nid >= 0)], nt_[agree & (nid >= 0)], rtol=1e-6)
+    assert (nid >= 0).sum() > 30
+
+
+def test_fp32_and_fp64_oracles_agree_on_c0(pt, orc):
+    s = pt.Scene().synth(0, seed=1)
+    W = H = 24
+    head, prm = s.push(W, H)
+    a32, c32 = orc.render(s.packed(), head, prm, W, H, 2)
+    a64, _ = orc.render(s.packed(), head, prm, W, H, 2, fp64=True)
+    assert np.isfinite(a32).all() and (a32[..., 3] == 2).all()
+    assert np.abs(a32 - a64).max() < 5e-2
+    assert np.mean(np.abs(a32 - a64)) < 1e-4
+    assert c32.ext_rays > W * H * 16 and c32.shadow_rays > 0
+
+
+def test_crop_render_equals_full_render_region(pt, orc):
+    s = pt.Scene().synth(0, seed=2)
+    W, H = 32, 20
+    head, prm = s.push(W, H)
+    full, _ = orc.render(s.packed(), head, prm, W, H, 1)
+    crop, _ = orc.render(s.packed(), head, prm, W, H, 1, crop=(5, 3, 17, 11))
+    np.testing.assert_array_equal(full[3:11, 5:17], crop[3:11, 5:17])
+    assert not crop[:3].any()
