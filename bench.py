@@ -134,22 +134,20 @@ def algorithmic_bytes(pt, orc, scene, head, prm):
 
 def cpu_baseline(pt, orc, scene, head, prm, budget_s=12.0):
     """fp32 oracle (the reference-semantics CPU port) on whole frames of the
-    same workload, all host threads, about `budget_s` seconds."""
+    same workload, all host threads, about `budget_s` seconds of CPU work."""
     cores = os.cpu_count() or 1
     acc = np.zeros((H_FULL, W_FULL, 4), np.float32)
-    segs, t_used, rows = 0, 0.0, 0
-    y = 0
-    band = 72
-    while t_used < budget_s and y < H_FULL:
+    segs, t_used, frames = 0, 0.0, 0
+    h0, p0 = head, prm
+    while t_used < budget_s and frames < FRAMES:
+        h0, p0 = scene.push(W_FULL, H_FULL, frame_index=head.frame_index + frames, reset=int(frames == 0))
         t0 = time.perf_counter()
-        _, c = orc.render(scene.packed(), head, prm, W_FULL, H_FULL, 1, accum=acc,
-                          crop=(0, y, W_FULL, min(H_FULL, y + band)), threads=cores)
+        _, c = orc.render(scene.packed(), h0, p0, W_FULL, H_FULL, 1, accum=acc, threads=cores)
         t_used += time.perf_counter() - t0
         segs += c.ext_rays + c.shadow_rays
-        rows += min(H_FULL, y + band) - y
-        y += band
+        frames += 1
     return {"value": segs / t_used / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
-            "sample": f"frame 0 of the workload, rows 0..{rows} of 1080 (1920 wide), 1 spp, "
+            "sample": f"frames 0..{frames - 1} of the 64 (1920x1080, 1 spp each), "
                       f"{segs} segments in {t_used:.1f} s"}
 
 
@@ -168,14 +166,12 @@ def run_reference(args):
     scene = pt.Scene().synth(1, seed=0)
     head, prm = scene.push(W_FULL, H_FULL, 0, 1)
     cores = os.cpu_count() or 1
-    band = 120
     acc = np.zeros((H_FULL, W_FULL, 4), np.float32)
 
     def step(i):
-        y = (i * band) % H_FULL
+        h, p = scene.push(W_FULL, H_FULL, frame_index=i, reset=int(i == 0))
         t0 = time.perf_counter()
-        _, c = orc.render(scene.packed(), head, prm, W_FULL, H_FULL, 1, accum=acc,
-                          crop=(0, y, W_FULL, y + band), threads=cores)
+        _, c = orc.render(scene.packed(), h, p, W_FULL, H_FULL, 1, accum=acc, threads=cores)
         return time.perf_counter() - t0, c.ext_rays + c.shadow_rays
 
     for i in range(args.warmup):
@@ -191,9 +187,9 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "triangles+analytic 1920x1080 1spp x64 frames depth 8 (2,460,288 tris, "
-                                   "1024 spheres, 2048x1024 env)", "step": f"1920x{band} band of one frame"},
+                                   "1024 spheres, 2048x1024 env)", "step": "one 1920x1080 1 spp frame of the 64"},
             "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port",
-                             "sample": f"1920x{band} bands of frame 0, {ss} segments over {args.steps} steps"},
+                             "sample": f"{args.steps} whole frames after {args.warmup} warm-up frames, {ss} segments"},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -240,7 +236,7 @@ def main():
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    t_dev, segs, ext, ext_ms, ext_launch, launches = 0.0, 0, 0, 0.0, 0, 0
+    t_dev, segs, ext, ext_ms, ext_launch, launches, sh_ms = 0.0, 0, 0, 0.0, 0, 0, 0.0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         dev.render(head, prm, args.frames)
@@ -249,6 +245,7 @@ def main():
         segs += st.extension_rays + st.shadow_rays
         ext += st.extension_rays
         ext_ms += st.extend_ms
+        sh_ms += st.shadow_ms
         ext_launch += st.extend_launches
         launches += st.waves * (2 + head.spp) + 4 * st.extend_launches
     t_wall = time.perf_counter() - t0
@@ -299,7 +296,9 @@ def main():
                 "traffic": (tpr * per_launch_rays) if tpr else None,
                 "algorithmic_bytes_per_launch": bseg * per_launch_rays,
                 "avg_launch_ms": ext_ms / max(ext_launch, 1), "launches": ext_launch,
-                "B_seg": bseg, "N_per_segment": nbar, "peak_kind": peak_kind}
+                "B_seg": bseg, "N_per_segment": nbar, "peak_kind": peak_kind,
+                "step_share": {"k_extend": ext_ms / max(1e3 * t_dev, 1e-9),
+                               "k_shadow": sh_ms / max(1e3 * t_dev, 1e-9)}}
     line = {"metric": METRIC, "value": segs / t_dev / 1e6, "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
             "wall_ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -59,6 +59,12 @@ class PtStats(ctypes.Structure):
                 ("extend_launches", u32), ("shadow_launches", u32)]
 
 
+class PtAccelInfo(ctypes.Structure):
+    _fields_ = [("traversal", u32), ("mesh_wide", u32), ("prims_wide", u32), ("mesh_wide_nodes", u32),
+                ("mesh_wide_depth", u32), ("mesh_binary_nodes", u32), ("prims_wide_nodes", u32),
+                ("reserved", u32), ("mesh_build_ms", ctypes.c_double)]
+
+
 class PtPackedScene(ctypes.Structure):
     _fields_ = [("prims", P(f32)), ("prim_count", u32), ("linear_prim_count", u32),
                 ("bvh_nodes", P(PtBvhNode)), ("bvh_node_count", u32),
@@ -96,6 +102,8 @@ SIGNATURES = {
     "pt_gpu_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtStats)]),
     "pt_gpu_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_set_wave_frames": (ctypes.c_int, [ctypes.c_void_p, u32]),
+    "pt_gpu_set_traversal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pt_gpu_get_accel_info": (ctypes.c_int, [ctypes.c_void_p, P(PtAccelInfo)]),
     "pt_gpu_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     # pt_scene.h
@@ -366,6 +374,14 @@ class Device:
 
     def set_profiling(self, on=True):
         self._check(self.lib.pt_gpu_set_profiling(self.h, 1 if on else 0))
+
+    def set_traversal(self, mode):
+        self._check(self.lib.pt_gpu_set_traversal(self.h, mode))
+
+    def accel_info(self) -> PtAccelInfo:
+        a = PtAccelInfo()
+        self._check(self.lib.pt_gpu_get_accel_info(self.h, ctypes.byref(a)))
+        return a
 
     def set_wave_frames(self, n):
         self._check(self.lib.pt_gpu_set_wave_frames(self.h, n))

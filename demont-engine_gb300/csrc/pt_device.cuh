@@ -210,6 +210,14 @@ struct DScene {
     float4 hdri_dir[8];
     float4 hdri_col[8];
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
+    // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
+    uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs
+    uint32_t a_wide, t_wide;     // 1: walk the wide tree for that part
+    const float4* a4;            // analytic wide nodes (8 float4 each)
+    const float4* a4_geo;        // finite analytic prims in wide-leaf order
+    const uint4* a4_meta;        // (record slot, type, tie key, 0)
+    const float4* t4;            // mesh wide nodes
+    const float4* tri4;          // triangles in wide-leaf order: (v0, orig id) (e1, material) (e2, tie rank)
 };
 
 struct HitRec {
@@ -265,12 +273,14 @@ __device__ __forceinline__ void test_prim(const DScene& S, uint32_t idx, V3 ro, 
 // traceScene closest hit (shaders/PathTrace.slang:2331-2693): planes linearly,
 // analytic BVH (stack 32, right child popped first), then the triangle BVH
 // (stack 64) which only replaces the analytic hit when strictly closer.
-__device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, float t_init) {
+// parts: bit 0 analytic records, bit 1 triangle mesh.
+__device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, float t_init, uint32_t parts = 3u) {
     HitRec h{t_init, kMiss};
-    const uint32_t linear = S.linear_count;
+    const uint32_t linear = (parts & 1u) ? S.linear_count : 0u;
     for (uint32_t i = 0; i < linear; ++i) test_prim(S, i, ro, rd, h);
     uint32_t iters = 0;
-    if (S.bvh_nodes == 0u) {
+    if (!(parts & 1u)) {
+    } else if (S.bvh_nodes == 0u) {
         for (uint32_t i = linear; i < S.prim_count; ++i) test_prim(S, i, ro, rd, h);
     } else {
         const V3 inv = safe_inv(rd);
@@ -292,7 +302,7 @@ __device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, floa
             }
         }
     }
-    if (S.tri_enabled != 0u && S.tri_nodes > 0u) {
+    if ((parts & 2u) && S.tri_enabled != 0u && S.tri_nodes > 0u) {
         float t_mesh = h.t;
         uint32_t slot_hit = 0;
         bool found = false;
@@ -343,6 +353,191 @@ __device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, floa
     return h;
 }
 
+
+// ---------------------------------------------------------------------------
+// Wide-tree traversal.  Front-to-back over 4-wide nodes; a popped entry is
+// skipped when its entry distance exceeds the current best (ties are still
+// visited).  A candidate replaces the best when it is strictly closer, or
+// equally close with a lower tie key: the key is the primitive's position in
+// the reference's own test order (planes by index, then the analytic BVH
+// leaves in right-child-first depth-first order, then the triangle BVH the
+// same way), which reproduces the reference's first-tested-wins rule.
+// ---------------------------------------------------------------------------
+struct Best {
+    float t;
+    uint32_t key;
+    uint32_t id;
+};
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kWideStackDev = 64;
+
+__device__ __forceinline__ bool better(float t, uint32_t key, const Best& b) {
+    return t < b.t || (t == b.t && key < b.key);
+}
+
+__device__ __forceinline__ float isect_geo(uint32_t type, float4 g, V3 ro, V3 rd) {
+    if (type == 0u) {
+        const V3 oc = ro - v3(g);
+        const float b = dot(oc, rd);
+        const float k = dot(oc, oc) - g.w * g.w;
+        float hh = b * b - k;
+        if (hh < 0.0f) return -1.0f;
+        hh = sqrtf(hh);
+        const float t0 = -b - hh, t1 = -b + hh;
+        return (t0 > 1e-3f) ? t0 : t1;
+    }
+    if (type == 1u) {
+        const V3 n = v3(g);
+        const float denom = dot(rd, n);
+        if (fabsf(denom) < 1e-4f) return -1.0f;
+        return -(dot(ro, n) + g.w) / denom;
+    }
+    return -1.0f;
+}
+
+template <bool kTri>
+__device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, V3 ro, V3 rd, V3 inv,
+                                          Best& b, uint32_t key_base, uint32_t& iters, uint32_t* st_code,
+                                          float* st_t) {
+    int sp = 0;
+    st_code[0] = 0u;
+    st_t[0] = -3.0e38f;
+    sp = 1;
+    while (sp > 0) {
+        if (++iters > kTraverseCap) { atomicOr(S.err, 1u); return; }
+        --sp;
+        const uint32_t code = st_code[sp];
+        if (st_t[sp] > b.t) continue;
+        if (code & kLeafBit) {
+            const uint32_t first = code & 0x0FFFFFFFu;
+            const uint32_t cnt = ((code >> 28) & 7u) + 1u;
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const uint32_t p = first + k;
+                if (kTri) {
+                    const float4 a = __ldg(S.tri4 + 3u * p);
+                    const float4 bb = __ldg(S.tri4 + 3u * p + 1u);
+                    const float4 c = __ldg(S.tri4 + 3u * p + 2u);
+                    const V3 v0 = v3(a), e1 = v3(bb), e2 = v3(c);
+                    const V3 pv = cross(rd, e2);
+                    const float det = dot(e1, pv);
+                    if (fabsf(det) < 1e-8f) continue;
+                    const float inv_det = 1.0f / det;
+                    const V3 tvec = ro - v0;
+                    const float u = dot(tvec, pv) * inv_det;
+                    if (u < 0.0f || u > 1.0f) continue;
+                    const V3 qv = cross(tvec, e1);
+                    const float v = dot(rd, qv) * inv_det;
+                    if (v < 0.0f || u + v > 1.0f) continue;
+                    const float tt = dot(e2, qv) * inv_det;
+                    const uint32_t key = key_base | __float_as_uint(c.w);
+                    if (tt > 1e-3f && better(tt, key, b)) {
+                        b.t = tt;
+                        b.key = key;
+                        b.id = kTriBit | p;
+                    }
+                } else {
+                    const float4 g = __ldg(S.a4_geo + p);
+                    const uint4 m = __ldg(S.a4_meta + p);
+                    const float t = isect_geo(m.y, g, ro, rd);
+                    if (t > 1e-3f && better(t, m.z, b)) {
+                        b.t = t;
+                        b.key = m.z;
+                        b.id = m.x;
+                    }
+                }
+            }
+            continue;
+        }
+        const float4* nd = nodes + 8u * code;
+        const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
+        const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
+        const int4 ch = *reinterpret_cast<const int4*>(nd + 6);
+        const int4 cn = *reinterpret_cast<const int4*>(nd + 7);
+        const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+        const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+        const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+        const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
+        float dist[4];
+        uint32_t codes[4];
+        int nh = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (nn[k] < 0) continue;
+            const float t0x = (lx[k] - ro.x) * inv.x, t1x = (hx[k] - ro.x) * inv.x;
+            const float t0y = (ly[k] - ro.y) * inv.y, t1y = (hy[k] - ro.y) * inv.y;
+            const float t0z = (lz[k] - ro.z) * inv.z, t1z = (hz[k] - ro.z) * inv.z;
+            const float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+            const float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+            if (tmx >= fmaxf(tmin, 0.0f) && tmin <= b.t) {
+                dist[nh] = tmin;
+                codes[nh] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k]))
+                                        : uint32_t(cc[k]);
+                ++nh;
+            }
+        }
+        if (sp + nh > kWideStackDev) { atomicOr(S.err, 2u); return; }
+        // push farthest first so the nearest child is popped next
+        for (int i = 0; i < nh; ++i) {
+            int far = i;
+            for (int j = i + 1; j < nh; ++j)
+                if (dist[j] > dist[far]) far = j;
+            const float td = dist[far];
+            const uint32_t tc = codes[far];
+            dist[far] = dist[i];
+            codes[far] = codes[i];
+            st_t[sp] = td;
+            st_code[sp] = tc;
+            ++sp;
+        }
+    }
+}
+
+// traceScene on the wide trees (analytic part falls back to the reference walk
+// when its wide tree is not built).
+__device__ __noinline__ HitRec trace_wide(const DScene& S, V3 ro, V3 rd, float t_init) {
+    Best b{t_init, 0u, kMiss};
+    const uint32_t linear = S.linear_count;
+    for (uint32_t i = 0; i < linear; ++i) {
+        const float t = isect_geo(__ldg(S.prim_type + i), __ldg(S.prim_geo + i), ro, rd);
+        if (t > 1e-3f && better(t, i, b)) {
+            b.t = t;
+            b.key = i;
+            b.id = i;
+        }
+    }
+    uint32_t iters = 0;
+    const V3 inv = safe_inv(rd);
+    uint32_t st_code[kWideStackDev];
+    float st_t[kWideStackDev];
+    if (S.a_wide) {
+        wide_walk<false>(S, S.a4, ro, rd, inv, b, 0u, iters, st_code, st_t);
+    } else if (S.prim_count > linear) {
+        // the reference's own analytic walk (it re-tests the planes: same result)
+        const HitRec h = trace_closest(S, ro, rd, t_init, 1u);
+        if (h.id != kMiss && better(h.t, h.id, b)) {
+            b.t = h.t;
+            b.key = h.id;
+            b.id = h.id;
+        }
+    }
+    if (S.tri_enabled != 0u && S.tri_nodes > 0u) {
+        if (S.t_wide) {
+            wide_walk<true>(S, S.t4, ro, rd, inv, b, 0x80000000u, iters, st_code, st_t);
+        } else {
+            const HitRec h = trace_closest(S, ro, rd, b.t, 2u);
+            if (h.id != kMiss) {
+                b.t = h.t;
+                b.id = h.id;
+            }
+        }
+    }
+    return HitRec{b.t, b.id};
+}
+
+__device__ __forceinline__ HitRec trace_any_mode(const DScene& S, V3 ro, V3 rd, float t_init, bool wide) {
+    return wide ? trace_wide(S, ro, rd, t_init) : trace_closest(S, ro, rd, t_init);
+}
+
 // Surface attributes of a hit (the HitInfo fields testAnalyticPrim and the
 // mesh branch fill in, shaders/PathTrace.slang:2101-2146, 2639-2690).
 struct Surface {
@@ -358,8 +553,9 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
     Surface s;
     if (h.id & kTriBit) {
         const uint32_t slot = h.id & ~kTriBit;
-        const float4 b = __ldg(S.tri + 3u * slot + 1u);
-        const float4 c = __ldg(S.tri + 3u * slot + 2u);
+        const float4* T = S.t_wide ? S.tri4 : S.tri;
+        const float4 b = __ldg(T + 3u * slot + 1u);
+        const float4 c = __ldg(T + 3u * slot + 2u);
         s.normal = normalize(cross(v3(b), v3(c)));
         if (S.mesh_has_mat && S.mat_count > 0u) {
             uint32_t m = __float_as_uint(b.w);
@@ -419,11 +615,11 @@ __device__ __forceinline__ V3 cos_hemi(V3 n, uint32_t& seed) {
 // transmittance (shaders/PathTrace.slang:5089-5196) with clouds and water off.
 // Counts the closest-hit queries it makes in *segs.
 __device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t_max, int kmax,
-                                            uint32_t& segs) {
+                                            uint32_t& segs, bool wide) {
     V3 t = v3(1.0f, 1.0f, 1.0f);
     for (int i = 0; i <= kmax; ++i) {
         ++segs;
-        const HitRec h = trace_closest(S, o, d, 1e30f);
+        const HitRec h = trace_any_mode(S, o, d, 1e30f, wide);
         if (h.id == kMiss || h.t >= t_max) return t;
         const Surface sf = surface_at(S, o, d, h);
         if (sf.mat != kMatDielectric) return v3(0.0f, 0.0f, 0.0f);

@@ -22,6 +22,7 @@
 
 #include "pt_gpu.h"
 #include "pt_device.cuh"
+#include "bvh_build.cuh"
 
 #include <algorithm>
 #include <cstdio>
@@ -300,7 +301,7 @@ __global__ void k_prep_prims(const float4* rec, uint32_t n, float4* geo, uint32_
 
 // triangle records in BVH leaf-slot order: (v0, orig id) (v1 - v0, material) (v2 - v0, 0)
 __global__ void k_prep_tris(const float* pos, const uint32_t* idx, const uint32_t* perm,
-                            const uint32_t* mat, uint32_t slots, float4* tri) {
+                            const uint32_t* mat, uint32_t slots, float4* tri, float4* blo, float4* bhi) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= slots) return;
     const uint32_t t = perm[j];
@@ -312,6 +313,63 @@ __global__ void k_prep_tris(const float* pos, const uint32_t* idx, const uint32_
     tri[3u * j] = f4(v0, __uint_as_float(t));
     tri[3u * j + 1u] = f4(v1 - v0, __uint_as_float(m));
     tri[3u * j + 2u] = f4(v2 - v0, 0.0f);
+    blo[j] = make_float4(fminf(v0.x, fminf(v1.x, v2.x)), fminf(v0.y, fminf(v1.y, v2.y)),
+                         fminf(v0.z, fminf(v1.z, v2.z)), 0.0f);
+    bhi[j] = make_float4(fmaxf(v0.x, fmaxf(v1.x, v2.x)), fmaxf(v0.y, fmaxf(v1.y, v2.y)),
+                         fmaxf(v0.z, fmaxf(v1.z, v2.z)), 0.0f);
+}
+
+// boxes of the finite analytic records (item k = record linear + k)
+__global__ void k_prim_boxes(const float4* geo, const uint32_t* type, uint32_t linear, uint32_t n,
+                             float4* blo, float4* bhi) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 g = geo[linear + k];
+    const uint32_t t = type[linear + k];
+    if (t == 0u) {
+        blo[k] = make_float4(g.x - g.w, g.y - g.w, g.z - g.w, 0.0f);
+        bhi[k] = make_float4(g.x + g.w, g.y + g.w, g.z + g.w, 0.0f);
+    } else if (t == 1u) {
+        blo[k] = make_float4(-1e30f, -1e30f, -1e30f, 0.0f);
+        bhi[k] = make_float4(1e30f, 1e30f, 1e30f, 0.0f);
+    } else {
+        blo[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        bhi[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+// wide-leaf-order gathers
+__global__ void k_gather_tris(const float4* tri, const uint32_t* order, const uint32_t* rank, uint32_t n,
+                              float4* tri4) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t j = order[p];
+    tri4[3u * p] = tri[3u * j];
+    tri4[3u * p + 1u] = tri[3u * j + 1u];
+    const float4 c = tri[3u * j + 2u];
+    tri4[3u * p + 2u] = make_float4(c.x, c.y, c.z, __uint_as_float(rank[j]));
+}
+
+__global__ void k_gather_prims(const float4* geo, const uint32_t* type, const uint32_t* order,
+                               const uint32_t* rank, uint32_t linear, uint32_t n, float4* g4, uint4* m4) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t k = order[p];
+    const uint32_t slot = linear + k;
+    g4[p] = geo[slot];
+    m4[p] = make_uint4(slot, type[slot], linear + rank[k], 0u);
+}
+
+__global__ void k_iota(uint32_t* a, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = i;
+}
+
+__global__ void kb_init_bins(uint32_t* bins, uint32_t nwords) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nwords) return;
+    const uint32_t w = i % ptb::kBinWords;
+    bins[i] = (w == 0u) ? 0u : ((w <= 3u || (w >= 7u && w <= 9u)) ? 0xFFFFFFFFu : 0u);
 }
 
 __global__ void k_init_wave(DFrame F, DPaths P, uint32_t npaths, uint32_t frame0) {
@@ -354,6 +412,7 @@ __global__ void k_camera(DFrame F, DPaths P, uint32_t npaths, uint32_t s) {
     P.q[0][p] = p;
 }
 
+template <bool kWide>
 __global__ void __launch_bounds__(kThreads) k_extend(DScene S, DPaths P, int qsel) {
     const uint32_t n = P.cnt[qsel];
     const uint32_t* q = P.q[qsel];
@@ -361,7 +420,7 @@ __global__ void __launch_bounds__(kThreads) k_extend(DScene S, DPaths P, int qse
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
         const float4 o = P.ray_o[p], d = P.ray_d[p];
-        const HitRec h = trace_closest(S, v3(o), v3(d), 1e30f);
+        const HitRec h = trace_any_mode(S, v3(o), v3(d), 1e30f, kWide);
         P.hit_t[p] = h.t;
         P.hit_id[p] = h.id;
         ++done;
@@ -533,13 +592,14 @@ __global__ void __launch_bounds__(kThreads) k_shade(DScene S, DFrame F, DPaths P
     }
 }
 
+template <bool kWide>
 __global__ void __launch_bounds__(kThreads) k_shadow(DScene S, DPaths P, int kmax) {
     const uint32_t n = P.cnt[2];
     uint32_t segs = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t e = P.sq[i];
         const float4 o = P.sh_o[e], d = P.sh_d[e];
-        const V3 tr = transmittance(S, v3(o), v3(d), o.w, kmax, segs);
+        const V3 tr = transmittance(S, v3(o), v3(d), o.w, kmax, segs, kWide);
         P.sh_tr[e] = f4(tr, 0.0f);
     }
     warp_add(P.stat + 1, segs);
@@ -614,10 +674,10 @@ __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint
     if (i >= n) return;
     const float4 o = ro[i], d = rd[i];
     const float tinit = (d.w > 0.0f) ? d.w : 1e30f;
-    const HitRec h = trace_closest(S, v3(o), v3(d), tinit);
+    const HitRec h = trace_any_mode(S, v3(o), v3(d), tinit, S.use_wide != 0u);
     uint32_t id = h.id;
     if (id != kMiss && (id & kTriBit)) {
-        const float4 a = S.tri[3u * (id & ~kTriBit)];
+        const float4 a = (S.use_wide && S.t_wide) ? S.tri4[3u * (id & ~kTriBit)] : S.tri[3u * (id & ~kTriBit)];
         id = kTriBit | __float_as_uint(a.w);
     }
     hit[i] = id;
@@ -659,6 +719,14 @@ struct pt_gpu_ctx {
     DBuf<float> hit_t;
     DBuf<unsigned long long> stat;
     uint32_t wave_frames_override = 0;
+    // wide SAH trees built on the device at upload
+    int traversal = 0;   // 0 wide (default), 1 reference BVHs
+    bool a_wide = false, t_wide = false;
+    uint32_t a4_count = 0, t4_count = 0, a4_depth = 0, t4_depth = 0;
+    DBuf<float4> a4, a4_geo, t4, tri4, tri_lo, tri_hi;
+    DBuf<uint4> a4_meta;
+    double build_ms = 0.0;
+    uint32_t t4_bin_nodes = 0;
     PtStats stats{};
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -754,7 +822,18 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
                                     c->hdri_col[4 * i + 3]);
     }
     S.err = c->err_word.p;
+    S.use_wide = (c->traversal == 0) ? 1u : 0u;
+    S.a_wide = c->a_wide ? 1u : 0u;
+    S.t_wide = c->t_wide ? 1u : 0u;
+    S.a4 = c->a4.p;
+    S.a4_geo = c->a4_geo.p;
+    S.a4_meta = c->a4_meta.p;
+    S.t4 = c->t4.p;
+    S.tri4 = c->tri4.p;
     if (prm) {
+        // a linear-scan request over prims uploaded with a BVH changes the
+        // reference test order: use the reference walk for that dispatch
+        if (prm->bvh_params[1] == 0u && c->bvh_nodes != 0u) S.a_wide = 0u;
         // the push tail decides what the kernel walks (bvh_params), as in the reference
         S.linear_count = prm->bvh_params[0];
         S.bvh_nodes = prm->bvh_params[1];
@@ -794,6 +873,198 @@ int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     rc |= dalloc(ctx, ctx->sh_tr, 3 * npaths);
     if (rc) return PT_ERR_OOM;
     ctx->cap = npaths;
+    return PT_OK;
+}
+
+
+float o2f_host(uint32_t u) {
+    const uint32_t v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    float f;
+    std::memcpy(&f, &v, 4);
+    return f;
+}
+
+// Binned-SAH binary tree over n items with boxes lo/hi (device), item order in idx.
+int gpu_build_tree(pt_gpu_ctx* ctx, const float4* lo, const float4* hi, uint32_t n,
+                   std::vector<ptb::Node2H>& nodes, DBuf<uint32_t>& idx) {
+    nodes.clear();
+    if (n == 0) return PT_OK;
+    DBuf<uint32_t> tmp, ctr, bins, cnt2, cb;
+    DBuf<float4> dnodes, tcmin, tcmax, ccmin, ccmax;
+    DBuf<uint4> tinfo, chunks, cinfo, sinfo;
+    DBuf<int4> split;
+    auto cleanup = [&]() {
+        dfree(tmp); dfree(ctr); dfree(bins); dfree(cnt2); dfree(cb); dfree(dnodes); dfree(tcmin);
+        dfree(tcmax); dfree(ccmin); dfree(ccmax); dfree(tinfo); dfree(chunks); dfree(cinfo); dfree(sinfo);
+        dfree(split);
+    };
+    int rc = 0;
+    if ((rc = dalloc(ctx, idx, n)) || (rc = dalloc(ctx, tmp, n)) || (rc = dalloc(ctx, dnodes, 4 * size_t(n))) ||
+        (rc = dalloc(ctx, ctr, 1)) || (rc = dalloc(ctx, cb, 6))) {
+        cleanup();
+        return rc;
+    }
+#define BK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e__ = (call);                                                         \
+        if (e__ != cudaSuccess) {                                                         \
+            cleanup();                                                                    \
+            return set_err(ctx, PT_ERR_CUDA, std::string("bvh build: ") + cudaGetErrorString(e__)); \
+        }                                                                                 \
+    } while (0)
+    k_iota<<<(n + 255) / 256, 256, 0, ctx->stream>>>(idx.p, n);
+    const uint32_t init[7] = {1u, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    BK(cudaMemcpyAsync(ctr.p, init, 4, cudaMemcpyHostToDevice, ctx->stream));
+    BK(cudaMemcpyAsync(cb.p, init + 1, 24, cudaMemcpyHostToDevice, ctx->stream));
+    ptb::kb_cbounds<<<std::min<uint32_t>((n + 255) / 256, 1024), 256, 0, ctx->stream>>>(lo, hi, n, cb.p);
+    uint32_t cbh[6];
+    BK(cudaMemcpyAsync(cbh, cb.p, 24, cudaMemcpyDeviceToHost, ctx->stream));
+    BK(cudaStreamSynchronize(ctx->stream));
+    std::vector<uint4> large, small;
+    std::vector<float4> lmin, lmax;
+    const float4 rmin = make_float4(o2f_host(cbh[0]), o2f_host(cbh[1]), o2f_host(cbh[2]), 0.0f);
+    const float4 rmax = make_float4(o2f_host(cbh[3]), o2f_host(cbh[4]), o2f_host(cbh[5]), 0.0f);
+    if (n > ptb::kSmallTask) {
+        large.push_back(make_uint4(0, n, 0, 0));
+        lmin.push_back(rmin);
+        lmax.push_back(rmax);
+    } else {
+        small.push_back(make_uint4(0, n, 0, 0));
+    }
+    while (!large.empty()) {
+        const uint32_t T = uint32_t(large.size());
+        std::vector<uint4> ch;
+        for (uint32_t t = 0; t < T; ++t)
+            for (uint32_t b = large[t].x; b < large[t].y; b += ptb::kChunk)
+                ch.push_back(make_uint4(t, b, std::min(b + ptb::kChunk, large[t].y), 0));
+        const uint32_t nch = uint32_t(ch.size());
+        if ((rc = dupload(ctx, tinfo, large.data(), T)) || (rc = dupload(ctx, tcmin, lmin.data(), T)) ||
+            (rc = dupload(ctx, tcmax, lmax.data(), T)) || (rc = dupload(ctx, chunks, ch.data(), nch)) ||
+            (rc = dalloc(ctx, bins, size_t(T) * ptb::kTaskBinWords)) || (rc = dalloc(ctx, split, T)) ||
+            (rc = dalloc(ctx, cinfo, 2 * size_t(T))) || (rc = dalloc(ctx, ccmin, 2 * size_t(T))) ||
+            (rc = dalloc(ctx, ccmax, 2 * size_t(T))) || (rc = dalloc(ctx, cnt2, 2 * size_t(T)))) {
+            cleanup();
+            return rc;
+        }
+        const uint32_t nw = T * ptb::kTaskBinWords;
+        kb_init_bins<<<(nw + 255) / 256, 256, 0, ctx->stream>>>(bins.p, nw);
+        ptb::kb_bin<<<nch, 256, 0, ctx->stream>>>(chunks.p, tcmin.p, tcmax.p, idx.p, lo, hi, bins.p);
+        ptb::kb_split<<<(T + 127) / 128, 128, 0, ctx->stream>>>(T, tinfo.p, bins.p, dnodes.p, ctr.p, split.p,
+                                                               cinfo.p, ccmin.p, ccmax.p, tcmin.p, tcmax.p);
+        BK(cudaMemsetAsync(cnt2.p, 0, 8 * size_t(T), ctx->stream));
+        ptb::kb_partition<<<nch, 256, 0, ctx->stream>>>(chunks.p, tinfo.p, split.p, tcmin.p, tcmax.p, idx.p, lo,
+                                                         hi, cnt2.p, tmp.p);
+        ptb::kb_copy<<<nch, 256, 0, ctx->stream>>>(chunks.p, tmp.p, idx.p);
+        std::vector<uint4> ci(2 * T);
+        std::vector<float4> cmn(2 * T), cmx(2 * T);
+        BK(cudaGetLastError());
+        BK(cudaMemcpyAsync(ci.data(), cinfo.p, 2 * size_t(T) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+        BK(cudaMemcpyAsync(cmn.data(), ccmin.p, 2 * size_t(T) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+        BK(cudaMemcpyAsync(cmx.data(), ccmax.p, 2 * size_t(T) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+        BK(cudaStreamSynchronize(ctx->stream));
+        large.clear();
+        lmin.clear();
+        lmax.clear();
+        for (uint32_t c = 0; c < 2 * T; ++c) {
+            const uint32_t cnt = ci[c].y - ci[c].x;
+            if (cnt > ptb::kSmallTask) {
+                large.push_back(ci[c]);
+                lmin.push_back(cmn[c]);
+                lmax.push_back(cmx[c]);
+            } else {
+                small.push_back(ci[c]);
+            }
+        }
+    }
+    if (!small.empty()) {
+        const uint32_t S = uint32_t(small.size());
+        if ((rc = dupload(ctx, sinfo, small.data(), S))) {
+            cleanup();
+            return rc;
+        }
+        ptb::kb_small<<<(S + 127) / 128, 128, 0, ctx->stream>>>(S, sinfo.p, idx.p, lo, hi, dnodes.p, ctr.p);
+    }
+    uint32_t count = 0;
+    BK(cudaGetLastError());
+    BK(cudaMemcpyAsync(&count, ctr.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    BK(cudaStreamSynchronize(ctx->stream));
+    if (count > 2 * n) {
+        cleanup();
+        return set_err(ctx, PT_ERR_KERNEL, "bvh build: node count overflow");
+    }
+    nodes.resize(count);
+    BK(cudaMemcpyAsync(nodes.data(), dnodes.p, size_t(count) * 32, cudaMemcpyDeviceToHost, ctx->stream));
+    BK(cudaStreamSynchronize(ctx->stream));
+#undef BK
+    cleanup();
+    return PT_OK;
+}
+
+// Wide tree over the triangle slots of the uploaded (reference) mesh BVH.
+int build_wide_mesh(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref, uint32_t n_slots) {
+    ctx->t_wide = false;
+    ctx->t4_count = 0;
+    if (n_slots == 0 || n_ref == 0) return PT_OK;
+    std::vector<uint32_t> rank;
+    if (!ptb::ref_ranks(ref_nodes, n_ref, n_slots, 64, rank)) return PT_OK;   // keep the reference walk
+    std::vector<ptb::Node2H> bin;
+    DBuf<uint32_t> order, drank;
+    int rc = gpu_build_tree(ctx, ctx->tri_lo.p, ctx->tri_hi.p, n_slots, bin, order);
+    if (rc) { dfree(order); return rc; }
+    std::vector<ptb::Wide4> wide;
+    const int depth = ptb::collapse4(bin, wide);
+    ctx->t4_bin_nodes = uint32_t(bin.size());
+    if (3 * depth + 1 > kWideStackDev) { dfree(order); return PT_OK; }
+    if ((rc = dupload(ctx, drank, rank.data(), n_slots)) || (rc = dalloc(ctx, ctx->tri4, 3 * size_t(n_slots))) ||
+        (rc = dupload(ctx, ctx->t4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
+        dfree(order); dfree(drank);
+        return rc;
+    }
+    k_gather_tris<<<(n_slots + 255) / 256, 256, 0, ctx->stream>>>(ctx->tri.p, order.p, drank.p, n_slots, ctx->tri4.p);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    dfree(order);
+    dfree(drank);
+    if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("gather tris: ") + cudaGetErrorString(e));
+    ctx->t4_count = uint32_t(wide.size());
+    ctx->t4_depth = uint32_t(depth);
+    ctx->t_wide = true;
+    return PT_OK;
+}
+
+// Wide tree over the finite analytic records [linear, n).
+int build_wide_prims(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref) {
+    ctx->a_wide = false;
+    ctx->a4_count = 0;
+    const uint32_t nf = ctx->prim_count - ctx->linear_count;
+    if (nf == 0) return PT_OK;
+    std::vector<uint32_t> rank;
+    if (!ptb::ref_ranks(ref_nodes, n_ref, nf, 32, rank)) return PT_OK;
+    DBuf<float4> blo, bhi;
+    DBuf<uint32_t> order, drank;
+    auto cleanup = [&]() { dfree(blo); dfree(bhi); dfree(order); dfree(drank); };
+    int rc = 0;
+    if ((rc = dalloc(ctx, blo, nf)) || (rc = dalloc(ctx, bhi, nf))) { cleanup(); return rc; }
+    k_prim_boxes<<<(nf + 255) / 256, 256, 0, ctx->stream>>>(ctx->prim_geo.p, ctx->prim_type.p, ctx->linear_count,
+                                                           nf, blo.p, bhi.p);
+    std::vector<ptb::Node2H> bin;
+    if ((rc = gpu_build_tree(ctx, blo.p, bhi.p, nf, bin, order))) { cleanup(); return rc; }
+    std::vector<ptb::Wide4> wide;
+    const int depth = ptb::collapse4(bin, wide);
+    if (3 * depth + 1 > kWideStackDev) { cleanup(); return PT_OK; }
+    if ((rc = dupload(ctx, drank, rank.data(), nf)) || (rc = dalloc(ctx, ctx->a4_geo, nf)) ||
+        (rc = dalloc(ctx, ctx->a4_meta, nf)) ||
+        (rc = dupload(ctx, ctx->a4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
+        cleanup();
+        return rc;
+    }
+    k_gather_prims<<<(nf + 255) / 256, 256, 0, ctx->stream>>>(ctx->prim_geo.p, ctx->prim_type.p, order.p, drank.p,
+                                                             ctx->linear_count, nf, ctx->a4_geo.p, ctx->a4_meta.p);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("gather prims: ") + cudaGetErrorString(e));
+    ctx->a4_count = uint32_t(wide.size());
+    ctx->a4_depth = uint32_t(depth);
+    ctx->a_wide = true;
     return PT_OK;
 }
 
@@ -851,6 +1122,8 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
         dfree(*b);
     dfree(ctx->marg);
     dfree(ctx->cond);
+    for (auto* b : {&ctx->a4, &ctx->a4_geo, &ctx->t4, &ctx->tri4, &ctx->tri_lo, &ctx->tri_hi}) dfree(*b);
+    dfree(ctx->a4_meta);
     dfree(ctx->hit_t);
     dfree(ctx->stat);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
@@ -884,7 +1157,7 @@ int pt_gpu_upload_prims(pt_gpu_ctx* ctx, const float* recs28, uint32_t n, uint32
     ctx->linear_count = linear_count;
     ctx->bvh_nodes = n_nodes;
     CK(cudaStreamSynchronize(ctx->stream));
-    return PT_OK;
+    return build_wide_prims(ctx, nodes, n_nodes);
 }
 
 int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv, const uint32_t* indices,
@@ -909,13 +1182,15 @@ int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv, con
         (rc = dupload(ctx, didx, indices, size_t(nt) * 3)) ||
         (rc = dupload(ctx, dperm, perm, n_perm)) ||
         (rc = dupload(ctx, dmat, mat_ids, mat_ids ? nt : 0)) ||
-        (rc = dalloc(ctx, ctx->tri, size_t(n_perm) * 3))) {
+        (rc = dalloc(ctx, ctx->tri, size_t(n_perm) * 3)) || (rc = dalloc(ctx, ctx->tri_lo, n_perm)) ||
+        (rc = dalloc(ctx, ctx->tri_hi, n_perm))) {
         dfree(dpos); dfree(didx); dfree(dperm); dfree(dmat);
         return rc;
     }
     if (n_perm) {
         k_prep_tris<<<(n_perm + 255) / 256, 256, 0, ctx->stream>>>(dpos.p, didx.p, dperm.p, dmat.p,
-                                                                   n_perm, ctx->tri.p);
+                                                                   n_perm, ctx->tri.p, ctx->tri_lo.p,
+                                                                   ctx->tri_hi.p);
     }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -927,7 +1202,19 @@ int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv, con
     ctx->tri_count = nt;
     ctx->mesh_has_mat = (mat_ids != nullptr);
     CK(cudaStreamSynchronize(ctx->stream));
-    return PT_OK;
+    cudaEvent_t b0, b1;
+    cudaEventCreate(&b0);
+    cudaEventCreate(&b1);
+    cudaEventRecord(b0, ctx->stream);
+    rc = build_wide_mesh(ctx, nodes, n_nodes, n_perm);
+    cudaEventRecord(b1, ctx->stream);
+    cudaEventSynchronize(b1);
+    float bms = 0.0f;
+    cudaEventElapsedTime(&bms, b0, b1);
+    ctx->build_ms = bms;
+    cudaEventDestroy(b0);
+    cudaEventDestroy(b1);
+    return rc;
 }
 
 int pt_gpu_upload_materials(pt_gpu_ctx* ctx, const float* mats12, uint32_t n) {
@@ -1096,11 +1383,15 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
                 CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
                 const int ge = grid_for(ctx, npaths, 8);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                k_extend<<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                if (S.use_wide) k_extend<true><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                else k_extend<false><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                k_shadow<<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                if (S.use_wide)
+                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                else
+                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 k_resolve<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, qs);
                 ctx->stats.extend_launches++;
@@ -1151,6 +1442,26 @@ int pt_gpu_render_to_host(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathP
 int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out) {
     if (!ctx || !out) return PT_ERR_INVALID;
     *out = ctx->stats;
+    return PT_OK;
+}
+
+int pt_gpu_set_traversal(pt_gpu_ctx* ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 1) return PT_ERR_INVALID;
+    ctx->traversal = mode;
+    return PT_OK;
+}
+
+int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out) {
+    if (!ctx || !out) return PT_ERR_INVALID;
+    std::memset(out, 0, sizeof(*out));
+    out->traversal = uint32_t(ctx->traversal);
+    out->mesh_wide = ctx->t_wide ? 1u : 0u;
+    out->prims_wide = ctx->a_wide ? 1u : 0u;
+    out->mesh_wide_nodes = ctx->t4_count;
+    out->mesh_wide_depth = ctx->t4_depth;
+    out->mesh_binary_nodes = ctx->t4_bin_nodes;
+    out->prims_wide_nodes = ctx->a4_count;
+    out->mesh_build_ms = ctx->build_ms;
     return PT_OK;
 }
 

@@ -175,6 +175,25 @@ int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out);
  * launch so PtStats.extend_ms / shadow_ms report their device time. */
 int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on);
 
+/* Traversal structure: 0 (default) = 4-wide SAH trees built on the device at
+ * upload from the same primitives (hit ids and distances still follow the
+ * reference's first-tested-wins order exactly, via per-primitive reference
+ * ranks); 1 = walk the uploaded reference BVHs in the reference's own order. */
+int pt_gpu_set_traversal(pt_gpu_ctx* ctx, int mode);
+
+typedef struct PtAccelInfo {
+    uint32_t traversal;          /* current mode */
+    uint32_t mesh_wide;          /* 1 if the mesh wide tree is in use */
+    uint32_t prims_wide;         /* 1 if the analytic wide tree is in use */
+    uint32_t mesh_wide_nodes;
+    uint32_t mesh_wide_depth;
+    uint32_t mesh_binary_nodes;  /* SAH binary nodes before the 4-wide collapse */
+    uint32_t prims_wide_nodes;
+    uint32_t reserved;
+    double   mesh_build_ms;      /* device build time of the mesh wide tree */
+} PtAccelInfo;
+int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out);
+
 /* Max number of frames batched into one device wave (default: chosen from the
  * frame size so a wave holds about 16 M paths). 0 restores the default. */
 int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave);

@@ -9,6 +9,8 @@ from conftest import xorshift_rays, xorshift_spheres
 
 pytestmark = pytest.mark.gpu
 
+MODES = [pytest.param(0, id="wide_sah"), pytest.param(1, id="reference_bvh")]
+
 
 def random_rays(n, lo, hi, seed):
     rng = np.random.default_rng(seed)
@@ -20,7 +22,8 @@ def random_rays(n, lo, hi, seed):
     return ro, rd
 
 
-def check_trace(pt, orc, dev, s, ro, rd):
+def check_trace(pt, orc, dev, s, ro, rd, mode=0):
+    dev.set_traversal(mode)
     dev.upload(s)
     head, prm = s.push(8, 8)
     g_hit, g_t = dev.trace(ro, rd)
@@ -30,29 +33,63 @@ def check_trace(pt, orc, dev, s, ro, rd):
     return o_hit
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("n,seed", [(50, 0xABCDEF01), (2000, 0x12345678)])
-def test_trace_xorshift_spheres(pt, orc, dev, n, seed):
+def test_trace_xorshift_spheres(pt, orc, dev, n, seed, mode):
     s = pt.Scene()
     for i, c in enumerate(xorshift_spheres(n, seed)):
         s.sphere(i, *map(float, c[:3]), float(c[3]), 0, (0.5, 0.5, 0.5))
     s.env(np.zeros((2, 4, 3), np.float32))
     ro, rd = xorshift_rays(1000, 0x12345678)
-    hit = check_trace(pt, orc, dev, s, ro, rd)
+    hit = check_trace(pt, orc, dev, s, ro, rd, mode)
     assert (hit != 0xFFFFFFFF).sum() > 50
 
 
-def test_trace_c0_scene(pt, orc, dev):
+@pytest.mark.parametrize("mode", MODES)
+def test_trace_c0_scene(pt, orc, dev, mode):
     s = pt.Scene().synth(0, seed=0)
     ro, rd = random_rays(20000, -12, 12, 1)
-    hit = check_trace(pt, orc, dev, s, ro, rd)
+    hit = check_trace(pt, orc, dev, s, ro, rd, mode)
     assert ((hit & (1 << 30)) != 0).sum() > 100 and (hit < (1 << 30)).sum() > 100
 
 
-def test_trace_c1_scene_small(pt, orc, dev):
+@pytest.mark.parametrize("mode", MODES)
+def test_trace_c1_scene_small(pt, orc, dev, mode):
     s = pt.Scene().synth(1, seed=0, scale=0.02)
     ro, rd = random_rays(20000, -60, 60, 2)
     ro[:, 1] = np.abs(ro[:, 1]) + 0.5
-    check_trace(pt, orc, dev, s, ro, rd)
+    check_trace(pt, orc, dev, s, ro, rd, mode)
+    if mode == 0:
+        info = dev.accel_info()
+        assert info.mesh_wide == 1 and info.prims_wide == 1 and info.mesh_wide_nodes > 0
+
+
+def test_trace_shared_edges_ties_follow_the_reference_order(pt, orc, dev):
+    """A triangle grid hit exactly on shared edges and vertices: equal distances
+    on several triangles; the winner must be the reference's first-tested one."""
+    n = 24
+    xs = np.linspace(-6, 6, n + 1, dtype=np.float32)
+    pos = np.array([[x, 0.0, z] for z in xs for x in xs], np.float32)
+    idx = []
+    for j in range(n):
+        for i in range(n):
+            a = j * (n + 1) + i
+            idx += [[a, a + n + 1, a + 1], [a + 1, a + n + 1, a + n + 2]]
+    s = pt.Scene()
+    s.mesh(pos, np.array(idx, np.uint32))
+    s.env(np.zeros((2, 4, 3), np.float32))
+    m = 4000
+    rng = np.random.default_rng(9)
+    ro = np.zeros((m, 4), np.float32)
+    rd = np.zeros((m, 4), np.float32)
+    gx = rng.integers(0, n + 1, m).astype(np.float32)
+    gz = rng.integers(0, n + 1, m).astype(np.float32)
+    tx = xs[0] + gx * np.float32(0.5)        # every other target on a grid line or vertex
+    tz = xs[0] + gz * np.float32(0.5)
+    ro[:, 0], ro[:, 1], ro[:, 2] = tx, 5.0, tz
+    rd[:, 1] = -1.0
+    for mode in (0, 1):
+        check_trace(pt, orc, dev, s, ro, rd, mode)
 
 
 def test_trace_tmax_is_the_initial_distance(pt, orc, dev):
@@ -62,7 +99,8 @@ def test_trace_tmax_is_the_initial_distance(pt, orc, dev):
     check_trace(pt, orc, dev, s, ro, rd)
 
 
-def render_both(pt, orc, dev, s, W, H, frames):
+def render_both(pt, orc, dev, s, W, H, frames, mode=0):
+    dev.set_traversal(mode)
     dev.upload(s)
     dev.set_target(W, H)
     head, prm = s.push(W, H, frame_index=11, reset=1)
@@ -72,9 +110,10 @@ def render_both(pt, orc, dev, s, W, H, frames):
     return g, o, c
 
 
-def test_render_c0_bit_exact(pt, orc, dev):
+@pytest.mark.parametrize("mode", MODES)
+def test_render_c0_bit_exact(pt, orc, dev, mode):
     s = pt.Scene().synth(0, seed=3)
-    g, o, c = render_both(pt, orc, dev, s, 48, 40, 2)
+    g, o, c = render_both(pt, orc, dev, s, 48, 40, 2, mode)
     st = dev.stats()
     assert st.extension_rays == c.ext_rays
     assert st.shadow_rays == c.shadow_rays
@@ -82,9 +121,10 @@ def test_render_c0_bit_exact(pt, orc, dev):
     assert (g[..., 3] == 2).all() and g[..., :3].max() > 0
 
 
-def test_render_c1_small_bit_exact(pt, orc, dev):
+@pytest.mark.parametrize("mode", MODES)
+def test_render_c1_small_bit_exact(pt, orc, dev, mode):
     s = pt.Scene().synth(1, seed=4, scale=0.02)
-    g, o, c = render_both(pt, orc, dev, s, 64, 36, 3)
+    g, o, c = render_both(pt, orc, dev, s, 64, 36, 3, mode)
     assert dev.stats().shadow_rays == c.shadow_rays
     np.testing.assert_array_equal(g, o)
     assert g[..., :3].max() > 0
@@ -179,7 +219,10 @@ def test_full_size_c1_frame_matches_oracle_on_crops(pt, orc, dev):
     """1920x1080 C1 frame: finite, count 1, and three 16x16 crops identical to the oracle."""
     s = pt.Scene().synth(1, seed=0)
     W, H = 1920, 1080
+    dev.set_traversal(0)
     dev.upload(s)
+    info = dev.accel_info()
+    assert info.mesh_wide == 1 and info.prims_wide == 1
     dev.set_target(W, H)
     head, prm = s.push(W, H, 0, 1)
     dev.render(head, prm, 1)
