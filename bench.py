@@ -203,6 +203,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traversal", type=int, default=0, choices=[0, 1],
+                    help="0: 4-wide SAH trees built on the device (default); 1: the reference BVHs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -219,7 +221,9 @@ def main():
     pt = load_pkg()
     scene = pt.Scene().synth(1, seed=0)
     dev = pt.Device(local)
+    dev.set_traversal(args.traversal)
     dev.upload(scene)
+    accel = dev.accel_info()
     dev.set_target(W_FULL, H_FULL)
     # replicas: each rank renders its own disjoint frame range of the same workload
     head, prm = scene.push(W_FULL, H_FULL, frame_index=rank * 1_000_000, reset=1)
@@ -306,6 +310,9 @@ def main():
             "config": {"workload": "triangles+analytic 1920x1080 1spp x64 frames depth 8 (2,460,288 tris, "
                                    "1024 spheres, 2048x1024 env)", "frames_per_step": args.frames,
                        "parallelism": f"replicas x{world}",
+                       "traversal": ("4-wide SAH (device-built, %d nodes, depth %d, build %.1f ms)"
+                                     % (accel.mesh_wide_nodes, accel.mesh_wide_depth, accel.mesh_build_ms))
+                       if (accel.mesh_wide and args.traversal == 0) else "reference binary BVH",
                        "l2": "no flush: per-wave path state (~6 GB) and scene (~250 MB) exceed the 129 MB L2"},
             "e2e": {"value": e2e_segs / t_e2e / 1e6, "unit": "Mrays/s",
                     "h2d_bytes_per_step": args.frames * (ctypes.sizeof(pt.PtPushHead) + ctypes.sizeof(pt.PtPathParams)),

@@ -396,98 +396,119 @@ __device__ __forceinline__ float isect_geo(uint32_t type, float4 g, V3 ro, V3 rd
 }
 
 template <bool kTri>
+__device__ __forceinline__ void wide_leaf(const DScene& S, uint32_t code, V3 ro, V3 rd, Best& b,
+                                          uint32_t key_base) {
+    const uint32_t first = code & 0x0FFFFFFFu;
+    const uint32_t cnt = ((code >> 28) & 7u) + 1u;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t p = first + k;
+        if (kTri) {
+            const float4 a = __ldg(S.tri4 + 3u * p);
+            const float4 bb = __ldg(S.tri4 + 3u * p + 1u);
+            const float4 c = __ldg(S.tri4 + 3u * p + 2u);
+            const V3 v0 = v3(a), e1 = v3(bb), e2 = v3(c);
+            const V3 pv = cross(rd, e2);
+            const float det = dot(e1, pv);
+            if (fabsf(det) < 1e-8f) continue;
+            const float inv_det = 1.0f / det;
+            const V3 tvec = ro - v0;
+            const float u = dot(tvec, pv) * inv_det;
+            if (u < 0.0f || u > 1.0f) continue;
+            const V3 qv = cross(tvec, e1);
+            const float v = dot(rd, qv) * inv_det;
+            if (v < 0.0f || u + v > 1.0f) continue;
+            const float tt = dot(e2, qv) * inv_det;
+            const uint32_t key = key_base | __float_as_uint(c.w);
+            if (tt > 1e-3f && better(tt, key, b)) {
+                b.t = tt;
+                b.key = key;
+                b.id = kTriBit | p;
+            }
+        } else {
+            const float4 g = __ldg(S.a4_geo + p);
+            const uint4 m = __ldg(S.a4_meta + p);
+            const float t = isect_geo(m.y, g, ro, rd);
+            if (t > 1e-3f && better(t, m.z, b)) {
+                b.t = t;
+                b.key = m.z;
+                b.id = m.x;
+            }
+        }
+    }
+}
+
+// Front-to-back walk of one wide tree.  Leaves found while descending are
+// postponed until every active lane of the warp holds one (or has run out of
+// nodes), so the warp intersects primitives together instead of interleaving
+// box and primitive work lane by lane.  The slab test uses fma on -ro*inv and
+// widens the interval by 4e-7 relative: with the outward-padded boxes no true
+// hit can be culled by rounding (culling never changes the result, only the
+// work; the tie keys decide equal distances).
+template <bool kTri>
 __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, V3 ro, V3 rd, V3 inv,
                                           Best& b, uint32_t key_base, uint32_t& iters, uint32_t* st_code,
                                           float* st_t) {
-    int sp = 0;
+    const float nx = -ro.x * inv.x, ny = -ro.y * inv.y, nz = -ro.z * inv.z;
+    int sp = 1;
     st_code[0] = 0u;
     st_t[0] = -3.0e38f;
-    sp = 1;
-    while (sp > 0) {
-        if (++iters > kTraverseCap) { atomicOr(S.err, 1u); return; }
-        --sp;
-        const uint32_t code = st_code[sp];
-        if (st_t[sp] > b.t) continue;
-        if (code & kLeafBit) {
-            const uint32_t first = code & 0x0FFFFFFFu;
-            const uint32_t cnt = ((code >> 28) & 7u) + 1u;
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const uint32_t p = first + k;
-                if (kTri) {
-                    const float4 a = __ldg(S.tri4 + 3u * p);
-                    const float4 bb = __ldg(S.tri4 + 3u * p + 1u);
-                    const float4 c = __ldg(S.tri4 + 3u * p + 2u);
-                    const V3 v0 = v3(a), e1 = v3(bb), e2 = v3(c);
-                    const V3 pv = cross(rd, e2);
-                    const float det = dot(e1, pv);
-                    if (fabsf(det) < 1e-8f) continue;
-                    const float inv_det = 1.0f / det;
-                    const V3 tvec = ro - v0;
-                    const float u = dot(tvec, pv) * inv_det;
-                    if (u < 0.0f || u > 1.0f) continue;
-                    const V3 qv = cross(tvec, e1);
-                    const float v = dot(rd, qv) * inv_det;
-                    if (v < 0.0f || u + v > 1.0f) continue;
-                    const float tt = dot(e2, qv) * inv_det;
-                    const uint32_t key = key_base | __float_as_uint(c.w);
-                    if (tt > 1e-3f && better(tt, key, b)) {
-                        b.t = tt;
-                        b.key = key;
-                        b.id = kTriBit | p;
-                    }
-                } else {
-                    const float4 g = __ldg(S.a4_geo + p);
-                    const uint4 m = __ldg(S.a4_meta + p);
-                    const float t = isect_geo(m.y, g, ro, rd);
-                    if (t > 1e-3f && better(t, m.z, b)) {
-                        b.t = t;
-                        b.key = m.z;
-                        b.id = m.x;
-                    }
+    uint32_t leaf = 0u;   // postponed leaf (0 = none; leaf codes always carry kLeafBit)
+    while (sp > 0 || leaf) {
+        while (sp > 0 && !leaf) {
+            if (++iters > kTraverseCap) { atomicOr(S.err, 1u); return; }
+            --sp;
+            const uint32_t code = st_code[sp];
+            if (st_t[sp] > b.t) continue;
+            if (code & kLeafBit) {
+                leaf = code;
+                break;
+            }
+            const float4* nd = nodes + 8u * code;
+            const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
+            const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+            const int4 cn = __ldg(reinterpret_cast<const int4*>(nd + 7));
+            const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+            const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+            const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+            const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
+            float dist[4];
+            uint32_t codes[4];
+            int nh = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
+                const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
+                const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
+                float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+                float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+                tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
+                tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
+                if (nn[k] >= 0 && tmx >= fmaxf(tmin, 0.0f) && tmin <= b.t) {
+                    dist[nh] = tmin;
+                    codes[nh] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k]))
+                                            : uint32_t(cc[k]);
+                    ++nh;
                 }
             }
-            continue;
-        }
-        const float4* nd = nodes + 8u * code;
-        const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
-        const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
-        const int4 ch = *reinterpret_cast<const int4*>(nd + 6);
-        const int4 cn = *reinterpret_cast<const int4*>(nd + 7);
-        const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-        const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-        const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
-        const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
-        float dist[4];
-        uint32_t codes[4];
-        int nh = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (nn[k] < 0) continue;
-            const float t0x = (lx[k] - ro.x) * inv.x, t1x = (hx[k] - ro.x) * inv.x;
-            const float t0y = (ly[k] - ro.y) * inv.y, t1y = (hy[k] - ro.y) * inv.y;
-            const float t0z = (lz[k] - ro.z) * inv.z, t1z = (hz[k] - ro.z) * inv.z;
-            const float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-            const float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-            if (tmx >= fmaxf(tmin, 0.0f) && tmin <= b.t) {
-                dist[nh] = tmin;
-                codes[nh] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k]))
-                                        : uint32_t(cc[k]);
-                ++nh;
+            if (sp + nh > kWideStackDev) { atomicOr(S.err, 2u); return; }
+            for (int i = 0; i < nh; ++i) {   // farthest first: the nearest child is popped next
+                int far = i;
+                for (int j = i + 1; j < nh; ++j)
+                    if (dist[j] > dist[far]) far = j;
+                const float td = dist[far];
+                const uint32_t tc = codes[far];
+                dist[far] = dist[i];
+                codes[far] = codes[i];
+                st_t[sp] = td;
+                st_code[sp] = tc;
+                ++sp;
             }
+            if (!__any_sync(__activemask(), leaf == 0u && sp > 0)) break;
         }
-        if (sp + nh > kWideStackDev) { atomicOr(S.err, 2u); return; }
-        // push farthest first so the nearest child is popped next
-        for (int i = 0; i < nh; ++i) {
-            int far = i;
-            for (int j = i + 1; j < nh; ++j)
-                if (dist[j] > dist[far]) far = j;
-            const float td = dist[far];
-            const uint32_t tc = codes[far];
-            dist[far] = dist[i];
-            codes[far] = codes[i];
-            st_t[sp] = td;
-            st_code[sp] = tc;
-            ++sp;
+        if (leaf) {
+            wide_leaf<kTri>(S, leaf, ro, rd, b, key_base);
+            leaf = 0u;
         }
     }
 }

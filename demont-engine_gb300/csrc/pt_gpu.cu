@@ -372,11 +372,27 @@ __global__ void kb_init_bins(uint32_t* bins, uint32_t nwords) {
     bins[i] = (w == 0u) ? 0u : ((w <= 3u || (w >= 7u && w <= 9u)) ? 0xFFFFFFFFu : 0u);
 }
 
+// Path slot -> pixel: slots run through 8x4 pixel tiles (one warp per tile)
+// in row-major tile order, so a warp's primary rays are spatially coherent.
+// Frames whose size is not a multiple of the tile fall back to row order.
+__device__ __forceinline__ void slot_pixel(const DFrame& F, uint32_t pix, uint32_t& x, uint32_t& y) {
+    if ((F.W & 7u) == 0u && (F.H & 3u) == 0u) {
+        const uint32_t tile = pix >> 5, in = pix & 31u;
+        const uint32_t tw = F.W >> 3;
+        x = (tile % tw) * 8u + (in & 7u);
+        y = (tile / tw) * 4u + (in >> 3);
+    } else {
+        x = pix % F.W;
+        y = pix / F.W;
+    }
+}
+
 __global__ void k_init_wave(DFrame F, DPaths P, uint32_t npaths, uint32_t frame0) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npaths) return;
     const uint32_t f = p / F.npix, pix = p - f * F.npix;
-    const uint32_t x = pix % F.W, y = pix / F.W;
+    uint32_t x, y;
+    slot_pixel(F, pix, x, y);
     P.seed[p] = pcg_hash(x * 1973u + y * 9277u + (frame0 + f) * 26699u);
     P.fsum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
@@ -387,7 +403,8 @@ __global__ void k_camera(DFrame F, DPaths P, uint32_t npaths, uint32_t s) {
     if (p == 0) P.cnt[0] = npaths;
     if (p >= npaths) return;
     const uint32_t f = p / F.npix, pix = p - f * F.npix;
-    const uint32_t x = pix % F.W, y = pix / F.W;
+    uint32_t x, y;
+    slot_pixel(F, pix, x, y);
     uint32_t seed = P.seed[p];
     float jx, jy;
     if (F.denoiser != 0u && s == 0u) {
@@ -593,7 +610,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(DScene S, DFrame F, DPaths P
 }
 
 template <bool kWide>
-__global__ void __launch_bounds__(kThreads) k_shadow(DScene S, DPaths P, int kmax) {
+__global__ void __launch_bounds__(kThreads, 4) k_shadow(DScene S, DPaths P, int kmax) {
     const uint32_t n = P.cnt[2];
     uint32_t segs = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -640,9 +657,12 @@ __device__ __forceinline__ float clean(float v) { return (isnan(v) || isinf(v)) 
 
 __global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes, bool reset_first,
                              float ema_in) {
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;   // path slot within a frame
     if (pix >= F.npix) return;
-    float4 a = accum[pix];
+    uint32_t x, y;
+    slot_pixel(F, pix, x, y);
+    const size_t out = size_t(y) * F.W + x;
+    float4 a = accum[out];
     const float nspp = float(F.spp == 0u ? 1u : F.spp);
     const float ema = clampf(ema_in, 0.0f, 0.999f);
     for (uint32_t f = 0; f < nframes; ++f) {
@@ -665,7 +685,7 @@ __global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes
         }
         a = f4(avg, n_new);
     }
-    accum[pix] = a;
+    accum[out] = a;
 }
 
 __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint32_t n, uint32_t* hit,
@@ -823,8 +843,8 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     }
     S.err = c->err_word.p;
     S.use_wide = (c->traversal == 0) ? 1u : 0u;
-    S.a_wide = c->a_wide ? 1u : 0u;
-    S.t_wide = c->t_wide ? 1u : 0u;
+    S.a_wide = (S.use_wide && c->a_wide) ? 1u : 0u;
+    S.t_wide = (S.use_wide && c->t_wide) ? 1u : 0u;
     S.a4 = c->a4.p;
     S.a4_geo = c->a4_geo.p;
     S.a4_meta = c->a4_meta.p;
