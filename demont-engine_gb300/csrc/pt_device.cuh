@@ -634,13 +634,19 @@ __device__ __forceinline__ V3 cos_hemi(V3 n, uint32_t& seed) {
 }
 
 // transmittance (shaders/PathTrace.slang:5089-5196) with clouds and water off.
-// Counts the closest-hit queries it makes in *segs.
-__device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t_max, int kmax,
-                                            uint32_t& segs, bool wide) {
+// `first` is the closest hit of segment 0 when the caller already traced it
+// (first.t < 0: trace it here).  Counts the closest-hit queries made here.
+__device__ __forceinline__ V3 transmittance_from(const DScene& S, V3 o, V3 d, float t_max, int kmax,
+                                                 HitRec first, uint32_t& segs, bool wide) {
     V3 t = v3(1.0f, 1.0f, 1.0f);
     for (int i = 0; i <= kmax; ++i) {
-        ++segs;
-        const HitRec h = trace_any_mode(S, o, d, 1e30f, wide);
+        HitRec h;
+        if (i == 0 && first.t >= 0.0f) {
+            h = first;
+        } else {
+            ++segs;
+            h = trace_any_mode(S, o, d, 1e30f, wide);
+        }
         if (h.id == kMiss || h.t >= t_max) return t;
         const Surface sf = surface_at(S, o, d, h);
         if (sf.mat != kMatDielectric) return v3(0.0f, 0.0f, 0.0f);
@@ -662,6 +668,174 @@ __device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t
         t_max = fmaxf(t_max - adv, 0.0f);
     }
     return v3(0.0f, 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t_max, int kmax,
+                                            uint32_t& segs, bool wide) {
+    return transmittance_from(S, o, d, t_max, kmax, HitRec{-1.0f, kMiss}, segs, wide);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent closest-hit kernel over the wide trees (dynamic ray fetch).
+// Each lane holds one ray; when it finishes, the lane takes the next queued
+// ray at once (warp-aggregated atomic on a fetch counter) instead of waiting
+// for the slowest ray of its warp.  Within a round, the node phase runs while
+// any lane still has nodes to descend (lanes that popped a leaf hold it), then
+// every lane holding a leaf intersects it together.  Same hit semantics as
+// trace_wide: planes linearly, analytic tree, then the triangle tree.
+// ---------------------------------------------------------------------------
+constexpr int kPStack = 64;
+
+__device__ __forceinline__ void persistent_closest(const DScene& S, const uint32_t* queue, uint32_t n,
+                                                   const float4* ray_o, const float4* ray_d, float* out_t,
+                                                   uint32_t* out_id, uint32_t* fetch_ctr, uint32_t& done) {
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const bool has_a = S.a_wide && S.prim_count > S.linear_count;
+    const bool has_t = S.t_wide && S.tri_enabled != 0u && S.tri_nodes > 0u;
+    bool active = false, exhausted = false;
+    uint32_t item = 0, leaf = 0u, iters = 0;
+    int phase = 0, sp = 0;
+    V3 ro = v3(0.0f, 0.0f, 0.0f), rd = ro, inv = ro;
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    Best b{1e30f, 0u, kMiss};
+    uint32_t st_code[kPStack];
+    float st_t[kPStack];
+    for (;;) {
+        const bool need = !active && !exhausted;
+        const uint32_t m = __ballot_sync(FULL, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch_ctr, uint32_t(__popc(m)));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const uint32_t slot = base + uint32_t(__popc(m & ((1u << lane) - 1u)));
+                if (slot >= n) {
+                    exhausted = true;
+                } else {
+                    item = queue[slot];
+                    const float4 o = ray_o[item], d = ray_d[item];
+                    ro = v3(o);
+                    rd = v3(d);
+                    inv = safe_inv(rd);
+                    nx = -ro.x * inv.x;
+                    ny = -ro.y * inv.y;
+                    nz = -ro.z * inv.z;
+                    b = Best{1e30f, 0u, kMiss};
+                    for (uint32_t i = 0; i < S.linear_count; ++i) {
+                        const float t = isect_geo(__ldg(S.prim_type + i), __ldg(S.prim_geo + i), ro, rd);
+                        if (t > 1e-3f && better(t, i, b)) {
+                            b.t = t;
+                            b.key = i;
+                            b.id = i;
+                        }
+                    }
+                    sp = 0;
+                    leaf = 0u;
+                    iters = 0;
+                    if (has_a) {
+                        phase = 1;
+                        st_code[0] = 0u;
+                        st_t[0] = -3.0e38f;
+                        sp = 1;
+                    } else {
+                        phase = 2;
+                        if (has_t) {
+                            st_code[0] = 0u;
+                            st_t[0] = -3.0e38f;
+                            sp = 1;
+                        }
+                    }
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) break;
+        // node phase
+        for (;;) {
+            const bool want = active && leaf == 0u && sp > 0;
+            if (!__any_sync(FULL, want)) break;
+            if (!want) continue;
+            if (++iters > kTraverseCap) {
+                atomicOr(S.err, 1u);
+                sp = 0;
+                continue;
+            }
+            --sp;
+            const uint32_t code = st_code[sp];
+            if (st_t[sp] > b.t) continue;
+            if (code & kLeafBit) {
+                leaf = code;
+                continue;
+            }
+            const float4* nd = (phase == 1 ? S.a4 : S.t4) + 8u * code;
+            const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
+            const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+            const int4 cn = __ldg(reinterpret_cast<const int4*>(nd + 7));
+            const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+            const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+            const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+            const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
+            float dist[4];
+            uint32_t codes[4];
+            int nh = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
+                const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
+                const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
+                float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+                float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+                tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
+                tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
+                if (nn[k] >= 0 && tmx >= fmaxf(tmin, 0.0f) && tmin <= b.t) {
+                    dist[nh] = tmin;
+                    codes[nh] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k]))
+                                            : uint32_t(cc[k]);
+                    ++nh;
+                }
+            }
+            if (sp + nh > kPStack) {
+                atomicOr(S.err, 2u);
+                sp = 0;
+                continue;
+            }
+            for (int i = 0; i < nh; ++i) {
+                int far = i;
+                for (int j = i + 1; j < nh; ++j)
+                    if (dist[j] > dist[far]) far = j;
+                const float td = dist[far];
+                const uint32_t tc = codes[far];
+                dist[far] = dist[i];
+                codes[far] = codes[i];
+                st_t[sp] = td;
+                st_code[sp] = tc;
+                ++sp;
+            }
+        }
+        // leaf phase
+        if (active && leaf != 0u) {
+            if (phase == 1) wide_leaf<false>(S, leaf, ro, rd, b, 0u);
+            else wide_leaf<true>(S, leaf, ro, rd, b, 0x80000000u);
+            leaf = 0u;
+        }
+        // end of a tree
+        if (active && leaf == 0u && sp == 0) {
+            if (phase == 1 && has_t) {
+                phase = 2;
+                st_code[0] = 0u;
+                st_t[0] = -3.0e38f;
+                sp = 1;
+            } else {
+                out_t[item] = b.t;
+                out_id[item] = b.id;
+                active = false;
+                ++done;
+            }
+        }
+    }
 }
 
 }  // namespace ptd

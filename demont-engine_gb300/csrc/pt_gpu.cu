@@ -71,7 +71,9 @@ struct DPaths {
     float4* sh_tr;     // transmittance result
     uint32_t* q[2];
     uint32_t* sq;
-    uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue
+    uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue, [3] fetch counter
+    float* sh_hit_t;   // 3 per path: closest hit of the first shadow segment
+    uint32_t* sh_hit_id;
     unsigned long long* stat;   // [0] extension rays, [1] shadow segments
 };
 
@@ -622,6 +624,32 @@ __global__ void __launch_bounds__(kThreads, 4) k_shadow(DScene S, DPaths P, int 
     warp_add(P.stat + 1, segs);
 }
 
+
+// persistent closest hit for a queue of rays (extension rays or first shadow segments)
+__global__ void __launch_bounds__(kThreads, 4) k_closest(DScene S, const uint32_t* queue,
+                                                         const uint32_t* count, const float4* ray_o,
+                                                         const float4* ray_d, float* out_t, uint32_t* out_id,
+                                                         uint32_t* fetch_ctr, unsigned long long* stat) {
+    uint32_t done = 0;
+    persistent_closest(S, queue, *count, ray_o, ray_d, out_t, out_id, fetch_ctr, done);
+    warp_add(stat, done);
+}
+
+// transmittance of every queued shadow ray, given the closest hit of its first
+// segment; refracted continuations (dielectric chains) are traced inline.
+__global__ void __launch_bounds__(kThreads, 4) k_shadow_rest(DScene S, DPaths P, int kmax) {
+    const uint32_t n = P.cnt[2];
+    uint32_t segs = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t e = P.sq[i];
+        const float4 o = P.sh_o[e], d = P.sh_d[e];
+        const HitRec first{P.sh_hit_t[e], P.sh_hit_id[e]};
+        const V3 tr = transmittance_from(S, v3(o), v3(d), o.w, kmax, first, segs, true);
+        P.sh_tr[e] = f4(tr, 0.0f);
+    }
+    warp_add(P.stat + 1, segs);
+}
+
 // NEE terms in the reference order (light, env, HDRI), then the sample's
 // radiance for paths that ended (shaders/PathTrace.slang:6341-6520, 7701).
 __global__ void k_resolve(DFrame F, DPaths P, int qsel) {
@@ -736,7 +764,8 @@ struct pt_gpu_ctx {
     size_t cap = 0;
     DBuf<float4> ray_o, ray_d, thr, rad, fsum, sh_o, sh_d, sh_pre, sh_brdf, sh_tr;
     DBuf<uint32_t> seed, state, hit_id, shmask, q0, q1, sq, cnt;
-    DBuf<float> hit_t;
+    DBuf<float> hit_t, sh_hit_t;
+    DBuf<uint32_t> sh_hit_id;
     DBuf<unsigned long long> stat;
     uint32_t wave_frames_override = 0;
     // wide SAH trees built on the device at upload
@@ -891,6 +920,8 @@ int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     rc |= dalloc(ctx, ctx->sh_pre, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_brdf, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_tr, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_hit_t, 3 * npaths);
+    rc |= dalloc(ctx, ctx->sh_hit_id, 3 * npaths);
     if (rc) return PT_ERR_OOM;
     ctx->cap = npaths;
     return PT_OK;
@@ -1119,7 +1150,7 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
     CK(cudaEventCreate(&ctx->ev1));
     int rc = dalloc(ctx, ctx->err_word, 1);
     if (rc) { *out = ctx; return rc; }
-    rc = dalloc(ctx, ctx->cnt, 4);
+    rc = dalloc(ctx, ctx->cnt, 8);
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->stat, 4);
     if (rc) { *out = ctx; return rc; }
@@ -1145,6 +1176,8 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     for (auto* b : {&ctx->a4, &ctx->a4_geo, &ctx->t4, &ctx->tri4, &ctx->tri_lo, &ctx->tri_hi}) dfree(*b);
     dfree(ctx->a4_meta);
     dfree(ctx->hit_t);
+    dfree(ctx->sh_hit_t);
+    dfree(ctx->sh_hit_id);
     dfree(ctx->stat);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -1382,6 +1415,11 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
     P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
     P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
     P.q[0] = ctx->q0.p; P.q[1] = ctx->q1.p; P.sq = ctx->sq.p; P.cnt = ctx->cnt.p; P.stat = ctx->stat.p;
+    P.sh_hit_t = ctx->sh_hit_t.p; P.sh_hit_id = ctx->sh_hit_id.p;
+    // persistent wide-tree kernels need both wide trees (or no such part)
+    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
+                            (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
+    const int gpers = ctx->sm_count * 4;
 
     CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
@@ -1403,15 +1441,28 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
                 CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
                 const int ge = grid_for(ctx, npaths, 8);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                if (S.use_wide) k_extend<true><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
-                else k_extend<false><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                if (persistent) {
+                    CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
+                    k_closest<<<gpers, kThreads, 0, ctx->stream>>>(S, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
+                                                                   P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                } else if (S.use_wide) {
+                    k_extend<true><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                } else {
+                    k_extend<false><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                if (S.use_wide)
+                if (persistent) {
+                    CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
+                    k_closest<<<gpers, kThreads, 0, ctx->stream>>>(S, P.sq, P.cnt + 2, P.sh_o, P.sh_d, P.sh_hit_t,
+                                                                   P.sh_hit_id, P.cnt + 3, P.stat + 1);
+                    k_shadow_rest<<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
-                else
+                } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 k_resolve<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, qs);
                 ctx->stats.extend_launches++;

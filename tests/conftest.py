@@ -110,3 +110,62 @@ def xorshift_rays(n, seed):
         ro[i, :3] = o
         rd[i, :3] = d * inv
     return ro, rd
+
+
+def reference_ranks(nodes, n_slots):
+    """Visit ordinal of every leaf slot in the reference traversal: depth first,
+    right child popped first (shaders/PathTrace.slang:2592-2636)."""
+    rank = np.full(n_slots, -1, np.int64)
+    st, o = [0], 0
+    while st:
+        i = st.pop()
+        lf, cnt = int(nodes[i][3]), int(nodes[i][7])
+        if cnt > 0:
+            rank[lf:lf + cnt] = np.arange(o, o + cnt)
+            o += cnt
+        else:
+            st += [lf, lf + 1]
+    return rank
+
+
+def mt_all(e1, e2, v0, o, d):
+    """Two-sided Moller-Trumbore of one ray against every triangle, float32,
+    the shader's operation order (shaders/PathTrace.slang:2610-2627)."""
+    f = np.float32
+    pv = np.stack([d[1] * e2[:, 2] - d[2] * e2[:, 1], d[2] * e2[:, 0] - d[0] * e2[:, 2],
+                   d[0] * e2[:, 1] - d[1] * e2[:, 0]], 1).astype(f)
+    det = ((e1[:, 0] * pv[:, 0] + e1[:, 1] * pv[:, 1]) + e1[:, 2] * pv[:, 2]).astype(f)
+    ok = np.abs(det) >= f(1e-8)
+    inv = (f(1) / np.where(ok, det, f(1))).astype(f)
+    tv = (o - v0).astype(f)
+    u = (((tv[:, 0] * pv[:, 0] + tv[:, 1] * pv[:, 1]) + tv[:, 2] * pv[:, 2]) * inv).astype(f)
+    qv = np.stack([tv[:, 1] * e1[:, 2] - tv[:, 2] * e1[:, 1], tv[:, 2] * e1[:, 0] - tv[:, 0] * e1[:, 2],
+                   tv[:, 0] * e1[:, 1] - tv[:, 1] * e1[:, 0]], 1).astype(f)
+    v = (((d[0] * qv[:, 0] + d[1] * qv[:, 1]) + d[2] * qv[:, 2]) * inv).astype(f)
+    t = (((e2[:, 0] * qv[:, 0] + e2[:, 1] * qv[:, 1]) + e2[:, 2] * qv[:, 2]) * inv).astype(f)
+    ok &= (u >= 0) & (u <= 1) & (v >= 0) & (u + v <= 1) & (t > f(1e-3))
+    return ok, t
+
+
+def first_tested_wins(arrays, ro, rd):
+    """The reference's closest-hit rule over EVERY triangle its intersector
+    accepts: smallest t, ties to the earliest in the reference traversal order.
+    Returns hit ids in the pt_gpu_trace_closest encoding, and t."""
+    pos, idx = arrays["positions"], arrays["indices"]
+    perm = arrays["tri_perm"]
+    rank_slot = reference_ranks(arrays["tri_bvh"], perm.size)
+    rank = np.full(idx.shape[0], np.iinfo(np.int64).max)
+    rank[perm] = rank_slot
+    v0 = pos[idx[:, 0]]
+    e1 = (pos[idx[:, 1]] - v0).astype(np.float32)
+    e2 = (pos[idx[:, 2]] - v0).astype(np.float32)
+    hit = np.full(ro.shape[0], 0xFFFFFFFF, np.uint32)
+    tout = np.zeros(ro.shape[0], np.float32)
+    for i in range(ro.shape[0]):
+        ok, t = mt_all(e1, e2, v0, ro[i, :3], rd[i, :3])
+        if ok.any():
+            tm = t[ok].min()
+            cand = np.flatnonzero(ok & (t == tm))
+            hit[i] = (1 << 30) | int(cand[np.argmin(rank[cand])])
+            tout[i] = tm
+    return hit, tout

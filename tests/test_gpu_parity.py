@@ -5,7 +5,7 @@ hit ids and t, identical accumulation buffers."""
 import numpy as np
 import pytest
 
-from conftest import xorshift_rays, xorshift_spheres
+from conftest import first_tested_wins, xorshift_rays, xorshift_spheres
 
 pytestmark = pytest.mark.gpu
 
@@ -99,23 +99,21 @@ def test_trace_shared_vertex_ties_reference_walk_is_bit_exact(pt, orc, dev):
 
 
 def test_trace_shared_vertex_ties_wide_tree(pt, orc, dev):
-    """On the wide tree the reference rank resolves exact ties; the only
-    possible difference is a triangle the reference's own boxes cull by a
-    rounding of its slab test at the shared vertex (the wide tree's boxes are
-    padded and never cull a true hit)."""
+    """Equal distances on several triangles are resolved by the reference rank:
+    the wide tree returns exactly the reference's first-tested-wins result over
+    every triangle the reference intersector accepts.  (The reference walk itself
+    can additionally lose a triangle whose box the ray only touches at a corner,
+    where its unpadded slab test rounds tmax below tmin; the wide tree's padded
+    boxes never cull a true hit, so those rays legitimately differ from the
+    reference walk and the test compares against the brute-force rule.)"""
     s, xs = grid_mesh_scene(pt)
-    ro, rd = vertex_rays(xs, 4000, 9)
+    ro, rd = vertex_rays(xs, 1500, 9)
     dev.set_traversal(0)
     dev.upload(s)
-    head, prm = s.push(8, 8)
     g_hit, g_t = dev.trace(ro, rd)
-    o_hit, o_t, _ = orc.trace(s.packed(), head, prm, ro, rd)
-    # a ray aimed exactly at a vertex may fall through the crack between the
-    # triangles' strict barycentric bounds: then both walks report a miss
-    both = (g_hit != 0xFFFFFFFF) & (o_hit != 0xFFFFFFFF)
-    assert both.mean() > 0.9
-    np.testing.assert_allclose(g_t[both], o_t[both], rtol=1e-6)
-    assert (g_hit == o_hit).mean() >= 0.99
+    want_hit, want_t = first_tested_wins(s.arrays(), ro, rd)
+    np.testing.assert_array_equal(g_hit, want_hit)
+    np.testing.assert_array_equal(g_t, want_t)
 
 
 def test_trace_full_c1_rays_agreement(pt, orc, dev):
