@@ -251,7 +251,7 @@ def main():
         ext_ms += st.extend_ms
         sh_ms += st.shadow_ms
         ext_launch += st.extend_launches
-        launches += st.waves * (2 + head.spp) + 4 * st.extend_launches
+        launches += st.kernel_launches
     t_wall = time.perf_counter() - t0
     barrier()
     clk = clocks.stop()

@@ -56,7 +56,8 @@ class PtStats(ctypes.Structure):
     _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
                 ("paths", ctypes.c_uint64), ("frames", u32), ("waves", u32), ("gpu_ms", ctypes.c_double),
                 ("extend_ms", ctypes.c_double), ("shadow_ms", ctypes.c_double),
-                ("extend_launches", u32), ("shadow_launches", u32)]
+                ("extend_launches", u32), ("shadow_launches", u32), ("kernel_launches", u32),
+                ("reserved", u32)]
 
 
 class PtAccelInfo(ctypes.Structure):

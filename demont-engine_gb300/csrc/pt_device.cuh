@@ -686,9 +686,20 @@ __device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t
 // ---------------------------------------------------------------------------
 constexpr int kPStack = 64;
 
+// Shadow-ray state kept by the lane across the segments of one transmittance
+// chain (shaders/PathTrace.slang:5116-5194).
+struct ShadowIO {
+    float4* sh_o;       // origin + t_max (updated per segment)
+    float4* sh_d;       // direction (w: NEE factor, kept)
+    float4* sh_tr;      // transmittance result
+    int kmax;
+};
+
+template <bool kShadow>
 __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32_t* queue, uint32_t n,
                                                    const float4* ray_o, const float4* ray_d, float* out_t,
-                                                   uint32_t* out_id, uint32_t* fetch_ctr, uint32_t& done) {
+                                                   uint32_t* out_id, uint32_t* fetch_ctr, uint32_t& done,
+                                                   const ShadowIO& io) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const bool has_a = S.a_wide && S.prim_count > S.linear_count;
@@ -701,6 +712,44 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
     Best b{1e30f, 0u, kMiss};
     uint32_t st_code[kPStack];
     float st_t[kPStack];
+    // transmittance chain state (kShadow)
+    V3 trans = v3(1.0f, 1.0f, 1.0f);
+    float t_max = 0.0f;
+    int seg = 0;
+
+    auto start_segment = [&]() {
+        inv = safe_inv(rd);
+        nx = -ro.x * inv.x;
+        ny = -ro.y * inv.y;
+        nz = -ro.z * inv.z;
+        b = Best{1e30f, 0u, kMiss};
+        for (uint32_t i = 0; i < S.linear_count; ++i) {
+            const float t = isect_geo(__ldg(S.prim_type + i), __ldg(S.prim_geo + i), ro, rd);
+            if (t > 1e-3f && better(t, i, b)) {
+                b.t = t;
+                b.key = i;
+                b.id = i;
+            }
+        }
+        sp = 0;
+        leaf = 0u;
+        iters = 0;
+        if (has_a) {
+            phase = 1;
+            st_code[0] = 0u;
+            st_t[0] = -3.0e38f;
+            sp = 1;
+        } else {
+            phase = 2;
+            if (has_t) {
+                st_code[0] = 0u;
+                st_t[0] = -3.0e38f;
+                sp = 1;
+            }
+        }
+        ++done;
+    };
+
     for (;;) {
         const bool need = !active && !exhausted;
         const uint32_t m = __ballot_sync(FULL, need);
@@ -718,35 +767,12 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
                     const float4 o = ray_o[item], d = ray_d[item];
                     ro = v3(o);
                     rd = v3(d);
-                    inv = safe_inv(rd);
-                    nx = -ro.x * inv.x;
-                    ny = -ro.y * inv.y;
-                    nz = -ro.z * inv.z;
-                    b = Best{1e30f, 0u, kMiss};
-                    for (uint32_t i = 0; i < S.linear_count; ++i) {
-                        const float t = isect_geo(__ldg(S.prim_type + i), __ldg(S.prim_geo + i), ro, rd);
-                        if (t > 1e-3f && better(t, i, b)) {
-                            b.t = t;
-                            b.key = i;
-                            b.id = i;
-                        }
+                    if (kShadow) {
+                        t_max = o.w;
+                        trans = v3(1.0f, 1.0f, 1.0f);
+                        seg = 0;
                     }
-                    sp = 0;
-                    leaf = 0u;
-                    iters = 0;
-                    if (has_a) {
-                        phase = 1;
-                        st_code[0] = 0u;
-                        st_t[0] = -3.0e38f;
-                        sp = 1;
-                    } else {
-                        phase = 2;
-                        if (has_t) {
-                            st_code[0] = 0u;
-                            st_t[0] = -3.0e38f;
-                            sp = 1;
-                        }
-                    }
+                    start_segment();
                     active = true;
                 }
             }
@@ -828,11 +854,45 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
                 st_code[0] = 0u;
                 st_t[0] = -3.0e38f;
                 sp = 1;
-            } else {
+            } else if (!kShadow) {
                 out_t[item] = b.t;
                 out_id[item] = b.id;
                 active = false;
-                ++done;
+            } else {
+                // transmittance: unoccluded, blocked, or refract and trace the next segment
+                bool finished = true;
+                if (!(b.id == kMiss || b.t >= t_max)) {
+                    const Surface sf = surface_at(S, ro, rd, HitRec{b.t, b.id});
+                    bool zero = (sf.mat != kMatDielectric) || (seg == io.kmax);
+                    if (!zero) {
+                        const float ndi = dot(sf.normal, rd);
+                        const V3 nf = (ndi < 0.0f) ? sf.normal : -sf.normal;
+                        const float ia = (ndi < 0.0f) ? 1.0f : sf.ior;
+                        const float ib = (ndi < 0.0f) ? sf.ior : 1.0f;
+                        const float eta = ia / ib;
+                        const float cos_i = fabsf(dot(nf, -rd));
+                        const float r0 = ((ia - ib) / (ia + ib)) * ((ia - ib) / (ia + ib));
+                        const float fr = schlick(cos_i, r0);
+                        const V3 refr = refract(rd, nf, eta);
+                        if (length(refr) < 1e-3f) {
+                            zero = true;
+                        } else {
+                            trans = trans * ((1.0f - fr) * sf.albedo);
+                            const float adv = b.t + 1e-3f;
+                            ro = ro + rd * adv;
+                            rd = normalize(refr);
+                            t_max = fmaxf(t_max - adv, 0.0f);
+                            ++seg;
+                            start_segment();
+                            finished = false;
+                        }
+                    }
+                    if (zero) trans = v3(0.0f, 0.0f, 0.0f);
+                }
+                if (finished) {
+                    io.sh_tr[item] = f4(trans, 0.0f);
+                    active = false;
+                }
             }
         }
     }

@@ -634,8 +634,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_closest(DScene S, const uint32_
                                                          const float4* ray_d, float* out_t, uint32_t* out_id,
                                                          uint32_t* fetch_ctr, unsigned long long* stat) {
     uint32_t done = 0;
-    persistent_closest(S, queue, *count, ray_o, ray_d, out_t, out_id, fetch_ctr, done);
+    persistent_closest<false>(S, queue, *count, ray_o, ray_d, out_t, out_id, fetch_ctr, done, ShadowIO{});
     warp_add(stat, done);
+}
+
+// persistent transmittance: whole dielectric chains per lane (every segment
+// counted as a shadow segment)
+__global__ void __launch_bounds__(kThreads, 4) k_transmit(DScene S, DPaths P, int kmax) {
+    uint32_t done = 0;
+    const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax};
+    persistent_closest<true>(S, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr, nullptr, P.cnt + 3, done, io);
+    warp_add(P.stat + 1, done);
 }
 
 // transmittance of every queued shadow ray, given the closest hit of its first
@@ -1492,8 +1501,10 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
         F.frame_index0 = head->frame_index + f0;
         const int gp = (npaths + 255) / 256;
         k_init_wave<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, head->frame_index + f0);
+        ctx->stats.kernel_launches += 2;   // init + accumulate
         for (uint32_t s = 0; s < F.spp; ++s) {
             k_camera<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, s);
+            ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const int qs = int(b & 1u);
                 CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
@@ -1513,21 +1524,8 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
                 k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 if (persistent) {
-                    // transmittance, one segment per pass over a shrinking queue
-                    const uint32_t* qin = P.sq;
-                    uint32_t* nin = P.cnt + 2;
-                    for (int seg = 0; seg <= F.kmax; ++seg) {
-                        uint32_t* qout = (seg & 1) ? P.sq2b : P.sq2;
-                        uint32_t* nout = P.cnt + 4 + (seg & 1);
-                        CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
-                        CK(cudaMemsetAsync(nout, 0, 4, ctx->stream));
-                        k_closest<<<gpers, kThreads, 0, ctx->stream>>>(S, qin, nin, P.sh_o, P.sh_d, P.sh_hit_t,
-                                                                       P.sh_hit_id, P.cnt + 3, P.stat + 1);
-                        k_shadow_step<<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(
-                            S, P, F.kmax, seg, qin, nin, qout, nout);
-                        qin = qout;
-                        nin = nout;
-                    }
+                    CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
+                    k_transmit<<<gpers, kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {

@@ -102,6 +102,8 @@ typedef struct PtStats {
     double   shadow_ms;       /* device time inside the transmittance kernel */
     uint32_t extend_launches;
     uint32_t shadow_launches;
+    uint32_t kernel_launches; /* every kernel this render call launched */
+    uint32_t reserved;
 } PtStats;
 
 /* ---- lifecycle (replaces Device::Create(BackendType), src/rhi/Device.cpp:20-48) ---- */
