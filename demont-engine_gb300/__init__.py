@@ -105,6 +105,8 @@ SIGNATURES = {
     "pt_gpu_set_wave_frames": (ctypes.c_int, [ctypes.c_void_p, u32]),
     "pt_gpu_set_traversal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_get_accel_info": (ctypes.c_int, [ctypes.c_void_p, P(PtAccelInfo)]),
+    "pt_gpu_render_noalloc": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32, u32, u32,
+                                             ctypes.c_void_p]),
     "pt_gpu_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     # pt_scene.h

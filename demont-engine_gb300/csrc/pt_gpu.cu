@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -1658,3 +1659,222 @@ int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free render: pt_gpu_render_noalloc
+//
+// Some callers of this library must not allocate device memory while they
+// render: an engine that reserved its whole device-memory budget up front and
+// treats any later cudaMalloc as a budget violation, a real-time frame loop in
+// which cudaMalloc/cudaFree can stall on an implicit device synchronisation,
+// or a plugin hosted by an application whose own allocator accounts for every
+// device byte.  For them this entry point renders with no allocation at all:
+// the per-wave path state lives in one file-scope device array of fixed size,
+// the caller passes its own accumulation buffer, and nothing here calls
+// cudaMalloc, cudaFree or an allocating library routine.
+//
+// Limits and sharing rules:
+//   - at most kNoAllocMaxPixels pixels per frame (256 x 256); larger frames are
+//     rejected with PT_ERR_INVALID;
+//   - the array (kNoAllocBytes, about 24 MB) is held by every GPU that loads
+//     the library until the process exits;
+//   - every call on a device uses the same array and leaves its contents
+//     behind; what must start at zero (queue counters, statistics) is cleared
+//     by each call, the rest is written before it is read;
+//   - calls that overlap on the same GPU (two contexts, or concurrent threads)
+//     race on the array and must be serialised by the caller;
+//   - the first call on a device resolves the array's device address with
+//     cudaGetSymbolAddress (that device made current for the call); make this
+//     first call before any stream capture.
+// ===========================================================================
+namespace {
+
+constexpr uint32_t kNoAllocMaxPixels = 65536u;
+constexpr size_t kNoAllocAlign = 256;
+constexpr size_t align_up(size_t v) { return (v + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+constexpr size_t kNA_P = kNoAllocMaxPixels;
+// 5 float4 path arrays, 5 float4 x 3 shadow slots, 7 u32 path arrays, 1 u32 x 3 shadow queue,
+// 8 u32 counters, 4 u64 statistics
+constexpr size_t kNoAllocBytes = 5 * align_up(16 * kNA_P) + 5 * align_up(16 * 3 * kNA_P) +
+                                 7 * align_up(4 * kNA_P) + align_up(4 * 3 * kNA_P) + align_up(32) +
+                                 align_up(32);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 64;
+unsigned char* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on ctx's device (resolved once per device).
+int noalloc_base(pt_gpu_ctx* ctx, unsigned char** out) {
+    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+        return set_err(ctx, PT_ERR_INVALID, "render_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[ctx->device]) {
+        int prev = 0;
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e == cudaSuccess) e = cudaSetDevice(ctx->device);
+        void* p = nullptr;
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaSetDevice(prev);
+        if (e != cudaSuccess || !p)
+            return set_err(ctx, PT_ERR_CUDA, std::string("render_noalloc: cudaGetSymbolAddress: ") +
+                                                 cudaGetErrorString(e));
+        g_noalloc_base[ctx->device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_base[ctx->device];
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm,
+                                     uint32_t width, uint32_t height, uint32_t frames, float* accum_device) {
+    if (!ctx || !head || !prm || !accum_device) return PT_ERR_INVALID;
+    if (width == 0 || height == 0) return set_err(ctx, PT_ERR_INVALID, "render_noalloc: empty frame");
+    if (uint64_t(width) * height > kNoAllocMaxPixels)
+        return set_err(ctx, PT_ERR_INVALID,
+                       "render_noalloc: " + std::to_string(uint64_t(width) * height) +
+                           " pixels exceed the static scratch limit of " + std::to_string(kNoAllocMaxPixels) +
+                           " pixels per frame");
+    if ((reinterpret_cast<uintptr_t>(accum_device) & 15u) != 0)
+        return set_err(ctx, PT_ERR_INVALID, "render_noalloc: accumulation buffer must be 16-byte aligned");
+    if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: tlas_present has no CUDA path");
+    if (prm->light_tree_enabled) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: light tree not built");
+    if (!head->env_map_present)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: procedural sky modes (no env map) not built");
+    if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
+        (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))
+        return set_err(ctx, PT_ERR_INVALID, "render_noalloc: prim_count / bvh_params disagree with the uploaded prims");
+    if (prm->bvh_params[2] != 0u && prm->bvh_params[3] != 0u && prm->bvh_params[3] != ctx->tri_nodes)
+        return set_err(ctx, PT_ERR_INVALID, "render_noalloc: bvh_params.w disagrees with the uploaded mesh BVH");
+    if (prm->light_count > ctx->light_count)
+        return set_err(ctx, PT_ERR_INVALID, "render_noalloc: light_count exceeds the uploaded lights");
+    if (ctx->env_w == 0 || ctx->env_h == 0) return set_err(ctx, PT_ERR_STATE, "render_noalloc: env map not uploaded");
+    if (frames == 0) return PT_OK;
+    unsigned char* base = nullptr;
+    if (int rc = noalloc_base(ctx, &base)) return rc;
+
+    // carve the path state out of the static array
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char* p = base + off;
+        off += align_up(bytes);
+        return p;
+    };
+    DPaths P{};
+    P.ray_o = reinterpret_cast<float4*>(take(16 * kNA_P));
+    P.ray_d = reinterpret_cast<float4*>(take(16 * kNA_P));
+    P.thr = reinterpret_cast<float4*>(take(16 * kNA_P));
+    P.rad = reinterpret_cast<float4*>(take(16 * kNA_P));
+    P.fsum = reinterpret_cast<float4*>(take(16 * kNA_P));
+    P.sh_o = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
+    P.sh_d = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
+    P.sh_pre = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
+    P.sh_brdf = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
+    P.sh_tr = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
+    P.seed = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
+    P.state = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
+    P.hit_t = reinterpret_cast<float*>(take(4 * kNA_P));
+    P.hit_id = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
+    P.shmask = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
+    P.q[0] = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
+    P.q[1] = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
+    P.sq = reinterpret_cast<uint32_t*>(take(4 * 3 * kNA_P));
+    P.cnt = reinterpret_cast<uint32_t*>(take(32));
+    P.stat = reinterpret_cast<unsigned long long*>(take(32));
+    if (off > kNoAllocBytes) return set_err(ctx, PT_ERR_KERNEL, "render_noalloc: scratch layout overflow");
+
+    DFrame F{};
+    F.cam_pos = v3(head->pos_fovtan[0], head->pos_fovtan[1], head->pos_fovtan[2]);
+    F.tanf = head->pos_fovtan[3];
+    F.fwd = v3(head->fwd_aspect[0], head->fwd_aspect[1], head->fwd_aspect[2]);
+    F.aspect = head->fwd_aspect[3];
+    F.right = v3(head->right_xyz[0], head->right_xyz[1], head->right_xyz[2]);
+    F.up = v3(head->up_xyz[0], head->up_xyz[1], head->up_xyz[2]);
+    F.W = width;
+    F.H = height;
+    F.npix = width * height;
+    F.spp = head->spp == 0u ? 1u : head->spp;
+    F.maxb = head->max_bounces;
+    F.denoiser = head->denoiser_enabled;
+    F.jx = head->halton_jitter[0];
+    F.jy = head->halton_jitter[1];
+    F.env_present = head->env_map_present;
+    F.env_intensity = head->env_intensity;
+    F.env_total = head->env_total_luminance;
+    F.kmax = int(prm->refract_budget);
+    F.firefly = prm->firefly_clamp;
+    F.mis = prm->mis_enabled;
+    F.rr_start = prm->rr_start;
+    F.light_count = prm->light_count;
+    const DScene S = make_scene(ctx, prm);
+    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
+                            (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
+    const int gpers = ctx->sm_count * 4;
+    const uint32_t fpw = std::max<uint32_t>(1u, std::min<uint32_t>(frames, kNoAllocMaxPixels / F.npix));
+    float4* accum = reinterpret_cast<float4*>(accum_device);
+
+    CK(cudaMemsetAsync(P.stat, 0, 32, ctx->stream));
+    CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
+    ctx->stats = PtStats{};
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
+        const uint32_t nf = std::min(fpw, frames - f0);
+        const uint32_t npaths = nf * F.npix;
+        F.nframes = nf;
+        F.frame_index0 = head->frame_index + f0;
+        const int gp = (npaths + 255) / 256;
+        k_init_wave<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, head->frame_index + f0);
+        ctx->stats.kernel_launches += 2;
+        for (uint32_t s = 0; s < F.spp; ++s) {
+            k_camera<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, s);
+            ctx->stats.kernel_launches += 1 + 4 * F.maxb;
+            for (uint32_t b = 0; b < F.maxb; ++b) {
+                const int qs = int(b & 1u);
+                CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
+                CK(cudaMemsetAsync(P.cnt + 2, 0, 4, ctx->stream));
+                if (persistent) {
+                    CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
+                    k_closest<<<gpers, kThreads, 0, ctx->stream>>>(S, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
+                                                                   P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                } else if (S.use_wide) {
+                    k_extend<true><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
+                } else {
+                    k_extend<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
+                }
+                k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
+                if (persistent) {
+                    CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
+                    k_transmit<<<gpers, kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                } else if (S.use_wide) {
+                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                } else {
+                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                }
+                k_resolve<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, qs);
+                ctx->stats.extend_launches++;
+                ctx->stats.shadow_launches++;
+            }
+        }
+        k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, accum, nf,
+                                                                   f0 == 0 && head->reset_accum != 0u, prm->accum_ema_alpha);
+        ctx->stats.waves++;
+        ctx->stats.paths += uint64_t(npaths) * F.spp;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.gpu_ms = ms;
+    ctx->stats.frames = frames;
+    unsigned long long st[4];
+    uint32_t errw = 0;
+    CK(cudaMemcpy(st, P.stat, sizeof(st), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
+    ctx->stats.extension_rays = st[0];
+    ctx->stats.shadow_rays = st[1];
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "render_noalloc: traversal iteration cap reached");
+    return PT_OK;
+}

@@ -200,6 +200,27 @@ int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out);
  * frame size so a wave holds about 16 M paths). 0 restores the default. */
 int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave);
 
+/* ---- allocation-free render (no counterpart in the reference) ----
+ * For callers that must not allocate device memory while rendering: an engine
+ * that reserved its whole device budget up front, a frame loop that cannot
+ * afford the implicit synchronisation cudaMalloc/cudaFree may cause, or a
+ * plugin whose host application accounts for every device byte.  Same result
+ * as pt_gpu_render on the same inputs, but the per-wave path state lives in a
+ * fixed file-scope device array inside the library and the caller passes its
+ * own accumulation buffer: accum_device = width*height*4 floats of DEVICE
+ * memory, 16-byte aligned, read and updated in place (.a = frame count).
+ * Nothing in this call allocates (no cudaMalloc, cudaFree or allocating
+ * library routine).  The scene must have been uploaded to ctx beforehand.
+ * Limits: width*height <= 65536 pixels (e.g. 256 x 256); larger frames return
+ * PT_ERR_INVALID.  The array (about 22.5 MiB) is held by every GPU that loads
+ * the library until the process exits.  All calls on a device share it and it
+ * keeps the last call's contents (each call clears what must start at zero);
+ * calls that overlap on the same GPU race and must be serialised.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress
+ * with that device current): make that first call before any stream capture. */
+int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
+                          uint32_t width, uint32_t height, uint32_t frames, float* accum_device);
+
 /* ---- parity probe: traceScene for arbitrary rays (shaders/PathTrace.slang:2331-2693) ----
  * ray_o: n float4 (origin xyz, w unused); ray_d: n float4 (direction xyz,
  * w = initial closest distance; <= 0 means the reference's 1e30).
