@@ -72,11 +72,7 @@ struct DPaths {
     float4* sh_tr;     // transmittance result
     uint32_t* q[2];
     uint32_t* sq;
-    uint32_t* sq2;     // shadow continuation queue (ping-pong with sq2b)
-    uint32_t* sq2b;
-    uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue, [3] fetch counter, [4],[5] continuation queues
-    float* sh_hit_t;   // 3 per path: closest hit of the first shadow segment
-    uint32_t* sh_hit_id;
+    uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue, [3] fetch counter
     unsigned long long* stat;   // [0] extension rays, [1] shadow segments
 };
 
@@ -648,74 +644,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_transmit(DScene S, DPaths P, in
     warp_add(P.stat + 1, done);
 }
 
-// transmittance of every queued shadow ray, given the closest hit of its first
-// segment; refracted continuations (dielectric chains) are traced inline.
-__global__ void __launch_bounds__(kThreads, 4) k_shadow_rest(DScene S, DPaths P, int kmax) {
-    const uint32_t n = P.cnt[2];
-    uint32_t segs = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t e = P.sq[i];
-        const float4 o = P.sh_o[e], d = P.sh_d[e];
-        const HitRec first{P.sh_hit_t[e], P.sh_hit_id[e]};
-        const V3 tr = transmittance_from(S, v3(o), v3(d), o.w, kmax, first, segs, true);
-        P.sh_tr[e] = f4(tr, 0.0f);
-    }
-    warp_add(P.stat + 1, segs);
-}
-
-
-// One segment of transmittance (shaders/PathTrace.slang:5116-5194) for every
-// queued shadow ray, given that segment's closest hit: the ray ends (miss or
-// past t_max: transmittance kept; opaque, budget or TIR: 0), or refracts
-// through the dielectric and is queued for the next segment.
-__global__ void k_shadow_step(DScene S, DPaths P, int kmax, int seg, const uint32_t* qin, const uint32_t* nin,
-                              uint32_t* qout, uint32_t* nout) {
-    const uint32_t n = *nin;
-    const uint32_t iters = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
-    for (uint32_t it = 0; it < iters; ++it) {
-        const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        bool cont = false;
-        uint32_t e = 0;
-        if (i < n) {
-            e = qin[i];
-            const float4 o4 = P.sh_o[e], d4 = P.sh_d[e];
-            const HitRec h{P.sh_hit_t[e], P.sh_hit_id[e]};
-            const float t_max = o4.w;
-            if (!(h.id == kMiss || h.t >= t_max)) {
-                const V3 o = v3(o4), d = v3(d4);
-                const Surface sf = surface_at(S, o, d, h);
-                bool zero = (sf.mat != kMatDielectric) || (seg == kmax);
-                V3 refr = v3(0.0f, 0.0f, 0.0f);
-                float fr = 0.0f;
-                if (!zero) {
-                    const float ndi = dot(sf.normal, d);
-                    const V3 nf = (ndi < 0.0f) ? sf.normal : -sf.normal;
-                    const float ia = (ndi < 0.0f) ? 1.0f : sf.ior;
-                    const float ib = (ndi < 0.0f) ? sf.ior : 1.0f;
-                    const float eta = ia / ib;
-                    const float cos_i = fabsf(dot(nf, -d));
-                    const float r0 = ((ia - ib) / (ia + ib)) * ((ia - ib) / (ia + ib));
-                    fr = schlick(cos_i, r0);
-                    refr = refract(d, nf, eta);
-                    if (length(refr) < 1e-3f) zero = true;
-                }
-                if (zero) {
-                    P.sh_tr[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                } else {
-                    const V3 t = v3(P.sh_tr[e]) * ((1.0f - fr) * sf.albedo);
-                    const float adv = h.t + 1e-3f;
-                    P.sh_tr[e] = f4(t, 0.0f);
-                    P.sh_o[e] = f4(o + d * adv, fmaxf(t_max - adv, 0.0f));
-                    P.sh_d[e] = f4(normalize(refr), d4.w);
-                    cont = true;
-                }
-            }
-        }
-        const uint32_t slot = warp_push(nout, cont);
-        if (cont) qout[slot] = e;
-    }
-}
-
 // NEE terms in the reference order (light, env, HDRI), then the sample's
 // radiance for paths that ended (shaders/PathTrace.slang:6341-6520, 7701).
 __global__ void k_resolve(DFrame F, DPaths P, int qsel) {
@@ -829,9 +757,8 @@ struct pt_gpu_ctx {
     // wave buffers
     size_t cap = 0;
     DBuf<float4> ray_o, ray_d, thr, rad, fsum, sh_o, sh_d, sh_pre, sh_brdf, sh_tr;
-    DBuf<uint32_t> seed, state, hit_id, shmask, q0, q1, sq, sq2, sq2b, cnt;
-    DBuf<float> hit_t, sh_hit_t;
-    DBuf<uint32_t> sh_hit_id;
+    DBuf<uint32_t> seed, state, hit_id, shmask, q0, q1, sq, cnt;
+    DBuf<float> hit_t;
     DBuf<unsigned long long> stat;
     uint32_t wave_frames_override = 0;
     // wide SAH trees built on the device at upload
@@ -981,15 +908,13 @@ int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     rc |= dalloc(ctx, ctx->q0, npaths);
     rc |= dalloc(ctx, ctx->q1, npaths);
     rc |= dalloc(ctx, ctx->sq, 3 * npaths);
-    rc |= dalloc(ctx, ctx->sq2, 3 * npaths);
-    rc |= dalloc(ctx, ctx->sq2b, 3 * npaths);
+
     rc |= dalloc(ctx, ctx->sh_o, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_d, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_pre, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_brdf, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_tr, 3 * npaths);
-    rc |= dalloc(ctx, ctx->sh_hit_t, 3 * npaths);
-    rc |= dalloc(ctx, ctx->sh_hit_id, 3 * npaths);
+
     if (rc) return PT_ERR_OOM;
     ctx->cap = npaths;
     return PT_OK;
@@ -1237,15 +1162,13 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
                     &ctx->sh_tr})
         dfree(*b);
     for (auto* b : {&ctx->prim_type, &ctx->seed, &ctx->state, &ctx->hit_id, &ctx->shmask, &ctx->q0,
-                    &ctx->q1, &ctx->sq, &ctx->sq2, &ctx->sq2b, &ctx->cnt, &ctx->err_word})
+                    &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word})
         dfree(*b);
     dfree(ctx->marg);
     dfree(ctx->cond);
     for (auto* b : {&ctx->a4, &ctx->a4_geo, &ctx->t4, &ctx->tri4, &ctx->tri_lo, &ctx->tri_hi}) dfree(*b);
     dfree(ctx->a4_meta);
     dfree(ctx->hit_t);
-    dfree(ctx->sh_hit_t);
-    dfree(ctx->sh_hit_id);
     dfree(ctx->stat);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -1483,8 +1406,6 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
     P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
     P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
     P.q[0] = ctx->q0.p; P.q[1] = ctx->q1.p; P.sq = ctx->sq.p; P.cnt = ctx->cnt.p; P.stat = ctx->stat.p;
-    P.sh_hit_t = ctx->sh_hit_t.p; P.sh_hit_id = ctx->sh_hit_id.p;
-    P.sq2 = ctx->sq2.p; P.sq2b = ctx->sq2b.p;
     // persistent wide-tree kernels need both wide trees (or no such part)
     const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
