@@ -66,6 +66,16 @@ class PtAccelInfo(ctypes.Structure):
                 ("reserved", u32), ("mesh_build_ms", ctypes.c_double)]
 
 
+class PtBatchView(ctypes.Structure):
+    _fields_ = [("scene", u32), ("width", u32), ("height", u32), ("reserved", u32),
+                ("head", PtPushHead), ("params", PtPathParams)]
+
+
+class PtBatchTuning(ctypes.Structure):
+    _fields_ = [("persistent_blocks_per_sm", u32), ("stream_blocks_per_sm", u32), ("use_graph", u32),
+                ("reserved", u32)]
+
+
 class PtPackedScene(ctypes.Structure):
     _fields_ = [("prims", P(f32)), ("prim_count", u32), ("linear_prim_count", u32),
                 ("bvh_nodes", P(PtBvhNode)), ("bvh_node_count", u32),
@@ -105,6 +115,12 @@ SIGNATURES = {
     "pt_gpu_set_wave_frames": (ctypes.c_int, [ctypes.c_void_p, u32]),
     "pt_gpu_set_traversal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_get_accel_info": (ctypes.c_int, [ctypes.c_void_p, P(PtAccelInfo)]),
+    "pt_gpu_batch_render": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p), u32, P(PtBatchView), u32, u32]),
+    "pt_gpu_batch_read_accum": (ctypes.c_int, [ctypes.c_void_p, u32, P(f32)]),
+    "pt_gpu_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, P(PtBatchTuning)]),
+    "pt_gpu_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, P(PtBatchTuning)]),
+    "pt_gpu_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p), u32, P(PtBatchView), u32,
+                                             P(PtBatchTuning)]),
     "pt_gpu_render_noalloc": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32, u32, u32,
                                              ctypes.c_void_p]),
     "pt_gpu_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32,
@@ -388,6 +404,37 @@ class Device:
 
     def set_wave_frames(self, n):
         self._check(self.lib.pt_gpu_set_wave_frames(self.h, n))
+
+    # ---- batched renders ----
+    def batch_render(self, scene_devs, views, frames=1):
+        """scene_devs: list of Device (each holding an uploaded scene); views: list of
+        (scene index, width, height, head, params)."""
+        arr = (ctypes.c_void_p * len(scene_devs))(*[d.h.value if hasattr(d.h, "value") else d.h for d in scene_devs])
+        va = (PtBatchView * len(views))()
+        for i, (sc, w, h, head, prm) in enumerate(views):
+            va[i].scene, va[i].width, va[i].height = sc, w, h
+            va[i].head, va[i].params = head, prm
+        self._batch_keep = (arr, va)
+        self._check(self.lib.pt_gpu_batch_render(self.h, arr, len(scene_devs), va, len(views), frames))
+
+    def batch_read(self, view, w, h):
+        out = np.empty((h, w, 4), np.float32)
+        self._check(self.lib.pt_gpu_batch_read_accum(self.h, view, fptr(out)))
+        return out
+
+    def batch_autotune(self, scene_devs, views):
+        arr = (ctypes.c_void_p * len(scene_devs))(*[d.h.value if hasattr(d.h, "value") else d.h for d in scene_devs])
+        va = (PtBatchView * len(views))()
+        for i, (sc, w, h, head, prm) in enumerate(views):
+            va[i].scene, va[i].width, va[i].height = sc, w, h
+            va[i].head, va[i].params = head, prm
+        t = PtBatchTuning()
+        self._check(self.lib.pt_gpu_batch_autotune(self.h, arr, len(scene_devs), va, len(views), ctypes.byref(t)))
+        return t
+
+    def batch_set_tuning(self, persistent_blocks_per_sm=4, stream_blocks_per_sm=8, use_graph=1):
+        t = PtBatchTuning(persistent_blocks_per_sm, stream_blocks_per_sm, use_graph, 0)
+        self._check(self.lib.pt_gpu_batch_set_tuning(self.h, ctypes.byref(t)))
 
     def trace(self, ro4, rd4):
         ro4 = np.ascontiguousarray(ro4, np.float32)

@@ -695,18 +695,26 @@ struct ShadowIO {
     int kmax;
 };
 
-template <bool kShadow>
-__device__ __forceinline__ void persistent_closest(const DScene& S, const uint32_t* queue, uint32_t n,
-                                                   const float4* ray_o, const float4* ray_d, float* out_t,
-                                                   uint32_t* out_id, uint32_t* fetch_ctr, uint32_t& done,
-                                                   const ShadowIO& io) {
+// Batched renders: per-path scene of a queued item (extension rays: item = path;
+// shadow rays: item = 3 * path + slot).
+struct ItemScenes {
+    const DScene* table;        // device array of scene descriptors (batched renders)
+    const uint32_t* path_scene; // scene index per path
+};
+
+template <bool kShadow, bool kBatch>
+__device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes isc, const uint32_t* queue,
+                                                   uint32_t n, const float4* ray_o, const float4* ray_d,
+                                                   float* out_t, uint32_t* out_id, uint32_t* fetch_ctr,
+                                                   uint32_t& done, const ShadowIO& io) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
-    const bool has_a = S.a_wide && S.prim_count > S.linear_count;
-    const bool has_t = S.t_wide && S.tri_enabled != 0u && S.tri_nodes > 0u;
+    const DScene* Sp = S0;
+    bool has_a = false, has_t = false;
     bool active = false, exhausted = false;
     uint32_t item = 0, leaf = 0u, iters = 0;
     int phase = 0, sp = 0;
+    const float4* nodes = nullptr;
     V3 ro = v3(0.0f, 0.0f, 0.0f), rd = ro, inv = ro;
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
     Best b{1e30f, 0u, kMiss};
@@ -723,8 +731,11 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
         ny = -ro.y * inv.y;
         nz = -ro.z * inv.z;
         b = Best{1e30f, 0u, kMiss};
-        for (uint32_t i = 0; i < S.linear_count; ++i) {
-            const float t = isect_geo(__ldg(S.prim_type + i), __ldg(S.prim_geo + i), ro, rd);
+        const uint32_t linear = Sp->linear_count;
+        const float4* pg = Sp->prim_geo;
+        const uint32_t* pty = Sp->prim_type;
+        for (uint32_t i = 0; i < linear; ++i) {
+            const float t = isect_geo(__ldg(pty + i), __ldg(pg + i), ro, rd);
             if (t > 1e-3f && better(t, i, b)) {
                 b.t = t;
                 b.key = i;
@@ -736,11 +747,13 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
         iters = 0;
         if (has_a) {
             phase = 1;
+            nodes = Sp->a4;
             st_code[0] = 0u;
             st_t[0] = -3.0e38f;
             sp = 1;
         } else {
             phase = 2;
+            nodes = Sp->t4;
             if (has_t) {
                 st_code[0] = 0u;
                 st_t[0] = -3.0e38f;
@@ -764,6 +777,9 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
                     exhausted = true;
                 } else {
                     item = queue[slot];
+                    if (kBatch) Sp = isc.table + isc.path_scene[kShadow ? item / 3u : item];
+                    has_a = Sp->a_wide && Sp->prim_count > Sp->linear_count;
+                    has_t = Sp->t_wide && Sp->tri_enabled != 0u && Sp->tri_nodes > 0u;
                     const float4 o = ray_o[item], d = ray_d[item];
                     ro = v3(o);
                     rd = v3(d);
@@ -784,7 +800,7 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
             if (!__any_sync(FULL, want)) break;
             if (!want) continue;
             if (++iters > kTraverseCap) {
-                atomicOr(S.err, 1u);
+                atomicOr(Sp->err, 1u);
                 sp = 0;
                 continue;
             }
@@ -795,7 +811,7 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
                 leaf = code;
                 continue;
             }
-            const float4* nd = (phase == 1 ? S.a4 : S.t4) + 8u * code;
+            const float4* nd = nodes + 8u * code;
             const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
             const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
             const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
@@ -824,7 +840,7 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
                 }
             }
             if (sp + nh > kPStack) {
-                atomicOr(S.err, 2u);
+                atomicOr(Sp->err, 2u);
                 sp = 0;
                 continue;
             }
@@ -843,14 +859,15 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
         }
         // leaf phase
         if (active && leaf != 0u) {
-            if (phase == 1) wide_leaf<false>(S, leaf, ro, rd, b, 0u);
-            else wide_leaf<true>(S, leaf, ro, rd, b, 0x80000000u);
+            if (phase == 1) wide_leaf<false>(*Sp, leaf, ro, rd, b, 0u);
+            else wide_leaf<true>(*Sp, leaf, ro, rd, b, 0x80000000u);
             leaf = 0u;
         }
         // end of a tree
         if (active && leaf == 0u && sp == 0) {
             if (phase == 1 && has_t) {
                 phase = 2;
+                nodes = Sp->t4;
                 st_code[0] = 0u;
                 st_t[0] = -3.0e38f;
                 sp = 1;
@@ -862,7 +879,7 @@ __device__ __forceinline__ void persistent_closest(const DScene& S, const uint32
                 // transmittance: unoccluded, blocked, or refract and trace the next segment
                 bool finished = true;
                 if (!(b.id == kMiss || b.t >= t_max)) {
-                    const Surface sf = surface_at(S, ro, rd, HitRec{b.t, b.id});
+                    const Surface sf = surface_at(*Sp, ro, rd, HitRec{b.t, b.id});
                     bool zero = (sf.mat != kMatDielectric) || (seg == io.kmax);
                     if (!zero) {
                         const float ndi = dot(sf.normal, rd);

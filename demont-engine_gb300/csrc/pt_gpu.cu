@@ -52,6 +52,24 @@ struct DFrame {
     int kmax;
     float firefly;
     uint32_t mis, rr_start, light_count;
+    // batched renders: per-view fields
+    uint32_t scene;          // index into the batch's scene table
+    uint32_t slot_base;      // first path slot of the view in the wave
+    uint32_t reset;          // reset_accum of the view's first frame
+    float ema;               // accum_params.x
+    size_t accum_base;       // first texel of the view in the batch accumulation buffer
+};
+
+// Batched renders: device tables of per-view frame constants and per-scene
+// descriptors; every path records its view and scene.
+struct Batch {
+    const DFrame* views;
+    const DScene* scenes;
+    uint32_t* path_view;
+    uint32_t* path_scene;
+    const uint32_t* view_base;   // n_views + 1 slot offsets
+    float4* accum;
+    uint32_t n_views;
 };
 
 struct DPaths {
@@ -388,46 +406,79 @@ __device__ __forceinline__ void slot_pixel(const DFrame& F, uint32_t pix, uint32
     }
 }
 
-__global__ void k_init_wave(DFrame F, DPaths P, uint32_t npaths, uint32_t frame0) {
+__device__ __forceinline__ uint32_t view_of_slot(const Batch& B, uint32_t p) {
+    uint32_t lo = 0, hi = B.n_views;   // last view with view_base[v] <= p
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (B.view_base[mid] <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <bool kB>
+__global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths, uint32_t frame0) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npaths) return;
-    const uint32_t f = p / F.npix, pix = p - f * F.npix;
-    uint32_t x, y;
-    slot_pixel(F, pix, x, y);
-    P.seed[p] = pcg_hash(x * 1973u + y * 9277u + (frame0 + f) * 26699u);
+    uint32_t x, y, fidx;
+    if (kB) {
+        const uint32_t v = view_of_slot(B, p);
+        const DFrame& V = B.views[v];
+        B.path_view[p] = v;
+        B.path_scene[p] = V.scene;
+        slot_pixel(V, p - V.slot_base, x, y);
+        fidx = V.frame_index0;
+    } else {
+        const uint32_t f = p / F.npix, pix = p - f * F.npix;
+        slot_pixel(F, pix, x, y);
+        fidx = frame0 + f;
+    }
+    P.seed[p] = pcg_hash(x * 1973u + y * 9277u + fidx * 26699u);
     P.fsum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // primary rays (shaders/PathTrace.slang:5722-5778)
-__global__ void k_camera(DFrame F, DPaths P, uint32_t npaths, uint32_t s) {
+template <bool kB>
+__global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths, uint32_t s) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p == 0) P.cnt[0] = npaths;
-    if (p >= npaths) return;
-    const uint32_t f = p / F.npix, pix = p - f * F.npix;
+    if (!kB && p == 0) P.cnt[0] = npaths;
+    bool live = p < npaths;
+    const DFrame& V = (kB && live) ? B.views[B.path_view[p]] : F;
+    if (kB && live && s >= V.spp) live = false;   // this view has fewer samples
+    if (kB) {   // compacted queue (views may differ in spp)
+        const uint32_t slot = warp_push(P.cnt, live);
+        if (live) P.q[0][slot] = p;
+    }
+    if (!live) return;
     uint32_t x, y;
-    slot_pixel(F, pix, x, y);
+    if (kB) {
+        slot_pixel(V, p - V.slot_base, x, y);
+    } else {
+        const uint32_t f = p / F.npix, pix = p - f * F.npix;
+        slot_pixel(F, pix, x, y);
+    }
     uint32_t seed = P.seed[p];
     float jx, jy;
-    if (F.denoiser != 0u && s == 0u) {
-        jx = F.jx;
-        jy = F.jy;
+    if (V.denoiser != 0u && s == 0u) {
+        jx = V.jx;
+        jy = V.jy;
     } else {
         const float a = randf(seed);
         const float b = randf(seed);
         jx = a - 0.5f;
         jy = b - 0.5f;
     }
-    const float ux = ((float(x) + 0.5f + jx) / float(F.W)) * 2.0f - 1.0f;
-    float uy = ((float(y) + 0.5f + jy) / float(F.H)) * 2.0f - 1.0f;
+    const float ux = ((float(x) + 0.5f + jx) / float(V.W)) * 2.0f - 1.0f;
+    float uy = ((float(y) + 0.5f + jy) / float(V.H)) * 2.0f - 1.0f;
     uy = -uy;
-    const V3 rd = normalize(F.fwd + F.right * (ux * F.aspect * F.tanf) + F.up * (uy * F.tanf));
+    const V3 rd = normalize(V.fwd + V.right * (ux * V.aspect * V.tanf) + V.up * (uy * V.tanf));
     P.seed[p] = seed;
-    P.ray_o[p] = f4(F.cam_pos, 0.0f);
+    P.ray_o[p] = f4(V.cam_pos, 0.0f);
     P.ray_d[p] = f4(rd, 0.0f);
     P.thr[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     P.rad[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     P.state[p] = 0u;
-    P.q[0][p] = p;
+    if (!kB) P.q[0][p] = p;
 }
 
 template <bool kWide>
@@ -459,7 +510,10 @@ __device__ __forceinline__ void issue_shadow(const DPaths& P, uint32_t p, int k,
 }
 
 // one bounce of the loop body (shaders/PathTrace.slang:5921-6914)
-__global__ void __launch_bounds__(kThreads) k_shade(DScene S, DFrame F, DPaths P, int qsel, uint32_t b) {
+template <bool kB>
+__global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DScene S0,
+                                                     const __grid_constant__ DFrame F0, DPaths P, Batch B,
+                                                     int qsel, uint32_t b) {
     const uint32_t n = P.cnt[qsel];
     const uint32_t* q = P.q[qsel];
     uint32_t* qn = P.q[qsel ^ 1];
@@ -471,6 +525,9 @@ __global__ void __launch_bounds__(kThreads) k_shade(DScene S, DFrame F, DPaths P
         uint32_t p = 0;
         if (i < n) {
             p = q[i];
+            const DFrame& F = kB ? B.views[B.path_view[p]] : F0;
+            const DScene& S = kB ? B.scenes[F.scene] : S0;
+            if (!kB || b < F.maxb) {
             const float4 o4 = P.ray_o[p], d4 = P.ray_d[p], t4 = P.thr[p], r4 = P.rad[p];
             V3 ro = v3(o4), rd = v3(d4), thr = v3(t4), rad = v3(r4);
             float prev_pdf = t4.w;
@@ -599,6 +656,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(DScene S, DFrame F, DPaths P
             P.seed[p] = seed;
             P.shmask[p] = shadow_mask;
             cont = !ended;
+            }
         }
         // compaction: survivors to the next queue, shadow rays to the shadow queue
         const uint32_t slot = warp_push(P.cnt + (qsel ^ 1), cont);
@@ -626,31 +684,39 @@ __global__ void __launch_bounds__(kThreads, 4) k_shadow(DScene S, DPaths P, int 
 
 
 // persistent closest hit for a queue of rays (extension rays or first shadow segments)
-__global__ void __launch_bounds__(kThreads, 4) k_closest(DScene S, const uint32_t* queue,
-                                                         const uint32_t* count, const float4* ray_o,
-                                                         const float4* ray_d, float* out_t, uint32_t* out_id,
-                                                         uint32_t* fetch_ctr, unsigned long long* stat) {
+template <bool kB>
+__global__ void __launch_bounds__(kThreads, 4) k_closest(const __grid_constant__ DScene S, Batch B,
+                                                         const uint32_t* queue, const uint32_t* count,
+                                                         const float4* ray_o, const float4* ray_d, float* out_t,
+                                                         uint32_t* out_id, uint32_t* fetch_ctr,
+                                                         unsigned long long* stat) {
     uint32_t done = 0;
-    persistent_closest<false>(S, queue, *count, ray_o, ray_d, out_t, out_id, fetch_ctr, done, ShadowIO{});
+    persistent_closest<false, kB>(&S, ItemScenes{B.scenes, B.path_scene}, queue, *count, ray_o, ray_d, out_t,
+                                  out_id, fetch_ctr, done, ShadowIO{});
     warp_add(stat, done);
 }
 
 // persistent transmittance: whole dielectric chains per lane (every segment
 // counted as a shadow segment)
-__global__ void __launch_bounds__(kThreads, 4) k_transmit(DScene S, DPaths P, int kmax) {
+template <bool kB>
+__global__ void __launch_bounds__(kThreads, 4) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
+                                                          int kmax) {
     uint32_t done = 0;
     const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax};
-    persistent_closest<true>(S, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr, nullptr, P.cnt + 3, done, io);
+    persistent_closest<true, kB>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
+                                 nullptr, P.cnt + 3, done, io);
     warp_add(P.stat + 1, done);
 }
 
 // NEE terms in the reference order (light, env, HDRI), then the sample's
 // radiance for paths that ended (shaders/PathTrace.slang:6341-6520, 7701).
-__global__ void k_resolve(DFrame F, DPaths P, int qsel) {
+template <bool kB>
+__global__ void k_resolve(const __grid_constant__ DFrame F0, DPaths P, Batch B, int qsel) {
     const uint32_t n = P.cnt[qsel];
     const uint32_t* q = P.q[qsel];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
+        const DFrame& F = kB ? B.views[B.path_view[p]] : F0;
         const uint32_t mask = P.shmask[p];
         const uint32_t st = P.state[p];
         if (mask == 0u && !(st & kEnded)) continue;
@@ -677,6 +743,27 @@ __global__ void k_resolve(DFrame F, DPaths P, int qsel) {
 // running mean / EMA (shaders/PathTrace.slang:7707-7781)
 __device__ __forceinline__ float clean(float v) { return (isnan(v) || isinf(v)) ? 0.0f : fmaxf(v, 0.0f); }
 
+__device__ __forceinline__ float4 accum_update(float4 a, float4 fs, float nspp, bool reset, float ema_in) {
+    const float ema = clampf(ema_in, 0.0f, 0.999f);
+    V3 fr = v3(fs) / nspp;
+    fr = v3(clean(fr.x), clean(fr.y), clean(fr.z));
+    if (reset) a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (isnan(a.x) || isinf(a.x) || isnan(a.y) || isinf(a.y) || isnan(a.z) || isinf(a.z) || isnan(a.w) ||
+        isinf(a.w))
+        a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V3 pr = v3(a);
+    float n_new;
+    V3 avg;
+    if (a.w < 0.5f || ema <= 0.0f) {
+        n_new = a.w + 1.0f;
+        avg = (pr * a.w + fr) / n_new;
+    } else {
+        avg = pr * ema + fr * (1.0f - ema);
+        n_new = fminf(a.w + 1.0f, 1.0f / fmaxf(1.0f - ema, 1e-3f));
+    }
+    return f4(avg, n_new);
+}
+
 __global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes, bool reset_first,
                              float ema_in) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;   // path slot within a frame
@@ -686,28 +773,20 @@ __global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes
     const size_t out = size_t(y) * F.W + x;
     float4 a = accum[out];
     const float nspp = float(F.spp == 0u ? 1u : F.spp);
-    const float ema = clampf(ema_in, 0.0f, 0.999f);
-    for (uint32_t f = 0; f < nframes; ++f) {
-        const float4 s = P.fsum[size_t(f) * F.npix + pix];
-        V3 fr = v3(s) / nspp;
-        fr = v3(clean(fr.x), clean(fr.y), clean(fr.z));
-        if (f == 0 && reset_first) a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (isnan(a.x) || isinf(a.x) || isnan(a.y) || isinf(a.y) || isnan(a.z) || isinf(a.z) ||
-            isnan(a.w) || isinf(a.w))
-            a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        const V3 pr = v3(a);
-        float n_new;
-        V3 avg;
-        if (a.w < 0.5f || ema <= 0.0f) {
-            n_new = a.w + 1.0f;
-            avg = (pr * a.w + fr) / n_new;
-        } else {
-            avg = pr * ema + fr * (1.0f - ema);
-            n_new = fminf(a.w + 1.0f, 1.0f / fmaxf(1.0f - ema, 1e-3f));
-        }
-        a = f4(avg, n_new);
-    }
+    for (uint32_t f = 0; f < nframes; ++f)
+        a = accum_update(a, P.fsum[size_t(f) * F.npix + pix], nspp, f == 0 && reset_first, ema_in);
     accum[out] = a;
+}
+
+// batched renders: one frame of every view, each into its own region
+__global__ void k_accumulate_batch(DPaths P, Batch B, uint32_t npaths) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npaths) return;
+    const DFrame& V = B.views[B.path_view[p]];
+    uint32_t x, y;
+    slot_pixel(V, p - V.slot_base, x, y);
+    const size_t out = V.accum_base + size_t(y) * V.W + x;
+    B.accum[out] = accum_update(B.accum[out], P.fsum[p], float(V.spp == 0u ? 1u : V.spp), V.reset != 0u, V.ema);
 }
 
 __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint32_t n, uint32_t* hit,
@@ -769,6 +848,17 @@ struct pt_gpu_ctx {
     DBuf<uint4> a4_meta;
     double build_ms = 0.0;
     uint32_t t4_bin_nodes = 0;
+    // batched renders
+    DBuf<DFrame> b_views;
+    DBuf<DScene> b_scenes;
+    DBuf<uint32_t> b_view_base, b_path_view, b_path_scene;
+    DBuf<float4> b_accum;
+    std::vector<size_t> b_accum_off;
+    std::vector<uint32_t> b_w, b_h;
+    std::vector<DFrame> b_views_h;
+    cudaGraphExec_t b_graph = nullptr;
+    std::vector<uint64_t> b_sig;
+    PtBatchTuning b_tune{4u, 8u, 1u, 0u};
     PtStats stats{};
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -1170,6 +1260,13 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     dfree(ctx->a4_meta);
     dfree(ctx->hit_t);
     dfree(ctx->stat);
+    if (ctx->b_graph) cudaGraphExecDestroy(ctx->b_graph);
+    dfree(ctx->b_views);
+    dfree(ctx->b_scenes);
+    dfree(ctx->b_view_base);
+    dfree(ctx->b_path_view);
+    dfree(ctx->b_path_scene);
+    dfree(ctx->b_accum);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -1422,10 +1519,10 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
         F.nframes = nf;
         F.frame_index0 = head->frame_index + f0;
         const int gp = (npaths + 255) / 256;
-        k_init_wave<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, head->frame_index + f0);
+        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
         ctx->stats.kernel_launches += 2;   // init + accumulate
         for (uint32_t s = 0; s < F.spp; ++s) {
-            k_camera<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, s);
+            k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const int qs = int(b & 1u);
@@ -1435,26 +1532,27 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
-                    k_closest<<<gpers, kThreads, 0, ctx->stream>>>(S, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
-                                                                   P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                    k_closest<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o,
+                                                                          P.ray_d, P.hit_t, P.hit_id, P.cnt + 3,
+                                                                          P.stat);
                 } else if (S.use_wide) {
                     k_extend<true><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
                 } else {
                     k_extend<false><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
                 }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
+                k_shade<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, qs, b);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
-                    k_transmit<<<gpers, kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                k_resolve<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, qs);
+                k_resolve<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, Batch{}, qs);
                 ctx->stats.extend_launches++;
                 ctx->stats.shadow_launches++;
             }
@@ -1576,6 +1674,303 @@ int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d
     uint32_t errw = 0;
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
     if (errw) return set_err(ctx, PT_ERR_KERNEL, "trace_closest: traversal iteration cap reached");
+    return PT_OK;
+}
+
+}  // extern "C"
+
+
+// ===========================================================================
+// Batched renders
+// ===========================================================================
+namespace {
+
+int validate_view(pt_gpu_ctx* ctx, pt_gpu_ctx* sc, const PtBatchView& v, uint32_t i) {
+    const std::string w = "batch view " + std::to_string(i) + ": ";
+    const PtPushHead* head = &v.head;
+    const PtPathParams* prm = &v.params;
+    if (v.width == 0 || v.height == 0) return set_err(ctx, PT_ERR_INVALID, w + "empty frame");
+    if (head->tlas_present || prm->light_tree_enabled || !head->env_map_present)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, w + "tlas / light tree / procedural sky not built");
+    if (head->prim_count != sc->prim_count || prm->bvh_params[0] != sc->linear_count ||
+        prm->bvh_params[1] != sc->bvh_nodes)
+        return set_err(ctx, PT_ERR_INVALID, w + "prim_count / bvh_params disagree with its scene");
+    if ((prm->bvh_params[2] != 0u) != (sc->tri_nodes != 0u) ||
+        (prm->bvh_params[2] != 0u && prm->bvh_params[3] != sc->tri_nodes))
+        return set_err(ctx, PT_ERR_INVALID, w + "mesh bvh_params disagree with its scene");
+    if (prm->light_count != sc->light_count) return set_err(ctx, PT_ERR_INVALID, w + "light_count disagrees");
+    if (sc->env_w == 0) return set_err(ctx, PT_ERR_STATE, w + "scene has no env map");
+    if (!sc->a_wide && sc->prim_count > sc->linear_count)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, w + "scene has no wide analytic tree");
+    if (!sc->t_wide && sc->tri_nodes > 0u)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, w + "scene has no wide mesh tree");
+    return PT_OK;
+}
+
+DFrame frame_of(const PtBatchView& v) {
+    const PtPushHead* head = &v.head;
+    const PtPathParams* prm = &v.params;
+    DFrame F{};
+    F.cam_pos = v3(head->pos_fovtan[0], head->pos_fovtan[1], head->pos_fovtan[2]);
+    F.tanf = head->pos_fovtan[3];
+    F.fwd = v3(head->fwd_aspect[0], head->fwd_aspect[1], head->fwd_aspect[2]);
+    F.aspect = head->fwd_aspect[3];
+    F.right = v3(head->right_xyz[0], head->right_xyz[1], head->right_xyz[2]);
+    F.up = v3(head->up_xyz[0], head->up_xyz[1], head->up_xyz[2]);
+    F.W = v.width;
+    F.H = v.height;
+    F.npix = v.width * v.height;
+    F.nframes = 1;
+    F.frame_index0 = head->frame_index;
+    F.spp = head->spp == 0u ? 1u : head->spp;
+    F.maxb = head->max_bounces;
+    F.denoiser = head->denoiser_enabled;
+    F.jx = head->halton_jitter[0];
+    F.jy = head->halton_jitter[1];
+    F.env_present = head->env_map_present;
+    F.env_intensity = head->env_intensity;
+    F.env_total = head->env_total_luminance;
+    F.kmax = int(prm->refract_budget);
+    F.firefly = prm->firefly_clamp;
+    F.mis = prm->mis_enabled;
+    F.rr_start = prm->rr_start;
+    F.light_count = prm->light_count;
+    F.scene = v.scene;
+    F.reset = head->reset_accum;
+    F.ema = prm->accum_ema_alpha;
+    return F;
+}
+
+// Issue one wave (one frame of every view) on ctx->stream.
+int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t npaths, uint32_t max_spp,
+                     uint32_t max_b, int kmax_any, const DScene& S0) {
+    const DFrame F0{};
+    const int gp = (npaths + 255) / 256;
+    const int gpers = ctx->sm_count * int(ctx->b_tune.persistent_blocks_per_sm);
+    const int gstream = int(std::max<size_t>(1, std::min<size_t>((npaths + kThreads - 1) / kThreads,
+                                                                 size_t(ctx->sm_count) * ctx->b_tune.stream_blocks_per_sm)));
+    CK(cudaMemsetAsync(P.stat, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    k_init_wave<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths, 0u);
+    for (uint32_t s = 0; s < max_spp; ++s) {
+        CK(cudaMemsetAsync(P.cnt, 0, 4, ctx->stream));
+        k_camera<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths, s);
+        for (uint32_t b = 0; b < max_b; ++b) {
+            const int qs = int(b & 1u);
+            CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
+            CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
+            k_closest<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
+                                                                 P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+            k_shade<true><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, qs, b);
+            CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
+            k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any);
+            k_resolve<true><<<gstream, kThreads, 0, ctx->stream>>>(F0, P, Bt, qs);
+        }
+    }
+    k_accumulate_batch<<<gp, 256, 0, ctx->stream>>>(P, Bt, npaths);
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_gpu_batch_set_tuning(pt_gpu_ctx* ctx, const PtBatchTuning* t) {
+    if (!ctx || !t || t->persistent_blocks_per_sm < 1 || t->persistent_blocks_per_sm > 4 ||
+        t->stream_blocks_per_sm < 1 || t->stream_blocks_per_sm > 64)
+        return PT_ERR_INVALID;
+    ctx->b_tune = *t;
+    if (ctx->b_graph) {
+        cudaGraphExecDestroy(ctx->b_graph);
+        ctx->b_graph = nullptr;
+    }
+    ctx->b_sig.clear();
+    return PT_OK;
+}
+
+int pt_gpu_batch_get_tuning(pt_gpu_ctx* ctx, PtBatchTuning* t) {
+    if (!ctx || !t) return PT_ERR_INVALID;
+    *t = ctx->b_tune;
+    return PT_OK;
+}
+
+int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, const PtBatchView* views,
+                        uint32_t n_views, uint32_t frames) {
+    if (!ctx || !scenes || !views || n_scenes == 0 || n_views == 0) return PT_ERR_INVALID;
+    for (uint32_t k = 0; k < n_scenes; ++k)
+        if (!scenes[k] || scenes[k]->device != ctx->device)
+            return set_err(ctx, PT_ERR_INVALID, "batch: scene contexts must be on the batch context's device");
+    uint64_t total = 0;
+    uint32_t max_spp = 0, max_b = 0;
+    int kmax_any = -1;
+    for (uint32_t i = 0; i < n_views; ++i) {
+        if (views[i].scene >= n_scenes) return set_err(ctx, PT_ERR_INVALID, "batch: view scene index out of range");
+        if (int rc = validate_view(ctx, scenes[views[i].scene], views[i], i)) return rc;
+        total += uint64_t(views[i].width) * views[i].height;
+        max_spp = std::max(max_spp, views[i].head.spp == 0u ? 1u : views[i].head.spp);
+        max_b = std::max(max_b, views[i].head.max_bounces);
+        const int km = int(views[i].params.refract_budget);
+        if (kmax_any >= 0 && km != kmax_any)
+            return set_err(ctx, PT_ERR_INVALID, "batch: all views must share the refraction budget");
+        kmax_any = km;
+    }
+    if (total > (64ull << 20)) return set_err(ctx, PT_ERR_INVALID, "batch: more than 64 M pixels per frame");
+    const uint32_t npaths = uint32_t(total);
+    if (frames == 0) return PT_OK;
+
+    // layout signature: views' sizes and scenes, tuning
+    std::vector<uint64_t> sig;
+    sig.push_back(n_views);
+    for (uint32_t i = 0; i < n_views; ++i) {
+        sig.push_back((uint64_t(views[i].width) << 32) | views[i].height);
+        sig.push_back(uint64_t(reinterpret_cast<uintptr_t>(scenes[views[i].scene])));
+        sig.push_back((uint64_t(views[i].head.spp) << 32) | views[i].head.max_bounces);
+    }
+    const bool same_layout = (sig == ctx->b_sig);
+    int rc = ensure_wave(ctx, npaths);
+    if (rc) return rc;
+    if (!same_layout) {
+        if (ctx->b_graph) {
+            cudaGraphExecDestroy(ctx->b_graph);
+            ctx->b_graph = nullptr;
+        }
+        std::vector<uint32_t> base(n_views + 1, 0);
+        std::vector<size_t> aoff(n_views, 0);
+        size_t acc = 0;
+        for (uint32_t i = 0; i < n_views; ++i) {
+            base[i + 1] = base[i] + views[i].width * views[i].height;
+            aoff[i] = acc;
+            acc += size_t(views[i].width) * views[i].height;
+        }
+        if ((rc = dupload(ctx, ctx->b_view_base, base.data(), n_views + 1)) ||
+            (rc = dalloc(ctx, ctx->b_path_view, npaths)) || (rc = dalloc(ctx, ctx->b_path_scene, npaths)) ||
+            (rc = dalloc(ctx, ctx->b_views, n_views)) || (rc = dalloc(ctx, ctx->b_scenes, n_scenes)) ||
+            (rc = dalloc(ctx, ctx->b_accum, acc)))
+            return rc;
+        CK(cudaMemsetAsync(ctx->b_accum.p, 0, acc * 16, ctx->stream));
+        ctx->b_accum_off = aoff;
+        ctx->b_w.resize(n_views);
+        ctx->b_h.resize(n_views);
+        for (uint32_t i = 0; i < n_views; ++i) {
+            ctx->b_w[i] = views[i].width;
+            ctx->b_h[i] = views[i].height;
+        }
+    }
+    // scene table (pointers may change after re-uploads)
+    std::vector<DScene> st(n_scenes);
+    for (uint32_t k = 0; k < n_scenes; ++k) {
+        st[k] = make_scene(scenes[k], nullptr);
+        st[k].err = ctx->err_word.p;
+    }
+    CK(cudaMemcpyAsync(ctx->b_scenes.p, st.data(), n_scenes * sizeof(DScene), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->b_views_h.resize(n_views);
+    uint32_t base_slot = 0;
+    for (uint32_t i = 0; i < n_views; ++i) {
+        ctx->b_views_h[i] = frame_of(views[i]);
+        ctx->b_views_h[i].slot_base = base_slot;
+        ctx->b_views_h[i].accum_base = ctx->b_accum_off[i];
+        base_slot += views[i].width * views[i].height;
+    }
+
+    DPaths P{};
+    P.ray_o = ctx->ray_o.p; P.ray_d = ctx->ray_d.p; P.thr = ctx->thr.p; P.rad = ctx->rad.p;
+    P.fsum = ctx->fsum.p; P.seed = ctx->seed.p; P.state = ctx->state.p; P.hit_t = ctx->hit_t.p;
+    P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
+    P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
+    P.q[0] = ctx->q0.p; P.q[1] = ctx->q1.p; P.sq = ctx->sq.p; P.cnt = ctx->cnt.p; P.stat = ctx->stat.p;
+    Batch Bt{};
+    Bt.views = ctx->b_views.p;
+    Bt.scenes = ctx->b_scenes.p;
+    Bt.path_view = ctx->b_path_view.p;
+    Bt.path_scene = ctx->b_path_scene.p;
+    Bt.view_base = ctx->b_view_base.p;
+    Bt.accum = ctx->b_accum.p;
+    Bt.n_views = n_views;
+    const DScene S0 = st[0];
+
+    CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
+    ctx->stats = PtStats{};
+    unsigned long long tot_ext = 0, tot_sh = 0;
+    const uint32_t launches_per_wave = 2 + max_spp * (1 + 4 * max_b);
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    for (uint32_t f = 0; f < frames; ++f) {
+        for (uint32_t i = 0; i < n_views; ++i) {
+            DFrame& V = ctx->b_views_h[i];
+            V.frame_index0 = views[i].head.frame_index + f;
+            V.reset = (f == 0 && views[i].head.reset_accum) ? 1u : 0u;
+        }
+        CK(cudaMemcpyAsync(ctx->b_views.p, ctx->b_views_h.data(), n_views * sizeof(DFrame), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        if (ctx->b_tune.use_graph) {
+            if (!ctx->b_graph) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+                const int irc = issue_batch_wave(ctx, Bt, P, npaths, max_spp, max_b, kmax_any, S0);
+                cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+                if (irc) return irc;
+                if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+                e = cudaGraphInstantiate(&ctx->b_graph, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    ctx->b_graph = nullptr;
+                    return set_err(ctx, PT_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+                }
+            }
+            CK(cudaGraphLaunch(ctx->b_graph, ctx->stream));
+        } else {
+            if (int irc = issue_batch_wave(ctx, Bt, P, npaths, max_spp, max_b, kmax_any, S0)) return irc;
+        }
+        unsigned long long st2[4];
+        CK(cudaMemcpyAsync(st2, ctx->stat.p, sizeof(st2), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        tot_ext += st2[0];
+        tot_sh += st2[1];
+        ctx->stats.kernel_launches += launches_per_wave;
+        ctx->stats.waves++;
+        ctx->stats.paths += uint64_t(npaths) * max_spp;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->b_sig = sig;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.gpu_ms = ms;
+    ctx->stats.frames = frames;
+    ctx->stats.extension_rays = tot_ext;
+    ctx->stats.shadow_rays = tot_sh;
+    uint32_t errw = 0;
+    CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "batch: traversal iteration cap reached");
+    return PT_OK;
+}
+
+int pt_gpu_batch_read_accum(pt_gpu_ctx* ctx, uint32_t view, float* host_rgba) {
+    if (!ctx || !host_rgba) return PT_ERR_INVALID;
+    if (view >= ctx->b_accum_off.size()) return set_err(ctx, PT_ERR_INVALID, "batch_read_accum: no such view");
+    CK(cudaMemcpyAsync(host_rgba, ctx->b_accum.p + ctx->b_accum_off[view],
+                       size_t(ctx->b_w[view]) * ctx->b_h[view] * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, const PtBatchView* views,
+                          uint32_t n_views, PtBatchTuning* chosen) {
+    if (!ctx) return PT_ERR_INVALID;
+    const PtBatchTuning cands[] = {{4u, 8u, 1u, 0u}, {3u, 8u, 1u, 0u}, {2u, 8u, 1u, 0u},
+                                   {4u, 4u, 1u, 0u}, {4u, 16u, 1u, 0u}};
+    double best = 1e30;
+    PtBatchTuning pick = cands[0];
+    for (const auto& c : cands) {
+        if (int rc = pt_gpu_batch_set_tuning(ctx, &c)) return rc;
+        if (int rc = pt_gpu_batch_render(ctx, scenes, n_scenes, views, n_views, 1)) return rc;   // capture
+        if (int rc = pt_gpu_batch_render(ctx, scenes, n_scenes, views, n_views, 1)) return rc;   // timed
+        if (ctx->stats.gpu_ms < best) {
+            best = ctx->stats.gpu_ms;
+            pick = c;
+        }
+    }
+    if (int rc = pt_gpu_batch_set_tuning(ctx, &pick)) return rc;
+    if (chosen) *chosen = pick;
     return PT_OK;
 }
 
@@ -1746,10 +2141,10 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         F.nframes = nf;
         F.frame_index0 = head->frame_index + f0;
         const int gp = (npaths + 255) / 256;
-        k_init_wave<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, head->frame_index + f0);
+        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
         ctx->stats.kernel_launches += 2;
         for (uint32_t s = 0; s < F.spp; ++s) {
-            k_camera<<<gp, 256, 0, ctx->stream>>>(F, P, npaths, s);
+            k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const int qs = int(b & 1u);
@@ -1757,23 +2152,24 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                 CK(cudaMemsetAsync(P.cnt + 2, 0, 4, ctx->stream));
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_closest<<<gpers, kThreads, 0, ctx->stream>>>(S, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
-                                                                   P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                    k_closest<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o,
+                                                                          P.ray_d, P.hit_t, P.hit_id, P.cnt + 3,
+                                                                          P.stat);
                 } else if (S.use_wide) {
                     k_extend<true><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
                 } else {
                     k_extend<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
                 }
-                k_shade<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, qs, b);
+                k_shade<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, qs, b);
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_transmit<<<gpers, kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 }
-                k_resolve<<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, qs);
+                k_resolve<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, Batch{}, qs);
                 ctx->stats.extend_launches++;
                 ctx->stats.shadow_launches++;
             }

@@ -200,6 +200,41 @@ int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out);
  * frame size so a wave holds about 16 M paths). 0 restores the default. */
 int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave);
 
+/* ---- batched render (extension: many views of several scenes in one wavefront) ----
+ * Each scene is a context that holds its own uploads; `ctx` owns the batch's
+ * path state and one RGBA32F accumulation region per view.  One frame of every
+ * view is one device wave: all views' pixels run through the same kernels (the
+ * persistent traversal mixes scenes within a warp), and the wave's launch
+ * sequence is captured once as a CUDA graph and replayed per frame.  Each view
+ * behaves exactly like pt_gpu_render of that view on its scene (bit-identical
+ * accumulation), frame f of a view using frame_index = head.frame_index + f and
+ * reset_accum only for f == 0. */
+typedef struct PtBatchView {
+    uint32_t     scene;      /* index into the scenes array */
+    uint32_t     width, height;
+    uint32_t     reserved;
+    PtPushHead   head;
+    PtPathParams params;
+} PtBatchView;
+
+typedef struct PtBatchTuning {
+    uint32_t persistent_blocks_per_sm;   /* grid of the persistent traversal kernels (1..4) */
+    uint32_t stream_blocks_per_sm;       /* grid cap of the streaming kernels (shade/resolve) */
+    uint32_t use_graph;                  /* 1: replay the captured wave graph */
+    uint32_t reserved;
+} PtBatchTuning;
+
+int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes,
+                        const PtBatchView* views, uint32_t n_views, uint32_t frames);
+int pt_gpu_batch_read_accum(pt_gpu_ctx* ctx, uint32_t view, float* host_rgba);
+int pt_gpu_batch_set_tuning(pt_gpu_ctx* ctx, const PtBatchTuning* tuning);
+int pt_gpu_batch_get_tuning(pt_gpu_ctx* ctx, PtBatchTuning* tuning);
+/* Times each candidate launch shape on one frame of this batch (the views'
+ * accumulation is reset afterwards by the next render with reset_accum) and
+ * keeps the fastest.  Writes the choice to *chosen (nullable). */
+int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes,
+                          const PtBatchView* views, uint32_t n_views, PtBatchTuning* chosen);
+
 /* ---- allocation-free render (no counterpart in the reference) ----
  * For callers that must not allocate device memory while rendering: an engine
  * that reserved its whole device budget up front, a frame loop that cannot

@@ -282,3 +282,49 @@ def test_full_size_c1_frame_matches_oracle_on_crops(pt, orc, dev):
     for (x0, y0) in ((952, 532), (100, 900), (1700, 200)):
         orc.render(s.packed(), head, prm, W, H, 1, accum=acc, crop=(x0, y0, x0 + 16, y0 + 16))
         np.testing.assert_array_equal(g[y0:y0 + 16, x0:x0 + 16], acc[y0:y0 + 16, x0:x0 + 16])
+
+
+def _batch_setup(pt):
+    scenes = [pt.Scene().synth(1, seed=k, scale=0.02) for k in range(3)] + [pt.Scene().synth(0, seed=9)]
+    devs = []
+    for s in scenes:
+        d = pt.Device(0)
+        d.upload(s)
+        devs.append(d)
+    sizes = [(32, 24), (48, 40), (16, 16), (40, 32), (30, 18), (64, 36), (8, 4)]
+    views = []
+    for i, (w, h) in enumerate(sizes):
+        k = i % len(scenes)
+        head, prm = scenes[k].push(w, h, frame_index=10 + 3 * i, reset=1)
+        head.spp = 1 + (i % 3)
+        head.max_bounces = 3 + (i % 6)
+        views.append((k, w, h, head, prm))
+    return scenes, devs, views
+
+
+def test_batch_render_equals_plain_render_per_view(pt, dev):
+    scenes, devs, views = _batch_setup(pt)
+    for use_graph in (1, 0):
+        batch = pt.Device(0)
+        batch.batch_set_tuning(4, 8, use_graph)
+        batch.batch_render(devs, views, frames=2)
+        st = batch.stats()
+        assert st.extension_rays > 0 and st.shadow_rays > 0
+        for i, (k, w, h, head, prm) in enumerate(views):
+            d = devs[k]
+            d.set_target(w, h)
+            d.render(head, prm, 2)
+            np.testing.assert_array_equal(batch.batch_read(i, w, h), d.read_accum(), err_msg=f"view {i}")
+        batch.close()
+
+
+def test_batch_autotune_keeps_results(pt, dev):
+    scenes, devs, views = _batch_setup(pt)
+    batch = pt.Device(0)
+    t = batch.batch_autotune(devs, views)
+    assert 1 <= t.persistent_blocks_per_sm <= 4
+    batch.batch_render(devs, views, frames=1)
+    k, w, h, head, prm = views[1]
+    devs[k].set_target(w, h)
+    devs[k].render(head, prm, 1)
+    np.testing.assert_array_equal(batch.batch_read(1, w, h), devs[k].read_accum())
