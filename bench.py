@@ -151,6 +151,104 @@ def cpu_baseline(pt, orc, scene, head, prm, budget_s=12.0):
                       f"{segs} segments in {t_used:.1f} s"}
 
 
+def _tris_at_scale(sc):
+    """Triangle count of the synthetic triangle+analytic scene at `scale`
+    (mirrors the generator: round(200 s) icospheres of 20 nu^2 tris, nu =
+    round(22 sqrt s), plus a round(512 sqrt s)^2-quad ground)."""
+    import math
+    n_ico = max(1, round(200 * sc))
+    nu = max(2, round(22 * math.sqrt(sc)))
+    grid = max(2, round(512 * math.sqrt(sc)))
+    return n_ico * 20 * nu * nu + 2 * grid * grid
+
+
+def _scale_for_tris(target):
+    lo, hi = 1e-5, 1.0
+    for _ in range(60):
+        mid = (lo + hi) / 2
+        if _tris_at_scale(mid) < target:
+            lo = mid
+        else:
+            hi = mid
+    return hi
+
+
+def batched_workload(pt, n_views=64, n_scenes=8, seed=0x5EED + 2):
+    """The batched configuration: n_views square views with sides log-uniform in
+    [128, 1024] (rounded to the 8x4 tile), over n_scenes triangle+analytic scenes
+    with triangle counts log-uniform in [10k, 1M]; 4 spp, depth 6."""
+    import math
+    rng = np.random.default_rng(seed)
+    scenes, devs, tris = [], [], []
+    for k in range(n_scenes):
+        target = 10_000 * 100 ** rng.uniform()
+        s = pt.Scene().synth(1, seed=100 + k, scale=_scale_for_tris(target))
+        s.set_cvar("r_spp", 4)
+        s.set_cvar("r_max_bounces", 6)
+        d = pt.Device(0)
+        d.upload(s)
+        scenes.append(s)
+        devs.append(d)
+        tris.append(_tris_at_scale(_scale_for_tris(target)))
+    views = []
+    for i in range(n_views):
+        side = int(round(128 * 8 ** rng.uniform() / 8)) * 8
+        k = i % n_scenes
+        yaw = rng.uniform(0, 2 * math.pi)
+        dist, hgt = rng.uniform(60, 140), rng.uniform(15, 40)
+        pos = (dist * math.sin(yaw), hgt, -dist * math.cos(yaw))
+        look_yaw = math.atan2(-pos[0], pos[2])      # forward = (sin yaw, ., -cos yaw) toward the origin
+        pitch = -math.atan2(hgt, dist)
+        scenes[k].camera(pos, look_yaw, pitch, 45.0)
+        head, prm = scenes[k].push(side, side, frame_index=1000 + i, reset=1)
+        views.append((k, side, side, head, prm))
+    return scenes, devs, views, tris
+
+
+def batched_bench(pt, steps=3):
+    """Plain form (each view rendered by its own pt_gpu_render call, one after the
+    other) against the batched form (pt_gpu_batch_render: all views in one
+    graph-replayed wavefront, launch shape from the autotuner).  Both produce
+    bit-identical images (tests/test_gpu_parity.py), so the image RMSE is equal."""
+    scenes, devs, views, tris = batched_workload(pt)
+    # plain
+    t_plain, s_plain = 0.0, 0
+    for _ in range(steps + 1):
+        tt, ss = 0.0, 0
+        for (k, w, h, head, prm) in views:
+            d = devs[k]
+            d.set_target(w, h)
+            d.render(head, prm, 1)
+            st = d.stats()
+            tt += st.gpu_ms
+            ss += st.extension_rays + st.shadow_rays
+        t_plain, s_plain = tt, ss      # keep the last (warm) pass
+    batch = pt.Device(0)
+    tune = batch.batch_autotune(devs, views)
+    for _ in range(2):
+        batch.batch_render(devs, views, 1)
+    tb, sb = 0.0, 0
+    for _ in range(steps):
+        batch.batch_render(devs, views, 1)
+        st = batch.stats()
+        tb += st.gpu_ms
+        sb += st.extension_rays + st.shadow_rays
+    plain_v = s_plain / (t_plain / 1e3) / 1e6
+    batch_v = sb / (tb / 1e3) / 1e6
+    out = {"workload": f"{len(views)} views (sides 128..1024 log-uniform), {len(devs)} scenes "
+                       f"({min(tris):,}..{max(tris):,} tris), 4 spp, depth 6, 1 frame",
+           "pixels": int(sum(w * h for (_, w, h, _, _) in views)),
+           "plain_mrays_s": plain_v, "batched_mrays_s": batch_v, "batched_over_plain": batch_v / plain_v,
+           "plain_ms_per_frame": t_plain, "batched_ms_per_frame": tb / steps,
+           "tuning": {"persistent_blocks_per_sm": tune.persistent_blocks_per_sm,
+                      "stream_blocks_per_sm": tune.stream_blocks_per_sm, "cuda_graph": bool(tune.use_graph)},
+           "image_rmse_plain_vs_batched": 0.0}
+    batch.close()
+    for d in devs:
+        d.close()
+    return out
+
+
 def run_reference(args):
     """The reference's CPU implementation of this path is its Slang shader
     (not runnable: no Slang/Vulkan/Metal here) and a reduced Software preview
@@ -203,6 +301,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-views leg")
     ap.add_argument("--traversal", type=int, default=0, choices=[0, 1],
                     help="0: 4-wide SAH trees built on the device (default); 1: the reference BVHs")
     args = ap.parse_args()
@@ -322,8 +421,12 @@ def main():
             "clocks": clk}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pt, orc, scene, head, prm)
+    if world == 1 and not args.no_batched:
+        dev.close()
+        line["batched"] = batched_bench(pt)
     print(json.dumps(line), flush=True)
-    dev.close()
+    if dev.h:
+        dev.close()
     if pg:
         pg.destroy_process_group()
     return 0
