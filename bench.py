@@ -249,6 +249,103 @@ def batched_bench(pt, steps=3):
     return out
 
 
+def adjoint_bench(pt, fd_params=32, seed=0x5EED + 3):
+    """Differentiable render (512x512, 32 spp, depth 6, roulette from bounce 3,
+    256 material rows of which 16 emissive, ~200k triangles + 512 spheres).
+    Target: 32 frames x 32 spp (1024 spp) with the albedos perturbed by
+    N(0, 0.1) and clamped to [0.02, 0.98]; loss = L2 over HDR pixels.  One
+    gradient evaluation = pt_gpu_diff_forward + pt_gpu_diff_backward.  Central
+    differences (eps 1e-3, common random numbers = the same pixel seeds) on 32
+    random parameters, once with the configured roulette and once with it off
+    (the per-sample estimator is then smooth in the parameters)."""
+    W = H = 512
+    sc = pt.Scene().synth(3, seed=0)
+    pk = sc.packed()
+    nm = pk.material_count
+    mats = np.ctypeslib.as_array(pk.materials, (nm * 12,)).reshape(nm, 12).copy()
+    tris = pk.tri_count
+    dev = pt.Device(0)
+    dev.upload(sc)
+    dev.set_target(W, H)
+    rng = np.random.default_rng(seed)
+    tgt_m = mats.copy()
+    tgt_m[:, :3] = np.clip(mats[:, :3] + rng.normal(0.0, 0.1, (nm, 3)), 0.02, 0.98).astype(np.float32)
+    dev.materials(tgt_m)
+    h_t, p_t = sc.push(W, H, frame_index=500, reset=1)
+    dev.render(h_t, p_t, 32)
+    target = dev.read_accum()[..., :3].astype(np.float64)
+    dev.materials(mats)
+    head, prm = sc.push(W, H, frame_index=0, reset=1)
+
+    def grad_eval():
+        dev.diff_forward(head, prm, 1)
+        f = dev.stats()
+        img = dev.read_accum()[..., :3].astype(np.float64)
+        dl = (2.0 * (img - target)).astype(np.float32)
+        ga, ge = dev.diff_backward(dl, nm)
+        b = dev.backward_stats()
+        return f, b, ga, ge, float(((img - target) ** 2).sum())
+
+    for _ in range(3):
+        grad_eval()
+    fwd_ms, bwd_ms, n = 0.0, 0.0, 5
+    t0 = time.perf_counter()
+    for _ in range(n):
+        f, b, ga, ge, loss0 = grad_eval()
+        fwd_ms += f.gpu_ms
+        bwd_ms += b.gpu_ms
+    wall = (time.perf_counter() - t0) / n
+    fwd_ms /= n
+    bwd_ms /= n
+
+    emissive = [r for r in range(nm) if mats[r, 4:7].max() > 0]
+    pool = [("a", r, c) for r in range(nm) for c in range(3)] + [("e", r, c) for r in emissive for c in range(3)]
+    pick = [pool[i] for i in rng.choice(len(pool), fd_params, replace=False)]
+
+    def fd_check(rr_start):
+        p2 = type(prm).from_buffer_copy(prm)
+        p2.rr_start = rr_start
+        dev.materials(mats)
+        dev.diff_forward(head, p2, 1)
+        img = dev.read_accum()[..., :3].astype(np.float64)
+        ga, ge = dev.diff_backward((2.0 * (img - target)).astype(np.float32), nm)
+
+        def loss(m):
+            dev.materials(m)
+            dev.render(head, p2, 1)
+            return float(((dev.read_accum()[..., :3].astype(np.float64) - target) ** 2).sum())
+
+        g_adj, g_fd = [], []
+        for kind, r, c in pick:
+            col = c if kind == "a" else 4 + c
+            mp, mm = mats.copy(), mats.copy()
+            mp[r, col] += 1e-3
+            mm[r, col] -= 1e-3
+            g_fd.append((loss(mp) - loss(mm)) / 2e-3)
+            g_adj.append(ga[r, c] if kind == "a" else ge[r, c])
+        dev.materials(mats)
+        g_adj, g_fd = np.array(g_adj), np.array(g_fd)
+        rel = np.abs(g_adj - g_fd) / np.maximum(np.abs(g_fd), 1e-30)
+        big = np.abs(g_fd) >= 0.01 * np.abs(g_fd).max()
+        return {"rr_start": rr_start,
+                "rel_l2_error": float(np.linalg.norm(g_adj - g_fd) / max(np.linalg.norm(g_fd), 1e-30)),
+                "within_2pct": int((rel <= 0.02).sum()), "params": len(pick),
+                "median_rel_error_significant": float(np.median(rel[big])) if big.any() else None,
+                "max_rel_error_significant": float(rel[big].max()) if big.any() else None}
+
+    fd_rr = fd_check(int(prm.rr_start))
+    fd_smooth = fd_check(int(head.max_bounces))
+    out = {"workload": f"512x512, 32 spp, depth 6, roulette from bounce {int(prm.rr_start)}, {tris:,} tris + "
+                       f"{pk.prim_count} spheres, {nm} material rows ({len(emissive)} emissive)",
+           "params": nm * 3 + len(emissive) * 3,
+           "grad_evals_per_s": 1e3 / (fwd_ms + bwd_ms), "grad_evals_per_s_wall": 1.0 / wall,
+           "forward_ms": fwd_ms, "backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+           "loss": loss0, "fd_check": [fd_rr, fd_smooth],
+           "fd_equivalent_renders_per_eval": 2 * (nm * 3 + len(emissive) * 3)}
+    dev.close()
+    return out
+
+
 def run_reference(args):
     """The reference's CPU implementation of this path is its Slang shader
     (not runnable: no Slang/Vulkan/Metal here) and a reduced Software preview
@@ -302,6 +399,7 @@ def main():
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-views leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-render leg")
     ap.add_argument("--traversal", type=int, default=0, choices=[0, 1],
                     help="0: 4-wide SAH trees built on the device (default); 1: the reference BVHs")
     args = ap.parse_args()
@@ -424,6 +522,10 @@ def main():
     if world == 1 and not args.no_batched:
         dev.close()
         line["batched"] = batched_bench(pt)
+    if world == 1 and not args.no_adjoint:
+        if dev.h:
+            dev.close()
+        line["adjoint"] = adjoint_bench(pt)
     print(json.dumps(line), flush=True)
     if dev.h:
         dev.close()

@@ -86,7 +86,7 @@ class PtPackedScene(ctypes.Structure):
                 ("env_rgba", P(f32)), ("env_w", u32), ("env_h", u32), ("env_marginal", P(f32)),
                 ("env_conditional", P(f32)), ("env_total_luminance", ctypes.c_double),
                 ("hdri_count", u32), ("hdri_dir_pmf", P(f32)), ("hdri_col", P(f32)),
-                ("env_present", u32)]
+                ("env_present", u32), ("prim_mat_ids", P(u32))]
 
 
 # every entry point include/*.h declares, with its ctypes signature
@@ -100,6 +100,7 @@ SIGNATURES = {
     "pt_gpu_upload_mesh": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, P(u32), u32, P(PtBvhNode), u32,
                                           P(u32), u32, P(u32)]),
     "pt_gpu_upload_materials": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
+    "pt_gpu_upload_prim_materials": (ctypes.c_int, [ctypes.c_void_p, P(u32), u32]),
     "pt_gpu_upload_lights": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
     "pt_gpu_upload_env": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32, P(f32), P(f32), P(f32),
                                          P(f32), u32]),
@@ -121,6 +122,10 @@ SIGNATURES = {
     "pt_gpu_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, P(PtBatchTuning)]),
     "pt_gpu_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p), u32, P(PtBatchView), u32,
                                              P(PtBatchTuning)]),
+    "pt_gpu_diff_forward": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32]),
+    "pt_gpu_diff_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            P(ctypes.c_double), P(ctypes.c_double)]),
+    "pt_gpu_diff_get_backward_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtStats)]),
     "pt_gpu_render_noalloc": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32, u32, u32,
                                              ctypes.c_void_p]),
     "pt_gpu_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32,
@@ -136,6 +141,7 @@ SIGNATURES = {
                                            f32, f32, f32, f32]),
     "pt_scene_prim_set_emission": (ctypes.c_int, [ctypes.c_void_p, u32, f32, f32, f32]),
     "pt_scene_prim_set_orient": (ctypes.c_int, [ctypes.c_void_p, u32, f32, f32, f32, f32]),
+    "pt_scene_prim_set_material": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
     "pt_scene_light_quad": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 14),
     "pt_scene_light_point": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 6),
     "pt_scene_light_sphere": (ctypes.c_int, [ctypes.c_void_p, u32] + [f32] * 7),
@@ -252,6 +258,9 @@ class Scene:
 
     def emission(self, id, rgb):
         self._check(self.lib.pt_scene_prim_set_emission(self.h, id, *rgb))
+
+    def prim_material(self, id, mat):
+        self._check(self.lib.pt_scene_prim_set_material(self.h, id, mat))
 
     def orient(self, id, q):
         self._check(self.lib.pt_scene_prim_set_orient(self.h, id, *q))
@@ -435,6 +444,34 @@ class Device:
     def batch_set_tuning(self, persistent_blocks_per_sm=4, stream_blocks_per_sm=8, use_graph=1):
         t = PtBatchTuning(persistent_blocks_per_sm, stream_blocks_per_sm, use_graph, 0)
         self._check(self.lib.pt_gpu_batch_set_tuning(self.h, ctypes.byref(t)))
+
+    # ---- differentiable renders ----
+    def materials(self, mats12):
+        """Replace the material table (n x 12 floats: albedo rgb, roughness,
+        emission rgb, ior, type, 3 pad) -- the differentiable parameters."""
+        m = np.ascontiguousarray(mats12, np.float32).reshape(-1, 12)
+        self._check(self.lib.pt_gpu_upload_materials(self.h, fptr(m), m.shape[0]))
+
+    def diff_forward(self, head, prm, frames=1):
+        self._check(self.lib.pt_gpu_diff_forward(self.h, ctypes.byref(head), ctypes.byref(prm), frames))
+
+    def diff_backward(self, dl_di, nmat):
+        """dl_di: (H, W, 3 or 4) float32 dLoss/dImage.  Returns (grad_albedo,
+        grad_emission), each (nmat, 3) float64."""
+        g = np.zeros((self.H, self.W, 4), np.float32)
+        d = np.asarray(dl_di, np.float32)
+        g[..., :3] = d[..., :3]
+        ga = np.zeros((nmat, 3), np.float64)
+        ge = np.zeros((nmat, 3), np.float64)
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.pt_gpu_diff_backward(self.h, g.ctypes.data, 0, ga.ctypes.data_as(dp),
+                                                  ge.ctypes.data_as(dp)))
+        return ga, ge
+
+    def backward_stats(self) -> PtStats:
+        s = PtStats()
+        self._check(self.lib.pt_gpu_diff_get_backward_stats(self.h, ctypes.byref(s)))
+        return s
 
     def trace(self, ro4, rd4):
         ro4 = np.ascontiguousarray(ro4, np.float32)

@@ -200,6 +200,7 @@ struct DScene {
     uint32_t mesh_has_mat;
     const float4* mats;          // 3 float4 per material
     uint32_t mat_count;
+    const uint32_t* prim_mat;    // extension: material-table row per analytic record (nullable)
     const float4* lights;        // 5 float4 per light
     uint32_t light_count;
     const float4* env;           // W*H texels
@@ -561,6 +562,8 @@ __device__ __forceinline__ HitRec trace_any_mode(const DScene& S, V3 ro, V3 rd, 
 
 // Surface attributes of a hit (the HitInfo fields testAnalyticPrim and the
 // mesh branch fill in, shaders/PathTrace.slang:2101-2146, 2639-2690).
+constexpr uint32_t kNoMat = 0xFFFFFFFFu;
+
 struct Surface {
     V3 normal;
     uint32_t mat;
@@ -568,7 +571,19 @@ struct Surface {
     float rough;
     float ior;
     V3 emission;
+    uint32_t mid;   // material-table row the attributes came from, kNoMat otherwise
 };
+
+__device__ __forceinline__ void table_material(const DScene& S, uint32_t m, Surface& s) {
+    if (m >= S.mat_count) m = S.mat_count - 1u;
+    const float4 m0 = __ldg(S.mats + 3u * m), m1 = __ldg(S.mats + 3u * m + 1u), m2 = __ldg(S.mats + 3u * m + 2u);
+    s.albedo = v3(m0);
+    s.rough = m0.w;
+    s.emission = v3(m1);
+    s.ior = m1.w;
+    s.mat = uint32_t(m2.x);
+    s.mid = m;
+}
 
 __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, HitRec h) {
     Surface s;
@@ -579,16 +594,9 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
         const float4 c = __ldg(T + 3u * slot + 2u);
         s.normal = normalize(cross(v3(b), v3(c)));
         if (S.mesh_has_mat && S.mat_count > 0u) {
-            uint32_t m = __float_as_uint(b.w);
-            if (m >= S.mat_count) m = S.mat_count - 1u;
-            const float4 m0 = __ldg(S.mats + 3u * m), m1 = __ldg(S.mats + 3u * m + 1u),
-                         m2 = __ldg(S.mats + 3u * m + 2u);
-            s.albedo = v3(m0);
-            s.rough = m0.w;
-            s.emission = v3(m1);
-            s.ior = m1.w;
-            s.mat = uint32_t(m2.x);
+            table_material(S, __float_as_uint(b.w), s);
         } else {
+            s.mid = kNoMat;
             s.mat = kMatMetal;
             s.albedo = v3(1.00f, 0.85f, 0.45f);
             s.rough = 0.05f;
@@ -600,14 +608,20 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
         const uint32_t type = __ldg(S.prim_type + h.id);
         if (type == 0u) s.normal = normalize(ro + rd * h.t - v3(g));
         else s.normal = v3(g);
-        const float4 r1 = __ldg(S.prim_rec + 7u * h.id + 1u);
-        const float4 r2 = __ldg(S.prim_rec + 7u * h.id + 2u);
-        const float4 r4 = __ldg(S.prim_rec + 7u * h.id + 4u);
-        s.mat = uint32_t(r2.y);
-        s.albedo = v3(r1);
-        s.rough = r1.w;
-        s.ior = r2.z;
-        s.emission = v3(r4);
+        const uint32_t pm = S.prim_mat ? __ldg(S.prim_mat + h.id) : kNoMat;
+        if (pm != kNoMat && S.mat_count > 0u) {
+            table_material(S, pm, s);
+        } else {
+            const float4 r1 = __ldg(S.prim_rec + 7u * h.id + 1u);
+            const float4 r2 = __ldg(S.prim_rec + 7u * h.id + 2u);
+            const float4 r4 = __ldg(S.prim_rec + 7u * h.id + 4u);
+            s.mat = uint32_t(r2.y);
+            s.albedo = v3(r1);
+            s.rough = r1.w;
+            s.ior = r2.z;
+            s.emission = v3(r4);
+            s.mid = kNoMat;
+        }
     }
     return s;
 }
@@ -693,6 +707,7 @@ struct ShadowIO {
     float4* sh_d;       // direction (w: NEE factor, kept)
     float4* sh_tr;      // transmittance result
     int kmax;
+    uint4* sh_mats;     // adjoint replay: material-table rows of the dielectrics crossed (<= 4), or null
 };
 
 // Batched renders: per-path scene of a queued item (extension rays: item = path;
@@ -724,6 +739,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     V3 trans = v3(1.0f, 1.0f, 1.0f);
     float t_max = 0.0f;
     int seg = 0;
+    uint32_t xm[4] = {kNoMat, kNoMat, kNoMat, kNoMat};   // dielectric rows crossed (adjoint)
 
     auto start_segment = [&]() {
         inv = safe_inv(rd);
@@ -787,6 +803,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                         t_max = o.w;
                         trans = v3(1.0f, 1.0f, 1.0f);
                         seg = 0;
+                        xm[0] = xm[1] = xm[2] = xm[3] = kNoMat;
                     }
                     start_segment();
                     active = true;
@@ -895,6 +912,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                             zero = true;
                         } else {
                             trans = trans * ((1.0f - fr) * sf.albedo);
+                            if (seg < 4) xm[seg] = sf.mid;
                             const float adv = b.t + 1e-3f;
                             ro = ro + rd * adv;
                             rd = normalize(refr);
@@ -908,6 +926,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 }
                 if (finished) {
                     io.sh_tr[item] = f4(trans, 0.0f);
+                    if (io.sh_mats) io.sh_mats[item] = make_uint4(xm[0], xm[1], xm[2], xm[3]);
                     active = false;
                 }
             }

@@ -60,6 +60,17 @@ struct DFrame {
     size_t accum_base;       // first texel of the view in the batch accumulation buffer
 };
 
+// Adjoint replay state (differentiable renders)
+struct Adj {
+    const float4* srad;    // per-sample radiance recorded by the forward pass
+    const float4* dldi;    // dLoss/dI per pixel (rgb)
+    double* grad;          // global: [2][nmat][3] albedo then emission
+    const uint4* sh_mats;  // dielectric rows crossed per shadow slot
+    size_t srec_base;      // srad index of path slot 0 for the current sample
+    uint32_t nmat;
+    float scale;           // 1 / (frames * spp)
+};
+
 // Batched renders: device tables of per-view frame constants and per-scene
 // descriptors; every path records its view and scene.
 struct Batch {
@@ -91,6 +102,7 @@ struct DPaths {
     uint32_t* q[2];
     uint32_t* sq;
     uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue, [3] fetch counter
+    float4* srad;      // differentiable renders: radiance of every sample [s * npaths + p], or null
     unsigned long long* stat;   // [0] extension rays, [1] shadow segments
 };
 
@@ -510,14 +522,46 @@ __device__ __forceinline__ void issue_shadow(const DPaths& P, uint32_t p, int k,
 }
 
 // one bounce of the loop body (shaders/PathTrace.slang:5921-6914)
-template <bool kB>
+// Differentiable replay: per-block double accumulators of the parameter
+// gradients in dynamic shared memory ([2][nmat][3]: albedo, emission), flushed
+// to the global gradient once per block.
+extern __shared__ double s_grad[];
+
+__device__ __forceinline__ void adj_begin(const Adj& A) {
+    for (uint32_t i = threadIdx.x; i < 6u * A.nmat; i += blockDim.x) s_grad[i] = 0.0;
+    __syncthreads();
+}
+__device__ __forceinline__ void adj_end(const Adj& A) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < 6u * A.nmat; i += blockDim.x)
+        if (s_grad[i] != 0.0) atomicAdd(A.grad + i, s_grad[i]);
+}
+__device__ __forceinline__ void adj_add(const Adj& A, int which, uint32_t m, V3 v) {
+    double* g = s_grad + (size_t(which) * A.nmat + m) * 3u;
+    atomicAdd(g + 0, double(v.x));
+    atomicAdd(g + 1, double(v.y));
+    atomicAdd(g + 2, double(v.z));
+}
+// dLoss/d(sample radiance) of path p: dL/dI of its pixel times 1/(frames*spp)
+__device__ __forceinline__ V3 adj_weight(const Adj& A, const DFrame& F, uint32_t p) {
+    const uint32_t f = p / F.npix, pix = p - f * F.npix;
+    uint32_t x, y;
+    slot_pixel(F, pix, x, y);
+    return v3(A.dldi[size_t(y) * F.W + x]) * A.scale;
+}
+__device__ __forceinline__ V3 safe_div(V3 a, V3 b) {
+    return v3(b.x > 0.0f ? a.x / b.x : 0.0f, b.y > 0.0f ? a.y / b.y : 0.0f, b.z > 0.0f ? a.z / b.z : 0.0f);
+}
+
+template <bool kB, bool kAdj>
 __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DScene S0,
                                                      const __grid_constant__ DFrame F0, DPaths P, Batch B,
-                                                     int qsel, uint32_t b) {
+                                                     const __grid_constant__ Adj A, int qsel, uint32_t b) {
     const uint32_t n = P.cnt[qsel];
     const uint32_t* q = P.q[qsel];
     uint32_t* qn = P.q[qsel ^ 1];
     const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
+    if (kAdj) adj_begin(A);
     for (uint32_t it = 0; it < n_iter; ++it) {
         const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
         bool cont = false;
@@ -555,6 +599,18 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
                 if (any_pos(sf.emission)) {
                     if (b == 0u) rad = rad + thr * sf.emission;
                     else rad = rad + clamp_ind(thr * sf.emission, F.firefly);
+                }
+                if (kAdj && sf.mid != kNoMat) {
+                    // emission term thr*E: d/dE = thr; albedo factor of this vertex
+                    // scales everything the path collects after its emission
+                    // (this vertex's NEE through the brdf, later vertices through
+                    // the throughput): d/da = (R_total - R_so_far) / a
+                    const V3 g = adj_weight(A, F, p);
+                    if (any_pos(sf.emission)) adj_add(A, 1, sf.mid, g * thr);
+                    if (sf.mat == kMatLambert || sf.mat == kMatMetal) {
+                        const V3 total = v3(A.srad[A.srec_base + p]);
+                        adj_add(A, 0, sf.mid, g * safe_div(total - rad, sf.albedo));
+                    }
                 }
                 if (sf.mat == kMatLambert) {
                     const V3 so = hp + nf * 1e-3f;
@@ -667,6 +723,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
             if (has) P.sq[ss] = 3u * p + uint32_t(k);
         }
     }
+    if (kAdj) adj_end(A);
 }
 
 template <bool kWide>
@@ -700,9 +757,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_closest(const __grid_constant__
 // counted as a shadow segment)
 template <bool kB>
 __global__ void __launch_bounds__(kThreads, 4) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
-                                                          int kmax) {
+                                                          int kmax, uint4* sh_mats) {
     uint32_t done = 0;
-    const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax};
+    const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax, sh_mats};
     persistent_closest<true, kB>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
                                  nullptr, P.cnt + 3, done, io);
     warp_add(P.stat + 1, done);
@@ -710,11 +767,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_transmit(const __grid_constant_
 
 // NEE terms in the reference order (light, env, HDRI), then the sample's
 // radiance for paths that ended (shaders/PathTrace.slang:6341-6520, 7701).
-template <bool kB>
-__global__ void k_resolve(const __grid_constant__ DFrame F0, DPaths P, Batch B, int qsel) {
+template <bool kB, bool kAdj>
+__global__ void k_resolve(const __grid_constant__ DScene S0, const __grid_constant__ DFrame F0, DPaths P, Batch B,
+                          const __grid_constant__ Adj A, int qsel, size_t srec_base) {
     const uint32_t n = P.cnt[qsel];
     const uint32_t* q = P.q[qsel];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
+    if (kAdj) adj_begin(A);
+    for (uint32_t it = 0; it < n_iter; ++it) {
+        const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        if (i >= n) continue;
         const uint32_t p = q[i];
         const DFrame& F = kB ? B.views[B.path_view[p]] : F0;
         const uint32_t mask = P.shmask[p];
@@ -731,13 +793,25 @@ __global__ void k_resolve(const __grid_constant__ DFrame F0, DPaths P, Batch B, 
             const float s1 = P.sh_d[e].w;
             const V3 c = v3(pre) * tr * v3(br) * s1 * pre.w / br.w;
             rad = rad + (((mask >> (4 + k)) & 1u) ? clamp_ind(c, F.firefly) : c);
+            if (kAdj) {   // each dielectric the shadow ray crossed multiplied c by its albedo
+                const uint4 xm = A.sh_mats[e];
+                const uint32_t ms[4] = {xm.x, xm.y, xm.z, xm.w};
+                const V3 g = adj_weight(A, F, p);
+                for (int j = 0; j < 4; ++j) {
+                    if (ms[j] == kNoMat) continue;
+                    const uint32_t m = min(ms[j], S0.mat_count - 1u);
+                    adj_add(A, 0, m, g * safe_div(c, v3(__ldg(S0.mats + 3u * m))));
+                }
+            }
         }
         if (mask) P.rad[p] = f4(rad, 0.0f);
         if (st & kEnded) {
             const float4 fs = P.fsum[p];
             P.fsum[p] = make_float4(fs.x + rad.x, fs.y + rad.y, fs.z + rad.z, 0.0f);
+            if (P.srad) P.srad[srec_base + p] = f4(rad, 0.0f);
         }
     }
+    if (kAdj) adj_end(A);
 }
 
 // running mean / EMA (shaders/PathTrace.slang:7707-7781)
@@ -823,7 +897,8 @@ struct pt_gpu_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // scene
     DBuf<float4> prim_rec, prim_geo, bvh, tri, tri_bvh, mats, lights, env;
-    DBuf<uint32_t> prim_type;
+    DBuf<uint32_t> prim_type, prim_mat;
+    bool has_prim_mat = false;
     DBuf<float> marg, cond;
     uint32_t prim_count = 0, linear_count = 0, bvh_nodes = 0, tri_slots = 0, tri_nodes = 0, tri_count = 0;
     uint32_t mat_count = 0, light_count = 0, env_w = 0, env_h = 0, hdri_count = 0;
@@ -859,6 +934,17 @@ struct pt_gpu_ctx {
     cudaGraphExec_t b_graph = nullptr;
     std::vector<uint64_t> b_sig;
     PtBatchTuning b_tune{4u, 8u, 1u, 0u};
+    // differentiable renders: the recorded forward and the replay's buffers
+    DBuf<float4> d_srad, d_dldi;
+    DBuf<double> d_grad;
+    DBuf<uint4> d_sh_mats;
+    bool d_valid = false;
+    uint64_t d_gen = 0;
+    PtPushHead d_head{};
+    PtPathParams d_prm{};
+    uint32_t d_frames = 0;
+    uint64_t gen = 0;   // bumped by every upload / target change
+    PtStats d_bwd_stats{};
     PtStats stats{};
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -939,6 +1025,7 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     S.mesh_has_mat = c->mesh_has_mat ? 1u : 0u;
     S.mats = c->mats.p;
     S.mat_count = c->mat_count;
+    S.prim_mat = c->has_prim_mat ? c->prim_mat.p : nullptr;
     S.lights = c->lights.p;
     S.light_count = c->light_count;
     S.env = c->env.p;
@@ -1251,6 +1338,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
                     &ctx->rad, &ctx->fsum, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
                     &ctx->sh_tr})
         dfree(*b);
+    dfree(ctx->prim_mat);
     for (auto* b : {&ctx->prim_type, &ctx->seed, &ctx->state, &ctx->hit_id, &ctx->shmask, &ctx->q0,
                     &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word})
         dfree(*b);
@@ -1279,6 +1367,7 @@ const char* pt_gpu_last_error(const pt_gpu_ctx* ctx) { return ctx ? ctx->err.c_s
 
 int pt_gpu_upload_prims(pt_gpu_ctx* ctx, const float* recs28, uint32_t n, uint32_t linear_count,
                         const PtBvhNode* nodes, uint32_t n_nodes) {
+    if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
     if ((n && !recs28) || (n_nodes && !nodes) || linear_count > n)
         return set_err(ctx, PT_ERR_INVALID, "upload_prims: bad arguments");
@@ -1304,6 +1393,7 @@ int pt_gpu_upload_prims(pt_gpu_ctx* ctx, const float* recs28, uint32_t n, uint32
 int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv, const uint32_t* indices,
                        uint32_t nt, const PtBvhNode* nodes, uint32_t n_nodes, const uint32_t* perm,
                        uint32_t n_perm, const uint32_t* mat_ids) {
+    if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
     if ((nv && !positions) || (nt && !indices) || (n_nodes && !nodes) || (n_perm && !perm))
         return set_err(ctx, PT_ERR_INVALID, "upload_mesh: null buffer");
@@ -1359,6 +1449,7 @@ int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv, con
 }
 
 int pt_gpu_upload_materials(pt_gpu_ctx* ctx, const float* mats12, uint32_t n) {
+    if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
     if (n && !mats12) return set_err(ctx, PT_ERR_INVALID, "upload_materials: null buffer");
     int rc = dupload(ctx, ctx->mats, mats12, size_t(n) * 3);
@@ -1368,7 +1459,24 @@ int pt_gpu_upload_materials(pt_gpu_ctx* ctx, const float* mats12, uint32_t n) {
     return PT_OK;
 }
 
+int pt_gpu_upload_prim_materials(pt_gpu_ctx* ctx, const uint32_t* mat_ids, uint32_t n) {
+    if (ctx) ctx->gen++;
+    if (!ctx) return PT_ERR_INVALID;
+    if (!mat_ids || n == 0) {
+        ctx->has_prim_mat = false;
+        return PT_OK;
+    }
+    if (n != ctx->prim_count)
+        return set_err(ctx, PT_ERR_INVALID, "upload_prim_materials: count differs from the uploaded records");
+    int rc = dupload(ctx, ctx->prim_mat, mat_ids, n);
+    if (rc) return rc;
+    ctx->has_prim_mat = true;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
 int pt_gpu_upload_lights(pt_gpu_ctx* ctx, const float* recs20, uint32_t n) {
+    if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
     if (n && !recs20) return set_err(ctx, PT_ERR_INVALID, "upload_lights: null buffer");
     int rc = dupload(ctx, ctx->lights, recs20, size_t(n) * 5);
@@ -1381,6 +1489,7 @@ int pt_gpu_upload_lights(pt_gpu_ctx* ctx, const float* recs20, uint32_t n) {
 int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H, const float* marginal,
                       const float* conditional, const float* hdri_dir_pmf, const float* hdri_col,
                       uint32_t n_hdri) {
+    if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
     if (n_hdri > 8) return set_err(ctx, PT_ERR_INVALID, "upload_env: at most 8 HDRI lights");
     if ((W || H) && (!rgba || !marginal || !conditional || W == 0 || H == 0))
@@ -1404,6 +1513,7 @@ int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H
 }
 
 int pt_gpu_set_target(pt_gpu_ctx* ctx, uint32_t width, uint32_t height) {
+    if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
     if (width == 0 || height == 0 || uint64_t(width) * height > (1ull << 28))
         return set_err(ctx, PT_ERR_INVALID, "set_target: bad size");
@@ -1447,7 +1557,22 @@ int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave) {
     return PT_OK;
 }
 
-int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm, uint32_t frames) {
+}  // extern "C"
+
+namespace {
+
+// What a run of waves does besides rendering: record every sample's radiance
+// (forward half of a differentiable render) or replay the recorded paths and
+// accumulate parameter gradients instead of the image (backward half).
+enum class RunMode { kRender, kRecord, kAdjoint };
+struct DiffRun {
+    RunMode mode = RunMode::kRender;
+    const float4* dldi = nullptr;
+    uint32_t nmat = 0;
+};
+
+int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm, uint32_t frames,
+                 const DiffRun& dr) {
     if (!ctx || !head || !prm) return PT_ERR_INVALID;
     if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "render: no target (pt_gpu_set_target)");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: tlas_present (hardware RT) has no CUDA path");
@@ -1507,6 +1632,38 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
     const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
     const int gpers = ctx->sm_count * 4;
+    const bool adj = dr.mode == RunMode::kAdjoint;
+    const size_t total_paths = size_t(frames) * F.npix;
+    size_t smem = 0;
+    if (dr.mode != RunMode::kRender) {
+        if (!persistent)
+            return set_err(ctx, PT_ERR_UNSUPPORTED, "differentiable render: needs the wide trees (traversal mode 0)");
+        rc = dalloc(ctx, ctx->d_srad, size_t(F.spp) * total_paths);
+        if (rc) return rc;
+    }
+    if (adj) {
+        rc = dalloc(ctx, ctx->d_sh_mats, 3 * size_t(fpw) * F.npix);
+        if (rc) return rc;
+        rc = dalloc(ctx, ctx->d_grad, 6 * size_t(dr.nmat));
+        if (rc) return rc;
+        CK(cudaMemsetAsync(ctx->d_grad.p, 0, 6 * size_t(dr.nmat) * sizeof(double), ctx->stream));
+        smem = 6 * size_t(dr.nmat) * sizeof(double);
+        if (smem > 48u * 1024u) {
+            CK(cudaFuncSetAttribute(k_shade<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            CK(cudaFuncSetAttribute(k_resolve<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        }
+    }
+    P.srad = (dr.mode == RunMode::kRecord) ? ctx->d_srad.p : nullptr;
+    Adj A{};
+    if (adj) {
+        A.srad = ctx->d_srad.p;
+        A.dldi = dr.dldi;
+        A.grad = ctx->d_grad.p;
+        A.sh_mats = ctx->d_sh_mats.p;
+        A.nmat = dr.nmat;
+        A.scale = 1.0f / float(double(frames) * double(F.spp));
+    }
+    const int gadj = ctx->sm_count * 4;
 
     CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
@@ -1520,8 +1677,10 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
         F.frame_index0 = head->frame_index + f0;
         const int gp = (npaths + 255) / 256;
         k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
-        ctx->stats.kernel_launches += 2;   // init + accumulate
+        ctx->stats.kernel_launches += adj ? 1 : 2;   // init (+ accumulate)
         for (uint32_t s = 0; s < F.spp; ++s) {
+            const size_t srec = size_t(s) * total_paths + size_t(f0) * F.npix;
+            A.srec_base = srec;
             k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
@@ -1541,24 +1700,35 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
                     k_extend<false><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
                 }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                k_shade<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, qs, b);
+                if (adj)
+                    k_shade<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, b);
+                else
+                    k_shade<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                                                                                                  Adj{}, qs, b);
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
-                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax);
+                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
+                                                                           adj ? ctx->d_sh_mats.p : nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                k_resolve<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, Batch{}, qs);
+                if (adj)
+                    k_resolve<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, srec);
+                else
+                    k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                                                                                                    Adj{}, qs, srec);
                 ctx->stats.extend_launches++;
                 ctx->stats.shadow_launches++;
             }
         }
-        k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf,
-                                                                   f0 == 0 && head->reset_accum != 0u, prm->accum_ema_alpha);
+        if (!adj)
+            k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf,
+                                                                       f0 == 0 && head->reset_accum != 0u,
+                                                                       prm->accum_ema_alpha);
         ctx->stats.waves++;
         ctx->stats.paths += uint64_t(npaths) * F.spp;
     }
@@ -1591,6 +1761,77 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
     return PT_OK;
 }
 
+
+}  // namespace
+
+extern "C" {
+
+int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm, uint32_t frames) {
+    return render_waves(ctx, head, prm, frames, DiffRun{});
+}
+
+int pt_gpu_diff_forward(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm, uint32_t frames) {
+    if (!ctx || !head || !prm) return PT_ERR_INVALID;
+    ctx->d_valid = false;
+    if (frames == 0) return set_err(ctx, PT_ERR_INVALID, "diff_forward: frames == 0");
+    if (ctx->mat_count == 0) return set_err(ctx, PT_ERR_STATE, "diff_forward: no material table (the parameters)");
+    if (prm->firefly_clamp > 0.0f)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, "diff_forward: the firefly clamp is not differentiable (set it to 0)");
+    if (prm->refract_budget > 4u)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, "diff_forward: refract budget above 4");
+    if (head->reset_accum == 0u || prm->accum_ema_alpha > 0.0f)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, "diff_forward: needs reset_accum and no EMA (image = mean of the samples)");
+    if (ctx->mat_count > 4096u) return set_err(ctx, PT_ERR_UNSUPPORTED, "diff_forward: more than 4096 materials");
+    DiffRun dr;
+    dr.mode = RunMode::kRecord;
+    const int rc = render_waves(ctx, head, prm, frames, dr);
+    if (rc) return rc;
+    ctx->d_valid = true;
+    ctx->d_gen = ctx->gen;
+    ctx->d_head = *head;
+    ctx->d_prm = *prm;
+    ctx->d_frames = frames;
+    return PT_OK;
+}
+
+int pt_gpu_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_device, double* grad_albedo,
+                         double* grad_emission) {
+    if (!ctx || !dl_di_rgba) return PT_ERR_INVALID;
+    if (!ctx->d_valid) return set_err(ctx, PT_ERR_STATE, "diff_backward: no recorded forward (pt_gpu_diff_forward)");
+    if (ctx->d_gen != ctx->gen)
+        return set_err(ctx, PT_ERR_STATE, "diff_backward: the scene or target changed since the recorded forward");
+    const size_t npix = size_t(ctx->W) * ctx->H;
+    const float4* dldi = reinterpret_cast<const float4*>(dl_di_rgba);
+    if (!on_device) {
+        int rc = dupload(ctx, ctx->d_dldi, dl_di_rgba, npix);
+        if (rc) return rc;
+        dldi = ctx->d_dldi.p;
+    } else if ((reinterpret_cast<uintptr_t>(dl_di_rgba) & 15u) != 0u) {
+        return set_err(ctx, PT_ERR_INVALID, "diff_backward: device dL/dI must be 16-byte aligned");
+    }
+    DiffRun dr;
+    dr.mode = RunMode::kAdjoint;
+    dr.dldi = dldi;
+    dr.nmat = ctx->mat_count;
+    const PtStats keep = ctx->stats;
+    const int rc = render_waves(ctx, &ctx->d_head, &ctx->d_prm, ctx->d_frames, dr);
+    if (rc) return rc;
+    ctx->d_bwd_stats = ctx->stats;
+    ctx->stats = keep;
+    std::vector<double> g(6 * size_t(ctx->mat_count));
+    CK(cudaMemcpy(g.data(), ctx->d_grad.p, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const size_t n3 = 3 * size_t(ctx->mat_count);
+    if (grad_albedo) std::memcpy(grad_albedo, g.data(), n3 * sizeof(double));
+    if (grad_emission) std::memcpy(grad_emission, g.data() + n3, n3 * sizeof(double));
+    return PT_OK;
+}
+
+int pt_gpu_diff_get_backward_stats(pt_gpu_ctx* ctx, PtStats* out) {
+    if (!ctx || !out) return PT_ERR_INVALID;
+    *out = ctx->d_bwd_stats;
+    return PT_OK;
+}
+
 int pt_gpu_render_to_host(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
                           uint32_t frames, float* host_rgba) {
     int rc = pt_gpu_render(ctx, head, params, frames);
@@ -1605,6 +1846,7 @@ int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out) {
 }
 
 int pt_gpu_set_traversal(pt_gpu_ctx* ctx, int mode) {
+    if (ctx) ctx->gen++;
     if (!ctx || mode < 0 || mode > 1) return PT_ERR_INVALID;
     ctx->traversal = mode;
     return PT_OK;
@@ -1760,10 +2002,10 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
             CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
             k_closest<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
                                                                  P.hit_t, P.hit_id, P.cnt + 3, P.stat);
-            k_shade<true><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, qs, b);
+            k_shade<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
             CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-            k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any);
-            k_resolve<true><<<gstream, kThreads, 0, ctx->stream>>>(F0, P, Bt, qs);
+            k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
+            k_resolve<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, 0);
         }
     }
     k_accumulate_batch<<<gp, 256, 0, ctx->stream>>>(P, Bt, npaths);
@@ -2160,16 +2402,18 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                 } else {
                     k_extend<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
                 }
-                k_shade<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, qs, b);
+                k_shade<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
+                                                                                              qs, b);
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax);
+                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 }
-                k_resolve<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(F, P, Batch{}, qs);
+                k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
+                                                                                                qs, 0);
                 ctx->stats.extend_launches++;
                 ctx->stats.shadow_launches++;
             }

@@ -402,6 +402,7 @@ struct Prim {
     float emission[3] = {0, 0, 0};
     float orient[4] = {0, 0, 0, 1};
     uint32_t tex[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    uint32_t mat_id = 0xFFFFFFFFu;   // extension: material-table row
 };
 
 struct Light {
@@ -452,6 +453,8 @@ struct pt_scene {
     // packed state
     bool dirty_prims = true, dirty_mesh = true, dirty_lights = true, dirty_env = true;
     std::vector<float> packed_prims;
+    std::vector<uint32_t> packed_prim_mats;
+    bool any_prim_mat = false;
     uint32_t linear_count = 0;
     std::vector<PtBvhNode> bvh;
     std::vector<PtBvhNode> tri_bvh;
@@ -516,6 +519,11 @@ void pack_prims(pt_scene* s) {
     };
     for (size_t i = 0; i < inf.size(); ++i) pack(i, *inf[i].p, inf[i].id);
     for (size_t i = 0; i < order.size(); ++i) pack(s->linear_count + i, *fin[order[i]].p, fin[order[i]].id);
+    s->packed_prim_mats.assign(count, 0xFFFFFFFFu);
+    s->any_prim_mat = false;
+    for (size_t i = 0; i < inf.size(); ++i) s->packed_prim_mats[i] = inf[i].p->mat_id;
+    for (size_t i = 0; i < order.size(); ++i) s->packed_prim_mats[s->linear_count + i] = fin[order[i]].p->mat_id;
+    for (uint32_t m : s->packed_prim_mats) s->any_prim_mat = s->any_prim_mat || (m != 0xFFFFFFFFu);
     s->dirty_prims = false;
 }
 
@@ -746,6 +754,86 @@ void synth_c0(pt_scene* s, uint64_t seed, double scale) {
     set_cv(s, "r_light_tree", 0);
 }
 
+// Differentiable-render scene: the analytic scene above grown to 512 spheres
+// in [-20,20]^3 plus ~200k triangles (20 displaced icospheres of 9,680
+// triangles, 4 boxes and a 56x56-quad floor), all on a 256-row material table
+// drawn like the analytic scene's materials; 16 rows (every 16th) are
+// emissive Lambert rows.  512x512, 32 spp, depth 6, roulette from bounce 3,
+// no firefly clamp.
+void synth_c3(pt_scene* s, uint64_t seed, double scale) {
+    Pcg32 rng(0x5EEDull + 3ull, seed);
+    const double lin = std::sqrt(scale);
+    std::vector<float> mats;
+    for (uint32_t i = 0; i < 256; ++i) {
+        MatDraw m = draw_material(rng);
+        if (i % 16u == 0u) m.type = 0;
+        if (m.type == 0 && m.albedo[0] == 1.0f) m.albedo[0] = m.albedo[1] = m.albedo[2] = 0.5f;
+        push_material(mats, m);
+        if (i % 16u == 0u) {
+            for (int a = 0; a < 3; ++a) {
+                float& al = mats[mats.size() - 12 + a];
+                if (al > 0.95f) al = rng.range(0.05f, 0.95f);
+                mats[mats.size() - 12 + 4 + a] = rng.range(1.0f, 4.0f);
+            }
+        }
+    }
+    const uint32_t n_spheres = std::max<uint32_t>(1, uint32_t(std::lround(512 * scale)));
+    for (uint32_t i = 0; i < n_spheres; ++i) {
+        const float cx = rng.range(-20, 20), cy = rng.range(-20, 20), cz = rng.range(-20, 20);
+        const float r = float(0.2 * std::pow(10.0, double(rng.unit())));
+        const uint32_t row = std::min<uint32_t>(uint32_t(rng.unit() * 256.0f), 255u);
+        const float* m = mats.data() + 12 * size_t(row);
+        pt_scene_prim_sphere(s, 1 + i, cx, cy, cz, r, int(m[8]), m[0], m[1], m[2], m[3], m[7]);
+        pt_scene_prim_set_material(s, 1 + i, row);
+    }
+    std::vector<float> pos;
+    std::vector<uint32_t> idx, mid;
+    const uint32_t n_ico = std::max<uint32_t>(1, uint32_t(std::lround(20 * scale)));
+    const uint32_t nu = std::max<uint32_t>(2, uint32_t(std::lround(22 * lin)));
+    for (uint32_t k = 0; k < n_ico; ++k) {
+        const float r = rng.range(1.5f, 3.5f);
+        const float c[3] = {rng.range(-16, 16), rng.range(-16, 16), rng.range(-16, 16)};
+        const uint32_t row = std::min<uint32_t>(uint32_t(rng.unit() * 256.0f), 255u);
+        add_icosphere(pos, idx, mid, c, r, nu, 0.1f, 3000u + 7u * k, row);
+    }
+    for (uint32_t b = 0; b < 4; ++b) {
+        const float h[3] = {rng.range(0.5f, 3.0f), rng.range(0.5f, 3.0f), rng.range(0.5f, 3.0f)};
+        const float c[3] = {rng.range(-20, 20), rng.range(-20, 20), rng.range(-20, 20)};
+        add_box(pos, idx, mid, c, h, std::min<uint32_t>(uint32_t(rng.unit() * 256.0f), 255u));
+    }
+    const uint32_t grid = std::max<uint32_t>(2, uint32_t(std::lround(56 * lin)));
+    const uint32_t floor_row = 1;
+    const uint32_t fb = uint32_t(pos.size() / 3);
+    for (uint32_t j = 0; j <= grid; ++j)
+        for (uint32_t i = 0; i <= grid; ++i) {
+            pos.push_back(-25.0f + 50.0f * float(i) / float(grid));
+            pos.push_back(-20.5f);
+            pos.push_back(-25.0f + 50.0f * float(j) / float(grid));
+        }
+    for (uint32_t j = 0; j < grid; ++j)
+        for (uint32_t i = 0; i < grid; ++i) {
+            const uint32_t a = fb + j * (grid + 1) + i, b = a + 1, c = a + grid + 1, d = c + 1;
+            idx.insert(idx.end(), {a, c, b, b, c, d});
+            mid.push_back(floor_row);
+            mid.push_back(floor_row);
+        }
+    pt_scene_set_materials(s, mats.data(), uint32_t(mats.size() / 12));
+    pt_scene_set_mesh(s, pos.data(), uint32_t(pos.size() / 3), idx.data(), uint32_t(idx.size() / 3),
+                      mid.data());
+    pt_scene_light_quad(s, 1, 0, 24, 0, 0, -1, 0, 1, 0, 0, 0.5f, 0.5f, 15, 15, 15);
+    std::vector<float> black(8 * 4 * 3, 0.0f);
+    pt_scene_set_env(s, black.data(), 8, 4);
+    pt_scene_set_camera(s, 0, 0, 56, 0, 0, 45);
+    set_cv(s, "r_max_bounces", 6);
+    set_cv(s, "r_spp", 32);
+    set_cv(s, "r_rr_start", 3);
+    set_cv(s, "r_mis", 1);
+    set_cv(s, "r_caustics", 1);
+    set_cv(s, "r_refract_bounces", 4);
+    set_cv(s, "r_firefly_clamp", 0);
+    set_cv(s, "r_light_tree", 0);
+}
+
 void synth_c1(pt_scene* s, uint64_t seed, double scale) {
     Pcg32 rng(0x5EEDull + 1ull, seed);
     const double lin = std::sqrt(scale);
@@ -908,6 +996,15 @@ int pt_scene_prim_set_orient(pt_scene* s, uint32_t id, float qx, float qy, float
     if (it == s->prims.end()) return fail(s, "prim_set_rotation: unknown id");
     it->second.orient[0] = qx; it->second.orient[1] = qy;
     it->second.orient[2] = qz; it->second.orient[3] = qw;
+    s->dirty_prims = true;
+    return PT_OK;
+}
+
+int pt_scene_prim_set_material(pt_scene* s, uint32_t id, uint32_t mat) {
+    if (!s) return PT_ERR_INVALID;
+    auto it = s->prims.find(id);
+    if (it == s->prims.end()) return fail(s, "prim_set_material: unknown id");
+    it->second.mat_id = mat;
     s->dirty_prims = true;
     return PT_OK;
 }
@@ -1097,6 +1194,7 @@ int pt_scene_packed(pt_scene* s, PtPackedScene* o) {
     o->hdri_count = uint32_t(s->hdri.size());
     o->hdri_dir_pmf = s->hdri_dir;
     o->hdri_col = s->hdri_col;
+    o->prim_mat_ids = s->any_prim_mat ? s->packed_prim_mats.data() : nullptr;
     return PT_OK;
 }
 
@@ -1176,6 +1274,7 @@ int pt_scene_synth(pt_scene* s, int config_id, uint64_t seed, double scale) {
     pt_scene_clear(s);
     if (config_id == 0) synth_c0(s, seed, scale);
     else if (config_id == 1) synth_c1(s, seed, scale);
+    else if (config_id == 3) synth_c3(s, seed, scale);
     else return fail(s, "synth: unknown config id");
     return pt_scene_pack(s);
 }
@@ -1188,6 +1287,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx) {
                                  p.bvh_node_count);
     if (rc) return rc;
     rc = pt_gpu_upload_materials(ctx, p.materials, p.material_count);
+    if (rc) return rc;
+    rc = pt_gpu_upload_prim_materials(ctx, p.prim_mat_ids, p.prim_mat_ids ? p.prim_count : 0);
     if (rc) return rc;
     rc = pt_gpu_upload_mesh(ctx, p.positions, p.vertex_count, p.indices, p.tri_count, p.tri_nodes,
                             p.tri_node_count, p.tri_perm, p.tri_perm_count, p.tri_mat_ids);

@@ -141,6 +141,10 @@ int pt_gpu_upload_mesh(pt_gpu_ctx* ctx, const float* positions, uint32_t nv,
  * mats: n records of 12 floats: albedo rgb, roughness, emission rgb, ior,
  *       material type (0 Lambert, 1 metal, 2 dielectric) as float, 3 pad. */
 int pt_gpu_upload_materials(pt_gpu_ctx* ctx, const float* mats12, uint32_t n);
+/* Extension: per analytic record (n == uploaded record count), the material
+ * table row it takes albedo / roughness / ior / emission / type from
+ * (0xFFFFFFFF = its own record).  NULL, 0 clears. */
+int pt_gpu_upload_prim_materials(pt_gpu_ctx* ctx, const uint32_t* mat_ids, uint32_t n);
 
 /* ---- analytic lights (replaces Engine::EnsureLightsUploaded, src/engine/Engine.cpp:5235-5330,
  *      slot 27): n records of 20 floats (5 float4) in the reference packing. ---- */
@@ -234,6 +238,37 @@ int pt_gpu_batch_get_tuning(pt_gpu_ctx* ctx, PtBatchTuning* tuning);
  * keeps the fastest.  Writes the choice to *chosen (nullable). */
 int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes,
                           const PtBatchView* views, uint32_t n_views, PtBatchTuning* chosen);
+
+/* ---- differentiable render (extension: path-replay adjoint) ----
+ * The reference has no derivative path; these two calls are shaped like the
+ * forward/backward of a torch.autograd.Function whose inputs are the material
+ * table (pt_gpu_upload_materials: per-row albedo and emission) and whose output
+ * is the accumulation image.
+ *
+ * pt_gpu_diff_forward renders exactly like pt_gpu_render (same image, bit for
+ * bit) and also records the radiance of every sample (16 B per pixel, frame
+ * and sample).  It needs head.reset_accum != 0 and no EMA (the image is the
+ * mean of the samples), firefly_clamp <= 0 (the clamp is not differentiable),
+ * refract_budget <= 4, a material table of at most 4096 rows, and traversal
+ * mode 0.
+ *
+ * pt_gpu_diff_backward takes dLoss/dImage (width*height RGBA floats, .a
+ * ignored; on_device != 0: a 16-byte aligned device pointer) and replays the
+ * recorded paths from their stored seeds -- nothing per vertex is stored -- to
+ * produce dLoss/d(albedo) and dLoss/d(emission) per material row (3 doubles a
+ * row each, nullable).  Per path vertex the albedo factor scales everything the
+ * path collects after that vertex's emission, so its derivative is
+ * (sample radiance - radiance so far) / albedo; emission's is the throughput;
+ * a dielectric crossed by a visible shadow ray contributes that NEE term over
+ * its albedo.  Russian-roulette survival probabilities are held fixed (an
+ * unbiased gradient of the expected image).  Uploads or a target change after
+ * the forward invalidate it (PT_ERR_STATE). */
+int pt_gpu_diff_forward(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
+                        uint32_t frames);
+int pt_gpu_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_device,
+                         double* grad_albedo, double* grad_emission);
+/* PtStats of the last backward replay (pt_gpu_get_stats keeps the forward's). */
+int pt_gpu_diff_get_backward_stats(pt_gpu_ctx* ctx, PtStats* out);
 
 /* ---- allocation-free render (no counterpart in the reference) ----
  * For callers that must not allocate device memory while rendering: an engine

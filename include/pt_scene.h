@@ -51,6 +51,10 @@ int pt_scene_prim_plane(pt_scene* s, uint32_t id, float nx, float ny, float nz, 
 /* per-prim emission (W/sr per channel) and orientation quaternion (xyzw) */
 int pt_scene_prim_set_emission(pt_scene* s, uint32_t id, float r, float g, float b);
 int pt_scene_prim_set_orient(pt_scene* s, uint32_t id, float qx, float qy, float qz, float qw);
+/* Extension: make the prim take albedo, roughness, ior, emission and material
+ * type from row `mat` of the material table (the differentiable parameters);
+ * 0xFFFFFFFF restores the prim's own record values. */
+int pt_scene_prim_set_material(pt_scene* s, uint32_t id, uint32_t mat);
 
 /* light_quad <id> <x y z> <nx ny nz> <ux uy uz> <u_half> <v_half> <r g b>
  * (src/engine/Engine.cpp:20403-20450) */
@@ -121,6 +125,7 @@ typedef struct PtPackedScene {
     const float*     hdri_dir_pmf;  /* 8 float4 */
     const float*     hdri_col;      /* 8 float4 */
     uint32_t         env_present;
+    const uint32_t*  prim_mat_ids;  /* per packed record, NULL when no prim uses the table */
 } PtPackedScene;
 int pt_scene_packed(pt_scene* s, PtPackedScene* out);
 
@@ -134,7 +139,10 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
 /* Seeded synthetic scenes (PCG32 stream, seed 0x5EED + config id):
  *   0: 64 spheres + 4 boxes (12-tri meshes) + one 1x1 quad light (radiance 15), black env;
  *   1: 200 displaced icospheres (nu = 22, 9680 tris each) on a 512x512 quad-grid ground,
- *      1024 spheres, 2048x1024 log-normal env with a 0.5 deg sun disc of 1e4, 256 materials.
+ *      1024 spheres, 2048x1024 log-normal env with a 0.5 deg sun disc of 1e4, 256 materials;
+ *   3: differentiable-render scene: 512 spheres in [-20,20]^3 and ~200k triangles (20
+ *      icospheres, 4 boxes, a 56x56-quad floor) on a 256-row material table of which 16
+ *      rows are emissive, the 1x1 quad light, black env; 32 spp, depth 6, no firefly clamp.
  * scale (0 < scale <= 1) shrinks the triangle/sphere/env counts for fast tests
  * (1 = the full configuration).  Sets the camera and cvars of the config. */
 int pt_scene_synth(pt_scene* s, int config_id, uint64_t seed, double scale);

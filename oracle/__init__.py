@@ -57,6 +57,7 @@ def load():
         _lib = ctypes.CDLL(LIB)
         _lib.oracle_trace.restype = ctypes.c_int
         _lib.oracle_render.restype = ctypes.c_int
+        _lib.oracle_adjoint.restype = ctypes.c_int
         for n in ("oracle_sinf", "oracle_cosf", "oracle_acosf"):
             getattr(_lib, n).restype = f32
             getattr(_lib, n).argtypes = [f32]
@@ -88,6 +89,24 @@ def render(packed, head, prm, W, H, frames=1, accum=None, crop=None, fp64=False,
     if rc != 0:
         raise RuntimeError(f"oracle_render failed: {rc}")
     return accum, c
+
+
+def adjoint(packed, head, prm, W, H, frames, dl_di, threads=0):
+    """FP64 adjoint: (grad_albedo, grad_emission), each (material_count, 3) float64,
+    of a `frames`-frame render from reset for dLoss/dImage = dl_di (H, W, 3|4)."""
+    lib = load()
+    d = np.zeros((H, W, 4), np.float32)
+    d[..., :3] = np.asarray(dl_di, np.float32)[..., :3]
+    n = packed.material_count
+    ga = np.zeros((max(n, 1), 3), np.float64)
+    ge = np.zeros((max(n, 1), 3), np.float64)
+    dp = P(ctypes.c_double)
+    rc = lib.oracle_adjoint(ctypes.byref(packed), ctypes.byref(head), ctypes.byref(prm), u32(W), u32(H),
+                            u32(frames), d.ctypes.data_as(P(f32)), ctypes.c_int(threads),
+                            ga.ctypes.data_as(dp), ge.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"oracle_adjoint failed: {rc}")
+    return ga[:n], ge[:n]
 
 
 def trace(packed, head, prm, ro4, rd4, fp64=False):

@@ -205,6 +205,7 @@ template <class R> struct Hit {
     R ior = R(1);
     V3<R> emission{R(0), R(0), R(0)};
     uint32_t id = kHitMiss;   // (0<<30 | record slot) or (1<<30 | triangle)
+    uint32_t mid = 0xFFFFFFFFu;   // material-table row of the attributes, if any
 };
 
 struct Counters {
@@ -217,7 +218,46 @@ struct Counters {
     }
 };
 
+// Gradient sink of the adjoint oracle: every radiance contribution of a
+// sample is a product of the albedo factors of the Lambert/metal vertices
+// before it (including the vertex whose NEE it is) and of the dielectrics its
+// shadow ray crossed, so d(contribution)/d(albedo_m) = contribution / albedo_m
+// per occurrence of m; an emission term thr*E has d/dE = thr.  Accumulated in
+// double, weighted by dLoss/d(sample radiance).
+struct AdjSink {
+    const float* mats = nullptr;   // 12 floats per row
+    uint32_t nmat = 0;
+    std::vector<double> g_alb, g_em;   // nmat*3 each
+    double w[3] = {0, 0, 0};
+    uint32_t vm[64];
+    int nv = 0;
+    uint32_t xm[16];
+    int nx = 0;
+    void add(uint32_t m, double c0, double c1, double c2, std::vector<double>& g) {
+        g[3 * m + 0] += w[0] * c0;
+        g[3 * m + 1] += w[1] * c1;
+        g[3 * m + 2] += w[2] * c2;
+    }
+    template <class V> void contrib(const V& c, bool shadow) {
+        auto one = [&](uint32_t m) {
+            if (m >= nmat) return;
+            const float* a = mats + 12 * size_t(m);
+            const double c0 = a[0] > 0.0f ? double(c.x) / double(a[0]) : 0.0;
+            const double c1 = a[1] > 0.0f ? double(c.y) / double(a[1]) : 0.0;
+            const double c2 = a[2] > 0.0f ? double(c.z) / double(a[2]) : 0.0;
+            add(m, c0, c1, c2, g_alb);
+        };
+        for (int i = 0; i < nv; ++i) one(vm[i]);
+        if (shadow)
+            for (int i = 0; i < nx; ++i) one(xm[i]);
+    }
+    template <class V> void emission(const V& thr, uint32_t m) {
+        if (m < nmat) add(m, double(thr.x), double(thr.y), double(thr.z), g_em);
+    }
+};
+
 template <class R> struct Tracer {
+    AdjSink* adj = nullptr;
     const PtPackedScene& S;
     const PtPushHead& P;
     const PtPathParams& Q;
@@ -265,12 +305,29 @@ template <class R> struct Tracer {
         } else {
             return;
         }
+        h.id = idx;
+        const uint32_t pm = S.prim_mat_ids ? S.prim_mat_ids[idx] : 0xFFFFFFFFu;
+        if (pm != 0xFFFFFFFFu && S.material_count > 0) {   // material-table extension
+            table_material(pm, h);
+            return;
+        }
         h.mat = uint32_t(v[9]);
         h.albedo = ld3<R>(v + 4);
         h.roughness = R(v[7]);
         h.ior = R(v[10]);
         h.emission = ld3<R>(v + 16);
-        h.id = idx;
+        h.mid = 0xFFFFFFFFu;
+    }
+
+    void table_material(uint32_t m, Hit<R>& h) const {
+        if (m >= S.material_count) m = S.material_count - 1;
+        const float* mt = S.materials + size_t(m) * 12;
+        h.mat = uint32_t(mt[8]);
+        h.albedo = ld3<R>(mt);
+        h.roughness = R(mt[3]);
+        h.emission = ld3<R>(mt + 4);
+        h.ior = R(mt[7]);
+        h.mid = m;
     }
 
     static bool slab(V3<R> ro, V3<R> inv, const PtBvhNode& n, R tmax) {
@@ -371,15 +428,9 @@ template <class R> struct Tracer {
                 h.normal = normalize(cross(v1 - v0, v2 - v0));
                 h.id = (1u << 30) | prim_hit;
                 if (S.tri_mat_ids && S.material_count > 0) {   // material table extension
-                    uint32_t m = S.tri_mat_ids[prim_hit];
-                    if (m >= S.material_count) m = S.material_count - 1;
-                    const float* mt = S.materials + size_t(m) * 12;
-                    h.mat = uint32_t(mt[8]);
-                    h.albedo = ld3<R>(mt);
-                    h.roughness = R(mt[3]);
-                    h.emission = ld3<R>(mt + 4);
-                    h.ior = R(mt[7]);
-                } else {   // MESH_ALBEDO gold metal (PathTrace.slang:1428, 2655-2658)
+                    table_material(S.tri_mat_ids[prim_hit], h);
+                } else {
+                    h.mid = 0xFFFFFFFFu;   // MESH_ALBEDO gold metal (PathTrace.slang:1428, 2655-2658)
                     h.mat = kMatMetal;
                     h.albedo = {R(1.00), R(0.85), R(0.45)};
                     h.roughness = R(0.05);
@@ -592,6 +643,7 @@ template <class R> struct Tracer {
     V3<R> transmittance(V3<R> o, V3<R> d, R t_max) {
         const int kmax = int(Q.refract_budget);
         V3<R> t{R(1), R(1), R(1)};
+        if (adj) adj->nx = 0;
         for (int i = 0; i <= kmax; ++i) {
             cnt.shadow++;
             const Hit<R> h = trace(o, d);
@@ -609,6 +661,7 @@ template <class R> struct Tracer {
             const V3<R> refr = refract(d, nf, eta);
             if (length(refr) < R(1e-3)) return {R(0), R(0), R(0)};
             t = t * ((R(1) - fr) * h.albedo);
+            if (adj && adj->nx < 16) adj->xm[adj->nx++] = h.mid;
             const R adv = h.t + R(1e-3);
             o = o + d * adv;
             d = normalize(refr);
@@ -661,6 +714,12 @@ template <class R> struct Tracer {
         R prev_pdf = R(0);
         const bool env = P.env_map_present != 0u;
         const uint32_t maxb = P.max_bounces;
+        if (adj) adj->nv = 0;
+        // adds c to the sample radiance (and its albedo derivatives to the sink)
+        auto add = [&](V3<R> c, bool shadow) {
+            rad = rad + c;
+            if (adj) adj->contrib(c, shadow);
+        };
         for (uint32_t b = 0; b < maxb; ++b) {
             cnt.ext++;
             const uint64_t n0 = cnt.nodes, t0 = cnt.tris, p0 = cnt.prims;
@@ -676,11 +735,11 @@ template <class R> struct Tracer {
                         // transmittance(ro, rd, 1e30) re-traces this same ray, which
                         // just missed everything: it returns exactly (1,1,1).
                         const V3<R> trans{R(1), R(1), R(1)};
-                        rad = rad + clamp_ind(thr * sky_color(rd) * trans * wb);
+                        add(clamp_ind(thr * sky_color(rd) * trans * wb), false);
                     }
                 } else if (!skip_sky) {
-                    if (b == 0u) rad = rad + thr * sky_color(rd);
-                    else rad = rad + clamp_ind(thr * sky_color(rd));
+                    if (b == 0u) add(thr * sky_color(rd), false);
+                    else add(clamp_ind(thr * sky_color(rd)), false);
                 }
                 break;
             }
@@ -688,9 +747,11 @@ template <class R> struct Tracer {
             const R ndi = dot(h.normal, rd);
             const V3<R> nf = (ndi < R(0)) ? h.normal : -h.normal;
             if (any_pos(h.emission)) {
-                if (b == 0u) rad = rad + thr * h.emission;
-                else rad = rad + clamp_ind(thr * h.emission);
+                if (b == 0u) add(thr * h.emission, false);
+                else add(clamp_ind(thr * h.emission), false);
+                if (adj) adj->emission(thr, h.mid);
             }
+            if (adj && (h.mat == kMatLambert || h.mat == kMatMetal) && adj->nv < 64) adj->vm[adj->nv++] = h.mid;
             if (h.mat == kMatLambert) {
                 if (Q.light_count > 0u) {
                     const LightSample ls = sample_light(hp, seed);
@@ -701,7 +762,7 @@ template <class R> struct Tracer {
                         if (any_pos(tr)) {
                             const V3<R> brdf = h.albedo / kPi;
                             const V3<R> c = thr * ls.Le * tr * brdf * ndl / ls.pdf;
-                            rad = rad + ((b == 0u) ? c : clamp_ind(c));
+                            add((b == 0u) ? c : clamp_ind(c), true);
                         }
                     }
                 }
@@ -717,7 +778,7 @@ template <class R> struct Tracer {
                             const R pdf_brdf = ndl * kInvPi;
                             const bool fire = (Q.mis_enabled != 0u) && ((b + 1u) < maxb);
                             const R wl = fire ? mis_balance(es.pdf, pdf_brdf) : R(1);
-                            rad = rad + clamp_ind(thr * es.color * tr * brdf * ndl * wl / es.pdf);
+                            add(clamp_ind(thr * es.color * tr * brdf * ndl * wl / es.pdf), true);
                         }
                     }
                     if (S.hdri_count > 0u) {
@@ -854,6 +915,47 @@ void render(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, 
             }
 }
 
+// adjoint oracle: fp32 paths (the GPU's, bit for bit), derivatives in double
+void adjoint(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, uint32_t W, uint32_t H,
+             uint32_t frames, const float* dldi, int threads, double* g_alb, double* g_em) {
+    const uint32_t spp = (P.spp == 0u) ? 1u : P.spp;
+    const double scale = 1.0 / (double(frames) * double(spp));
+    int nt = threads > 0 ? threads : int(std::thread::hardware_concurrency());
+    if (nt < 1) nt = 1;
+    std::vector<AdjSink> sinks(nt);
+    std::atomic<uint32_t> next{0};
+    auto worker = [&](int tid) {
+        AdjSink& a = sinks[tid];
+        a.mats = S.materials;
+        a.nmat = S.material_count;
+        a.g_alb.assign(3 * size_t(S.material_count), 0.0);
+        a.g_em.assign(3 * size_t(S.material_count), 0.0);
+        Tracer<float> tr(S, P, Q, W, H);
+        tr.adj = &a;
+        for (;;) {
+            const uint32_t y = next.fetch_add(1);
+            if (y >= H) break;
+            for (uint32_t x = 0; x < W; ++x) {
+                const float* d = dldi + (size_t(y) * W + x) * 4;
+                if (d[0] == 0.0f && d[1] == 0.0f && d[2] == 0.0f) continue;
+                for (int c = 0; c < 3; ++c) a.w[c] = double(d[c]) * scale;
+                for (uint32_t f = 0; f < frames; ++f) {
+                    uint32_t seed = pcg_hash(x * 1973u + y * 9277u + (P.frame_index + f) * 26699u);
+                    for (uint32_t s = 0; s < spp; ++s) (void)tr.sample_path(x, y, s, seed);
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < nt; ++i) pool.emplace_back(worker, i);
+    for (auto& t : pool) t.join();
+    for (const auto& a : sinks)
+        for (size_t i = 0; i < a.g_alb.size(); ++i) {
+            g_alb[i] += a.g_alb[i];
+            g_em[i] += a.g_em[i];
+        }
+}
+
 template <class R>
 void trace_rays(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q,
                 const float* ro, const float* rd, uint32_t n, uint32_t* hit, float* t,
@@ -913,6 +1015,18 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
     else
         orc::render<float>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
     orc::export_counters(c, counters);
+    return 0;
+}
+
+int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                   uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
+                   double* grad_albedo, double* grad_emission) {
+    if (!scene || !head || !params || !dl_di_rgba || !grad_albedo || !grad_emission || W == 0 || H == 0)
+        return -1;
+    if (head->tlas_present || params->light_tree_enabled || !head->env_map_present) return -6;
+    if (params->firefly_clamp > 0.0f) return -7;   // the clamp is not differentiable
+    for (size_t i = 0; i < 3 * size_t(scene->material_count); ++i) grad_albedo[i] = grad_emission[i] = 0.0;
+    orc::adjoint(*scene, *head, *params, W, H, frames, dl_di_rgba, threads, grad_albedo, grad_emission);
     return 0;
 }
 

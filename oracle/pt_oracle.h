@@ -53,6 +53,16 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
                   uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
                   int fp64, int threads, OracleCounters* counters);
 
+/* Adjoint oracle: dLoss/d(albedo) and dLoss/d(emission) per material-table
+ * row (3 doubles a row each) of a render of `frames` frames from reset, for
+ * dLoss/dImage = dl_di_rgba (W*H*4 floats, .a ignored).  The paths are the
+ * fp32 instance's (the GPU's paths bit for bit); each sample's contributions
+ * are differentiated term by term in double (no suffix sums), with the
+ * Russian-roulette probabilities held fixed.  -7: firefly clamp enabled. */
+int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                   uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
+                   double* grad_albedo, double* grad_emission);
+
 /* The polynomial transcendentals shared (by restatement) with the GPU kernels. */
 float oracle_sinf(float x);
 float oracle_cosf(float x);
