@@ -67,7 +67,7 @@ class PtAccelInfo(ctypes.Structure):
 
 
 class PtBatchView(ctypes.Structure):
-    _fields_ = [("scene", u32), ("width", u32), ("height", u32), ("reserved", u32),
+    _fields_ = [("scene", u32), ("width", u32), ("height", u32), ("frames_per_wave", u32),
                 ("head", PtPushHead), ("params", PtPathParams)]
 
 
@@ -126,6 +126,9 @@ SIGNATURES = {
     "pt_gpu_diff_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                             P(ctypes.c_double), P(ctypes.c_double)]),
     "pt_gpu_diff_get_backward_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtStats)]),
+    "pt_gpu_batch_diff_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, P(PtBatchView), u32]),
+    "pt_gpu_batch_diff_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                  P(ctypes.c_double), P(ctypes.c_double)]),
     "pt_gpu_render_noalloc": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32, u32, u32,
                                              ctypes.c_void_p]),
     "pt_gpu_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32,
@@ -339,6 +342,16 @@ class Scene:
         return out
 
 
+def _views_array(views):
+    """(scene, width, height, head, params[, frames_per_wave]) tuples -> PtBatchView[]."""
+    va = (PtBatchView * len(views))()
+    for i, v in enumerate(views):
+        va[i].scene, va[i].width, va[i].height = v[0], v[1], v[2]
+        va[i].head, va[i].params = v[3], v[4]
+        va[i].frames_per_wave = v[5] if len(v) > 5 else 1
+    return va
+
+
 class Device:
     """One CUDA device context (pt_gpu_*)."""
 
@@ -419,10 +432,7 @@ class Device:
         """scene_devs: list of Device (each holding an uploaded scene); views: list of
         (scene index, width, height, head, params)."""
         arr = (ctypes.c_void_p * len(scene_devs))(*[d.h.value if hasattr(d.h, "value") else d.h for d in scene_devs])
-        va = (PtBatchView * len(views))()
-        for i, (sc, w, h, head, prm) in enumerate(views):
-            va[i].scene, va[i].width, va[i].height = sc, w, h
-            va[i].head, va[i].params = head, prm
+        va = _views_array(views)
         self._batch_keep = (arr, va)
         self._check(self.lib.pt_gpu_batch_render(self.h, arr, len(scene_devs), va, len(views), frames))
 
@@ -433,10 +443,7 @@ class Device:
 
     def batch_autotune(self, scene_devs, views):
         arr = (ctypes.c_void_p * len(scene_devs))(*[d.h.value if hasattr(d.h, "value") else d.h for d in scene_devs])
-        va = (PtBatchView * len(views))()
-        for i, (sc, w, h, head, prm) in enumerate(views):
-            va[i].scene, va[i].width, va[i].height = sc, w, h
-            va[i].head, va[i].params = head, prm
+        va = _views_array(views)
         t = PtBatchTuning()
         self._check(self.lib.pt_gpu_batch_autotune(self.h, arr, len(scene_devs), va, len(views), ctypes.byref(t)))
         return t
@@ -466,6 +473,28 @@ class Device:
         dp = ctypes.POINTER(ctypes.c_double)
         self._check(self.lib.pt_gpu_diff_backward(self.h, g.ctypes.data, 0, ga.ctypes.data_as(dp),
                                                   ge.ctypes.data_as(dp)))
+        return ga, ge
+
+    def batch_diff_forward(self, scene_dev, views):
+        """views: list of (width, height, head, params[, frames_per_wave]) of the one
+        scene held by scene_dev."""
+        va = _views_array([(0,) + tuple(v) for v in views])
+        self._diff_views = [(v[0], v[1]) for v in views]
+        self._check(self.lib.pt_gpu_batch_diff_forward(self.h, scene_dev.h, va, len(views)))
+
+    def batch_diff_backward(self, dl_di_list, nmat):
+        """dl_di_list: per view (H, W, 3|4) dLoss/dImage.  Returns (grad_albedo, grad_emission)."""
+        parts = []
+        for (w, h), d in zip(self._diff_views, dl_di_list):
+            g = np.zeros((h, w, 4), np.float32)
+            g[..., :3] = np.asarray(d, np.float32)[..., :3]
+            parts.append(g.reshape(-1, 4))
+        flat = np.ascontiguousarray(np.concatenate(parts, axis=0))
+        ga = np.zeros((nmat, 3), np.float64)
+        ge = np.zeros((nmat, 3), np.float64)
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.pt_gpu_batch_diff_backward(self.h, flat.ctypes.data, 0, ga.ctypes.data_as(dp),
+                                                        ge.ctypes.data_as(dp)))
         return ga, ge
 
     def backward_stats(self) -> PtStats:

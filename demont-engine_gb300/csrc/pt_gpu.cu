@@ -428,6 +428,14 @@ __device__ __forceinline__ uint32_t view_of_slot(const Batch& B, uint32_t p) {
     return lo;
 }
 
+// pixel and frame of batch path slot p in its view (frames of a view are
+// consecutive blocks of npix slots)
+__device__ __forceinline__ void view_pixel(const DFrame& V, uint32_t p, uint32_t& x, uint32_t& y, uint32_t& f) {
+    const uint32_t local = p - V.slot_base;
+    f = local / V.npix;
+    slot_pixel(V, local - f * V.npix, x, y);
+}
+
 template <bool kB>
 __global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths, uint32_t frame0) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -438,8 +446,9 @@ __global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B,
         const DFrame& V = B.views[v];
         B.path_view[p] = v;
         B.path_scene[p] = V.scene;
-        slot_pixel(V, p - V.slot_base, x, y);
-        fidx = V.frame_index0;
+        uint32_t f;
+        view_pixel(V, p, x, y, f);
+        fidx = V.frame_index0 + f;
     } else {
         const uint32_t f = p / F.npix, pix = p - f * F.npix;
         slot_pixel(F, pix, x, y);
@@ -464,7 +473,8 @@ __global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, ui
     if (!live) return;
     uint32_t x, y;
     if (kB) {
-        slot_pixel(V, p - V.slot_base, x, y);
+        uint32_t f;
+        view_pixel(V, p, x, y, f);
     } else {
         const uint32_t f = p / F.npix, pix = p - f * F.npix;
         slot_pixel(F, pix, x, y);
@@ -542,10 +552,18 @@ __device__ __forceinline__ void adj_add(const Adj& A, int which, uint32_t m, V3 
     atomicAdd(g + 1, double(v.y));
     atomicAdd(g + 2, double(v.z));
 }
-// dLoss/d(sample radiance) of path p: dL/dI of its pixel times 1/(frames*spp)
+// dLoss/d(sample radiance) of path p: dL/dI of its pixel over the samples
+// averaged into it (frames * spp; batched views: one frame, the view's spp,
+// dL/dI laid out like the batch accumulation buffer)
+template <bool kB>
 __device__ __forceinline__ V3 adj_weight(const Adj& A, const DFrame& F, uint32_t p) {
-    const uint32_t f = p / F.npix, pix = p - f * F.npix;
     uint32_t x, y;
+    if (kB) {
+        uint32_t f;
+        view_pixel(F, p, x, y, f);
+        return v3(A.dldi[F.accum_base + size_t(y) * F.W + x]) * (1.0f / float(F.spp * F.nframes));
+    }
+    const uint32_t f = p / F.npix, pix = p - f * F.npix;
     slot_pixel(F, pix, x, y);
     return v3(A.dldi[size_t(y) * F.W + x]) * A.scale;
 }
@@ -605,7 +623,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
                     // scales everything the path collects after its emission
                     // (this vertex's NEE through the brdf, later vertices through
                     // the throughput): d/da = (R_total - R_so_far) / a
-                    const V3 g = adj_weight(A, F, p);
+                    const V3 g = adj_weight<kB>(A, F, p);
                     if (any_pos(sf.emission)) adj_add(A, 1, sf.mid, g * thr);
                     if (sf.mat == kMatLambert || sf.mat == kMatMetal) {
                         const V3 total = v3(A.srad[A.srec_base + p]);
@@ -794,13 +812,14 @@ __global__ void k_resolve(const __grid_constant__ DScene S0, const __grid_consta
             const V3 c = v3(pre) * tr * v3(br) * s1 * pre.w / br.w;
             rad = rad + (((mask >> (4 + k)) & 1u) ? clamp_ind(c, F.firefly) : c);
             if (kAdj) {   // each dielectric the shadow ray crossed multiplied c by its albedo
+                const DScene& S = kB ? B.scenes[F.scene] : S0;
                 const uint4 xm = A.sh_mats[e];
                 const uint32_t ms[4] = {xm.x, xm.y, xm.z, xm.w};
-                const V3 g = adj_weight(A, F, p);
+                const V3 g = adj_weight<kB>(A, F, p);
                 for (int j = 0; j < 4; ++j) {
-                    if (ms[j] == kNoMat) continue;
-                    const uint32_t m = min(ms[j], S0.mat_count - 1u);
-                    adj_add(A, 0, m, g * safe_div(c, v3(__ldg(S0.mats + 3u * m))));
+                    if (ms[j] == kNoMat || S.mat_count == 0u) continue;
+                    const uint32_t m = min(ms[j], S.mat_count - 1u);
+                    adj_add(A, 0, m, g * safe_div(c, v3(__ldg(S.mats + 3u * m))));
                 }
             }
         }
@@ -853,14 +872,27 @@ __global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes
 }
 
 // batched renders: one frame of every view, each into its own region
-__global__ void k_accumulate_batch(DPaths P, Batch B, uint32_t npaths) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npaths) return;
-    const DFrame& V = B.views[B.path_view[p]];
+// one thread per pixel of every view (npix_total = sum of the views' pixels):
+// the view's frames of this wave in order, as consecutive running-mean updates
+__global__ void k_accumulate_batch(DPaths P, Batch B, uint32_t npix_total) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npix_total) return;
+    uint32_t lo = 0, hi = B.n_views;   // last view with accum_base <= t
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (B.views[mid].accum_base <= t) lo = mid;
+        else hi = mid;
+    }
+    const DFrame& V = B.views[lo];
+    const uint32_t pix = uint32_t(t - V.accum_base);
     uint32_t x, y;
-    slot_pixel(V, p - V.slot_base, x, y);
+    slot_pixel(V, pix, x, y);
     const size_t out = V.accum_base + size_t(y) * V.W + x;
-    B.accum[out] = accum_update(B.accum[out], P.fsum[p], float(V.spp == 0u ? 1u : V.spp), V.reset != 0u, V.ema);
+    float4 a = B.accum[out];
+    const float nspp = float(V.spp == 0u ? 1u : V.spp);
+    for (uint32_t f = 0; f < V.nframes; ++f)
+        a = accum_update(a, P.fsum[V.slot_base + f * V.npix + pix], nspp, f == 0u && V.reset != 0u, V.ema);
+    B.accum[out] = a;
 }
 
 __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint32_t n, uint32_t* hit,
@@ -945,6 +977,8 @@ struct pt_gpu_ctx {
     uint32_t d_frames = 0;
     uint64_t gen = 0;   // bumped by every upload / target change
     PtStats d_bwd_stats{};
+    pt_gpu_ctx* d_batch_scene = nullptr;
+    std::vector<PtBatchView> d_batch_views;
     PtStats stats{};
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -1782,6 +1816,8 @@ int pt_gpu_diff_forward(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathPar
     if (head->reset_accum == 0u || prm->accum_ema_alpha > 0.0f)
         return set_err(ctx, PT_ERR_UNSUPPORTED, "diff_forward: needs reset_accum and no EMA (image = mean of the samples)");
     if (ctx->mat_count > 4096u) return set_err(ctx, PT_ERR_UNSUPPORTED, "diff_forward: more than 4096 materials");
+    ctx->d_batch_scene = nullptr;
+    ctx->d_batch_views.clear();
     DiffRun dr;
     dr.mode = RunMode::kRecord;
     const int rc = render_waves(ctx, head, prm, frames, dr);
@@ -1797,7 +1833,8 @@ int pt_gpu_diff_forward(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathPar
 int pt_gpu_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_device, double* grad_albedo,
                          double* grad_emission) {
     if (!ctx || !dl_di_rgba) return PT_ERR_INVALID;
-    if (!ctx->d_valid) return set_err(ctx, PT_ERR_STATE, "diff_backward: no recorded forward (pt_gpu_diff_forward)");
+    if (!ctx->d_valid || ctx->d_batch_scene)
+        return set_err(ctx, PT_ERR_STATE, "diff_backward: no recorded forward (pt_gpu_diff_forward)");
     if (ctx->d_gen != ctx->gen)
         return set_err(ctx, PT_ERR_STATE, "diff_backward: the scene or target changed since the recorded forward");
     const size_t npix = size_t(ctx->W) * ctx->H;
@@ -1962,7 +1999,7 @@ DFrame frame_of(const PtBatchView& v) {
     F.W = v.width;
     F.H = v.height;
     F.npix = v.width * v.height;
-    F.nframes = 1;
+    F.nframes = v.frames_per_wave == 0u ? 1u : v.frames_per_wave;
     F.frame_index0 = head->frame_index;
     F.spp = head->spp == 0u ? 1u : head->spp;
     F.maxb = head->max_bounces;
@@ -1984,8 +2021,9 @@ DFrame frame_of(const PtBatchView& v) {
 }
 
 // Issue one wave (one frame of every view) on ctx->stream.
-int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t npaths, uint32_t max_spp,
-                     uint32_t max_b, int kmax_any, const DScene& S0) {
+int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t npaths, uint32_t npix_total,
+                     uint32_t max_spp, uint32_t max_b, int kmax_any, const DScene& S0, const Adj* adj = nullptr,
+                     size_t smem = 0) {
     const DFrame F0{};
     const int gp = (npaths + 255) / 256;
     const int gpers = ctx->sm_count * int(ctx->b_tune.persistent_blocks_per_sm);
@@ -2002,13 +2040,26 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
             CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
             k_closest<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
                                                                  P.hit_t, P.hit_id, P.cnt + 3, P.stat);
-            k_shade<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+            const size_t srec = size_t(s) * npaths;
+            Adj A{};
+            if (adj) {
+                A = *adj;
+                A.srec_base = srec;
+                k_shade<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs, b);
+            } else {
+                k_shade<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+            }
             CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-            k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
-            k_resolve<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, 0);
+            k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any,
+                                                                  adj ? ctx->d_sh_mats.p : nullptr);
+            if (adj)
+                k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs,
+                                                                                          srec);
+            else
+                k_resolve<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, srec);
         }
     }
-    k_accumulate_batch<<<gp, 256, 0, ctx->stream>>>(P, Bt, npaths);
+    if (!adj) k_accumulate_batch<<<(npix_total + 255) / 256, 256, 0, ctx->stream>>>(P, Bt, npix_total);
     return PT_OK;
 }
 
@@ -2035,19 +2086,26 @@ int pt_gpu_batch_get_tuning(pt_gpu_ctx* ctx, PtBatchTuning* t) {
     return PT_OK;
 }
 
-int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, const PtBatchView* views,
-                        uint32_t n_views, uint32_t frames) {
+}  // extern "C"
+
+namespace {
+
+int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, const PtBatchView* views,
+                uint32_t n_views, uint32_t frames, const DiffRun& dr) {
     if (!ctx || !scenes || !views || n_scenes == 0 || n_views == 0) return PT_ERR_INVALID;
     for (uint32_t k = 0; k < n_scenes; ++k)
         if (!scenes[k] || scenes[k]->device != ctx->device)
             return set_err(ctx, PT_ERR_INVALID, "batch: scene contexts must be on the batch context's device");
-    uint64_t total = 0;
+    uint64_t total = 0, total_pix = 0;
     uint32_t max_spp = 0, max_b = 0;
     int kmax_any = -1;
+    auto fpw = [&](uint32_t i) { return views[i].frames_per_wave == 0u ? 1u : views[i].frames_per_wave; };
     for (uint32_t i = 0; i < n_views; ++i) {
         if (views[i].scene >= n_scenes) return set_err(ctx, PT_ERR_INVALID, "batch: view scene index out of range");
         if (int rc = validate_view(ctx, scenes[views[i].scene], views[i], i)) return rc;
-        total += uint64_t(views[i].width) * views[i].height;
+        if (views[i].frames_per_wave > 1024u) return set_err(ctx, PT_ERR_INVALID, "batch: frames_per_wave above 1024");
+        total += uint64_t(fpw(i)) * views[i].width * views[i].height;
+        total_pix += uint64_t(views[i].width) * views[i].height;
         max_spp = std::max(max_spp, views[i].head.spp == 0u ? 1u : views[i].head.spp);
         max_b = std::max(max_b, views[i].head.max_bounces);
         const int km = int(views[i].params.refract_budget);
@@ -2055,8 +2113,8 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
             return set_err(ctx, PT_ERR_INVALID, "batch: all views must share the refraction budget");
         kmax_any = km;
     }
-    if (total > (64ull << 20)) return set_err(ctx, PT_ERR_INVALID, "batch: more than 64 M pixels per frame");
-    const uint32_t npaths = uint32_t(total);
+    if (total > (64ull << 20)) return set_err(ctx, PT_ERR_INVALID, "batch: more than 64 M path slots per wave");
+    const uint32_t npaths = uint32_t(total), npix_total = uint32_t(total_pix);
     if (frames == 0) return PT_OK;
 
     // layout signature: views' sizes and scenes, tuning
@@ -2066,6 +2124,7 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
         sig.push_back((uint64_t(views[i].width) << 32) | views[i].height);
         sig.push_back(uint64_t(reinterpret_cast<uintptr_t>(scenes[views[i].scene])));
         sig.push_back((uint64_t(views[i].head.spp) << 32) | views[i].head.max_bounces);
+        sig.push_back(fpw(i));
     }
     const bool same_layout = (sig == ctx->b_sig);
     int rc = ensure_wave(ctx, npaths);
@@ -2079,7 +2138,7 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
         std::vector<size_t> aoff(n_views, 0);
         size_t acc = 0;
         for (uint32_t i = 0; i < n_views; ++i) {
-            base[i + 1] = base[i] + views[i].width * views[i].height;
+            base[i + 1] = base[i] + fpw(i) * views[i].width * views[i].height;
             aoff[i] = acc;
             acc += size_t(views[i].width) * views[i].height;
         }
@@ -2110,7 +2169,7 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
         ctx->b_views_h[i] = frame_of(views[i]);
         ctx->b_views_h[i].slot_base = base_slot;
         ctx->b_views_h[i].accum_base = ctx->b_accum_off[i];
-        base_slot += views[i].width * views[i].height;
+        base_slot += fpw(i) * views[i].width * views[i].height;
     }
 
     DPaths P{};
@@ -2128,6 +2187,31 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
     Bt.accum = ctx->b_accum.p;
     Bt.n_views = n_views;
     const DScene S0 = st[0];
+    const bool adj = dr.mode == RunMode::kAdjoint;
+    size_t smem = 0;
+    Adj A{};
+    if (dr.mode != RunMode::kRender) {
+        rc = dalloc(ctx, ctx->d_srad, size_t(max_spp) * npaths);
+        if (rc) return rc;
+        P.srad = (dr.mode == RunMode::kRecord) ? ctx->d_srad.p : nullptr;
+    }
+    if (adj) {
+        if ((rc = dalloc(ctx, ctx->d_sh_mats, 3 * size_t(npaths))) || (rc = dalloc(ctx, ctx->d_grad, 6 * size_t(dr.nmat))))
+            return rc;
+        CK(cudaMemsetAsync(ctx->d_grad.p, 0, 6 * size_t(dr.nmat) * sizeof(double), ctx->stream));
+        smem = 6 * size_t(dr.nmat) * sizeof(double);
+        if (smem > 48u * 1024u) {
+            CK(cudaFuncSetAttribute(k_shade<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            CK(cudaFuncSetAttribute(k_resolve<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        }
+        A.srad = ctx->d_srad.p;
+        A.dldi = dr.dldi;
+        A.grad = ctx->d_grad.p;
+        A.sh_mats = ctx->d_sh_mats.p;
+        A.nmat = dr.nmat;
+        A.scale = 1.0f;
+    }
+    const bool graph = ctx->b_tune.use_graph && dr.mode == RunMode::kRender;
 
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     ctx->stats = PtStats{};
@@ -2137,16 +2221,16 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
     for (uint32_t f = 0; f < frames; ++f) {
         for (uint32_t i = 0; i < n_views; ++i) {
             DFrame& V = ctx->b_views_h[i];
-            V.frame_index0 = views[i].head.frame_index + f;
+            V.frame_index0 = views[i].head.frame_index + f * fpw(i);
             V.reset = (f == 0 && views[i].head.reset_accum) ? 1u : 0u;
         }
         CK(cudaMemcpyAsync(ctx->b_views.p, ctx->b_views_h.data(), n_views * sizeof(DFrame), cudaMemcpyHostToDevice,
                            ctx->stream));
-        if (ctx->b_tune.use_graph) {
+        if (graph) {
             if (!ctx->b_graph) {
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-                const int irc = issue_batch_wave(ctx, Bt, P, npaths, max_spp, max_b, kmax_any, S0);
+                const int irc = issue_batch_wave(ctx, Bt, P, npaths, npix_total, max_spp, max_b, kmax_any, S0);
                 cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
                 if (irc) return irc;
                 if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
@@ -2159,14 +2243,16 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
             }
             CK(cudaGraphLaunch(ctx->b_graph, ctx->stream));
         } else {
-            if (int irc = issue_batch_wave(ctx, Bt, P, npaths, max_spp, max_b, kmax_any, S0)) return irc;
+            if (int irc = issue_batch_wave(ctx, Bt, P, npaths, npix_total, max_spp, max_b, kmax_any, S0,
+                                           adj ? &A : nullptr, smem))
+                return irc;
         }
         unsigned long long st2[4];
         CK(cudaMemcpyAsync(st2, ctx->stat.p, sizeof(st2), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         tot_ext += st2[0];
         tot_sh += st2[1];
-        ctx->stats.kernel_launches += launches_per_wave;
+        ctx->stats.kernel_launches += launches_per_wave - (adj ? 1u : 0u);
         ctx->stats.waves++;
         ctx->stats.paths += uint64_t(npaths) * max_spp;
     }
@@ -2183,6 +2269,76 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
     uint32_t errw = 0;
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
     if (errw) return set_err(ctx, PT_ERR_KERNEL, "batch: traversal iteration cap reached");
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, const PtBatchView* views,
+                        uint32_t n_views, uint32_t frames) {
+    return batch_waves(ctx, scenes, n_scenes, views, n_views, frames, DiffRun{});
+}
+
+int pt_gpu_batch_diff_forward(pt_gpu_ctx* ctx, pt_gpu_ctx* scene, const PtBatchView* views, uint32_t n_views) {
+    if (!ctx || !scene || !views || n_views == 0) return PT_ERR_INVALID;
+    ctx->d_valid = false;
+    if (scene->mat_count == 0) return set_err(ctx, PT_ERR_STATE, "batch_diff_forward: no material table");
+    if (scene->mat_count > 4096u) return set_err(ctx, PT_ERR_UNSUPPORTED, "batch_diff_forward: more than 4096 materials");
+    for (uint32_t i = 0; i < n_views; ++i) {
+        const PtBatchView& v = views[i];
+        if (v.scene != 0u) return set_err(ctx, PT_ERR_INVALID, "batch_diff_forward: views index the one scene (0)");
+        if (v.params.firefly_clamp > 0.0f || v.params.refract_budget > 4u || v.head.reset_accum == 0u ||
+            v.params.accum_ema_alpha > 0.0f)
+            return set_err(ctx, PT_ERR_UNSUPPORTED,
+                           "batch_diff_forward: needs no firefly clamp, refract budget <= 4, reset_accum, no EMA");
+    }
+    DiffRun dr;
+    dr.mode = RunMode::kRecord;
+    pt_gpu_ctx* const sc[1] = {scene};
+    const int rc = batch_waves(ctx, sc, 1, views, n_views, 1, dr);
+    if (rc) return rc;
+    ctx->d_valid = true;
+    ctx->d_gen = scene->gen;
+    ctx->d_batch_scene = scene;
+    ctx->d_batch_views.assign(views, views + n_views);
+    return PT_OK;
+}
+
+int pt_gpu_batch_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_device, double* grad_albedo,
+                               double* grad_emission) {
+    if (!ctx || !dl_di_rgba) return PT_ERR_INVALID;
+    if (!ctx->d_valid || !ctx->d_batch_scene || ctx->d_batch_views.empty())
+        return set_err(ctx, PT_ERR_STATE, "batch_diff_backward: no recorded batched forward");
+    pt_gpu_ctx* scene = ctx->d_batch_scene;
+    if (ctx->d_gen != scene->gen)
+        return set_err(ctx, PT_ERR_STATE, "batch_diff_backward: the scene changed since the recorded forward");
+    size_t npix = 0;
+    for (const auto& v : ctx->d_batch_views) npix += size_t(v.width) * v.height;
+    const float4* dldi = reinterpret_cast<const float4*>(dl_di_rgba);
+    if (!on_device) {
+        int rc = dupload(ctx, ctx->d_dldi, dl_di_rgba, npix);
+        if (rc) return rc;
+        dldi = ctx->d_dldi.p;
+    } else if ((reinterpret_cast<uintptr_t>(dl_di_rgba) & 15u) != 0u) {
+        return set_err(ctx, PT_ERR_INVALID, "batch_diff_backward: device dL/dI must be 16-byte aligned");
+    }
+    DiffRun dr;
+    dr.mode = RunMode::kAdjoint;
+    dr.dldi = dldi;
+    dr.nmat = scene->mat_count;
+    const PtStats keep = ctx->stats;
+    pt_gpu_ctx* const sc[1] = {scene};
+    const int rc = batch_waves(ctx, sc, 1, ctx->d_batch_views.data(), uint32_t(ctx->d_batch_views.size()), 1, dr);
+    if (rc) return rc;
+    ctx->d_bwd_stats = ctx->stats;
+    ctx->stats = keep;
+    std::vector<double> g(6 * size_t(dr.nmat));
+    CK(cudaMemcpy(g.data(), ctx->d_grad.p, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const size_t n3 = 3 * size_t(dr.nmat);
+    if (grad_albedo) std::memcpy(grad_albedo, g.data(), n3 * sizeof(double));
+    if (grad_emission) std::memcpy(grad_emission, g.data() + n3, n3 * sizeof(double));
     return PT_OK;
 }
 

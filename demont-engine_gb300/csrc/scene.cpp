@@ -834,6 +834,102 @@ void synth_c3(pt_scene* s, uint64_t seed, double scale) {
     set_cv(s, "r_light_tree", 0);
 }
 
+// env: log-normal radiance per texel (mu 0, sigma 1.5) + 0.5 deg sun disc of
+// 1e4 at elevation 40 deg, azimuth 30 deg
+void set_sky_env(pt_scene* s, Pcg32& rng, uint32_t envw, uint32_t envh) {
+    std::vector<float> rgb(size_t(envw) * envh * 3);
+    const double sun_el = 40.0 * std::numbers::pi / 180.0, sun_az = 30.0 * std::numbers::pi / 180.0;
+    const double sd[3] = {std::cos(sun_el) * std::cos(sun_az), std::sin(sun_el),
+                          std::cos(sun_el) * std::sin(sun_az)};
+    const double cos_disc = std::cos(0.25 * std::numbers::pi / 180.0);
+    for (uint32_t v = 0; v < envh; ++v) {
+        const double theta = std::numbers::pi * (v + 0.5) / envh;
+        for (uint32_t u = 0; u < envw; ++u) {
+            const double phi = 2.0 * std::numbers::pi * (u + 0.5) / envw - std::numbers::pi;
+            const double d[3] = {std::sin(theta) * std::cos(phi), std::cos(theta),
+                                 std::sin(theta) * std::sin(phi)};
+            float L0 = float(std::exp(1.5 * rng.gauss()));
+            if (d[0] * sd[0] + d[1] * sd[1] + d[2] * sd[2] >= cos_disc) L0 = 1e4f;
+            const size_t pi = size_t(v) * envw + u;
+            rgb[pi * 3 + 0] = L0;
+            rgb[pi * 3 + 1] = L0;
+            rgb[pi * 3 + 2] = L0;
+        }
+    }
+    pt_scene_set_env(s, rgb.data(), envw, envh);
+}
+
+// Inverse-rendering scene: the procedural terrain scene in a 120 x 120 arena,
+// ~1M triangles (80 displaced icospheres of 9,680 triangles + a 340x340-quad
+// ground), 256 spheres and the log-normal + sun env, on 1,024 Lambert material
+// rows with albedos U[0.2, 0.8].  The ground is cut into 56 x 56 patches that
+// take the rows in a scattered order, every row on 3-4 patches, so an object
+// covering a patch hides no row; icospheres and spheres take random rows.  Depth 8, roulette from bounce 2, no firefly clamp.
+void synth_c4(pt_scene* s, uint64_t seed, double scale) {
+    Pcg32 rng(0x5EEDull + 4ull, seed);
+    const double lin = std::sqrt(scale);
+    const uint32_t n_ico = std::max<uint32_t>(1, uint32_t(std::lround(80 * scale)));
+    const uint32_t nu = std::max<uint32_t>(2, uint32_t(std::lround(22 * lin)));
+    const uint32_t grid = std::max<uint32_t>(32, uint32_t(std::lround(340 * lin)));
+    const uint32_t n_sph = std::max<uint32_t>(1, uint32_t(std::lround(256 * scale)));
+    uint32_t envw = std::max<uint32_t>(16, uint32_t(std::lround(2048 * lin)));
+    envw &= ~1u;
+    const uint32_t envh = envw / 2;
+    constexpr uint32_t kRows = 1024, kPatches = 56;
+    std::vector<float> mats;
+    for (uint32_t i = 0; i < kRows; ++i) {
+        MatDraw m{0, {rng.range(0.2f, 0.8f), rng.range(0.2f, 0.8f), rng.range(0.2f, 0.8f)}, 0.0f, 1.5f};
+        push_material(mats, m);
+    }
+    std::vector<float> pos;
+    std::vector<uint32_t> idx, mid;
+    const float L = 60.0f;
+    for (uint32_t j = 0; j <= grid; ++j)
+        for (uint32_t i = 0; i <= grid; ++i) {
+            pos.push_back(-L + 2.0f * L * float(i) / float(grid));
+            pos.push_back(0.0f);
+            pos.push_back(-L + 2.0f * L * float(j) / float(grid));
+        }
+    for (uint32_t j = 0; j < grid; ++j)
+        for (uint32_t i = 0; i < grid; ++i) {
+            const uint32_t a = j * (grid + 1) + i, b = a + 1, c = a + grid + 1, d = c + 1;
+            idx.insert(idx.end(), {a, c, b, b, c, d});
+            // patch k takes row (389 k) mod 1024: every row covers 3-4 patches
+            // about 18 patch rows apart, so no row is hidden by one object
+            const uint32_t k = (j * kPatches / grid) * kPatches + (i * kPatches / grid);
+            const uint32_t row = (k * 389u) % kRows;
+            mid.push_back(row);
+            mid.push_back(row);
+        }
+    for (uint32_t k = 0; k < n_ico; ++k) {
+        const float r = rng.range(1.5f, 4.0f);
+        const float c[3] = {rng.range(-52, 52), r, rng.range(-52, 52)};
+        add_icosphere(pos, idx, mid, c, r, nu, 0.1f, 5000u + 7u * k,
+                      std::min<uint32_t>(uint32_t(rng.unit() * float(kRows)), kRows - 1u));
+    }
+    pt_scene_set_materials(s, mats.data(), uint32_t(mats.size() / 12));
+    pt_scene_set_mesh(s, pos.data(), uint32_t(pos.size() / 3), idx.data(), uint32_t(idx.size() / 3),
+                      mid.data());
+    for (uint32_t i = 0; i < n_sph; ++i) {
+        const float r = float(0.3 * std::pow(5.0, double(rng.unit())));
+        const float cx = rng.range(-55, 55), cz = rng.range(-55, 55);
+        const uint32_t row = std::min<uint32_t>(uint32_t(rng.unit() * float(kRows)), kRows - 1u);
+        const float* m = mats.data() + 12 * size_t(row);
+        pt_scene_prim_sphere(s, 1 + i, cx, r, cz, r, 0, m[0], m[1], m[2], 0.0f, 1.5f);
+        pt_scene_prim_set_material(s, 1 + i, row);
+    }
+    set_sky_env(s, rng, envw, envh);
+    pt_scene_set_camera(s, 0.0f, 45.0f, 70.0f, 0.0f, -0.57f, 45.0f);
+    set_cv(s, "r_max_bounces", 8);
+    set_cv(s, "r_spp", 16);
+    set_cv(s, "r_rr_start", 2);
+    set_cv(s, "r_mis", 1);
+    set_cv(s, "r_caustics", 1);
+    set_cv(s, "r_refract_bounces", 4);
+    set_cv(s, "r_firefly_clamp", 0);
+    set_cv(s, "r_light_tree", 0);
+}
+
 void synth_c1(pt_scene* s, uint64_t seed, double scale) {
     Pcg32 rng(0x5EEDull + 1ull, seed);
     const double lin = std::sqrt(scale);
@@ -881,27 +977,7 @@ void synth_c1(pt_scene* s, uint64_t seed, double scale) {
         pt_scene_prim_sphere(s, 1 + i, cx, r, cz, r, m.type, m.albedo[0], m.albedo[1], m.albedo[2],
                              m.rough, m.ior);
     }
-    // env: log-normal radiance per texel (mu 0, sigma 1.5) + 0.5 deg sun disc of 1e4
-    std::vector<float> rgb(size_t(envw) * envh * 3);
-    const double sun_el = 40.0 * std::numbers::pi / 180.0, sun_az = 30.0 * std::numbers::pi / 180.0;
-    const double sd[3] = {std::cos(sun_el) * std::cos(sun_az), std::sin(sun_el),
-                          std::cos(sun_el) * std::sin(sun_az)};
-    const double cos_disc = std::cos(0.25 * std::numbers::pi / 180.0);
-    for (uint32_t v = 0; v < envh; ++v) {
-        const double theta = std::numbers::pi * (v + 0.5) / envh;
-        for (uint32_t u = 0; u < envw; ++u) {
-            const double phi = 2.0 * std::numbers::pi * (u + 0.5) / envw - std::numbers::pi;
-            const double d[3] = {std::sin(theta) * std::cos(phi), std::cos(theta),
-                                 std::sin(theta) * std::sin(phi)};
-            float L0 = float(std::exp(1.5 * rng.gauss()));
-            if (d[0] * sd[0] + d[1] * sd[1] + d[2] * sd[2] >= cos_disc) L0 = 1e4f;
-            const size_t pi = size_t(v) * envw + u;
-            rgb[pi * 3 + 0] = L0;
-            rgb[pi * 3 + 1] = L0;
-            rgb[pi * 3 + 2] = L0;
-        }
-    }
-    pt_scene_set_env(s, rgb.data(), envw, envh);
+    set_sky_env(s, rng, envw, envh);
     pt_scene_set_camera(s, 0.0f, 30.0f, 150.0f, 0.0f, -0.197f, 45.0f);
     set_cv(s, "r_max_bounces", 8);
     set_cv(s, "r_spp", 1);
@@ -1275,6 +1351,7 @@ int pt_scene_synth(pt_scene* s, int config_id, uint64_t seed, double scale) {
     if (config_id == 0) synth_c0(s, seed, scale);
     else if (config_id == 1) synth_c1(s, seed, scale);
     else if (config_id == 3) synth_c3(s, seed, scale);
+    else if (config_id == 4) synth_c4(s, seed, scale);
     else return fail(s, "synth: unknown config id");
     return pt_scene_pack(s);
 }

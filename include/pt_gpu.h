@@ -212,11 +212,13 @@ int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave);
  * sequence is captured once as a CUDA graph and replayed per frame.  Each view
  * behaves exactly like pt_gpu_render of that view on its scene (bit-identical
  * accumulation), frame f of a view using frame_index = head.frame_index + f and
- * reset_accum only for f == 0. */
+ * reset_accum only for f == 0.  A view with frames_per_wave = n renders n
+ * consecutive frames in every wave (a call with `frames` waves renders
+ * frames * n frames of it), which fills the device with fewer, larger views. */
 typedef struct PtBatchView {
     uint32_t     scene;      /* index into the scenes array */
     uint32_t     width, height;
-    uint32_t     reserved;
+    uint32_t     frames_per_wave;   /* consecutive frames of this view in each wave (0 = 1, <= 1024) */
     PtPushHead   head;
     PtPathParams params;
 } PtBatchView;
@@ -267,6 +269,15 @@ int pt_gpu_diff_forward(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathPar
                         uint32_t frames);
 int pt_gpu_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_device,
                          double* grad_albedo, double* grad_emission);
+/* Batched form (many views of one scene in one wavefront, one frame each):
+ * the gradient of a loss over all views' images.  views[i].scene must be 0
+ * (the one scene context); the views' accumulation regions are read with
+ * pt_gpu_batch_read_accum.  dl_di_rgba holds every view's dLoss/dImage
+ * back to back in view order (sum of width*height RGBA floats). */
+int pt_gpu_batch_diff_forward(pt_gpu_ctx* ctx, pt_gpu_ctx* scene, const PtBatchView* views,
+                              uint32_t n_views);
+int pt_gpu_batch_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_device,
+                               double* grad_albedo, double* grad_emission);
 /* PtStats of the last backward replay (pt_gpu_get_stats keeps the forward's). */
 int pt_gpu_diff_get_backward_stats(pt_gpu_ctx* ctx, PtStats* out);
 

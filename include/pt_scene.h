@@ -142,7 +142,11 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
  *      1024 spheres, 2048x1024 log-normal env with a 0.5 deg sun disc of 1e4, 256 materials;
  *   3: differentiable-render scene: 512 spheres in [-20,20]^3 and ~200k triangles (20
  *      icospheres, 4 boxes, a 56x56-quad floor) on a 256-row material table of which 16
- *      rows are emissive, the 1x1 quad light, black env; 32 spp, depth 6, no firefly clamp.
+ *      rows are emissive, the 1x1 quad light, black env; 32 spp, depth 6, no firefly clamp;
+ *   4: inverse-rendering scene: config 1's terrain in a 120 x 120 arena with ~1M triangles
+ *      (80 icospheres + 340x340-quad ground), 256 spheres, the same env, 1024 Lambert rows
+ *      with albedo U[0.2,0.8]; ground patch k (56x56 patches) takes row 389k mod 1024; 16 spp, depth 8,
+ *      no firefly clamp.
  * scale (0 < scale <= 1) shrinks the triangle/sphere/env counts for fast tests
  * (1 = the full configuration).  Sets the camera and cvars of the config. */
 int pt_scene_synth(pt_scene* s, int config_id, uint64_t seed, double scale);

@@ -104,3 +104,67 @@ def test_adjoint_state_and_argument_errors(pt, dev):
     dev.materials(mats)                            # an upload invalidates the record
     with pytest.raises(pt.PtError):
         dev.diff_backward(dl, mats.shape[0])
+
+
+def test_batched_adjoint_equals_per_view_adjoints(pt, dev):
+    import math
+    s = pt.Scene().synth(4, seed=0, scale=0.02)
+    s.set_cvar("r_spp", 2)
+    pk = s.packed()
+    nm = pk.material_count
+    scene = pt.Device(0)
+    scene.upload(s)
+    views = []
+    for i, side in enumerate((64, 40, 96)):
+        yaw = 2 * math.pi * i / 3
+        pos = (60 * math.sin(yaw), 40.0, -60 * math.cos(yaw))
+        s.camera(pos, math.atan2(-pos[0], pos[2]), -math.atan2(40.0, 60.0), 50.0)
+        head, prm = s.push(side, side, frame_index=100 * i, reset=1)
+        views.append((side, side, head, prm))
+    rng = np.random.default_rng(5)
+    dls = [rng.standard_normal((h, w, 3)).astype(np.float32) for (w, h, _, _) in views]
+    batch = pt.Device(0)
+    batch.batch_diff_forward(scene, views)
+    imgs = [batch.batch_read(i, w, h).copy() for i, (w, h, _, _) in enumerate(views)]
+    ga, ge = batch.batch_diff_backward(dls, nm)
+    sa, se = np.zeros_like(ga), np.zeros_like(ge)
+    for i, (w, h, head, prm) in enumerate(views):
+        scene.set_target(w, h)
+        scene.diff_forward(head, prm, 1)
+        assert np.array_equal(scene.read_accum().view(np.uint32), imgs[i].view(np.uint32))
+        a, e = scene.diff_backward(dls[i], nm)
+        sa += a
+        se += e
+    assert np.abs(sa).max() > 0
+    np.testing.assert_allclose(ga, sa, rtol=1e-9, atol=1e-12 * np.abs(sa).max())
+    np.testing.assert_allclose(ge, se, rtol=1e-9, atol=1e-12 * max(np.abs(se).max(), 1e-30))
+    batch.close()
+    scene.close()
+
+
+def test_batch_frames_per_wave_equals_plain_frames(pt, dev):
+    """A batched view with frames_per_wave = n accumulates the same n frames as
+    a plain n-frame render, bit for bit (and the adjoint of one such view equals
+    the plain adjoint of the n frames)."""
+    s = pt.Scene().synth(4, seed=0, scale=0.02)
+    s.set_cvar("r_spp", 1)
+    nm = s.packed().material_count
+    scene = pt.Device(0)
+    scene.upload(s)
+    W, H, n = 72, 40, 4
+    head, prm = s.push(W, H, frame_index=77, reset=1)
+    batch = pt.Device(0)
+    batch.batch_render([scene], [(0, W, H, head, prm, n)], 2)    # 2 waves x 4 frames
+    b = batch.batch_read(0, W, H)
+    scene.set_target(W, H)
+    scene.render(head, prm, 2 * n)
+    assert np.array_equal(b.view(np.uint32), scene.read_accum().view(np.uint32))
+    dl = np.random.default_rng(2).standard_normal((H, W, 3)).astype(np.float32)
+    batch.batch_diff_forward(scene, [(W, H, head, prm, n)])
+    ga, ge = batch.batch_diff_backward([dl], nm)
+    scene.diff_forward(head, prm, n)
+    pa, pe = scene.diff_backward(dl, nm)
+    assert np.abs(pa).max() > 0
+    np.testing.assert_allclose(ga, pa, rtol=1e-9, atol=1e-12 * np.abs(pa).max())
+    batch.close()
+    scene.close()
