@@ -511,3 +511,42 @@ class Device:
         self._check(self.lib.pt_gpu_trace_closest(self.h, ro4.ctypes.data, rd4.ctypes.data, n,
                                                   hit.ctypes.data, t.ctypes.data, 0))
         return hit, t
+
+
+def material_render_fn(dev: "Device", scene: "Scene", width: int, height: int, frames: int = 1,
+                       frame_index: int = 0):
+    """A torch.autograd.Function over the differentiable render:
+    image = f(albedo, emission), both (n_materials, 3) float tensors, image
+    (height, width, 3) float32.  forward uploads the material table with the
+    given albedo and emission and runs pt_gpu_diff_forward; backward hands
+    dLoss/dImage to pt_gpu_diff_backward (path replay).  Torch is only the
+    caller's autograd plumbing here: all rendering runs in the CUDA library."""
+    import torch
+
+    packed = scene.packed()
+    n = packed.material_count
+    base = np.ctypeslib.as_array(packed.materials, (n * 12,)).reshape(n, 12).copy()
+    head, prm = scene.push(width, height, frame_index=frame_index, reset=1)
+
+    class _Render(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, albedo, emission):
+            m = base.copy()
+            m[:, 0:3] = albedo.detach().cpu().numpy().astype(np.float32)
+            m[:, 4:7] = emission.detach().cpu().numpy().astype(np.float32)
+            dev.set_target(width, height)
+            dev.materials(m)
+            dev.diff_forward(head, prm, frames)
+            img = dev.read_accum()[..., :3].copy()
+            ctx.dtypes = (albedo.dtype, emission.dtype, albedo.device)
+            return torch.from_numpy(img)
+
+        @staticmethod
+        def backward(ctx, grad_img):
+            ga, ge = dev.diff_backward(grad_img.detach().cpu().numpy().astype(np.float32), n)
+            adt, edt, device = ctx.dtypes
+            return (torch.from_numpy(ga).to(device=device, dtype=adt),
+                    torch.from_numpy(ge).to(device=device, dtype=edt))
+
+    return _Render.apply
+

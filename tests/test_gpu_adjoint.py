@@ -168,3 +168,24 @@ def test_batch_frames_per_wave_equals_plain_frames(pt, dev):
     np.testing.assert_allclose(ga, pa, rtol=1e-9, atol=1e-12 * np.abs(pa).max())
     batch.close()
     scene.close()
+
+
+def test_torch_autograd_function_wraps_forward_backward(pt, dev):
+    torch = pytest.importorskip("torch")
+    W, H = 48, 32
+    s, head, prm, pk, mats = _scene(pt, 0.2, 2, 3, W, H)
+    dev.upload(s)
+    fn = pt.material_render_fn(dev, s, W, H, frames=1)
+    albedo = torch.tensor(mats[:, 0:3], dtype=torch.float64, requires_grad=True)
+    emission = torch.tensor(mats[:, 4:7], dtype=torch.float64, requires_grad=True)
+    img = fn(albedo, emission)
+    target = torch.zeros_like(img)
+    loss = ((img - target) ** 2).sum()
+    loss.backward()
+    # the same gradient straight through the C-ABI
+    dev.diff_forward(head, prm, 1)
+    ref = dev.read_accum()[..., :3]
+    assert np.array_equal(ref, img.numpy())
+    ga, ge = dev.diff_backward(2.0 * ref, mats.shape[0])
+    np.testing.assert_allclose(albedo.grad.numpy(), ga, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(emission.grad.numpy(), ge, rtol=1e-12, atol=0)
