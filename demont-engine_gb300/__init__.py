@@ -45,7 +45,9 @@ class PtPathParams(ctypes.Structure):
     _fields_ = [("refract_budget", f32), ("firefly_clamp", f32), ("mis_enabled", u32),
                 ("accum_ema_alpha", f32), ("bvh_params", u32 * 4), ("light_count", u32),
                 ("light_tree_enabled", u32), ("light_tree_node_count", u32), ("rr_start", u32),
-                ("sun_and_mode", f32 * 4), ("reserved", u32 * 4)]
+                ("sun_and_mode", f32 * 4), ("reserved", u32 * 4),
+                ("moon_dir_phase", f32 * 4), ("moon_extra", f32 * 4), ("sun_extra", f32 * 4),
+                ("sun_extra2", f32 * 4)]
 
 
 class PtBvhNode(ctypes.Structure):
@@ -86,7 +88,8 @@ class PtPackedScene(ctypes.Structure):
                 ("env_rgba", P(f32)), ("env_w", u32), ("env_h", u32), ("env_marginal", P(f32)),
                 ("env_conditional", P(f32)), ("env_total_luminance", ctypes.c_double),
                 ("hdri_count", u32), ("hdri_dir_pmf", P(f32)), ("hdri_col", P(f32)),
-                ("env_present", u32), ("prim_mat_ids", P(u32))]
+                ("env_present", u32), ("prim_mat_ids", P(u32)), ("moon_rgba", P(f32)),
+                ("moon_w", u32), ("moon_h", u32)]
 
 
 # every entry point include/*.h declares, with its ctypes signature
@@ -104,6 +107,7 @@ SIGNATURES = {
     "pt_gpu_upload_lights": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
     "pt_gpu_upload_env": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32, P(f32), P(f32), P(f32),
                                          P(f32), u32]),
+    "pt_gpu_upload_moon": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32]),
     "pt_gpu_set_target": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
     "pt_gpu_read_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
     "pt_gpu_write_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
@@ -152,6 +156,7 @@ SIGNATURES = {
     "pt_scene_set_mesh": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, P(u32), u32, P(u32)]),
     "pt_scene_set_materials": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
     "pt_scene_set_env": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32]),
+    "pt_scene_set_moon": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32]),
     "pt_scene_set_camera": (ctypes.c_int, [ctypes.c_void_p, f32, f32, f32, f32, f32, f32]),
     "pt_scene_set_cvar": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double]),
     "pt_scene_get_cvar": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, P(ctypes.c_double)]),
@@ -301,6 +306,15 @@ class Scene:
         H, W = a.shape[:2]
         self._check(self.lib.pt_scene_set_env(self.h, fptr(a), W, H))
 
+    def moon(self, rgba):
+        """Moon surface map (H, W, 4) float32 for the gradient sky, or None."""
+        if rgba is None:
+            self._check(self.lib.pt_scene_set_moon(self.h, None, 0, 0))
+            return
+        a = np.ascontiguousarray(rgba, np.float32)
+        self._moon_keep = a
+        self._check(self.lib.pt_scene_set_moon(self.h, fptr(a), a.shape[1], a.shape[0]))
+
     def camera(self, pos, yaw, pitch, fov_deg):
         self._check(self.lib.pt_scene_set_camera(self.h, *pos, yaw, pitch, fov_deg))
 
@@ -385,6 +399,11 @@ class Device:
 
     def upload(self, scene: Scene):
         self._check(self.lib.pt_scene_upload(scene.h, self.h))
+
+    def upload_moon(self, rgba):
+        """Moon surface map (H, W, 4) float32 for the gradient sky's moon disc."""
+        a = np.ascontiguousarray(rgba, np.float32)
+        self._check(self.lib.pt_gpu_upload_moon(self.h, fptr(a), a.shape[1], a.shape[0]))
 
     def set_target(self, width, height):
         self._check(self.lib.pt_gpu_set_target(self.h, width, height))

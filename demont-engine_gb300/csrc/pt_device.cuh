@@ -146,6 +146,71 @@ __device__ __forceinline__ float f_acos(float x) {
     return f_atan2(s, x);
 }
 
+// exp, log, pow, asin (procedural sky).  exp: Cody-Waite reduction by ln 2
+// (k = rint(x log2 e), r = x - k ln2_hi - k ln2_lo, |r| <= ln2 / 2) and the
+// Taylor series of e^r to degree 8, scaled by 2^k.  log: x = m 2^e with m in
+// [sqrt(1/2), sqrt(2)), log m = 2 atanh(s), s = (m - 1) / (m + 1), odd series to
+// s^11.  pow(x, y) = exp(y log x) for x > 0.  asin(x) = atan2(x, sqrt(1 - x^2)).
+constexpr float kLog2E = 0x1.715476p+0f;
+constexpr float kLn2Hi = 0x1.62e4p-1f;            // 16 significant bits: k * hi exact for |k| < 256
+constexpr float kLn2Lo = 0x1.7f7d1cp-20f;         // float(ln 2 - hi)
+constexpr float kLn2F = 0x1.62e43p-1f;
+constexpr float kSqrtHalf = 0x1.6a09e6p-1f;
+constexpr float kE2 = 0.5f, kE3 = float(1.0 / 6.0), kE4 = float(1.0 / 24.0), kE5 = float(1.0 / 120.0),
+                kE6 = float(1.0 / 720.0), kE7 = float(1.0 / 5040.0), kE8 = float(1.0 / 40320.0);
+constexpr float kL3 = float(1.0 / 3.0), kL5 = float(1.0 / 5.0), kL7 = float(1.0 / 7.0), kL9 = float(1.0 / 9.0),
+                kL11 = float(1.0 / 11.0);
+
+__device__ __forceinline__ float f_exp(float x) {
+    if (!(x < 88.7f)) return (x != x) ? x : __int_as_float(0x7f800000);
+    if (x < -103.0f) return 0.0f;
+    const float k = rintf(x * kLog2E);
+    float r = x - k * kLn2Hi;
+    r = r - k * kLn2Lo;
+    float p = kE8;
+    p = p * r + kE7;
+    p = p * r + kE6;
+    p = p * r + kE5;
+    p = p * r + kE4;
+    p = p * r + kE3;
+    p = p * r + kE2;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    const int ki = int(k);
+    // 2^k in two exact steps (k may leave the normal exponent range)
+    const int k1 = ki / 2, k2 = ki - k1;
+    return (p * __int_as_float((127 + k1) << 23)) * __int_as_float((127 + k2) << 23);
+}
+__device__ __forceinline__ float f_log(float x) {
+    if (!(x > 0.0f)) return (x == 0.0f) ? __int_as_float(0xff800000) : __int_as_float(0x7fc00000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    int e;
+    float m = frexpf(x, &e);   // x = m 2^e, m in [0.5, 1)
+    if (m < kSqrtHalf) {
+        m = m * 2.0f;
+        e -= 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = kL11;
+    p = p * s2 + kL9;
+    p = p * s2 + kL7;
+    p = p * s2 + kL5;
+    p = p * s2 + kL3;
+    const float lm = 2.0f * s + (2.0f * s) * (s2 * p);
+    return float(e) * kLn2F + lm;
+}
+__device__ __forceinline__ float f_pow(float x, float y) {
+    if (y == 0.0f || x == 1.0f) return 1.0f;
+    if (x == 0.0f) return (y > 0.0f) ? 0.0f : __int_as_float(0x7f800000);
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    return f_exp(y * f_log(x));
+}
+__device__ __forceinline__ float f_asin(float x) {
+    const float c = sqrtf((1.0f - x) * (1.0f + x));
+    return f_atan2(x, c);
+}
+
 // shader literal constants, rounded once to float
 constexpr float kPi = float(3.14159265358979);
 constexpr float kTwoPi = float(6.28318530717958);
@@ -210,6 +275,8 @@ struct DScene {
     uint32_t hdri_count;
     float4 hdri_dir[8];
     float4 hdri_col[8];
+    const float4* moon_tex;      // moon surface map (gradient sky), W*H texels, or null
+    uint32_t moon_w, moon_h;
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs

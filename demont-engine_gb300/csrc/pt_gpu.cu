@@ -36,6 +36,7 @@ using namespace ptd;
 namespace {
 
 constexpr uint32_t kEnded = 4u, kSkipSky = 1u, kPrevLambert = 2u;
+constexpr uint32_t kAmbBit = 1u << 8;   // shadow mask: the path has a skylight ambient term (P.amb)
 constexpr int kThreads = 256;
 
 struct DFrame {
@@ -58,6 +59,12 @@ struct DFrame {
     uint32_t reset;          // reset_accum of the view's first frame
     float ema;               // accum_params.x
     size_t accum_base;       // first texel of the view in the batch accumulation buffer
+    // gradient sky (no env map): sun_and_mode.xyz, moon_dir_phase, moon_extra, sun_extra, sun_extra2.x
+    V3 sun_dir;
+    float sun_bright;
+    float4 moon;
+    float4 moon_extra;
+    float4 sun_extra;
 };
 
 // Adjoint replay state (differentiable renders)
@@ -102,6 +109,7 @@ struct DPaths {
     uint32_t* q[2];
     uint32_t* sq;
     uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue, [3] fetch counter
+    float4* amb;       // gradient sky: skylight ambient of the bounce, added after its NEE terms
     float4* srad;      // differentiable renders: radiance of every sample [s * npaths + p], or null
     unsigned long long* stat;   // [0] extension rays, [1] shadow segments
 };
@@ -119,8 +127,153 @@ __device__ __forceinline__ V3 env_texel(const DScene& S, uint32_t u, uint32_t v)
     return v3(__ldg(S.env + (size_t(v) * S.env_w + u)));
 }
 
-// skyColor, env-map branch (shaders/PathTrace.slang:3401-3431)
+__device__ __forceinline__ float saturatef(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return a + t * (b - a); }
+__device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {
+    const float t = saturatef((x - e0) / (e1 - e0));
+    return t * t * (3.0f - 2.0f * t);
+}
+
+// sky dome of the gradient mode (skyColorBase, shaders/PathTrace.slang:3461-3463)
+__device__ __forceinline__ V3 sky_gradient(V3 rd) {
+    const float t = clampf(0.5f * (rd.y + 1.0f), 0.0f, 1.0f);
+    return lerp3(v3(0.50f, 0.55f, 0.62f), v3(1.0f, 1.0f, 1.0f), t);
+}
+
+// sun disc + halo (sunDisc, shaders/PathTrace.slang:3112-3195)
+__device__ V3 sun_disc(const DFrame& F, V3 rd) {
+    const V3 sd = F.sun_dir;
+    if (sd.y < -0.10f) return v3(0.0f, 0.0f, 0.0f);
+    const float ang = dot(rd, sd);
+    const float sun_mult = fmaxf(F.sun_extra.x * F.sun_extra.y, 0.1f);
+    const float r_deg = 0.55f * sun_mult;
+    const float cos_r = f_cos(r_deg * 0.0174533f);
+    const float halo_deg = lerpf(2.0f, 8.0f, saturatef(1.0f - sd.y));
+    const float halo_rad = halo_deg * 0.0174533f;
+    const float cos_halo = f_cos(halo_rad);
+    if (ang <= cos_halo) return v3(0.0f, 0.0f, 0.0f);
+    const float vflat = F.sun_extra.z;
+    const bool oval = vflat < 0.999f;
+    bool inside = false;
+    if (ang > cos_r) {
+        if (!oval) {
+            inside = true;
+        } else {
+            const V3 lr = normalize(cross(v3(0.0f, 1.0f, 0.0f), sd));
+            const V3 lu = cross(sd, lr);
+            const V3 delta = rd - sd * ang;
+            const float h_off = dot(delta, lr), v_off = dot(delta, lu);
+            const float r_h = r_deg * 0.0174533f;
+            const float r_v = r_h * vflat;
+            const float ellipse = (h_off * h_off) / (r_h * r_h) + (v_off * v_off) / (r_v * r_v);
+            inside = ellipse <= 1.0f;
+        }
+    }
+    const float am = 1.0f / fmaxf(sd.y, 0.04f);
+    const float atm = f_exp(-0.30f * am);
+    const float warmth = saturatef((am - 1.0f) * 0.18f);
+    const V3 col = lerp3(v3(1.00f, 0.98f, 0.94f), v3(1.55f, 0.55f, 0.20f), warmth);
+    float halo = 0.0f;
+    if (ang > cos_halo) {
+        const float t_h = (ang - cos_halo) / (1.0f - cos_halo);
+        const float falloff = lerpf(8.0f, 3.0f, saturatef(1.0f - sd.y));
+        halo = f_pow(t_h, falloff);
+    }
+    const float bright = fmaxf(F.sun_bright, 0.0f);
+    if (inside) return (col * (250.0f * atm) + col * halo * atm * 4.0f) * bright;
+    return col * halo * atm * 4.0f * bright;
+}
+
+__device__ __forceinline__ V3 moon_texel(const DScene& S, int32_t x, int32_t y) {
+    return v3(__ldg(S.moon_tex + (size_t(y) * S.moon_w + x)));
+}
+
+// moon disc + surface + halo (moonDisc, shaders/PathTrace.slang:3212-3353)
+__device__ V3 moon_disc(const DScene& S, const DFrame& F, V3 rd) {
+    const float4 mph = F.moon;
+    if (mph.y < -0.10f) return v3(0.0f, 0.0f, 0.0f);
+    const V3 m_dir = v3(mph);
+    const V3 sun = F.sun_dir;
+    const float ang = dot(rd, m_dir);
+    const float size_mult = fmaxf(F.moon_extra.x * F.moon_extra.y, 0.1f);
+    const float r_deg = 0.55f * size_mult;
+    const float halo_deg = 1.5f * size_mult;
+    const float cos_r = f_cos(r_deg * 0.0174533f);
+    const float cos_halo = f_cos(halo_deg * 0.0174533f);
+    if (ang <= cos_halo) return v3(0.0f, 0.0f, 0.0f);
+    const V3 col_tint = v3(0.92f, 0.94f, 1.00f);
+    const float moon_am = 1.0f / fmaxf(mph.y, 0.04f);
+    const float moon_atm = f_exp(-0.30f * moon_am);
+    const float warmth_m = saturatef((moon_am - 1.0f) * 0.18f);
+    const V3 col_atm = lerp3(v3(1.00f, 1.00f, 1.00f), v3(1.20f, 0.65f, 0.40f), warmth_m);
+    float halo = 0.0f;
+    if (ang > cos_halo) {
+        const float t_h = (ang - cos_halo) / (1.0f - cos_halo);
+        halo = f_pow(t_h, 4.0f) * 0.6f;
+    }
+    if (ang > cos_r) {
+        const float t_d = (ang - cos_r) / (1.0f - cos_r);
+        const V3 ax = (fabsf(m_dir.y) < 0.99f) ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+        const V3 t_a = normalize(cross(ax, m_dir));
+        const V3 t_b = cross(m_dir, t_a);
+        const float disc_scale = 1.0f / fmaxf(f_sin(r_deg * 0.0174533f), 1e-5f);
+        const float du = dot(rd, t_a) * disc_scale;
+        const float dv = dot(rd, t_b) * disc_scale;
+        const float r2 = du * du + dv * dv;
+        const float zz = sqrtf(fmaxf(1.0f - r2, 0.0f));
+        const V3 n_world = t_a * du + t_b * dv - m_dir * zz;
+        const float lit = saturatef(dot(n_world, sun) * 10.0f + 0.05f);
+        if (lit <= 0.0f) return col_tint * col_atm * halo * moon_atm * 0.05f;
+        const float anti_sun_dot = -dot(m_dir, sun);
+        const float anti_sun_ang = f_acos(saturatef(anti_sun_dot));
+        const float eclipse = 1.0f - smoothstepf(0.0122f, 0.0218f, anti_sun_ang);
+        const float lon = f_atan2(du, zz);
+        const float lat = f_asin(clampf(dv, -1.0f, 1.0f));
+        const float u_tex = saturatef(0.5f + lon / 6.28318530718f);
+        const float v_tex = saturatef(0.5f - lat / 3.14159265358979f);
+        const int32_t mw = int32_t(S.moon_w), mh = int32_t(S.moon_h);
+        const float fx = u_tex * float(mw) - 0.5f, fy = v_tex * float(mh) - 0.5f;
+        const int32_t ix = int32_t(floorf(fx)), iy = int32_t(floorf(fy));
+        const float tx = fx - float(ix), ty = fy - float(iy);
+        const int32_t x0 = min(max(ix, 0), mw - 1), x1 = min(max(ix + 1, 0), mw - 1);
+        const int32_t y0 = min(max(iy, 0), mh - 1), y1 = min(max(iy + 1, 0), mh - 1);
+        const V3 surface = lerp3(lerp3(moon_texel(S, x0, y0), moon_texel(S, x1, y0), tx),
+                                 lerp3(moon_texel(S, x0, y1), moon_texel(S, x1, y1), tx), ty);
+        const float limb = 0.55f + 0.45f * sqrtf(saturatef(t_d));
+        const float bright_mult = fmaxf(F.moon_extra.z, 0.0f);
+        const float disc_scale_b = 3.5f * bright_mult;
+        const V3 lit_col = col_tint * col_atm * surface * (disc_scale_b * lit * limb * moon_atm) +
+                           col_tint * col_atm * halo * lit * moon_atm * (0.6f * bright_mult);
+        const V3 eclipse_col = v3(0.55f, 0.15f, 0.04f) * surface * (limb * moon_atm * 1.2f);
+        return lerp3(lit_col, eclipse_col, eclipse);
+    }
+    const float phase_b = 0.5f * (1.0f - f_cos(mph.w));
+    return col_tint * col_atm * halo * phase_b * moon_atm * 0.3f;
+}
+
+// sampleSunDisc (shaders/PathTraceMath.slang:55-68)
+__device__ __forceinline__ V3 sample_sun_disc(V3 sun_dir, uint32_t& seed) {
+    const float u1 = randf(seed);
+    const float u2 = randf(seed);
+    const float r = sqrtf(u1) * 0.00465f;
+    const float phi = kTwoPiHemi * u2;
+    const float dx = f_cos(phi) * r, dy = f_sin(phi) * r;
+    const V3 ax = (fabsf(sun_dir.y) < 0.99f) ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+    const V3 t = normalize(cross(ax, sun_dir));
+    const V3 b = cross(sun_dir, t);
+    return normalize(sun_dir + t * dx + b * dy);
+}
+
+// skyColor (shaders/PathTrace.slang:3373-3434): the env map (mode 1), else the
+// gradient dome with the moon and sun discs on top (mode 0)
+__device__ V3 sky_env(const DScene& S, const DFrame& F, V3 rd);
 __device__ V3 sky_color(const DScene& S, const DFrame& F, V3 rd) {
+    if (F.env_present) return sky_env(S, F, rd);
+    return sky_gradient(rd) + moon_disc(S, F, rd) + sun_disc(F, rd);
+}
+
+// skyColor, env-map branch (shaders/PathTrace.slang:3401-3431)
+__device__ V3 sky_env(const DScene& S, const DFrame& F, V3 rd) {
     const int32_t w = int32_t(S.env_w), hh = int32_t(S.env_h);
     const float u = f_atan2(rd.z, rd.x) * kInvTwoPiSky + 0.5f;
     const float v = f_acos(clampf(rd.y, -1.0f, 1.0f)) * kInvPiSky;
@@ -676,6 +829,44 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
                                              ndl2, hpdf, b != 0u, shadow_mask);
                         }
                         st = (F.mis == 0u) ? (st | kSkipSky) : (st & ~kSkipSky);
+                    } else {
+                        // gradient sky: sun NEE (slot 1), moon NEE (slot 2), skylight
+                        // ambient (shaders/PathTrace.slang:6546-6667); none clamped
+                        const V3 sun_dir = F.sun_dir;
+                        if (sun_dir.y > 0.0f) {
+                            const float n_dot_l = fmaxf(0.0f, dot(nf, sun_dir));
+                            const V3 sun_jit = sample_sun_disc(sun_dir, seed);
+                            const float am = 1.0f / fmaxf(sun_dir.y, 0.04f);
+                            const float trans_atm = f_exp(-0.30f * am);
+                            const float warmth = saturatef((am - 1.0f) * 0.18f);
+                            const V3 sun_col = lerp3(v3(1.00f, 0.97f, 0.92f), v3(1.55f, 0.55f, 0.20f), warmth);
+                            const float strength = 80.0f * trans_atm;
+                            const V3 sun_rad = sun_col * strength;
+                            if (n_dot_l > 0.0f)
+                                issue_shadow(P, p, 1, so, sun_jit, 1e30f, thr * sun_rad, 1.0f, sf.albedo / kPi,
+                                             n_dot_l, 1.0f, false, shadow_mask);
+                        }
+                        if (F.moon.y > 0.0f) {
+                            const float phase_b = 0.5f * (1.0f - f_cos(F.moon.w));
+                            if (phase_b > 0.01f) {
+                                const V3 moon_jit = sample_sun_disc(v3(F.moon), seed);
+                                const float ndl = fmaxf(0.0f, dot(nf, moon_jit));
+                                if (ndl > 0.0f) {
+                                    const float m_elev = fmaxf(F.moon.y, 0.04f);
+                                    const float m_am = 1.0f / m_elev;
+                                    const float m_atm = f_exp(-0.30f * m_am);
+                                    const float m_warmth = saturatef((m_am - 1.0f) * 0.18f);
+                                    const V3 m_col =
+                                        lerp3(v3(0.92f, 0.94f, 1.00f), v3(1.20f, 0.65f, 0.40f), m_warmth);
+                                    const V3 moon_rad = m_col * (0.3f * phase_b * m_atm);
+                                    issue_shadow(P, p, 2, so, moon_jit, 1e30f, thr * moon_rad, 1.0f,
+                                                 sf.albedo / kPi, ndl, 1.0f, false, shadow_mask);
+                                }
+                            }
+                        }
+                        P.amb[p] = f4(thr * sf.albedo * sky_gradient(nf), 0.0f);
+                        shadow_mask |= kAmbBit;
+                        st |= kSkipSky;
                     }
                     thr = thr * sf.albedo;
                     ro = hp + nf * 1e-3f;
@@ -823,6 +1014,7 @@ __global__ void k_resolve(const __grid_constant__ DScene S0, const __grid_consta
                 }
             }
         }
+        if (mask & kAmbBit) rad = rad + v3(P.amb[p]);
         if (mask) P.rad[p] = f4(rad, 0.0f);
         if (st & kEnded) {
             const float4 fs = P.fsum[p];
@@ -936,13 +1128,15 @@ struct pt_gpu_ctx {
     uint32_t mat_count = 0, light_count = 0, env_w = 0, env_h = 0, hdri_count = 0;
     bool mesh_has_mat = false;
     float hdri_dir[32] = {0}, hdri_col[32] = {0};
+    DBuf<float4> moon;
+    uint32_t moon_w = 0, moon_h = 0;
     DBuf<uint32_t> err_word;
     // target
     uint32_t W = 0, H = 0;
     DBuf<float4> accum;
     // wave buffers
     size_t cap = 0;
-    DBuf<float4> ray_o, ray_d, thr, rad, fsum, sh_o, sh_d, sh_pre, sh_brdf, sh_tr;
+    DBuf<float4> ray_o, ray_d, thr, rad, fsum, amb, sh_o, sh_d, sh_pre, sh_brdf, sh_tr;
     DBuf<uint32_t> seed, state, hit_id, shmask, q0, q1, sq, cnt;
     DBuf<float> hit_t;
     DBuf<unsigned long long> stat;
@@ -1074,6 +1268,9 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
         S.hdri_col[i] = make_float4(c->hdri_col[4 * i], c->hdri_col[4 * i + 1], c->hdri_col[4 * i + 2],
                                     c->hdri_col[4 * i + 3]);
     }
+    S.moon_tex = c->moon.p;
+    S.moon_w = c->moon_w;
+    S.moon_h = c->moon_h;
     S.err = c->err_word.p;
     S.use_wide = (c->traversal == 0) ? 1u : 0u;
     S.a_wide = (S.use_wide && c->a_wide) ? 1u : 0u;
@@ -1097,6 +1294,31 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     return S;
 }
 
+// Sky of a dispatch: env map (mode 1, or 0 with a map), else the gradient
+// dome with sun/moon discs and their NEE (mode 0).  The procedural and
+// Hosek-Wilkie domes (modes 2, 3) are not built.
+int check_sky(pt_gpu_ctx* ctx, const pt_gpu_ctx* sc, const PtPushHead* head, const PtPathParams* prm,
+              const std::string& who) {
+    const float mode = prm->sun_and_mode[3];
+    if (mode == 2.0f || mode == 3.0f)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, who + "procedural / Hosek-Wilkie sky modes (2, 3) are not built");
+    if (head->env_map_present) {
+        if (sc->env_w == 0 || sc->env_h == 0) return set_err(ctx, PT_ERR_STATE, who + "env map not uploaded");
+    } else if (prm->moon_dir_phase[1] >= -0.10f && sc->moon_w == 0) {
+        return set_err(ctx, PT_ERR_STATE, who + "moon above the horizon but no moon texture (pt_gpu_upload_moon)");
+    }
+    return PT_OK;
+}
+
+void sky_of(DFrame& F, const PtPathParams* prm) {
+    F.sun_dir = v3(prm->sun_and_mode[0], prm->sun_and_mode[1], prm->sun_and_mode[2]);
+    F.moon = make_float4(prm->moon_dir_phase[0], prm->moon_dir_phase[1], prm->moon_dir_phase[2],
+                         prm->moon_dir_phase[3]);
+    F.moon_extra = make_float4(prm->moon_extra[0], prm->moon_extra[1], prm->moon_extra[2], prm->moon_extra[3]);
+    F.sun_extra = make_float4(prm->sun_extra[0], prm->sun_extra[1], prm->sun_extra[2], prm->sun_extra[3]);
+    F.sun_bright = prm->sun_extra2[0];
+}
+
 int grid_for(pt_gpu_ctx* c, size_t work, int per_sm) {
     const size_t need = (work + kThreads - 1) / kThreads;
     const size_t cap = size_t(c->sm_count) * per_sm;
@@ -1111,6 +1333,7 @@ int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     rc |= dalloc(ctx, ctx->thr, npaths);
     rc |= dalloc(ctx, ctx->rad, npaths);
     rc |= dalloc(ctx, ctx->fsum, npaths);
+    rc |= dalloc(ctx, ctx->amb, npaths);
     rc |= dalloc(ctx, ctx->seed, npaths);
     rc |= dalloc(ctx, ctx->state, npaths);
     rc |= dalloc(ctx, ctx->hit_t, npaths);
@@ -1369,9 +1592,11 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto* b : {&ctx->prim_rec, &ctx->prim_geo, &ctx->bvh, &ctx->tri, &ctx->tri_bvh, &ctx->mats,
                     &ctx->lights, &ctx->env, &ctx->accum, &ctx->ray_o, &ctx->ray_d, &ctx->thr,
-                    &ctx->rad, &ctx->fsum, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
-                    &ctx->sh_tr})
+                    &ctx->rad, &ctx->fsum, &ctx->amb, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
+                    &ctx->sh_tr, &ctx->moon, &ctx->d_srad, &ctx->d_dldi})
         dfree(*b);
+    dfree(ctx->d_grad);
+    dfree(ctx->d_sh_mats);
     dfree(ctx->prim_mat);
     for (auto* b : {&ctx->prim_type, &ctx->seed, &ctx->state, &ctx->hit_id, &ctx->shmask, &ctx->q0,
                     &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word})
@@ -1546,6 +1771,21 @@ int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H
     return PT_OK;
 }
 
+int pt_gpu_upload_moon(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H) {
+    if (ctx) ctx->gen++;
+    if (!ctx) return PT_ERR_INVALID;
+    if (W == 0 || H == 0) {
+        dfree(ctx->moon);
+        ctx->moon_w = ctx->moon_h = 0;
+        return PT_OK;
+    }
+    if (!rgba || uint64_t(W) * H > (1ull << 26)) return set_err(ctx, PT_ERR_INVALID, "upload_moon: bad image");
+    if (int rc = dupload(ctx, ctx->moon, rgba, size_t(W) * H)) return rc;
+    ctx->moon_w = W;
+    ctx->moon_h = H;
+    return PT_OK;
+}
+
 int pt_gpu_set_target(pt_gpu_ctx* ctx, uint32_t width, uint32_t height) {
     if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
@@ -1611,8 +1851,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "render: no target (pt_gpu_set_target)");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: tlas_present (hardware RT) has no CUDA path");
     if (prm->light_tree_enabled) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: light tree not built");
-    if (!head->env_map_present)
-        return set_err(ctx, PT_ERR_UNSUPPORTED, "render: procedural sky modes (no env map) not built");
+    if (int rc = check_sky(ctx, ctx, head, prm, "render: ")) return rc;
     if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
         (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))
         return set_err(ctx, PT_ERR_INVALID, "render: prim_count / bvh_params disagree with the uploaded prims");
@@ -1622,7 +1861,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         return set_err(ctx, PT_ERR_INVALID, "render: bvh_params.w disagrees with the uploaded mesh BVH");
     if (prm->light_count > ctx->light_count)
         return set_err(ctx, PT_ERR_INVALID, "render: light_count exceeds the uploaded lights");
-    if (ctx->env_w == 0 || ctx->env_h == 0) return set_err(ctx, PT_ERR_STATE, "render: env map not uploaded");
+
     if (frames == 0) return PT_OK;
 
     DFrame F{};
@@ -1648,6 +1887,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     F.mis = prm->mis_enabled;
     F.rr_start = prm->rr_start;
     F.light_count = prm->light_count;
+    sky_of(F, prm);
     const DScene S = make_scene(ctx, prm);
 
     uint32_t fpw = ctx->wave_frames_override;
@@ -1657,7 +1897,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     if (rc) return rc;
 
     DPaths P{};
-    P.ray_o = ctx->ray_o.p; P.ray_d = ctx->ray_d.p; P.thr = ctx->thr.p; P.rad = ctx->rad.p;
+    P.ray_o = ctx->ray_o.p; P.ray_d = ctx->ray_d.p; P.thr = ctx->thr.p; P.rad = ctx->rad.p; P.amb = ctx->amb.p;
     P.fsum = ctx->fsum.p; P.seed = ctx->seed.p; P.state = ctx->state.p; P.hit_t = ctx->hit_t.p;
     P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
     P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
@@ -1969,8 +2209,9 @@ int validate_view(pt_gpu_ctx* ctx, pt_gpu_ctx* sc, const PtBatchView& v, uint32_
     const PtPushHead* head = &v.head;
     const PtPathParams* prm = &v.params;
     if (v.width == 0 || v.height == 0) return set_err(ctx, PT_ERR_INVALID, w + "empty frame");
-    if (head->tlas_present || prm->light_tree_enabled || !head->env_map_present)
-        return set_err(ctx, PT_ERR_UNSUPPORTED, w + "tlas / light tree / procedural sky not built");
+    if (head->tlas_present || prm->light_tree_enabled)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, w + "tlas / light tree not built");
+    if (int rc = check_sky(ctx, sc, head, prm, w)) return rc;
     if (head->prim_count != sc->prim_count || prm->bvh_params[0] != sc->linear_count ||
         prm->bvh_params[1] != sc->bvh_nodes)
         return set_err(ctx, PT_ERR_INVALID, w + "prim_count / bvh_params disagree with its scene");
@@ -1978,7 +2219,6 @@ int validate_view(pt_gpu_ctx* ctx, pt_gpu_ctx* sc, const PtBatchView& v, uint32_
         (prm->bvh_params[2] != 0u && prm->bvh_params[3] != sc->tri_nodes))
         return set_err(ctx, PT_ERR_INVALID, w + "mesh bvh_params disagree with its scene");
     if (prm->light_count != sc->light_count) return set_err(ctx, PT_ERR_INVALID, w + "light_count disagrees");
-    if (sc->env_w == 0) return set_err(ctx, PT_ERR_STATE, w + "scene has no env map");
     if (!sc->a_wide && sc->prim_count > sc->linear_count)
         return set_err(ctx, PT_ERR_UNSUPPORTED, w + "scene has no wide analytic tree");
     if (!sc->t_wide && sc->tri_nodes > 0u)
@@ -2014,6 +2254,7 @@ DFrame frame_of(const PtBatchView& v) {
     F.mis = prm->mis_enabled;
     F.rr_start = prm->rr_start;
     F.light_count = prm->light_count;
+    sky_of(F, prm);
     F.scene = v.scene;
     F.reset = head->reset_accum;
     F.ema = prm->accum_ema_alpha;
@@ -2173,7 +2414,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     }
 
     DPaths P{};
-    P.ray_o = ctx->ray_o.p; P.ray_d = ctx->ray_d.p; P.thr = ctx->thr.p; P.rad = ctx->rad.p;
+    P.ray_o = ctx->ray_o.p; P.ray_d = ctx->ray_d.p; P.thr = ctx->thr.p; P.rad = ctx->rad.p; P.amb = ctx->amb.p;
     P.fsum = ctx->fsum.p; P.seed = ctx->seed.p; P.state = ctx->state.p; P.hit_t = ctx->hit_t.p;
     P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
     P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
@@ -2390,7 +2631,7 @@ int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n
 // Limits and sharing rules:
 //   - at most kNoAllocMaxPixels pixels per frame (256 x 256); larger frames are
 //     rejected with PT_ERR_INVALID;
-//   - the array (kNoAllocBytes, about 24 MB) is held by every GPU that loads
+//   - the array (kNoAllocBytes, about 23.5 MiB) is held by every GPU that loads
 //     the library until the process exits;
 //   - every call on a device uses the same array and leaves its contents
 //     behind; what must start at zero (queue counters, statistics) is cleared
@@ -2407,9 +2648,9 @@ constexpr uint32_t kNoAllocMaxPixels = 65536u;
 constexpr size_t kNoAllocAlign = 256;
 constexpr size_t align_up(size_t v) { return (v + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
 constexpr size_t kNA_P = kNoAllocMaxPixels;
-// 5 float4 path arrays, 5 float4 x 3 shadow slots, 7 u32 path arrays, 1 u32 x 3 shadow queue,
+// 6 float4 path arrays, 5 float4 x 3 shadow slots, 7 u32 path arrays, 1 u32 x 3 shadow queue,
 // 8 u32 counters, 4 u64 statistics
-constexpr size_t kNoAllocBytes = 5 * align_up(16 * kNA_P) + 5 * align_up(16 * 3 * kNA_P) +
+constexpr size_t kNoAllocBytes = 6 * align_up(16 * kNA_P) + 5 * align_up(16 * 3 * kNA_P) +
                                  7 * align_up(4 * kNA_P) + align_up(4 * 3 * kNA_P) + align_up(32) +
                                  align_up(32);
 
@@ -2455,8 +2696,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         return set_err(ctx, PT_ERR_INVALID, "render_noalloc: accumulation buffer must be 16-byte aligned");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: tlas_present has no CUDA path");
     if (prm->light_tree_enabled) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: light tree not built");
-    if (!head->env_map_present)
-        return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: procedural sky modes (no env map) not built");
+    if (int rc = check_sky(ctx, ctx, head, prm, "render_noalloc: ")) return rc;
     if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
         (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))
         return set_err(ctx, PT_ERR_INVALID, "render_noalloc: prim_count / bvh_params disagree with the uploaded prims");
@@ -2464,7 +2704,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         return set_err(ctx, PT_ERR_INVALID, "render_noalloc: bvh_params.w disagrees with the uploaded mesh BVH");
     if (prm->light_count > ctx->light_count)
         return set_err(ctx, PT_ERR_INVALID, "render_noalloc: light_count exceeds the uploaded lights");
-    if (ctx->env_w == 0 || ctx->env_h == 0) return set_err(ctx, PT_ERR_STATE, "render_noalloc: env map not uploaded");
+
     if (frames == 0) return PT_OK;
     unsigned char* base = nullptr;
     if (int rc = noalloc_base(ctx, &base)) return rc;
@@ -2482,6 +2722,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     P.thr = reinterpret_cast<float4*>(take(16 * kNA_P));
     P.rad = reinterpret_cast<float4*>(take(16 * kNA_P));
     P.fsum = reinterpret_cast<float4*>(take(16 * kNA_P));
+    P.amb = reinterpret_cast<float4*>(take(16 * kNA_P));
     P.sh_o = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
     P.sh_d = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
     P.sh_pre = reinterpret_cast<float4*>(take(16 * 3 * kNA_P));
@@ -2522,6 +2763,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     F.mis = prm->mis_enabled;
     F.rr_start = prm->rr_start;
     F.light_count = prm->light_count;
+    sky_of(F, prm);
     const DScene S = make_scene(ctx, prm);
     const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);

@@ -437,6 +437,8 @@ struct pt_scene {
     std::vector<float> env_rgb;
     uint32_t env_w = 0, env_h = 0;
     bool env_present = false;
+    std::vector<float> moon_rgba;
+    uint32_t moon_w = 0, moon_h = 0;
     float cam_pos[3] = {0.0f, 1.5f, 4.0f};
     float cam_yaw = 0.0f, cam_pitch = -0.20f, cam_fov = 60.0f;
     std::vector<CVar> cvars = {
@@ -448,6 +450,10 @@ struct pt_scene {
         {"r_hdri_extract_percentile", 0.005},
         {"r_light_tree", 0},         {"r_rr_start", 2},
         {"r_denoiser", 0},
+        {"r_sun_elevation", 30},     {"r_sun_azimuth", 135},
+        {"r_sun_size", 1},           {"r_sun_disc_brightness", 1},
+        {"r_sun_horizon_flatten", 1},
+        {"r_moon_size", 1},          {"r_moon_disc_brightness", 0.7},
     };
 
     // packed state
@@ -1192,6 +1198,20 @@ int pt_scene_set_env(pt_scene* s, const float* rgb, uint32_t W, uint32_t H) {
     return PT_OK;
 }
 
+int pt_scene_set_moon(pt_scene* s, const float* rgba, uint32_t W, uint32_t H) {
+    if (!s) return PT_ERR_INVALID;
+    if (W == 0 || H == 0) {
+        s->moon_rgba.clear();
+        s->moon_w = s->moon_h = 0;
+        return PT_OK;
+    }
+    if (!rgba) return fail(s, "set_moon: null image");
+    s->moon_rgba.assign(rgba, rgba + size_t(W) * H * 4);
+    s->moon_w = W;
+    s->moon_h = H;
+    return PT_OK;
+}
+
 int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float pitch,
                         float fov_deg) {
     if (!s) return PT_ERR_INVALID;
@@ -1261,6 +1281,9 @@ int pt_scene_packed(pt_scene* s, PtPackedScene* o) {
     o->lights = s->packed_lights.data();
     o->light_count = uint32_t(s->lights.size());
     o->env_present = s->env_present ? 1u : 0u;
+    o->moon_rgba = s->moon_rgba.empty() ? nullptr : s->moon_rgba.data();
+    o->moon_w = s->moon_w;
+    o->moon_h = s->moon_h;
     o->env_rgba = s->env_rgba.data();
     o->env_w = s->env_w;
     o->env_h = s->env_h;
@@ -1337,10 +1360,45 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
     params->light_tree_enabled = 0;
     params->light_tree_node_count = 0;
     params->rr_start = uint32_t(std::max(0.0, s->cvar("r_rr_start")));
-    params->sun_and_mode[0] = 0.0f;
-    params->sun_and_mode[1] = 1.0f;
-    params->sun_and_mode[2] = 0.0f;
-    params->sun_and_mode[3] = 0.0f;
+    // Sky (src/engine/Engine.cpp:8304-8470, 8533-8545): env map -> mode 1, else the
+    // gradient dome (mode 0, the reference's fallback for "hdri" without a map).
+    // The sun comes from r_sun_elevation / r_sun_azimuth (the non-astronomical
+    // driver); the moon is hidden (it is placed only by the astronomical date
+    // driver, which is not part of this path); distance ratios are the mean 1.0.
+    const float elev_deg = float(s->cvar("r_sun_elevation"));
+    const float azim_deg = float(s->cvar("r_sun_azimuth"));
+    const float elev_r = elev_deg * 0.01745329251994329576923690768489f;
+    const float azim_r = azim_deg * 0.01745329251994329576923690768489f;
+    const float ce = std::cos(elev_r), se = std::sin(elev_r);
+    params->sun_and_mode[0] = ce * std::sin(azim_r);
+    params->sun_and_mode[1] = se;
+    params->sun_and_mode[2] = -ce * std::cos(azim_r);
+    params->sun_and_mode[3] = s->env_present ? 1.0f : 0.0f;
+    params->moon_dir_phase[0] = 0.0f;
+    params->moon_dir_phase[1] = -1.0f;
+    params->moon_dir_phase[2] = 0.0f;
+    params->moon_dir_phase[3] = 0.0f;
+    params->moon_extra[0] = std::clamp(float(s->cvar("r_moon_size")), 0.1f, 50.0f);
+    params->moon_extra[1] = 1.0f;
+    params->moon_extra[2] = std::clamp(float(s->cvar("r_moon_disc_brightness")), 0.0f, 5.0f);
+    params->moon_extra[3] = std::clamp(float(s->cvar("r_sun_disc_brightness")), 0.0f, 5.0f);
+    params->sun_extra[0] = std::clamp(float(s->cvar("r_sun_size")), 0.1f, 50.0f);
+    params->sun_extra[1] = 1.0f;
+    float vflat = 1.0f;
+    if (s->cvar("r_sun_horizon_flatten") != 0.0) {
+        // atmospheric refraction R(h) = 1 / tan(h + 7.31 / (h + 4.4)) arcmin
+        // (Saemundsson 1986) at the real disc's upper and lower limb
+        constexpr float kRealSunRadiusDeg = 0.265f;
+        auto refraction = [](float h_deg) {
+            const float h = std::max(h_deg, -1.5f);
+            return 1.0f / std::tan((h + 7.31f / (h + 4.4f)) * 3.14159265358979323846f / 180.0f);
+        };
+        const float lift = (refraction(elev_deg - kRealSunRadiusDeg) - refraction(elev_deg + kRealSunRadiusDeg)) / 60.0f;
+        vflat = std::clamp(1.0f - lift / (2.0f * kRealSunRadiusDeg), 0.5f, 1.0f);
+    }
+    params->sun_extra[2] = vflat;
+    params->sun_extra[3] = 0.0f;
+    params->sun_extra2[0] = params->moon_extra[3];
     return PT_OK;
 }
 
@@ -1377,7 +1435,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx) {
                                p.hdri_dir_pmf, p.hdri_col, p.hdri_count);
     else
         rc = pt_gpu_upload_env(ctx, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, 0);
-    return rc;
+    if (rc) return rc;
+    return pt_gpu_upload_moon(ctx, p.moon_rgba, p.moon_w, p.moon_h);
 }
 
 int pt_build_analytic_bvh(const float* cr, uint32_t n, PtBvhNode* nodes_out, uint32_t* n_nodes,

@@ -77,8 +77,15 @@ typedef struct PtPathParams {
     uint32_t light_tree_enabled;    /* must be 0 (uniform pick); the tree is not built here */
     uint32_t light_tree_node_count;
     uint32_t rr_start;              /* Russian roulette starts at bounce b >= rr_start; reference: 2 */
-    float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 2 procedural, 3 Hosek) */
+    float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 1 env map, 2 procedural,
+                                       3 Hosek-Wilkie; 2 and 3 are not built) */
     uint32_t reserved[4];
+    /* gradient sky (no env map): the moon and the sun-disc shape
+       (shaders/PathTrace.slang:766, 1222-1241; engine fill src/engine/Engine.cpp:8324-8410) */
+    float    moon_dir_phase[4];     /* moon dir xyz (y < -0.1: hidden), phase angle in w */
+    float    moon_extra[4];         /* size multiplier, distance ratio, disc brightness, - */
+    float    sun_extra[4];          /* size multiplier, distance ratio, vertical flatten (1 = round), - */
+    float    sun_extra2[4];         /* sun disc brightness, -, -, - */
 } PtPathParams;
 
 /* 32-byte BVH node, identical to the reference's BvhNode / TriBvhNode
@@ -158,6 +165,12 @@ int pt_gpu_upload_lights(pt_gpu_ctx* ctx, const float* recs20, uint32_t n);
 int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H,
                       const float* marginal, const float* conditional,
                       const float* hdri_dir_pmf, const float* hdri_col, uint32_t n_hdri);
+
+/* ---- moon surface map (the moon_map texture of the gradient sky's moon disc,
+ *      moonDisc, shaders/PathTrace.slang:3212-3353) ----
+ * RGBA32F W x H, lat-long over the moon's near side.  Needed only when a dispatch
+ * shows the moon (moon_dir_phase.y >= -0.1 with no env map).  W = H = 0 removes it. */
+int pt_gpu_upload_moon(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H);
 
 /* ---- render target: the reference's accum_hdr RGBA32F texture, .a = frame count ---- */
 int pt_gpu_set_target(pt_gpu_ctx* ctx, uint32_t width, uint32_t height);
@@ -293,7 +306,7 @@ int pt_gpu_diff_get_backward_stats(pt_gpu_ctx* ctx, PtStats* out);
  * Nothing in this call allocates (no cudaMalloc, cudaFree or allocating
  * library routine).  The scene must have been uploaded to ctx beforehand.
  * Limits: width*height <= 65536 pixels (e.g. 256 x 256); larger frames return
- * PT_ERR_INVALID.  The array (about 22.5 MiB) is held by every GPU that loads
+ * PT_ERR_INVALID.  The array (about 23.5 MiB) is held by every GPU that loads
  * the library until the process exits.  All calls on a device share it and it
  * keeps the last call's contents (each call clears what must start at zero);
  * calls that overlap on the same GPU race and must be serialised.  The first

@@ -81,6 +81,10 @@ int pt_scene_set_materials(pt_scene* s, const float* mats12, uint32_t n);
  * A "black env" is an all-zero image: present, total luminance 0. */
 int pt_scene_set_env(pt_scene* s, const float* rgb, uint32_t W, uint32_t H);
 
+/* Moon surface map for the gradient sky (the reference engine's moon_map
+ * texture): RGBA float[4*W*H].  W = H = 0 clears it. */
+int pt_scene_set_moon(pt_scene* s, const float* rgba, uint32_t W, uint32_t H);
+
 /* Camera (src/renderer/Camera.h): position, yaw/pitch (radians), vertical fov (deg). */
 int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float pitch,
                         float fov_deg);
@@ -89,7 +93,9 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
  * r_max_bounces 8, r_spp 1, r_mis 1, r_firefly_clamp 10, r_caustics 1,
  * r_refract_bounces 4, r_env_intensity 1, r_accum_ema_alpha 0,
  * r_analytic_bvh_threshold 16, r_hdri_extract_percentile 0.005, r_light_tree 0,
- * r_rr_start 2 (extension), r_denoiser 0. Returns PT_ERR_INVALID for unknown names. */
+ * r_rr_start 2 (extension), r_denoiser 0; gradient sky (no env map): r_sun_elevation 30,
+ * r_sun_azimuth 135 (degrees), r_sun_size 1, r_sun_disc_brightness 1, r_sun_horizon_flatten 1,
+ * r_moon_size 1, r_moon_disc_brightness 0.7. Returns PT_ERR_INVALID for unknown names. */
 int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
 int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);
 
@@ -126,6 +132,8 @@ typedef struct PtPackedScene {
     const float*     hdri_col;      /* 8 float4 */
     uint32_t         env_present;
     const uint32_t*  prim_mat_ids;  /* per packed record, NULL when no prim uses the table */
+    const float*     moon_rgba;     /* moon surface map (RGBA, moon_w x moon_h), NULL when unset */
+    uint32_t         moon_w, moon_h;
 } PtPackedScene;
 int pt_scene_packed(pt_scene* s, PtPackedScene* out);
 

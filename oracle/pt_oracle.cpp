@@ -10,6 +10,7 @@
 
 #include <atomic>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -117,6 +118,76 @@ inline float f_acos(float x) {
     const float s = std::sqrt((1.0f - x) * (1.0f + x));
     return f_atan2(s, x);
 }
+inline float bits_f(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// exp, log, pow, asin (procedural sky).  exp: Cody-Waite reduction by ln 2
+// (k = rint(x log2 e), r = x - k ln2_hi - k ln2_lo, |r| <= ln2 / 2) and the
+// Taylor series of e^r to degree 8, scaled by 2^k.  log: x = m 2^e with m in
+// [sqrt(1/2), sqrt(2)), log m = 2 atanh(s), s = (m - 1) / (m + 1), odd series to
+// s^11.  pow(x, y) = exp(y log x) for x > 0.  asin(x) = atan2(x, sqrt(1 - x^2)).
+constexpr float kLog2E = 0x1.715476p+0f;
+constexpr float kLn2Hi = 0x1.62e4p-1f;            // 16 significant bits: k * hi exact for |k| < 256
+constexpr float kLn2Lo = 0x1.7f7d1cp-20f;         // float(ln 2 - hi)
+constexpr float kLn2F = 0x1.62e43p-1f;
+constexpr float kSqrtHalf = 0x1.6a09e6p-1f;
+constexpr float kE2 = 0.5f, kE3 = float(1.0 / 6.0), kE4 = float(1.0 / 24.0), kE5 = float(1.0 / 120.0),
+                kE6 = float(1.0 / 720.0), kE7 = float(1.0 / 5040.0), kE8 = float(1.0 / 40320.0);
+constexpr float kL3 = float(1.0 / 3.0), kL5 = float(1.0 / 5.0), kL7 = float(1.0 / 7.0), kL9 = float(1.0 / 9.0),
+                kL11 = float(1.0 / 11.0);
+
+inline float f_exp(float x) {
+    if (!(x < 88.7f)) return (x != x) ? x : std::numeric_limits<float>::infinity();
+    if (x < -103.0f) return 0.0f;
+    const float k = std::rint(x * kLog2E);
+    float r = x - k * kLn2Hi;
+    r = r - k * kLn2Lo;
+    float p = kE8;
+    p = p * r + kE7;
+    p = p * r + kE6;
+    p = p * r + kE5;
+    p = p * r + kE4;
+    p = p * r + kE3;
+    p = p * r + kE2;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    const int ki = int(k);
+    // 2^k in two exact steps (k may leave the normal exponent range)
+    const int k1 = ki / 2, k2 = ki - k1;
+    return (p * bits_f(uint32_t(127 + k1) << 23)) * bits_f(uint32_t(127 + k2) << 23);
+}
+inline float f_log(float x) {
+    if (!(x > 0.0f)) return (x == 0.0f) ? -std::numeric_limits<float>::infinity() : std::numeric_limits<float>::quiet_NaN();
+    if (x == std::numeric_limits<float>::infinity()) return x;
+    int e;
+    float m = std::frexp(x, &e);   // x = m 2^e, m in [0.5, 1)
+    if (m < kSqrtHalf) {
+        m = m * 2.0f;
+        e -= 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = kL11;
+    p = p * s2 + kL9;
+    p = p * s2 + kL7;
+    p = p * s2 + kL5;
+    p = p * s2 + kL3;
+    const float lm = 2.0f * s + (2.0f * s) * (s2 * p);
+    return float(e) * kLn2F + lm;
+}
+inline float f_pow(float x, float y) {
+    if (y == 0.0f || x == 1.0f) return 1.0f;
+    if (x == 0.0f) return (y > 0.0f) ? 0.0f : std::numeric_limits<float>::infinity();
+    if (x < 0.0f) return std::numeric_limits<float>::quiet_NaN();
+    return f_exp(y * f_log(x));
+}
+inline float f_asin(float x) {
+    const float c = std::sqrt((1.0f - x) * (1.0f + x));
+    return f_atan2(x, c);
+}
 
 template <class R> struct M;
 template <> struct M<float> {
@@ -124,12 +195,18 @@ template <> struct M<float> {
     static float cos(float x) { return f_cos(x); }
     static float atan2(float y, float x) { return f_atan2(y, x); }
     static float acos(float x) { return f_acos(x); }
+    static float exp(float x) { return f_exp(x); }
+    static float pow(float x, float y) { return f_pow(x, y); }
+    static float asin(float x) { return f_asin(x); }
 };
 template <> struct M<double> {
     static double sin(double x) { return std::sin(x); }
     static double cos(double x) { return std::cos(x); }
     static double atan2(double y, double x) { return std::atan2(y, x); }
     static double acos(double x) { return std::acos(x); }
+    static double exp(double x) { return std::exp(x); }
+    static double pow(double x, double y) { return std::pow(x, y); }
+    static double asin(double x) { return std::asin(x); }
 };
 
 // HLSL min/max return the non-NaN operand (IEEE minNum/maxNum).
@@ -454,12 +531,140 @@ template <class R> struct Tracer {
     V3<R> texel(uint32_t u, uint32_t v) const {
         return ld3<R>(S.env_rgba + (size_t(v) * S.env_w + u) * 4);
     }
-    V3<R> sky_color(V3<R> rd) const {
-        if (!P.env_map_present) {
-            // gradient sky (PathTrace.slang:3391-3392); sun/moon discs are not built
-            const R t = clampv(R(0.5) * (rd.y + R(1)), R(0), R(1));
-            return lerp(V3<R>{R(0.50), R(0.55), R(0.62)}, V3<R>{R(1), R(1), R(1)}, t);
+    // ---- gradient sky (no env map): PathTrace.slang:3112-3353, 3373-3464 ----
+    static R sat(R x) { return clampv(x, R(0), R(1)); }
+    static R smoothstep(R e0, R e1, R x) {
+        const R t = sat((x - e0) / (e1 - e0));
+        return t * t * (R(3) - R(2) * t);
+    }
+    V3<R> sun_dir() const { return ld3<R>(Q.sun_and_mode); }
+    static V3<R> sky_gradient(V3<R> rd) {   // skyColorBase, gradient mode
+        const R t = clampv(R(0.5) * (rd.y + R(1)), R(0), R(1));
+        return lerp(V3<R>{R(0.50), R(0.55), R(0.62)}, V3<R>{R(1), R(1), R(1)}, t);
+    }
+    V3<R> sun_disc(V3<R> rd) const {   // sunDisc
+        const V3<R> sd = sun_dir();
+        const V3<R> zero{R(0), R(0), R(0)};
+        if (sd.y < R(-0.10)) return zero;
+        const R ang = dot(rd, sd);
+        const R sun_mult = mx(R(Q.sun_extra[0]) * R(Q.sun_extra[1]), R(0.1));
+        const R r_deg = R(0.55) * sun_mult;
+        const R cos_r = M<R>::cos(r_deg * R(0.0174533));
+        const R halo_deg = lerp(R(2.0), R(8.0), sat(R(1) - sd.y));
+        const R halo_rad = halo_deg * R(0.0174533);
+        const R cos_halo = M<R>::cos(halo_rad);
+        if (ang <= cos_halo) return zero;
+        const R vflat = R(Q.sun_extra[2]);
+        const bool oval = vflat < R(0.999);
+        bool inside = false;
+        if (ang > cos_r) {
+            if (!oval) {
+                inside = true;
+            } else {
+                const V3<R> lr = normalize(cross(V3<R>{R(0), R(1), R(0)}, sd));
+                const V3<R> lu = cross(sd, lr);
+                const V3<R> delta = rd - sd * ang;
+                const R h_off = dot(delta, lr), v_off = dot(delta, lu);
+                const R r_h = r_deg * R(0.0174533);
+                const R r_v = r_h * vflat;
+                const R ellipse = (h_off * h_off) / (r_h * r_h) + (v_off * v_off) / (r_v * r_v);
+                inside = ellipse <= R(1);
+            }
         }
+        const R am = R(1) / mx(sd.y, R(0.04));
+        const R atm = M<R>::exp(R(-0.30) * am);
+        const R warmth = sat((am - R(1)) * R(0.18));
+        const V3<R> col = lerp(V3<R>{R(1.00), R(0.98), R(0.94)}, V3<R>{R(1.55), R(0.55), R(0.20)}, warmth);
+        R halo = R(0);
+        if (ang > cos_halo) {
+            const R t_h = (ang - cos_halo) / (R(1) - cos_halo);
+            const R falloff = lerp(R(8.0), R(3.0), sat(R(1) - sd.y));
+            halo = M<R>::pow(t_h, falloff);
+        }
+        const R bright = mx(R(Q.sun_extra2[0]), R(0));
+        if (inside) return (col * (R(250.0) * atm) + col * halo * atm * R(4.0)) * bright;
+        return col * halo * atm * R(4.0) * bright;
+    }
+    V3<R> moon_texel(int32_t x, int32_t y) const {
+        return ld3<R>(S.moon_rgba + (size_t(y) * S.moon_w + x) * 4);
+    }
+    V3<R> moon_disc(V3<R> rd) const {   // moonDisc
+        const float* mph = Q.moon_dir_phase;
+        const V3<R> zero{R(0), R(0), R(0)};
+        if (R(mph[1]) < R(-0.10)) return zero;
+        const V3<R> m_dir = ld3<R>(mph);
+        const V3<R> sun = sun_dir();
+        const R ang = dot(rd, m_dir);
+        const R size_mult = mx(R(Q.moon_extra[0]) * R(Q.moon_extra[1]), R(0.1));
+        const R r_deg = R(0.55) * size_mult;
+        const R halo_deg = R(1.5) * size_mult;
+        const R cos_r = M<R>::cos(r_deg * R(0.0174533));
+        const R cos_halo = M<R>::cos(halo_deg * R(0.0174533));
+        if (ang <= cos_halo) return zero;
+        const V3<R> col_tint{R(0.92), R(0.94), R(1.00)};
+        const R moon_am = R(1) / mx(R(mph[1]), R(0.04));
+        const R moon_atm = M<R>::exp(R(-0.30) * moon_am);
+        const R warmth_m = sat((moon_am - R(1)) * R(0.18));
+        const V3<R> col_atm = lerp(V3<R>{R(1), R(1), R(1)}, V3<R>{R(1.20), R(0.65), R(0.40)}, warmth_m);
+        R halo = R(0);
+        if (ang > cos_halo) {
+            const R t_h = (ang - cos_halo) / (R(1) - cos_halo);
+            halo = M<R>::pow(t_h, R(4.0)) * R(0.6);
+        }
+        if (ang > cos_r) {
+            const R t_d = (ang - cos_r) / (R(1) - cos_r);
+            const V3<R> ax = (std::fabs(m_dir.y) < R(0.99)) ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(1), R(0), R(0)};
+            const V3<R> t_a = normalize(cross(ax, m_dir));
+            const V3<R> t_b = cross(m_dir, t_a);
+            const R disc_scale = R(1) / mx(M<R>::sin(r_deg * R(0.0174533)), R(1e-5));
+            const R du = dot(rd, t_a) * disc_scale;
+            const R dv = dot(rd, t_b) * disc_scale;
+            const R r2 = du * du + dv * dv;
+            const R zz = std::sqrt(mx(R(1) - r2, R(0)));
+            const V3<R> n_world = t_a * du + t_b * dv - m_dir * zz;
+            const R lit = sat(dot(n_world, sun) * R(10.0) + R(0.05));
+            if (lit <= R(0)) return col_tint * col_atm * halo * moon_atm * R(0.05);
+            const R anti_sun_dot = -dot(m_dir, sun);
+            const R anti_sun_ang = M<R>::acos(sat(anti_sun_dot));
+            const R eclipse = R(1) - smoothstep(R(0.0122), R(0.0218), anti_sun_ang);
+            const R lon = M<R>::atan2(du, zz);
+            const R lat = M<R>::asin(clampv(dv, R(-1), R(1)));
+            const R u_tex = sat(R(0.5) + lon / R(6.28318530718));
+            const R v_tex = sat(R(0.5) - lat / R(3.14159265358979));
+            const int32_t mw = int32_t(S.moon_w), mh = int32_t(S.moon_h);
+            const R fx = u_tex * R(mw) - R(0.5), fy = v_tex * R(mh) - R(0.5);
+            const int32_t ix = int32_t(std::floor(fx)), iy = int32_t(std::floor(fy));
+            const R tx = fx - R(ix), ty = fy - R(iy);
+            const int32_t x0 = std::min(std::max(ix, 0), mw - 1), x1 = std::min(std::max(ix + 1, 0), mw - 1);
+            const int32_t y0 = std::min(std::max(iy, 0), mh - 1), y1 = std::min(std::max(iy + 1, 0), mh - 1);
+            const V3<R> surface = lerp(lerp(moon_texel(x0, y0), moon_texel(x1, y0), tx),
+                                       lerp(moon_texel(x0, y1), moon_texel(x1, y1), tx), ty);
+            const R limb = R(0.55) + R(0.45) * std::sqrt(sat(t_d));
+            const R bright_mult = mx(R(Q.moon_extra[2]), R(0));
+            const R disc_scale_b = R(3.5) * bright_mult;
+            const V3<R> lit_col = col_tint * col_atm * surface * (disc_scale_b * lit * limb * moon_atm) +
+                                  col_tint * col_atm * halo * lit * moon_atm * (R(0.6) * bright_mult);
+            const V3<R> eclipse_col = V3<R>{R(0.55), R(0.15), R(0.04)} * surface * (limb * moon_atm * R(1.2));
+            return lerp(lit_col, eclipse_col, eclipse);
+        }
+        const R phase_b = R(0.5) * (R(1) - M<R>::cos(R(mph[3])));
+        return col_tint * col_atm * halo * phase_b * moon_atm * R(0.3);
+    }
+    // sampleSunDisc (PathTraceMath.slang:55-68)
+    V3<R> sample_sun_disc(V3<R> sd, uint32_t& seed) const {
+        const R u1 = randf<R>(seed);
+        const R u2 = randf<R>(seed);
+        const R r = std::sqrt(u1) * R(0.00465);
+        const R phi = R(6.28318530718) * u2;
+        const R dx = M<R>::cos(phi) * r, dy = M<R>::sin(phi) * r;
+        const V3<R> ax = (std::fabs(sd.y) < R(0.99)) ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(1), R(0), R(0)};
+        const V3<R> t = normalize(cross(ax, sd));
+        const V3<R> b = cross(sd, t);
+        return normalize(sd + t * dx + b * dy);
+    }
+
+    V3<R> sky_color(V3<R> rd) const {
+        if (!P.env_map_present) return sky_gradient(rd) + moon_disc(rd) + sun_disc(rd);
         const int32_t w = int32_t(S.env_w), hh = int32_t(S.env_h);
         const R u = M<R>::atan2(rd.z, rd.x) * R(1.0 / 6.28318530718) + R(0.5);
         const R v = M<R>::acos(clampv(rd.y, R(-1), R(1))) * R(1.0 / 3.14159265359);
@@ -794,6 +999,48 @@ template <class R> struct Tracer {
                         }
                     }
                     skip_sky = (Q.mis_enabled == 0u);
+                } else {
+                    // gradient sky: sun NEE, moon NEE, skylight ambient (PathTrace.slang:6546-6667)
+                    const V3<R> sd = sun_dir();
+                    if (sd.y > R(0)) {
+                        const R n_dot_l = mx(R(0), dot(nf, sd));
+                        const V3<R> sun_jit = sample_sun_disc(sd, seed);
+                        const V3<R> trans = (n_dot_l > R(0)) ? transmittance(hp + nf * R(1e-3), sun_jit, R(1e30))
+                                                              : V3<R>{R(0), R(0), R(0)};
+                        const R am = R(1) / mx(sd.y, R(0.04));
+                        const R trans_atm = M<R>::exp(R(-0.30) * am);
+                        const R warmth = sat((am - R(1)) * R(0.18));
+                        const V3<R> sun_col =
+                            lerp(V3<R>{R(1.00), R(0.97), R(0.92)}, V3<R>{R(1.55), R(0.55), R(0.20)}, warmth);
+                        const R strength = R(80.0) * trans_atm;
+                        const V3<R> sun_rad = sun_col * strength;
+                        const V3<R> brdf = h.albedo / kPi;
+                        if (n_dot_l > R(0) && any_pos(trans)) add(thr * sun_rad * trans * brdf * n_dot_l, true);
+                    }
+                    const float* mph = Q.moon_dir_phase;
+                    if (R(mph[1]) > R(0)) {
+                        const R phase_b = R(0.5) * (R(1) - M<R>::cos(R(mph[3])));
+                        if (phase_b > R(0.01)) {
+                            const V3<R> moon_jit = sample_sun_disc(ld3<R>(mph), seed);
+                            const R ndl = mx(R(0), dot(nf, moon_jit));
+                            if (ndl > R(0)) {
+                                const V3<R> t_m = transmittance(hp + nf * R(1e-3), moon_jit, R(1e30));
+                                if (any_pos(t_m)) {
+                                    const R m_elev = mx(R(mph[1]), R(0.04));
+                                    const R m_am = R(1) / m_elev;
+                                    const R m_atm = M<R>::exp(R(-0.30) * m_am);
+                                    const R m_warmth = sat((m_am - R(1)) * R(0.18));
+                                    const V3<R> m_col = lerp(V3<R>{R(0.92), R(0.94), R(1.00)},
+                                                             V3<R>{R(1.20), R(0.65), R(0.40)}, m_warmth);
+                                    const V3<R> moon_rad = m_col * (R(0.3) * phase_b * m_atm);
+                                    const V3<R> brdf = h.albedo / kPi;
+                                    add(thr * moon_rad * t_m * brdf * ndl, true);
+                                }
+                            }
+                        }
+                    }
+                    add(thr * h.albedo * sky_gradient(nf), false);
+                    skip_sky = true;
                 }
                 thr = thr * h.albedo;
                 ro = hp + nf * R(1e-3);
@@ -1008,7 +1255,9 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
     if (x1 > W || y1 > H || x0 > x1 || y0 > y1) return -1;
     // tlas (hardware RT), the light tree and the no-env-map sky branch
     // (procedural sun/moon NEE) are not restated.
-    if (head->tlas_present || params->light_tree_enabled || !head->env_map_present) return -6;
+    if (head->tlas_present || params->light_tree_enabled) return -6;
+    if (params->sun_and_mode[3] == 2.0f || params->sun_and_mode[3] == 3.0f) return -6;
+    if (!head->env_map_present && params->moon_dir_phase[1] >= -0.10f && !scene->moon_rgba) return -6;
     orc::Counters c;
     if (fp64)
         orc::render<double>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
@@ -1023,7 +1272,9 @@ int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtP
                    double* grad_albedo, double* grad_emission) {
     if (!scene || !head || !params || !dl_di_rgba || !grad_albedo || !grad_emission || W == 0 || H == 0)
         return -1;
-    if (head->tlas_present || params->light_tree_enabled || !head->env_map_present) return -6;
+    if (head->tlas_present || params->light_tree_enabled) return -6;
+    if (params->sun_and_mode[3] == 2.0f || params->sun_and_mode[3] == 3.0f) return -6;
+    if (!head->env_map_present && params->moon_dir_phase[1] >= -0.10f && !scene->moon_rgba) return -6;
     if (params->firefly_clamp > 0.0f) return -7;   // the clamp is not differentiable
     for (size_t i = 0; i < 3 * size_t(scene->material_count); ++i) grad_albedo[i] = grad_emission[i] = 0.0;
     orc::adjoint(*scene, *head, *params, W, H, frames, dl_di_rgba, threads, grad_albedo, grad_emission);
@@ -1035,5 +1286,9 @@ float oracle_cosf(float x) { return orc::f_cos(x); }
 float oracle_atan2f(float y, float x) { return orc::f_atan2(y, x); }
 float oracle_acosf(float x) { return orc::f_acos(x); }
 uint32_t oracle_pcg_hash(uint32_t x) { return orc::pcg_hash(x); }
+float oracle_expf(float x) { return orc::f_exp(x); }
+float oracle_logf(float x) { return orc::f_log(x); }
+float oracle_powf(float x, float y) { return orc::f_pow(x, y); }
+float oracle_asinf(float x) { return orc::f_asin(x); }
 
 }  // extern "C"

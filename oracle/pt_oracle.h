@@ -69,6 +69,10 @@ float oracle_cosf(float x);
 float oracle_atan2f(float y, float x);
 float oracle_acosf(float x);
 uint32_t oracle_pcg_hash(uint32_t x);
+float oracle_expf(float x);
+float oracle_logf(float x);
+float oracle_powf(float x, float y);
+float oracle_asinf(float x);
 
 #ifdef __cplusplus
 }

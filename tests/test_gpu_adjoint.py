@@ -185,7 +185,7 @@ def test_torch_autograd_function_wraps_forward_backward(pt, dev):
     # the same gradient straight through the C-ABI
     dev.diff_forward(head, prm, 1)
     ref = dev.read_accum()[..., :3]
-    assert np.array_equal(ref, img.numpy())
+    assert np.array_equal(ref, img.detach().numpy())
     ga, ge = dev.diff_backward(2.0 * ref, mats.shape[0])
     np.testing.assert_allclose(albedo.grad.numpy(), ga, rtol=1e-12, atol=0)
     np.testing.assert_allclose(emission.grad.numpy(), ge, rtol=1e-12, atol=0)
