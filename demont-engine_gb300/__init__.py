@@ -45,7 +45,7 @@ class PtPathParams(ctypes.Structure):
     _fields_ = [("refract_budget", f32), ("firefly_clamp", f32), ("mis_enabled", u32),
                 ("accum_ema_alpha", f32), ("bvh_params", u32 * 4), ("light_count", u32),
                 ("light_tree_enabled", u32), ("light_tree_node_count", u32), ("rr_start", u32),
-                ("sun_and_mode", f32 * 4), ("reserved", u32 * 4),
+                ("sun_and_mode", f32 * 4), ("stars", u32), ("reserved", u32 * 3),
                 ("moon_dir_phase", f32 * 4), ("moon_extra", f32 * 4), ("sun_extra", f32 * 4),
                 ("sun_extra2", f32 * 4)]
 
@@ -165,6 +165,11 @@ SIGNATURES = {
     "pt_scene_fill_push": (ctypes.c_int, [ctypes.c_void_p, u32, u32, u32, u32, P(PtPushHead),
                                           P(PtPathParams)]),
     "pt_scene_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pt_scene_exec_cfg": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                         ctypes.c_size_t, P(u32)]),
+    "pt_scene_load_cfg": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                         ctypes.c_size_t, P(u32)]),
+    "pt_load_radiance_hdr": (ctypes.c_int, [ctypes.c_char_p, P(f32), u32, P(u32), P(u32)]),
     "pt_scene_synth": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double]),
     "pt_build_analytic_bvh": (ctypes.c_int, [P(f32), u32, P(PtBvhNode), P(u32), P(u32)]),
     "pt_build_triangle_bvh": (ctypes.c_int, [P(f32), u32, P(u32), u32, P(PtBvhNode), P(u32), P(u32),
@@ -315,6 +320,21 @@ class Scene:
         self._moon_keep = a
         self._check(self.lib.pt_scene_set_moon(self.h, fptr(a), a.shape[1], a.shape[0]))
 
+    def exec_cfg(self, text: str, base_dir: str = "."):
+        """Run console/.cfg text; returns (report of skipped lines, count)."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = u32(0)
+        rc = self.lib.pt_scene_exec_cfg(self.h, text.encode(), base_dir.encode(), buf, len(buf), ctypes.byref(n))
+        self._check(rc)
+        return buf.value.decode(), n.value
+
+    def load_cfg(self, path: str, base_dir: str | None = None):
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = u32(0)
+        self._check(self.lib.pt_scene_load_cfg(self.h, path.encode(), base_dir.encode() if base_dir else None,
+                                               buf, len(buf), ctypes.byref(n)))
+        return buf.value.decode(), n.value
+
     def camera(self, pos, yaw, pitch, fov_deg):
         self._check(self.lib.pt_scene_set_camera(self.h, *pos, yaw, pitch, fov_deg))
 
@@ -364,6 +384,19 @@ def _views_array(views):
         va[i].head, va[i].params = v[3], v[4]
         va[i].frames_per_wave = v[5] if len(v) > 5 else 1
     return va
+
+
+def load_hdr(path: str) -> np.ndarray:
+    """Radiance .hdr file -> (H, W, 3) float32 (pt_load_radiance_hdr)."""
+    lib = load()
+    w, h = u32(0), u32(0)
+    if lib.pt_load_radiance_hdr(path.encode(), None, 0, ctypes.byref(w), ctypes.byref(h)) != PT_OK:
+        raise PtError(-1, f"cannot read {path}")
+    out = np.empty((h.value, w.value, 3), np.float32)
+    rc = lib.pt_load_radiance_hdr(path.encode(), fptr(out), out.size, ctypes.byref(w), ctypes.byref(h))
+    if rc != PT_OK:
+        raise PtError(rc, f"cannot read {path}")
+    return out
 
 
 class Device:

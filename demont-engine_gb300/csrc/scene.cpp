@@ -454,6 +454,9 @@ struct pt_scene {
         {"r_sun_size", 1},           {"r_sun_disc_brightness", 1},
         {"r_sun_horizon_flatten", 1},
         {"r_moon_size", 1},          {"r_moon_disc_brightness", 0.7},
+        {"r_sky_mode", 1},           {"r_show_stars", 0},
+        {"r_capture_seed", 0},
+        {"app_window_width", 0},     {"app_window_height", 0},
     };
 
     // packed state
@@ -1373,7 +1376,16 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
     params->sun_and_mode[0] = ce * std::sin(azim_r);
     params->sun_and_mode[1] = se;
     params->sun_and_mode[2] = -ce * std::cos(azim_r);
-    params->sun_and_mode[3] = s->env_present ? 1.0f : 0.0f;
+    {
+        // r_sky_mode: 0 gradient, 1 hdri (gradient when no map is loaded), 2 procedural,
+        // 3 hosek; the env map is bound only in hdri mode (Engine.cpp:8533-8545)
+        int mode = int(s->cvar("r_sky_mode"));
+        if (mode < 0 || mode > 3) mode = 1;
+        if (mode == 1 && !s->env_present) mode = 0;
+        params->sun_and_mode[3] = float(mode);
+        head->env_map_present = (mode == 1) ? 1u : 0u;
+        params->stars = (mode == 2 && s->cvar("r_show_stars") != 0.0) ? 1u : 0u;
+    }
     params->moon_dir_phase[0] = 0.0f;
     params->moon_dir_phase[1] = -1.0f;
     params->moon_dir_phase[2] = 0.0f;
@@ -1474,6 +1486,374 @@ int pt_build_env_cdf(const float* rgb, uint32_t W, uint32_t H, const uint8_t* ma
     if (!rgb || !marginal || !conditional || !total) return PT_ERR_INVALID;
     *total = env_cdf(rgb, W, H, mask, marginal, conditional);
     return PT_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Radiance .hdr (RGBE) loader and the .cfg scene-fixture front end.
+// ===========================================================================
+namespace {
+
+bool read_line(std::FILE* f, std::string& out) {
+    out.clear();
+    int c;
+    while ((c = std::fgetc(f)) != EOF) {
+        if (c == '\n') return true;
+        out.push_back(char(c));
+    }
+    return !out.empty();
+}
+
+// One scanline of RGBE quadruples: adaptive run-length (marker 2 2 hi lo, then
+// each of the 4 components as runs (byte > 128: count - 128 copies of the next
+// byte) or literals (byte = count raw bytes)), or flat quadruples otherwise.
+bool read_scanline(std::FILE* f, uint32_t width, std::vector<uint8_t>& q) {
+    q.assign(size_t(width) * 4, 0);
+    if (width < 8 || width > 0x7fff) return std::fread(q.data(), 1, q.size(), f) == q.size();
+    uint8_t m[4];
+    if (std::fread(m, 1, 4, f) != 4) return false;
+    if (m[0] != 2 || m[1] != 2 || (m[2] & 0x80) != 0) {
+        std::memcpy(q.data(), m, 4);
+        return std::fread(q.data() + 4, 1, q.size() - 4, f) == q.size() - 4;
+    }
+    if (((uint32_t(m[2]) << 8) | m[3]) != width) return false;
+    for (int c = 0; c < 4; ++c) {
+        uint32_t x = 0;
+        while (x < width) {
+            int lead = std::fgetc(f);
+            if (lead == EOF) return false;
+            const bool run = lead > 128;
+            const uint32_t n = run ? uint32_t(lead - 128) : uint32_t(lead);
+            if (n == 0 || x + n > width) return false;
+            if (run) {
+                const int v = std::fgetc(f);
+                if (v == EOF) return false;
+                for (uint32_t i = 0; i < n; ++i) q[size_t(x + i) * 4 + c] = uint8_t(v);
+            } else {
+                for (uint32_t i = 0; i < n; ++i) {
+                    const int v = std::fgetc(f);
+                    if (v == EOF) return false;
+                    q[size_t(x + i) * 4 + c] = uint8_t(v);
+                }
+            }
+            x += n;
+        }
+    }
+    return true;
+}
+
+bool load_hdr(const char* path, std::vector<float>& rgb, uint32_t& W, uint32_t& H, std::string& why) {
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) {
+        why = std::string("cannot open ") + path;
+        return false;
+    }
+    std::string line;
+    bool ok = read_line(f, line) && (line.find("RADIANCE") != std::string::npos ||
+                                      line.find("RGBE") != std::string::npos);
+    if (!ok) why = "not a Radiance HDR file";
+    while (ok && read_line(f, line)) {
+        if (line.empty()) break;
+        if (line.rfind("FORMAT=", 0) == 0 && line.substr(7) != "32-bit_rle_rgbe") {
+            why = "unsupported FORMAT (only 32-bit_rle_rgbe)";
+            ok = false;
+        }
+    }
+    int h = 0, w = 0;
+    if (ok && !(read_line(f, line) && std::sscanf(line.c_str(), "-Y %d +X %d", &h, &w) == 2 && w > 0 && h > 0 &&
+                uint64_t(w) * uint64_t(h) <= (1ull << 28))) {
+        why = "only -Y h +X w resolution lines are supported";
+        ok = false;
+    }
+    if (ok) {
+        W = uint32_t(w);
+        H = uint32_t(h);
+        rgb.assign(size_t(W) * H * 3, 0.0f);
+        std::vector<uint8_t> q;
+        for (uint32_t y = 0; y < H && ok; ++y) {
+            if (!read_scanline(f, W, q)) {
+                why = "scanline " + std::to_string(y) + " is truncated or malformed";
+                ok = false;
+                break;
+            }
+            float* row = rgb.data() + size_t(y) * W * 3;
+            for (uint32_t x = 0; x < W; ++x) {
+                const uint8_t* e = q.data() + size_t(x) * 4;
+                // the format's value: mantissa * 2^(exponent - 136), zero exponent = black
+                const float sc = e[3] ? std::ldexp(1.0f, int(e[3]) - 136) : 0.0f;
+                row[3 * x + 0] = float(e[0]) * sc;
+                row[3 * x + 1] = float(e[1]) * sc;
+                row[3 * x + 2] = float(e[2]) * sc;
+            }
+        }
+    }
+    std::fclose(f);
+    return ok;
+}
+
+bool to_f(const std::string& t, float& v) {
+    if (t.empty()) return false;
+    char* e = nullptr;
+    v = std::strtof(t.c_str(), &e);
+    return e && *e == '\0';
+}
+bool to_u(const std::string& t, uint32_t& v) {
+    if (t.empty() || t[0] == '-') return false;
+    char* e = nullptr;
+    const unsigned long long x = std::strtoull(t.c_str(), &e, 10);
+    if (!e || *e != '\0' || x > 0xFFFFFFFFull) return false;
+    v = uint32_t(x);
+    return true;
+}
+// lambert / metal / dielectric -> 0 / 1 / 2; water -> -2 (not part of this path); else -1
+int to_mat(const std::string& m) {
+    if (m == "lambert") return PT_MAT_LAMBERT;
+    if (m == "metal") return PT_MAT_METAL;
+    if (m == "dielectric") return PT_MAT_DIELECTRIC;
+    if (m == "water") return -2;
+    return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_load_radiance_hdr(const char* path, float* rgb, uint32_t capacity_floats, uint32_t* width,
+                         uint32_t* height) {
+    if (!path || !width || !height) return PT_ERR_INVALID;
+    std::vector<float> img;
+    uint32_t W = 0, H = 0;
+    std::string why;
+    if (!load_hdr(path, img, W, H, why)) return PT_ERR_INVALID;
+    *width = W;
+    *height = H;
+    if (rgb) {
+        if (capacity_floats < img.size()) return PT_ERR_INVALID;
+        std::memcpy(rgb, img.data(), img.size() * sizeof(float));
+    }
+    return PT_OK;
+}
+
+int pt_scene_exec_cfg(pt_scene* s, const char* text, const char* base_dir, char* skipped, size_t skipped_len,
+                      uint32_t* n_skipped) {
+    if (!s || !text) return PT_ERR_INVALID;
+    std::string report, first_error;
+    uint32_t nskip = 0, nerr = 0, lineno = 0;
+    auto skip = [&](const std::string& line, const char* why) {
+        ++nskip;
+        report += line + "    # " + why + "\n";
+    };
+    auto bad = [&](const std::string& line, const std::string& why) {
+        ++nerr;
+        if (first_error.empty()) first_error = "cfg line " + std::to_string(lineno) + ": " + why + ": " + line;
+        report += line + "    # ERROR: " + why + "\n";
+    };
+    const char* p = text;
+    while (*p) {
+        const char* e = std::strchr(p, '\n');
+        std::string line = e ? std::string(p, size_t(e - p)) : std::string(p);
+        p = e ? e + 1 : p + line.size();
+        ++lineno;
+        const size_t cpos = line.find("//");
+        if (cpos != std::string::npos) line.resize(cpos);
+        while (!line.empty() && (line.back() == '\r' || line.back() == ' ' || line.back() == '\t')) line.pop_back();
+        size_t b = 0;
+        while (b < line.size() && (line[b] == ' ' || line[b] == '\t')) ++b;
+        line = line.substr(b);
+        if (line.empty() || line[0] == '#') continue;
+        std::vector<std::string> tok;
+        {
+            size_t i = 0;
+            while (i < line.size()) {
+                while (i < line.size() && (line[i] == ' ' || line[i] == '\t')) ++i;
+                size_t j = i;
+                while (j < line.size() && line[j] != ' ' && line[j] != '\t') ++j;
+                if (j > i) tok.push_back(line.substr(i, j - i));
+                i = j;
+            }
+        }
+        const std::string& cmd = tok[0];
+        const size_t na = tok.size() - 1;
+        auto F = [&](size_t k, float& v) { return k < tok.size() && to_f(tok[k], v); };
+        auto U = [&](size_t k, uint32_t& v) { return k < tok.size() && to_u(tok[k], v); };
+        float f[16] = {0};
+        uint32_t id = 0;
+        auto floats = [&](size_t first, size_t n) {
+            for (size_t k = 0; k < n; ++k)
+                if (!F(first + k, f[k])) return false;
+            return true;
+        };
+        auto find_prim = [&](Prim*& pr) {
+            if (!U(1, id)) return false;
+            auto it = s->prims.find(id);
+            if (it == s->prims.end()) return false;
+            pr = &it->second;
+            return true;
+        };
+        if (cmd == "prim_sphere" || cmd == "prim_plane") {
+            const bool sph = cmd == "prim_sphere";
+            if ((sph && (na < 9 || na > 11)) || (!sph && na != 9)) { bad(line, "wrong argument count"); continue; }
+            const int m = to_mat(tok[6]);
+            if (m == -2) { skip(line, "water material: not part of this path"); continue; }
+            float rough = 0.0f, ior = 1.5f;
+            if (!U(1, id) || !floats(2, 4) || m < 0 || !F(7, f[4]) || !F(8, f[5]) || !F(9, f[6]) ||
+                (na >= 10 && !F(10, rough)) || (na >= 11 && !F(11, ior))) {
+                bad(line, "malformed arguments");
+                continue;
+            }
+            const int rc = sph ? pt_scene_prim_sphere(s, id, f[0], f[1], f[2], f[3], m, f[4], f[5], f[6], rough, ior)
+                               : pt_scene_prim_plane(s, id, f[0], f[1], f[2], f[3], m, f[4], f[5], f[6], 0.0f, 1.0f);
+            if (rc) bad(line, s->err);
+        } else if (cmd == "prim_set_albedo" || cmd == "prim_set_emission" || cmd == "prim_set_pos" ||
+                   cmd == "prim_set_normal") {
+            Prim* pr = nullptr;
+            if (na != 4 || !find_prim(pr) || !floats(2, 3)) { bad(line, "malformed arguments or unknown id"); continue; }
+            if (cmd == "prim_set_albedo") {
+                std::memcpy(pr->albedo, f, 12);
+            } else if (cmd == "prim_set_emission") {
+                std::memcpy(pr->emission, f, 12);
+            } else {
+                if (cmd == "prim_set_normal" && pr->type != 1) { bad(line, "not a plane"); continue; }
+                if (pr->type == 1) {
+                    const float len = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+                    if (len < 1e-6f) { bad(line, "zero-length normal"); continue; }
+                    for (int k = 0; k < 3; ++k) f[k] /= len;
+                }
+                std::memcpy(pr->pos, f, 12);
+                std::memcpy(pr->prev, f, 12);
+            }
+            s->dirty_prims = true;
+        } else if (cmd == "prim_set_roughness" || cmd == "prim_set_ior" || cmd == "prim_set_radius" ||
+                   cmd == "prim_set_plane_d") {
+            Prim* pr = nullptr;
+            if (na != 2 || !find_prim(pr) || !F(2, f[0])) { bad(line, "malformed arguments or unknown id"); continue; }
+            if (cmd == "prim_set_roughness") {
+                pr->roughness = std::min(std::max(f[0], 0.0f), 1.0f);
+            } else if (cmd == "prim_set_ior") {
+                pr->ior = std::min(std::max(f[0], 1.0f), 2.4f);
+            } else if (cmd == "prim_set_radius") {
+                if (pr->type != 0 || !(f[0] > 0.0f)) { bad(line, "not a sphere or radius <= 0"); continue; }
+                pr->radius_or_d = f[0];
+            } else {
+                if (pr->type != 1) { bad(line, "not a plane"); continue; }
+                pr->radius_or_d = f[0];
+            }
+            s->dirty_prims = true;
+        } else if (cmd == "prim_set_material") {
+            Prim* pr = nullptr;
+            const int m = na == 2 ? to_mat(tok[2]) : -1;
+            if (m == -2) { skip(line, "water material: not part of this path"); continue; }
+            if (na != 2 || !find_prim(pr) || m < 0) { bad(line, "malformed arguments or unknown id"); continue; }
+            pr->material = uint8_t(m);
+            s->dirty_prims = true;
+        } else if (cmd == "prim_set_rotation") {
+            Prim* pr = nullptr;
+            if (na != 5 || !find_prim(pr) || !floats(2, 4)) { bad(line, "malformed arguments or unknown id"); continue; }
+            const float mag = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2] + f[3] * f[3]);
+            if (mag < 1e-6f) { bad(line, "zero-magnitude quaternion"); continue; }
+            const float inv = 1.0f / mag;
+            for (int k = 0; k < 4; ++k) pr->orient[k] = f[k] * inv;
+            s->dirty_prims = true;
+        } else if (cmd == "prim_remove" || cmd == "light_remove") {
+            if (na != 1 || !U(1, id)) { bad(line, "malformed id"); continue; }
+            if (cmd == "prim_remove") {
+                if (!s->prims.erase(id)) { bad(line, "unknown id"); continue; }
+                s->dirty_prims = true;
+            } else {
+                if (!s->lights.erase(id)) { bad(line, "unknown id"); continue; }
+                s->dirty_lights = true;
+            }
+        } else if (cmd == "prim_clear") {
+            s->prims.clear();
+            s->dirty_prims = true;
+        } else if (cmd == "light_clear") {
+            s->lights.clear();
+            s->dirty_lights = true;
+        } else if (cmd == "light_point" || cmd == "light_spot" || cmd == "light_sphere" || cmd == "light_quad") {
+            const size_t want = cmd == "light_point" ? 7 : cmd == "light_spot" ? 12 : cmd == "light_sphere" ? 8 : 15;
+            if (na != want || !U(1, id) || !floats(2, want - 1)) { bad(line, "malformed arguments"); continue; }
+            int rc;
+            if (cmd == "light_point") {
+                rc = pt_scene_light_point(s, id, f[0], f[1], f[2], f[3], f[4], f[5]);
+            } else if (cmd == "light_spot") {
+                rc = pt_scene_light_spot(s, id, f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10]);
+            } else if (cmd == "light_sphere") {
+                rc = pt_scene_light_sphere(s, id, f[0], f[1], f[2], f[3], f[4], f[5], f[6]);
+            } else {
+                rc = pt_scene_light_quad(s, id, f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10],
+                                         f[11], f[12], f[13]);
+            }
+            if (rc) bad(line, s->err);
+        } else if (cmd == "cam_pos") {
+            if (na != 3 || !floats(1, 3)) { bad(line, "want x y z"); continue; }
+            std::memcpy(s->cam_pos, f, 12);
+        } else if (cmd == "cam_yaw" || cmd == "cam_pitch" || cmd == "cam_fov") {
+            if (na != 1 || !F(1, f[0])) { bad(line, "want one number"); continue; }
+            constexpr float kRad = 0.01745329251994329576923690768489f;
+            if (cmd == "cam_yaw") s->cam_yaw = f[0] * kRad;
+            else if (cmd == "cam_fov") s->cam_fov = f[0];
+            else pt_scene_set_camera(s, s->cam_pos[0], s->cam_pos[1], s->cam_pos[2], s->cam_yaw, f[0] * kRad, s->cam_fov);
+        } else if (cmd == "r_sky_mode") {
+            const std::string v = na == 1 ? tok[1] : "";
+            const int mode = v == "gradient" ? 0 : v == "hdri" ? 1 : v == "procedural" ? 2 : v == "hosek" ? 3 : -1;
+            if (mode < 0) { bad(line, "want gradient|hdri|procedural|hosek"); continue; }
+            pt_scene_set_cvar(s, "r_sky_mode", mode);
+        } else if (cmd == "r_env_map") {
+            std::string path = na >= 1 ? line.substr(line.find(tok[1])) : std::string();
+            if (path.size() >= 2 && path.front() == '"' && path.back() == '"') path = path.substr(1, path.size() - 2);
+            if (path.empty()) {   // r_env_map "" : no env map
+                pt_scene_set_env(s, nullptr, 0, 0);
+                continue;
+            }
+            if (path[0] != '/' && base_dir && *base_dir) path = std::string(base_dir) + "/" + path;
+            std::vector<float> img;
+            uint32_t W = 0, H = 0;
+            std::string why;
+            if (!load_hdr(path.c_str(), img, W, H, why)) { bad(line, why); continue; }
+            pt_scene_set_env(s, img.data(), W, H);
+        } else if (cmd == "r_denoiser") {
+            if (na != 1) { bad(line, "want one value"); continue; }
+            pt_scene_set_cvar(s, "r_denoiser", (tok[1] == "off" || tok[1] == "0") ? 0.0 : 1.0);
+        } else {
+            double have = 0.0;
+            if (pt_scene_get_cvar(s, cmd.c_str(), &have) == PT_OK) {   // an in-scope numeric cvar
+                if (na != 1 || !F(1, f[0])) { bad(line, "want one number"); continue; }
+                pt_scene_set_cvar(s, cmd.c_str(), f[0]);
+            } else if (cmd.rfind("r_", 0) == 0 || cmd.rfind("app_", 0) == 0 || cmd.rfind("cam_", 0) == 0 ||
+                       cmd.rfind("pt_", 0) == 0) {
+                skip(line, "setting outside the path tracer's inputs");
+            } else {
+                skip(line, "command outside this path");
+            }
+        }
+    }
+    if (n_skipped) *n_skipped = nskip;
+    if (skipped && skipped_len) {
+        const size_t n = std::min(report.size(), skipped_len - 1);
+        std::memcpy(skipped, report.data(), n);
+        skipped[n] = '\0';
+    }
+    if (nerr) return fail(s, first_error + (nerr > 1 ? " (+" + std::to_string(nerr - 1) + " more)" : ""));
+    return PT_OK;
+}
+
+int pt_scene_load_cfg(pt_scene* s, const char* path, const char* base_dir, char* skipped, size_t skipped_len,
+                      uint32_t* n_skipped) {
+    if (!s || !path) return PT_ERR_INVALID;
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(s, std::string("load_cfg: cannot open ") + path);
+    std::string text;
+    char buf[4096];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, n);
+    std::fclose(f);
+    std::string dir = base_dir ? std::string(base_dir) : std::string(path);
+    if (!base_dir) {
+        const size_t slash = dir.find_last_of('/');
+        dir = (slash == std::string::npos) ? std::string(".") : dir.substr(0, slash);
+    }
+    return pt_scene_exec_cfg(s, text.c_str(), dir.c_str(), skipped, skipped_len, n_skipped);
 }
 
 }  // extern "C"

@@ -78,8 +78,9 @@ typedef struct PtPathParams {
     uint32_t light_tree_node_count;
     uint32_t rr_start;              /* Russian roulette starts at bounce b >= rr_start; reference: 2 */
     float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 1 env map, 2 procedural,
-                                       3 Hosek-Wilkie; 2 and 3 are not built) */
-    uint32_t reserved[4];
+                                       3 Hosek-Wilkie, not built) */
+    uint32_t stars;                 /* exposure_pad.y/z: procedural-sky stars (must be 0: not built) */
+    uint32_t reserved[3];
     /* gradient sky (no env map): the moon and the sun-disc shape
        (shaders/PathTrace.slang:766, 1222-1241; engine fill src/engine/Engine.cpp:8324-8410) */
     float    moon_dir_phase[4];     /* moon dir xyz (y < -0.1: hidden), phase angle in w */

@@ -144,6 +144,37 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
 /* Upload the packed scene into a GPU context (all pt_gpu_upload_* calls). */
 int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
 
+/* ---- scene fixtures in the reference's console (.cfg) syntax ----
+ * One command per line; `//` starts a comment, a line starting with `#` is a
+ * comment.  Executed (src/engine/Engine.cpp:16783-18060, 20308-20450, 2487-2502):
+ *   prim_sphere <id> <x y z> <r> <lambert|metal|dielectric> <r g b> [rough] [ior]
+ *   prim_plane <id> <nx ny nz> <d> <material> <r g b>
+ *   prim_set_albedo|emission|pos|normal <id> <x y z>, prim_set_roughness|ior|radius|plane_d <id> <v>,
+ *   prim_set_material <id> <material>, prim_set_rotation <id> <qx qy qz qw>, prim_remove <id>, prim_clear
+ *   light_point|spot|sphere|quad (argument orders as the reference's commands), light_remove <id>, light_clear
+ *   cam_pos <x y z>, cam_yaw <deg>, cam_pitch <deg>, cam_fov <deg>
+ *   r_sky_mode <gradient|hdri|procedural|hosek>, r_env_map <path.hdr> (relative to base_dir),
+ *   r_denoiser <off|...>, and every numeric cvar of pt_scene_set_cvar (incl. app_window_width/height,
+ *   r_capture_seed, r_show_stars).
+ * Lines outside the path (water, post-processing, denoiser settings, clouds,
+ * SDF, editor, ...) are skipped: `skipped` (nullable, NUL-terminated, truncated
+ * to skipped_len) lists each with the reason and *n_skipped counts them.  A
+ * malformed in-scope line is reported too; the other lines still run and the
+ * call returns PT_ERR_INVALID naming the first bad line. */
+int pt_scene_exec_cfg(pt_scene* s, const char* text, const char* base_dir, char* skipped, size_t skipped_len,
+                      uint32_t* n_skipped);
+/* base_dir NULL: paths relative to the file's directory (the reference engine
+ * resolves them against its working directory: pass that). */
+int pt_scene_load_cfg(pt_scene* s, const char* path, const char* base_dir, char* skipped, size_t skipped_len,
+                      uint32_t* n_skipped);
+
+/* Radiance RGBE .hdr reader (the reference's LoadRadianceHdr contract,
+ * src/renderer/HdrImage.cpp:104-167: -Y h +X w layout, adaptive RLE or flat
+ * scanlines, value = mantissa * 2^(exponent - 136)).  rgb NULL: size query;
+ * else capacity_floats >= 3*w*h. */
+int pt_load_radiance_hdr(const char* path, float* rgb, uint32_t capacity_floats, uint32_t* width,
+                         uint32_t* height);
+
 /* Seeded synthetic scenes (PCG32 stream, seed 0x5EED + config id):
  *   0: 64 spheres + 4 boxes (12-tri meshes) + one 1x1 quad light (radiance 15), black env;
  *   1: 200 displaced icospheres (nu = 22, 9680 tris each) on a 512x512 quad-grid ground,

@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstring>
 #include <span>
+#include <string>
 #include <vector>
 
 #include "core/Log.h"
@@ -26,6 +27,20 @@ std::atomic<int> g_diag_level{0};
 }  // namespace pt::diag
 
 extern "C" {
+
+// LoadRadianceHdr: rgb NULL -> size query; returns 0 on success.
+int ref_load_radiance_hdr(const char* path, float* rgb, uint32_t cap, uint32_t* w, uint32_t* h) {
+    std::string err;
+    const pt::renderer::HdrImage img = pt::renderer::LoadRadianceHdr(path, &err);
+    if (img.width == 0 || img.height == 0) return -1;
+    *w = img.width;
+    *h = img.height;
+    if (rgb) {
+        if (cap < img.rgb.size()) return -2;
+        std::memcpy(rgb, img.rgb.data(), img.rgb.size() * sizeof(float));
+    }
+    return 0;
+}
 
 // centers_radii: 4 floats per prim; prim_id = input index.
 int ref_build_analytic_bvh(const float* cr, uint32_t n, void* nodes_out, uint32_t* n_nodes,
