@@ -62,6 +62,7 @@ struct DFrame {
     // gradient sky (no env map): sun_and_mode.xyz, moon_dir_phase, moon_extra, sun_extra, sun_extra2.x
     V3 sun_dir;
     float sun_bright;
+    uint32_t sky_mode;       // sun_and_mode.w: 0 gradient, 1 env map, 2 procedural
     float4 moon;
     float4 moon_extra;
     float4 sun_extra;
@@ -251,6 +252,59 @@ __device__ V3 moon_disc(const DScene& S, const DFrame& F, V3 rd) {
     return col_tint * col_atm * halo * phase_b * moon_atm * 0.3f;
 }
 
+// procSkyInlineSunDiscAndHalo (shaders/PathTrace.slang:2860-2872)
+__device__ V3 proc_sun_inline(V3 rd, V3 sun) {
+    const float cos_gamma = clampf(dot(rd, sun), -1.0f, 1.0f);
+    const float day = smoothstepf(-0.10f, 0.20f, sun.y);
+    const float disk = smoothstepf(0.99996f, 0.99999f, cos_gamma);
+    const V3 sun_col = lerp3(v3(1.00f, 0.55f, 0.20f), v3(1.00f, 0.95f, 0.85f), day);
+    V3 result = sun_col * (disk * 50.0f) * day;
+    const float halo = f_pow(fmaxf(0.0f, cos_gamma), 80.0f);
+    result = result + sun_col * halo * 0.30f * day;
+    return result;
+}
+
+// procSky with the stars off (shaders/PathTrace.slang:2990-3103)
+__device__ V3 proc_sky(const DFrame& F, V3 rd) {
+    const V3 sun = F.sun_dir;
+    const float cos_theta_raw = clampf(rd.y, -1.0f, 1.0f);
+    const float cos_gamma = clampf(dot(rd, sun), -1.0f, 1.0f);
+    const float sun_elev = sun.y;
+    const float cam_h = fmaxf(F.cam_pos.y, 0.0f);
+    const float planet_r = F.sun_extra.w;
+    float dip = 0.0f;
+    if (planet_r > 0.0f && cam_h > 0.0f) {
+        const float ratio = cam_h / planet_r;
+        dip = sqrtf(2.0f * ratio + ratio * ratio);
+        dip = fminf(dip, 0.5f);
+    }
+    const float cos_theta = clampf(cos_theta_raw + dip, -1.0f, 1.0f);
+    const float day = smoothstepf(-0.10f, 0.20f, sun_elev);
+    const float sunset = smoothstepf(0.30f, -0.05f, sun_elev) * smoothstepf(-0.20f, 0.05f, sun_elev);
+    const V3 zenith_day = v3(0.32f, 0.55f, 0.92f), horizon_day = v3(0.78f, 0.88f, 1.00f);
+    const float side_factor =
+        smoothstepf(0.0f, 0.7f, dot(normalize(v3(rd.x, 0.0f, rd.z)), normalize(v3(sun.x, 0.0f, sun.z))));
+    const V3 horizon_sunset = lerp3(v3(0.95f, 0.45f, 0.20f), v3(1.00f, 0.65f, 0.30f), side_factor);
+    const V3 horizon_col = lerp3(horizon_day, horizon_sunset, sunset);
+    const V3 zenith_col = lerp3(zenith_day, v3(0.18f, 0.18f, 0.30f), sunset * 0.6f);
+    const float t = smoothstepf(0.0f, 0.40f, cos_theta);
+    V3 sky = lerp3(horizon_col, zenith_col, t);
+    const V3 night = v3(0.005f, 0.010f, 0.030f);   // + smoothstep(...) * 0.0 in the source: adds +0
+    sky = lerp3(night, sky, day);
+    sky = sky + proc_sun_inline(rd, sun);          // the stars term is zero with the stars off
+    const V3 sun_col = lerp3(v3(1.00f, 0.55f, 0.20f), v3(1.00f, 0.95f, 0.85f), day);
+    const float wide = f_pow(fmaxf(0.0f, cos_gamma), 6.0f);
+    sky = sky + sun_col * wide * sunset * 0.50f;
+    return v3(fmaxf(sky.x, 0.0f), fmaxf(sky.y, 0.0f), fmaxf(sky.z, 0.0f));
+}
+
+// skyColorBase without an env map (shaders/PathTrace.slang:3445-3464): the dome
+// without celestial overlays, seen by the skylight ambient
+__device__ __forceinline__ V3 sky_base(const DFrame& F, V3 rd) {
+    if (F.sky_mode == 2u) return proc_sky(F, rd) - proc_sun_inline(rd, F.sun_dir);
+    return sky_gradient(rd);
+}
+
 // sampleSunDisc (shaders/PathTraceMath.slang:55-68)
 __device__ __forceinline__ V3 sample_sun_disc(V3 sun_dir, uint32_t& seed) {
     const float u1 = randf(seed);
@@ -269,7 +323,8 @@ __device__ __forceinline__ V3 sample_sun_disc(V3 sun_dir, uint32_t& seed) {
 __device__ V3 sky_env(const DScene& S, const DFrame& F, V3 rd);
 __device__ V3 sky_color(const DScene& S, const DFrame& F, V3 rd) {
     if (F.env_present) return sky_env(S, F, rd);
-    return sky_gradient(rd) + moon_disc(S, F, rd) + sun_disc(F, rd);
+    const V3 base = (F.sky_mode == 2u) ? proc_sky(F, rd) : sky_gradient(rd);
+    return base + moon_disc(S, F, rd) + sun_disc(F, rd);
 }
 
 // skyColor, env-map branch (shaders/PathTrace.slang:3401-3431)
@@ -864,7 +919,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
                                 }
                             }
                         }
-                        P.amb[p] = f4(thr * sf.albedo * sky_gradient(nf), 0.0f);
+                        P.amb[p] = f4(thr * sf.albedo * sky_base(F, nf), 0.0f);
                         shadow_mask |= kAmbBit;
                         st |= kSkipSky;
                     }
@@ -1295,13 +1350,14 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
 }
 
 // Sky of a dispatch: env map (mode 1, or 0 with a map), else the gradient
-// dome with sun/moon discs and their NEE (mode 0).  The procedural and
-// Hosek-Wilkie domes (modes 2, 3) are not built.
+// (mode 0) or procedural (mode 2, stars off) dome with sun/moon discs and
+// their NEE.  The Hosek-Wilkie dome (mode 3) and the stars are not built.
 int check_sky(pt_gpu_ctx* ctx, const pt_gpu_ctx* sc, const PtPushHead* head, const PtPathParams* prm,
               const std::string& who) {
     const float mode = prm->sun_and_mode[3];
-    if (mode == 2.0f || mode == 3.0f)
-        return set_err(ctx, PT_ERR_UNSUPPORTED, who + "procedural / Hosek-Wilkie sky modes (2, 3) are not built");
+    if (mode == 3.0f) return set_err(ctx, PT_ERR_UNSUPPORTED, who + "the Hosek-Wilkie sky (mode 3) is not built");
+    if (mode == 2.0f && prm->stars != 0u)
+        return set_err(ctx, PT_ERR_UNSUPPORTED, who + "procedural-sky stars are not built (set stars = 0)");
     if (head->env_map_present) {
         if (sc->env_w == 0 || sc->env_h == 0) return set_err(ctx, PT_ERR_STATE, who + "env map not uploaded");
     } else if (prm->moon_dir_phase[1] >= -0.10f && sc->moon_w == 0) {
@@ -1317,6 +1373,7 @@ void sky_of(DFrame& F, const PtPathParams* prm) {
     F.moon_extra = make_float4(prm->moon_extra[0], prm->moon_extra[1], prm->moon_extra[2], prm->moon_extra[3]);
     F.sun_extra = make_float4(prm->sun_extra[0], prm->sun_extra[1], prm->sun_extra[2], prm->sun_extra[3]);
     F.sun_bright = prm->sun_extra2[0];
+    F.sky_mode = (prm->sun_and_mode[3] == 2.0f) ? 2u : 0u;
 }
 
 int grid_for(pt_gpu_ctx* c, size_t work, int per_sm) {

@@ -455,6 +455,7 @@ struct pt_scene {
         {"r_sun_horizon_flatten", 1},
         {"r_moon_size", 1},          {"r_moon_disc_brightness", 0.7},
         {"r_sky_mode", 1},           {"r_show_stars", 0},
+        {"r_planet_radius", 6378137.0},
         {"r_capture_seed", 0},
         {"app_window_width", 0},     {"app_window_height", 0},
     };
@@ -1409,7 +1410,7 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
         vflat = std::clamp(1.0f - lift / (2.0f * kRealSunRadiusDeg), 0.5f, 1.0f);
     }
     params->sun_extra[2] = vflat;
-    params->sun_extra[3] = 0.0f;
+    params->sun_extra[3] = std::max(float(s->cvar("r_planet_radius")), 0.0f);
     params->sun_extra2[0] = params->moon_extra[3];
     return PT_OK;
 }

@@ -650,6 +650,57 @@ template <class R> struct Tracer {
         const R phase_b = R(0.5) * (R(1) - M<R>::cos(R(mph[3])));
         return col_tint * col_atm * halo * phase_b * moon_atm * R(0.3);
     }
+    // procSkyInlineSunDiscAndHalo (PathTrace.slang:2860-2872)
+    static V3<R> proc_sun_inline(V3<R> rd, V3<R> sun) {
+        const R cos_gamma = clampv(dot(rd, sun), R(-1), R(1));
+        const R day = smoothstep(R(-0.10), R(0.20), sun.y);
+        const R disk = smoothstep(R(0.99996), R(0.99999), cos_gamma);
+        const V3<R> sun_col = lerp(V3<R>{R(1.00), R(0.55), R(0.20)}, V3<R>{R(1.00), R(0.95), R(0.85)}, day);
+        V3<R> result = disk * R(50.0) * sun_col * day;
+        const R halo = M<R>::pow(mx(R(0), cos_gamma), R(80.0));
+        result = result + halo * sun_col * R(0.30) * day;
+        return result;
+    }
+    // procSky, stars off (PathTrace.slang:2990-3103)
+    V3<R> proc_sky(V3<R> rd) const {
+        const V3<R> sun = sun_dir();
+        const R cos_theta_raw = clampv(rd.y, R(-1), R(1));
+        const R cos_gamma = clampv(dot(rd, sun), R(-1), R(1));
+        const R sun_elev = sun.y;
+        const R cam_h = mx(R(P.pos_fovtan[1]), R(0));
+        const R planet_r = R(Q.sun_extra[3]);
+        R dip = R(0);
+        if (planet_r > R(0) && cam_h > R(0)) {
+            const R ratio = cam_h / planet_r;
+            dip = std::sqrt(R(2) * ratio + ratio * ratio);
+            dip = mn(dip, R(0.5));
+        }
+        const R cos_theta = clampv(cos_theta_raw + dip, R(-1), R(1));
+        const R day = smoothstep(R(-0.10), R(0.20), sun_elev);
+        const R sunset = smoothstep(R(0.30), R(-0.05), sun_elev) * smoothstep(R(-0.20), R(0.05), sun_elev);
+        const V3<R> zenith_day{R(0.32), R(0.55), R(0.92)}, horizon_day{R(0.78), R(0.88), R(1.00)};
+        const R side_factor = smoothstep(R(0), R(0.7), dot(normalize(V3<R>{rd.x, R(0), rd.z}),
+                                                          normalize(V3<R>{sun.x, R(0), sun.z})));
+        const V3<R> horizon_sunset =
+            lerp(V3<R>{R(0.95), R(0.45), R(0.20)}, V3<R>{R(1.00), R(0.65), R(0.30)}, side_factor);
+        const V3<R> horizon_col = lerp(horizon_day, horizon_sunset, sunset);
+        const V3<R> zenith_col = lerp(zenith_day, V3<R>{R(0.18), R(0.18), R(0.30)}, sunset * R(0.6));
+        const R t = smoothstep(R(0), R(0.40), cos_theta);
+        V3<R> sky = lerp(horizon_col, zenith_col, t);
+        const V3<R> night{R(0.005), R(0.010), R(0.030)};
+        sky = lerp(night, sky, day);
+        sky = sky + proc_sun_inline(rd, sun);
+        const V3<R> sun_col = lerp(V3<R>{R(1.00), R(0.55), R(0.20)}, V3<R>{R(1.00), R(0.95), R(0.85)}, day);
+        const R wide = M<R>::pow(mx(R(0), cos_gamma), R(6.0));
+        sky = sky + wide * sun_col * sunset * R(0.50);
+        return {mx(sky.x, R(0)), mx(sky.y, R(0)), mx(sky.z, R(0))};
+    }
+    bool procedural() const { return Q.sun_and_mode[3] == 2.0f; }
+    V3<R> sky_base(V3<R> rd) const {   // skyColorBase without an env map
+        if (procedural()) return proc_sky(rd) - proc_sun_inline(rd, sun_dir());
+        return sky_gradient(rd);
+    }
+
     // sampleSunDisc (PathTraceMath.slang:55-68)
     V3<R> sample_sun_disc(V3<R> sd, uint32_t& seed) const {
         const R u1 = randf<R>(seed);
@@ -664,7 +715,7 @@ template <class R> struct Tracer {
     }
 
     V3<R> sky_color(V3<R> rd) const {
-        if (!P.env_map_present) return sky_gradient(rd) + moon_disc(rd) + sun_disc(rd);
+        if (!P.env_map_present) return (procedural() ? proc_sky(rd) : sky_gradient(rd)) + moon_disc(rd) + sun_disc(rd);
         const int32_t w = int32_t(S.env_w), hh = int32_t(S.env_h);
         const R u = M<R>::atan2(rd.z, rd.x) * R(1.0 / 6.28318530718) + R(0.5);
         const R v = M<R>::acos(clampv(rd.y, R(-1), R(1))) * R(1.0 / 3.14159265359);
@@ -1039,7 +1090,7 @@ template <class R> struct Tracer {
                             }
                         }
                     }
-                    add(thr * h.albedo * sky_gradient(nf), false);
+                    add(thr * h.albedo * sky_base(nf), false);
                     skip_sky = true;
                 }
                 thr = thr * h.albedo;
@@ -1256,7 +1307,7 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
     // tlas (hardware RT), the light tree and the no-env-map sky branch
     // (procedural sun/moon NEE) are not restated.
     if (head->tlas_present || params->light_tree_enabled) return -6;
-    if (params->sun_and_mode[3] == 2.0f || params->sun_and_mode[3] == 3.0f) return -6;
+    if (params->sun_and_mode[3] == 3.0f || (params->sun_and_mode[3] == 2.0f && params->stars)) return -6;
     if (!head->env_map_present && params->moon_dir_phase[1] >= -0.10f && !scene->moon_rgba) return -6;
     orc::Counters c;
     if (fp64)
@@ -1273,7 +1324,7 @@ int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtP
     if (!scene || !head || !params || !dl_di_rgba || !grad_albedo || !grad_emission || W == 0 || H == 0)
         return -1;
     if (head->tlas_present || params->light_tree_enabled) return -6;
-    if (params->sun_and_mode[3] == 2.0f || params->sun_and_mode[3] == 3.0f) return -6;
+    if (params->sun_and_mode[3] == 3.0f || (params->sun_and_mode[3] == 2.0f && params->stars)) return -6;
     if (!head->env_map_present && params->moon_dir_phase[1] >= -0.10f && !scene->moon_rgba) return -6;
     if (params->firefly_clamp > 0.0f) return -7;   // the clamp is not differentiable
     for (size_t i = 0; i < 3 * size_t(scene->material_count); ++i) grad_albedo[i] = grad_emission[i] = 0.0;

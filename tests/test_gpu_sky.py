@@ -81,7 +81,7 @@ def test_moon_above_horizon_needs_a_texture(pt, dev):
     with pytest.raises(pt.PtError):
         dev.render(head, prm, 1)
     prm.moon_dir_phase[1] = -1.0
-    prm.sun_and_mode[3] = 2.0                  # procedural dome: not built
+    prm.sun_and_mode[3] = 3.0                  # Hosek-Wilkie dome: not built
     with pytest.raises(pt.PtError):
         dev.render(head, prm, 1)
 
@@ -107,3 +107,52 @@ def test_adjoint_under_the_gradient_sky_matches_fp64_oracle(pt, orc, dev):
     for g, og in ((ga, oa), (ge, oe)):
         tol = 1e-5 * np.abs(og).max() + 1e-4 * np.abs(og)
         assert np.all(np.abs(g - og) <= tol)
+
+
+PROC = """
+cam_pos 0 2 7
+cam_yaw {yaw}
+cam_pitch {pitch}
+cam_fov 60
+r_sky_mode procedural
+r_show_stars 0
+r_sun_elevation {elev}
+r_sun_azimuth 30
+r_spp 2
+r_max_bounces 3
+prim_plane 1 0 1 0 0 lambert 0.6 0.6 0.6
+prim_sphere 10 0 1 0 1 lambert 0.85 0.85 0.85
+prim_sphere 11 -2.2 0.8 0.5 0.8 dielectric 1 1 1 0 1.5
+light_point 1 -3 2.5 -1 20 8 8
+light_spot 2 -1 2.5 -1 0 -1 0 25 15 10 30 10
+"""
+
+
+@pytest.mark.parametrize("elev,yaw,pitch", [(55.0, 0, -12), (1.5, 30, 1), (-30.0, 0, -10)],
+                         ids=["noon", "sunset_facing_sun", "night"])
+def test_procedural_sky_bit_exact(pt, orc, dev, elev, yaw, pitch):
+    s = pt.Scene()
+    rep, n = s.exec_cfg(PROC.format(elev=elev, yaw=yaw, pitch=pitch))
+    assert n == 0, rep
+    W, H = 72, 48
+    head, prm = s.push(W, H, frame_index=11, reset=1)
+    assert prm.sun_and_mode[3] == 2.0 and prm.stars == 0 and prm.sun_extra[3] > 6e6
+    dev.set_traversal(0)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.render(head, prm, 2)
+    g = dev.read_accum()
+    o, _ = orc.render(s.packed(), head, prm, W, H, 2)
+    assert g[..., :3].mean() > 0.003
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_procedural_stars_are_refused(pt, dev):
+    s = pt.Scene()
+    s.exec_cfg(PROC.format(elev=-20, yaw=0, pitch=0) + "r_show_stars 1\n")
+    dev.upload(s)
+    dev.set_target(16, 16)
+    head, prm = s.push(16, 16)
+    assert prm.stars == 1
+    with pytest.raises(pt.PtError):
+        dev.render(head, prm, 1)
