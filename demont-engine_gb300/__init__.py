@@ -78,6 +78,16 @@ class PtBatchTuning(ctypes.Structure):
                 ("reserved", u32)]
 
 
+class PtLightTreeNode(ctypes.Structure):
+    _fields_ = [("aabb_min", f32 * 3), ("left_first", u32), ("aabb_max", f32 * 3), ("count", u32),
+                ("cone_axis", f32 * 3), ("cone_cos_half", f32), ("intensity", f32), ("pad", f32 * 3)]
+
+
+class PtLightInput(ctypes.Structure):
+    _fields_ = [("type", u32), ("pos", f32 * 3), ("radius", f32), ("intensity", f32 * 3), ("dir", f32 * 3),
+                ("cos_outer", f32), ("u_vec", f32 * 3), ("v_half", f32)]
+
+
 class PtPackedScene(ctypes.Structure):
     _fields_ = [("prims", P(f32)), ("prim_count", u32), ("linear_prim_count", u32),
                 ("bvh_nodes", P(PtBvhNode)), ("bvh_node_count", u32),
@@ -89,7 +99,8 @@ class PtPackedScene(ctypes.Structure):
                 ("env_conditional", P(f32)), ("env_total_luminance", ctypes.c_double),
                 ("hdri_count", u32), ("hdri_dir_pmf", P(f32)), ("hdri_col", P(f32)),
                 ("env_present", u32), ("prim_mat_ids", P(u32)), ("moon_rgba", P(f32)),
-                ("moon_w", u32), ("moon_h", u32)]
+                ("moon_w", u32), ("moon_h", u32), ("light_tree", P(PtLightTreeNode)),
+                ("light_tree_node_count", u32)]
 
 
 # every entry point include/*.h declares, with its ctypes signature
@@ -108,6 +119,7 @@ SIGNATURES = {
     "pt_gpu_upload_env": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32, P(f32), P(f32), P(f32),
                                          P(f32), u32]),
     "pt_gpu_upload_moon": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32]),
+    "pt_gpu_upload_light_tree": (ctypes.c_int, [ctypes.c_void_p, P(PtLightTreeNode), u32]),
     "pt_gpu_set_target": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
     "pt_gpu_read_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
     "pt_gpu_write_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
@@ -170,6 +182,7 @@ SIGNATURES = {
     "pt_scene_load_cfg": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                          ctypes.c_size_t, P(u32)]),
     "pt_load_radiance_hdr": (ctypes.c_int, [ctypes.c_char_p, P(f32), u32, P(u32), P(u32)]),
+    "pt_build_light_tree": (ctypes.c_int, [P(PtLightInput), u32, P(PtLightTreeNode), P(u32)]),
     "pt_scene_synth": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double]),
     "pt_build_analytic_bvh": (ctypes.c_int, [P(f32), u32, P(PtBvhNode), P(u32), P(u32)]),
     "pt_build_triangle_bvh": (ctypes.c_int, [P(f32), u32, P(u32), u32, P(PtBvhNode), P(u32), P(u32),
@@ -384,6 +397,26 @@ def _views_array(views):
         va[i].head, va[i].params = v[3], v[4]
         va[i].frames_per_wave = v[5] if len(v) > 5 else 1
     return va
+
+
+LIGHT_TREE_DTYPE = np.dtype([("aabb_min", "<f4", 3), ("left_first", "<u4"), ("aabb_max", "<f4", 3),
+                             ("count", "<u4"), ("cone_axis", "<f4", 3), ("cone_cos_half", "<f4"),
+                             ("intensity", "<f4"), ("pad", "<f4", 3)])
+LIGHT_INPUT_DTYPE = np.dtype([("type", "<u4"), ("pos", "<f4", 3), ("radius", "<f4"), ("intensity", "<f4", 3),
+                              ("dir", "<f4", 3), ("cos_outer", "<f4"), ("u_vec", "<f4", 3), ("v_half", "<f4")])
+
+
+def build_light_tree(lights: np.ndarray) -> np.ndarray:
+    """lights: structured array of LIGHT_INPUT_DTYPE -> nodes (LIGHT_TREE_DTYPE), pt_build_light_tree."""
+    lib = load()
+    lights = np.ascontiguousarray(lights, LIGHT_INPUT_DTYPE)
+    out = np.zeros(max(2 * len(lights) - 1, 1), LIGHT_TREE_DTYPE)
+    n = u32(0)
+    rc = lib.pt_build_light_tree(lights.ctypes.data_as(P(PtLightInput)), len(lights),
+                                 out.ctypes.data_as(P(PtLightTreeNode)), ctypes.byref(n))
+    if rc != PT_OK:
+        raise PtError(rc, "build_light_tree failed")
+    return out[:n.value]
 
 
 def load_hdr(path: str) -> np.ndarray:

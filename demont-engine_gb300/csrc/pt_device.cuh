@@ -277,6 +277,8 @@ struct DScene {
     float4 hdri_col[8];
     const float4* moon_tex;      // moon surface map (gradient sky), W*H texels, or null
     uint32_t moon_w, moon_h;
+    const float4* ltree;         // light tree, 4 float4 per node (LightTreeNode layout)
+    uint32_t ltree_nodes;
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs

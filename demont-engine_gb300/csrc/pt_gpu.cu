@@ -63,6 +63,7 @@ struct DFrame {
     V3 sun_dir;
     float sun_bright;
     uint32_t sky_mode;       // sun_and_mode.w: 0 gradient, 1 env map, 2 procedural
+    uint32_t light_tree;     // pick NEE lights from the light tree
     float4 moon;
     float4 moon_extra;
     float4 sun_extra;
@@ -417,7 +418,52 @@ __device__ float pdf_env_dir(const DScene& S, const DFrame& F, V3 d) {
 __device__ __forceinline__ float mis_balance(float a, float b) { return a / fmaxf(a + b, 1e-12f); }
 
 // sampleAnalyticLight, uniform pick (shaders/PathTrace.slang:4035-4179)
-__device__ void sample_light(const DScene& S, const DFrame& F, V3 hp, uint32_t& seed, V3& dir, V3& Le,
+// lightTreeImportance (shaders/PathTrace.slang:3932-3966)
+__device__ __forceinline__ float lt_importance(const float4* T, uint32_t idx, V3 hp, V3 n_face) {
+    const float4 v0 = __ldg(T + 4u * idx), v1 = __ldg(T + 4u * idx + 1u);
+    const float4 v2 = __ldg(T + 4u * idx + 2u), v3n = __ldg(T + 4u * idx + 3u);
+    const V3 lo = v3(v0), hi = v3(v1);
+    const V3 to_c = (lo + hi) * 0.5f - hp;
+    const float d2 = fmaxf(dot(to_c, to_c), 1e-12f);
+    const float d = sqrtf(d2);
+    const V3 dir_to = to_c / d;
+    const V3 ext = (hi - lo) * 0.5f;
+    const float rad2 = fmaxf(dot(ext, ext), 1e-12f);
+    const float falloff = 1.0f / fmaxf(d2, rad2);
+    float orient = 1.0f;
+    if (v2.w > -0.999f) {
+        const float cos_emit = -dot(v3(v2), dir_to);
+        orient = saturatef((cos_emit - (v2.w - 0.2f)) / 0.2f);
+    }
+    const float recv = fmaxf(0.0f, dot(n_face, dir_to));
+    return fmaxf(v3n.x * falloff * orient * recv, 1e-8f);
+}
+
+// pickLightFromTree (shaders/PathTrace.slang:3978-4016): one draw per level
+__device__ __forceinline__ uint32_t lt_pick(const DScene& S, V3 hp, V3 n_face, uint32_t& seed, float& pick_pdf) {
+    const float4* T = S.ltree;
+    uint32_t idx = 0;
+    pick_pdf = 1.0f;
+    for (int d = 0; d < 32; ++d) {
+        const uint32_t left_first = __float_as_uint(__ldg(T + 4u * idx).w);
+        if (__float_as_uint(__ldg(T + 4u * idx + 1u).w) > 0u) return left_first;
+        const float il = lt_importance(T, left_first, hp, n_face);
+        const float ir = lt_importance(T, left_first + 1u, hp, n_face);
+        const float total = il + ir;
+        const float p_l = (total > 1e-30f) ? (il / total) : 0.5f;
+        const float u = randf(seed);
+        if (u < p_l) {
+            idx = left_first;
+            pick_pdf *= p_l;
+        } else {
+            idx = left_first + 1u;
+            pick_pdf *= (1.0f - p_l);
+        }
+    }
+    return 0u;
+}
+
+__device__ void sample_light(const DScene& S, const DFrame& F, V3 hp, V3 n_face, uint32_t& seed, V3& dir, V3& Le,
                              float& pdf, float& dist) {
     dir = v3(0.0f, 1.0f, 0.0f);
     Le = v3(0.0f, 0.0f, 0.0f);
@@ -425,9 +471,15 @@ __device__ void sample_light(const DScene& S, const DFrame& F, V3 hp, uint32_t& 
     dist = 1e30f;
     const uint32_t n = F.light_count;
     if (n == 0u) return;
-    const float u_pick = randf(seed);
-    const uint32_t pick = min(uint32_t(u_pick * float(n)), n - 1u);
-    const float pick_pdf = 1.0f / float(n);
+    uint32_t pick;
+    float pick_pdf;
+    if (F.light_tree) {
+        pick = min(lt_pick(S, hp, n_face, seed, pick_pdf), n - 1u);
+    } else {
+        const float u_pick = randf(seed);
+        pick = min(uint32_t(u_pick * float(n)), n - 1u);
+        pick_pdf = 1.0f / float(n);
+    }
     const float4* L = S.lights + 5u * pick;
     const float4 l0 = __ldg(L), l1 = __ldg(L + 1), l2 = __ldg(L + 2), l3 = __ldg(L + 3),
                  l4 = __ldg(L + 4);
@@ -843,7 +895,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
                     if (F.light_count > 0u) {
                         V3 ldir, Le;
                         float lpdf, ldist;
-                        sample_light(S, F, hp, seed, ldir, Le, lpdf, ldist);
+                        sample_light(S, F, hp, nf, seed, ldir, Le, lpdf, ldist);
                         const float ndl = dot(nf, ldir);
                         if (lpdf > 0.0f && ndl > 0.0f) {
                             const float tmax = fmaxf(ldist - 1e-3f, 0.0f);
@@ -1185,6 +1237,8 @@ struct pt_gpu_ctx {
     float hdri_dir[32] = {0}, hdri_col[32] = {0};
     DBuf<float4> moon;
     uint32_t moon_w = 0, moon_h = 0;
+    DBuf<float4> ltree;
+    uint32_t ltree_nodes = 0;
     DBuf<uint32_t> err_word;
     // target
     uint32_t W = 0, H = 0;
@@ -1323,6 +1377,8 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
         S.hdri_col[i] = make_float4(c->hdri_col[4 * i], c->hdri_col[4 * i + 1], c->hdri_col[4 * i + 2],
                                     c->hdri_col[4 * i + 3]);
     }
+    S.ltree = c->ltree.p;
+    S.ltree_nodes = c->ltree_nodes;
     S.moon_tex = c->moon.p;
     S.moon_w = c->moon_w;
     S.moon_h = c->moon_h;
@@ -1374,6 +1430,15 @@ void sky_of(DFrame& F, const PtPathParams* prm) {
     F.sun_extra = make_float4(prm->sun_extra[0], prm->sun_extra[1], prm->sun_extra[2], prm->sun_extra[3]);
     F.sun_bright = prm->sun_extra2[0];
     F.sky_mode = (prm->sun_and_mode[3] == 2.0f) ? 2u : 0u;
+    F.light_tree = (prm->light_tree_enabled != 0u && prm->light_tree_node_count > 0u) ? 1u : 0u;
+}
+
+// the dispatch's light tree must be the uploaded one
+int check_light_tree(pt_gpu_ctx* ctx, const pt_gpu_ctx* sc, const PtPathParams* prm, const std::string& who) {
+    if (prm->light_tree_enabled == 0u || prm->light_tree_node_count == 0u) return PT_OK;
+    if (prm->light_tree_node_count != sc->ltree_nodes)
+        return set_err(ctx, PT_ERR_INVALID, who + "light_tree_node_count disagrees with the uploaded light tree");
+    return PT_OK;
 }
 
 int grid_for(pt_gpu_ctx* c, size_t work, int per_sm) {
@@ -1650,7 +1715,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     for (auto* b : {&ctx->prim_rec, &ctx->prim_geo, &ctx->bvh, &ctx->tri, &ctx->tri_bvh, &ctx->mats,
                     &ctx->lights, &ctx->env, &ctx->accum, &ctx->ray_o, &ctx->ray_d, &ctx->thr,
                     &ctx->rad, &ctx->fsum, &ctx->amb, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
-                    &ctx->sh_tr, &ctx->moon, &ctx->d_srad, &ctx->d_dldi})
+                    &ctx->sh_tr, &ctx->moon, &ctx->ltree, &ctx->d_srad, &ctx->d_dldi})
         dfree(*b);
     dfree(ctx->d_grad);
     dfree(ctx->d_sh_mats);
@@ -1828,6 +1893,24 @@ int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H
     return PT_OK;
 }
 
+int pt_gpu_upload_light_tree(pt_gpu_ctx* ctx, const PtLightTreeNode* nodes, uint32_t n) {
+    if (ctx) ctx->gen++;
+    if (!ctx) return PT_ERR_INVALID;
+    if (n && !nodes) return set_err(ctx, PT_ERR_INVALID, "upload_light_tree: null buffer");
+    // children after their parent and inside the array: every walk ends within 32 levels' reach
+    for (uint32_t i = 0; i < n; ++i) {
+        const PtLightTreeNode& nd = nodes[i];
+        if (nd.count > 1u) return set_err(ctx, PT_ERR_INVALID, "upload_light_tree: leaf count above 1");
+        if (nd.count == 0u && (nd.left_first <= i || uint64_t(nd.left_first) + 1u >= n))
+            return set_err(ctx, PT_ERR_INVALID, "upload_light_tree: bad child index at node " + std::to_string(i));
+    }
+    static_assert(sizeof(PtLightTreeNode) == 64, "light tree node is 4 float4");
+    if (int rc = dupload(ctx, ctx->ltree, nodes, 4 * size_t(n))) return rc;
+    ctx->ltree_nodes = n;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
 int pt_gpu_upload_moon(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H) {
     if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
@@ -1907,7 +1990,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     if (!ctx || !head || !prm) return PT_ERR_INVALID;
     if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "render: no target (pt_gpu_set_target)");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: tlas_present (hardware RT) has no CUDA path");
-    if (prm->light_tree_enabled) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: light tree not built");
+    if (int rc = check_light_tree(ctx, ctx, prm, "render: ")) return rc;
     if (int rc = check_sky(ctx, ctx, head, prm, "render: ")) return rc;
     if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
         (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))
@@ -2266,8 +2349,8 @@ int validate_view(pt_gpu_ctx* ctx, pt_gpu_ctx* sc, const PtBatchView& v, uint32_
     const PtPushHead* head = &v.head;
     const PtPathParams* prm = &v.params;
     if (v.width == 0 || v.height == 0) return set_err(ctx, PT_ERR_INVALID, w + "empty frame");
-    if (head->tlas_present || prm->light_tree_enabled)
-        return set_err(ctx, PT_ERR_UNSUPPORTED, w + "tlas / light tree not built");
+    if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, w + "tlas (hardware RT) has no CUDA path");
+    if (int rc = check_light_tree(ctx, sc, prm, w)) return rc;
     if (int rc = check_sky(ctx, sc, head, prm, w)) return rc;
     if (head->prim_count != sc->prim_count || prm->bvh_params[0] != sc->linear_count ||
         prm->bvh_params[1] != sc->bvh_nodes)
@@ -2752,7 +2835,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     if ((reinterpret_cast<uintptr_t>(accum_device) & 15u) != 0)
         return set_err(ctx, PT_ERR_INVALID, "render_noalloc: accumulation buffer must be 16-byte aligned");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: tlas_present has no CUDA path");
-    if (prm->light_tree_enabled) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: light tree not built");
+    if (int rc = check_light_tree(ctx, ctx, prm, "render_noalloc: ")) return rc;
     if (int rc = check_sky(ctx, ctx, head, prm, "render_noalloc: ")) return rc;
     if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
         (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))

@@ -448,7 +448,7 @@ struct pt_scene {
         {"r_env_intensity", 1},      {"r_accum_ema_alpha", 0},
         {"r_analytic_bvh_threshold", 16},
         {"r_hdri_extract_percentile", 0.005},
-        {"r_light_tree", 0},         {"r_rr_start", 2},
+        {"r_light_tree", 1},         {"r_rr_start", 2},
         {"r_denoiser", 0},
         {"r_sun_elevation", 30},     {"r_sun_azimuth", 135},
         {"r_sun_size", 1},           {"r_sun_disc_brightness", 1},
@@ -470,6 +470,7 @@ struct pt_scene {
     std::vector<PtBvhNode> tri_bvh;
     std::vector<uint32_t> tri_perm;
     std::vector<float> packed_lights;
+    std::vector<PtLightTreeNode> light_tree;
     std::vector<float> env_rgba, env_marg, env_cond;
     double env_total = 0.0;
     std::vector<HdriLight> hdri;
@@ -543,7 +544,187 @@ void pack_mesh(pt_scene* s) {
     s->dirty_mesh = false;
 }
 
+// ---- light tree (src/renderer/LightTree.cpp:BuildLightTree, restated) ----
+struct LtLeaf {
+    float lo[3], hi[3], axis[3];
+    float cos_half;
+    float power;       // scalar luminance x emitter area
+    uint32_t light;
+};
+
+LtLeaf lt_leaf(const PtLightInput& L, uint32_t id) {
+    LtLeaf s{};
+    s.light = id;
+    if (L.type == 0u || L.type == 1u) {          // point, spot: a 1 mm box
+        for (int k = 0; k < 3; ++k) {
+            s.lo[k] = L.pos[k] - 1e-3f;
+            s.hi[k] = L.pos[k] + 1e-3f;
+        }
+    } else if (L.type == 2u) {                    // sphere
+        const float r = std::max(L.radius, 1e-3f);
+        for (int k = 0; k < 3; ++k) {
+            s.lo[k] = L.pos[k] - r;
+            s.hi[k] = L.pos[k] + r;
+        }
+    } else {                                      // quad: |u| + v_half per axis
+        const float vh = std::fabs(L.v_half);
+        for (int k = 0; k < 3; ++k) {
+            const float ext = std::fabs(L.u_vec[k]) + vh;
+            s.lo[k] = L.pos[k] - ext;
+            s.hi[k] = L.pos[k] + ext;
+        }
+    }
+    if (L.type == 0u || L.type == 2u) {           // emits in every direction
+        s.axis[0] = 0.0f; s.axis[1] = 1.0f; s.axis[2] = 0.0f;
+        s.cos_half = -1.0f;
+    } else {
+        for (int k = 0; k < 3; ++k) s.axis[k] = L.dir[k];
+        s.cos_half = (L.type == 1u) ? L.cos_outer : 0.0f;   // quads: the front hemisphere
+    }
+    float lum = 0.2126f * L.intensity[0] + 0.7152f * L.intensity[1] + 0.0722f * L.intensity[2];
+    if (L.type == 2u) {
+        const float r = std::max(L.radius, 1e-3f);
+        lum *= 4.0f * 3.14159265358979f * r * r;
+    } else if (L.type == 3u) {
+        const float ul = std::sqrt(L.u_vec[0] * L.u_vec[0] + L.u_vec[1] * L.u_vec[1] + L.u_vec[2] * L.u_vec[2]);
+        lum *= 4.0f * ul * std::fabs(L.v_half);
+    }
+    s.power = lum;
+    return s;
+}
+
+// smallest cone holding both cones (axis, cosine of the half angle; -1 = sphere)
+void lt_cone_union(const float* a, float ca, const float* b, float cb, float* out, float& cout) {
+    auto keep = [&](const float* ax, float c) {
+        out[0] = ax[0]; out[1] = ax[1]; out[2] = ax[2];
+        cout = c;
+    };
+    if (ca <= -0.999f || cb <= -0.999f) return keep(a, -1.0f);
+    float d = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    d = std::min(std::max(d, -1.0f), 1.0f);
+    const float td = std::acos(d);
+    const float ta = std::acos(std::clamp(ca, -1.0f, 1.0f));
+    const float tb = std::acos(std::clamp(cb, -1.0f, 1.0f));
+    if (td + tb <= ta) return keep(a, ca);
+    if (td + ta <= tb) return keep(b, cb);
+    const float tc = 0.5f * (ta + tb + td);
+    if (tc >= 3.14159265358979f) return keep(a, -1.0f);
+    cout = std::cos(tc);
+    const float rot = tc - ta;
+    const float cr = std::cos(rot), sr = std::sin(rot);
+    float perp[3] = {b[0] - d * a[0], b[1] - d * a[1], b[2] - d * a[2]};
+    const float pl = std::sqrt(perp[0] * perp[0] + perp[1] * perp[1] + perp[2] * perp[2]);
+    if (!(pl > 1e-6f)) {
+        out[0] = a[0]; out[1] = a[1]; out[2] = a[2];
+        if (d < 0.0f) cout = -1.0f;
+        return;
+    }
+    const float inv = 1.0f / pl;
+    for (float& v : perp) v *= inv;
+    for (int k = 0; k < 3; ++k) out[k] = cr * a[k] + sr * perp[k];
+    const float al = std::sqrt(out[0] * out[0] + out[1] * out[1] + out[2] * out[2]);
+    if (al > 1e-6f) {
+        const float ia = 1.0f / al;
+        for (int k = 0; k < 3; ++k) out[k] *= ia;
+    }
+}
+
+void lt_build(std::vector<LtLeaf>& lv, std::vector<PtLightTreeNode>& nodes, uint32_t b, uint32_t e, uint32_t dst) {
+    const uint32_t n = e - b;
+    if (n == 1) {
+        PtLightTreeNode& o = nodes[dst];
+        const LtLeaf& l = lv[b];
+        for (int k = 0; k < 3; ++k) {
+            o.aabb_min[k] = l.lo[k];
+            o.aabb_max[k] = l.hi[k];
+            o.cone_axis[k] = l.axis[k];
+        }
+        o.cone_cos_half = l.cos_half;
+        o.intensity = l.power;
+        o.left_first = l.light;
+        o.count = 1u;
+        return;
+    }
+    float cmin[3], cmax[3];
+    for (int k = 0; k < 3; ++k) {
+        cmin[k] = std::numeric_limits<float>::infinity();
+        cmax[k] = -std::numeric_limits<float>::infinity();
+    }
+    for (uint32_t i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const float c = 0.5f * (lv[i].lo[k] + lv[i].hi[k]);
+            cmin[k] = std::min(cmin[k], c);
+            cmax[k] = std::max(cmax[k], c);
+        }
+    int axis = 0;
+    float widest = cmax[0] - cmin[0];
+    for (int k = 1; k < 3; ++k)
+        if (cmax[k] - cmin[k] > widest) {
+            widest = cmax[k] - cmin[k];
+            axis = k;
+        }
+    const uint32_t mid = b + n / 2;
+    if (!(widest < 1e-6f))
+        std::nth_element(lv.begin() + b, lv.begin() + mid, lv.begin() + e, [axis](const LtLeaf& x, const LtLeaf& y) {
+            return 0.5f * (x.lo[axis] + x.hi[axis]) < 0.5f * (y.lo[axis] + y.hi[axis]);
+        });
+    const uint32_t left = uint32_t(nodes.size());
+    nodes.emplace_back();
+    nodes.emplace_back();
+    lt_build(lv, nodes, b, mid, left);
+    lt_build(lv, nodes, mid, e, left + 1u);
+    PtLightTreeNode& o = nodes[dst];
+    const PtLightTreeNode& l = nodes[left];
+    const PtLightTreeNode& r = nodes[left + 1u];
+    for (int k = 0; k < 3; ++k) {
+        o.aabb_min[k] = std::min(l.aabb_min[k], r.aabb_min[k]);
+        o.aabb_max[k] = std::max(l.aabb_max[k], r.aabb_max[k]);
+    }
+    o.intensity = l.intensity + r.intensity;
+    lt_cone_union(l.cone_axis, l.cone_cos_half, r.cone_axis, r.cone_cos_half, o.cone_axis, o.cone_cos_half);
+    o.left_first = left;
+    o.count = 0u;
+}
+
+void light_tree_of(const std::vector<PtLightInput>& in, std::vector<PtLightTreeNode>& nodes) {
+    nodes.clear();
+    if (in.empty()) return;
+    std::vector<LtLeaf> lv;
+    lv.reserve(in.size());
+    for (uint32_t i = 0; i < in.size(); ++i) lv.push_back(lt_leaf(in[i], i));
+    nodes.reserve(2 * in.size());
+    nodes.emplace_back();
+    lt_build(lv, nodes, 0u, uint32_t(lv.size()), 0u);
+}
+
+// rotate v by the unit quaternion q (xyzw), in the engine's operation order
+void quat_rot_host(const float* q, const float* v, float* out) {
+    const float cx = q[1] * v[2] - q[2] * v[1] + q[3] * v[0];
+    const float cy = q[2] * v[0] - q[0] * v[2] + q[3] * v[1];
+    const float cz = q[0] * v[1] - q[1] * v[0] + q[3] * v[2];
+    out[0] = v[0] + 2.0f * (q[1] * cz - q[2] * cy);
+    out[1] = v[1] + 2.0f * (q[2] * cx - q[0] * cz);
+    out[2] = v[2] + 2.0f * (q[0] * cy - q[1] * cx);
+}
+
 void pack_lights(pt_scene* s) {
+    std::vector<PtLightInput> in;
+    in.reserve(s->lights.size());
+    for (const auto& [id, L] : s->lights) {
+        PtLightInput li{};
+        li.type = L.type;
+        quat_rot_host(L.orient, L.dir, li.dir);
+        quat_rot_host(L.orient, L.u_vec, li.u_vec);
+        for (int k = 0; k < 3; ++k) {
+            li.pos[k] = L.pos[k];
+            li.intensity[k] = L.intensity[k];
+        }
+        li.radius = L.radius;
+        li.cos_outer = L.cos_outer;
+        li.v_half = L.v_half;
+        in.push_back(li);
+    }
+    light_tree_of(in, s->light_tree);
     s->packed_lights.assign(s->lights.size() * 20, 0.0f);
     size_t i = 0;
     for (const auto& [id, L] : s->lights) {
@@ -1285,6 +1466,8 @@ int pt_scene_packed(pt_scene* s, PtPackedScene* o) {
     o->lights = s->packed_lights.data();
     o->light_count = uint32_t(s->lights.size());
     o->env_present = s->env_present ? 1u : 0u;
+    o->light_tree = s->light_tree.empty() ? nullptr : s->light_tree.data();
+    o->light_tree_node_count = uint32_t(s->light_tree.size());
     o->moon_rgba = s->moon_rgba.empty() ? nullptr : s->moon_rgba.data();
     o->moon_w = s->moon_w;
     o->moon_h = s->moon_h;
@@ -1361,8 +1544,11 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
     params->bvh_params[2] = mesh ? uint32_t(s->mesh_idx.size() / 3) : 0u;
     params->bvh_params[3] = mesh ? uint32_t(s->tri_bvh.size()) : 0u;
     params->light_count = uint32_t(s->lights.size());
-    params->light_tree_enabled = 0;
-    params->light_tree_node_count = 0;
+    {
+        const bool tree = s->cvar("r_light_tree") != 0.0 && !s->light_tree.empty();
+        params->light_tree_enabled = tree ? 1u : 0u;
+        params->light_tree_node_count = tree ? uint32_t(s->light_tree.size()) : 0u;
+    }
     params->rr_start = uint32_t(std::max(0.0, s->cvar("r_rr_start")));
     // Sky (src/engine/Engine.cpp:8304-8470, 8533-8545): env map -> mode 1, else the
     // gradient dome (mode 0, the reference's fallback for "hdri" without a map).
@@ -1442,6 +1628,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx) {
                             p.tri_node_count, p.tri_perm, p.tri_perm_count, p.tri_mat_ids);
     if (rc) return rc;
     rc = pt_gpu_upload_lights(ctx, p.lights, p.light_count);
+    if (rc) return rc;
+    rc = pt_gpu_upload_light_tree(ctx, p.light_tree, p.light_tree_node_count);
     if (rc) return rc;
     if (p.env_present)
         rc = pt_gpu_upload_env(ctx, p.env_rgba, p.env_w, p.env_h, p.env_marginal, p.env_conditional,
@@ -1858,3 +2046,13 @@ int pt_scene_load_cfg(pt_scene* s, const char* path, const char* base_dir, char*
 }
 
 }  // extern "C"
+
+extern "C" int pt_build_light_tree(const PtLightInput* lights, uint32_t n, PtLightTreeNode* out, uint32_t* n_nodes) {
+    if ((n && (!lights || !out)) || !n_nodes) return PT_ERR_INVALID;
+    std::vector<PtLightInput> in(lights, lights + n);
+    std::vector<PtLightTreeNode> nodes;
+    light_tree_of(in, nodes);
+    if (!nodes.empty()) std::memcpy(out, nodes.data(), nodes.size() * sizeof(PtLightTreeNode));
+    *n_nodes = uint32_t(nodes.size());
+    return PT_OK;
+}

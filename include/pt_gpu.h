@@ -167,6 +167,24 @@ int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H
                       const float* marginal, const float* conditional,
                       const float* hdri_dir_pmf, const float* hdri_col, uint32_t n_hdri);
 
+/* ---- light tree (replaces the light_tree_nodes buffer of Engine::EnsureLightsUploaded,
+ *      src/engine/Engine.cpp:5420-5545; node layout src/renderer/LightTree.h LightTreeNode) ----
+ * 64 bytes per node: node 0 is the root; internal nodes (count 0) have children
+ * left_first and left_first + 1; leaves (count 1) hold the light index in
+ * left_first.  Used when PtPathParams.light_tree_enabled != 0 and
+ * light_tree_node_count equals the uploaded count. */
+typedef struct PtLightTreeNode {
+    float    aabb_min[3];
+    uint32_t left_first;
+    float    aabb_max[3];
+    uint32_t count;
+    float    cone_axis[3];
+    float    cone_cos_half;
+    float    intensity;
+    float    pad[3];
+} PtLightTreeNode;
+int pt_gpu_upload_light_tree(pt_gpu_ctx* ctx, const PtLightTreeNode* nodes, uint32_t n_nodes);
+
 /* ---- moon surface map (the moon_map texture of the gradient sky's moon disc,
  *      moonDisc, shaders/PathTrace.slang:3212-3353) ----
  * RGBA32F W x H, lat-long over the moon's near side.  Needed only when a dispatch

@@ -92,7 +92,7 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
 /* In-scope cvars with the reference defaults (names as in src/engine/Engine.cpp):
  * r_max_bounces 8, r_spp 1, r_mis 1, r_firefly_clamp 10, r_caustics 1,
  * r_refract_bounces 4, r_env_intensity 1, r_accum_ema_alpha 0,
- * r_analytic_bvh_threshold 16, r_hdri_extract_percentile 0.005, r_light_tree 0,
+ * r_analytic_bvh_threshold 16, r_hdri_extract_percentile 0.005, r_light_tree 1,
  * r_rr_start 2 (extension), r_denoiser 0; gradient sky (no env map): r_sun_elevation 30,
  * r_sun_azimuth 135 (degrees), r_sun_size 1, r_sun_disc_brightness 1, r_sun_horizon_flatten 1,
  * r_moon_size 1, r_moon_disc_brightness 0.7. Returns PT_ERR_INVALID for unknown names. */
@@ -134,6 +134,8 @@ typedef struct PtPackedScene {
     const uint32_t*  prim_mat_ids;  /* per packed record, NULL when no prim uses the table */
     const float*     moon_rgba;     /* moon surface map (RGBA, moon_w x moon_h), NULL when unset */
     uint32_t         moon_w, moon_h;
+    const PtLightTreeNode* light_tree;   /* built over the packed lights, NULL when there are none */
+    uint32_t         light_tree_node_count;
 } PtPackedScene;
 int pt_scene_packed(pt_scene* s, PtPackedScene* out);
 
@@ -174,6 +176,23 @@ int pt_scene_load_cfg(pt_scene* s, const char* path, const char* base_dir, char*
  * else capacity_floats >= 3*w*h. */
 int pt_load_radiance_hdr(const char* path, float* rgb, uint32_t capacity_floats, uint32_t* width,
                          uint32_t* height);
+
+/* Light-tree builder (src/renderer/LightTree.cpp:BuildLightTree): binary
+ * centroid-median tree over the lights, leaves of one light, cone-bounded
+ * clusters, bit-identical to the reference's.  One input per light, in light
+ * order, with dir and u_vec already rotated by the light's orientation
+ * (src/engine/Engine.cpp:5479-5506).  out: capacity 2n - 1 nodes. */
+typedef struct PtLightInput {
+    uint32_t type;          /* 0 point, 1 spot, 2 sphere, 3 quad */
+    float    pos[3];
+    float    radius;
+    float    intensity[3];
+    float    dir[3];
+    float    cos_outer;
+    float    u_vec[3];
+    float    v_half;
+} PtLightInput;
+int pt_build_light_tree(const PtLightInput* lights, uint32_t n, PtLightTreeNode* out, uint32_t* n_nodes);
 
 /* Seeded synthetic scenes (PCG32 stream, seed 0x5EED + config id):
  *   0: 64 spheres + 4 boxes (12-tri meshes) + one 1x1 quad light (radiance 15), black env;

@@ -126,6 +126,19 @@ def trace(packed, head, prm, ro4, rd4, fp64=False):
     return hit, t, c
 
 
+def ref_light_tree(inputs):
+    """The reference's BuildLightTree over a structured array of the
+    LightInput layout (demont_gb300.LIGHT_INPUT_DTYPE); returns the node bytes
+    as a uint8 array of n x 64."""
+    lib = load_ref()
+    inputs = np.ascontiguousarray(inputs)
+    out = np.zeros(max(2 * len(inputs) - 1, 1) * 64, np.uint8)
+    n = u32(0)
+    lib.ref_build_light_tree.argtypes = [ctypes.c_void_p, u32, ctypes.c_void_p, P(u32)]
+    lib.ref_build_light_tree(inputs.ctypes.data, u32(len(inputs)), out.ctypes.data, ctypes.byref(n))
+    return out[: n.value * 64].reshape(n.value, 64)
+
+
 def ref_analytic_bvh(centers_radii):
     """AnalyticBvh::Build of the reference itself: (nodes (m, 8) uint32, perm)."""
     lib = load_ref()

@@ -814,13 +814,61 @@ template <class R> struct Tracer {
 
     // --- sampleAnalyticLight, uniform pick (PathTrace.slang:4035-4179) ---
     struct LightSample { V3<R> dir; V3<R> Le; R pdf; R dist; };
-    LightSample sample_light(V3<R> hp, uint32_t& seed) const {
+    // lightTreeImportance (PathTrace.slang:3932-3966)
+    R lt_importance(uint32_t idx, V3<R> hp, V3<R> n_face) const {
+        const PtLightTreeNode& nd = S.light_tree[idx];
+        const V3<R> lo = ld3<R>(nd.aabb_min), hi = ld3<R>(nd.aabb_max);
+        const V3<R> to_c = (lo + hi) * R(0.5) - hp;
+        const R d2 = mx(dot(to_c, to_c), R(1e-12));
+        const R d = std::sqrt(d2);
+        const V3<R> dir_to = to_c / d;
+        const V3<R> ext = (hi - lo) * R(0.5);
+        const R rad2 = mx(dot(ext, ext), R(1e-12));
+        const R falloff = R(1) / mx(d2, rad2);
+        R orient = R(1);
+        if (R(nd.cone_cos_half) > R(-0.999)) {
+            const R cos_emit = -dot(ld3<R>(nd.cone_axis), dir_to);
+            orient = sat((cos_emit - (R(nd.cone_cos_half) - R(0.2))) / R(0.2));
+        }
+        const R recv = mx(R(0), dot(n_face, dir_to));
+        return mx(R(nd.intensity) * falloff * orient * recv, R(1e-8));
+    }
+    // pickLightFromTree (PathTrace.slang:3978-4016)
+    uint32_t lt_pick(V3<R> hp, V3<R> n_face, uint32_t& seed, R& pick_pdf) const {
+        uint32_t idx = 0;
+        pick_pdf = R(1);
+        for (int d = 0; d < 32; ++d) {
+            const PtLightTreeNode& nd = S.light_tree[idx];
+            if (nd.count > 0u) return nd.left_first;
+            const R il = lt_importance(nd.left_first, hp, n_face);
+            const R ir = lt_importance(nd.left_first + 1u, hp, n_face);
+            const R total = il + ir;
+            const R p_l = (total > R(1e-30)) ? (il / total) : R(0.5);
+            const R u = randf<R>(seed);
+            if (u < p_l) {
+                idx = nd.left_first;
+                pick_pdf = pick_pdf * p_l;
+            } else {
+                idx = nd.left_first + 1u;
+                pick_pdf = pick_pdf * (R(1) - p_l);
+            }
+        }
+        return 0u;
+    }
+
+    LightSample sample_light(V3<R> hp, V3<R> n_face, uint32_t& seed) const {
         LightSample s{{R(0), R(1), R(0)}, {R(0), R(0), R(0)}, R(0), R(1e30)};
         const uint32_t n = Q.light_count;
         if (n == 0u) return s;
-        const R u_pick = randf<R>(seed);
-        const uint32_t pick = std::min(uint32_t(u_pick * R(n)), n - 1u);
-        const R pick_pdf = R(1) / R(n);
+        uint32_t pick;
+        R pick_pdf;
+        if (Q.light_tree_enabled != 0u && Q.light_tree_node_count > 0u) {
+            pick = std::min(lt_pick(hp, n_face, seed, pick_pdf), n - 1u);
+        } else {
+            const R u_pick = randf<R>(seed);
+            pick = std::min(uint32_t(u_pick * R(n)), n - 1u);
+            pick_pdf = R(1) / R(n);
+        }
         const float* L = S.lights + size_t(pick) * 20;
         const uint32_t type = uint32_t(L[7] + 0.5f);
         const V3<R> pos = ld3<R>(L);
@@ -1010,7 +1058,7 @@ template <class R> struct Tracer {
             if (adj && (h.mat == kMatLambert || h.mat == kMatMetal) && adj->nv < 64) adj->vm[adj->nv++] = h.mid;
             if (h.mat == kMatLambert) {
                 if (Q.light_count > 0u) {
-                    const LightSample ls = sample_light(hp, seed);
+                    const LightSample ls = sample_light(hp, nf, seed);
                     const R ndl = dot(nf, ls.dir);
                     if (ls.pdf > R(0) && ndl > R(0)) {
                         const R tmax = mx(ls.dist - R(1e-3), R(0));
@@ -1306,7 +1354,10 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
     if (x1 > W || y1 > H || x0 > x1 || y0 > y1) return -1;
     // tlas (hardware RT), the light tree and the no-env-map sky branch
     // (procedural sun/moon NEE) are not restated.
-    if (head->tlas_present || params->light_tree_enabled) return -6;
+    if (head->tlas_present) return -6;
+    if (params->light_tree_enabled && params->light_tree_node_count &&
+        (!scene->light_tree || params->light_tree_node_count != scene->light_tree_node_count))
+        return -6;
     if (params->sun_and_mode[3] == 3.0f || (params->sun_and_mode[3] == 2.0f && params->stars)) return -6;
     if (!head->env_map_present && params->moon_dir_phase[1] >= -0.10f && !scene->moon_rgba) return -6;
     orc::Counters c;
@@ -1323,7 +1374,10 @@ int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtP
                    double* grad_albedo, double* grad_emission) {
     if (!scene || !head || !params || !dl_di_rgba || !grad_albedo || !grad_emission || W == 0 || H == 0)
         return -1;
-    if (head->tlas_present || params->light_tree_enabled) return -6;
+    if (head->tlas_present) return -6;
+    if (params->light_tree_enabled && params->light_tree_node_count &&
+        (!scene->light_tree || params->light_tree_node_count != scene->light_tree_node_count))
+        return -6;
     if (params->sun_and_mode[3] == 3.0f || (params->sun_and_mode[3] == 2.0f && params->stars)) return -6;
     if (!head->env_map_present && params->moon_dir_phase[1] >= -0.10f && !scene->moon_rgba) return -6;
     if (params->firefly_clamp > 0.0f) return -7;   // the clamp is not differentiable

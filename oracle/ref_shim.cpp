@@ -1,8 +1,9 @@
 // TEST INFRASTRUCTURE ONLY -- C-ABI shim around the reference's own builders.
 //
 // Built by oracle/Makefile together with the reference's unmodified sources
-// src/renderer/AnalyticBvh.cpp, src/renderer/TriangleBvh.cpp and
-// src/renderer/HdrImage.cpp (compiled where they lie, never copied), into
+// src/renderer/AnalyticBvh.cpp, src/renderer/TriangleBvh.cpp,
+// src/renderer/HdrImage.cpp and src/renderer/LightTree.cpp (compiled where
+// they lie, never copied), into
 // oracle/_ref/libref_builders.so.  Tests use it to pin this repository's host
 // builders and the oracle against the reference itself.
 
@@ -16,6 +17,7 @@
 #include "core/Log.h"
 #include "renderer/AnalyticBvh.h"
 #include "renderer/HdrImage.h"
+#include "renderer/LightTree.h"
 #include "renderer/TriangleBvh.h"
 
 // Logging symbols the reference sources reference; the shim discards output.
@@ -27,6 +29,18 @@ std::atomic<int> g_diag_level{0};
 }  // namespace pt::diag
 
 extern "C" {
+
+// BuildLightTree over inputs laid out as LightInput; nodes_out: 2n-1 x 64 B.
+int ref_build_light_tree(const void* inputs, uint32_t n, void* nodes_out, uint32_t* n_nodes) {
+    std::vector<pt::renderer::LightInput> in(n);
+    if (n) std::memcpy(in.data(), inputs, size_t(n) * sizeof(pt::renderer::LightInput));
+    pt::renderer::LightTree tree;
+    pt::renderer::BuildLightTree(in, tree);
+    if (!tree.nodes.empty())
+        std::memcpy(nodes_out, tree.nodes.data(), tree.nodes.size() * sizeof(pt::renderer::LightTreeNode));
+    *n_nodes = uint32_t(tree.nodes.size());
+    return 0;
+}
 
 // LoadRadianceHdr: rgb NULL -> size query; returns 0 on success.
 int ref_load_radiance_hdr(const char* path, float* rgb, uint32_t cap, uint32_t* w, uint32_t* h) {

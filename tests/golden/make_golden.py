@@ -1,5 +1,5 @@
 """Regenerates tests/golden/*.npz from the reference's OWN builders
-(AnalyticBvh::Build, TriangleBvh::Build, BuildEnvCdf), compiled from the
+(AnalyticBvh::Build, TriangleBvh::Build, BuildEnvCdf, BuildLightTree), compiled from the
 reference sources by `make -C oracle ref` into oracle/_ref.  Run where the
 reference tree is present:
 
@@ -14,7 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, os.path.dirname(HERE))
 import oracle  # noqa: E402
-from conftest import XorShift32, xorshift_spheres  # noqa: E402
+from conftest import XorShift32, load_pkg, xorshift_spheres  # noqa: E402
+
+LIGHT_INPUT_DTYPE = load_pkg().LIGHT_INPUT_DTYPE
 
 
 def tri_soup(n, seed):
@@ -32,6 +34,26 @@ def tri_soup(n, seed):
     idx.append([base, base + 1, base + 2])
     idx.append([0, 1, 10 ** 6])
     return np.array(pos, np.float32), np.array(idx, np.uint32)
+
+
+def light_inputs(n, seed, coincident=False):
+    """Mixed point/spot/sphere/quad lights (xorshift32) with tilted spot and
+    quad axes; `coincident`: every light at the same position."""
+    rng = XorShift32(seed)
+    a = np.zeros(n, LIGHT_INPUT_DTYPE)
+    for i in range(n):
+        a[i]["type"] = i % 4
+        p = [rng.rangef(-10, 10) for _ in range(3)]
+        a[i]["pos"] = [1.0, 2.0, 3.0] if coincident else p
+        a[i]["radius"] = rng.rangef(0.05, 1.0)
+        a[i]["intensity"] = [rng.rangef(0.1, 50) for _ in range(3)]
+        d = np.array([rng.rangef(-1, 1), rng.rangef(-1, 0.2), rng.rangef(-1, 1)], np.float64)
+        d /= np.linalg.norm(d) + 1e-12
+        a[i]["dir"] = d.astype(np.float32)
+        a[i]["cos_outer"] = rng.rangef(0.2, 0.95)
+        a[i]["u_vec"] = [rng.rangef(-1, 1) for _ in range(3)]
+        a[i]["v_half"] = rng.rangef(0.1, 1.5)
+    return a
 
 
 def main():
@@ -53,6 +75,10 @@ def main():
     margm, condm, totm = oracle.ref_env_cdf(img, mask)
     out.update(env_img=img, env_mask=mask, env_marg=marg, env_cond=cond, env_total=np.float64(tot),
                env_marg_m=margm, env_cond_m=condm, env_total_m=np.float64(totm))
+    for name, (n, seed, co) in {"lt1": (1, 5, False), "lt7": (7, 11, False), "lt200": (200, 0x1157, False),
+                                "lt16c": (16, 3, True)}.items():
+        inp = light_inputs(n, seed, co)
+        out[f"{name}_in"], out[f"{name}_nodes"] = inp.view(np.uint8).reshape(n, -1), oracle.ref_light_tree(inp)
     np.savez_compressed(os.path.join(HERE, "reference_builders.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_builders.npz"))
 
