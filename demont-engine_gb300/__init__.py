@@ -88,6 +88,11 @@ class PtLightInput(ctypes.Structure):
                 ("cos_outer", f32), ("u_vec", f32 * 3), ("v_half", f32)]
 
 
+class PtDiffStats(ctypes.Structure):
+    _fields_ = [("max_delta", ctypes.c_double), ("mean_delta", ctypes.c_double), ("rms_delta", ctypes.c_double),
+                ("bad_percent", ctypes.c_double), ("total_pixels", ctypes.c_uint64), ("bad_pixels", ctypes.c_uint64)]
+
+
 class PtPackedScene(ctypes.Structure):
     _fields_ = [("prims", P(f32)), ("prim_count", u32), ("linear_prim_count", u32),
                 ("bvh_nodes", P(PtBvhNode)), ("bvh_node_count", u32),
@@ -128,6 +133,7 @@ SIGNATURES = {
     "pt_gpu_render_to_host": (ctypes.c_int, [ctypes.c_void_p, P(PtPushHead), P(PtPathParams), u32,
                                              P(f32)]),
     "pt_gpu_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtStats)]),
+    "pt_gpu_tonemap": (ctypes.c_int, [ctypes.c_void_p, f32, u32, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_set_wave_frames": (ctypes.c_int, [ctypes.c_void_p, u32]),
     "pt_gpu_set_traversal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
@@ -182,6 +188,10 @@ SIGNATURES = {
     "pt_scene_load_cfg": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                          ctypes.c_size_t, P(u32)]),
     "pt_load_radiance_hdr": (ctypes.c_int, [ctypes.c_char_p, P(f32), u32, P(u32), P(u32)]),
+    "pt_write_png": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, u32, u32]),
+    "pt_write_ppm": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, u32, u32]),
+    "pt_imgdiff": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, u32, u32, ctypes.c_double, P(PtDiffStats),
+                                  ctypes.c_void_p]),
     "pt_build_light_tree": (ctypes.c_int, [P(PtLightInput), u32, P(PtLightTreeNode), P(u32)]),
     "pt_scene_synth": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double]),
     "pt_build_analytic_bvh": (ctypes.c_int, [P(f32), u32, P(PtBvhNode), P(u32), P(u32)]),
@@ -419,6 +429,31 @@ def build_light_tree(lights: np.ndarray) -> np.ndarray:
     return out[:n.value]
 
 
+def write_png(path: str, rgba8: np.ndarray):
+    a = np.ascontiguousarray(rgba8, np.uint8)
+    if load().pt_write_png(path.encode(), a.ctypes.data, a.shape[1], a.shape[0]) != PT_OK:
+        raise PtError(-1, f"cannot write {path}")
+
+
+def write_ppm(path: str, rgba8: np.ndarray):
+    a = np.ascontiguousarray(rgba8, np.uint8)
+    if load().pt_write_ppm(path.encode(), a.ctypes.data, a.shape[1], a.shape[0]) != PT_OK:
+        raise PtError(-1, f"cannot write {path}")
+
+
+def imgdiff(a: np.ndarray, b: np.ndarray, bad_threshold: float = 0.0, heatmap: bool = False):
+    """RGBA8 images -> (PtDiffStats, heat map or None), pt_imgdiff."""
+    a = np.ascontiguousarray(a, np.uint8)
+    b = np.ascontiguousarray(b, np.uint8)
+    st = PtDiffStats()
+    hm = np.zeros_like(a) if heatmap else None
+    rc = load().pt_imgdiff(a.ctypes.data, b.ctypes.data, a.shape[1], a.shape[0], bad_threshold, ctypes.byref(st),
+                           hm.ctypes.data if heatmap else None)
+    if rc != PT_OK:
+        raise PtError(rc, "imgdiff failed")
+    return st, hm
+
+
 def load_hdr(path: str) -> np.ndarray:
     """Radiance .hdr file -> (H, W, 3) float32 (pt_load_radiance_hdr)."""
     lib = load()
@@ -492,6 +527,12 @@ class Device:
     def write_accum(self, a):
         a = np.ascontiguousarray(a, np.float32)
         self._check(self.lib.pt_gpu_write_accum(self.h, fptr(a)))
+
+    def tonemap(self, exposure=1.5, op=0, srgb=False):
+        """The accumulation buffer through exposure + tone map -> (H, W, 4) uint8."""
+        out = np.empty((self.H, self.W, 4), np.uint8)
+        self._check(self.lib.pt_gpu_tonemap(self.h, exposure, op, 1 if srgb else 0, out.ctypes.data, 0))
+        return out
 
     def stats(self) -> PtStats:
         s = PtStats()

@@ -1194,6 +1194,91 @@ __global__ void k_accumulate_batch(DPaths P, Batch B, uint32_t npix_total) {
     B.accum[out] = a;
 }
 
+// ---------------------------------------------------------------------------
+// Output step: exposure, tone map and 8-bit quantisation of the accumulation
+// buffer (shaders/PathTrace.slang:3466-3607, 7925-7929).
+// ---------------------------------------------------------------------------
+constexpr float kInvLn2 = 0x1.715476p+0f;
+__device__ __forceinline__ float f_log2(float x) { return f_log(x) * kInvLn2; }
+__device__ __forceinline__ float pow_nz(float x, float y) { return (y == 1.0f) ? x : f_pow(x, y); }
+__device__ __forceinline__ V3 div3(V3 a, V3 b) { return v3(a.x / b.x, a.y / b.y, a.z / b.z); }
+
+__device__ __forceinline__ V3 tm_aces(V3 c) {
+    const float a = 2.51f, b = 0.03f, d = 2.43f, e = 0.59f, f = 0.14f;
+    const V3 num = c * (c * a + v3(b, b, b));
+    const V3 den = c * (c * d + v3(e, e, e)) + v3(f, f, f);
+    const V3 r = div3(num, den);
+    return v3(saturatef(r.x), saturatef(r.y), saturatef(r.z));
+}
+__device__ __forceinline__ float agx_contrast(float x) {
+    const float x2 = x * x, x4 = x2 * x2;
+    return 15.5f * x4 * x2 - 40.14f * x4 * x + 31.96f * x4 - 6.868f * x2 * x + 0.4298f * x2 + 0.1191f * x -
+           0.00232f;
+}
+__device__ V3 tm_agx(V3 c) {
+    const V3 ir0 = v3(0.842479062253094f, 0.0784335999999992f, 0.0792237451477643f);
+    const V3 ir1 = v3(0.0423282422610123f, 0.878468636469772f, 0.0791661274605434f);
+    const V3 ir2 = v3(0.0423756549057051f, 0.0784336f, 0.879142973793104f);
+    V3 v = v3(dot(ir0, c), dot(ir1, c), dot(ir2, c));
+    const float kMinEv = -12.47393f, kMaxEv = 4.026069f;
+    float t[3] = {v.x, v.y, v.z};
+    for (int k = 0; k < 3; ++k) {
+        float l = clampf(f_log2(fmaxf(t[k], 1e-10f)), kMinEv, kMaxEv);
+        l = (l - kMinEv) / (kMaxEv - kMinEv);
+        t[k] = agx_contrast(l);
+    }
+    v = v3(t[0], t[1], t[2]);
+    const float luma = dot(v, v3(0.2126f, 0.7152f, 0.0722f));
+    v = v3(pow_nz(fmaxf(v.x * 1.0f + 0.0f, 0.0f), 1.0f), pow_nz(fmaxf(v.y * 1.0f + 0.0f, 0.0f), 1.0f),
+           pow_nz(fmaxf(v.z * 1.0f + 0.0f, 0.0f), 1.0f));
+    v = v3(luma, luma, luma) + (v - v3(luma, luma, luma)) * 1.0f;
+    const V3 or0 = v3(1.19687900512017f, -0.0980208811401368f, -0.0990297440797205f);
+    const V3 or1 = v3(-0.0528968517574562f, 1.15190312990417f, -0.0989611768448433f);
+    const V3 or2 = v3(-0.0529716355144438f, -0.0980434501171241f, 1.15107367264116f);
+    v = v3(dot(or0, v), dot(or1, v), dot(or2, v));
+    v = v3(pow_nz(fmaxf(v.x, 0.0f), 2.2f), pow_nz(fmaxf(v.y, 0.0f), 2.2f), pow_nz(fmaxf(v.z, 0.0f), 2.2f));
+    return v3(saturatef(v.x), saturatef(v.y), saturatef(v.z));
+}
+__device__ V3 tm_khronos(V3 c) {
+    const float start = 0.8f - 0.04f, desat = 0.15f;
+    const float x = fminf(c.x, fminf(c.y, c.z));
+    const float offset = (x < 0.08f) ? (x - 6.25f * x * x) : 0.04f;
+    c = c - v3(offset, offset, offset);
+    const float peak = fmaxf(c.x, fmaxf(c.y, c.z));
+    if (peak < start) return c;
+    const float d = 1.0f - start;
+    const float new_peak = 1.0f - d * d / (peak + d - start);
+    c = c * (new_peak / peak);
+    const float g = 1.0f - 1.0f / (desat * (peak - new_peak) + 1.0f);
+    return lerp3(c, v3(new_peak, new_peak, new_peak), g);
+}
+__device__ __forceinline__ float srgb_oetf(float c) {
+    c = fmaxf(c, 0.0f);
+    return (c < 0.0031308f) ? c * 12.92f : 1.055f * f_pow(c, 1.0f / 2.4f) - 0.055f;
+}
+__device__ __forceinline__ V3 tonemap_op(V3 c, uint32_t op) {
+    switch (op) {
+        case 1u: return tm_agx(c);
+        case 2u: return tm_khronos(c);
+        case 3u: {
+            const V3 r = div3(c, v3(1.0f, 1.0f, 1.0f) + c);
+            return v3(saturatef(r.x), saturatef(r.y), saturatef(r.z));
+        }
+        case 4u: return v3(saturatef(c.x), saturatef(c.y), saturatef(c.z));
+        default: return tm_aces(c);
+    }
+}
+__device__ __forceinline__ uint32_t unorm8(float v) { return uint32_t(saturatef(v) * 255.0f + 0.5f); }
+
+__global__ void k_tonemap(const float4* accum, uint32_t n, float exposure, uint32_t op, uint32_t srgb,
+                          uchar4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 ldr = tonemap_op(v3(accum[i]) * exposure, op);
+    if (srgb) ldr = v3(srgb_oetf(ldr.x), srgb_oetf(ldr.y), srgb_oetf(ldr.z));
+    out[i] = make_uchar4(uint8_t(unorm8(ldr.x)), uint8_t(unorm8(ldr.y)), uint8_t(unorm8(ldr.z)), 255);
+}
+
 __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint32_t n, uint32_t* hit,
                               float* t) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1237,6 +1322,7 @@ struct pt_gpu_ctx {
     float hdri_dir[32] = {0}, hdri_col[32] = {0};
     DBuf<float4> moon;
     uint32_t moon_w = 0, moon_h = 0;
+    DBuf<uchar4> ldr;
     DBuf<float4> ltree;
     uint32_t ltree_nodes = 0;
     DBuf<uint32_t> err_word;
@@ -1719,6 +1805,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
         dfree(*b);
     dfree(ctx->d_grad);
     dfree(ctx->d_sh_mats);
+    dfree(ctx->ldr);
     dfree(ctx->prim_mat);
     for (auto* b : {&ctx->prim_type, &ctx->seed, &ctx->state, &ctx->hit_id, &ctx->shmask, &ctx->q0,
                     &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word})
@@ -2254,6 +2341,26 @@ int pt_gpu_render_to_host(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathP
     int rc = pt_gpu_render(ctx, head, params, frames);
     if (rc) return rc;
     return pt_gpu_read_accum(ctx, host_rgba);
+}
+
+int pt_gpu_tonemap(pt_gpu_ctx* ctx, float exposure, uint32_t op, int srgb_oetf, uint8_t* rgba8, int on_device) {
+    if (!ctx || !rgba8) return PT_ERR_INVALID;
+    if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "tonemap: no target");
+    if (op > 4u) return set_err(ctx, PT_ERR_INVALID, "tonemap: operator must be 0..4");
+    const size_t n = size_t(ctx->W) * ctx->H;
+    uchar4* dst = reinterpret_cast<uchar4*>(rgba8);
+    if (!on_device) {
+        if (int rc = dalloc(ctx, ctx->ldr, n)) return rc;
+        dst = ctx->ldr.p;
+    } else if (reinterpret_cast<uintptr_t>(rgba8) & 3u) {
+        return set_err(ctx, PT_ERR_INVALID, "tonemap: device output must be 4-byte aligned");
+    }
+    k_tonemap<<<uint32_t((n + 255) / 256), 256, 0, ctx->stream>>>(ctx->accum.p, uint32_t(n), exposure, op,
+                                                                   srgb_oetf ? 1u : 0u, dst);
+    CK(cudaGetLastError());
+    if (!on_device) CK(cudaMemcpyAsync(rgba8, dst, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
 }
 
 int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out) {

@@ -456,6 +456,7 @@ struct pt_scene {
         {"r_moon_size", 1},          {"r_moon_disc_brightness", 0.7},
         {"r_sky_mode", 1},           {"r_show_stars", 0},
         {"r_planet_radius", 6378137.0},
+        {"r_exposure", 1.5},         {"r_tonemap_op", 0},
         {"r_capture_seed", 0},
         {"app_window_width", 0},     {"app_window_height", 0},
     };
@@ -2001,6 +2002,12 @@ int pt_scene_exec_cfg(pt_scene* s, const char* text, const char* base_dir, char*
             std::string why;
             if (!load_hdr(path.c_str(), img, W, H, why)) { bad(line, why); continue; }
             pt_scene_set_env(s, img.data(), W, H);
+        } else if (cmd == "r_tonemap_op") {
+            const std::string v = na == 1 ? tok[1] : "";
+            const int op = v == "aces" ? 0 : v == "agx" ? 1 : v == "khronos_pbr_neutral" ? 2 : v == "reinhard" ? 3
+                         : v == "linear" ? 4 : -1;
+            if (op < 0) { bad(line, "want aces|agx|khronos_pbr_neutral|reinhard|linear"); continue; }
+            pt_scene_set_cvar(s, "r_tonemap_op", op);
         } else if (cmd == "r_denoiser") {
             if (na != 1) { bad(line, "want one value"); continue; }
             pt_scene_set_cvar(s, "r_denoiser", (tok[1] == "off" || tok[1] == "0") ? 0.0 : 1.0);
@@ -2056,3 +2063,153 @@ extern "C" int pt_build_light_tree(const PtLightInput* lights, uint32_t n, PtLig
     *n_nodes = uint32_t(nodes.size());
     return PT_OK;
 }
+
+// ===========================================================================
+// Capture and image comparison (the reference's r_capture_format png|ppm,
+// src/engine/CaptureFormat.h, and tools/imgdiff/ImgDiff.h's metrics).
+// ===========================================================================
+namespace {
+
+uint32_t crc32_of(const uint8_t* p, size_t n, uint32_t crc = 0) {
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; ++k) c = (c & 1u) ? (0xEDB88320u ^ (c >> 1)) : (c >> 1);
+            table[i] = c;
+        }
+        init = true;
+    }
+    crc = ~crc;
+    for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
+    return ~crc;
+}
+
+void put_be32(std::vector<uint8_t>& v, uint32_t x) {
+    v.push_back(uint8_t(x >> 24));
+    v.push_back(uint8_t(x >> 16));
+    v.push_back(uint8_t(x >> 8));
+    v.push_back(uint8_t(x));
+}
+
+void png_chunk(std::vector<uint8_t>& out, const char* type, const std::vector<uint8_t>& data) {
+    put_be32(out, uint32_t(data.size()));
+    std::vector<uint8_t> td(type, type + 4);
+    td.insert(td.end(), data.begin(), data.end());
+    out.insert(out.end(), td.begin(), td.end());
+    put_be32(out, crc32_of(td.data(), td.size()));
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_write_png(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h) {
+    if (!path || !rgba8 || w == 0 || h == 0) return PT_ERR_INVALID;
+    // scanlines with filter byte 0, wrapped in a zlib stream of stored deflate blocks
+    std::vector<uint8_t> raw;
+    raw.reserve(size_t(h) * (size_t(w) * 4 + 1));
+    for (uint32_t y = 0; y < h; ++y) {
+        raw.push_back(0);
+        raw.insert(raw.end(), rgba8 + size_t(y) * w * 4, rgba8 + size_t(y + 1) * w * 4);
+    }
+    std::vector<uint8_t> z = {0x78, 0x01};
+    size_t pos = 0;
+    do {
+        const size_t n = std::min<size_t>(65535, raw.size() - pos);
+        z.push_back((pos + n == raw.size()) ? 1 : 0);
+        z.push_back(uint8_t(n));
+        z.push_back(uint8_t(n >> 8));
+        z.push_back(uint8_t(~n));
+        z.push_back(uint8_t(~n >> 8));
+        z.insert(z.end(), raw.begin() + pos, raw.begin() + pos + n);
+        pos += n;
+    } while (pos < raw.size());
+    uint32_t a = 1, b = 0;   // Adler-32 of the uncompressed data
+    for (uint8_t c : raw) {
+        a = (a + c) % 65521u;
+        b = (b + a) % 65521u;
+    }
+    put_be32(z, (b << 16) | a);
+    std::vector<uint8_t> png = {0x89, 'P', 'N', 'G', 0x0D, 0x0A, 0x1A, 0x0A};
+    std::vector<uint8_t> ihdr;
+    put_be32(ihdr, w);
+    put_be32(ihdr, h);
+    ihdr.insert(ihdr.end(), {8, 6, 0, 0, 0});   // 8-bit RGBA, deflate, no filter, no interlace
+    png_chunk(png, "IHDR", ihdr);
+    png_chunk(png, "IDAT", z);
+    png_chunk(png, "IEND", {});
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return PT_ERR_INVALID;
+    const bool ok = std::fwrite(png.data(), 1, png.size(), f) == png.size();
+    return (std::fclose(f) == 0 && ok) ? PT_OK : PT_ERR_INVALID;
+}
+
+int pt_write_ppm(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h) {
+    if (!path || !rgba8 || w == 0 || h == 0) return PT_ERR_INVALID;
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return PT_ERR_INVALID;
+    std::fprintf(f, "P6\n%u %u\n255\n", w, h);
+    std::vector<uint8_t> rgb(size_t(w) * h * 3);
+    for (size_t i = 0; i < size_t(w) * h; ++i)
+        for (int c = 0; c < 3; ++c) rgb[3 * i + c] = rgba8[4 * i + c];
+    const bool ok = std::fwrite(rgb.data(), 1, rgb.size(), f) == rgb.size();
+    return (std::fclose(f) == 0 && ok) ? PT_OK : PT_ERR_INVALID;
+}
+
+// per-pixel Euclidean distance over the four 8-bit channels; mean, RMS, max and
+// the share above bad_threshold; diff (nullable) = the distance as a heat map
+int pt_imgdiff(const uint8_t* a, const uint8_t* b, uint32_t w, uint32_t h, double bad_threshold,
+               PtDiffStats* out, uint8_t* diff_rgba) {
+    if (!a || !b || !out) return PT_ERR_INVALID;
+    *out = PtDiffStats{};
+    const uint64_t n = uint64_t(w) * h;
+    out->total_pixels = n;
+    if (n == 0) return PT_OK;
+    std::vector<double> dist(n);
+    double sum = 0.0, sum2 = 0.0, mx = 0.0;
+    uint64_t bad = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        int s2 = 0;
+        for (int c = 0; c < 4; ++c) {
+            const int d = int(a[4 * i + c]) - int(b[4 * i + c]);
+            s2 += d * d;
+        }
+        const double d = std::sqrt(double(s2));
+        dist[i] = d;
+        sum += d;
+        sum2 += d * d;
+        mx = std::max(mx, d);
+        if (d > bad_threshold) ++bad;
+    }
+    out->max_delta = mx;
+    out->mean_delta = sum / double(n);
+    out->rms_delta = std::sqrt(sum2 / double(n));
+    out->bad_pixels = bad;
+    out->bad_percent = 100.0 * double(bad) / double(n);
+    if (diff_rgba) {
+        const double scale = mx > 0.0 ? 1.0 / mx : 0.0;
+        for (uint64_t i = 0; i < n; ++i) {
+            const double t = std::clamp(dist[i] * scale, 0.0, 1.0);
+            double r, g, bl;   // black -> purple -> orange -> yellow
+            if (t < 0.33) {
+                const double u = t / 0.33;
+                r = u * 128.0, g = 0.0, bl = u * 192.0;
+            } else if (t < 0.66) {
+                const double u = (t - 0.33) / 0.33;
+                r = 128.0 + u * 127.0, g = u * 80.0, bl = 192.0 * (1.0 - u);
+            } else {
+                const double u = (t - 0.66) / 0.34;
+                r = 255.0, g = 80.0 + u * 175.0, bl = u * 100.0;
+            }
+            diff_rgba[4 * i + 0] = uint8_t(std::clamp(r, 0.0, 255.0) + 0.5);
+            diff_rgba[4 * i + 1] = uint8_t(std::clamp(g, 0.0, 255.0) + 0.5);
+            diff_rgba[4 * i + 2] = uint8_t(std::clamp(bl, 0.0, 255.0) + 0.5);
+            diff_rgba[4 * i + 3] = 255;
+        }
+    }
+    return PT_OK;
+}
+
+}  // extern "C"

@@ -209,6 +209,19 @@ int pt_gpu_render(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* p
 int pt_gpu_render_to_host(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* params,
                           uint32_t frames, float* host_rgba);
 int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out);
+
+/* ---- output step (the `output` store of shaders/PathTrace.slang:7925-7929) ----
+ * The accumulation buffer times `exposure` (the reference's exposure_state: r_exposure
+ * when auto exposure is off) through the tone-map operator (tonemapDispatch,
+ * :3466-3607; r_tonemap_op: 0 aces, 1 agx, 2 khronos_pbr_neutral, 3 reinhard,
+ * 4 linear), optionally the sRGB OETF (the SPIR-V target's), quantised to RGBA8
+ * (round to nearest, alpha 255).  rgba8: width*height*4 bytes, host or device. */
+#define PT_TONEMAP_ACES     0
+#define PT_TONEMAP_AGX      1
+#define PT_TONEMAP_KHRONOS  2
+#define PT_TONEMAP_REINHARD 3
+#define PT_TONEMAP_LINEAR   4
+int pt_gpu_tonemap(pt_gpu_ctx* ctx, float exposure, uint32_t op, int srgb_oetf, uint8_t* rgba8, int on_device);
 /* on != 0: record CUDA events around every closest-hit and transmittance
  * launch so PtStats.extend_ms / shadow_ms report their device time. */
 int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on);

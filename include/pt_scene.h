@@ -95,7 +95,8 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
  * r_analytic_bvh_threshold 16, r_hdri_extract_percentile 0.005, r_light_tree 1,
  * r_rr_start 2 (extension), r_denoiser 0; gradient sky (no env map): r_sun_elevation 30,
  * r_sun_azimuth 135 (degrees), r_sun_size 1, r_sun_disc_brightness 1, r_sun_horizon_flatten 1,
- * r_moon_size 1, r_moon_disc_brightness 0.7. Returns PT_ERR_INVALID for unknown names. */
+ * r_moon_size 1, r_moon_disc_brightness 0.7; output step: r_exposure 1.5, r_tonemap_op 0 (aces).
+ * Returns PT_ERR_INVALID for unknown names. */
 int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
 int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);
 
@@ -193,6 +194,21 @@ typedef struct PtLightInput {
     float    v_half;
 } PtLightInput;
 int pt_build_light_tree(const PtLightInput* lights, uint32_t n, PtLightTreeNode* out, uint32_t* n_nodes);
+
+/* ---- capture and comparison (r_capture_format png|ppm, src/engine/CaptureFormat.h;
+ *      tools/imgdiff/ImgDiff.h) ----
+ * rgba8: w*h*4 bytes, rows top to bottom.  The PNG is 8-bit RGBA (stored deflate
+ * blocks); the PPM is binary P6 RGB. */
+int pt_write_png(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h);
+int pt_write_ppm(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h);
+typedef struct PtDiffStats {
+    double   max_delta, mean_delta, rms_delta;   /* per-pixel Euclidean RGBA distance */
+    double   bad_percent;                        /* share of pixels above bad_threshold */
+    uint64_t total_pixels, bad_pixels;
+} PtDiffStats;
+/* diff_rgba (nullable): w*h*4 heat map of the distance, scaled to the maximum. */
+int pt_imgdiff(const uint8_t* a, const uint8_t* b, uint32_t w, uint32_t h, double bad_threshold,
+               PtDiffStats* out, uint8_t* diff_rgba);
 
 /* Seeded synthetic scenes (PCG32 stream, seed 0x5EED + config id):
  *   0: 64 spheres + 4 boxes (12-tri meshes) + one 1x1 quad light (radiance 15), black env;

@@ -109,6 +109,19 @@ def adjoint(packed, head, prm, W, H, frames, dl_di, threads=0):
     return ga[:n], ge[:n]
 
 
+def tonemap(accum, exposure, op=0, srgb=False):
+    """(H, W, 4) accumulation -> (H, W, 4) uint8 (oracle_tonemap)."""
+    lib = load()
+    a = np.ascontiguousarray(accum, np.float32)
+    out = np.zeros(a.shape[:2] + (4,), np.uint8)
+    lib.oracle_tonemap.argtypes = [P(f32), u32, f32, u32, ctypes.c_int, ctypes.c_void_p]
+    rc = lib.oracle_tonemap(a.ctypes.data_as(P(f32)), u32(a.shape[0] * a.shape[1]), f32(exposure), u32(op),
+                            ctypes.c_int(1 if srgb else 0), out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle_tonemap failed")
+    return out
+
+
 def trace(packed, head, prm, ro4, rd4, fp64=False):
     lib = load()
     ro4 = np.ascontiguousarray(ro4, np.float32)

@@ -1386,6 +1386,88 @@ int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtP
     return 0;
 }
 
+// Output step (PathTrace.slang:3466-3607, 7925-7929), fp32, the kernels' order.
+namespace {
+using orc::V3;
+float satf(float x) { return std::fmin(std::fmax(x, 0.0f), 1.0f); }
+float log2o(float x) { return orc::f_log(x) * 0x1.715476p+0f; }
+float pow_nz(float x, float y) { return (y == 1.0f) ? x : orc::f_pow(x, y); }
+V3<float> sat3(V3<float> v) { return {satf(v.x), satf(v.y), satf(v.z)}; }
+V3<float> div3(V3<float> a, V3<float> b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+V3<float> tm_aces(V3<float> c) {
+    const float a = 2.51f, b = 0.03f, d = 2.43f, e = 0.59f, f = 0.14f;
+    const V3<float> num = c * (c * a + V3<float>{b, b, b});
+    const V3<float> den = c * (c * d + V3<float>{e, e, e}) + V3<float>{f, f, f};
+    return sat3(div3(num, den));
+}
+float agx_contrast(float x) {
+    const float x2 = x * x, x4 = x2 * x2;
+    return 15.5f * x4 * x2 - 40.14f * x4 * x + 31.96f * x4 - 6.868f * x2 * x + 0.4298f * x2 + 0.1191f * x -
+           0.00232f;
+}
+V3<float> tm_agx(V3<float> c) {
+    const V3<float> ir0{0.842479062253094f, 0.0784335999999992f, 0.0792237451477643f};
+    const V3<float> ir1{0.0423282422610123f, 0.878468636469772f, 0.0791661274605434f};
+    const V3<float> ir2{0.0423756549057051f, 0.0784336f, 0.879142973793104f};
+    float t[3] = {orc::dot(ir0, c), orc::dot(ir1, c), orc::dot(ir2, c)};
+    const float kMinEv = -12.47393f, kMaxEv = 4.026069f;
+    for (float& x : t) {
+        float l = std::fmin(std::fmax(log2o(std::fmax(x, 1e-10f)), kMinEv), kMaxEv);
+        l = (l - kMinEv) / (kMaxEv - kMinEv);
+        x = agx_contrast(l);
+    }
+    V3<float> v{t[0], t[1], t[2]};
+    const float luma = orc::dot(v, V3<float>{0.2126f, 0.7152f, 0.0722f});
+    v = {pow_nz(std::fmax(v.x * 1.0f + 0.0f, 0.0f), 1.0f), pow_nz(std::fmax(v.y * 1.0f + 0.0f, 0.0f), 1.0f),
+         pow_nz(std::fmax(v.z * 1.0f + 0.0f, 0.0f), 1.0f)};
+    v = V3<float>{luma, luma, luma} + (v - V3<float>{luma, luma, luma}) * 1.0f;
+    const V3<float> or0{1.19687900512017f, -0.0980208811401368f, -0.0990297440797205f};
+    const V3<float> or1{-0.0528968517574562f, 1.15190312990417f, -0.0989611768448433f};
+    const V3<float> or2{-0.0529716355144438f, -0.0980434501171241f, 1.15107367264116f};
+    v = {orc::dot(or0, v), orc::dot(or1, v), orc::dot(or2, v)};
+    v = {pow_nz(std::fmax(v.x, 0.0f), 2.2f), pow_nz(std::fmax(v.y, 0.0f), 2.2f), pow_nz(std::fmax(v.z, 0.0f), 2.2f)};
+    return sat3(v);
+}
+V3<float> tm_khronos(V3<float> c) {
+    const float start = 0.8f - 0.04f, desat = 0.15f;
+    const float x = std::fmin(c.x, std::fmin(c.y, c.z));
+    const float offset = (x < 0.08f) ? (x - 6.25f * x * x) : 0.04f;
+    c = c - V3<float>{offset, offset, offset};
+    const float peak = std::fmax(c.x, std::fmax(c.y, c.z));
+    if (peak < start) return c;
+    const float d = 1.0f - start;
+    const float new_peak = 1.0f - d * d / (peak + d - start);
+    c = c * (new_peak / peak);
+    const float g = 1.0f - 1.0f / (desat * (peak - new_peak) + 1.0f);
+    return orc::lerp(c, V3<float>{new_peak, new_peak, new_peak}, g);
+}
+float srgb_oetf(float c) {
+    c = std::fmax(c, 0.0f);
+    return (c < 0.0031308f) ? c * 12.92f : 1.055f * orc::f_pow(c, 1.0f / 2.4f) - 0.055f;
+}
+}  // namespace
+
+int oracle_tonemap(const float* accum_rgba, uint32_t n, float exposure, uint32_t op, int srgb, uint8_t* out) {
+    if ((n && (!accum_rgba || !out)) || op > 4u) return -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        const V3<float> c = V3<float>{accum_rgba[4 * i], accum_rgba[4 * i + 1], accum_rgba[4 * i + 2]} * exposure;
+        V3<float> l;
+        switch (op) {
+            case 1: l = tm_agx(c); break;
+            case 2: l = tm_khronos(c); break;
+            case 3: l = sat3(div3(c, V3<float>{1.0f, 1.0f, 1.0f} + c)); break;
+            case 4: l = sat3(c); break;
+            default: l = tm_aces(c); break;
+        }
+        if (srgb) l = {srgb_oetf(l.x), srgb_oetf(l.y), srgb_oetf(l.z)};
+        out[4 * i + 0] = uint8_t(uint32_t(satf(l.x) * 255.0f + 0.5f));
+        out[4 * i + 1] = uint8_t(uint32_t(satf(l.y) * 255.0f + 0.5f));
+        out[4 * i + 2] = uint8_t(uint32_t(satf(l.z) * 255.0f + 0.5f));
+        out[4 * i + 3] = 255;
+    }
+    return 0;
+}
+
 float oracle_sinf(float x) { return orc::f_sin(x); }
 float oracle_cosf(float x) { return orc::f_cos(x); }
 float oracle_atan2f(float y, float x) { return orc::f_atan2(y, x); }

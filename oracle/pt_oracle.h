@@ -63,6 +63,10 @@ int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtP
                    uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
                    double* grad_albedo, double* grad_emission);
 
+/* Output step: RGBA8 of n accumulation texels (the kernels' exposure, tone map,
+ * optional sRGB OETF and rounding). */
+int oracle_tonemap(const float* accum_rgba, uint32_t n, float exposure, uint32_t op, int srgb, uint8_t* out);
+
 /* The polynomial transcendentals shared (by restatement) with the GPU kernels. */
 float oracle_sinf(float x);
 float oracle_cosf(float x);

@@ -80,3 +80,22 @@ def test_gradient_sky_scene_from_cfg_bit_exact(pt, orc, dev, mode):
     o, _ = orc.render(s.packed(), head, prm, W, H, 2)
     assert g[..., :3].mean() > 0.05
     assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+@pytest.mark.parametrize("srgb", [False, True])
+def test_tonemap_kernel_equals_oracle_for_every_operator(pt, orc, dev, srgb, tmp_path):
+    s = pt.Scene()
+    s.exec_cfg(GRADIENT)
+    W, H = 64, 40
+    head, prm = s.push(W, H, frame_index=3, reset=1)
+    dev.set_traversal(0)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.render(head, prm, 4)
+    acc = dev.read_accum()
+    for op in range(5):
+        g = dev.tonemap(exposure=1.3, op=op, srgb=srgb)
+        o = orc.tonemap(acc, 1.3, op, srgb)
+        st, _ = pt.imgdiff(g, o)
+        assert st.max_delta == 0.0, (op, st.max_delta)
+    pt.write_png(str(tmp_path / "frame.png"), g)
