@@ -49,6 +49,22 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def replica_frame_index(rank):
+    """Replicas render disjoint frame ranges of the same workload (independent seeds)."""
+    return rank * 1_000_000
+
+
+def reduce_replicas(dist, times, counts, device):
+    """Whole-job figures over the ranks: the max of each timing (the job ends
+    with its slowest replica) and the sum of each count."""
+    import torch
+    tt = torch.tensor(times, dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    cc = torch.tensor(counts, dtype=torch.float64, device=device)
+    dist.all_reduce(cc, op=dist.ReduceOp.SUM)
+    return tt.tolist(), cc.tolist()
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms (read-only)."""
 
@@ -550,7 +566,7 @@ def main():
     accel = dev.accel_info()
     dev.set_target(W_FULL, H_FULL)
     # replicas: each rank renders its own disjoint frame range of the same workload
-    head, prm = scene.push(W_FULL, H_FULL, frame_index=rank * 1_000_000, reset=1)
+    head, prm = scene.push(W_FULL, H_FULL, frame_index=replica_frame_index(rank), reset=1)
 
     def barrier():
         if pg:
@@ -599,13 +615,7 @@ def main():
     barrier()
 
     if pg:
-        import torch
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        ss = torch.tensor([segs, e2e_segs], dtype=torch.float64, device="cuda")
-        pg.all_reduce(ss, op=pg.ReduceOp.SUM)
-        t_dev, t_e2e = tt.tolist()
-        segs, e2e_segs = ss.tolist()
+        (t_dev, t_e2e), (segs, e2e_segs) = reduce_replicas(pg, [t_dev, t_e2e], [segs, e2e_segs], "cuda")
     if rank != 0:
         if pg:
             pg.destroy_process_group()
