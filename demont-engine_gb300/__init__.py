@@ -47,7 +47,7 @@ class PtPathParams(ctypes.Structure):
                 ("light_tree_enabled", u32), ("light_tree_node_count", u32), ("rr_start", u32),
                 ("sun_and_mode", f32 * 4), ("stars", u32), ("reserved", u32 * 3),
                 ("moon_dir_phase", f32 * 4), ("moon_extra", f32 * 4), ("sun_extra", f32 * 4),
-                ("sun_extra2", f32 * 4)]
+                ("sun_extra2", f32 * 4), ("sdf_params", u32 * 4), ("sdf_params_f", f32 * 4)]
 
 
 class PtBvhNode(ctypes.Structure):
@@ -105,7 +105,7 @@ class PtPackedScene(ctypes.Structure):
                 ("hdri_count", u32), ("hdri_dir_pmf", P(f32)), ("hdri_col", P(f32)),
                 ("env_present", u32), ("prim_mat_ids", P(u32)), ("moon_rgba", P(f32)),
                 ("moon_w", u32), ("moon_h", u32), ("light_tree", P(PtLightTreeNode)),
-                ("light_tree_node_count", u32)]
+                ("light_tree_node_count", u32), ("sdf_clusters", P(f32)), ("sdf_count", u32)]
 
 
 # every entry point include/*.h declares, with its ctypes signature
@@ -125,6 +125,7 @@ SIGNATURES = {
                                          P(f32), u32]),
     "pt_gpu_upload_moon": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32, u32]),
     "pt_gpu_upload_light_tree": (ctypes.c_int, [ctypes.c_void_p, P(PtLightTreeNode), u32]),
+    "pt_gpu_upload_sdf": (ctypes.c_int, [ctypes.c_void_p, P(f32), u32]),
     "pt_gpu_set_target": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
     "pt_gpu_read_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
     "pt_gpu_write_accum": (ctypes.c_int, [ctypes.c_void_p, P(f32)]),
@@ -192,6 +193,11 @@ SIGNATURES = {
     "pt_write_ppm": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, u32, u32]),
     "pt_imgdiff": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, u32, u32, ctypes.c_double, P(PtDiffStats),
                                   ctypes.c_void_p]),
+    "pt_scene_sdf_leaf": (ctypes.c_int, [ctypes.c_void_p, u32, u32, P(f32), f32, f32, f32, u32, f32, f32, f32]),
+    "pt_scene_sdf_combine": (ctypes.c_int, [ctypes.c_void_p, u32, u32, u32, u32, f32, u32, f32, f32, f32]),
+    "pt_scene_sdf_remove": (ctypes.c_int, [ctypes.c_void_p, u32]),
+    "pt_scene_sdf_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "pt_sdf_cluster_box": (ctypes.c_int, [P(f32), u32, P(f32), P(f32)]),
     "pt_build_light_tree": (ctypes.c_int, [P(PtLightInput), u32, P(PtLightTreeNode), P(u32)]),
     "pt_scene_synth": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double]),
     "pt_build_analytic_bvh": (ctypes.c_int, [P(f32), u32, P(PtBvhNode), P(u32), P(u32)]),
@@ -357,6 +363,15 @@ class Scene:
         self._check(self.lib.pt_scene_load_cfg(self.h, path.encode(), base_dir.encode() if base_dir else None,
                                                buf, len(buf), ctypes.byref(n)))
         return buf.value.decode(), n.value
+
+    def sdf_leaf(self, id, shape, params, center, mat, rgb):
+        """shape 0 sphere, 1 box, 2 rounded box, 3 torus, 4 capsule; params up to 4 floats."""
+        q = (f32 * 4)(*(list(params) + [0.0] * (4 - len(params))))
+        self._check(self.lib.pt_scene_sdf_leaf(self.h, id, shape, q, *center, mat, *rgb))
+
+    def sdf_combine(self, id, a, b, op, k, mat, rgb):
+        """op 1 smooth union, 2 smooth subtract (b from a), 3 smooth intersect."""
+        self._check(self.lib.pt_scene_sdf_combine(self.h, id, a, b, op, k, mat, *rgb))
 
     def camera(self, pos, yaw, pitch, fov_deg):
         self._check(self.lib.pt_scene_set_camera(self.h, *pos, yaw, pitch, fov_deg))

@@ -41,6 +41,7 @@ __device__ __forceinline__ bool any_pos(V3 a) { return a.x > 0.0f || a.y > 0.0f 
 __device__ __forceinline__ float lerpf(float a, float b, float t) { return a + t * (b - a); }
 __device__ __forceinline__ V3 lerp3(V3 a, V3 b, float t) { return a + t * (b - a); }
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+__device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + t * (b - a); }
 // HLSL reflect(i, n) = i - 2 dot(n, i) n; refract per the HLSL/GLSL definition.
 __device__ __forceinline__ V3 reflect(V3 i, V3 n) { return i - (2.0f * dot(n, i)) * n; }
 __device__ __forceinline__ V3 refract(V3 i, V3 n, float eta) {
@@ -279,6 +280,9 @@ struct DScene {
     uint32_t moon_w, moon_h;
     const float4* ltree;         // light tree, 4 float4 per node (LightTreeNode layout)
     uint32_t ltree_nodes;
+    const float4* sdf;           // SDF clusters, 28 float4 each (4 header + 8 nodes x 3)
+    uint32_t sdf_count, sdf_iters;
+    float sdf_eps;
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs
@@ -344,7 +348,230 @@ __device__ __forceinline__ void test_prim(const DScene& S, uint32_t idx, V3 ro, 
 // analytic BVH (stack 32, right child popped first), then the triangle BVH
 // (stack 64) which only replaces the analytic hit when strictly closer.
 // parts: bit 0 analytic records, bit 1 triangle mesh.
-__device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, float t_init, uint32_t parts = 3u) {
+// ---------------------------------------------------------------------------
+// SDF clusters (shaders/SdfPrimitives.slang, the reference's default build:
+// the phase-1 ops; shaders/PathTrace.slang:2177-2305 for the layout and the
+// per-cluster sphere trace).  A cluster is <= 8 nodes evaluated in order,
+// leaves at `center` with shape parameters, ops combining earlier nodes.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kSdfBit = 0x80000000u;      // hit id kind: SDF cluster
+constexpr uint32_t kSdfStride = 28u;            // float4 per cluster
+constexpr uint32_t kSdfMaxNodes = 8u;
+
+__device__ __forceinline__ float len2(float x, float y) { return sqrtf(x * x + y * y); }
+__device__ __forceinline__ float signf(float x) { return (x > 0.0f) ? 1.0f : ((x < 0.0f) ? -1.0f : 0.0f); }
+
+__device__ __forceinline__ float sd_leaf(V3 p, uint32_t shape, float4 q) {
+    switch (shape) {
+        case 0u: return length(p) - q.x;                                        // sphere
+        case 1u:                                                                // box
+        case 2u: {                                                              // rounded box
+            const V3 d = v3(fabsf(p.x) - q.x, fabsf(p.y) - q.y, fabsf(p.z) - q.z);
+            const float o = length(v3(fmaxf(d.x, 0.0f), fmaxf(d.y, 0.0f), fmaxf(d.z, 0.0f))) +
+                            fminf(fmaxf(d.x, fmaxf(d.y, d.z)), 0.0f);
+            return shape == 1u ? o : o - q.w;
+        }
+        case 3u: return len2(len2(p.x, p.z) - q.x, p.y) - q.y;               // torus (XZ plane)
+        case 4u: {                                                              // capsule along Y
+            const float y = clampf(p.y, -q.x, q.x);
+            return length(v3(p.x, p.y - y, p.z)) - q.y;
+        }
+        case 5u: return dot(p, v3(q)) + q.w;                                    // plane
+        default: return 1e30f;
+    }
+}
+
+__device__ __forceinline__ V3 sd_leaf_normal(V3 p, uint32_t shape, float4 q) {
+    switch (shape) {
+        case 0u: {
+            const float l = length(p);
+            return l > 1e-12f ? p / l : v3(0.0f, 1.0f, 0.0f);
+        }
+        case 1u:
+        case 2u: {
+            const V3 d = v3(fabsf(p.x) - q.x, fabsf(p.y) - q.y, fabsf(p.z) - q.z);
+            const V3 sg = v3(signf(p.x), signf(p.y), signf(p.z));
+            if (fmaxf(d.x, fmaxf(d.y, d.z)) > 0.0f) {
+                const V3 m = v3(fmaxf(d.x, 0.0f), fmaxf(d.y, 0.0f), fmaxf(d.z, 0.0f));
+                const float lm = length(m);
+                if (lm < 1e-12f) return sg * v3(0.0f, 1.0f, 0.0f);
+                return (m / lm) * sg;
+            }
+            V3 n = v3(0.0f, 0.0f, 0.0f);
+            if (d.x > d.y && d.x > d.z) n.x = sg.x;
+            else if (d.y > d.z) n.y = sg.y;
+            else n.z = sg.z;
+            return n;
+        }
+        case 3u: {
+            const float lxz = len2(p.x, p.z);
+            if (lxz < 1e-12f) return v3(0.0f, signf(p.y), 0.0f);
+            const float k = q.x / lxz;
+            const V3 d = p - v3(p.x * k, 0.0f, p.z * k);
+            const float ld = length(d);
+            return ld > 1e-12f ? d / ld : v3(0.0f, 1.0f, 0.0f);
+        }
+        case 4u: {
+            const float y = clampf(p.y, -q.x, q.x);
+            const V3 d = p - v3(0.0f, y, 0.0f);
+            const float l = length(d);
+            return l > 1e-12f ? d / l : v3(0.0f, 1.0f, 0.0f);
+        }
+        case 5u: return v3(q);
+        default: return v3(0.0f, 1.0f, 0.0f);
+    }
+}
+
+struct SdfNodeD {
+    uint32_t op, shape, a, b;
+    float4 q;
+    V3 c;
+};
+
+__device__ __forceinline__ SdfNodeD sdf_node(const float4* C, uint32_t i) {
+    const float4 n0 = __ldg(C + 4u + 3u * i), n1 = __ldg(C + 5u + 3u * i), n2 = __ldg(C + 6u + 3u * i);
+    return SdfNodeD{__float_as_uint(n0.x), __float_as_uint(n0.y), __float_as_uint(n0.z), __float_as_uint(n0.w),
+                    n1, v3(n2)};
+}
+
+// sdfClusterDist: node i's value from its leaf or from earlier nodes
+__device__ float sdf_dist(const float4* C, uint32_t count, V3 p) {
+    float d[kSdfMaxNodes];
+    for (uint32_t i = 0; i < kSdfMaxNodes; ++i) {
+        if (i >= count) break;
+        const SdfNodeD n = sdf_node(C, i);
+        float v;
+        if (n.op == 0u) {
+            v = sd_leaf(p - n.c, n.shape, n.q);
+        } else if (n.op >= 1u && n.op <= 4u) {
+            const float da = d[min(n.a, i - 1u)], db = d[min(n.b, i - 1u)], k = n.q.x;
+            if (n.op == 1u) {            // smooth union
+                if (k <= 0.0f) v = fminf(da, db);
+                else {
+                    const float h = clampf(0.5f + 0.5f * (db - da) / k, 0.0f, 1.0f);
+                    v = lerpf_(db, da, h) - k * h * (1.0f - h);
+                }
+            } else if (n.op == 2u) {     // smooth subtract
+                if (k <= 0.0f) v = fmaxf(da, -db);
+                else {
+                    const float h = clampf(0.5f - 0.5f * (db + da) / k, 0.0f, 1.0f);
+                    v = lerpf_(da, -db, h) + k * h * (1.0f - h);
+                }
+            } else if (n.op == 3u) {     // smooth intersect
+                if (k <= 0.0f) v = fmaxf(da, db);
+                else {
+                    const float h = clampf(0.5f - 0.5f * (db - da) / k, 0.0f, 1.0f);
+                    v = lerpf_(db, da, h) + k * h * (1.0f - h);
+                }
+            } else {                     // displace
+                v = da + k;
+            }
+        } else {
+            v = 1e30f;                   // procedural ops: compiled out of the reference's default build
+        }
+        d[i] = v;
+    }
+    return count > 0u ? d[count - 1u] : 1e30f;
+}
+
+// sdfClusterNormal: analytic gradients carried through the same node order
+__device__ V3 sdf_normal(const float4* C, uint32_t count, V3 p) {
+    float d[kSdfMaxNodes];
+    V3 g[kSdfMaxNodes];
+    for (uint32_t i = 0; i < kSdfMaxNodes; ++i) {
+        if (i >= count) break;
+        const SdfNodeD n = sdf_node(C, i);
+        float v;
+        V3 gr;
+        if (n.op == 0u) {
+            const V3 pl = p - n.c;
+            v = sd_leaf(pl, n.shape, n.q);
+            gr = sd_leaf_normal(pl, n.shape, n.q);
+        } else if (n.op >= 1u && n.op <= 4u) {
+            const uint32_t ia = min(n.a, i - 1u), ib = min(n.b, i - 1u);
+            const float da = d[ia], db = d[ib], k = n.q.x;
+            if (n.op == 1u) {
+                if (k <= 0.0f) {
+                    v = fminf(da, db);
+                    gr = (da < db) ? g[ia] : g[ib];
+                } else {
+                    const float h = clampf(0.5f + 0.5f * (db - da) / k, 0.0f, 1.0f);
+                    v = lerpf_(db, da, h) - k * h * (1.0f - h);
+                    gr = normalize(lerp3(g[ib], g[ia], h));
+                }
+            } else if (n.op == 2u) {
+                if (k <= 0.0f) {
+                    v = fmaxf(da, -db);
+                    gr = (da > -db) ? g[ia] : -g[ib];
+                } else {
+                    const float h = clampf(0.5f - 0.5f * (db + da) / k, 0.0f, 1.0f);
+                    v = lerpf_(da, -db, h) + k * h * (1.0f - h);
+                    gr = normalize(lerp3(g[ia], -g[ib], h));
+                }
+            } else if (n.op == 3u) {
+                if (k <= 0.0f) {
+                    v = fmaxf(da, db);
+                    gr = (da > db) ? g[ia] : g[ib];
+                } else {
+                    const float h = clampf(0.5f - 0.5f * (db - da) / k, 0.0f, 1.0f);
+                    v = lerpf_(db, da, h) + k * h * (1.0f - h);
+                    gr = normalize(lerp3(g[ib], g[ia], h));
+                }
+            } else {
+                v = da + k;
+                gr = g[ia];
+            }
+        } else {
+            v = 1e30f;
+            gr = v3(0.0f, 1.0f, 0.0f);
+        }
+        d[i] = v;
+        g[i] = gr;
+    }
+    return count > 0u ? g[count - 1u] : v3(0.0f, 1.0f, 0.0f);
+}
+
+// sdfClusterTrace: clip to the cluster box, then sphere-trace
+__device__ bool sdf_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float t_min, float t_max, float& out_t) {
+    const float4 h0 = __ldg(C), h1 = __ldg(C + 1);
+    const uint32_t count = __float_as_uint(h0.w);
+    const V3 rs = v3(fabsf(rd.x) > 1e-30f ? rd.x : 1e-30f, fabsf(rd.y) > 1e-30f ? rd.y : 1e-30f,
+                     fabsf(rd.z) > 1e-30f ? rd.z : 1e-30f);
+    const V3 ri = v3(1.0f / rs.x, 1.0f / rs.y, 1.0f / rs.z);
+    const V3 t0 = (v3(h0) - ro) * ri, t1 = (v3(h1) - ro) * ri;
+    const float enter = fmaxf(fmaxf(fminf(t0.x, t1.x), fminf(t0.y, t1.y)), fminf(t0.z, t1.z));
+    const float exit = fminf(fminf(fmaxf(t0.x, t1.x), fmaxf(t0.y, t1.y)), fmaxf(t0.z, t1.z));
+    float t = fmaxf(enter, t_min);
+    const float t_end = fminf(exit, t_max);
+    if (t >= t_end) return false;
+    const uint32_t iters = min(S.sdf_iters, 256u);
+    for (uint32_t i = 0; i < iters; ++i) {
+        const V3 p = ro + rd * t;
+        const float ad = fabsf(sdf_dist(C, count, p));
+        if (ad < S.sdf_eps) {
+            out_t = t;
+            return true;
+        }
+        t += fmaxf(ad, S.sdf_eps);
+        if (t >= t_end) return false;
+    }
+    return false;
+}
+
+// traceSdfClusters: every cluster in order, a hit replaces the best only when
+// strictly closer (the reference's `t < h.t`)
+__device__ __forceinline__ void trace_sdf(const DScene& S, V3 ro, V3 rd, float& best_t, uint32_t& best_id) {
+    for (uint32_t i = 0; i < S.sdf_count; ++i) {
+        float t;
+        if (sdf_trace(S, S.sdf + size_t(kSdfStride) * i, ro, rd, 1e-3f, best_t, t) && t < best_t) {
+            best_t = t;
+            best_id = kSdfBit | i;
+        }
+    }
+}
+
+// parts: 1 analytic prims, 4 SDF clusters, 2 triangle mesh (the reference order)
+__device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, float t_init, uint32_t parts = 7u) {
     HitRec h{t_init, kMiss};
     const uint32_t linear = (parts & 1u) ? S.linear_count : 0u;
     for (uint32_t i = 0; i < linear; ++i) test_prim(S, i, ro, rd, h);
@@ -372,6 +599,7 @@ __device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, floa
             }
         }
     }
+    if (parts & 4u) trace_sdf(S, ro, rd, h.t, h.id);
     if ((parts & 2u) && S.tri_enabled != 0u && S.tri_nodes > 0u) {
         float t_mesh = h.t;
         uint32_t slot_hit = 0;
@@ -611,6 +839,16 @@ __device__ __noinline__ HitRec trace_wide(const DScene& S, V3 ro, V3 rd, float t
             b.id = h.id;
         }
     }
+    if (S.sdf_count) {
+        float t = b.t;
+        uint32_t id = kMiss;
+        trace_sdf(S, ro, rd, t, id);
+        if (id != kMiss) {
+            b.t = t;
+            b.key = 0x40000000u | (id & ~kSdfBit);
+            b.id = id;
+        }
+    }
     if (S.tri_enabled != 0u && S.tri_nodes > 0u) {
         if (S.t_wide) {
             wide_walk<true>(S, S.t4, ro, rd, inv, b, 0x80000000u, iters, st_code, st_t);
@@ -656,7 +894,17 @@ __device__ __forceinline__ void table_material(const DScene& S, uint32_t m, Surf
 
 __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, HitRec h) {
     Surface s;
-    if (h.id & kTriBit) {
+    if (h.id & kSdfBit) {   // SDF cluster: header material, normal at the hit point
+        const float4* C = S.sdf + size_t(kSdfStride) * (h.id & ~kSdfBit);
+        const float4 h0 = __ldg(C), h1 = __ldg(C + 1), h2 = __ldg(C + 2), h3 = __ldg(C + 3);
+        s.normal = normalize(sdf_normal(C, __float_as_uint(h0.w), ro + rd * h.t));
+        s.mat = __float_as_uint(h1.w);
+        s.albedo = v3(h2);
+        s.rough = h2.w;
+        s.ior = h3.x;
+        s.emission = v3(0.0f, 0.0f, 0.0f);
+        s.mid = kNoMat;
+    } else if (h.id & kTriBit) {
         const uint32_t slot = h.id & ~kTriBit;
         const float4* T = S.t_wide ? S.tri4 : S.tri;
         const float4 b = __ldg(T + 3u * slot + 1u);
@@ -810,6 +1058,17 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     int seg = 0;
     uint32_t xm[4] = {kNoMat, kNoMat, kNoMat, kNoMat};   // dielectric rows crossed (adjoint)
 
+    // SDF clusters, once the analytic part of the best hit is final
+    auto sdf_pass = [&]() {
+        float t = b.t;
+        uint32_t id = kMiss;
+        trace_sdf(*Sp, ro, rd, t, id);
+        if (id != kMiss) {
+            b.t = t;
+            b.key = 0x40000000u | (id & ~kSdfBit);
+            b.id = id;
+        }
+    };
     auto start_segment = [&]() {
         inv = safe_inv(rd);
         nx = -ro.x * inv.x;
@@ -839,6 +1098,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         } else {
             phase = 2;
             nodes = Sp->t4;
+            if (Sp->sdf_count) sdf_pass();
             if (has_t) {
                 st_code[0] = 0u;
                 st_t[0] = -3.0e38f;
@@ -951,6 +1211,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         }
         // end of a tree
         if (active && leaf == 0u && sp == 0) {
+            if (phase == 1 && Sp->sdf_count) sdf_pass();
             if (phase == 1 && has_t) {
                 phase = 2;
                 nodes = Sp->t4;

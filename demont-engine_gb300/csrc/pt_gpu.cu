@@ -1325,6 +1325,8 @@ struct pt_gpu_ctx {
     DBuf<uchar4> ldr;
     DBuf<float4> ltree;
     uint32_t ltree_nodes = 0;
+    DBuf<float4> sdf;
+    uint32_t sdf_count = 0;
     DBuf<uint32_t> err_word;
     // target
     uint32_t W = 0, H = 0;
@@ -1465,6 +1467,10 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     }
     S.ltree = c->ltree.p;
     S.ltree_nodes = c->ltree_nodes;
+    S.sdf = c->sdf.p;
+    S.sdf_count = c->sdf_count;   // a dispatch's push overrides these three
+    S.sdf_iters = 128;            // r_sdf_max_iters default
+    S.sdf_eps = 1e-4f;            // r_sdf_epsilon default
     S.moon_tex = c->moon.p;
     S.moon_w = c->moon_w;
     S.moon_h = c->moon_h;
@@ -1487,6 +1493,9 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
         S.tri_enabled = (prm->bvh_params[2] != 0u) ? 1u : 0u;
         S.tri_nodes = prm->bvh_params[3];
         S.light_count = prm->light_count;
+        S.sdf_count = prm->sdf_params[0];
+        S.sdf_iters = prm->sdf_params[1];
+        S.sdf_eps = prm->sdf_params_f[0];
     }
     return S;
 }
@@ -1517,6 +1526,13 @@ void sky_of(DFrame& F, const PtPathParams* prm) {
     F.sun_bright = prm->sun_extra2[0];
     F.sky_mode = (prm->sun_and_mode[3] == 2.0f) ? 2u : 0u;
     F.light_tree = (prm->light_tree_enabled != 0u && prm->light_tree_node_count > 0u) ? 1u : 0u;
+}
+
+// the dispatch's SDF cluster count must be the uploaded one
+int check_sdf(pt_gpu_ctx* ctx, const pt_gpu_ctx* sc, const PtPathParams* prm, const std::string& who) {
+    if (prm->sdf_params[0] != sc->sdf_count)
+        return set_err(ctx, PT_ERR_INVALID, who + "sdf_params.x disagrees with the uploaded SDF clusters");
+    return PT_OK;
 }
 
 // the dispatch's light tree must be the uploaded one
@@ -1801,7 +1817,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     for (auto* b : {&ctx->prim_rec, &ctx->prim_geo, &ctx->bvh, &ctx->tri, &ctx->tri_bvh, &ctx->mats,
                     &ctx->lights, &ctx->env, &ctx->accum, &ctx->ray_o, &ctx->ray_d, &ctx->thr,
                     &ctx->rad, &ctx->fsum, &ctx->amb, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
-                    &ctx->sh_tr, &ctx->moon, &ctx->ltree, &ctx->d_srad, &ctx->d_dldi})
+                    &ctx->sh_tr, &ctx->moon, &ctx->ltree, &ctx->sdf, &ctx->d_srad, &ctx->d_dldi})
         dfree(*b);
     dfree(ctx->d_grad);
     dfree(ctx->d_sh_mats);
@@ -1998,6 +2014,33 @@ int pt_gpu_upload_light_tree(pt_gpu_ctx* ctx, const PtLightTreeNode* nodes, uint
     return PT_OK;
 }
 
+int pt_gpu_upload_sdf(pt_gpu_ctx* ctx, const float* clusters, uint32_t n) {
+    if (ctx) ctx->gen++;
+    if (!ctx) return PT_ERR_INVALID;
+    if (n && !clusters) return set_err(ctx, PT_ERR_INVALID, "upload_sdf: null buffer");
+    const uint32_t* u = reinterpret_cast<const uint32_t*>(clusters);
+    for (uint32_t c = 0; c < n; ++c) {
+        const uint32_t* h = u + size_t(c) * kSdfStride * 4u;
+        const uint32_t count = h[3];
+        const std::string at = "upload_sdf: cluster " + std::to_string(c) + ": ";
+        if (count == 0u || count > kSdfMaxNodes) return set_err(ctx, PT_ERR_INVALID, at + "node count must be 1..8");
+        for (uint32_t i = 0; i < count; ++i) {
+            const uint32_t* nd = h + 16u + 12u * i;
+            const uint32_t op = nd[0], shape = nd[1], a = nd[2], b = nd[3];
+            if (op == 0u && shape >= 6u && shape <= 8u)
+                return set_err(ctx, PT_ERR_UNSUPPORTED, at + "fractal leaves (Mandelbulb/Mandelbox/Apollonian) are not built");
+            if (op > 9u || (op == 0u && shape > 8u)) return set_err(ctx, PT_ERR_INVALID, at + "bad op or shape");
+            if (op >= 1u && op <= 3u && (a >= i || b >= i))
+                return set_err(ctx, PT_ERR_INVALID, at + "an op must combine earlier nodes");
+            if (op >= 4u && a >= i) return set_err(ctx, PT_ERR_INVALID, at + "an op must combine earlier nodes");
+        }
+    }
+    if (int rc = dupload(ctx, ctx->sdf, clusters, size_t(n) * kSdfStride)) return rc;
+    ctx->sdf_count = n;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
 int pt_gpu_upload_moon(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H) {
     if (ctx) ctx->gen++;
     if (!ctx) return PT_ERR_INVALID;
@@ -2078,6 +2121,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     if (!ctx->accum.p) return set_err(ctx, PT_ERR_STATE, "render: no target (pt_gpu_set_target)");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render: tlas_present (hardware RT) has no CUDA path");
     if (int rc = check_light_tree(ctx, ctx, prm, "render: ")) return rc;
+    if (int rc = check_sdf(ctx, ctx, prm, "render: ")) return rc;
     if (int rc = check_sky(ctx, ctx, head, prm, "render: ")) return rc;
     if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
         (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))
@@ -2406,6 +2450,9 @@ int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d
     prm.bvh_params[2] = ctx->tri_count;
     prm.bvh_params[3] = ctx->tri_nodes;
     prm.light_count = ctx->light_count;
+    prm.sdf_params[0] = ctx->sdf_count;   // every uploaded SDF cluster, with the
+    prm.sdf_params[1] = 128u;             // reference's default trace settings
+    prm.sdf_params_f[0] = 1e-4f;
     const DScene S = make_scene(ctx, &prm);
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     const float4 *dro, *drd;
@@ -2458,6 +2505,7 @@ int validate_view(pt_gpu_ctx* ctx, pt_gpu_ctx* sc, const PtBatchView& v, uint32_
     if (v.width == 0 || v.height == 0) return set_err(ctx, PT_ERR_INVALID, w + "empty frame");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, w + "tlas (hardware RT) has no CUDA path");
     if (int rc = check_light_tree(ctx, sc, prm, w)) return rc;
+    if (int rc = check_sdf(ctx, sc, prm, w)) return rc;
     if (int rc = check_sky(ctx, sc, head, prm, w)) return rc;
     if (head->prim_count != sc->prim_count || prm->bvh_params[0] != sc->linear_count ||
         prm->bvh_params[1] != sc->bvh_nodes)
@@ -2644,11 +2692,26 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             ctx->b_h[i] = views[i].height;
         }
     }
-    // scene table (pointers may change after re-uploads)
+    // scene table (pointers may change after re-uploads); SDF trace settings
+    // come from the views of each scene, which must agree
     std::vector<DScene> st(n_scenes);
     for (uint32_t k = 0; k < n_scenes; ++k) {
         st[k] = make_scene(scenes[k], nullptr);
         st[k].err = ctx->err_word.p;
+    }
+    {
+        std::vector<int> seen(n_scenes, 0);
+        for (uint32_t i = 0; i < n_views; ++i) {
+            DScene& d = st[views[i].scene];
+            const PtPathParams& q = views[i].params;
+            if (seen[views[i].scene] && (d.sdf_count != q.sdf_params[0] || d.sdf_iters != q.sdf_params[1] ||
+                                         d.sdf_eps != q.sdf_params_f[0]))
+                return set_err(ctx, PT_ERR_INVALID, "batch: views of one scene disagree on the SDF settings");
+            d.sdf_count = q.sdf_params[0];
+            d.sdf_iters = q.sdf_params[1];
+            d.sdf_eps = q.sdf_params_f[0];
+            seen[views[i].scene] = 1;
+        }
     }
     CK(cudaMemcpyAsync(ctx->b_scenes.p, st.data(), n_scenes * sizeof(DScene), cudaMemcpyHostToDevice, ctx->stream));
     ctx->b_views_h.resize(n_views);
@@ -2943,6 +3006,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         return set_err(ctx, PT_ERR_INVALID, "render_noalloc: accumulation buffer must be 16-byte aligned");
     if (head->tlas_present) return set_err(ctx, PT_ERR_UNSUPPORTED, "render_noalloc: tlas_present has no CUDA path");
     if (int rc = check_light_tree(ctx, ctx, prm, "render_noalloc: ")) return rc;
+    if (int rc = check_sdf(ctx, ctx, prm, "render_noalloc: ")) return rc;
     if (int rc = check_sky(ctx, ctx, head, prm, "render_noalloc: ")) return rc;
     if (head->prim_count != ctx->prim_count || prm->bvh_params[0] != ctx->linear_count ||
         (prm->bvh_params[1] != 0u && prm->bvh_params[1] != ctx->bvh_nodes))

@@ -418,6 +418,19 @@ struct Light {
     float orient[4] = {0, 0, 0, 1};
 };
 
+struct SdfNodeH {
+    uint32_t op = 0, shape = 0, a = 0, b = 0;
+    float params[4] = {0, 0, 0, 0};
+    float center[3] = {0, 0, 0};
+};
+struct SdfClusterH {
+    SdfNodeH nodes[8];
+    uint32_t count = 0, material = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    float albedo[3] = {0.7f, 0.7f, 0.7f};
+    float roughness = 0.0f, ior = 1.5f;
+};
+
 struct CVar {
     const char* name;
     double value;
@@ -439,6 +452,8 @@ struct pt_scene {
     bool env_present = false;
     std::vector<float> moon_rgba;
     uint32_t moon_w = 0, moon_h = 0;
+    std::map<uint32_t, SdfClusterH> sdf;
+    std::vector<float> packed_sdf;
     float cam_pos[3] = {0.0f, 1.5f, 4.0f};
     float cam_yaw = 0.0f, cam_pitch = -0.20f, cam_fov = 60.0f;
     std::vector<CVar> cvars = {
@@ -457,6 +472,7 @@ struct pt_scene {
         {"r_sky_mode", 1},           {"r_show_stars", 0},
         {"r_planet_radius", 6378137.0},
         {"r_exposure", 1.5},         {"r_tonemap_op", 0},
+        {"r_sdf_max_iters", 128},    {"r_sdf_epsilon", 1e-4},
         {"r_capture_seed", 0},
         {"app_window_width", 0},     {"app_window_height", 0},
     };
@@ -1467,6 +1483,34 @@ int pt_scene_packed(pt_scene* s, PtPackedScene* o) {
     o->lights = s->packed_lights.data();
     o->light_count = uint32_t(s->lights.size());
     o->env_present = s->env_present ? 1u : 0u;
+    s->packed_sdf.clear();
+    for (const auto& [id, c] : s->sdf) {   // 28 float4 per cluster, id order
+        float blk[112] = {0};
+        auto u2f = [](uint32_t u) {
+            float f;
+            std::memcpy(&f, &u, 4);
+            return f;
+        };
+        for (int k = 0; k < 3; ++k) {
+            blk[k] = c.lo[k];
+            blk[4 + k] = c.hi[k];
+            blk[8 + k] = c.albedo[k];
+        }
+        blk[3] = u2f(c.count);
+        blk[7] = u2f(c.material);
+        blk[11] = c.roughness;
+        blk[12] = c.ior;
+        for (uint32_t i = 0; i < 8; ++i) {
+            const SdfNodeH& n = c.nodes[i];
+            float* q = blk + 16 + 12 * i;
+            q[0] = u2f(n.op); q[1] = u2f(n.shape); q[2] = u2f(n.a); q[3] = u2f(n.b);
+            for (int k = 0; k < 4; ++k) q[4 + k] = n.params[k];
+            for (int k = 0; k < 3; ++k) q[8 + k] = n.center[k];
+        }
+        s->packed_sdf.insert(s->packed_sdf.end(), blk, blk + 112);
+    }
+    o->sdf_clusters = s->packed_sdf.empty() ? nullptr : s->packed_sdf.data();
+    o->sdf_count = uint32_t(s->sdf.size());
     o->light_tree = s->light_tree.empty() ? nullptr : s->light_tree.data();
     o->light_tree_node_count = uint32_t(s->light_tree.size());
     o->moon_rgba = s->moon_rgba.empty() ? nullptr : s->moon_rgba.data();
@@ -1599,6 +1643,15 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
     params->sun_extra[2] = vflat;
     params->sun_extra[3] = std::max(float(s->cvar("r_planet_radius")), 0.0f);
     params->sun_extra2[0] = params->moon_extra[3];
+    {   // SDF trace settings (Engine.cpp:7940-7981)
+        int it = int(s->cvar("r_sdf_max_iters"));
+        it = std::min(std::max(it, 1), 256);
+        float eps = float(s->cvar("r_sdf_epsilon"));
+        if (eps < 1e-7f) eps = 1e-7f;
+        params->sdf_params[0] = uint32_t(s->sdf.size());
+        params->sdf_params[1] = uint32_t(it);
+        params->sdf_params_f[0] = eps;
+    }
     return PT_OK;
 }
 
@@ -1631,6 +1684,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx) {
     rc = pt_gpu_upload_lights(ctx, p.lights, p.light_count);
     if (rc) return rc;
     rc = pt_gpu_upload_light_tree(ctx, p.light_tree, p.light_tree_node_count);
+    if (rc) return rc;
+    rc = pt_gpu_upload_sdf(ctx, p.sdf_clusters, p.sdf_count);
     if (rc) return rc;
     if (p.env_present)
         rc = pt_gpu_upload_env(ctx, p.env_rgba, p.env_w, p.env_h, p.env_marginal, p.env_conditional,
@@ -1675,6 +1730,193 @@ int pt_build_env_cdf(const float* rgb, uint32_t W, uint32_t H, const uint8_t* ma
                      float* marginal, float* conditional, double* total) {
     if (!rgb || !marginal || !conditional || !total) return PT_ERR_INVALID;
     *total = env_cdf(rgb, W, H, mask, marginal, conditional);
+    return PT_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// SDF clusters: bounding boxes (src/renderer/AnalyticBvh.cpp ComputeSdfAabb,
+// restated) and the sdf_* commands.
+// ===========================================================================
+namespace {
+
+bool sdf_leaf_box(const SdfNodeH& n, float* mn, float* mx) {
+    const float* q = n.params;
+    switch (n.shape) {
+        case 0: {
+            if (q[0] <= 0.0f) return false;
+            for (int k = 0; k < 3; ++k) { mn[k] = -q[0]; mx[k] = q[0]; }
+            return true;
+        }
+        case 1: {
+            if (q[0] <= 0.0f || q[1] <= 0.0f || q[2] <= 0.0f) return false;
+            for (int k = 0; k < 3; ++k) { mn[k] = -q[k]; mx[k] = q[k]; }
+            return true;
+        }
+        case 2: {
+            const float h[3] = {q[0] + q[3], q[1] + q[3], q[2] + q[3]};
+            if (h[0] <= 0.0f || h[1] <= 0.0f || h[2] <= 0.0f) return false;
+            for (int k = 0; k < 3; ++k) { mn[k] = -h[k]; mx[k] = h[k]; }
+            return true;
+        }
+        case 3: {
+            if (q[0] <= 0.0f || q[1] <= 0.0f) return false;
+            mn[0] = -(q[0] + q[1]); mn[1] = -q[1]; mn[2] = -(q[0] + q[1]);
+            mx[0] = q[0] + q[1];    mx[1] = q[1];  mx[2] = q[0] + q[1];
+            return true;
+        }
+        case 4: {
+            if (q[0] < 0.0f || q[1] <= 0.0f) return false;
+            mn[0] = -q[1]; mn[1] = -q[0] - q[1]; mn[2] = -q[1];
+            mx[0] = q[1];  mx[1] = q[0] + q[1];  mx[2] = q[1];
+            return true;
+        }
+        default:
+            return false;   // planes are unbounded; fractals are not built
+    }
+}
+
+bool sdf_node_box(const SdfClusterH& c, uint32_t i, float* mn, float* mx) {
+    if (i >= c.count) return false;
+    const SdfNodeH& n = c.nodes[i];
+    auto widen = [&](float k) {
+        for (int j = 0; j < 3; ++j) { mn[j] -= k; mx[j] += k; }
+    };
+    if (n.op == 0) {
+        if (!sdf_leaf_box(n, mn, mx)) return false;
+        for (int j = 0; j < 3; ++j) { mn[j] += n.center[j]; mx[j] += n.center[j]; }
+        return true;
+    }
+    float an[3], ax[3], bn[3], bx[3];
+    if (!sdf_node_box(c, n.a, an, ax)) return false;
+    if (n.op == 4) {   // displace
+        for (int j = 0; j < 3; ++j) { mn[j] = an[j]; mx[j] = ax[j]; }
+        widen(std::abs(n.params[0]));
+        return true;
+    }
+    if (n.op > 3) return false;
+    if (!sdf_node_box(c, n.b, bn, bx)) return false;
+    if (n.op == 2) {   // subtract: a's box
+        for (int j = 0; j < 3; ++j) { mn[j] = an[j]; mx[j] = ax[j]; }
+    } else {
+        bool disjoint = false;
+        for (int j = 0; j < 3; ++j) {
+            if (n.op == 1) {
+                mn[j] = std::min(an[j], bn[j]);
+                mx[j] = std::max(ax[j], bx[j]);
+            } else {
+                mn[j] = std::max(an[j], bn[j]);
+                mx[j] = std::min(ax[j], bx[j]);
+                if (mn[j] > mx[j]) disjoint = true;
+            }
+        }
+        if (disjoint)   // an empty intersection keeps the union box
+            for (int j = 0; j < 3; ++j) {
+                mn[j] = std::min(an[j], bn[j]);
+                mx[j] = std::max(ax[j], bx[j]);
+            }
+    }
+    widen(std::max(0.0f, n.params[0]));
+    return true;
+}
+
+bool sdf_box(SdfClusterH& c) {
+    if (c.count == 0 || c.count > 8) return false;
+    return sdf_node_box(c, c.count - 1u, c.lo, c.hi);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_scene_sdf_leaf(pt_scene* s, uint32_t id, uint32_t shape, const float params[4], float x, float y,
+                      float z, uint32_t material, float r, float g, float b) {
+    if (!s || !params) return PT_ERR_INVALID;
+    if (material > 2u) return fail(s, "sdf: material must be 0, 1 or 2");
+    if (shape > 4u) return fail(s, "sdf: shape must be 0..4 (sphere, box, rounded box, torus, capsule)");
+    if (shape == 2u && (!(params[0] > 0.0f) || !(params[1] > 0.0f) || !(params[2] > 0.0f) || params[3] < 0.0f))
+        return fail(s, "sdf_round_box: half-extents must be > 0 and corner_r >= 0");
+    SdfClusterH c{};
+    c.count = 1;
+    c.material = material;
+    c.albedo[0] = r; c.albedo[1] = g; c.albedo[2] = b;
+    SdfNodeH& n = c.nodes[0];
+    n.op = 0;
+    n.shape = shape;
+    for (int k = 0; k < 4; ++k) n.params[k] = params[k];
+    n.center[0] = x; n.center[1] = y; n.center[2] = z;
+    if (!sdf_box(c)) return fail(s, "sdf: degenerate parameters");
+    s->sdf[id] = c;
+    return PT_OK;
+}
+
+int pt_scene_sdf_combine(pt_scene* s, uint32_t id, uint32_t a, uint32_t b, uint32_t op, float k, uint32_t material,
+                         float r, float g, float bl) {
+    if (!s) return PT_ERR_INVALID;
+    if (op < 1u || op > 3u) return fail(s, "sdf: op must be 1 (union), 2 (subtract) or 3 (intersect)");
+    if (material > 2u) return fail(s, "sdf: material must be 0, 1 or 2");
+    if (a == b) return fail(s, "sdf: the two children must differ");
+    auto ia = s->sdf.find(a), ib = s->sdf.find(b);
+    if (ia == s->sdf.end() || ib == s->sdf.end()) return fail(s, "sdf: child cluster not found");
+    const SdfClusterH A = ia->second, B = ib->second;
+    if (A.count + B.count + 1u > 8u) return fail(s, "sdf: more than 8 nodes");
+    SdfClusterH c{};
+    for (uint32_t i = 0; i < A.count; ++i) c.nodes[i] = A.nodes[i];
+    for (uint32_t i = 0; i < B.count; ++i) {
+        SdfNodeH nb = B.nodes[i];
+        if (nb.op != 0u) {
+            nb.a += A.count;
+            nb.b += A.count;
+        }
+        c.nodes[A.count + i] = nb;
+    }
+    SdfNodeH& o = c.nodes[A.count + B.count];
+    o.op = op;
+    o.a = A.count - 1u;
+    o.b = A.count + B.count - 1u;
+    o.params[0] = k;
+    c.count = A.count + B.count + 1u;
+    c.material = material;
+    c.albedo[0] = r; c.albedo[1] = g; c.albedo[2] = bl;
+    if (!sdf_box(c)) return fail(s, "sdf: bounding box failed");
+    s->sdf.erase(a);
+    s->sdf.erase(b);
+    s->sdf[id] = c;
+    return PT_OK;
+}
+
+int pt_scene_sdf_remove(pt_scene* s, uint32_t id) {
+    if (!s) return PT_ERR_INVALID;
+    return s->sdf.erase(id) ? PT_OK : fail(s, "sdf_remove: unknown id");
+}
+
+int pt_scene_sdf_clear(pt_scene* s) {
+    if (!s) return PT_ERR_INVALID;
+    s->sdf.clear();
+    return PT_OK;
+}
+
+// test hook: the bounding box of a raw cluster (the reference's SdfPrim node
+// layout), for pinning against ComputeSdfAabb
+int pt_sdf_cluster_box(const float* nodes12, uint32_t count, float* lo, float* hi) {
+    if (!nodes12 || !lo || !hi || count == 0 || count > 8) return PT_ERR_INVALID;
+    SdfClusterH c{};
+    c.count = count;
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* q = nodes12 + 12 * i;
+        std::memcpy(&c.nodes[i].op, q + 0, 4);
+        std::memcpy(&c.nodes[i].shape, q + 1, 4);
+        std::memcpy(&c.nodes[i].a, q + 2, 4);
+        std::memcpy(&c.nodes[i].b, q + 3, 4);
+        for (int k = 0; k < 4; ++k) c.nodes[i].params[k] = q[4 + k];
+        for (int k = 0; k < 3; ++k) c.nodes[i].center[k] = q[8 + k];
+    }
+    if (!sdf_box(c)) return PT_ERR_INVALID;
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = c.lo[k];
+        hi[k] = c.hi[k];
+    }
     return PT_OK;
 }
 
@@ -1975,6 +2217,37 @@ int pt_scene_exec_cfg(pt_scene* s, const char* text, const char* base_dir, char*
                                          f[11], f[12], f[13]);
             }
             if (rc) bad(line, s->err);
+        } else if (cmd == "sdf_sphere" || cmd == "sdf_box" || cmd == "sdf_round_box" || cmd == "sdf_torus" ||
+                   cmd == "sdf_capsule") {
+            // params first, then the center (the reference's argument orders)
+            const uint32_t shape = cmd == "sdf_sphere" ? 0u : cmd == "sdf_box" ? 1u : cmd == "sdf_round_box" ? 2u
+                                 : cmd == "sdf_torus" ? 3u : 4u;
+            const size_t np = shape == 0u ? 1 : shape == 1u ? 3 : shape == 2u ? 4 : 2;
+            const size_t want = 1 + np + 3 + 1 + 3;
+            const int m = na == want ? to_mat(tok[1 + np + 3 + 1]) : -1;
+            float prm4[4] = {0, 0, 0, 0};
+            if (na != want || !U(1, id) || !floats(2, np + 3) || m < 0) { bad(line, "malformed arguments"); continue; }
+            for (size_t k = 0; k < np; ++k) prm4[k] = f[k];
+            float rgb[3];
+            if (!F(want - 2, rgb[0]) || !F(want - 1, rgb[1]) || !F(want, rgb[2])) { bad(line, "bad colour"); continue; }
+            if (pt_scene_sdf_leaf(s, id, shape, prm4, f[np], f[np + 1], f[np + 2], uint32_t(m), rgb[0], rgb[1], rgb[2]))
+                bad(line, s->err);
+        } else if (cmd == "sdf_smin" || cmd == "sdf_smax" || cmd == "sdf_sdiff") {
+            uint32_t a = 0, bb = 0;
+            float k = 0.0f;
+            const int m = na == 8 ? to_mat(tok[5]) : -1;
+            if (na != 8 || !U(1, id) || !U(2, a) || !U(3, bb) || !F(4, k) || m < 0 || !floats(6, 3)) {
+                bad(line, "malformed arguments");
+                continue;
+            }
+            const uint32_t op = cmd == "sdf_smin" ? 1u : cmd == "sdf_sdiff" ? 2u : 3u;
+            if (pt_scene_sdf_combine(s, id, a, bb, op, k, uint32_t(m), f[0], f[1], f[2])) bad(line, s->err);
+        } else if (cmd == "sdf_remove") {
+            if (na != 1 || !U(1, id) || pt_scene_sdf_remove(s, id)) { bad(line, "unknown id"); continue; }
+        } else if (cmd == "sdf_clear") {
+            pt_scene_sdf_clear(s);
+        } else if (cmd.rfind("sdf_", 0) == 0) {
+            skip(line, "procedural SDF ops and fractal SDFs are not built");
         } else if (cmd == "cam_pos") {
             if (na != 3 || !floats(1, 3)) { bad(line, "want x y z"); continue; }
             std::memcpy(s->cam_pos, f, 12);

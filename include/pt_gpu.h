@@ -87,6 +87,9 @@ typedef struct PtPathParams {
     float    moon_extra[4];         /* size multiplier, distance ratio, disc brightness, - */
     float    sun_extra[4];          /* size multiplier, distance ratio, vertical flatten (1 = round), - */
     float    sun_extra2[4];         /* sun disc brightness, -, -, - */
+    /* SDF clusters (shaders/PathTrace.slang:859-885; engine fill src/engine/Engine.cpp:7940-7981) */
+    uint32_t sdf_params[4];         /* cluster count (= uploaded), sphere-trace iteration budget, -, - */
+    float    sdf_params_f[4];       /* hit epsilon, -, -, - */
 } PtPathParams;
 
 /* 32-byte BVH node, identical to the reference's BvhNode / TriBvhNode
@@ -184,6 +187,17 @@ typedef struct PtLightTreeNode {
     float    pad[3];
 } PtLightTreeNode;
 int pt_gpu_upload_light_tree(pt_gpu_ctx* ctx, const PtLightTreeNode* nodes, uint32_t n_nodes);
+
+/* ---- SDF clusters (replaces the sdf_clusters buffer, shaders/PathTrace.slang:2163-2305;
+ *      host layout src/renderer/AnalyticBvh.h SdfPrim) ----
+ * 28 float4 per cluster: aabb_min + asuint(node_count), aabb_max + asuint(material),
+ * albedo + roughness, ior + 3 pad, then 8 nodes of 3 float4: asuint(op, shape,
+ * child_a, child_b), params, center + pad.  Nodes are evaluated in order; an op
+ * combines earlier nodes (smooth union/subtract/intersect, displace); the last
+ * node is the cluster's distance.  Hit ids of SDF clusters are 0x80000000 | index.
+ * The procedural ops (5-9) evaluate as empty, as in the reference's default build;
+ * fractal leaves return PT_ERR_UNSUPPORTED. */
+int pt_gpu_upload_sdf(pt_gpu_ctx* ctx, const float* clusters, uint32_t n_clusters);
 
 /* ---- moon surface map (the moon_map texture of the gradient sky's moon disc,
  *      moonDisc, shaders/PathTrace.slang:3212-3353) ----
@@ -351,7 +365,9 @@ int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathP
  * ray_o: n float4 (origin xyz, w unused); ray_d: n float4 (direction xyz,
  * w = initial closest distance; <= 0 means the reference's 1e30).
  * hit_id out: 0xFFFFFFFF = miss; (0 << 30 | slot) = analytic record `slot` of the
- * uploaded buffer; (1u << 30 | tri) = original triangle index.  t out: hit distance.
+ * uploaded buffer; (1u << 30 | tri) = original triangle index; (1u << 31 | c) = SDF
+ * cluster c, sphere-traced with the reference's defaults (128 steps, epsilon 1e-4).
+ * t out: hit distance.
  * on_device != 0: all four pointers are device pointers. */
 int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d,
                          uint32_t n, uint32_t* hit_id, float* t, int on_device);

@@ -95,7 +95,8 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
  * r_analytic_bvh_threshold 16, r_hdri_extract_percentile 0.005, r_light_tree 1,
  * r_rr_start 2 (extension), r_denoiser 0; gradient sky (no env map): r_sun_elevation 30,
  * r_sun_azimuth 135 (degrees), r_sun_size 1, r_sun_disc_brightness 1, r_sun_horizon_flatten 1,
- * r_moon_size 1, r_moon_disc_brightness 0.7; output step: r_exposure 1.5, r_tonemap_op 0 (aces).
+ * r_moon_size 1, r_moon_disc_brightness 0.7; output step: r_exposure 1.5, r_tonemap_op 0 (aces);
+ * SDF: r_sdf_max_iters 128, r_sdf_epsilon 1e-4.
  * Returns PT_ERR_INVALID for unknown names. */
 int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
 int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);
@@ -137,6 +138,8 @@ typedef struct PtPackedScene {
     uint32_t         moon_w, moon_h;
     const PtLightTreeNode* light_tree;   /* built over the packed lights, NULL when there are none */
     uint32_t         light_tree_node_count;
+    const float*     sdf_clusters;  /* 28 float4 per cluster (pt_gpu_upload_sdf layout), id order */
+    uint32_t         sdf_count;
 } PtPackedScene;
 int pt_scene_packed(pt_scene* s, PtPackedScene* out);
 
@@ -157,6 +160,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
  *   light_point|spot|sphere|quad (argument orders as the reference's commands), light_remove <id>, light_clear
  *   cam_pos <x y z>, cam_yaw <deg>, cam_pitch <deg>, cam_fov <deg>
  *   r_sky_mode <gradient|hdri|procedural|hosek>, r_env_map <path.hdr> (relative to base_dir),
+ *   sdf_sphere|box|round_box|torus|capsule, sdf_smin|sdf_smax|sdf_sdiff, sdf_remove, sdf_clear
+ *   (argument orders as the reference's commands),
  *   r_denoiser <off|...>, and every numeric cvar of pt_scene_set_cvar (incl. app_window_width/height,
  *   r_capture_seed, r_show_stars).
  * Lines outside the path (water, post-processing, denoiser settings, clouds,
@@ -177,6 +182,24 @@ int pt_scene_load_cfg(pt_scene* s, const char* path, const char* base_dir, char*
  * else capacity_floats >= 3*w*h. */
 int pt_load_radiance_hdr(const char* path, float* rgb, uint32_t capacity_floats, uint32_t* width,
                          uint32_t* height);
+
+/* ---- SDF clusters (src/engine/Engine.cpp:18605-18990 sdf_* commands) ----
+ * A leaf cluster: shape 0 sphere (params: r), 1 box (hx hy hz), 2 rounded box
+ * (hx hy hz corner_r), 3 torus (R r, XZ plane), 4 capsule (half_h r, along Y),
+ * at center, material 0/1/2 with albedo.  A combined cluster: op 1 smooth union,
+ * 2 smooth subtract (b from a), 3 smooth intersect of clusters a and b with
+ * smoothing k; a and b are consumed (the reference's sdf_smin/sdf_sdiff/sdf_smax).
+ * Bounding boxes follow ComputeSdfAabb (src/renderer/AnalyticBvh.cpp:335-348). */
+int pt_scene_sdf_leaf(pt_scene* s, uint32_t id, uint32_t shape, const float params[4], float x, float y,
+                      float z, uint32_t material, float r, float g, float b);
+int pt_scene_sdf_combine(pt_scene* s, uint32_t id, uint32_t a, uint32_t b, uint32_t op, float k,
+                         uint32_t material, float r, float g, float bl);
+int pt_scene_sdf_remove(pt_scene* s, uint32_t id);
+int pt_scene_sdf_clear(pt_scene* s);
+/* Bounding box of `count` nodes in the reference's SdfNode layout (12 words
+ * each: op, shape, child_a, child_b as uint32, params[4], center[3], pad), as
+ * the scene builder computes it for a cluster (exposed for parity tests). */
+int pt_sdf_cluster_box(const float* nodes12, uint32_t count, float* lo, float* hi);
 
 /* Light-tree builder (src/renderer/LightTree.cpp:BuildLightTree): binary
  * centroid-median tree over the lights, leaves of one light, cone-bounded

@@ -152,6 +152,18 @@ def ref_light_tree(inputs):
     return out[: n.value * 64].reshape(n.value, 64)
 
 
+def ref_sdf_aabb(nodes12, count):
+    """The reference's ComputeSdfAabb over `count` SdfNode records (12 words
+    each); returns (lo, hi) or None when it rejects the cluster."""
+    lib = load_ref()
+    lo = np.zeros(3, np.float32)
+    hi = np.zeros(3, np.float32)
+    a = np.ascontiguousarray(nodes12, np.float32)
+    lib.ref_sdf_aabb.argtypes = [ctypes.c_void_p, u32, P(f32), P(f32)]
+    rc = lib.ref_sdf_aabb(a.ctypes.data, u32(count), lo.ctypes.data_as(P(f32)), hi.ctypes.data_as(P(f32)))
+    return (lo, hi) if rc == 0 else None
+
+
 def ref_analytic_bvh(centers_radii):
     """AnalyticBvh::Build of the reference itself: (nodes (m, 8) uint32, perm)."""
     lib = load_ref()

@@ -420,6 +420,184 @@ template <class R> struct Tracer {
         return {R(1) / s(rd.x), R(1) / s(rd.y), R(1) / s(rd.z)};
     }
 
+    // ---- SDF clusters (SdfPrimitives.slang phase-1 ops; PathTrace.slang:2223-2305) ----
+    struct SdfN {
+        uint32_t op, shape, a, b;
+        V3<R> c;
+        R q[4];
+    };
+    static float f_at(const float* p) { return *p; }
+    static uint32_t u_at(const float* p) {
+        uint32_t u;
+        std::memcpy(&u, p, 4);
+        return u;
+    }
+    SdfN sdf_node(const float* C, uint32_t i) const {
+        const float* n = C + 16 + 12 * i;
+        SdfN o{u_at(n), u_at(n + 1), u_at(n + 2), u_at(n + 3), ld3<R>(n + 8), {R(n[4]), R(n[5]), R(n[6]), R(n[7])}};
+        return o;
+    }
+    static R len2(R x, R y) { return std::sqrt(x * x + y * y); }
+    static R sgn(R x) { return (x > R(0)) ? R(1) : ((x < R(0)) ? R(-1) : R(0)); }
+    static R sd_leaf(V3<R> p, uint32_t shape, const R* q) {
+        switch (shape) {
+            case 0u: return length(p) - q[0];
+            case 1u:
+            case 2u: {
+                const V3<R> d{std::fabs(p.x) - q[0], std::fabs(p.y) - q[1], std::fabs(p.z) - q[2]};
+                const R o = length(V3<R>{mx(d.x, R(0)), mx(d.y, R(0)), mx(d.z, R(0))}) +
+                            mn(mx(d.x, mx(d.y, d.z)), R(0));
+                return shape == 1u ? o : o - q[3];
+            }
+            case 3u: return len2(len2(p.x, p.z) - q[0], p.y) - q[1];
+            case 4u: {
+                const R y = clampv(p.y, -q[0], q[0]);
+                return length(V3<R>{p.x, p.y - y, p.z}) - q[1];
+            }
+            case 5u: return dot(p, V3<R>{q[0], q[1], q[2]}) + q[3];
+            default: return R(1e30);
+        }
+    }
+    static V3<R> sd_leaf_normal(V3<R> p, uint32_t shape, const R* q) {
+        const V3<R> up{R(0), R(1), R(0)};
+        switch (shape) {
+            case 0u: {
+                const R l = length(p);
+                return l > R(1e-12) ? p / l : up;
+            }
+            case 1u:
+            case 2u: {
+                const V3<R> d{std::fabs(p.x) - q[0], std::fabs(p.y) - q[1], std::fabs(p.z) - q[2]};
+                const V3<R> sg{sgn(p.x), sgn(p.y), sgn(p.z)};
+                if (mx(d.x, mx(d.y, d.z)) > R(0)) {
+                    const V3<R> m{mx(d.x, R(0)), mx(d.y, R(0)), mx(d.z, R(0))};
+                    const R lm = length(m);
+                    if (lm < R(1e-12)) return sg * up;
+                    return (m / lm) * sg;
+                }
+                V3<R> n{R(0), R(0), R(0)};
+                if (d.x > d.y && d.x > d.z) n.x = sg.x;
+                else if (d.y > d.z) n.y = sg.y;
+                else n.z = sg.z;
+                return n;
+            }
+            case 3u: {
+                const R lxz = len2(p.x, p.z);
+                if (lxz < R(1e-12)) return {R(0), sgn(p.y), R(0)};
+                const R k = q[0] / lxz;
+                const V3<R> d = p - V3<R>{p.x * k, R(0), p.z * k};
+                const R ld = length(d);
+                return ld > R(1e-12) ? d / ld : up;
+            }
+            case 4u: {
+                const R y = clampv(p.y, -q[0], q[0]);
+                const V3<R> d = p - V3<R>{R(0), y, R(0)};
+                const R l = length(d);
+                return l > R(1e-12) ? d / l : up;
+            }
+            case 5u: return {q[0], q[1], q[2]};
+            default: return up;
+        }
+    }
+    R sdf_dist(const float* C, uint32_t count, V3<R> p, V3<R>* grad) const {
+        R d[8];
+        V3<R> g[8];
+        for (uint32_t i = 0; i < 8 && i < count; ++i) {
+            const SdfN n = sdf_node(C, i);
+            R v;
+            V3<R> gr{R(0), R(1), R(0)};
+            if (n.op == 0u) {
+                const V3<R> pl = p - n.c;
+                v = sd_leaf(pl, n.shape, n.q);
+                if (grad) gr = sd_leaf_normal(pl, n.shape, n.q);
+            } else if (n.op >= 1u && n.op <= 4u) {
+                const R da = d[n.a], db = d[n.b], k = n.q[0];
+                if (n.op == 1u) {
+                    if (k <= R(0)) {
+                        v = mn(da, db);
+                        if (grad) gr = (da < db) ? g[n.a] : g[n.b];
+                    } else {
+                        const R h = clampv(R(0.5) + R(0.5) * (db - da) / k, R(0), R(1));
+                        v = lerp(db, da, h) - k * h * (R(1) - h);
+                        if (grad) gr = normalize(lerp(g[n.b], g[n.a], h));
+                    }
+                } else if (n.op == 2u) {
+                    if (k <= R(0)) {
+                        v = mx(da, -db);
+                        if (grad) gr = (da > -db) ? g[n.a] : -g[n.b];
+                    } else {
+                        const R h = clampv(R(0.5) - R(0.5) * (db + da) / k, R(0), R(1));
+                        v = lerp(da, -db, h) + k * h * (R(1) - h);
+                        if (grad) gr = normalize(lerp(g[n.a], -g[n.b], h));
+                    }
+                } else if (n.op == 3u) {
+                    if (k <= R(0)) {
+                        v = mx(da, db);
+                        if (grad) gr = (da > db) ? g[n.a] : g[n.b];
+                    } else {
+                        const R h = clampv(R(0.5) - R(0.5) * (db - da) / k, R(0), R(1));
+                        v = lerp(db, da, h) + k * h * (R(1) - h);
+                        if (grad) gr = normalize(lerp(g[n.b], g[n.a], h));
+                    }
+                } else {
+                    v = da + k;
+                    if (grad) gr = g[n.a];
+                }
+            } else {
+                v = R(1e30);
+            }
+            d[i] = v;
+            g[i] = gr;
+        }
+        if (grad) *grad = count > 0u ? g[count - 1u] : V3<R>{R(0), R(1), R(0)};
+        return count > 0u ? d[count - 1u] : R(1e30);
+    }
+    bool sdf_trace(const float* C, V3<R> ro, V3<R> rd, R t_min, R t_max, R& out_t) const {
+        const uint32_t count = u_at(C + 3);
+        auto safe = [](R x) { return std::fabs(x) > R(1e-30) ? x : R(1e-30); };
+        const V3<R> ri{R(1) / safe(rd.x), R(1) / safe(rd.y), R(1) / safe(rd.z)};
+        const V3<R> t0 = (ld3<R>(C) - ro) * ri, t1 = (ld3<R>(C + 4) - ro) * ri;
+        const R enter = mx(mx(mn(t0.x, t1.x), mn(t0.y, t1.y)), mn(t0.z, t1.z));
+        const R exit = mn(mn(mx(t0.x, t1.x), mx(t0.y, t1.y)), mx(t0.z, t1.z));
+        R t = mx(enter, t_min);
+        const R t_end = mn(exit, t_max);
+        if (t >= t_end) return false;
+        const uint32_t iters = std::min(Q.sdf_params[1], 256u);
+        const R eps = R(Q.sdf_params_f[0]);
+        for (uint32_t i = 0; i < iters; ++i) {
+            const V3<R> p = ro + rd * t;
+            const R ad = std::fabs(sdf_dist(C, count, p, nullptr));
+            if (ad < eps) {
+                out_t = t;
+                return true;
+            }
+            t += mx(ad, eps);
+            if (t >= t_end) return false;
+        }
+        return false;
+    }
+    void trace_sdf(V3<R> ro, V3<R> rd, Hit<R>& h) {
+        const uint32_t n = std::min(Q.sdf_params[0], S.sdf_count);
+        for (uint32_t i = 0; i < n; ++i) {
+            const float* C = S.sdf_clusters + size_t(i) * 112;
+            R t;
+            if (sdf_trace(C, ro, rd, R(1e-3), h.t, t) && t < h.t) {
+                V3<R> g;
+                sdf_dist(C, u_at(C + 3), ro + rd * t, &g);
+                h.hit = true;
+                h.t = t;
+                h.normal = normalize(g);
+                h.mat = u_at(C + 7);
+                h.albedo = ld3<R>(C + 8);
+                h.roughness = R(C[11]);
+                h.ior = R(C[12]);
+                h.emission = {R(0), R(0), R(0)};
+                h.id = 0x80000000u | i;
+                h.mid = 0xFFFFFFFFu;
+            }
+        }
+    }
+
     Hit<R> trace(V3<R> ro, V3<R> rd, R t_init = R(1e30)) {
         cnt.rays++;
         const R shutter = R(1);   // motion blur off
@@ -450,6 +628,7 @@ template <class R> struct Tracer {
                 }
             }
         }
+        trace_sdf(ro, rd, h);
         if (Q.bvh_params[2] != 0u) {
             const uint32_t tnodes = Q.bvh_params[3];
             R t_mesh = h.t;

@@ -42,6 +42,18 @@ int ref_build_light_tree(const void* inputs, uint32_t n, void* nodes_out, uint32
     return 0;
 }
 
+// ComputeSdfAabb over `count` nodes laid out as SdfNode; 0 on success.
+int ref_sdf_aabb(const void* nodes, uint32_t count, float* lo, float* hi) {
+    pt::renderer::SdfPrim prim{};
+    if (count > pt::renderer::SdfPrim::kMaxNodes) return -1;
+    std::memcpy(prim.nodes.data(), nodes, size_t(count) * sizeof(pt::renderer::SdfNode));
+    prim.node_count = count;
+    if (!pt::renderer::ComputeSdfAabb(prim)) return -2;
+    std::memcpy(lo, prim.aabb_min, 12);
+    std::memcpy(hi, prim.aabb_max, 12);
+    return 0;
+}
+
 // LoadRadianceHdr: rgb NULL -> size query; returns 0 on success.
 int ref_load_radiance_hdr(const char* path, float* rgb, uint32_t cap, uint32_t* w, uint32_t* h) {
     std::string err;

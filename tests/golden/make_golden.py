@@ -56,6 +56,38 @@ def light_inputs(n, seed, coincident=False):
     return a
 
 
+def sdf_clusters(n, seed):
+    """Random SDF clusters as SdfNode records (12 words each): single leaves of
+    the five bounded shapes and smooth union/subtract/intersect/displace trees."""
+    rng = XorShift32(seed)
+    out = []
+    for c in range(n):
+        def leaf():
+            shape = int(rng.next() % 5)
+            p = [rng.rangef(0.2, 2.0) for _ in range(4)]
+            if shape == 2:
+                p[3] = rng.rangef(0.0, 0.5)
+            node = np.zeros(12, np.float32)
+            node[:4].view(np.uint32)[:] = [0, shape, 0, 0]
+            node[4:8] = p
+            node[8:11] = [rng.rangef(-5, 5) for _ in range(3)]
+            return node
+        kind = c % 5
+        if kind == 0:
+            nodes = [leaf()]
+        else:
+            a, b = leaf(), leaf()
+            op = np.zeros(12, np.float32)
+            opc = [1, 2, 3, 4][kind - 1]
+            op[:4].view(np.uint32)[:] = [opc, 0, 0, 1]
+            op[4] = rng.rangef(-0.3, 0.8)
+            nodes = [a, b, op]
+        arr = np.zeros((8, 12), np.float32)
+        arr[:len(nodes)] = nodes
+        out.append((arr, len(nodes)))
+    return out
+
+
 def main():
     if oracle.load_ref() is None:
         sys.exit("oracle/_ref/libref_builders.so missing: run `make -C oracle ref` first")
@@ -79,6 +111,13 @@ def main():
                                 "lt16c": (16, 3, True)}.items():
         inp = light_inputs(n, seed, co)
         out[f"{name}_in"], out[f"{name}_nodes"] = inp.view(np.uint8).reshape(n, -1), oracle.ref_light_tree(inp)
+    cl = sdf_clusters(60, 0x5DF5EED)
+    boxes = []
+    for arr, n in cl:
+        r = oracle.ref_sdf_aabb(arr, n)
+        boxes.append(np.concatenate([r[0], r[1], [1.0]]) if r else np.array([0, 0, 0, 0, 0, 0, 0], np.float32))
+    out.update(sdf_nodes=np.stack([a for a, _ in cl]), sdf_counts=np.array([n for _, n in cl], np.uint32),
+               sdf_boxes=np.stack(boxes).astype(np.float32))
     np.savez_compressed(os.path.join(HERE, "reference_builders.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_builders.npz"))
 
