@@ -283,6 +283,8 @@ struct DScene {
     const float4* sdf;           // SDF clusters, 28 float4 each (4 header + 8 nodes x 3)
     uint32_t sdf_count, sdf_iters;
     float sdf_eps;
+    uint32_t frac_iters;         // fractal leaves: DE iterations, default power, epsilon growth per step
+    float frac_power, frac_eps_scale;
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs
@@ -558,12 +560,131 @@ __device__ bool sdf_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float 
     return false;
 }
 
+// ---- fractal leaves (shaders/SdfFractals.slang): distance estimators ----
+__device__ __forceinline__ float fracf(float x) { return x - floorf(x); }
+
+__device__ float de_fractal(V3 p, uint32_t shape, float4 q, float power_default, uint32_t iters) {
+    if (shape == 6u) {   // Mandelbulb
+        const float power = (q.x > 0.0f) ? q.x : power_default;
+        V3 z = p;
+        float dr = 1.0f, r = 0.0f;
+        for (uint32_t i = 0; i < iters; ++i) {
+            r = length(z);
+            if (r > 2.0f) break;
+            const float theta = f_acos(clampf(z.z / fmaxf(r, 1e-12f), -1.0f, 1.0f));
+            const float phi = f_atan2(z.y, z.x);
+            dr = f_pow(r, power - 1.0f) * power * dr + 1.0f;
+            const float rp = f_pow(r, power);
+            const float nt = theta * power, np = phi * power;
+            const float sn = f_sin(nt);
+            z = v3(sn * f_cos(np), sn * f_sin(np), f_cos(nt)) * rp;
+            z = z + p;
+        }
+        return 0.5f * f_log(fmaxf(r, 1.0001f)) * r / fmaxf(dr, 1e-12f);
+    }
+    if (shape == 7u) {   // Mandelbox
+        const float scale = (q.x != 0.0f) ? q.x : 2.5f;
+        V3 z = p;
+        float dr = 1.0f;
+        for (uint32_t i = 0; i < iters; ++i) {
+            z = v3(clampf(z.x, -1.0f, 1.0f) * 2.0f - z.x, clampf(z.y, -1.0f, 1.0f) * 2.0f - z.y,
+                   clampf(z.z, -1.0f, 1.0f) * 2.0f - z.z);
+            const float r2 = dot(z, z);
+            if (r2 < 0.25f) {
+                z = z * 4.0f;
+                dr = dr * 4.0f;
+            } else if (r2 < 1.0f) {
+                const float f = 1.0f / r2;
+                z = z * f;
+                dr = dr * f;
+            }
+            z = z * scale + p;
+            dr = fabsf(scale) * dr + 1.0f;
+        }
+        return length(z) / fabsf(dr);
+    }
+    if (shape == 8u) {   // Apollonian gasket
+        const float scale = (q.x != 0.0f) ? q.x : 1.3f;
+        V3 z = p;
+        float dr = 1.0f;
+        for (uint32_t i = 0; i < iters; ++i) {
+            z = v3(-1.0f + 2.0f * fracf(0.5f * z.x + 0.5f), -1.0f + 2.0f * fracf(0.5f * z.y + 0.5f),
+                   -1.0f + 2.0f * fracf(0.5f * z.z + 0.5f));
+            const float r2 = dot(z, z);
+            const float k = fmaxf(scale / fmaxf(r2, 1e-12f), 1.0f);
+            z = z * k;
+            dr = dr * k;
+        }
+        return (0.25f * fabsf(z.y) - 0.001f) / dr;
+    }
+    return 1e30f;
+}
+
+// evalFractalNormal: tetrahedral central differences of step h
+__device__ V3 fractal_normal(V3 p, uint32_t shape, float4 q, float power, uint32_t iters, float h) {
+    const V3 e1 = v3(1.0f, -1.0f, -1.0f), e2 = v3(-1.0f, -1.0f, 1.0f);
+    const V3 e3 = v3(-1.0f, 1.0f, -1.0f), e4 = v3(1.0f, 1.0f, 1.0f);
+    const float d1 = de_fractal(p + e1 * h, shape, q, power, iters);
+    const float d2 = de_fractal(p + e2 * h, shape, q, power, iters);
+    const float d3 = de_fractal(p + e3 * h, shape, q, power, iters);
+    const float d4 = de_fractal(p + e4 * h, shape, q, power, iters);
+    const V3 n = e1 * d1 + e2 * d2 + e3 * d3 + e4 * d4;
+    const float l = length(n);
+    return (l > 1e-12f) ? n / l : v3(0.0f, 1.0f, 0.0f);
+}
+
+// traceSdfFractal: the cluster box clip, then a march whose hit epsilon grows
+// with the step index (the normal's difference step follows it)
+__device__ bool fractal_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float t_min, float t_max, float& out_t,
+                              uint32_t& out_step) {
+    const float4 h0 = __ldg(C), h1 = __ldg(C + 1);
+    const SdfNodeD n = sdf_node(C, __float_as_uint(h0.w) - 1u);
+    const V3 rs = v3(fabsf(rd.x) > 1e-30f ? rd.x : 1e-30f, fabsf(rd.y) > 1e-30f ? rd.y : 1e-30f,
+                     fabsf(rd.z) > 1e-30f ? rd.z : 1e-30f);
+    const V3 ri = v3(1.0f / rs.x, 1.0f / rs.y, 1.0f / rs.z);
+    const V3 t0 = (v3(h0) - ro) * ri, t1 = (v3(h1) - ro) * ri;
+    const float enter = fmaxf(fmaxf(fminf(t0.x, t1.x), fminf(t0.y, t1.y)), fminf(t0.z, t1.z));
+    const float exit = fminf(fminf(fmaxf(t0.x, t1.x), fmaxf(t0.y, t1.y)), fmaxf(t0.z, t1.z));
+    float t = fmaxf(enter, t_min);
+    const float t_end = fminf(exit, t_max);
+    if (t >= t_end) return false;
+    const uint32_t steps = min(S.sdf_iters, 512u);
+    for (uint32_t i = 0; i < steps; ++i) {
+        const V3 pl = (ro + rd * t) - n.c;
+        const float ad = fabsf(de_fractal(pl, n.shape, n.q, S.frac_power, S.frac_iters));
+        const float eps_i = S.sdf_eps * (1.0f + S.frac_eps_scale * float(i));
+        if (ad < eps_i) {
+            out_t = t;
+            out_step = i;
+            return true;
+        }
+        t += fmaxf(ad, S.sdf_eps);
+        if (t >= t_end) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool sdf_is_fractal(const float4* C) {
+    const uint32_t count = __float_as_uint(__ldg(C).w);
+    if (count == 0u) return false;
+    const float4 n0 = __ldg(C + 4u + 3u * (count - 1u));
+    return __float_as_uint(n0.x) == 0u && __float_as_uint(n0.y) >= 6u;
+}
+
 // traceSdfClusters: every cluster in order, a hit replaces the best only when
-// strictly closer (the reference's `t < h.t`)
+// strictly closer (the reference's `t < h.t`).  Fractal hits carry their
+// accepted step in bits 20-28 of the id.
 __device__ __forceinline__ void trace_sdf(const DScene& S, V3 ro, V3 rd, float& best_t, uint32_t& best_id) {
     for (uint32_t i = 0; i < S.sdf_count; ++i) {
+        const float4* C = S.sdf + size_t(kSdfStride) * i;
         float t;
-        if (sdf_trace(S, S.sdf + size_t(kSdfStride) * i, ro, rd, 1e-3f, best_t, t) && t < best_t) {
+        if (sdf_is_fractal(C)) {
+            uint32_t step = 0;
+            if (fractal_trace(S, C, ro, rd, 1e-3f, best_t, t, step) && t < best_t) {
+                best_t = t;
+                best_id = kSdfBit | (step << 20) | i;
+            }
+        } else if (sdf_trace(S, C, ro, rd, 1e-3f, best_t, t) && t < best_t) {
             best_t = t;
             best_id = kSdfBit | i;
         }
@@ -845,7 +966,7 @@ __device__ __noinline__ HitRec trace_wide(const DScene& S, V3 ro, V3 rd, float t
         trace_sdf(S, ro, rd, t, id);
         if (id != kMiss) {
             b.t = t;
-            b.key = 0x40000000u | (id & ~kSdfBit);
+            b.key = 0x40000000u | (id & 0xFFFFFu);
             b.id = id;
         }
     }
@@ -895,9 +1016,16 @@ __device__ __forceinline__ void table_material(const DScene& S, uint32_t m, Surf
 __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, HitRec h) {
     Surface s;
     if (h.id & kSdfBit) {   // SDF cluster: header material, normal at the hit point
-        const float4* C = S.sdf + size_t(kSdfStride) * (h.id & ~kSdfBit);
+        const float4* C = S.sdf + size_t(kSdfStride) * (h.id & 0xFFFFFu);
         const float4 h0 = __ldg(C), h1 = __ldg(C + 1), h2 = __ldg(C + 2), h3 = __ldg(C + 3);
-        s.normal = normalize(sdf_normal(C, __float_as_uint(h0.w), ro + rd * h.t));
+        if (sdf_is_fractal(C)) {
+            const SdfNodeD n = sdf_node(C, __float_as_uint(h0.w) - 1u);
+            const float eps_i = S.sdf_eps * (1.0f + S.frac_eps_scale * float((h.id >> 20) & 0x1FFu));
+            const float hh = fmaxf(eps_i * 8.0f, S.sdf_eps * 4.0f);
+            s.normal = fractal_normal((ro + rd * h.t) - n.c, n.shape, n.q, S.frac_power, S.frac_iters, hh);
+        } else {
+            s.normal = normalize(sdf_normal(C, __float_as_uint(h0.w), ro + rd * h.t));
+        }
         s.mat = __float_as_uint(h1.w);
         s.albedo = v3(h2);
         s.rough = h2.w;
@@ -1065,7 +1193,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         trace_sdf(*Sp, ro, rd, t, id);
         if (id != kMiss) {
             b.t = t;
-            b.key = 0x40000000u | (id & ~kSdfBit);
+            b.key = 0x40000000u | (id & 0xFFFFFu);
             b.id = id;
         }
     };

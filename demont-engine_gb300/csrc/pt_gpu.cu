@@ -1468,9 +1468,12 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     S.ltree = c->ltree.p;
     S.ltree_nodes = c->ltree_nodes;
     S.sdf = c->sdf.p;
-    S.sdf_count = c->sdf_count;   // a dispatch's push overrides these three
+    S.sdf_count = c->sdf_count;   // a dispatch's push overrides these
     S.sdf_iters = 128;            // r_sdf_max_iters default
     S.sdf_eps = 1e-4f;            // r_sdf_epsilon default
+    S.frac_iters = 12;            // r_sdf_fractal_iters default
+    S.frac_power = 8.0f;          // r_sdf_fractal_power default
+    S.frac_eps_scale = 1.0f;      // r_sdf_de_eps_scale default
     S.moon_tex = c->moon.p;
     S.moon_w = c->moon_w;
     S.moon_h = c->moon_h;
@@ -1496,6 +1499,9 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
         S.sdf_count = prm->sdf_params[0];
         S.sdf_iters = prm->sdf_params[1];
         S.sdf_eps = prm->sdf_params_f[0];
+        S.frac_iters = prm->sdf_params[3];
+        S.frac_power = prm->sdf_params_f[1];
+        S.frac_eps_scale = prm->sdf_params_f[2];
     }
     return S;
 }
@@ -2027,8 +2033,6 @@ int pt_gpu_upload_sdf(pt_gpu_ctx* ctx, const float* clusters, uint32_t n) {
         for (uint32_t i = 0; i < count; ++i) {
             const uint32_t* nd = h + 16u + 12u * i;
             const uint32_t op = nd[0], shape = nd[1], a = nd[2], b = nd[3];
-            if (op == 0u && shape >= 6u && shape <= 8u)
-                return set_err(ctx, PT_ERR_UNSUPPORTED, at + "fractal leaves (Mandelbulb/Mandelbox/Apollonian) are not built");
             if (op > 9u || (op == 0u && shape > 8u)) return set_err(ctx, PT_ERR_INVALID, at + "bad op or shape");
             if (op >= 1u && op <= 3u && (a >= i || b >= i))
                 return set_err(ctx, PT_ERR_INVALID, at + "an op must combine earlier nodes");
@@ -2452,7 +2456,10 @@ int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d
     prm.light_count = ctx->light_count;
     prm.sdf_params[0] = ctx->sdf_count;   // every uploaded SDF cluster, with the
     prm.sdf_params[1] = 128u;             // reference's default trace settings
+    prm.sdf_params[3] = 12u;
     prm.sdf_params_f[0] = 1e-4f;
+    prm.sdf_params_f[1] = 8.0f;
+    prm.sdf_params_f[2] = 1.0f;
     const DScene S = make_scene(ctx, &prm);
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     const float4 *dro, *drd;
@@ -2705,11 +2712,15 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             DScene& d = st[views[i].scene];
             const PtPathParams& q = views[i].params;
             if (seen[views[i].scene] && (d.sdf_count != q.sdf_params[0] || d.sdf_iters != q.sdf_params[1] ||
-                                         d.sdf_eps != q.sdf_params_f[0]))
+                                         d.sdf_eps != q.sdf_params_f[0] || d.frac_iters != q.sdf_params[3] ||
+                                         d.frac_power != q.sdf_params_f[1] || d.frac_eps_scale != q.sdf_params_f[2]))
                 return set_err(ctx, PT_ERR_INVALID, "batch: views of one scene disagree on the SDF settings");
             d.sdf_count = q.sdf_params[0];
             d.sdf_iters = q.sdf_params[1];
             d.sdf_eps = q.sdf_params_f[0];
+            d.frac_iters = q.sdf_params[3];
+            d.frac_power = q.sdf_params_f[1];
+            d.frac_eps_scale = q.sdf_params_f[2];
             seen[views[i].scene] = 1;
         }
     }

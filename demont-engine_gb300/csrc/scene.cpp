@@ -473,6 +473,8 @@ struct pt_scene {
         {"r_planet_radius", 6378137.0},
         {"r_exposure", 1.5},         {"r_tonemap_op", 0},
         {"r_sdf_max_iters", 128},    {"r_sdf_epsilon", 1e-4},
+        {"r_sdf_fractal_power", 8},  {"r_sdf_fractal_iters", 12},
+        {"r_sdf_de_eps_scale", 1},   {"r_sdf_normal_mode", 0},
         {"r_capture_seed", 0},
         {"app_window_width", 0},     {"app_window_height", 0},
     };
@@ -1648,9 +1650,17 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
         it = std::min(std::max(it, 1), 256);
         float eps = float(s->cvar("r_sdf_epsilon"));
         if (eps < 1e-7f) eps = 1e-7f;
+        const float power = std::min(std::max(float(s->cvar("r_sdf_fractal_power")), 2.0f), 64.0f);
+        const int fit = std::min(std::max(int(s->cvar("r_sdf_fractal_iters")), 1), 32);
+        const float de_sc = std::max(float(s->cvar("r_sdf_de_eps_scale")), 0.0f);
+        const int nm = std::min(std::max(int(s->cvar("r_sdf_normal_mode")), 0), 1);
         params->sdf_params[0] = uint32_t(s->sdf.size());
         params->sdf_params[1] = uint32_t(it);
+        params->sdf_params[3] = uint32_t(fit);
         params->sdf_params_f[0] = eps;
+        params->sdf_params_f[1] = power;
+        params->sdf_params_f[2] = de_sc;
+        params->sdf_params_f[3] = float(nm);
     }
     return PT_OK;
 }
@@ -1772,8 +1782,15 @@ bool sdf_leaf_box(const SdfNodeH& n, float* mn, float* mx) {
             mx[0] = q[1];  mx[1] = q[0] + q[1];  mx[2] = q[1];
             return true;
         }
+        case 6:
+        case 7:
+        case 8: {   // fractal leaves: +-bound
+            if (q[1] <= 0.0f) return false;
+            for (int k = 0; k < 3; ++k) { mn[k] = -q[1]; mx[k] = q[1]; }
+            return true;
+        }
         default:
-            return false;   // planes are unbounded; fractals are not built
+            return false;   // planes are unbounded
     }
 }
 
@@ -1834,7 +1851,9 @@ int pt_scene_sdf_leaf(pt_scene* s, uint32_t id, uint32_t shape, const float para
                       float z, uint32_t material, float r, float g, float b) {
     if (!s || !params) return PT_ERR_INVALID;
     if (material > 2u) return fail(s, "sdf: material must be 0, 1 or 2");
-    if (shape > 4u) return fail(s, "sdf: shape must be 0..4 (sphere, box, rounded box, torus, capsule)");
+    if (shape > 8u || shape == 5u)
+        return fail(s, "sdf: shape must be 0..4 (sphere, box, rounded box, torus, capsule) or 6..8 (fractals)");
+    if (shape >= 6u && params[0] < 0.0f) return fail(s, "sdf: fractal power/scale must be >= 0");
     if (shape == 2u && (!(params[0] > 0.0f) || !(params[1] > 0.0f) || !(params[2] > 0.0f) || params[3] < 0.0f))
         return fail(s, "sdf_round_box: half-extents must be > 0 and corner_r >= 0");
     SdfClusterH c{};
@@ -1860,6 +1879,10 @@ int pt_scene_sdf_combine(pt_scene* s, uint32_t id, uint32_t a, uint32_t b, uint3
     auto ia = s->sdf.find(a), ib = s->sdf.find(b);
     if (ia == s->sdf.end() || ib == s->sdf.end()) return fail(s, "sdf: child cluster not found");
     const SdfClusterH A = ia->second, B = ib->second;
+    for (const SdfClusterH* X : {&A, &B})
+        for (uint32_t i = 0; i < X->count; ++i)
+            if (X->nodes[i].op == 0u && X->nodes[i].shape >= 6u)
+                return fail(s, "sdf: fractal leaves cannot take part in smooth operations");
     if (A.count + B.count + 1u > 8u) return fail(s, "sdf: more than 8 nodes");
     SdfClusterH c{};
     for (uint32_t i = 0; i < A.count; ++i) c.nodes[i] = A.nodes[i];
@@ -2246,8 +2269,18 @@ int pt_scene_exec_cfg(pt_scene* s, const char* text, const char* base_dir, char*
             if (na != 1 || !U(1, id) || pt_scene_sdf_remove(s, id)) { bad(line, "unknown id"); continue; }
         } else if (cmd == "sdf_clear") {
             pt_scene_sdf_clear(s);
+        } else if (cmd == "sdf_mandelbulb" || cmd == "sdf_mandelbox" || cmd == "sdf_apollonian") {
+            // <id> <power|scale> <bound> <x y z> <material> <r g b>
+            const int m = na == 10 ? to_mat(tok[7]) : -1;
+            if (na != 10 || !U(1, id) || !floats(2, 5) || m < 0) { bad(line, "malformed arguments"); continue; }
+            float rgb[3];
+            if (!F(8, rgb[0]) || !F(9, rgb[1]) || !F(10, rgb[2])) { bad(line, "bad colour"); continue; }
+            const uint32_t shape = cmd == "sdf_mandelbulb" ? 6u : cmd == "sdf_mandelbox" ? 7u : 8u;
+            const float prm4[4] = {f[0], f[1], 0.0f, 0.0f};
+            if (pt_scene_sdf_leaf(s, id, shape, prm4, f[2], f[3], f[4], uint32_t(m), rgb[0], rgb[1], rgb[2]))
+                bad(line, s->err);
         } else if (cmd.rfind("sdf_", 0) == 0) {
-            skip(line, "procedural SDF ops and fractal SDFs are not built");
+            skip(line, "procedural SDF ops: compiled out of the reference's default build");
         } else if (cmd == "cam_pos") {
             if (na != 3 || !floats(1, 3)) { bad(line, "want x y z"); continue; }
             std::memcpy(s->cam_pos, f, 12);

@@ -88,8 +88,8 @@ typedef struct PtPathParams {
     float    sun_extra[4];          /* size multiplier, distance ratio, vertical flatten (1 = round), - */
     float    sun_extra2[4];         /* sun disc brightness, -, -, - */
     /* SDF clusters (shaders/PathTrace.slang:859-885; engine fill src/engine/Engine.cpp:7940-7981) */
-    uint32_t sdf_params[4];         /* cluster count (= uploaded), sphere-trace iteration budget, -, - */
-    float    sdf_params_f[4];       /* hit epsilon, -, -, - */
+    uint32_t sdf_params[4];         /* cluster count (= uploaded), march step budget, -, fractal DE iterations */
+    float    sdf_params_f[4];       /* hit epsilon, fractal default power, fractal epsilon growth per step, - */
 } PtPathParams;
 
 /* 32-byte BVH node, identical to the reference's BvhNode / TriBvhNode
@@ -194,9 +194,11 @@ int pt_gpu_upload_light_tree(pt_gpu_ctx* ctx, const PtLightTreeNode* nodes, uint
  * albedo + roughness, ior + 3 pad, then 8 nodes of 3 float4: asuint(op, shape,
  * child_a, child_b), params, center + pad.  Nodes are evaluated in order; an op
  * combines earlier nodes (smooth union/subtract/intersect, displace); the last
- * node is the cluster's distance.  Hit ids of SDF clusters are 0x80000000 | index.
- * The procedural ops (5-9) evaluate as empty, as in the reference's default build;
- * fractal leaves return PT_ERR_UNSUPPORTED. */
+ * node is the cluster's distance.  A cluster whose last node is a fractal leaf
+ * (shape 6 Mandelbulb, 7 Mandelbox, 8 Apollonian gasket; params: power or scale,
+ * bound) is marched with the fractal estimator (shaders/SdfFractals.slang).  Hit
+ * ids of SDF clusters are 0x80000000 | index (fractals: | accepted step << 20).
+ * The procedural ops (5-9) evaluate as empty, as in the reference's default build. */
 int pt_gpu_upload_sdf(pt_gpu_ctx* ctx, const float* clusters, uint32_t n_clusters);
 
 /* ---- moon surface map (the moon_map texture of the gradient sky's moon disc,
@@ -366,7 +368,9 @@ int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathP
  * w = initial closest distance; <= 0 means the reference's 1e30).
  * hit_id out: 0xFFFFFFFF = miss; (0 << 30 | slot) = analytic record `slot` of the
  * uploaded buffer; (1u << 30 | tri) = original triangle index; (1u << 31 | c) = SDF
- * cluster c, sphere-traced with the reference's defaults (128 steps, epsilon 1e-4).
+ * cluster c (fractal clusters also carry the accepted step << 20), sphere-traced
+ * with the reference's defaults (128 steps, epsilon 1e-4, fractal: 12 DE
+ * iterations, power 8, epsilon growth 1).
  * t out: hit distance.
  * on_device != 0: all four pointers are device pointers. */
 int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d,

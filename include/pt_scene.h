@@ -96,7 +96,8 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
  * r_rr_start 2 (extension), r_denoiser 0; gradient sky (no env map): r_sun_elevation 30,
  * r_sun_azimuth 135 (degrees), r_sun_size 1, r_sun_disc_brightness 1, r_sun_horizon_flatten 1,
  * r_moon_size 1, r_moon_disc_brightness 0.7; output step: r_exposure 1.5, r_tonemap_op 0 (aces);
- * SDF: r_sdf_max_iters 128, r_sdf_epsilon 1e-4.
+ * SDF: r_sdf_max_iters 128, r_sdf_epsilon 1e-4, r_sdf_fractal_power 8, r_sdf_fractal_iters 12,
+ * r_sdf_de_eps_scale 1, r_sdf_normal_mode 0.
  * Returns PT_ERR_INVALID for unknown names. */
 int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
 int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);
@@ -160,7 +161,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
  *   light_point|spot|sphere|quad (argument orders as the reference's commands), light_remove <id>, light_clear
  *   cam_pos <x y z>, cam_yaw <deg>, cam_pitch <deg>, cam_fov <deg>
  *   r_sky_mode <gradient|hdri|procedural|hosek>, r_env_map <path.hdr> (relative to base_dir),
- *   sdf_sphere|box|round_box|torus|capsule, sdf_smin|sdf_smax|sdf_sdiff, sdf_remove, sdf_clear
+ *   sdf_sphere|box|round_box|torus|capsule, sdf_mandelbulb|mandelbox|apollonian,
+ *   sdf_smin|sdf_smax|sdf_sdiff, sdf_remove, sdf_clear
  *   (argument orders as the reference's commands),
  *   r_denoiser <off|...>, and every numeric cvar of pt_scene_set_cvar (incl. app_window_width/height,
  *   r_capture_seed, r_show_stars).
@@ -186,7 +188,8 @@ int pt_load_radiance_hdr(const char* path, float* rgb, uint32_t capacity_floats,
 /* ---- SDF clusters (src/engine/Engine.cpp:18605-18990 sdf_* commands) ----
  * A leaf cluster: shape 0 sphere (params: r), 1 box (hx hy hz), 2 rounded box
  * (hx hy hz corner_r), 3 torus (R r, XZ plane), 4 capsule (half_h r, along Y),
- * at center, material 0/1/2 with albedo.  A combined cluster: op 1 smooth union,
+ * 6 Mandelbulb (power, bound), 7 Mandelbox (scale, bound), 8 Apollonian gasket
+ * (scale, bound), at center, material 0/1/2 with albedo.  A combined cluster: op 1 smooth union,
  * 2 smooth subtract (b from a), 3 smooth intersect of clusters a and b with
  * smoothing k; a and b are consumed (the reference's sdf_smin/sdf_sdiff/sdf_smax).
  * Bounding boxes follow ComputeSdfAabb (src/renderer/AnalyticBvh.cpp:335-348). */

@@ -198,6 +198,7 @@ template <> struct M<float> {
     static float exp(float x) { return f_exp(x); }
     static float pow(float x, float y) { return f_pow(x, y); }
     static float asin(float x) { return f_asin(x); }
+    static float log(float x) { return f_log(x); }
 };
 template <> struct M<double> {
     static double sin(double x) { return std::sin(x); }
@@ -207,6 +208,7 @@ template <> struct M<double> {
     static double exp(double x) { return std::exp(x); }
     static double pow(double x, double y) { return std::pow(x, y); }
     static double asin(double x) { return std::asin(x); }
+    static double log(double x) { return std::log(x); }
 };
 
 // HLSL min/max return the non-NaN operand (IEEE minNum/maxNum).
@@ -576,11 +578,133 @@ template <class R> struct Tracer {
         }
         return false;
     }
+    // ---- fractal leaves (SdfFractals.slang) ----
+    static R fracr(R x) { return x - std::floor(x); }
+    static R de_fractal(V3<R> p, uint32_t shape, const R* q, R power_default, uint32_t iters) {
+        if (shape == 6u) {
+            const R power = (q[0] > R(0)) ? q[0] : power_default;
+            V3<R> z = p;
+            R dr = R(1), r = R(0);
+            for (uint32_t i = 0; i < iters; ++i) {
+                r = length(z);
+                if (r > R(2)) break;
+                const R theta = M<R>::acos(clampv(z.z / mx(r, R(1e-12)), R(-1), R(1)));
+                const R phi = M<R>::atan2(z.y, z.x);
+                dr = M<R>::pow(r, power - R(1)) * power * dr + R(1);
+                const R rp = M<R>::pow(r, power);
+                const R nt = theta * power, np = phi * power;
+                const R sn = M<R>::sin(nt);
+                z = V3<R>{sn * M<R>::cos(np), sn * M<R>::sin(np), M<R>::cos(nt)} * rp;
+                z = z + p;
+            }
+            return R(0.5) * M<R>::log(mx(r, R(1.0001))) * r / mx(dr, R(1e-12));
+        }
+        if (shape == 7u) {
+            const R scale = (q[0] != R(0)) ? q[0] : R(2.5);
+            V3<R> z = p;
+            R dr = R(1);
+            for (uint32_t i = 0; i < iters; ++i) {
+                z = {clampv(z.x, R(-1), R(1)) * R(2) - z.x, clampv(z.y, R(-1), R(1)) * R(2) - z.y,
+                     clampv(z.z, R(-1), R(1)) * R(2) - z.z};
+                const R r2 = dot(z, z);
+                if (r2 < R(0.25)) {
+                    z = z * R(4);
+                    dr = dr * R(4);
+                } else if (r2 < R(1)) {
+                    const R f = R(1) / r2;
+                    z = z * f;
+                    dr = dr * f;
+                }
+                z = z * scale + p;
+                dr = std::fabs(scale) * dr + R(1);
+            }
+            return length(z) / std::fabs(dr);
+        }
+        if (shape == 8u) {
+            const R scale = (q[0] != R(0)) ? q[0] : R(1.3);
+            V3<R> z = p;
+            R dr = R(1);
+            for (uint32_t i = 0; i < iters; ++i) {
+                z = {R(-1) + R(2) * fracr(R(0.5) * z.x + R(0.5)), R(-1) + R(2) * fracr(R(0.5) * z.y + R(0.5)),
+                     R(-1) + R(2) * fracr(R(0.5) * z.z + R(0.5))};
+                const R r2 = dot(z, z);
+                const R k = mx(scale / mx(r2, R(1e-12)), R(1));
+                z = z * k;
+                dr = dr * k;
+            }
+            return (R(0.25) * std::fabs(z.y) - R(0.001)) / dr;
+        }
+        return R(1e30);
+    }
+    static V3<R> fractal_normal(V3<R> p, uint32_t shape, const R* q, R power, uint32_t iters, R h) {
+        const V3<R> e1{R(1), R(-1), R(-1)}, e2{R(-1), R(-1), R(1)}, e3{R(-1), R(1), R(-1)}, e4{R(1), R(1), R(1)};
+        const R d1 = de_fractal(p + e1 * h, shape, q, power, iters);
+        const R d2 = de_fractal(p + e2 * h, shape, q, power, iters);
+        const R d3 = de_fractal(p + e3 * h, shape, q, power, iters);
+        const R d4 = de_fractal(p + e4 * h, shape, q, power, iters);
+        const V3<R> n = e1 * d1 + e2 * d2 + e3 * d3 + e4 * d4;
+        const R l = length(n);
+        return (l > R(1e-12)) ? n / l : V3<R>{R(0), R(1), R(0)};
+    }
+    bool sdf_is_fractal(const float* C) const {
+        const uint32_t count = u_at(C + 3);
+        if (count == 0u) return false;
+        const float* n = C + 16 + 12 * (count - 1u);
+        return u_at(n) == 0u && u_at(n + 1) >= 6u;
+    }
+    bool fractal_trace(const float* C, V3<R> ro, V3<R> rd, R t_min, R t_max, R& out_t, uint32_t& step) const {
+        const SdfN n = sdf_node(C, u_at(C + 3) - 1u);
+        auto safe = [](R x) { return std::fabs(x) > R(1e-30) ? x : R(1e-30); };
+        const V3<R> ri{R(1) / safe(rd.x), R(1) / safe(rd.y), R(1) / safe(rd.z)};
+        const V3<R> t0 = (ld3<R>(C) - ro) * ri, t1 = (ld3<R>(C + 4) - ro) * ri;
+        const R enter = mx(mx(mn(t0.x, t1.x), mn(t0.y, t1.y)), mn(t0.z, t1.z));
+        const R exit = mn(mn(mx(t0.x, t1.x), mx(t0.y, t1.y)), mx(t0.z, t1.z));
+        R t = mx(enter, t_min);
+        const R t_end = mn(exit, t_max);
+        if (t >= t_end) return false;
+        const uint32_t steps = std::min(Q.sdf_params[1], 512u);
+        const R eps = R(Q.sdf_params_f[0]);
+        for (uint32_t i = 0; i < steps; ++i) {
+            const V3<R> pl = (ro + rd * t) - n.c;
+            const R ad = std::fabs(de_fractal(pl, n.shape, n.q, R(Q.sdf_params_f[1]), Q.sdf_params[3]));
+            const R eps_i = eps * (R(1) + R(Q.sdf_params_f[2]) * R(i));
+            if (ad < eps_i) {
+                out_t = t;
+                step = i;
+                return true;
+            }
+            t += mx(ad, eps);
+            if (t >= t_end) return false;
+        }
+        return false;
+    }
+
     void trace_sdf(V3<R> ro, V3<R> rd, Hit<R>& h) {
         const uint32_t n = std::min(Q.sdf_params[0], S.sdf_count);
         for (uint32_t i = 0; i < n; ++i) {
             const float* C = S.sdf_clusters + size_t(i) * 112;
             R t;
+            if (sdf_is_fractal(C)) {
+                uint32_t step = 0;
+                if (fractal_trace(C, ro, rd, R(1e-3), h.t, t, step) && t < h.t) {
+                    const SdfN nd = sdf_node(C, u_at(C + 3) - 1u);
+                    const R eps = R(Q.sdf_params_f[0]);
+                    const R eps_i = eps * (R(1) + R(Q.sdf_params_f[2]) * R(step));
+                    const R hh = mx(eps_i * R(8), eps * R(4));
+                    h.hit = true;
+                    h.t = t;
+                    h.normal = fractal_normal((ro + rd * t) - nd.c, nd.shape, nd.q, R(Q.sdf_params_f[1]),
+                                              Q.sdf_params[3], hh);
+                    h.mat = u_at(C + 7);
+                    h.albedo = ld3<R>(C + 8);
+                    h.roughness = R(C[11]);
+                    h.ior = R(C[12]);
+                    h.emission = {R(0), R(0), R(0)};
+                    h.id = 0x80000000u | (step << 20) | i;
+                    h.mid = 0xFFFFFFFFu;
+                }
+                continue;
+            }
             if (sdf_trace(C, ro, rd, R(1e-3), h.t, t) && t < h.t) {
                 V3<R> g;
                 sdf_dist(C, u_at(C + 3), ro + rd * t, &g);

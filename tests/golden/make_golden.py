@@ -88,6 +88,30 @@ def sdf_clusters(n, seed):
     return out
 
 
+def sdf_fractal_clusters(n, seed):
+    """Fractal leaves (Mandelbulb 6, Mandelbox 7, Apollonian 8) with bound radii
+    that are sometimes non-positive (refused), alone or under a smooth union."""
+    rng = XorShift32(seed)
+    out = []
+    for c in range(n):
+        node = np.zeros(12, np.float32)
+        node[:4].view(np.uint32)[:] = [0, 6 + c % 3, 0, 0]
+        node[4:8] = [rng.rangef(1.0, 9.0), rng.rangef(-0.5, 4.0), 0.0, 0.0]
+        node[8:11] = [rng.rangef(-5, 5) for _ in range(3)]
+        arr = np.zeros((8, 12), np.float32)
+        arr[0] = node
+        if c % 4 == 3:      # under a smooth union with a sphere leaf
+            arr[1, :4].view(np.uint32)[:] = [0, 0, 0, 0]
+            arr[1, 4] = rng.rangef(0.2, 1.5)
+            arr[1, 8:11] = [rng.rangef(-5, 5) for _ in range(3)]
+            arr[2, :4].view(np.uint32)[:] = [1, 0, 0, 1]
+            arr[2, 4] = rng.rangef(0.0, 0.5)
+            out.append((arr, 3))
+        else:
+            out.append((arr, 1))
+    return out
+
+
 def main():
     if oracle.load_ref() is None:
         sys.exit("oracle/_ref/libref_builders.so missing: run `make -C oracle ref` first")
@@ -118,6 +142,13 @@ def main():
         boxes.append(np.concatenate([r[0], r[1], [1.0]]) if r else np.array([0, 0, 0, 0, 0, 0, 0], np.float32))
     out.update(sdf_nodes=np.stack([a for a, _ in cl]), sdf_counts=np.array([n for _, n in cl], np.uint32),
                sdf_boxes=np.stack(boxes).astype(np.float32))
+    cl = sdf_fractal_clusters(24, 0xF4AC7A15)
+    boxes = []
+    for arr, n in cl:
+        r = oracle.ref_sdf_aabb(arr, n)
+        boxes.append(np.concatenate([r[0], r[1], [1.0]]) if r else np.array([0, 0, 0, 0, 0, 0, 0], np.float32))
+    out.update(sdf_frac_nodes=np.stack([a for a, _ in cl]), sdf_frac_counts=np.array([n for _, n in cl], np.uint32),
+               sdf_frac_boxes=np.stack(boxes).astype(np.float32))
     np.savez_compressed(os.path.join(HERE, "reference_builders.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_builders.npz"))
 

@@ -1,6 +1,8 @@
 """SDF clusters on the GPU against the oracle: closest-hit ids and distances
 bit for bit (analytic prims + SDF clusters + mesh together), and renders bit
-for bit in both traversal modes, with a dielectric SDF in the shadow rays."""
+for bit in both traversal modes, with a dielectric SDF in the shadow rays.
+Fractal leaves (Mandelbulb, Mandelbox, Apollonian) the same way, their hit ids
+carrying the accepted march step."""
 import numpy as np
 import pytest
 
@@ -90,7 +92,67 @@ def test_sdf_batch_equals_plain(pt, dev):
     scene.close()
 
 
-def test_sdf_count_mismatch_and_fractals_are_rejected(pt, dev):
+FRACTAL_SCENE = """
+cam_pos 0 3 9
+cam_pitch -14
+cam_fov 60
+r_sky_mode procedural
+r_sun_elevation 35
+r_spp 1
+r_max_bounces 3
+prim_plane 1 0 1 0 0 lambert 0.6 0.6 0.6
+sdf_mandelbulb 1 8 1.3 0 1.3 0 lambert 0.9 0.5 0.2
+sdf_mandelbox 2 2.5 4.2 -5 4.2 -7 metal 0.8 0.8 0.9
+sdf_apollonian 3 1.3 1.8 3.5 1.8 -1 lambert 0.4 0.7 0.9
+sdf_sphere 4 0.6 -2.5 0.6 2 dielectric 1 1 1
+light_point 1 2 5 4 25 25 25
+"""
+
+
+def _fractal_scene(pt):
+    s = pt.Scene()
+    rep, n = s.exec_cfg(FRACTAL_SCENE)
+    assert n == 0, rep
+    return s
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_sdf_fractal_probe_bit_exact(pt, orc, dev, mode):
+    s = _fractal_scene(pt)
+    dev.set_traversal(mode)
+    dev.upload(s)
+    head, prm = s.push(8, 8)
+    rng = np.random.default_rng(8)
+    n = 6000
+    ro = np.zeros((n, 4), np.float32)
+    ro[:, :3] = rng.uniform(-3, 3, (n, 3)) + np.array([0, 3, 9])
+    d = rng.uniform(-5, 5, (n, 3)) + np.array([-0.5, 2.0, -3]) - ro[:, :3]
+    rd = np.zeros((n, 4), np.float32)
+    rd[:, :3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    g_hit, g_t = dev.trace(ro, rd)
+    o_hit, o_t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+    frac = ((o_hit & 0xC0000000) == 0x80000000) & ((o_hit & 0xFFFFF) < 3)
+    assert frac.sum() > 300 and ((o_hit >> 20) & 0x1FF)[frac].max() > 4   # fractal hits with step bits
+    mism = np.flatnonzero((g_hit != o_hit) | (g_t != o_t))
+    assert mism.size == 0, (mism.size, mism[:5])
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_sdf_fractal_render_bit_exact(pt, orc, dev, mode):
+    s = _fractal_scene(pt)
+    W, H = 48, 32
+    head, prm = s.push(W, H, frame_index=1, reset=1)
+    dev.set_traversal(mode)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.render(head, prm, 1)
+    g = dev.read_accum()
+    o, _ = orc.render(s.packed(), head, prm, W, H, 1)
+    assert g[..., :3].mean() > 0.02
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_sdf_count_mismatch_and_bad_ops_are_rejected(pt, dev):
     s = _scene(pt, with_mesh=False)
     dev.upload(s)
     dev.set_target(16, 16)
@@ -100,6 +162,6 @@ def test_sdf_count_mismatch_and_fractals_are_rejected(pt, dev):
         dev.render(head, prm, 1)
     bad = np.zeros(112, np.float32)
     bad[3:4].view(np.uint32)[0] = 1
-    bad[16:20].view(np.uint32)[:] = [0, 6, 0, 0]           # a Mandelbulb leaf
+    bad[16:20].view(np.uint32)[:] = [10, 0, 0, 0]          # an op past the last one
     with pytest.raises(pt.PtError):
         dev._check(dev.lib.pt_gpu_upload_sdf(dev.h, bad.ctypes.data_as(pt.P(pt.f32)), 1))
