@@ -1095,6 +1095,10 @@ __device__ __forceinline__ V3 cos_hemi(V3 n, uint32_t& seed) {
 // transmittance (shaders/PathTrace.slang:5089-5196) with clouds and water off.
 // `first` is the closest hit of segment 0 when the caller already traced it
 // (first.t < 0: trace it here).  Counts the closest-hit queries made here.
+// Each segment's search starts at the segment's own t_max: the reference
+// traces an unbounded closest hit and then tests `h.t >= t_max`, and a hit
+// beyond t_max only ever leads to "unoccluded", so the bounded search gives the
+// same closest hit below t_max and the same answer with fewer nodes visited.
 __device__ __forceinline__ V3 transmittance_from(const DScene& S, V3 o, V3 d, float t_max, int kmax,
                                                  HitRec first, uint32_t& segs, bool wide) {
     V3 t = v3(1.0f, 1.0f, 1.0f);
@@ -1104,7 +1108,7 @@ __device__ __forceinline__ V3 transmittance_from(const DScene& S, V3 o, V3 d, fl
             h = first;
         } else {
             ++segs;
-            h = trace_any_mode(S, o, d, 1e30f, wide);
+            h = trace_any_mode(S, o, d, fminf(t_max, 1e30f), wide);
         }
         if (h.id == kMiss || h.t >= t_max) return t;
         const Surface sf = surface_at(S, o, d, h);
@@ -1202,7 +1206,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         nx = -ro.x * inv.x;
         ny = -ro.y * inv.y;
         nz = -ro.z * inv.z;
-        b = Best{1e30f, 0u, kMiss};
+        b = Best{kShadow ? fminf(t_max, 1e30f) : 1e30f, 0u, kMiss};   // shadow: bounded as in transmittance_from
         const uint32_t linear = Sp->linear_count;
         const float4* pg = Sp->prim_geo;
         const uint32_t* pty = Sp->prim_type;

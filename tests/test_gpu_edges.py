@@ -1,0 +1,93 @@
+"""Edge cases of the render call against the oracle: an empty scene (sky only),
+images of one pixel and of ragged sizes that are not multiples of a warp or a
+block, zero and one bounce, several samples per pixel, the exponential moving
+average accumulation, and an accumulation resumed across calls of different
+frame counts.  Every case is bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _render_both(dev, orc, s, W, H, frames=1, frame_index=0, reset=1, tweak=None):
+    head, prm = s.push(W, H, frame_index=frame_index, reset=reset)
+    if tweak:
+        tweak(head, prm)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.render(head, prm, frames)
+    g = dev.read_accum()
+    o, _ = orc.render(s.packed(), head, prm, W, H, frames)
+    return g, o
+
+
+def test_empty_scene_renders_the_sky(pt, orc, dev):
+    s = pt.Scene()
+    env = np.zeros((8, 16, 3), np.float32)
+    env[..., 0], env[..., 1], env[..., 2] = 0.25, 0.5, 1.0
+    s.env(env)
+    g, o = _render_both(dev, orc, s, 24, 16)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+    np.testing.assert_allclose(g[..., :3], np.broadcast_to([0.25, 0.5, 1.0], (16, 24, 3)), rtol=1e-6)
+    assert (g[..., 3] == 1.0).all()
+
+
+def test_empty_scene_without_a_sky_is_black(pt, orc, dev):
+    s = pt.Scene()
+    s.env(np.zeros((2, 4, 3), np.float32))
+    g, o = _render_both(dev, orc, s, 5, 3)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+    assert (g[..., :3] == 0).all()
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (1, 37), (33, 7), (257, 3), (31, 33)])
+def test_ragged_image_sizes(pt, orc, dev, W, H):
+    s = pt.Scene().synth(0, seed=3)
+    g, o = _render_both(dev, orc, s, W, H, frames=2, frame_index=5)
+    assert g.shape == (H, W, 4)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+@pytest.mark.parametrize("bounces,spp", [(0, 1), (1, 1), (1, 3), (3, 5)])
+def test_bounce_and_sample_counts(pt, orc, dev, bounces, spp):
+    s = pt.Scene().synth(0, seed=1)
+
+    def tweak(head, prm):
+        head.max_bounces = bounces
+        head.spp = spp
+
+    g, o = _render_both(dev, orc, s, 40, 24, frame_index=7, tweak=tweak)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+    if bounces == 0:        # the bounce loop runs max_bounces times: nothing is traced
+        assert (g[..., :3] == 0).all() and (g[..., 3] == 1).all()
+    else:
+        assert g[..., :3].mean() > 0.0
+
+
+def test_ema_accumulation(pt, orc, dev):
+    s = pt.Scene().synth(0, seed=2)
+
+    def tweak(head, prm):
+        prm.accum_ema_alpha = 0.25
+
+    g, o = _render_both(dev, orc, s, 32, 20, frames=4, frame_index=11, tweak=tweak)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_accumulation_resumed_in_uneven_calls(pt, orc, dev):
+    """3 + 1 + 2 frames in three calls equal 6 frames in one call (frame
+    indices advancing, no reset after the first call)."""
+    s = pt.Scene().synth(0, seed=4)
+    W, H = 20, 12
+    dev.upload(s)
+    dev.set_target(W, H)
+    fi = 30
+    for k, n in enumerate((3, 1, 2)):
+        head, prm = s.push(W, H, frame_index=fi, reset=1 if k == 0 else 0)
+        dev.render(head, prm, n)
+        fi += n
+    g = dev.read_accum()
+    head, prm = s.push(W, H, frame_index=30, reset=1)
+    o, _ = orc.render(s.packed(), head, prm, W, H, 6)
+    assert (g[..., 3] == 6).all()
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
