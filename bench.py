@@ -574,27 +574,40 @@ def main():
             torch.cuda.synchronize()
             pg.barrier()
 
-    dev.set_profiling(True)
+    dev.set_profiling(False)
     for _ in range(args.warmup):
         dev.render(head, prm, args.frames)
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    t_dev, segs, ext, ext_ms, ext_launch, launches, sh_ms = 0.0, 0, 0, 0.0, 0, 0, 0.0
+    t_dev, segs, launches = 0.0, 0, 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         dev.render(head, prm, args.frames)
         st = dev.stats()
         t_dev += st.gpu_ms / 1e3
         segs += st.extension_rays + st.shadow_rays
-        ext += st.extension_rays
-        ext_ms += st.extend_ms
-        sh_ms += st.shadow_ms
-        ext_launch += st.extend_launches
         launches += st.kernel_launches
     t_wall = time.perf_counter() - t0
     barrier()
     clk = clocks.stop()
+
+    # per-kernel device times: the same steps again with the stages serial and
+    # CUDA events around every closest-hit / transmittance launch on its stream
+    # (in the timed schedule above the next bounce's closest-hit pass overlaps
+    # this bounce's shadow rays, so their spans are not each kernel's own time)
+    dev.set_profiling(2)
+    dev.render(head, prm, args.frames)
+    ext, ext_ms, ext_launch, sh_ms, t_serial = 0, 0.0, 0, 0.0, 0.0
+    for _ in range(args.steps):
+        dev.render(head, prm, args.frames)
+        st = dev.stats()
+        ext += st.extension_rays
+        ext_ms += st.extend_ms
+        sh_ms += st.shadow_ms
+        ext_launch += st.extend_launches
+        t_serial += st.gpu_ms / 1e3
+    barrier()
 
     # end to end through the C-ABI with host buffers (pinned when torch can pin)
     dev.set_profiling(False)
@@ -642,9 +655,12 @@ def main():
                 "note": "achieved = algorithmic bytes of the reference binary structures per segment "
                         "(B_seg) x segments / k_closest time; those bytes are mostly served by L1/L2, so "
                         "frac can exceed 1; dram_frac is the measured DRAM traffic (ncu, "
-                        "profiles/k_closest_c1.md) over the same time",
-                "step_share": {"k_closest": ext_ms / max(1e3 * t_dev, 1e-9),
-                               "k_transmit": sh_ms / max(1e3 * t_dev, 1e-9)}}
+                        "profiles/k_closest_c1.md) over the same time.  Kernel times: CUDA events around "
+                        "each launch in a second pass of the same K steps with the stages serial (in the "
+                        "timed schedule the next bounce's k_closest overlaps this bounce's k_transmit)",
+                "step_share": {"k_closest": ext_ms / max(1e3 * t_serial, 1e-9),
+                               "k_transmit": sh_ms / max(1e3 * t_serial, 1e-9),
+                               "serial_ms_per_step": 1e3 * t_serial / args.steps}}
     line = {"metric": METRIC, "value": segs / t_dev / 1e6, "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
             "wall_ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True, "scaling": "weak",

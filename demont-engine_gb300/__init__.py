@@ -555,7 +555,9 @@ class Device:
         return s
 
     def set_profiling(self, on=True):
-        self._check(self.lib.pt_gpu_set_profiling(self.h, 1 if on else 0))
+        """True/1: events on the overlapped schedule; 2: stages serial (each
+        kernel timed alone); False/0: off."""
+        self._check(self.lib.pt_gpu_set_profiling(self.h, int(on)))
 
     def set_traversal(self, mode):
         self._check(self.lib.pt_gpu_set_traversal(self.h, mode))

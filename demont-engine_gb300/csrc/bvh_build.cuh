@@ -7,7 +7,11 @@
 //     lowest surface-area-heuristic cost, and the chunks partition the item
 //     index array around the chosen plane;
 //   tasks of at most kSmallTask items: one thread builds the whole subtree
-//     depth-first (8-bin SAH, in-place partition), leaves of <= kMaxLeaf items.
+//     depth-first (8-bin SAH, in-place partition).  A range of at most
+//     kMaxLeaf items becomes a leaf when the SAH says so: n*A <= kLeafCt*A +
+//     the best split's cost (A: half areas; kLeafCt: the cost of a node visit
+//     relative to one primitive test, 1.5 measured best on the C0/C1 scenes
+//     among 1, 1.5 and 2); single items are always leaves.
 // The binary tree is then collapsed on the host into 4-wide nodes of 128 bytes
 // (one L2 line): each node keeps its children's boxes in SoA form so a thread
 // tests four boxes per fetch.  Boxes are padded outward by a relative 2^-20 so
@@ -33,6 +37,7 @@ constexpr int kBins = 16;
 constexpr int kSmallBins = 8;
 constexpr uint32_t kSmallTask = 256;
 constexpr uint32_t kMaxLeaf = 4;
+constexpr float kLeafCt = 1.5f;
 constexpr uint32_t kChunk = 4096;
 constexpr int kBinWords = 13;   // count, box lo[3] hi[3], centroid lo[3] hi[3]
 constexpr int kTaskBinWords = 3 * kBins * kBinWords;
@@ -289,7 +294,7 @@ __global__ void kb_small(uint32_t ntasks, const uint4* tinfo, uint32_t* idx, con
             bh[0] = fmaxf(bh[0], h.x); bh[1] = fmaxf(bh[1], h.y); bh[2] = fmaxf(bh[2], h.z);
             for (int a = 0; a < 3; ++a) { cl[a] = fminf(cl[a], c[a]); ch[a] = fmaxf(ch[a], c[a]); }
         }
-        if (n <= kMaxLeaf) {
+        if (n <= 1u) {
             nodes[2u * node] = make_float4(bl[0], bl[1], bl[2], __uint_as_float(b0));
             nodes[2u * node + 1u] = make_float4(bh[0], bh[1], bh[2], __uint_as_float(n));
             continue;
@@ -328,6 +333,14 @@ __global__ void kb_small(uint32_t ntasks, const uint4* tinfo, uint32_t* idx, con
                 const float cost = float(c0) * half_area(l0[0], l0[1], l0[2], h0[0], h0[1], h0[2]) +
                                    float(c1) * half_area(l1[0], l1[1], l1[2], h1[0], h1[1], h1[2]);
                 if (cost < best) { best = cost; ba = a; bb = s; }
+            }
+        }
+        if (n <= kMaxLeaf) {   // SAH leaf test: n*A <= Ct/Ci*A + split cost
+            const float A = half_area(bl[0], bl[1], bl[2], bh[0], bh[1], bh[2]);
+            if (ba < 0 || float(n) * A <= kLeafCt * A + best) {
+                nodes[2u * node] = make_float4(bl[0], bl[1], bl[2], __uint_as_float(b0));
+                nodes[2u * node + 1u] = make_float4(bh[0], bh[1], bh[2], __uint_as_float(n));
+                continue;
             }
         }
         uint32_t mid;

@@ -1182,8 +1182,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     V3 ro = v3(0.0f, 0.0f, 0.0f), rd = ro, inv = ro;
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
     Best b{1e30f, 0u, kMiss};
-    uint32_t st_code[kPStack];
-    float st_t[kPStack];
+    uint2 st[kPStack];   // (node code, entry distance bits)
     // transmittance chain state (kShadow)
     V3 trans = v3(1.0f, 1.0f, 1.0f);
     float t_max = 0.0f;
@@ -1224,16 +1223,14 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         if (has_a) {
             phase = 1;
             nodes = Sp->a4;
-            st_code[0] = 0u;
-            st_t[0] = -3.0e38f;
+            st[0] = make_uint2(0u, __float_as_uint(-3.0e38f));
             sp = 1;
         } else {
             phase = 2;
             nodes = Sp->t4;
             if (Sp->sdf_count) sdf_pass();
             if (has_t) {
-                st_code[0] = 0u;
-                st_t[0] = -3.0e38f;
+                st[0] = make_uint2(0u, __float_as_uint(-3.0e38f));
                 sp = 1;
             }
         }
@@ -1283,8 +1280,9 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 continue;
             }
             --sp;
-            const uint32_t code = st_code[sp];
-            if (st_t[sp] > b.t) continue;
+            const uint2 top = st[sp];
+            const uint32_t code = top.x;
+            if (__uint_as_float(top.y) > b.t) continue;
             if (code & kLeafBit) {
                 leaf = code;
                 continue;
@@ -1330,8 +1328,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 const uint32_t tc = codes[far];
                 dist[far] = dist[i];
                 codes[far] = codes[i];
-                st_t[sp] = td;
-                st_code[sp] = tc;
+                st[sp] = make_uint2(tc, __float_as_uint(td));
                 ++sp;
             }
         }
@@ -1347,8 +1344,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
             if (phase == 1 && has_t) {
                 phase = 2;
                 nodes = Sp->t4;
-                st_code[0] = 0u;
-                st_t[0] = -3.0e38f;
+                st[0] = make_uint2(0u, __float_as_uint(-3.0e38f));
                 sp = 1;
             } else if (!kShadow) {
                 out_t[item] = b.t;

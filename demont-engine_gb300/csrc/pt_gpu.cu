@@ -1311,6 +1311,10 @@ struct pt_gpu_ctx {
     std::string err;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // second stream: the next bounce's closest-hit pass runs on it while the
+    // shadow rays of the current bounce run on `stream` (fork/join by events)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // scene
     DBuf<float4> prim_rec, prim_geo, bvh, tri, tri_bvh, mats, lights, env;
     DBuf<uint32_t> prim_type, prim_mat;
@@ -1371,7 +1375,7 @@ struct pt_gpu_ctx {
     pt_gpu_ctx* d_batch_scene = nullptr;
     std::vector<PtBatchView> d_batch_views;
     PtStats stats{};
-    bool profile = false;
+    int profile = 0;            // 0 off, 1 events on the overlapped schedule, 2 events, stages serial
     std::vector<cudaEvent_t> ev_pool;
 };
 
@@ -1803,8 +1807,11 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device_ordinal);
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
     CK(cudaEventCreate(&ctx->ev0));
     CK(cudaEventCreate(&ctx->ev1));
+    CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     int rc = dalloc(ctx, ctx->err_word, 1);
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->cnt, 8);
@@ -1820,6 +1827,7 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
 int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     if (!ctx) return PT_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     for (auto* b : {&ctx->prim_rec, &ctx->prim_geo, &ctx->bvh, &ctx->tri, &ctx->tri_bvh, &ctx->mats,
                     &ctx->lights, &ctx->env, &ctx->accum, &ctx->ray_o, &ctx->ray_d, &ctx->thr,
                     &ctx->rad, &ctx->fsum, &ctx->amb, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
@@ -1848,6 +1856,9 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PT_OK;
@@ -2213,11 +2224,35 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         A.scale = 1.0f / float(double(frames) * double(F.spp));
     }
     const int gadj = ctx->sm_count * 4;
+    // The next bounce's closest-hit pass overlaps this bounce's shadow rays
+    // (profiling mode 2 keeps the stages serial).  Profiling records an event
+    // pair around every closest-hit and shadow launch on the stream it runs on.
+    const bool overlap = ctx->profile != 2;
+    const int ge = grid_for(ctx, size_t(fpw) * F.npix, 8);
+    std::vector<std::pair<size_t, size_t>> ext_ev, sh_ev;
+    size_t ev_i = 0;
+    auto launch_extend = [&](cudaStream_t st, int qs, uint32_t* fetch) -> int {
+        if (ctx->profile) {
+            ext_ev.emplace_back(ev_i, ev_i + 1);
+            CK(cudaEventRecord(pool_event(ctx, ev_i++), st));
+            ++ev_i;
+        }
+        if (persistent) {
+            CK(cudaMemsetAsync(fetch, 0, 4, st));
+            k_closest<false><<<gpers, kThreads, 0, st>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
+                                                         P.hit_t, P.hit_id, fetch, P.stat);
+        } else if (S.use_wide) {
+            k_extend<true><<<ge, kThreads, 0, st>>>(S, P, qs);
+        } else {
+            k_extend<false><<<ge, kThreads, 0, st>>>(S, P, qs);
+        }
+        if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ext_ev.back().second), st));
+        return PT_OK;
+    };
 
     CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     ctx->stats = PtStats{};
-    size_t ev_i = 0;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
         const uint32_t nf = std::min(fpw, frames - f0);
@@ -2234,27 +2269,35 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const int qs = int(b & 1u);
-                CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
-                CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
-                const int ge = grid_for(ctx, npaths, 8);
-                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
-                if (persistent) {
-                    CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
-                    k_closest<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o,
-                                                                          P.ray_d, P.hit_t, P.hit_id, P.cnt + 3,
-                                                                          P.stat);
-                } else if (S.use_wide) {
-                    k_extend<true><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                if (b == 0u || !overlap) {
+                    CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
+                    CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
+                    if (int rc = launch_extend(ctx->stream, qs, ctx->cnt.p + 3)) return rc;
                 } else {
-                    k_extend<false><<<ge, kThreads, 0, ctx->stream>>>(S, P, qs);
+                    // this bounce's closest hits were traced on the side stream
+                    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+                    CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
+                    CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
                 }
-                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
                 if (adj)
                     k_shade<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, b);
                 else
                     k_shade<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{},
                                                                                                   Adj{}, qs, b);
-                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
+                if (overlap && b + 1u < F.maxb) {
+                    // fork: the next bounce's rays (written by k_shade) are traced
+                    // while this bounce's shadow rays are; k_resolve touches
+                    // neither the rays nor the hits
+                    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+                    CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+                    if (int rc = launch_extend(ctx->side, qs ^ 1, ctx->cnt.p + 4)) return rc;
+                    CK(cudaEventRecord(ctx->ev_join, ctx->side));
+                }
+                if (ctx->profile) {
+                    sh_ev.emplace_back(ev_i, ev_i + 1);
+                    CK(cudaEventRecord(pool_event(ctx, ev_i), ctx->stream));
+                    ev_i += 2;
+                }
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
                     k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
@@ -2264,7 +2307,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                 } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 }
-                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ev_i++), ctx->stream));
+                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, sh_ev.back().second), ctx->stream));
                 if (adj)
                     k_resolve<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, srec);
                 else
@@ -2290,11 +2333,14 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     ctx->stats.frames = frames;
     if (ctx->profile) {
         double ext = 0, sh = 0;
-        for (size_t i = 0; i + 3 < ev_i; i += 4) {
-            float a = 0, c = 0;
-            cudaEventElapsedTime(&a, ctx->ev_pool[i], ctx->ev_pool[i + 1]);
-            cudaEventElapsedTime(&c, ctx->ev_pool[i + 2], ctx->ev_pool[i + 3]);
+        for (const auto& e : ext_ev) {
+            float a = 0;
+            cudaEventElapsedTime(&a, ctx->ev_pool[e.first], ctx->ev_pool[e.second]);
             ext += a;
+        }
+        for (const auto& e : sh_ev) {
+            float c = 0;
+            cudaEventElapsedTime(&c, ctx->ev_pool[e.first], ctx->ev_pool[e.second]);
             sh += c;
         }
         ctx->stats.extend_ms = ext;
@@ -2440,7 +2486,8 @@ int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out) {
 
 int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on) {
     if (!ctx) return PT_ERR_INVALID;
-    ctx->profile = on != 0;
+    if (on < 0 || on > 2) return set_err(ctx, PT_ERR_INVALID, "set_profiling: on must be 0, 1 or 2");
+    ctx->profile = on;
     return PT_OK;
 }
 
@@ -2579,10 +2626,17 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
         k_camera<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths, s);
         for (uint32_t b = 0; b < max_b; ++b) {
             const int qs = int(b & 1u);
-            CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
-            CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
-            k_closest<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
-                                                                 P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+            if (b == 0u) {
+                CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
+                CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
+                k_closest<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
+                                                                     P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+            } else {
+                // this bounce's closest hits were traced on the side stream
+                CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+                CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
+                CK(cudaMemsetAsync(P.cnt + 2, 0, 4, ctx->stream));
+            }
             const size_t srec = size_t(s) * npaths;
             Adj A{};
             if (adj) {
@@ -2591,6 +2645,15 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
                 k_shade<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs, b);
             } else {
                 k_shade<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+            }
+            if (b + 1u < max_b) {
+                // fork: the next bounce's closest hits overlap this bounce's shadow rays
+                CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+                CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+                CK(cudaMemsetAsync(P.cnt + 4, 0, 4, ctx->side));
+                k_closest<true><<<gpers, kThreads, 0, ctx->side>>>(S0, Bt, P.q[qs ^ 1], P.cnt + (qs ^ 1), P.ray_o,
+                                                                   P.ray_d, P.hit_t, P.hit_id, P.cnt + 4, P.stat);
+                CK(cudaEventRecord(ctx->ev_join, ctx->side));
             }
             CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
             k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any,

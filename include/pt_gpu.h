@@ -239,7 +239,13 @@ int pt_gpu_get_stats(pt_gpu_ctx* ctx, PtStats* out);
 #define PT_TONEMAP_LINEAR   4
 int pt_gpu_tonemap(pt_gpu_ctx* ctx, float exposure, uint32_t op, int srgb_oetf, uint8_t* rgba8, int on_device);
 /* on != 0: record CUDA events around every closest-hit and transmittance
- * launch so PtStats.extend_ms / shadow_ms report their device time. */
+ * launch so PtStats.extend_ms / shadow_ms report their device time.
+ *   on == 1: the production schedule, in which the next bounce's closest-hit
+ *            pass runs on a second stream while this bounce's shadow rays
+ *            run (the two event spans overlap, so each kernel's span includes
+ *            time shared with the other);
+ *   on == 2: the stages run one after another on one stream, so each span is
+ *            the kernel's own device time (for per-kernel timing). */
 int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on);
 
 /* Traversal structure: 0 (default) = 4-wide SAH trees built on the device at

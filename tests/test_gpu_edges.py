@@ -91,3 +91,26 @@ def test_accumulation_resumed_in_uneven_calls(pt, orc, dev):
     o, _ = orc.render(s.packed(), head, prm, W, H, 6)
     assert (g[..., 3] == 6).all()
     assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_stage_schedules_and_profiling_modes_give_the_same_image(pt, dev):
+    """The overlapped schedule (next bounce's closest hits beside this bounce's
+    shadow rays), the same with events, and the serial schedule agree bit for
+    bit; the event modes report kernel times; other modes are refused."""
+    s = pt.Scene().synth(1, seed=2, scale=0.02)
+    W, H = 64, 40
+    head, prm = s.push(W, H, frame_index=3, reset=1)
+    dev.upload(s)
+    dev.set_target(W, H)
+    out = []
+    for mode in (0, 1, 2):
+        dev.set_profiling(mode)
+        dev.render(head, prm, 3)
+        out.append(dev.read_accum().copy())
+        st = dev.stats()
+        assert (st.extend_ms > 0 and st.shadow_ms > 0) == (mode != 0)
+    dev.set_profiling(0)
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+    assert np.array_equal(out[0].view(np.uint32), out[2].view(np.uint32))
+    with pytest.raises(pt.PtError):
+        dev.set_profiling(3)
