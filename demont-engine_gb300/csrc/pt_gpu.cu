@@ -1559,6 +1559,8 @@ int grid_for(pt_gpu_ctx* c, size_t work, int per_sm) {
     return int(std::max<size_t>(1, std::min(need, cap)));
 }
 
+constexpr size_t kWavePaths = size_t(1) << 26;
+
 int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     if (ctx->cap >= npaths) return PT_OK;
     int rc = 0;
@@ -1583,7 +1585,10 @@ int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     rc |= dalloc(ctx, ctx->sh_brdf, 3 * npaths);
     rc |= dalloc(ctx, ctx->sh_tr, 3 * npaths);
 
-    if (rc) return PT_ERR_OOM;
+    if (rc) {
+        ctx->cap = 0;   // some buffers were freed: the next call re-checks each one
+        return PT_ERR_OOM;
+    }
     ctx->cap = npaths;
     return PT_OK;
 }
@@ -2176,10 +2181,18 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     sky_of(F, prm);
     const DScene S = make_scene(ctx, prm);
 
+    // Frames per wave: about kWavePaths paths in flight (376 bytes of path and
+    // shadow-ray state each, ~25 GB at the cap).  Larger waves keep more rays
+    // per bounce in the later, sparser bounces; if the device cannot hold the
+    // wave, halve it until it fits.
     uint32_t fpw = ctx->wave_frames_override;
-    if (fpw == 0) fpw = std::max<uint32_t>(1, uint32_t((16u << 20) / std::max<uint32_t>(F.npix, 1)));
+    if (fpw == 0) fpw = std::max<uint32_t>(1, uint32_t(kWavePaths / std::max<uint32_t>(F.npix, 1)));
     fpw = std::min(fpw, frames);
     int rc = ensure_wave(ctx, size_t(fpw) * F.npix);
+    while (rc == PT_ERR_OOM && ctx->wave_frames_override == 0 && fpw > 1) {
+        fpw = (fpw + 1) / 2;
+        rc = ensure_wave(ctx, size_t(fpw) * F.npix);
+    }
     if (rc) return rc;
 
     DPaths P{};

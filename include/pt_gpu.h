@@ -268,7 +268,8 @@ typedef struct PtAccelInfo {
 int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out);
 
 /* Max number of frames batched into one device wave (default: chosen from the
- * frame size so a wave holds about 16 M paths). 0 restores the default. */
+ * frame size so a wave holds about 64 M paths, ~25 GB of path state, halved
+ * while the device cannot hold it). 0 restores the default. */
 int pt_gpu_set_wave_frames(pt_gpu_ctx* ctx, uint32_t frames_per_wave);
 
 /* ---- batched render (extension: many views of several scenes in one wavefront) ----
