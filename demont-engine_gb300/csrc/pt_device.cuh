@@ -856,13 +856,61 @@ __device__ __forceinline__ void wide_leaf(const DScene& S, uint32_t code, V3 ro,
     }
 }
 
+// One 4-wide node: test its four child boxes and order the children that pass
+// far to near in registers (a 5-exchange sorting network; children that fail
+// get -3e38 and sort last), so that pushing them in order leaves the nearest on
+// top.  Returns how many passed.  Static indices only: the arrays stay in
+// registers.  The slab test uses fma on -ro*inv and widens the interval by 4e-7
+// relative: with the outward-padded boxes no true hit can be culled by rounding.
+__device__ __forceinline__ int wide_children(const float4* nodes, uint32_t code, V3 inv, float nx, float ny,
+                                             float nz, float best_t, float (&dk)[4], uint32_t (&ck)[4]) {
+    const float4* nd = nodes + 8u * code;
+    const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
+    const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
+    const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+    const int4 cn = __ldg(reinterpret_cast<const int4*>(nd + 7));
+    const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+    const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+    const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+    const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
+    int nh = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
+        const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
+        const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
+        float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+        float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
+        tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
+        const bool ok = nn[k] >= 0 && tmx >= fmaxf(tmin, 0.0f) && tmin <= best_t;
+        dk[k] = ok ? tmin : -3.0e38f;
+        ck[k] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k])) : uint32_t(cc[k]);
+        nh += ok ? 1 : 0;
+    }
+    auto xchg = [&](int a, int c) {
+        if (dk[a] < dk[c]) {
+            const float td = dk[a];
+            dk[a] = dk[c];
+            dk[c] = td;
+            const uint32_t tc = ck[a];
+            ck[a] = ck[c];
+            ck[c] = tc;
+        }
+    };
+    xchg(0, 1);
+    xchg(2, 3);
+    xchg(0, 2);
+    xchg(1, 3);
+    xchg(1, 2);
+    return nh;
+}
+
 // Front-to-back walk of one wide tree.  Leaves found while descending are
 // postponed until every active lane of the warp holds one (or has run out of
 // nodes), so the warp intersects primitives together instead of interleaving
-// box and primitive work lane by lane.  The slab test uses fma on -ro*inv and
-// widens the interval by 4e-7 relative: with the outward-padded boxes no true
-// hit can be culled by rounding (culling never changes the result, only the
-// work; the tie keys decide equal distances).
+// box and primitive work lane by lane.  Culling never changes the result, only
+// the work: the tie keys decide equal distances.
 template <bool kTri>
 __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, V3 ro, V3 rd, V3 inv,
                                           Best& b, uint32_t key_base, uint32_t& iters, uint32_t* st_code,
@@ -882,47 +930,17 @@ __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, 
                 leaf = code;
                 break;
             }
-            const float4* nd = nodes + 8u * code;
-            const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
-            const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
-            const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
-            const int4 cn = __ldg(reinterpret_cast<const int4*>(nd + 7));
-            const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-            const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-            const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
-            const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
-            float dist[4];
-            uint32_t codes[4];
-            int nh = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
-                const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
-                const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
-                float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-                float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-                tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
-                tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
-                if (nn[k] >= 0 && tmx >= fmaxf(tmin, 0.0f) && tmin <= b.t) {
-                    dist[nh] = tmin;
-                    codes[nh] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k]))
-                                            : uint32_t(cc[k]);
-                    ++nh;
-                }
-            }
+            float dk[4];
+            uint32_t ck[4];
+            const int nh = wide_children(nodes, code, inv, nx, ny, nz, b.t, dk, ck);
             if (sp + nh > kWideStackDev) { atomicOr(S.err, 2u); return; }
-            for (int i = 0; i < nh; ++i) {   // farthest first: the nearest child is popped next
-                int far = i;
-                for (int j = i + 1; j < nh; ++j)
-                    if (dist[j] > dist[far]) far = j;
-                const float td = dist[far];
-                const uint32_t tc = codes[far];
-                dist[far] = dist[i];
-                codes[far] = codes[i];
-                st_t[sp] = td;
-                st_code[sp] = tc;
-                ++sp;
-            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < nh) {
+                    st_t[sp + k] = dk[k];
+                    st_code[sp + k] = ck[k];
+                }
+            sp += nh;
             if (!__any_sync(__activemask(), leaf == 0u && sp > 0)) break;
         }
         if (leaf) {
@@ -1166,7 +1184,7 @@ struct ItemScenes {
     const uint32_t* path_scene; // scene index per path
 };
 
-template <bool kShadow, bool kBatch>
+template <bool kShadow, bool kBatch, bool kMats = false>
 __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes isc, const uint32_t* queue,
                                                    uint32_t n, const float4* ray_o, const float4* ray_d,
                                                    float* out_t, uint32_t* out_id, uint32_t* fetch_ctr,
@@ -1261,7 +1279,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                         t_max = o.w;
                         trans = v3(1.0f, 1.0f, 1.0f);
                         seg = 0;
-                        xm[0] = xm[1] = xm[2] = xm[3] = kNoMat;
+                        if (kMats) xm[0] = xm[1] = xm[2] = xm[3] = kNoMat;
                     }
                     start_segment();
                     active = true;
@@ -1287,50 +1305,18 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 leaf = code;
                 continue;
             }
-            const float4* nd = nodes + 8u * code;
-            const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
-            const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
-            const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
-            const int4 cn = __ldg(reinterpret_cast<const int4*>(nd + 7));
-            const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-            const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-            const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
-            const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
-            float dist[4];
-            uint32_t codes[4];
-            int nh = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
-                const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
-                const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
-                float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-                float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-                tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
-                tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
-                if (nn[k] >= 0 && tmx >= fmaxf(tmin, 0.0f) && tmin <= b.t) {
-                    dist[nh] = tmin;
-                    codes[nh] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k]))
-                                            : uint32_t(cc[k]);
-                    ++nh;
-                }
-            }
+            float dk[4];
+            uint32_t ck[4];
+            const int nh = wide_children(nodes, code, inv, nx, ny, nz, b.t, dk, ck);
             if (sp + nh > kPStack) {
                 atomicOr(Sp->err, 2u);
                 sp = 0;
                 continue;
             }
-            for (int i = 0; i < nh; ++i) {
-                int far = i;
-                for (int j = i + 1; j < nh; ++j)
-                    if (dist[j] > dist[far]) far = j;
-                const float td = dist[far];
-                const uint32_t tc = codes[far];
-                dist[far] = dist[i];
-                codes[far] = codes[i];
-                st[sp] = make_uint2(tc, __float_as_uint(td));
-                ++sp;
-            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < nh) st[sp + k] = make_uint2(ck[k], __float_as_uint(dk[k]));
+            sp += nh;
         }
         // leaf phase
         if (active && leaf != 0u) {
@@ -1370,7 +1356,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                             zero = true;
                         } else {
                             trans = trans * ((1.0f - fr) * sf.albedo);
-                            if (seg < 4) xm[seg] = sf.mid;
+                            if (kMats && seg < 4) xm[seg] = sf.mid;
                             const float adv = b.t + 1e-3f;
                             ro = ro + rd * adv;
                             rd = normalize(refr);
@@ -1384,7 +1370,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 }
                 if (finished) {
                     io.sh_tr[item] = f4(trans, 0.0f);
-                    if (io.sh_mats) io.sh_mats[item] = make_uint4(xm[0], xm[1], xm[2], xm[3]);
+                    if (kMats && io.sh_mats) io.sh_mats[item] = make_uint4(xm[0], xm[1], xm[2], xm[3]);
                     active = false;
                 }
             }

@@ -787,7 +787,6 @@ __device__ __forceinline__ void issue_shadow(const DPaths& P, uint32_t p, int k,
     P.sh_d[e] = f4(d, s1);
     P.sh_pre[e] = f4(pre, s2);
     P.sh_brdf[e] = f4(brdf, pdf);
-    P.sh_tr[e] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     mask |= (1u << k) | (clamp ? (16u << k) : 0u);
 }
 
@@ -1020,8 +1019,10 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
                 if (b + 1u >= F.maxb) ended = true;
             }
             if (ended) st |= kEnded;
-            P.ray_o[p] = f4(ro, 0.0f);
-            P.ray_d[p] = f4(rd, 0.0f);
+            if (!ended) {
+                P.ray_o[p] = f4(ro, 0.0f);
+                P.ray_d[p] = f4(rd, 0.0f);
+            }
             P.thr[p] = f4(thr, prev_pdf);
             P.rad[p] = f4(rad, 0.0f);
             P.state[p] = st;
@@ -1071,12 +1072,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_closest(const __grid_constant__
 
 // persistent transmittance: whole dielectric chains per lane (every segment
 // counted as a shadow segment)
-template <bool kB>
+template <bool kB, bool kMats>
 __global__ void __launch_bounds__(kThreads, 4) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
                                                           int kmax, uint4* sh_mats) {
     uint32_t done = 0;
     const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax, sh_mats};
-    persistent_closest<true, kB>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
+    persistent_closest<true, kB, kMats>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
                                  nullptr, P.cnt + 3, done, io);
     warp_add(P.stat + 1, done);
 }
@@ -2313,8 +2314,11 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                 }
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
-                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
-                                                                           adj ? ctx->d_sh_mats.p : nullptr);
+                    if (adj)
+                        k_transmit<false, true><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
+                                                                                     ctx->d_sh_mats.p);
+                    else
+                        k_transmit<false, false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
@@ -2669,8 +2673,10 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
                 CK(cudaEventRecord(ctx->ev_join, ctx->side));
             }
             CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-            k_transmit<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any,
-                                                                  adj ? ctx->d_sh_mats.p : nullptr);
+            if (adj)
+                k_transmit<true, true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, ctx->d_sh_mats.p);
+            else
+                k_transmit<true, false><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
             if (adj)
                 k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs,
                                                                                           srec);
@@ -3202,7 +3208,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                                                                                               qs, b);
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_transmit<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                    k_transmit<false, false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
