@@ -385,10 +385,20 @@ struct Node2H {
     uint32_t count;
 };
 
+// Child codes are what the traversal pushes: an internal child is its node
+// index; a leaf is kWideLeafBit | (items - 1) << 28 | first item position.  An
+// empty slot has code 0 and the degenerate box at (kEmptyBox)^3, which every
+// slab test rejects (its entry distance is huge, infinite or NaN), so the
+// traversal needs no emptiness test.  The traversal loads the first 112 bytes.
+constexpr uint32_t kWideLeafBit = 0x80000000u;
+constexpr uint32_t kWideMaxLeafItems = 8u;          // 3 count bits
+constexpr uint32_t kWideMaxItem = 1u << 28;          // first-item field
+constexpr float kEmptyBox = 3.0e38f;
+
 struct Wide4 {   // 128 bytes, the device node
     float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
-    int32_t child[4];   // internal: node index; leaf: first item position
-    int32_t count[4];   // -1 empty, 0 internal, > 0 leaf item count
+    uint32_t code[4];   // traversal codes (above)
+    int32_t count[4];   // -1 empty, 0 internal, > 0 leaf item count (not read by the traversal)
 };
 static_assert(sizeof(Wide4) == 128, "wide node must be one 128-byte line");
 
@@ -401,7 +411,8 @@ inline float area2(const Node2H& n) {
 }
 
 // Collapse the binary tree into 4-wide nodes (greedy: open the largest child).
-// Returns the maximum depth in wide nodes.
+// Returns the maximum depth in wide nodes, or -1 when a leaf does not fit the
+// child code (more than 8 items, or a first item at or past 2^28).
 inline int collapse4(const std::vector<Node2H>& bin, std::vector<Wide4>& out) {
     out.clear();
     if (bin.empty()) return 0;
@@ -440,9 +451,9 @@ inline int collapse4(const std::vector<Node2H>& bin, std::vector<Wide4>& out) {
         Wide4 w{};
         for (int k = 0; k < 4; ++k) {
             if (k >= nk) {
-                w.lox[k] = w.loy[k] = w.loz[k] = 1.0f;
-                w.hix[k] = w.hiy[k] = w.hiz[k] = 0.0f;
-                w.child[k] = 0;
+                w.lox[k] = w.loy[k] = w.loz[k] = kEmptyBox;
+                w.hix[k] = w.hiy[k] = w.hiz[k] = kEmptyBox;
+                w.code[k] = 0u;
                 w.count[k] = -1;
                 continue;
             }
@@ -452,12 +463,13 @@ inline int collapse4(const std::vector<Node2H>& bin, std::vector<Wide4>& out) {
             w.loy[k] = pad_lo(c.lo[1], ext); w.hiy[k] = pad_hi(c.hi[1], ext);
             w.loz[k] = pad_lo(c.lo[2], ext); w.hiz[k] = pad_hi(c.hi[2], ext);
             if (c.count > 0) {
-                w.child[k] = int32_t(c.lf);
+                if (c.count > kWideMaxLeafItems || c.lf >= kWideMaxItem) return -1;
+                w.code[k] = kWideLeafBit | ((c.count - 1u) << 28) | c.lf;
                 w.count[k] = int32_t(c.count);
             } else {
                 const uint32_t wi = uint32_t(out.size());
                 out.push_back(Wide4{});
-                w.child[k] = int32_t(wi);
+                w.code[k] = wi;
                 w.count[k] = 0;
                 work.push_back({kids[k], wi, it.depth + 1});
             }

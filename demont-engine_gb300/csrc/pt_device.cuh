@@ -856,36 +856,50 @@ __device__ __forceinline__ void wide_leaf(const DScene& S, uint32_t code, V3 ro,
     }
 }
 
+// Three-input float max / min (PTX ISA 8.8, sm_100 and later): one ALU
+// instruction instead of two; the same selection as nesting fmaxf / fminf.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // One 4-wide node: test its four child boxes and order the children that pass
 // far to near in registers (a 5-exchange sorting network; children that fail
 // get -3e38 and sort last), so that pushing them in order leaves the nearest on
 // top.  Returns how many passed.  Static indices only: the arrays stay in
 // registers.  The slab test uses fma on -ro*inv and widens the interval by 4e-7
 // relative: with the outward-padded boxes no true hit can be culled by rounding.
+// The node's child codes are stored ready to push, and empty slots hold a box
+// no slab test accepts, so the last 16 bytes of the node are not loaded.
 __device__ __forceinline__ int wide_children(const float4* nodes, uint32_t code, V3 inv, float nx, float ny,
                                              float nz, float best_t, float (&dk)[4], uint32_t (&ck)[4]) {
     const float4* nd = nodes + 8u * code;
     const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
     const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
-    const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
-    const int4 cn = __ldg(reinterpret_cast<const int4*>(nd + 7));
+    const uint4 ch = __ldg(reinterpret_cast<const uint4*>(nd + 6));
     const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
     const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
     const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
-    const int cc[4] = {ch.x, ch.y, ch.z, ch.w}, nn[4] = {cn.x, cn.y, cn.z, cn.w};
+    const uint32_t cc[4] = {ch.x, ch.y, ch.z, ch.w};
     int nh = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
         const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
         const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
-        float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-        float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        float tmin = fmax3(fminf(t0x, t1x), fminf(t0y, t1y), fminf(t0z, t1z));
+        float tmx = fmin3(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fmaxf(t0z, t1z));
         tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
         tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
-        const bool ok = nn[k] >= 0 && tmx >= fmaxf(tmin, 0.0f) && tmin <= best_t;
+        const bool ok = tmx >= fmaxf(tmin, 0.0f) && tmin <= best_t;
         dk[k] = ok ? tmin : -3.0e38f;
-        ck[k] = (nn[k] > 0) ? (kLeafBit | (uint32_t(nn[k] - 1) << 28) | uint32_t(cc[k])) : uint32_t(cc[k]);
+        ck[k] = cc[k];
         nh += ok ? 1 : 0;
     }
     auto xchg = [&](int a, int c) {

@@ -37,7 +37,12 @@ namespace {
 
 constexpr uint32_t kEnded = 4u, kSkipSky = 1u, kPrevLambert = 2u;
 constexpr uint32_t kAmbBit = 1u << 8;   // shadow mask: the path has a skylight ambient term (P.amb)
+static_assert(ptb::kWideLeafBit == ptd::kLeafBit, "wide-node leaf codes must match the traversal's");
 constexpr int kThreads = 256;
+// k_transmit carries the dielectric-chain state besides the traversal state: at
+// 3 blocks of 256 per SM it needs no register spills (at 4 it spilled 230 bytes
+// per thread and ran 2% slower on the 1080p triangle scene).
+constexpr int kTransmitBlocks = 3;
 
 struct DFrame {
     V3 cam_pos;
@@ -1073,7 +1078,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_closest(const __grid_constant__
 // persistent transmittance: whole dielectric chains per lane (every segment
 // counted as a shadow segment)
 template <bool kB, bool kMats>
-__global__ void __launch_bounds__(kThreads, 4) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
+__global__ void __launch_bounds__(kThreads, kTransmitBlocks) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
                                                           int kmax, uint4* sh_mats) {
     uint32_t done = 0;
     const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax, sh_mats};
@@ -1732,7 +1737,7 @@ int build_wide_mesh(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref,
     std::vector<ptb::Wide4> wide;
     const int depth = ptb::collapse4(bin, wide);
     ctx->t4_bin_nodes = uint32_t(bin.size());
-    if (3 * depth + 1 > kWideStackDev) { dfree(order); return PT_OK; }
+    if (depth < 0 || 3 * depth + 1 > kWideStackDev) { dfree(order); return PT_OK; }
     if ((rc = dupload(ctx, drank, rank.data(), n_slots)) || (rc = dalloc(ctx, ctx->tri4, 3 * size_t(n_slots))) ||
         (rc = dupload(ctx, ctx->t4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
         dfree(order); dfree(drank);
@@ -1768,7 +1773,7 @@ int build_wide_prims(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref
     if ((rc = gpu_build_tree(ctx, blo.p, bhi.p, nf, bin, order))) { cleanup(); return rc; }
     std::vector<ptb::Wide4> wide;
     const int depth = ptb::collapse4(bin, wide);
-    if (3 * depth + 1 > kWideStackDev) { cleanup(); return PT_OK; }
+    if (depth < 0 || 3 * depth + 1 > kWideStackDev) { cleanup(); return PT_OK; }
     if ((rc = dupload(ctx, drank, rank.data(), nf)) || (rc = dalloc(ctx, ctx->a4_geo, nf)) ||
         (rc = dalloc(ctx, ctx->a4_meta, nf)) ||
         (rc = dupload(ctx, ctx->a4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
@@ -2206,6 +2211,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
     const int gpers = ctx->sm_count * 4;
+    const int gtr = ctx->sm_count * kTransmitBlocks;
     const bool adj = dr.mode == RunMode::kAdjoint;
     const size_t total_paths = size_t(frames) * F.npix;
     size_t smem = 0;
@@ -2315,10 +2321,10 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
                     if (adj)
-                        k_transmit<false, true><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
+                        k_transmit<false, true><<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
                                                                                      ctx->d_sh_mats.p);
                     else
-                        k_transmit<false, false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                        k_transmit<false, false><<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
@@ -2634,6 +2640,7 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
     const DFrame F0{};
     const int gp = (npaths + 255) / 256;
     const int gpers = ctx->sm_count * int(ctx->b_tune.persistent_blocks_per_sm);
+    const int gtr = ctx->sm_count * std::min(int(ctx->b_tune.persistent_blocks_per_sm), kTransmitBlocks);
     const int gstream = int(std::max<size_t>(1, std::min<size_t>((npaths + kThreads - 1) / kThreads,
                                                                  size_t(ctx->sm_count) * ctx->b_tune.stream_blocks_per_sm)));
     CK(cudaMemsetAsync(P.stat, 0, 4 * sizeof(unsigned long long), ctx->stream));
@@ -2674,9 +2681,9 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
             }
             CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
             if (adj)
-                k_transmit<true, true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, ctx->d_sh_mats.p);
+                k_transmit<true, true><<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, ctx->d_sh_mats.p);
             else
-                k_transmit<true, false><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
+                k_transmit<true, false><<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
             if (adj)
                 k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs,
                                                                                           srec);
@@ -3172,6 +3179,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
     const int gpers = ctx->sm_count * 4;
+    const int gtr = ctx->sm_count * kTransmitBlocks;
     const uint32_t fpw = std::max<uint32_t>(1u, std::min<uint32_t>(frames, kNoAllocMaxPixels / F.npix));
     float4* accum = reinterpret_cast<float4*>(accum_device);
 
@@ -3208,7 +3216,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                                                                                               qs, b);
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_transmit<false, false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                    k_transmit<false, false><<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
