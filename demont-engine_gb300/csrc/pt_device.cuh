@@ -875,17 +875,29 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 // top.  Returns how many passed.  Static indices only: the arrays stay in
 // registers.  The slab test uses fma on -ro*inv and widens the interval by 4e-7
 // relative: with the outward-padded boxes no true hit can be culled by rounding.
-// The node's child codes are stored ready to push, and empty slots hold a box
-// no slab test accepts, so the last 16 bytes of the node are not loaded.
+// Each axis's near and far planes are loaded by the ray's direction sign, so
+// the entry and exit distances need no per-axis min/max (fma is monotonic in
+// the plane, so this picks the same values min/max would).  The acceptance test
+// rejects NaN distances, which an empty slot's box can produce.  The node's
+// child codes are stored ready to push, and empty slots hold a box no slab test
+// accepts, so the last 16 bytes of the node are not loaded.
 __device__ __forceinline__ int wide_children(const float4* nodes, uint32_t code, V3 inv, float nx, float ny,
                                              float nz, float best_t, float (&dk)[4], uint32_t (&ck)[4]) {
-    const float4* nd = nodes + 8u * code;
-    const float4 lox = __ldg(nd), hix = __ldg(nd + 1), loy = __ldg(nd + 2), hiy = __ldg(nd + 3);
-    const float4 loz = __ldg(nd + 4), hiz = __ldg(nd + 5);
-    const uint4 ch = __ldg(reinterpret_cast<const uint4*>(nd + 6));
-    const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-    const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-    const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+    // near / far planes by the ray's direction signs: the node is 128-byte
+    // aligned, so picking lo (+0) or hi (+16) of an axis is an OR of the address
+    const uintptr_t nb = reinterpret_cast<uintptr_t>(nodes + 8u * code);
+    const uintptr_t sx = (__float_as_uint(inv.x) >> 31) << 4, sy = (__float_as_uint(inv.y) >> 31) << 4;
+    const uintptr_t sz = (__float_as_uint(inv.z) >> 31) << 4;
+    const float4 nxv = __ldg(reinterpret_cast<const float4*>(nb | sx));
+    const float4 fxv = __ldg(reinterpret_cast<const float4*>(nb | (sx ^ 16u)));
+    const float4 nyv = __ldg(reinterpret_cast<const float4*>((nb | sy) + 32u));
+    const float4 fyv = __ldg(reinterpret_cast<const float4*>((nb | (sy ^ 16u)) + 32u));
+    const float4 nzv = __ldg(reinterpret_cast<const float4*>((nb | sz) + 64u));
+    const float4 fzv = __ldg(reinterpret_cast<const float4*>((nb | (sz ^ 16u)) + 64u));
+    const uint4 ch = __ldg(reinterpret_cast<const uint4*>(nb + 96u));
+    const float lx[4] = {nxv.x, nxv.y, nxv.z, nxv.w}, hx[4] = {fxv.x, fxv.y, fxv.z, fxv.w};
+    const float ly[4] = {nyv.x, nyv.y, nyv.z, nyv.w}, hy[4] = {fyv.x, fyv.y, fyv.z, fyv.w};
+    const float lz[4] = {nzv.x, nzv.y, nzv.z, nzv.w}, hz[4] = {fzv.x, fzv.y, fzv.z, fzv.w};
     const uint32_t cc[4] = {ch.x, ch.y, ch.z, ch.w};
     int nh = 0;
 #pragma unroll
@@ -893,8 +905,8 @@ __device__ __forceinline__ int wide_children(const float4* nodes, uint32_t code,
         const float t0x = fmaf(lx[k], inv.x, nx), t1x = fmaf(hx[k], inv.x, nx);
         const float t0y = fmaf(ly[k], inv.y, ny), t1y = fmaf(hy[k], inv.y, ny);
         const float t0z = fmaf(lz[k], inv.z, nz), t1z = fmaf(hz[k], inv.z, nz);
-        float tmin = fmax3(fminf(t0x, t1x), fminf(t0y, t1y), fminf(t0z, t1z));
-        float tmx = fmin3(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fmaxf(t0z, t1z));
+        float tmin = fmax3(t0x, t0y, t0z);   // planes already ordered near / far per axis
+        float tmx = fmin3(t1x, t1y, t1z);
         tmin = fmaf(-fabsf(tmin), 4e-7f, tmin);
         tmx = fmaf(fabsf(tmx), 4e-7f, tmx);
         const bool ok = tmx >= fmaxf(tmin, 0.0f) && tmin <= best_t;
