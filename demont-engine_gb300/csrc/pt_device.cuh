@@ -1187,8 +1187,10 @@ __device__ __forceinline__ V3 transmittance(const DScene& S, V3 o, V3 d, float t
 // Each lane holds one ray; when it finishes, the lane takes the next queued
 // ray at once (warp-aggregated atomic on a fetch counter) instead of waiting
 // for the slowest ray of its warp.  Within a round, the node phase runs while
-// any lane still has nodes to descend (lanes that popped a leaf hold it), then
-// every lane holding a leaf intersects it together.  Same hit semantics as
+// any lane still has nodes to descend (lanes that popped a leaf hold it; the
+// phase also ends early when only a few lanes still descend and as many are
+// idle), then every lane holding a leaf intersects it together, finished lanes
+// write their result and idle lanes fetch new rays.  Same hit semantics as
 // trace_wide: planes linearly, analytic tree, then the triangle tree.
 // ---------------------------------------------------------------------------
 constexpr int kPStack = 64;
