@@ -11,7 +11,7 @@ One step = the 64-frame accumulation (reset on the first frame).  `value` =
 (extension + shadow segments) / device time of the K timed steps, inputs
 resident in HBM.  `e2e` = the same through pt_gpu_render_to_host: per-frame
 push data in from the host and the RGBA32F accumulation buffer copied back to
-pinned host memory inside the timed region.  The scene buffers (~250 MB) stay
+pinned host memory inside the timed region.  The scene buffers (~350 MB) stay
 resident across steps, as they do across frames in the reference engine.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
@@ -671,7 +671,8 @@ def main():
                        "traversal": ("4-wide SAH (device-built, %d nodes, depth %d, build %.1f ms)"
                                      % (accel.mesh_wide_nodes, accel.mesh_wide_depth, accel.mesh_build_ms))
                        if (accel.mesh_wide and args.traversal == 0) else "reference binary BVH",
-                       "l2": "no flush: per-wave path state (~6 GB) and scene (~250 MB) exceed the 129 MB L2"},
+                       "l2": "no flush: per-wave path state (376 B x up to 64 M paths, ~25 GB at 32 frames "
+                             "per wave) and scene (~350 MB) exceed the 129 MB L2"},
             "e2e": {"value": e2e_segs / t_e2e / 1e6, "unit": "Mrays/s",
                     "h2d_bytes_per_step": args.frames * (ctypes.sizeof(pt.PtPushHead) + ctypes.sizeof(pt.PtPathParams)),
                     "d2h_bytes_per_step": W_FULL * H_FULL * 16},
