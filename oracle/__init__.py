@@ -1,7 +1,8 @@
 """TEST INFRASTRUCTURE ONLY -- ctypes binding of the CPU oracle.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
-this package, as the checker / baseline; the product never imports it.
+this package, to verify the GPU results and as the CPU baseline; the product
+never imports it.
 
   liboracle.so        CPU restatement of the reference path tracer (fp32 + fp64),
                       built from oracle/pt_oracle.cpp by oracle/Makefile

@@ -2,7 +2,7 @@
  * pt_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement of the reference path tracer (shaders/PathTrace.slang,
- * shaders/PathTraceMath.slang) used as the checker for the GPU path.  Only
+ * shaders/PathTraceMath.slang) that the GPU results are verified against.  Only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
  * it; the product never links or calls it.
  *

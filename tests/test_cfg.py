@@ -6,9 +6,10 @@ import struct
 import numpy as np
 import pytest
 
+import oracle
 from conftest import load_pkg
 
-REF = "/root/reference"
+REF = oracle.REF_TREE   # the reference source tree, when present (fixtures are read from it)
 
 
 def write_hdr(path, quads, rle=True):

@@ -119,7 +119,7 @@ def test_trace_shared_vertex_ties_wide_tree(pt, orc, dev):
 def test_trace_full_c1_rays_agreement(pt, orc, dev):
     """2^17 camera + 2^17 random rays of the full 2.46 M-triangle scene: the
     reference walk is bit-exact, the wide tree agrees on >= 99.99 % of hit ids
-    (the spec bar) with t within 1e-5 relative."""
+    with t within 1e-5 relative."""
     s = pt.Scene().synth(1, seed=0)
     W, H = 1920, 1080
     head, prm = s.push(W, H)
