@@ -163,9 +163,25 @@ def cpu_baseline(pt, orc, scene, head, prm, budget_s=12.0):
         t_used += time.perf_counter() - t0
         segs += c.ext_rays + c.shadow_rays
         frames += 1
-    return {"value": segs / t_used / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
-            "sample": f"frames 0..{frames - 1} of the 64 (1920x1080, 1 spp each), "
-                      f"{segs} segments in {t_used:.1f} s"}
+    out = {"value": segs / t_used / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+           "sample": f"frames 0..{frames - 1} of the 64 (1920x1080, 1 spp each), "
+                     f"{segs} segments in {t_used:.1f} s"}
+    # the reference's own CPU estimator (Software backend preview: primary hit,
+    # sky ambient, one sun shadow ray), restated on the oracle's traversal
+    sw_acc = np.zeros((H_FULL, W_FULL, 4), np.float32)
+    sw_segs, sw_t, sw_frames = 0, 0.0, 0
+    while sw_t < budget_s / 3 and sw_frames < FRAMES:
+        h0, p0 = scene.push(W_FULL, H_FULL, frame_index=head.frame_index + sw_frames, reset=int(sw_frames == 0))
+        t0 = time.perf_counter()
+        _, c = orc.software_preview(scene.packed(), h0, p0, W_FULL, H_FULL, accum=sw_acc, threads=cores)
+        sw_t += time.perf_counter() - t0
+        sw_segs += c.ext_rays + c.shadow_rays
+        sw_frames += 1
+    out["software_preview"] = {
+        "value": sw_segs / sw_t / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+        "sample": f"{sw_frames} frames 1920x1080 of the reference's Software-backend preview estimator "
+                  f"(1 primary + <=1 sun shadow ray per pixel), {sw_segs} segments in {sw_t:.1f} s"}
+    return out
 
 
 def _tris_at_scale(sc):

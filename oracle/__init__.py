@@ -92,6 +92,20 @@ def render(packed, head, prm, W, H, frames=1, accum=None, crop=None, fp64=False,
     return accum, c
 
 
+def software_preview(packed, head, prm, W, H, accum=None, threads=0):
+    """The reference's Software-backend preview estimator, one frame into
+    `accum` (H, W, 4); returns (accum, OracleCounters).  A timed CPU baseline."""
+    lib = load()
+    if accum is None:
+        accum = np.zeros((H, W, 4), np.float32)
+    c = OracleCounters()
+    rc = lib.oracle_software_preview(ctypes.byref(packed), ctypes.byref(head), ctypes.byref(prm), u32(W), u32(H),
+                                     accum.ctypes.data_as(P(f32)), ctypes.c_int(threads), ctypes.byref(c))
+    if rc != 0:
+        raise RuntimeError(f"oracle_software_preview failed: {rc}")
+    return accum, c
+
+
 def adjoint(packed, head, prm, W, H, frames, dl_di, threads=0):
     """FP64 adjoint: (grad_albedo, grad_emission), each (material_count, 3) float64,
     of a `frames`-frame render from reset for dLoss/dImage = dl_di (H, W, 3|4)."""

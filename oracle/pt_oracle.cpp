@@ -1621,6 +1621,77 @@ void trace_rays(const PtPackedScene& S, const PtPushHead& P, const PtPathParams&
     total.add(tr.cnt);
 }
 
+// The reference's Software-backend preview estimator, restated as a timed CPU
+// baseline (src/rhi_software/SoftwareTracer.cpp:870-1014; the procedural sky of
+// :215-228, the default sun of :697-705).  Per pixel: one primary ray through
+// the pixel centre; on a miss the procedural sky; on a hit 0.3 x albedo x
+// sky(n) of ambient, one shadow ray to the sun and Lambert sun light, plus
+// emission; NaN/negative channels zeroed, then the running mean.  Rows are
+// handed out by an atomic counter as the reference does.  The reference
+// traces with Embree; this restatement uses the oracle's traversal of the
+// uploaded BVHs.
+static V3<float> sw_proc_sky(V3<float> d, V3<float> sun) {
+    const float t_y = clampv(d.y * 0.5f + 0.5f, 0.0f, 1.0f);
+    const V3<float> horizon{0.55f, 0.62f, 0.70f}, zenith{0.18f, 0.32f, 0.55f};
+    const float w = std::pow(t_y, 0.7f);
+    const V3<float> sky = horizon * (1.0f - w) + zenith * w;
+    const float cos_sun = clampv(dot(d, sun), 0.0f, 1.0f);
+    const float halo = std::pow(cos_sun, 6.0f) * 0.5f;
+    const float disc = (cos_sun > 0.9998f) ? 2.5f : 0.0f;
+    return sky + V3<float>{1.0f, 0.92f, 0.78f} * (halo + disc);
+}
+
+void software_preview(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, uint32_t W,
+                      uint32_t H, float* accum, int threads, Counters& total) {
+    V3<float> sun{Q.sun_and_mode[0], Q.sun_and_mode[1], Q.sun_and_mode[2]};
+    sun = (length(sun) > 1e-3f) ? normalize(sun) : normalize(V3<float>{0.4f, 0.8f, 0.3f});
+    int nt = threads > 0 ? threads : int(std::thread::hardware_concurrency());
+    if (nt < 1) nt = 1;
+    std::vector<Counters> per(nt);
+    std::atomic<uint32_t> next{0};
+    const float inv_w = 1.0f / float(W), inv_h = 1.0f / float(H);
+    const float tanf = P.pos_fovtan[3], aspect = P.fwd_aspect[3];
+    auto worker = [&](int tid) {
+        Tracer<float> tr(S, P, Q, W, H);
+        for (;;) {
+            const uint32_t y = next.fetch_add(1);
+            if (y >= H) break;
+            for (uint32_t x = 0; x < W; ++x) {
+                const float ndc_x = (float(x) + 0.5f) * inv_w * 2.0f - 1.0f;
+                const float ndc_y = 1.0f - (float(y) + 0.5f) * inv_h * 2.0f;
+                const V3<float> rd = normalize(ld3<float>(P.fwd_aspect) + ld3<float>(P.right_xyz) * (ndc_x * aspect * tanf) +
+                                               ld3<float>(P.up_xyz) * (ndc_y * tanf));
+                const V3<float> ro = ld3<float>(P.pos_fovtan);
+                const Hit<float> h0 = tr.trace(ro, rd);
+                tr.cnt.ext++;
+                V3<float> col{0.0f, 0.0f, 0.0f};
+                if (!h0.hit) {
+                    col = sw_proc_sky(rd, sun);
+                } else {
+                    const V3<float> hp = ro + rd * h0.t;
+                    const V3<float> nf = (dot(h0.normal, rd) < 0.0f) ? h0.normal : h0.normal * -1.0f;
+                    const float n_dot_l = std::max(0.0f, dot(nf, sun));
+                    const V3<float> ambient = h0.albedo * sw_proc_sky(nf, sun) * 0.30f;
+                    V3<float> lit{0.0f, 0.0f, 0.0f};
+                    if (n_dot_l > 0.0f) {
+                        const Hit<float> sh = tr.trace(hp + nf * 1e-3f, sun);
+                        tr.cnt.shadow++;
+                        if (!sh.hit) lit = h0.albedo * V3<float>{2.4f, 2.2f, 1.9f} * n_dot_l;
+                    }
+                    col = ambient + lit + h0.emission;
+                }
+                float* a = accum + (size_t(y) * W + x) * 4;
+                accumulate<float>(a, col, P.reset_accum != 0u, Q.accum_ema_alpha);
+            }
+        }
+        per[tid] = tr.cnt;
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < nt; ++i) pool.emplace_back(worker, i);
+    for (auto& t : pool) t.join();
+    for (const auto& c : per) total.add(c);
+}
+
 void export_counters(const Counters& c, OracleCounters* out) {
     if (!out) return;
     out->rays = c.rays;
@@ -1668,6 +1739,15 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
         orc::render<double>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
     else
         orc::render<float>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
+    orc::export_counters(c, counters);
+    return 0;
+}
+
+int oracle_software_preview(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                            uint32_t W, uint32_t H, float* accum_rgba, int threads, OracleCounters* counters) {
+    if (!scene || !head || !params || !accum_rgba || W == 0 || H == 0) return -1;
+    orc::Counters c;
+    orc::software_preview(*scene, *head, *params, W, H, accum_rgba, threads, c);
     orc::export_counters(c, counters);
     return 0;
 }

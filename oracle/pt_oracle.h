@@ -59,6 +59,11 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
  * fp32 instance's (the GPU's paths bit for bit); each sample's contributions
  * are differentiated term by term in double (no suffix sums), with the
  * Russian-roulette probabilities held fixed.  -7: firefly clamp enabled. */
+/* The reference's Software-backend preview estimator (primary hit, sky-lit
+ * ambient, one sun shadow ray, emission; running mean), for a timed CPU
+ * baseline only: one frame into accum_rgba (H x W x 4). */
+int oracle_software_preview(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                            uint32_t W, uint32_t H, float* accum_rgba, int threads, OracleCounters* counters);
 int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
                    uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
                    double* grad_albedo, double* grad_emission);

@@ -6,7 +6,7 @@ Moller-Trumbore, the polynomial transcendentals' accuracy, and fp32 vs fp64."""
 import numpy as np
 import pytest
 
-from conftest import xorshift_rays, xorshift_spheres
+from conftest import load_pkg, xorshift_rays, xorshift_spheres
 
 
 def pcg_py(x):
@@ -140,3 +140,34 @@ def test_crop_render_equals_full_render_region(pt, orc):
     crop, _ = orc.render(s.packed(), head, prm, W, H, 1, crop=(5, 3, 17, 11))
     np.testing.assert_array_equal(full[3:11, 5:17], crop[3:11, 5:17])
     assert not crop[:3].any()
+
+
+def test_software_preview_estimator_closed_form(orc):
+    """The reference's Software-backend preview estimator restated for the CPU
+    baseline: a Lambert ground plane under the procedural sky gives
+    0.3 * albedo * sky(n) + albedo * sun * max(n.l, 0) at every pixel, and a
+    ray that misses gives sky(d)."""
+    pt = load_pkg()
+    s = pt.Scene()
+    s.plane(1, (0.0, 1.0, 0.0), 0.0, 0, (0.5, 0.25, 0.75))
+    s.env(np.zeros((2, 4, 3), np.float32))
+    s.camera((0.0, 5.0, 0.0), 0.0, -89.0, 30.0)
+    W, H = 16, 12
+    head, prm = s.push(W, H)
+    acc, c = orc.software_preview(s.packed(), head, prm, W, H, threads=2)
+    sun = np.array(prm.sun_and_mode[:3], np.float64)
+    sun = sun / np.linalg.norm(sun) if np.linalg.norm(sun) > 1e-3 else np.array([0.4, 0.8, 0.3]) / np.linalg.norm([0.4, 0.8, 0.3])
+
+    def sky(d):
+        ty = np.clip(d[1] * 0.5 + 0.5, 0, 1)
+        w = ty ** 0.7
+        base = np.array([0.55, 0.62, 0.70]) * (1 - w) + np.array([0.18, 0.32, 0.55]) * w
+        cs = np.clip(d @ sun, 0, 1)
+        return base + np.array([1.0, 0.92, 0.78]) * (cs ** 6 * 0.5 + (2.5 if cs > 0.9998 else 0.0))
+
+    alb = np.array([0.5, 0.25, 0.75])
+    n = np.array([0.0, 1.0, 0.0])
+    want = 0.3 * alb * sky(n) + alb * np.array([2.4, 2.2, 1.9]) * max(n @ sun, 0.0)
+    np.testing.assert_allclose(acc[..., :3], np.broadcast_to(want, (H, W, 3)), rtol=2e-5)
+    assert (acc[..., 3] == 1).all()
+    assert c.ext_rays == W * H and c.shadow_rays == (W * H if n @ sun > 0 else 0)
