@@ -849,6 +849,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
         bool cont = false;
         uint32_t shadow_mask = 0;
         uint32_t p = 0;
+        uint32_t oct = 0;   // direction octant of the next ray
         if (i < n) {
             p = q[i];
             const DFrame& F = kB ? B.views[B.path_view[p]] : F0;
@@ -1027,6 +1028,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
             if (!ended) {
                 P.ray_o[p] = f4(ro, 0.0f);
                 P.ray_d[p] = f4(rd, 0.0f);
+                oct = (rd.x < 0.0f ? 1u : 0u) | (rd.y < 0.0f ? 2u : 0u) | (rd.z < 0.0f ? 4u : 0u);
             }
             P.thr[p] = f4(thr, prev_pdf);
             P.rad[p] = f4(rad, 0.0f);
@@ -1036,9 +1038,25 @@ __global__ void __launch_bounds__(kThreads) k_shade(const __grid_constant__ DSce
             cont = !ended;
             }
         }
-        // compaction: survivors to the next queue, shadow rays to the shadow queue
-        const uint32_t slot = warp_push(P.cnt + (qsel ^ 1), cont);
-        if (cont) qn[slot] = p;
+        // compaction: survivors to the next queue grouped by the direction octant
+        // of their next ray within the block (a counting sort in shared memory),
+        // so that the closest-hit kernel's warps, which take consecutive queue
+        // slots, mostly hold rays of one octant; shadow rays to the shadow queue
+        __shared__ uint32_t s_hist[8], s_base[8], s_block;
+        if (threadIdx.x < 8u) s_hist[threadIdx.x] = 0u;
+        __syncthreads();
+        const uint32_t rank = cont ? atomicAdd(&s_hist[oct], 1u) : 0u;
+        __syncthreads();
+        if (threadIdx.x == 0u) {
+            uint32_t tot = 0;
+            for (int o = 0; o < 8; ++o) {
+                s_base[o] = tot;
+                tot += s_hist[o];
+            }
+            s_block = tot ? atomicAdd(P.cnt + (qsel ^ 1), tot) : 0u;
+        }
+        __syncthreads();
+        if (cont) qn[s_block + s_base[oct] + rank] = p;
         for (int k = 0; k < 3; ++k) {
             const bool has = (shadow_mask >> k) & 1u;
             const uint32_t ss = warp_push(P.cnt + 2, has);
