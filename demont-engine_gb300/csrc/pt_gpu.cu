@@ -2246,10 +2246,10 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         if (rc) return rc;
         CK(cudaMemsetAsync(ctx->d_grad.p, 0, 6 * size_t(dr.nmat) * sizeof(double), ctx->stream));
         smem = 6 * size_t(dr.nmat) * sizeof(double);
-        if (smem > 48u * 1024u) {
-            CK(cudaFuncSetAttribute(k_shade<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            CK(cudaFuncSetAttribute(k_resolve<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        }
+        // always opted in: k_shade also holds static shared memory (its queue
+        // counting sort), and the 48 KB default bounds static + dynamic together
+        CK(cudaFuncSetAttribute(k_shade<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_resolve<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     }
     P.srad = (dr.mode == RunMode::kRecord) ? ctx->d_srad.p : nullptr;
     Adj A{};
@@ -2869,10 +2869,10 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             return rc;
         CK(cudaMemsetAsync(ctx->d_grad.p, 0, 6 * size_t(dr.nmat) * sizeof(double), ctx->stream));
         smem = 6 * size_t(dr.nmat) * sizeof(double);
-        if (smem > 48u * 1024u) {
-            CK(cudaFuncSetAttribute(k_shade<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            CK(cudaFuncSetAttribute(k_resolve<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        }
+        // always opted in: k_shade also holds static shared memory (its queue
+        // counting sort), and the 48 KB default bounds static + dynamic together
+        CK(cudaFuncSetAttribute(k_shade<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_resolve<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         A.srad = ctx->d_srad.p;
         A.dldi = dr.dldi;
         A.grad = ctx->d_grad.p;
