@@ -848,6 +848,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__
     uint32_t* qn = P.q[qsel ^ 1];
     const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
     if (kAdj) adj_begin(A);
+    __shared__ uint32_t s_hist[2][8], s_base[8], s_block;
+    if (threadIdx.x < 8u) s_hist[0][threadIdx.x] = 0u;
+    __syncthreads();
     for (uint32_t it = 0; it < n_iter; ++it) {
         const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
         bool cont = false;
@@ -1046,16 +1049,17 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__
         // of their next ray within the block (a counting sort in shared memory),
         // so that the closest-hit kernel's warps, which take consecutive queue
         // slots, mostly hold rays of one octant; shadow rays to the shadow queue
-        __shared__ uint32_t s_hist[8], s_base[8], s_block;
-        if (threadIdx.x < 8u) s_hist[threadIdx.x] = 0u;
+        // (two histograms used in turn: iteration it counts into s_hist[it & 1]
+        // and clears the other one for the next iteration, two barriers each)
+        const uint32_t hb = it & 1u;
+        const uint32_t rank = cont ? atomicAdd(&s_hist[hb][oct], 1u) : 0u;
         __syncthreads();
-        const uint32_t rank = cont ? atomicAdd(&s_hist[oct], 1u) : 0u;
-        __syncthreads();
+        if (threadIdx.x < 8u) s_hist[hb ^ 1u][threadIdx.x] = 0u;
         if (threadIdx.x == 0u) {
             uint32_t tot = 0;
             for (int o = 0; o < 8; ++o) {
                 s_base[o] = tot;
-                tot += s_hist[o];
+                tot += s_hist[hb][o];
             }
             s_block = tot ? atomicAdd(P.cnt + (qsel ^ 1), tot) : 0u;
         }
