@@ -2296,6 +2296,9 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         return PT_OK;
     };
 
+    // work a failed earlier call left on the side stream finishes first
+    CK(cudaEventRecord(ctx->ev_join, ctx->side));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     ctx->stats = PtStats{};
@@ -2890,6 +2893,9 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     }
     const bool graph = ctx->b_tune.use_graph && dr.mode == RunMode::kRender;
 
+    // work a failed earlier call left on the side stream finishes first
+    CK(cudaEventRecord(ctx->ev_join, ctx->side));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     ctx->stats = PtStats{};
     unsigned long long tot_ext = 0, tot_sh = 0;
