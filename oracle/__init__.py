@@ -106,6 +106,23 @@ def software_preview(packed, head, prm, W, H, accum=None, threads=0):
     return accum, c
 
 
+def env_sample(packed, head, prm, xu, xv):
+    """sampleEnvMap for uniform pairs -> (dirs (n, 3), pdf (n,), pdfEnvMapDir(dirs) (n,))."""
+    lib = load()
+    xu = np.ascontiguousarray(xu, np.float32)
+    xv = np.ascontiguousarray(xv, np.float32)
+    n = xu.shape[0]
+    d = np.zeros((n, 4), np.float32)
+    p = np.zeros(n, np.float32)
+    q = np.zeros(n, np.float32)
+    rc = lib.oracle_env_sample(ctypes.byref(packed), ctypes.byref(head), ctypes.byref(prm), u32(n),
+                               xu.ctypes.data_as(P(f32)), xv.ctypes.data_as(P(f32)), d.ctypes.data_as(P(f32)),
+                               p.ctypes.data_as(P(f32)), q.ctypes.data_as(P(f32)))
+    if rc != 0:
+        raise RuntimeError(f"oracle_env_sample failed: {rc}")
+    return d[:, :3], p, q
+
+
 def adjoint(packed, head, prm, W, H, frames, dl_di, threads=0):
     """FP64 adjoint: (grad_albedo, grad_emission), each (material_count, 3) float64,
     of a `frames`-frame render from reset for dLoss/dImage = dl_di (H, W, 3|4)."""

@@ -1752,6 +1752,26 @@ int oracle_software_preview(const PtPackedScene* scene, const PtPushHead* head, 
     return 0;
 }
 
+// Environment-map importance sampling and its pdf (sampleEnvMap / pdfEnvMapDir,
+// shaders/PathTrace.slang:3638-3727) for n given uniform pairs, with the fp32
+// instance the GPU matches: directions (x, y, z, 0), pdfs and the sampled
+// texel (v * W + u).  For the statistical tests of the sampler.
+int oracle_env_sample(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params, uint32_t n,
+                      const float* xu, const float* xv, float* dir4, float* pdf, float* pdf_of_dir) {
+    if (!scene || !head || !params || (n && (!xu || !xv || !dir4 || !pdf || !pdf_of_dir))) return -1;
+    orc::Tracer<float> tr(*scene, *head, *params, 1, 1);
+    for (uint32_t i = 0; i < n; ++i) {
+        const auto es = tr.sample_env(xu[i], xv[i]);
+        dir4[4 * size_t(i)] = es.dir.x;
+        dir4[4 * size_t(i) + 1] = es.dir.y;
+        dir4[4 * size_t(i) + 2] = es.dir.z;
+        dir4[4 * size_t(i) + 3] = 0.0f;
+        pdf[i] = es.pdf;
+        pdf_of_dir[i] = tr.pdf_env_dir(es.dir);
+    }
+    return 0;
+}
+
 int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
                    uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
                    double* grad_albedo, double* grad_emission) {

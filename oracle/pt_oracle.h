@@ -64,6 +64,10 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
  * baseline only: one frame into accum_rgba (H x W x 4). */
 int oracle_software_preview(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
                             uint32_t W, uint32_t H, float* accum_rgba, int threads, OracleCounters* counters);
+/* Environment importance sampling for n uniform pairs (xu, xv): sampled
+ * directions (x, y, z, 0), their pdf as sampled, and pdfEnvMapDir of each. */
+int oracle_env_sample(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params, uint32_t n,
+                      const float* xu, const float* xv, float* dir4, float* pdf, float* pdf_of_dir);
 int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
                    uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
                    double* grad_albedo, double* grad_emission);
