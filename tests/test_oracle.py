@@ -171,3 +171,61 @@ def test_software_preview_estimator_closed_form(orc):
     np.testing.assert_allclose(acc[..., :3], np.broadcast_to(want, (H, W, 3)), rtol=2e-5)
     assert (acc[..., 3] == 1).all()
     assert c.ext_rays == W * H and c.shadow_rays == (W * H if n @ sun > 0 else 0)
+
+
+def test_degenerate_zero_radius_prim_keeps_traversal_whole(pt, orc):
+    """After the reference's r=0 case (tests/pt_core_analytic_bvh_test.cpp:540-600):
+    a zero-radius sphere at z=3, a unit sphere at z=6 and 8 xorshift spheres
+    behind them.  Every prim is in the tree once; the axis ray agrees with the
+    linear scan; the ray 0.5 above the axis hits the unit sphere."""
+    from conftest import XorShift32
+    cr = [[0.0, 0.0, 3.0, 1e-6], [0.0, 0.0, 6.0, 1.0]]   # the engine refuses r <= 0: set in the record below
+    rng = XorShift32(0xFACEC0DE)
+    for _ in range(2, 10):
+        x, y, z = rng.rangef(-3.0, 3.0), rng.rangef(-3.0, 3.0), rng.rangef(8.0, 12.0)
+        cr.append([x, y, z, 0.4])
+    cr = np.array(cr, np.float32)
+    from test_builders import product_analytic_bvh
+    nodes, perm = product_analytic_bvh(pt, cr)
+    assert sorted(perm.tolist()) == list(range(10))
+    ro = np.array([[0, 0, 0, 0], [0, 0.5, 0, 0]], np.float32)
+    rd = np.array([[0, 0, 1, 0], [0, 0, 1, 0]], np.float32)
+    res = []
+    for thr in (2, 10 ** 6):   # BVH / linear scan
+        s = sphere_scene(pt, cr, thr)
+        head, prm = s.push(8, 8)
+        pk = s.packed()
+        rec = np.ctypeslib.as_array(pk.prims, (pk.prim_count * 28,)).reshape(-1, 28)
+        slot0 = int(np.flatnonzero(rec[:, 11].view(np.uint32) == 0)[0])
+        rec[slot0, 3] = 0.0                                   # radius 0: a degenerate box in the tree
+        hit, t, _ = orc.trace(pk, head, prm, ro, rd)
+        ids = np.where(hit == 0xFFFFFFFF, -1, slot_to_input(s.arrays())[np.minimum(hit, 9)].astype(np.int64))
+        res.append((ids, t))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    assert res[0][0][1] == 1
+
+
+def test_every_node_box_contains_its_leaf_prims(pt):
+    """After the reference's containment case (:629): in the analytic tree of
+    the 50-sphere xorshift scene, every node's box holds the boxes of all prims
+    reachable below it, and every internal node's box holds its children's."""
+    from test_builders import product_analytic_bvh
+    cr = xorshift_spheres(50, 0xABCDEF01)
+    nodes, perm = product_analytic_bvh(pt, cr)
+    lo = nodes[:, 0:3].view(np.float32)
+    hi = nodes[:, 4:7].view(np.float32)
+    lf, cnt = nodes[:, 3], nodes[:, 7]
+
+    def prims_below(i):
+        if cnt[i] > 0:
+            return list(perm[lf[i]:lf[i] + cnt[i]])
+        return prims_below(lf[i]) + prims_below(lf[i] + 1)
+
+    for i in range(nodes.shape[0]):
+        for p in prims_below(i):
+            c, r = cr[p, :3], cr[p, 3]
+            assert np.all(lo[i] <= c - r) and np.all(hi[i] >= c + r), (i, p)
+        if cnt[i] == 0:
+            for ch in (lf[i], lf[i] + 1):
+                assert np.all(lo[i] <= lo[ch]) and np.all(hi[i] >= hi[ch])
