@@ -139,6 +139,22 @@ def extend_traffic_per_ray():
     return None
 
 
+def closest_hit_alu_share():
+    """ALU-pipe utilisation of the closest-hit kernel at bounce 0 from the
+    committed ncu summary (profiles/k_closest_c1.md, the
+    `sm__inst_executed_pipe_alu` row), as a fraction; None if absent."""
+    p = os.path.join(ROOT, "profiles", "k_closest_c1.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("| sm__inst_executed_pipe_alu"):
+            try:
+                return float(line.split("|")[2].strip().rstrip("%")) / 100.0
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
 def algorithmic_bytes(pt, orc, scene, head, prm):
     """B_seg = 32 (ray) + 16 (hit) + 32 N_node + 52 N_tri + 112 N_prim per extension
     segment, N from the oracle walking the reference binary BVH on a crop of frame 0."""
@@ -668,10 +684,12 @@ def main():
                 if (tpr and ext_ms > 0) else None,
                 "dram_frac": (tpr * per_launch_rays / (ext_ms / max(ext_launch, 1)) / 1e6 / peak)
                 if (tpr and ext_ms > 0) else None,
+                "alu_pipe_frac_ncu": closest_hit_alu_share(),
                 "note": "achieved = algorithmic bytes of the reference binary structures per segment "
                         "(B_seg) x segments / k_closest time; those bytes are mostly served by L1/L2, so "
                         "frac can exceed 1; dram_frac is the measured DRAM traffic (ncu, "
-                        "profiles/k_closest_c1.md) over the same time.  Kernel times: CUDA events around "
+                        "profiles/k_closest_c1.md) over the same time; the kernel's limiter is its ALU pipe "
+                        "(alu_pipe_frac_ncu, same summary).  Kernel times: CUDA events around "
                         "each launch in a second pass of the same K steps with the stages serial (in the "
                         "timed schedule the next bounce's k_closest overlaps this bounce's k_transmit)",
                 "step_share": {"k_closest": ext_ms / max(1e3 * t_serial, 1e-9),
