@@ -2,10 +2,10 @@
 //
 // Semantics follow shaders/PathTrace.slang and shaders/PathTraceMath.slang
 // (citations inline).  Built with -fmad=false and IEEE division/sqrt, so
-// every expression rounds exactly as written; sin/cos/atan2/acos are the
-// polynomial versions below (not libdevice), which makes the whole render
-// reproducible bit for bit by a CPU restatement that evaluates the same
-// expressions.
+// every expression rounds exactly as written; sin/cos/atan2/acos/asin/exp/
+// log/pow are the polynomial versions below (not libdevice), which makes the
+// whole render reproducible bit for bit by a CPU restatement that evaluates
+// the same expressions.
 #pragma once
 
 #include <cstdint>

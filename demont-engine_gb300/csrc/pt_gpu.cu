@@ -17,6 +17,13 @@
 //                sample radiance of paths that ended this bounce
 //   accumulate  running mean over the wave's frames, in frame order
 //
+// Extend and shadow are persistent closest-hit kernels over 4-wide SAH trees
+// (pt_device.cuh).  Once shade has written bounce b's next rays, extend of
+// bounce b+1 runs on a second stream beside shadow and resolve of bounce b.
+// Shade writes the next queue grouped by ray-direction octant within each
+// block, so the next extend's warps are more coherent.  A wave holds up to
+// ~64 M paths.
+//
 // All float math is compiled with -fmad=false and follows the shader's
 // operation order, so the result equals a scalar restatement bit for bit.
 
