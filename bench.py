@@ -139,6 +139,26 @@ def extend_traffic_per_ray():
     return None
 
 
+def shade_bytes_per_vertex(scene):
+    """Algorithmic bytes the shading stage reads per path vertex of this
+    workload, on the reference's data layouts: a material row (3 float4, 48 B);
+    at a Lambert hit, the environment NEE (one 16-B texel and one 4-B load per
+    step of the two CDF binary searches) and the HDRI-cluster pick (a direction
+    + pmf and a colour float4, 32 B); at a miss, the bilinear sky lookup (four
+    16-B texels) and the MIS pdf texel (16 B).  No analytic lights in this
+    workload."""
+    import math
+    a = scene.arrays()
+    h, w = a["env_conditional"].shape
+    search = 4 * (math.ceil(math.log2(h)) + math.ceil(math.log2(w)))
+    lambert = 48 + 16 + search + (32 if a["hdri_count"] else 0)
+    miss = 4 * 16 + 16
+    hdri = " + HDRI pick 32" if a["hdri_count"] else ""
+    return {"lambert_hit": lambert, "miss": miss, "unit": "B",
+            "terms": f"material 48 + env texel 16 + CDF searches {search}{hdri}; "
+                     f"miss: 4 bilinear texels 64 + pdf texel 16"}
+
+
 def closest_hit_alu_share():
     """ALU-pipe utilisation of the closest-hit kernel at bounce 0 from the
     committed ncu summary (profiles/k_closest_c1.md, the
@@ -685,6 +705,7 @@ def main():
                 "dram_frac": (tpr * per_launch_rays / (ext_ms / max(ext_launch, 1)) / 1e6 / peak)
                 if (tpr and ext_ms > 0) else None,
                 "alu_pipe_frac_ncu": closest_hit_alu_share(),
+                "shade_bytes_per_vertex": shade_bytes_per_vertex(scene),
                 "note": "achieved = algorithmic bytes of the reference binary structures per segment "
                         "(B_seg) x segments / k_closest time; those bytes are mostly served by L1/L2, so "
                         "frac can exceed 1; dram_frac is the measured DRAM traffic (ncu, "
