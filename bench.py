@@ -632,13 +632,15 @@ def main():
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    t_dev, segs, launches = 0.0, 0, 0
+    t_dev, segs, launches, segs_ext, segs_sh = 0.0, 0, 0, 0, 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         dev.render(head, prm, args.frames)
         st = dev.stats()
         t_dev += st.gpu_ms / 1e3
         segs += st.extension_rays + st.shadow_rays
+        segs_ext += st.extension_rays
+        segs_sh += st.shadow_rays
         launches += st.kernel_launches
     t_wall = time.perf_counter() - t0
     barrier()
@@ -706,6 +708,7 @@ def main():
                 if (tpr and ext_ms > 0) else None,
                 "alu_pipe_frac_ncu": closest_hit_alu_share(),
                 "shade_bytes_per_vertex": shade_bytes_per_vertex(scene),
+                "compulsory_bytes_per_segment": 48,
                 "note": "achieved = algorithmic bytes of the reference binary structures per segment "
                         "(B_seg) x segments / k_closest time; those bytes are mostly served by L1/L2, so "
                         "frac can exceed 1; dram_frac is the measured DRAM traffic (ncu, "
@@ -731,6 +734,8 @@ def main():
             "e2e": {"value": e2e_segs / t_e2e / 1e6, "unit": "Mrays/s",
                     "h2d_bytes_per_step": args.frames * (ctypes.sizeof(pt.PtPushHead) + ctypes.sizeof(pt.PtPathParams)),
                     "d2h_bytes_per_step": W_FULL * H_FULL * 16},
+            "segments_per_step": {"extension": segs_ext // args.steps, "shadow": segs_sh // args.steps,
+                                  "total": segs // args.steps},
             "gpu_launches": launches,
             "roofline": roofline,
             "clocks": clk}
