@@ -682,7 +682,8 @@ def main():
     barrier()
 
     if pg:
-        (t_dev, t_e2e), (segs, e2e_segs) = reduce_replicas(pg, [t_dev, t_e2e], [segs, e2e_segs], "cuda")
+        (t_dev, t_e2e), (segs, e2e_segs, segs_ext, segs_sh) = reduce_replicas(
+            pg, [t_dev, t_e2e], [segs, e2e_segs, segs_ext, segs_sh], "cuda")
     if rank != 0:
         if pg:
             pg.destroy_process_group()
@@ -734,8 +735,8 @@ def main():
             "e2e": {"value": e2e_segs / t_e2e / 1e6, "unit": "Mrays/s",
                     "h2d_bytes_per_step": args.frames * (ctypes.sizeof(pt.PtPushHead) + ctypes.sizeof(pt.PtPathParams)),
                     "d2h_bytes_per_step": W_FULL * H_FULL * 16},
-            "segments_per_step": {"extension": segs_ext // args.steps, "shadow": segs_sh // args.steps,
-                                  "total": segs // args.steps},
+            "segments_per_step": {"extension": int(segs_ext) // args.steps, "shadow": int(segs_sh) // args.steps,
+                                  "total": int(segs) // args.steps},
             "gpu_launches": launches,
             "roofline": roofline,
             "clocks": clk}
