@@ -1794,8 +1794,8 @@ bool sdf_leaf_box(const SdfNodeH& n, float* mn, float* mx) {
     }
 }
 
-bool sdf_node_box(const SdfClusterH& c, uint32_t i, float* mn, float* mx) {
-    if (i >= c.count) return false;
+bool sdf_node_box(const SdfClusterH& c, uint32_t i, float* mn, float* mx, int depth = 0) {
+    if (i >= c.count || depth > 8) return false;   // a deeper chain than 8 nodes has a cycle
     const SdfNodeH& n = c.nodes[i];
     auto widen = [&](float k) {
         for (int j = 0; j < 3; ++j) { mn[j] -= k; mx[j] += k; }
@@ -1806,14 +1806,57 @@ bool sdf_node_box(const SdfClusterH& c, uint32_t i, float* mn, float* mx) {
         return true;
     }
     float an[3], ax[3], bn[3], bx[3];
-    if (!sdf_node_box(c, n.a, an, ax)) return false;
+    if (!sdf_node_box(c, n.a, an, ax, depth + 1)) return false;
     if (n.op == 4) {   // displace
         for (int j = 0; j < 3; ++j) { mn[j] = an[j]; mx[j] = ax[j]; }
         widen(std::abs(n.params[0]));
         return true;
     }
+    // The procedural ops (bounded on the host in every build, whether or not
+    // the renderer evaluates them): the child's box widened by the noise
+    // band's largest sum, or re-bounded around the warp axis / repetition.
+    if (n.op == 5) {   // displace by fBm noise: |amp| x sum of the octave amplitudes
+        for (int j = 0; j < 3; ++j) { mn[j] = an[j]; mx[j] = ax[j]; }
+        uint32_t oct = 0;
+        std::memcpy(&oct, &n.params[2], 4);
+        oct = std::min(std::max(oct, 1u), 6u);
+        const float sum_scale = 2.0f * (1.0f - std::ldexp(1.0f, -int(oct)));
+        widen(std::abs(n.params[0]) * sum_scale);
+        return true;
+    }
+    if (n.op == 6 || n.op == 7) {   // twist about y / bend about x: a cylinder around the axis
+        const int u = (n.op == 6) ? 0 : 1, w = 2, keep = (n.op == 6) ? 1 : 0;
+        const float ru = std::max(std::abs(an[u]), std::abs(ax[u]));
+        const float rw = std::max(std::abs(an[w]), std::abs(ax[w]));
+        const float r = std::sqrt(ru * ru + rw * rw);
+        mn[u] = -r; mx[u] = r;
+        mn[w] = -r; mx[w] = r;
+        mn[keep] = an[keep]; mx[keep] = ax[keep];
+        return true;
+    }
+    if (n.op == 8 || n.op == 9) {   // repetition: unbounded (1000 m), or the limited cells' span
+        uint32_t packed = 0;
+        std::memcpy(&packed, &n.params[3], 4);
+        const int lim[3] = {int(packed & 0x3FFu), int((packed >> 10) & 0x3FFu), int((packed >> 20) & 0x3FFu)};
+        for (int j = 0; j < 3; ++j) {
+            if (n.params[j] > 1e-6f) {
+                if (n.op == 8) {
+                    mn[j] = -1000.0f;
+                    mx[j] = 1000.0f;
+                } else {
+                    const float span = float(lim[j]) * n.params[j];
+                    mn[j] = an[j] - span;
+                    mx[j] = ax[j] + span;
+                }
+            } else {
+                mn[j] = an[j];
+                mx[j] = ax[j];
+            }
+        }
+        return true;
+    }
     if (n.op > 3) return false;
-    if (!sdf_node_box(c, n.b, bn, bx)) return false;
+    if (!sdf_node_box(c, n.b, bn, bx, depth + 1)) return false;
     if (n.op == 2) {   // subtract: a's box
         for (int j = 0; j < 3; ++j) { mn[j] = an[j]; mx[j] = ax[j]; }
     } else {

@@ -112,6 +112,29 @@ def sdf_fractal_clusters(n, seed):
     return out
 
 
+def sdf_procedural_clusters(n, seed):
+    """A leaf under one procedural op (5 fBm displace, 6 twist, 7 bend,
+    8 repeat, 9 limited repeat) with random parameters; the noise octave count
+    and the repeat limits are packed into the float words as the reference does."""
+    rng = XorShift32(seed)
+    out = []
+    for c in range(n):
+        arr = np.zeros((8, 12), np.float32)
+        arr[0, :4].view(np.uint32)[:] = [0, rng.next() % 5, 0, 0]
+        arr[0, 4:8] = [rng.rangef(0.2, 2.0) for _ in range(4)]
+        arr[0, 8:11] = [rng.rangef(-4, 4) for _ in range(3)]
+        op = 5 + c % 5
+        arr[1, :4].view(np.uint32)[:] = [op, 0, 0, 0]
+        arr[1, 4:8] = [rng.rangef(-0.5, 3.0) for _ in range(4)]
+        if op == 5:
+            arr[1, 6:7].view(np.uint32)[0] = rng.next() % 9
+        if op == 9:
+            arr[1, 7:8].view(np.uint32)[0] = (rng.next() % 1024) | ((rng.next() % 1024) << 10) | \
+                ((rng.next() % 1024) << 20)
+        out.append((arr, 2))
+    return out
+
+
 def main():
     if oracle.load_ref() is None:
         sys.exit("oracle/_ref/libref_builders.so missing: run `make -C oracle ref` first")
@@ -149,6 +172,13 @@ def main():
         boxes.append(np.concatenate([r[0], r[1], [1.0]]) if r else np.array([0, 0, 0, 0, 0, 0, 0], np.float32))
     out.update(sdf_frac_nodes=np.stack([a for a, _ in cl]), sdf_frac_counts=np.array([n for _, n in cl], np.uint32),
                sdf_frac_boxes=np.stack(boxes).astype(np.float32))
+    cl = sdf_procedural_clusters(40, 0x9A0CED)
+    boxes = []
+    for arr, n in cl:
+        r = oracle.ref_sdf_aabb(arr, n)
+        boxes.append(np.concatenate([r[0], r[1], [1.0]]) if r else np.array([0, 0, 0, 0, 0, 0, 0], np.float32))
+    out.update(sdf_proc_nodes=np.stack([a for a, _ in cl]), sdf_proc_counts=np.array([n for _, n in cl], np.uint32),
+               sdf_proc_boxes=np.stack(boxes).astype(np.float32))
     np.savez_compressed(os.path.join(HERE, "reference_builders.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_builders.npz"))
 

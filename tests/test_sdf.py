@@ -33,6 +33,18 @@ def test_sdf_boxes_equal_reference_golden():
             assert np.array_equal(np.concatenate(r), box[:6])
 
 
+def test_sdf_procedural_op_boxes_equal_reference_golden():
+    """Ops 5-9 (fBm displace, twist, bend, repeat, limited repeat): the
+    reference bounds them on the host in every build."""
+    pt = load_pkg()
+    g = np.load(GOLD)
+    for nodes, n, box in zip(g["sdf_proc_nodes"], g["sdf_proc_counts"], g["sdf_proc_boxes"]):
+        r = _box(pt, nodes, int(n))
+        assert (r is not None) == (box[6] == 1.0)
+        if r:
+            assert np.array_equal(np.concatenate(r), box[:6])
+
+
 def test_sdf_boxes_equal_reference_live():
     if orc_mod.load_ref() is None:
         pytest.skip("reference builders not built here")
@@ -49,6 +61,24 @@ def test_sdf_boxes_equal_reference_live():
         nodes[2, 4] = rng.uniform(-0.5, 1)
         want = orc_mod.ref_sdf_aabb(nodes, n)
         got = _box(pt, nodes, n)
+        assert (want is None) == (got is None)
+        if want:
+            assert np.array_equal(np.concatenate(got), np.concatenate(want))
+    for _ in range(300):   # a procedural op (5..9) over a leaf
+        nodes = np.zeros((8, 12), np.float32)
+        nodes[0, :4].view(np.uint32)[:] = [0, rng.integers(0, 5), 0, 0]
+        nodes[0, 4:8] = rng.uniform(0.1, 2, 4)
+        nodes[0, 8:11] = rng.uniform(-4, 4, 3)
+        op = int(rng.integers(5, 10))
+        nodes[1, :4].view(np.uint32)[:] = [op, 0, 0, 0]
+        nodes[1, 4:8] = rng.uniform(-0.5, 3, 4)
+        if op == 5:
+            nodes[1, 6:7].view(np.uint32)[0] = rng.integers(0, 9)
+        if op == 9:
+            nodes[1, 7:8].view(np.uint32)[0] = (int(rng.integers(0, 1024)) | (int(rng.integers(0, 1024)) << 10)
+                                                | (int(rng.integers(0, 1024)) << 20))
+        want = orc_mod.ref_sdf_aabb(nodes, 2)
+        got = _box(pt, nodes, 2)
         assert (want is None) == (got is None)
         if want:
             assert np.array_equal(np.concatenate(got), np.concatenate(want))
