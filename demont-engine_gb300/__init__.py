@@ -45,7 +45,7 @@ class PtPathParams(ctypes.Structure):
     _fields_ = [("refract_budget", f32), ("firefly_clamp", f32), ("mis_enabled", u32),
                 ("accum_ema_alpha", f32), ("bvh_params", u32 * 4), ("light_count", u32),
                 ("light_tree_enabled", u32), ("light_tree_node_count", u32), ("rr_start", u32),
-                ("sun_and_mode", f32 * 4), ("stars", u32), ("reserved", u32 * 3),
+                ("sun_and_mode", f32 * 4), ("stars", u32), ("sdf_procedural_ops", u32), ("reserved", u32 * 2),
                 ("moon_dir_phase", f32 * 4), ("moon_extra", f32 * 4), ("sun_extra", f32 * 4),
                 ("sun_extra2", f32 * 4), ("sdf_params", u32 * 4), ("sdf_params_f", f32 * 4)]
 
@@ -195,6 +195,7 @@ SIGNATURES = {
                                   ctypes.c_void_p]),
     "pt_scene_sdf_leaf": (ctypes.c_int, [ctypes.c_void_p, u32, u32, P(f32), f32, f32, f32, u32, f32, f32, f32]),
     "pt_scene_sdf_combine": (ctypes.c_int, [ctypes.c_void_p, u32, u32, u32, u32, f32, u32, f32, f32, f32]),
+    "pt_scene_sdf_wrap": (ctypes.c_int, [ctypes.c_void_p, u32, u32, u32, P(f32), u32, f32, f32, f32]),
     "pt_scene_sdf_remove": (ctypes.c_int, [ctypes.c_void_p, u32]),
     "pt_scene_sdf_clear": (ctypes.c_int, [ctypes.c_void_p]),
     "pt_sdf_cluster_box": (ctypes.c_int, [P(f32), u32, P(f32), P(f32)]),
@@ -372,6 +373,12 @@ class Scene:
     def sdf_combine(self, id, a, b, op, k, mat, rgb):
         """op 1 smooth union, 2 smooth subtract (b from a), 3 smooth intersect."""
         self._check(self.lib.pt_scene_sdf_combine(self.h, id, a, b, op, k, mat, *rgb))
+
+    def sdf_wrap(self, id, child, op, params, mat, rgb):
+        """op 5 fBm displace (amp, freq[, octaves]), 6 twist / 7 bend (rate), 8 repeat
+        (px, py, pz), 9 limited repeat (px, py, pz, lx, ly, lz); the child is consumed."""
+        q = (f32 * 6)(*(list(params) + [0.0] * (6 - len(params))))
+        self._check(self.lib.pt_scene_sdf_wrap(self.h, id, child, op, q, mat, *rgb))
 
     def camera(self, pos, yaw, pitch, fov_deg):
         self._check(self.lib.pt_scene_set_camera(self.h, *pos, yaw, pitch, fov_deg))

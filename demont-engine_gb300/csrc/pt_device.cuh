@@ -285,6 +285,7 @@ struct DScene {
     float sdf_eps;
     uint32_t frac_iters;         // fractal leaves: DE iterations, default power, epsilon growth per step
     float frac_power, frac_eps_scale;
+    uint32_t sdf_proc;           // 1: evaluate the procedural ops 5-9 (else they read as empty)
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs
@@ -533,7 +534,158 @@ __device__ V3 sdf_normal(const float4* C, uint32_t count, V3 p) {
     return count > 0u ? g[count - 1u] : v3(0.0f, 1.0f, 0.0f);
 }
 
-// sdfClusterTrace: clip to the cluster box, then sphere-trace
+// ---- procedural ops 5-9 (shaders/SdfPrimitives.slang:504-1245): the
+// reference's PT_SDF_PROCEDURAL_OPS=1 build without PT_SDF_AUTODIFF, so the
+// normal of a procedural cluster is the 6-tap central difference ----
+__device__ __forceinline__ uint32_t sdf_hash32(uint32_t x) {   // sdfHash32 (lowbias32 mixing)
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float sdf_hash3(uint32_t x, uint32_t y, uint32_t z) {   // sdfHash3, in [0, 1)
+    uint32_t h = sdf_hash32(x);
+    h = sdf_hash32(h ^ y);
+    h = sdf_hash32(h ^ z);
+    return __uint2float_rn(h) * (1.0f / 4294967296.0f);
+}
+// lattice cell of an integral float, as a two's-complement word (saturated to int range)
+__device__ __forceinline__ uint32_t sdf_cell(float x) {
+    return uint32_t(int(fminf(fmaxf(x, -2147483648.0f), 2147483520.0f)));
+}
+// sdfValueNoise3 (value only): quintic-smoothstep trilinear mix of hashed lattice values
+__device__ float sdf_value_noise(V3 p) {
+    const V3 ip = v3(floorf(p.x), floorf(p.y), floorf(p.z));
+    const V3 f = p - ip;
+    const uint32_t ix = sdf_cell(ip.x), iy = sdf_cell(ip.y), iz = sdf_cell(ip.z);
+    const V3 u = f * f * f * (f * (f * 6.0f - v3(15.0f, 15.0f, 15.0f)) + v3(10.0f, 10.0f, 10.0f));
+    const float n000 = sdf_hash3(ix, iy, iz), n100 = sdf_hash3(ix + 1u, iy, iz);
+    const float n010 = sdf_hash3(ix, iy + 1u, iz), n110 = sdf_hash3(ix + 1u, iy + 1u, iz);
+    const float n001 = sdf_hash3(ix, iy, iz + 1u), n101 = sdf_hash3(ix + 1u, iy, iz + 1u);
+    const float n011 = sdf_hash3(ix, iy + 1u, iz + 1u), n111 = sdf_hash3(ix + 1u, iy + 1u, iz + 1u);
+    const float k0 = n000, k1 = n100 - n000, k2 = n010 - n000, k3 = n001 - n000;
+    const float k4 = n000 - n100 - n010 + n110;
+    const float k5 = n000 - n010 - n001 + n011;
+    const float k6 = n000 - n100 - n001 + n101;
+    const float k7 = -n000 + n100 + n010 + n001 - n110 - n011 - n101 + n111;
+    return k0 + k1 * u.x + k2 * u.y + k3 * u.z + k4 * u.x * u.y + k5 * u.y * u.z + k6 * u.z * u.x +
+           k7 * u.x * u.y * u.z;
+}
+// sdfFbm3 (value only): at most 6 octaves, each re-centred to [-1, 1]
+__device__ float sdf_fbm(V3 p, uint32_t octaves) {
+    float v = 0.0f, amp = 1.0f, frq = 1.0f;
+    const uint32_t o = min(octaves, 6u);
+    for (uint32_t i = 0; i < o; ++i) {
+        const float vn = sdf_value_noise(p * frq);
+        v += amp * (2.0f * vn - 1.0f);
+        amp *= 0.5f;
+        frq *= 2.0f;
+    }
+    return v;
+}
+// sdfClusterDistProcN: the phase-1 walker over nodes [0, nc) plus the fBm
+// displacement band; a warp below the root reads as empty (1e30)
+__device__ float sdf_dist_proc(const float4* C, uint32_t nc, V3 p) {
+    float d[kSdfMaxNodes];
+    for (uint32_t i = 0; i < kSdfMaxNodes; ++i) {
+        if (i >= nc) break;
+        const SdfNodeD n = sdf_node(C, i);
+        float v;
+        if (n.op == 0u) {
+            v = sd_leaf(p - n.c, n.shape, n.q);
+        } else if (n.op >= 1u && n.op <= 5u) {
+            const float da = d[min(n.a, i - 1u)], db = d[min(n.b, i - 1u)], k = n.q.x;
+            if (n.op == 1u) {
+                if (k <= 0.0f) v = fminf(da, db);
+                else {
+                    const float h = clampf(0.5f + 0.5f * (db - da) / k, 0.0f, 1.0f);
+                    v = lerpf_(db, da, h) - k * h * (1.0f - h);
+                }
+            } else if (n.op == 2u) {
+                if (k <= 0.0f) v = fmaxf(da, -db);
+                else {
+                    const float h = clampf(0.5f - 0.5f * (db + da) / k, 0.0f, 1.0f);
+                    v = lerpf_(da, -db, h) + k * h * (1.0f - h);
+                }
+            } else if (n.op == 3u) {
+                if (k <= 0.0f) v = fmaxf(da, db);
+                else {
+                    const float h = clampf(0.5f - 0.5f * (db - da) / k, 0.0f, 1.0f);
+                    v = lerpf_(db, da, h) + k * h * (1.0f - h);
+                }
+            } else if (n.op == 4u) {
+                v = da + k;
+            } else {   // displace by amp x fBm(freq p), octaves as the bits of params.z
+                v = da + k * sdf_fbm(p * n.q.y, __float_as_uint(n.q.z));
+            }
+        } else {
+            v = 1e30f;
+        }
+        d[i] = v;
+    }
+    return nc > 0u ? d[nc - 1u] : 1e30f;
+}
+// sdfClusterDistWarped: a warp at the root moves the point once, then the
+// child sub-tree [0, child + 1) is walked; twist and bend halve the distance.
+// One walker call for every branch (x 1.0 leaves a distance unchanged).
+__device__ float sdf_dist_warped(const float4* C, uint32_t count, V3 p) {
+    const SdfNodeD r = sdf_node(C, count > 0u ? count - 1u : 0u);
+    V3 q = p;
+    uint32_t nc = count;
+    float scale = 1.0f;
+    if (r.op == 6u) {   // twist about the world y axis
+        const float c = f_cos(r.q.x * p.y), s = f_sin(r.q.x * p.y);
+        q = v3(c * p.x - s * p.z, p.y, s * p.x + c * p.z);
+        scale = 0.5f;
+    } else if (r.op == 7u) {   // bend about the world x axis
+        const float c = f_cos(r.q.x * p.x), s = f_sin(r.q.x * p.x);
+        q = v3(p.x, c * p.y - s * p.z, s * p.y + c * p.z);
+        scale = 0.5f;
+    } else if (r.op == 8u || r.op == 9u) {   // repetition, unbounded or clamped to +-limit cells
+        const uint32_t pk = __float_as_uint(r.q.w);
+        const float per[3] = {r.q.x, r.q.y, r.q.z};
+        const float lim[3] = {float(pk & 0x3FFu), float((pk >> 10) & 0x3FFu), float((pk >> 20) & 0x3FFu)};
+        float w[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            if (per[j] > 1e-6f) {
+                float idx = roundf(w[j] / per[j]);
+                if (r.op == 9u) idx = clampf(idx, -lim[j], lim[j]);
+                w[j] = w[j] - per[j] * idx;
+            }
+        }
+        q = v3(w[0], w[1], w[2]);
+    }
+    if (r.op >= 6u && r.op <= 9u) nc = min(r.a + 1u, kSdfMaxNodes);
+    return scale * sdf_dist_proc(C, nc, q);
+}
+// sdfClusterHasProcedural
+__device__ __forceinline__ bool sdf_has_proc(const float4* C, uint32_t count) {
+    for (uint32_t i = 0; i < kSdfMaxNodes; ++i) {
+        if (i >= count) break;
+        const uint32_t op = __float_as_uint(__ldg(C + 4u + 3u * i).x);
+        if (op >= 5u && op <= 9u) return true;
+    }
+    return false;
+}
+// sdfClusterNormalCentral: 6-tap central differences of step h (the taps in
+// a loop, so that the walker is compiled once)
+__device__ V3 sdf_normal_central(const float4* C, uint32_t count, V3 p, float h) {
+    float d[6];
+#pragma unroll 1
+    for (int k = 0; k < 6; ++k) {
+        const V3 e = v3(k < 2 ? h : 0.0f, (k >> 1) == 1 ? h : 0.0f, k >= 4 ? h : 0.0f);   // axis k / 2
+        d[k] = sdf_dist_warped(C, count, (k & 1) ? p - e : p + e);
+    }
+    const V3 g = v3(d[0] - d[1], d[2] - d[3], d[4] - d[5]);
+    const float l = length(g);
+    return l > 1e-12f ? g / l : v3(0.0f, 1.0f, 0.0f);
+}
+
+// (Proc: the procedural walker, for clusters holding ops 5-9 when they are enabled)
+template <bool Proc>
 __device__ bool sdf_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float t_min, float t_max, float& out_t) {
     const float4 h0 = __ldg(C), h1 = __ldg(C + 1);
     const uint32_t count = __float_as_uint(h0.w);
@@ -549,7 +701,7 @@ __device__ bool sdf_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float 
     const uint32_t iters = min(S.sdf_iters, 256u);
     for (uint32_t i = 0; i < iters; ++i) {
         const V3 p = ro + rd * t;
-        const float ad = fabsf(sdf_dist(C, count, p));
+        const float ad = fabsf(Proc ? sdf_dist_warped(C, count, p) : sdf_dist(C, count, p));
         if (ad < S.sdf_eps) {
             out_t = t;
             return true;
@@ -558,6 +710,11 @@ __device__ bool sdf_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float 
         if (t >= t_end) return false;
     }
     return false;
+}
+
+__device__ __forceinline__ bool sdf_trace_proc(const DScene& S, const float4* C, V3 ro, V3 rd, float t_min,
+                                               float t_max, float& out_t) {
+    return sdf_trace<true>(S, C, ro, rd, t_min, t_max, out_t);
 }
 
 // ---- fractal leaves (shaders/SdfFractals.slang): distance estimators ----
@@ -684,7 +841,10 @@ __device__ __forceinline__ void trace_sdf(const DScene& S, V3 ro, V3 rd, float& 
                 best_t = t;
                 best_id = kSdfBit | (step << 20) | i;
             }
-        } else if (sdf_trace(S, C, ro, rd, 1e-3f, best_t, t) && t < best_t) {
+        } else if ((S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(__ldg(C).w))
+                        ? sdf_trace_proc(S, C, ro, rd, 1e-3f, best_t, t)
+                        : sdf_trace<false>(S, C, ro, rd, 1e-3f, best_t, t)) &&
+                   t < best_t) {
             best_t = t;
             best_id = kSdfBit | i;
         }
@@ -1067,6 +1227,8 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
             const float eps_i = S.sdf_eps * (1.0f + S.frac_eps_scale * float((h.id >> 20) & 0x1FFu));
             const float hh = fmaxf(eps_i * 8.0f, S.sdf_eps * 4.0f);
             s.normal = fractal_normal((ro + rd * h.t) - n.c, n.shape, n.q, S.frac_power, S.frac_iters, hh);
+        } else if (S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(h0.w))) {
+            s.normal = sdf_normal_central(C, __float_as_uint(h0.w), ro + rd * h.t, S.sdf_eps);
         } else {
             s.normal = normalize(sdf_normal(C, __float_as_uint(h0.w), ro + rd * h.t));
         }

@@ -475,6 +475,7 @@ struct pt_scene {
         {"r_sdf_max_iters", 128},    {"r_sdf_epsilon", 1e-4},
         {"r_sdf_fractal_power", 8},  {"r_sdf_fractal_iters", 12},
         {"r_sdf_de_eps_scale", 1},   {"r_sdf_normal_mode", 0},
+        {"r_sdf_displace_octaves", 4}, {"r_sdf_procedural_ops", 0},
         {"r_capture_seed", 0},
         {"app_window_width", 0},     {"app_window_height", 0},
     };
@@ -1661,6 +1662,7 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
         params->sdf_params_f[1] = power;
         params->sdf_params_f[2] = de_sc;
         params->sdf_params_f[3] = float(nm);
+        params->sdf_procedural_ops = s->cvar("r_sdf_procedural_ops") != 0.0 ? 1u : 0u;
     }
     return PT_OK;
 }
@@ -1948,6 +1950,57 @@ int pt_scene_sdf_combine(pt_scene* s, uint32_t id, uint32_t a, uint32_t b, uint3
     if (!sdf_box(c)) return fail(s, "sdf: bounding box failed");
     s->sdf.erase(a);
     s->sdf.erase(b);
+    s->sdf[id] = c;
+    return PT_OK;
+}
+
+int pt_scene_sdf_wrap(pt_scene* s, uint32_t id, uint32_t child, uint32_t op, const float* params,
+                      uint32_t material, float r, float g, float b) {
+    if (!s || !params) return PT_ERR_INVALID;
+    if (op < 5u || op > 9u) return fail(s, "sdf: wrap op must be 5 (noise), 6 (twist), 7 (bend), 8 or 9 (repeat)");
+    if (material > 2u) return fail(s, "sdf: material must be 0, 1 or 2");
+    auto ia = s->sdf.find(child);
+    if (ia == s->sdf.end()) return fail(s, "sdf: child cluster not found");
+    const SdfClusterH A = ia->second;
+    float q[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (op == 5u) {   // amp, freq, octaves (clamped 1..6, stored as the bits of params[2])
+        if (!(params[0] > 0.0f) || !(params[1] > 0.0f)) return fail(s, "sdf_displace_noise: amp and freq must be > 0");
+        const float oct = std::min(std::max(params[2], 1.0f), 6.0f);
+        const uint32_t ou = uint32_t(int(oct));
+        q[0] = params[0];
+        q[1] = params[1];
+        std::memcpy(&q[2], &ou, 4);
+    } else if (op == 6u || op == 7u) {
+        q[0] = params[0];
+    } else {
+        for (int k = 0; k < 3; ++k) q[k] = params[k];
+        if (op == 9u) {   // half-extents in 10-bit lanes of params[3]
+            uint32_t pk = 0;
+            for (int k = 0; k < 3; ++k) {
+                const float l = params[3 + k];
+                if (!(l >= 0.0f && l <= 1023.0f) || l != std::floor(l))
+                    return fail(s, "sdf_repeat_limited: limits must be integers in 0..1023");
+                pk |= (uint32_t(l) & 0x3FFu) << (10 * k);
+            }
+            std::memcpy(&q[3], &pk, 4);
+        }
+    }
+    if (op >= 6u)
+        for (uint32_t i = 0; i < A.count; ++i)
+            if (A.nodes[i].op >= 6u && A.nodes[i].op <= 9u)
+                return fail(s, "sdf: the child already contains a warp (a warp applies only at the cluster root)");
+    if (A.count + 1u > 8u) return fail(s, "sdf: more than 8 nodes");
+    SdfClusterH c{};
+    for (uint32_t i = 0; i < A.count; ++i) c.nodes[i] = A.nodes[i];
+    SdfNodeH& o = c.nodes[A.count];
+    o.op = op;
+    o.a = A.count - 1u;
+    for (int k = 0; k < 4; ++k) o.params[k] = q[k];
+    c.count = A.count + 1u;
+    c.material = material;
+    c.albedo[0] = r; c.albedo[1] = g; c.albedo[2] = b;
+    if (!sdf_box(c)) return fail(s, "sdf: bounding box failed");
+    s->sdf.erase(child);
     s->sdf[id] = c;
     return PT_OK;
 }
@@ -2322,8 +2375,27 @@ int pt_scene_exec_cfg(pt_scene* s, const char* text, const char* base_dir, char*
             const float prm4[4] = {f[0], f[1], 0.0f, 0.0f};
             if (pt_scene_sdf_leaf(s, id, shape, prm4, f[2], f[3], f[4], uint32_t(m), rgb[0], rgb[1], rgb[2]))
                 bad(line, s->err);
+        } else if (cmd == "sdf_displace_noise" || cmd == "sdf_twist" || cmd == "sdf_bend" || cmd == "sdf_repeat" ||
+                   cmd == "sdf_repeat_limited") {
+            // <id> <child> <op args> <material> <r g b>; displace_noise's octaves are
+            // optional (default r_sdf_displace_octaves)
+            const uint32_t op = cmd == "sdf_displace_noise" ? 5u : cmd == "sdf_twist" ? 6u : cmd == "sdf_bend" ? 7u
+                              : cmd == "sdf_repeat" ? 8u : 9u;
+            const size_t nop = op == 5u ? (na == 9 ? 3 : 2) : op <= 7u ? 1 : op == 8u ? 3 : 6;
+            const size_t want = 2 + nop + 4;
+            uint32_t child = 0;
+            const int m = na == want ? to_mat(tok[3 + nop]) : -1;
+            if (na != want || !U(1, id) || !U(2, child) || !floats(3, nop) || m < 0) {
+                bad(line, "malformed arguments");
+                continue;
+            }
+            float prm[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
+            if (op == 5u && nop == 2) prm[2] = float(s->cvar("r_sdf_displace_octaves"));
+            float rgb[3];
+            if (!F(want - 2, rgb[0]) || !F(want - 1, rgb[1]) || !F(want, rgb[2])) { bad(line, "bad colour"); continue; }
+            if (pt_scene_sdf_wrap(s, id, child, op, prm, uint32_t(m), rgb[0], rgb[1], rgb[2])) bad(line, s->err);
         } else if (cmd.rfind("sdf_", 0) == 0) {
-            skip(line, "procedural SDF ops: compiled out of the reference's default build");
+            skip(line, "SDF command outside the path");
         } else if (cmd == "cam_pos") {
             if (na != 3 || !floats(1, 3)) { bad(line, "want x y z"); continue; }
             std::memcpy(s->cam_pos, f, 12);

@@ -80,7 +80,11 @@ typedef struct PtPathParams {
     float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 1 env map, 2 procedural,
                                        3 Hosek-Wilkie, not built) */
     uint32_t stars;                 /* exposure_pad.y/z: procedural-sky stars (must be 0: not built) */
-    uint32_t reserved[3];
+    uint32_t sdf_procedural_ops;    /* 1: SDF ops 5-9 (fBm displace, twist, bend, repeat, limited repeat)
+                                       are evaluated, with central-difference normals, as in the reference
+                                       built with PT_SDF_PROCEDURAL_OPS=1 (shaders/SdfPrimitives.slang:56-58,
+                                       504-1245); 0: they read as empty, as in its default build */
+    uint32_t reserved[2];
     /* gradient sky (no env map): the moon and the sun-disc shape
        (shaders/PathTrace.slang:766, 1222-1241; engine fill src/engine/Engine.cpp:8324-8410) */
     float    moon_dir_phase[4];     /* moon dir xyz (y < -0.1: hidden), phase angle in w */

@@ -97,7 +97,8 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
  * r_sun_azimuth 135 (degrees), r_sun_size 1, r_sun_disc_brightness 1, r_sun_horizon_flatten 1,
  * r_moon_size 1, r_moon_disc_brightness 0.7; output step: r_exposure 1.5, r_tonemap_op 0 (aces);
  * SDF: r_sdf_max_iters 128, r_sdf_epsilon 1e-4, r_sdf_fractal_power 8, r_sdf_fractal_iters 12,
- * r_sdf_de_eps_scale 1, r_sdf_normal_mode 0.
+ * r_sdf_de_eps_scale 1, r_sdf_normal_mode 0, r_sdf_displace_octaves 4; r_sdf_procedural_ops 0
+ * stands in for the reference's PT_SDF_PROCEDURAL_OPS build flag (1: ops 5-9 are evaluated).
  * Returns PT_ERR_INVALID for unknown names. */
 int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
 int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);
@@ -162,7 +163,8 @@ int pt_scene_upload(pt_scene* s, pt_gpu_ctx* ctx);
  *   cam_pos <x y z>, cam_yaw <deg>, cam_pitch <deg>, cam_fov <deg>
  *   r_sky_mode <gradient|hdri|procedural|hosek>, r_env_map <path.hdr> (relative to base_dir),
  *   sdf_sphere|box|round_box|torus|capsule, sdf_mandelbulb|mandelbox|apollonian,
- *   sdf_smin|sdf_smax|sdf_sdiff, sdf_remove, sdf_clear
+ *   sdf_smin|sdf_smax|sdf_sdiff, sdf_displace_noise|sdf_twist|sdf_bend|sdf_repeat|
+ *   sdf_repeat_limited, sdf_remove, sdf_clear
  *   (argument orders as the reference's commands),
  *   r_denoiser <off|...>, and every numeric cvar of pt_scene_set_cvar (incl. app_window_width/height,
  *   r_capture_seed, r_show_stars).
@@ -197,6 +199,17 @@ int pt_scene_sdf_leaf(pt_scene* s, uint32_t id, uint32_t shape, const float para
                       float z, uint32_t material, float r, float g, float b);
 int pt_scene_sdf_combine(pt_scene* s, uint32_t id, uint32_t a, uint32_t b, uint32_t op, float k,
                          uint32_t material, float r, float g, float bl);
+/* A wrapped cluster (the reference's sdf_displace_noise / sdf_twist / sdf_bend /
+ * sdf_repeat / sdf_repeat_limited, src/engine/Engine.cpp:19095-19400): one op node
+ * over the child cluster, which is consumed.  op 5 fBm displace (amp > 0, freq > 0,
+ * octaves clamped to 1..6), 6 twist about y (rate rad/m), 7 bend about x (rate rad/m),
+ * 8 repetition (periods px py pz; 0 = none on that axis), 9 limited repetition
+ * (periods, then integer half-extents 0..1023 per axis).  params: op 5 {amp, freq,
+ * octaves}, 6/7 {rate}, 8 {px, py, pz}, 9 {px, py, pz, lx, ly, lz}.  A warp (6-9)
+ * over a child that already holds one is refused, as in the reference.  The
+ * renderer evaluates these ops only when PtPathParams.sdf_procedural_ops is set. */
+int pt_scene_sdf_wrap(pt_scene* s, uint32_t id, uint32_t child, uint32_t op, const float* params,
+                      uint32_t material, float r, float g, float b);
 int pt_scene_sdf_remove(pt_scene* s, uint32_t id);
 int pt_scene_sdf_clear(pt_scene* s);
 /* Bounding box of `count` nodes in the reference's SdfNode layout (12 words

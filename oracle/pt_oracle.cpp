@@ -554,6 +554,147 @@ template <class R> struct Tracer {
         if (grad) *grad = count > 0u ? g[count - 1u] : V3<R>{R(0), R(1), R(0)};
         return count > 0u ? d[count - 1u] : R(1e30);
     }
+    // ---- procedural ops 5-9 (SdfPrimitives.slang:504-1245; the reference
+    // built with PT_SDF_PROCEDURAL_OPS=1 and without PT_SDF_AUTODIFF) ----
+    static uint32_t sdf_hash32(uint32_t x) {   // sdfHash32
+        x ^= x >> 16;
+        x *= 0x7feb352du;
+        x ^= x >> 15;
+        x *= 0x846ca68bu;
+        x ^= x >> 16;
+        return x;
+    }
+    static R sdf_hash3(uint32_t x, uint32_t y, uint32_t z) {   // sdfHash3: h / 2^32
+        uint32_t h = sdf_hash32(x);
+        h = sdf_hash32(h ^ y);
+        h = sdf_hash32(h ^ z);
+        return R(float(h)) * R(1.0f / 4294967296.0f);
+    }
+    static uint32_t sdf_cell(R x) {   // int3(floor(p)) as a two's-complement word
+        const R c = mn(mx(x, R(-2147483648.0)), R(2147483520.0));
+        return uint32_t(int32_t(c));
+    }
+    static R sdf_value_noise(V3<R> p) {   // sdfValueNoise3, value only
+        const V3<R> ip{std::floor(p.x), std::floor(p.y), std::floor(p.z)};
+        const V3<R> f = p - ip;
+        const uint32_t ix = sdf_cell(ip.x), iy = sdf_cell(ip.y), iz = sdf_cell(ip.z);
+        const V3<R> c15{R(15), R(15), R(15)}, c10{R(10), R(10), R(10)};
+        const V3<R> u = f * f * f * (f * (f * R(6) - c15) + c10);
+        const R n000 = sdf_hash3(ix, iy, iz), n100 = sdf_hash3(ix + 1u, iy, iz);
+        const R n010 = sdf_hash3(ix, iy + 1u, iz), n110 = sdf_hash3(ix + 1u, iy + 1u, iz);
+        const R n001 = sdf_hash3(ix, iy, iz + 1u), n101 = sdf_hash3(ix + 1u, iy, iz + 1u);
+        const R n011 = sdf_hash3(ix, iy + 1u, iz + 1u), n111 = sdf_hash3(ix + 1u, iy + 1u, iz + 1u);
+        const R k0 = n000, k1 = n100 - n000, k2 = n010 - n000, k3 = n001 - n000;
+        const R k4 = n000 - n100 - n010 + n110;
+        const R k5 = n000 - n010 - n001 + n011;
+        const R k6 = n000 - n100 - n001 + n101;
+        const R k7 = -n000 + n100 + n010 + n001 - n110 - n011 - n101 + n111;
+        return k0 + k1 * u.x + k2 * u.y + k3 * u.z + k4 * u.x * u.y + k5 * u.y * u.z + k6 * u.z * u.x +
+               k7 * u.x * u.y * u.z;
+    }
+    static R sdf_fbm(V3<R> p, uint32_t octaves) {   // sdfFbm3, value only
+        R v = R(0), amp = R(1), frq = R(1);
+        const uint32_t o = std::min(octaves, 6u);
+        for (uint32_t i = 0; i < o; ++i) {
+            const R vn = sdf_value_noise(p * frq);
+            v += amp * (R(2) * vn - R(1));
+            amp *= R(0.5);
+            frq *= R(2);
+        }
+        return v;
+    }
+    // sdfClusterDistProcN: nodes [0, nc), with the noise band; warps below the root read as 1e30
+    R sdf_dist_proc(const float* C, uint32_t nc, V3<R> p) const {
+        R d[8];
+        for (uint32_t i = 0; i < 8 && i < nc; ++i) {
+            const SdfN n = sdf_node(C, i);
+            R v;
+            if (n.op == 0u) {
+                v = sd_leaf(p - n.c, n.shape, n.q);
+            } else if (n.op >= 1u && n.op <= 5u) {
+                const R da = d[n.a], db = d[n.b], k = n.q[0];
+                if (n.op == 1u) {
+                    if (k <= R(0)) v = mn(da, db);
+                    else {
+                        const R h = clampv(R(0.5) + R(0.5) * (db - da) / k, R(0), R(1));
+                        v = lerp(db, da, h) - k * h * (R(1) - h);
+                    }
+                } else if (n.op == 2u) {
+                    if (k <= R(0)) v = mx(da, -db);
+                    else {
+                        const R h = clampv(R(0.5) - R(0.5) * (db + da) / k, R(0), R(1));
+                        v = lerp(da, -db, h) + k * h * (R(1) - h);
+                    }
+                } else if (n.op == 3u) {
+                    if (k <= R(0)) v = mx(da, db);
+                    else {
+                        const R h = clampv(R(0.5) - R(0.5) * (db - da) / k, R(0), R(1));
+                        v = lerp(db, da, h) + k * h * (R(1) - h);
+                    }
+                } else if (n.op == 4u) {
+                    v = da + k;
+                } else {   // sdfDisplaceNoiseBand: amp x fBm(freq p), octaves as the bits of params[2]
+                    float oct_f = float(n.q[2]);
+                    uint32_t oct = 0;
+                    std::memcpy(&oct, &oct_f, 4);
+                    v = da + k * sdf_fbm(p * n.q[1], oct);
+                }
+            } else {
+                v = R(1e30);
+            }
+            d[i] = v;
+        }
+        return nc > 0u ? d[std::min(nc, 8u) - 1u] : R(1e30);
+    }
+    // sdfClusterDistWarped: a root warp moves the point once; twist/bend halve the distance
+    R sdf_dist_warped(const float* C, uint32_t count, V3<R> p) const {
+        const SdfN r = sdf_node(C, count > 0u ? count - 1u : 0u);
+        const uint32_t nc = std::min(r.a + 1u, 8u);
+        if (r.op == 6u) {
+            const R c = M<R>::cos(r.q[0] * p.y), s = M<R>::sin(r.q[0] * p.y);
+            return R(0.5) * sdf_dist_proc(C, nc, V3<R>{c * p.x - s * p.z, p.y, s * p.x + c * p.z});
+        }
+        if (r.op == 7u) {
+            const R c = M<R>::cos(r.q[0] * p.x), s = M<R>::sin(r.q[0] * p.x);
+            return R(0.5) * sdf_dist_proc(C, nc, V3<R>{p.x, c * p.y - s * p.z, s * p.y + c * p.z});
+        }
+        if (r.op == 8u || r.op == 9u) {
+            float pk_f = float(r.q[3]);
+            uint32_t pk = 0;
+            std::memcpy(&pk, &pk_f, 4);
+            const R lim[3] = {R(pk & 0x3FFu), R((pk >> 10) & 0x3FFu), R((pk >> 20) & 0x3FFu)};
+            R q[3] = {p.x, p.y, p.z};
+            for (int j = 0; j < 3; ++j) {
+                const R per = r.q[j];
+                if (per > R(1e-6f)) {
+                    R idx = std::round(q[j] / per);
+                    if (r.op == 9u) idx = clampv(idx, -lim[j], lim[j]);
+                    q[j] = q[j] - per * idx;
+                }
+            }
+            return sdf_dist_proc(C, nc, V3<R>{q[0], q[1], q[2]});
+        }
+        return sdf_dist_proc(C, count, p);
+    }
+    static bool sdf_has_proc(const float* C, uint32_t count) {   // sdfClusterHasProcedural
+        for (uint32_t i = 0; i < count && i < 8; ++i) {
+            const uint32_t op = u_at(C + 16 + 12 * i);
+            if (op >= 5u && op <= 9u) return true;
+        }
+        return false;
+    }
+    // sdfClusterNormalCentral: 6-tap central differences of step h
+    V3<R> sdf_normal_central(const float* C, uint32_t count, V3<R> p, R h) const {
+        const R dxp = sdf_dist_warped(C, count, p + V3<R>{h, R(0), R(0)});
+        const R dxn = sdf_dist_warped(C, count, p - V3<R>{h, R(0), R(0)});
+        const R dyp = sdf_dist_warped(C, count, p + V3<R>{R(0), h, R(0)});
+        const R dyn = sdf_dist_warped(C, count, p - V3<R>{R(0), h, R(0)});
+        const R dzp = sdf_dist_warped(C, count, p + V3<R>{R(0), R(0), h});
+        const R dzn = sdf_dist_warped(C, count, p - V3<R>{R(0), R(0), h});
+        const V3<R> g{dxp - dxn, dyp - dyn, dzp - dzn};
+        const R l = length(g);
+        return l > R(1e-12) ? g / l : V3<R>{R(0), R(1), R(0)};
+    }
     bool sdf_trace(const float* C, V3<R> ro, V3<R> rd, R t_min, R t_max, R& out_t) const {
         const uint32_t count = u_at(C + 3);
         auto safe = [](R x) { return std::fabs(x) > R(1e-30) ? x : R(1e-30); };
@@ -564,11 +705,12 @@ template <class R> struct Tracer {
         R t = mx(enter, t_min);
         const R t_end = mn(exit, t_max);
         if (t >= t_end) return false;
+        const bool proc = Q.sdf_procedural_ops != 0u && sdf_has_proc(C, count);
         const uint32_t iters = std::min(Q.sdf_params[1], 256u);
         const R eps = R(Q.sdf_params_f[0]);
         for (uint32_t i = 0; i < iters; ++i) {
             const V3<R> p = ro + rd * t;
-            const R ad = std::fabs(sdf_dist(C, count, p, nullptr));
+            const R ad = std::fabs(proc ? sdf_dist_warped(C, count, p) : sdf_dist(C, count, p, nullptr));
             if (ad < eps) {
                 out_t = t;
                 return true;
@@ -706,11 +848,16 @@ template <class R> struct Tracer {
                 continue;
             }
             if (sdf_trace(C, ro, rd, R(1e-3), h.t, t) && t < h.t) {
-                V3<R> g;
-                sdf_dist(C, u_at(C + 3), ro + rd * t, &g);
+                const uint32_t count = u_at(C + 3);
                 h.hit = true;
+                if (Q.sdf_procedural_ops != 0u && sdf_has_proc(C, count)) {
+                    h.normal = sdf_normal_central(C, count, ro + rd * t, R(Q.sdf_params_f[0]));
+                } else {
+                    V3<R> g;
+                    sdf_dist(C, count, ro + rd * t, &g);
+                    h.normal = normalize(g);
+                }
                 h.t = t;
-                h.normal = normalize(g);
                 h.mat = u_at(C + 7);
                 h.albedo = ld3<R>(C + 8);
                 h.roughness = R(C[11]);

@@ -95,9 +95,10 @@ sdf_torus 4 1.2 0.3 -2 1 0 dielectric 1 1 1
 sdf_capsule 5 0.7 0.25 2 1 -1 lambert 0.3 0.9 0.3
 sdf_round_box 6 0.4 0.4 0.4 0.1 0 3 0 metal 0.9 0.9 0.2
 sdf_sdiff 7 6 5 0.05 lambert 0.4 0.4 0.4
-sdf_twist 8 4 0.5
+sdf_twist 8 4 0.5 dielectric 1 1 1
+sdf_displace_noise 9 3 0.05 2 lambert 0.5 0.6 0.7
 """)
-    assert n == 1 and "sdf_twist" in rep
+    assert n == 0, rep
     b = pt.Scene()
     b.sdf_leaf(1, 0, [0.8], (0, 1, 0), 0, (0.9, 0.2, 0.2))
     b.sdf_leaf(2, 1, [0.5, 0.6, 0.7], (1, 1, 0), 1, (0.8, 0.8, 0.8))
@@ -106,6 +107,8 @@ sdf_twist 8 4 0.5
     b.sdf_leaf(5, 4, [0.7, 0.25], (2, 1, -1), 0, (0.3, 0.9, 0.3))
     b.sdf_leaf(6, 2, [0.4, 0.4, 0.4, 0.1], (0, 3, 0), 1, (0.9, 0.9, 0.2))
     b.sdf_combine(7, 6, 5, 2, 0.05, 0, (0.4, 0.4, 0.4))
+    b.sdf_wrap(8, 4, 6, [0.5], 2, (1, 1, 1))
+    b.sdf_wrap(9, 3, 5, [0.05, 2, 4], 0, (0.5, 0.6, 0.7))     # octaves: r_sdf_displace_octaves
     pa, pb = a.packed(), b.packed()
     assert pa.sdf_count == pb.sdf_count == 3
     xa = np.ctypeslib.as_array(pa.sdf_clusters, (pa.sdf_count * 112,)).view(np.uint32)
@@ -219,3 +222,232 @@ def test_sdf_fractal_trace_accepts_within_the_step_epsilon(orc):
     assert np.all(np.abs(p - centres[clusters]).max(axis=1) <= bound * (1 + 1e-5))
     h64, t64, _ = orc.trace(s.packed(), head, prm, ro, rd, fp64=True)
     assert (h64 & 0xC00FFFFF == hit & 0xC00FFFFF).mean() > 0.95   # the float64 march sees the same clusters
+
+
+# ---- procedural ops 5-9 (shaders/SdfPrimitives.slang:504-1245) ----
+
+PROC = """
+sdf_box 1 1.5 0.25 1.5 0 -0.5 0 lambert 0.45 0.55 0.40
+sdf_displace_noise 2 1 0.25 0.5 5 lambert 0.45 0.55 0.40
+sdf_box 10 0.3 1.0 0.3 -2 1 0 metal 0.85 0.55 0.20
+sdf_twist 11 10 1.8 metal 0.85 0.55 0.20
+sdf_capsule 20 1.0 0.3 2 1.2 0 lambert 0.30 0.55 0.85
+sdf_bend 21 20 0.5 lambert 0.30 0.55 0.85
+sdf_sphere 30 0.18 0 1.8 -2.5 lambert 0.85 0.30 0.45
+sdf_repeat_limited 31 30 0.6 0 0 3 0 0 lambert 0.85 0.30 0.45
+sdf_sphere 40 0.2 3 0.5 0 lambert 0.5 0.5 0.5
+sdf_sphere 41 0.15 3.1 0.6 0.05 lambert 0.5 0.5 0.5
+sdf_smin 42 40 41 0.1 lambert 0.5 0.5 0.5
+sdf_repeat 43 42 0 0 0.9 lambert 0.5 0.5 0.5
+"""
+# cluster centres (id order: 2, 11, 21, 31, 43) and a span to aim across
+PROC_AIM = np.array([[0, -0.3, 0, 1.4], [-2, 1, 0, 0.6], [2, 1.2, 0, 1.2], [0, 1.8, -2.5, 1.9],
+                     [3, 0.5, 0, 3.0]], np.float32)
+
+
+def _proc_scene(pt, on=True):
+    s = pt.Scene()
+    rep, n = s.exec_cfg(("r_sdf_procedural_ops 1\n" if on else "") + PROC)
+    assert n == 0, rep
+    s.env(np.zeros((2, 4, 3), np.float32))
+    return s
+
+
+def _clusters(s):
+    ps = s.packed()
+    a = np.ctypeslib.as_array(ps.sdf_clusters, shape=(ps.sdf_count * 112,)).copy()
+    return a.reshape(ps.sdf_count, 112)
+
+
+# An independent float64 restatement of the reference's procedural field, over
+# the packed cluster layout: hash, value noise, fBm, the phase-1 walker with the
+# noise band, and the root warps.
+def _hash32(x):
+    x = x.astype(np.uint64) & np.uint64(0xFFFFFFFF)
+    x ^= x >> 16
+    x = (x * 0x7feb352d) & 0xFFFFFFFF
+    x ^= x >> 15
+    x = (x * 0x846ca68b) & 0xFFFFFFFF
+    x ^= x >> 16
+    return x
+
+
+def _hash3(i, j, k):
+    h = _hash32(i)
+    h = _hash32(h ^ j)
+    h = _hash32(h ^ k)
+    return h.astype(np.float32).astype(np.float64) * 2.0 ** -32
+
+
+def _noise(p):
+    ip = np.floor(p)
+    f = p - ip
+    c = (ip.astype(np.int64) & 0xFFFFFFFF).astype(np.uint64)
+    u = f * f * f * (f * (f * 6 - 15) + 10)
+    n = {}
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                n[dx, dy, dz] = _hash3((c[:, 0] + dx) & 0xFFFFFFFF, (c[:, 1] + dy) & 0xFFFFFFFF,
+                                       (c[:, 2] + dz) & 0xFFFFFFFF)
+    # trilinear mix of the eight lattice values with the quintic weights
+    x0 = n[0, 0, 0] + (n[1, 0, 0] - n[0, 0, 0]) * u[:, 0]
+    x1 = n[0, 1, 0] + (n[1, 1, 0] - n[0, 1, 0]) * u[:, 0]
+    x2 = n[0, 0, 1] + (n[1, 0, 1] - n[0, 0, 1]) * u[:, 0]
+    x3 = n[0, 1, 1] + (n[1, 1, 1] - n[0, 1, 1]) * u[:, 0]
+    y0 = x0 + (x1 - x0) * u[:, 1]
+    y1 = x2 + (x3 - x2) * u[:, 1]
+    return y0 + (y1 - y0) * u[:, 2]
+
+
+def _fbm(p, octaves):
+    v, amp, frq = 0.0, 1.0, 1.0
+    for _ in range(min(octaves, 6)):
+        v = v + amp * (2 * _noise(p * frq) - 1)
+        amp, frq = amp * 0.5, frq * 2
+    return v
+
+
+def _leaf(p, shape, q):
+    if shape == 0:
+        return np.linalg.norm(p, axis=1) - q[0]
+    if shape in (1, 2):
+        d = np.abs(p) - q[:3]
+        o = np.linalg.norm(np.maximum(d, 0), axis=1) + np.minimum(d.max(axis=1), 0)
+        return o if shape == 1 else o - q[3]
+    if shape == 4:
+        y = np.clip(p[:, 1], -q[0], q[0])
+        return np.linalg.norm(np.stack([p[:, 0], p[:, 1] - y, p[:, 2]], 1), axis=1) - q[1]
+    raise AssertionError(shape)
+
+
+def _walk(C, nc, p):
+    d = []
+    for i in range(nc):
+        node = C[16 + 12 * i:28 + 12 * i]
+        op, shape, a, b = node[:4].view(np.uint32)
+        q, c = node[4:8].astype(np.float64), node[8:11].astype(np.float64)
+        if op == 0:
+            v = _leaf(p - c, shape, q)
+        elif op == 1:   # smooth union
+            h = np.clip(0.5 + 0.5 * (d[b] - d[a]) / q[0], 0, 1)
+            v = d[b] + h * (d[a] - d[b]) - q[0] * h * (1 - h)
+        elif op == 5:   # fBm band
+            v = d[a] + q[0] * _fbm(p * q[1], int(node[6:7].view(np.uint32)[0]))
+        else:
+            raise AssertionError(op)
+        d.append(v)
+    return d[-1]
+
+
+def _field(C, p):
+    count = int(C[3:4].view(np.uint32)[0])
+    root = C[16 + 12 * (count - 1):28 + 12 * (count - 1)]
+    op, child = int(root[:1].view(np.uint32)[0]), int(root[2:3].view(np.uint32)[0])
+    r = root[4:8].astype(np.float64)
+    if op == 6:
+        th = r[0] * p[:, 1]
+        c, s = np.cos(th), np.sin(th)
+        return 0.5 * _walk(C, child + 1, np.stack([c * p[:, 0] - s * p[:, 2], p[:, 1], s * p[:, 0] + c * p[:, 2]], 1))
+    if op == 7:
+        th = r[0] * p[:, 0]
+        c, s = np.cos(th), np.sin(th)
+        return 0.5 * _walk(C, child + 1, np.stack([p[:, 0], c * p[:, 1] - s * p[:, 2], s * p[:, 1] + c * p[:, 2]], 1))
+    if op in (8, 9):
+        pk = int(root[7:8].view(np.uint32)[0])
+        lim = np.array([pk & 0x3FF, (pk >> 10) & 0x3FF, (pk >> 20) & 0x3FF], np.float64)
+        q = p.copy()
+        for j in range(3):
+            if r[j] > 1e-6:
+                k = np.sign(p[:, j] / r[j]) * np.floor(np.abs(p[:, j] / r[j]) + 0.5)   # half away from zero
+                if op == 9:
+                    k = np.clip(k, -lim[j], lim[j])
+                q[:, j] = p[:, j] - r[j] * k
+        return _walk(C, child + 1, q)
+    return _walk(C, count, p)
+
+
+def _proc_rays(n, seed):
+    rng = np.random.default_rng(seed)
+    which = rng.integers(0, len(PROC_AIM), n)
+    ro = np.zeros((n, 4), np.float32)
+    ro[:, :3] = np.array([0.5, 4.0, 9.0], np.float32) + rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    tgt = PROC_AIM[which, :3] + rng.uniform(-1, 1, (n, 3)) * PROC_AIM[which, 3:]
+    d = tgt - ro[:, :3]
+    rd = np.zeros((n, 4), np.float32)
+    rd[:, :3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    return ro, rd
+
+
+def test_sdf_wrap_commands_build_the_reference_nodes():
+    """sdf_displace_noise/twist/bend/repeat/repeat_limited append one op node over
+    the child's nodes (Engine.cpp wrap_proc): child_a = the child's root, octaves and
+    limits packed into float bits, the child consumed."""
+    pt = load_pkg()
+    s = _proc_scene(pt)
+    C = _clusters(s)
+    assert C.shape[0] == 5
+    expect = [(5, 2, [0.25, 0.5]), (6, 2, [1.8]), (7, 2, [0.5]), (9, 2, [0.6, 0, 0]), (8, 4, [0, 0, 0.9])]
+    for c, (op, count, prm) in zip(C, expect):
+        assert int(c[3:4].view(np.uint32)[0]) == count
+        root = c[16 + 12 * (count - 1):28 + 12 * (count - 1)]
+        assert list(root[:4].view(np.uint32)) == [op, 0, count - 2, 0]
+        assert np.allclose(root[4:4 + len(prm)], prm)
+    assert int(C[0, 16 + 12 + 6:16 + 12 + 7].view(np.uint32)[0]) == 5                 # octaves
+    assert int(C[3, 16 + 12 + 7:16 + 12 + 8].view(np.uint32)[0]) == 3                 # lx | ly<<10 | lz<<20
+    assert C[4, 2] == -1000.0 and C[4, 6] == 1000.0                                 # z repeats: +-1000 m
+
+
+def test_sdf_wrap_commands_refuse_what_the_reference_refuses():
+    pt = load_pkg()
+    for bad in ("sdf_twist 2 1 1.0 lambert 1 1 1",                                  # no child 1
+                "sdf_box 1 1 1 1 0 0 0 lambert 1 1 1\nsdf_displace_noise 2 1 0 0.5 lambert 1 1 1",   # amp 0
+                "sdf_box 1 1 1 1 0 0 0 lambert 1 1 1\nsdf_repeat_limited 2 1 1 1 1 1 1 1024 lambert 1 1 1",
+                "sdf_box 1 1 1 1 0 0 0 lambert 1 1 1\nsdf_bend 2 1 0.5 lambert 1 1 1\nsdf_twist 3 2 1 lambert 1 1 1"):
+        with pytest.raises(pt.PtError):
+            pt.Scene().exec_cfg(bad)
+    s = pt.Scene()   # displacement over a warp nests (a point-displacement op)
+    rep, n = s.exec_cfg("sdf_box 1 1 1 1 0 0 0 lambert 1 1 1\nsdf_bend 2 1 0.5 lambert 1 1 1\n"
+                        "sdf_displace_noise 3 2 0.1 1 3 lambert 1 1 1")
+    assert n == 0, rep
+
+
+def test_sdf_procedural_field_matches_a_float64_restatement(orc):
+    """Every fp64-oracle hit on a procedural cluster lies on the reference's field
+    (|d| below the trace epsilon) as an independent float64 restatement computes it."""
+    pt = load_pkg()
+    s = _proc_scene(pt)
+    head, prm = s.push(8, 8)
+    C = _clusters(s)
+    ro, rd = _proc_rays(3000, 11)
+    hit, t, _ = orc.trace(s.packed(), head, prm, ro, rd, fp64=True)
+    sdf = (hit & 0xC0000000) == 0x80000000
+    ids = hit & 0xFFFFF
+    assert sdf.sum() > 500 and set(np.unique(ids[sdf])) == {0, 1, 2, 3, 4}
+    for k in range(5):
+        m = sdf & (ids == k)
+        p = ro[m, :3].astype(np.float64) + rd[m, :3].astype(np.float64) * t[m, None].astype(np.float64)
+        d = _field(C[k], p)
+        # the march accepted |d| < 1e-4; t is returned as float32 (|dt| <= 6e-7 t)
+        assert np.abs(d).max() < 1e-4 + 2e-6 * np.abs(t[m]).max() * 2, (k, np.abs(d).max())
+
+
+def test_sdf_procedural_ops_off_reads_as_empty_and_fp32_tracks_fp64(orc):
+    """Flag off (the reference's default build): the wrapped clusters are never hit.
+    Flag on: the fp32 oracle sees the clusters the fp64 oracle sees, at nearly the same t."""
+    pt = load_pkg()
+    ro, rd = _proc_rays(2000, 12)
+    s0 = _proc_scene(pt, on=False)
+    head, prm = s0.push(8, 8)
+    assert prm.sdf_procedural_ops == 0
+    h0, _, _ = orc.trace(s0.packed(), head, prm, ro, rd)
+    assert np.all(h0 == 0xFFFFFFFF)
+    s1 = _proc_scene(pt)
+    head, prm = s1.push(8, 8)
+    assert prm.sdf_procedural_ops == 1
+    h32, t32, _ = orc.trace(s1.packed(), head, prm, ro, rd)
+    h64, t64, _ = orc.trace(s1.packed(), head, prm, ro, rd, fp64=True)
+    same = h32 == h64
+    assert same.mean() > 0.98
+    hit = same & (h32 != 0xFFFFFFFF)
+    assert np.median(np.abs(t32[hit] - t64[hit]) / t64[hit]) < 1e-4
