@@ -830,7 +830,9 @@ __device__ __forceinline__ bool sdf_is_fractal(const float4* C) {
 
 // traceSdfClusters: every cluster in order, a hit replaces the best only when
 // strictly closer (the reference's `t < h.t`).  Fractal hits carry their
-// accepted step in bits 20-28 of the id.
+// accepted step in bits 20-28 of the id.  Proc false compiles the procedural
+// walker out (for launches whose scenes hold no procedural cluster in use).
+template <bool Proc = true>
 __device__ __forceinline__ void trace_sdf(const DScene& S, V3 ro, V3 rd, float& best_t, uint32_t& best_id) {
     for (uint32_t i = 0; i < S.sdf_count; ++i) {
         const float4* C = S.sdf + size_t(kSdfStride) * i;
@@ -841,7 +843,7 @@ __device__ __forceinline__ void trace_sdf(const DScene& S, V3 ro, V3 rd, float& 
                 best_t = t;
                 best_id = kSdfBit | (step << 20) | i;
             }
-        } else if ((S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(__ldg(C).w))
+        } else if ((Proc && S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(__ldg(C).w))
                         ? sdf_trace_proc(S, C, ro, rd, 1e-3f, best_t, t)
                         : sdf_trace<false>(S, C, ro, rd, 1e-3f, best_t, t)) &&
                    t < best_t) {
@@ -1217,6 +1219,7 @@ __device__ __forceinline__ void table_material(const DScene& S, uint32_t m, Surf
     s.mid = m;
 }
 
+template <bool Proc = true>
 __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, HitRec h) {
     Surface s;
     if (h.id & kSdfBit) {   // SDF cluster: header material, normal at the hit point
@@ -1227,7 +1230,7 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
             const float eps_i = S.sdf_eps * (1.0f + S.frac_eps_scale * float((h.id >> 20) & 0x1FFu));
             const float hh = fmaxf(eps_i * 8.0f, S.sdf_eps * 4.0f);
             s.normal = fractal_normal((ro + rd * h.t) - n.c, n.shape, n.q, S.frac_power, S.frac_iters, hh);
-        } else if (S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(h0.w))) {
+        } else if (Proc && S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(h0.w))) {
             s.normal = sdf_normal_central(C, __float_as_uint(h0.w), ro + rd * h.t, S.sdf_eps);
         } else {
             s.normal = normalize(sdf_normal(C, __float_as_uint(h0.w), ro + rd * h.t));
@@ -1375,7 +1378,7 @@ struct ItemScenes {
     const uint32_t* path_scene; // scene index per path
 };
 
-template <bool kShadow, bool kBatch, bool kMats = false>
+template <bool kShadow, bool kBatch, bool kMats = false, bool kProc = true>
 __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes isc, const uint32_t* queue,
                                                    uint32_t n, const float4* ray_o, const float4* ray_d,
                                                    float* out_t, uint32_t* out_id, uint32_t* fetch_ctr,
@@ -1402,7 +1405,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     auto sdf_pass = [&]() {
         float t = b.t;
         uint32_t id = kMiss;
-        trace_sdf(*Sp, ro, rd, t, id);
+        trace_sdf<kProc>(*Sp, ro, rd, t, id);
         if (id != kMiss) {
             b.t = t;
             b.key = 0x40000000u | (id & 0xFFFFFu);
@@ -1545,7 +1548,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 // transmittance: unoccluded, blocked, or refract and trace the next segment
                 bool finished = true;
                 if (!(b.id == kMiss || b.t >= t_max)) {
-                    const Surface sf = surface_at(*Sp, ro, rd, HitRec{b.t, b.id});
+                    const Surface sf = surface_at<kProc>(*Sp, ro, rd, HitRec{b.t, b.id});
                     bool zero = (sf.mat != kMatDielectric) || (seg == io.kmax);
                     if (!zero) {
                         const float ndi = dot(sf.normal, rd);

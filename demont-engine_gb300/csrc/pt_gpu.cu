@@ -846,7 +846,7 @@ __device__ __forceinline__ V3 safe_div(V3 a, V3 b) {
     return v3(b.x > 0.0f ? a.x / b.x : 0.0f, b.y > 0.0f ? a.y / b.y : 0.0f, b.z > 0.0f ? a.z / b.z : 0.0f);
 }
 
-template <bool kB, bool kAdj>
+template <bool kB, bool kAdj, bool kProc = true>
 __global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__ DScene S0,
                                                      const __grid_constant__ DFrame F0, DPaths P, Batch B,
                                                      const __grid_constant__ Adj A, int qsel, uint32_t b) {
@@ -889,7 +889,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__
                 }
                 ended = true;
             } else {
-                const Surface sf = surface_at(S, ro, rd, h);
+                const Surface sf = surface_at<kProc>(S, ro, rd, h);
                 const V3 hp = ro + rd * h.t;
                 const float ndi = dot(sf.normal, rd);
                 const V3 nf = (ndi < 0.0f) ? sf.normal : -sf.normal;
@@ -1096,26 +1096,28 @@ __global__ void __launch_bounds__(kThreads, 4) k_shadow(DScene S, DPaths P, int 
 
 
 // persistent closest hit for a queue of rays (extension rays or first shadow segments)
-template <bool kB>
+// (kProc false: the procedural SDF walker compiled out, for launches whose scenes
+// hold no procedural cluster in use; it keeps the hot traversal loop lean)
+template <bool kB, bool kProc = true>
 __global__ void __launch_bounds__(kThreads, 4) k_closest(const __grid_constant__ DScene S, Batch B,
                                                          const uint32_t* queue, const uint32_t* count,
                                                          const float4* ray_o, const float4* ray_d, float* out_t,
                                                          uint32_t* out_id, uint32_t* fetch_ctr,
                                                          unsigned long long* stat) {
     uint32_t done = 0;
-    persistent_closest<false, kB>(&S, ItemScenes{B.scenes, B.path_scene}, queue, *count, ray_o, ray_d, out_t,
+    persistent_closest<false, kB, false, kProc>(&S, ItemScenes{B.scenes, B.path_scene}, queue, *count, ray_o, ray_d, out_t,
                                   out_id, fetch_ctr, done, ShadowIO{});
     warp_add(stat, done);
 }
 
 // persistent transmittance: whole dielectric chains per lane (every segment
 // counted as a shadow segment)
-template <bool kB, bool kMats>
+template <bool kB, bool kMats, bool kProc = true>
 __global__ void __launch_bounds__(kThreads, kTransmitBlocks) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
                                                           int kmax, uint4* sh_mats) {
     uint32_t done = 0;
     const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax, sh_mats};
-    persistent_closest<true, kB, kMats>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
+    persistent_closest<true, kB, kMats, kProc>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
                                  nullptr, P.cnt + 3, done, io);
     warp_add(P.stat + 1, done);
 }
@@ -1370,6 +1372,7 @@ struct pt_gpu_ctx {
     uint32_t ltree_nodes = 0;
     DBuf<float4> sdf;
     uint32_t sdf_count = 0;
+    bool sdf_proc_any = false;   // some cluster holds a procedural op (5-9)
     DBuf<uint32_t> err_word;
     // target
     uint32_t W = 0, H = 0;
@@ -2081,6 +2084,7 @@ int pt_gpu_upload_sdf(pt_gpu_ctx* ctx, const float* clusters, uint32_t n) {
     if (!ctx) return PT_ERR_INVALID;
     if (n && !clusters) return set_err(ctx, PT_ERR_INVALID, "upload_sdf: null buffer");
     const uint32_t* u = reinterpret_cast<const uint32_t*>(clusters);
+    bool proc_any = false;
     for (uint32_t c = 0; c < n; ++c) {
         const uint32_t* h = u + size_t(c) * kSdfStride * 4u;
         const uint32_t count = h[3];
@@ -2093,10 +2097,12 @@ int pt_gpu_upload_sdf(pt_gpu_ctx* ctx, const float* clusters, uint32_t n) {
             if (op >= 1u && op <= 3u && (a >= i || b >= i))
                 return set_err(ctx, PT_ERR_INVALID, at + "an op must combine earlier nodes");
             if (op >= 4u && a >= i) return set_err(ctx, PT_ERR_INVALID, at + "an op must combine earlier nodes");
+            proc_any = proc_any || (op >= 5u);
         }
     }
     if (int rc = dupload(ctx, ctx->sdf, clusters, size_t(n) * kSdfStride)) return rc;
     ctx->sdf_count = n;
+    ctx->sdf_proc_any = proc_any;
     CK(cudaStreamSynchronize(ctx->stream));
     return PT_OK;
 }
@@ -2220,6 +2226,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     F.light_count = prm->light_count;
     sky_of(F, prm);
     const DScene S = make_scene(ctx, prm);
+    const bool proc = S.sdf_proc != 0u && ctx->sdf_proc_any;   // procedural SDF walker needed
 
     // Frames per wave: about kWavePaths paths in flight (376 bytes of path and
     // shadow-ray state each, ~25 GB at the cap).  Larger waves keep more rays
@@ -2264,7 +2271,8 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         smem = 6 * size_t(dr.nmat) * sizeof(double);
         // always opted in: k_shade also holds static shared memory (its queue
         // counting sort), and the 48 KB default bounds static + dynamic together
-        CK(cudaFuncSetAttribute(k_shade<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_shade<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_shade<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         CK(cudaFuncSetAttribute(k_resolve<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     }
     P.srad = (dr.mode == RunMode::kRecord) ? ctx->d_srad.p : nullptr;
@@ -2293,8 +2301,8 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         }
         if (persistent) {
             CK(cudaMemsetAsync(fetch, 0, 4, st));
-            k_closest<false><<<gpers, kThreads, 0, st>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
-                                                         P.hit_t, P.hit_id, fetch, P.stat);
+            (proc ? k_closest<false, true> : k_closest<false, false>)<<<gpers, kThreads, 0, st>>>(
+                S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id, fetch, P.stat);
         } else if (S.use_wide) {
             k_extend<true><<<ge, kThreads, 0, st>>>(S, P, qs);
         } else {
@@ -2337,9 +2345,11 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                     CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
                 }
                 if (adj)
-                    k_shade<false, true><<<gadj / 2, kShadeThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, b);
+                    (proc ? k_shade<false, true, true> : k_shade<false, true, false>)
+                        <<<gadj / 2, kShadeThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, b);
                 else
-                    k_shade<false, false><<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                    (proc ? k_shade<false, false, true> : k_shade<false, false, false>)
+                        <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, P, Batch{},
                                                                                                   Adj{}, qs, b);
                 if (overlap && b + 1u < F.maxb) {
                     // fork: the next bounce's rays (written by k_shade) are traced
@@ -2358,10 +2368,12 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                 if (persistent) {
                     CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
                     if (adj)
-                        k_transmit<false, true><<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
+                        (proc ? k_transmit<false, true, true> : k_transmit<false, true, false>)
+                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
                                                                                      ctx->d_sh_mats.p);
                     else
-                        k_transmit<false, false><<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                        (proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
+                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {
@@ -2672,8 +2684,8 @@ DFrame frame_of(const PtBatchView& v) {
 
 // Issue one wave (one frame of every view) on ctx->stream.
 int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t npaths, uint32_t npix_total,
-                     uint32_t max_spp, uint32_t max_b, int kmax_any, const DScene& S0, const Adj* adj = nullptr,
-                     size_t smem = 0) {
+                     uint32_t max_spp, uint32_t max_b, int kmax_any, const DScene& S0, bool proc,
+                     const Adj* adj = nullptr, size_t smem = 0) {
     const DFrame F0{};
     const int gp = (npaths + 255) / 256;
     const int gpers = ctx->sm_count * int(ctx->b_tune.persistent_blocks_per_sm);
@@ -2690,8 +2702,8 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
             if (b == 0u) {
                 CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
                 CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
-                k_closest<true><<<gpers, kThreads, 0, ctx->stream>>>(S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d,
-                                                                     P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                (proc ? k_closest<true, true> : k_closest<true, false>)<<<gpers, kThreads, 0, ctx->stream>>>(
+                    S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id, P.cnt + 3, P.stat);
             } else {
                 // this bounce's closest hits were traced on the side stream
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
@@ -2703,24 +2715,28 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
             if (adj) {
                 A = *adj;
                 A.srec_base = srec;
-                k_shade<true, true><<<ctx->sm_count * 2, kShadeThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs, b);
+                (proc ? k_shade<true, true, true> : k_shade<true, true, false>)
+                    <<<ctx->sm_count * 2, kShadeThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs, b);
             } else {
-                k_shade<true, false><<<(gstream + 1) / 2, kShadeThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+                (proc ? k_shade<true, false, true> : k_shade<true, false, false>)
+                    <<<(gstream + 1) / 2, kShadeThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
             }
             if (b + 1u < max_b) {
                 // fork: the next bounce's closest hits overlap this bounce's shadow rays
                 CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
                 CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
                 CK(cudaMemsetAsync(P.cnt + 4, 0, 4, ctx->side));
-                k_closest<true><<<gpers, kThreads, 0, ctx->side>>>(S0, Bt, P.q[qs ^ 1], P.cnt + (qs ^ 1), P.ray_o,
-                                                                   P.ray_d, P.hit_t, P.hit_id, P.cnt + 4, P.stat);
+                (proc ? k_closest<true, true> : k_closest<true, false>)<<<gpers, kThreads, 0, ctx->side>>>(
+                    S0, Bt, P.q[qs ^ 1], P.cnt + (qs ^ 1), P.ray_o, P.ray_d, P.hit_t, P.hit_id, P.cnt + 4, P.stat);
                 CK(cudaEventRecord(ctx->ev_join, ctx->side));
             }
             CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
             if (adj)
-                k_transmit<true, true><<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, ctx->d_sh_mats.p);
+                (proc ? k_transmit<true, true, true> : k_transmit<true, true, false>)
+                    <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, ctx->d_sh_mats.p);
             else
-                k_transmit<true, false><<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
+                (proc ? k_transmit<true, false, true> : k_transmit<true, false, false>)
+                    <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
             if (adj)
                 k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs,
                                                                                           srec);
@@ -2786,9 +2802,15 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     const uint32_t npaths = uint32_t(total), npix_total = uint32_t(total_pix);
     if (frames == 0) return PT_OK;
 
-    // layout signature: views' sizes and scenes, tuning
+    // the procedural SDF walker is compiled into the wave's kernels only when a
+    // view enables it over a scene that holds a procedural cluster
+    bool proc = false;
+    for (uint32_t i = 0; i < n_views; ++i)
+        proc = proc || (views[i].params.sdf_procedural_ops != 0u && scenes[views[i].scene]->sdf_proc_any);
+    // layout signature: views' sizes and scenes, tuning, walker variant
     std::vector<uint64_t> sig;
     sig.push_back(n_views);
+    sig.push_back(proc ? 1u : 0u);
     for (uint32_t i = 0; i < n_views; ++i) {
         sig.push_back((uint64_t(views[i].width) << 32) | views[i].height);
         sig.push_back(uint64_t(reinterpret_cast<uintptr_t>(scenes[views[i].scene])));
@@ -2892,7 +2914,8 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
         smem = 6 * size_t(dr.nmat) * sizeof(double);
         // always opted in: k_shade also holds static shared memory (its queue
         // counting sort), and the 48 KB default bounds static + dynamic together
-        CK(cudaFuncSetAttribute(k_shade<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_shade<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_shade<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         CK(cudaFuncSetAttribute(k_resolve<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         A.srad = ctx->d_srad.p;
         A.dldi = dr.dldi;
@@ -2923,7 +2946,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             if (!ctx->b_graph) {
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-                const int irc = issue_batch_wave(ctx, Bt, P, npaths, npix_total, max_spp, max_b, kmax_any, S0);
+                const int irc = issue_batch_wave(ctx, Bt, P, npaths, npix_total, max_spp, max_b, kmax_any, S0, proc);
                 cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
                 if (irc) return irc;
                 if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
@@ -2936,7 +2959,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             }
             CK(cudaGraphLaunch(ctx->b_graph, ctx->stream));
         } else {
-            if (int irc = issue_batch_wave(ctx, Bt, P, npaths, npix_total, max_spp, max_b, kmax_any, S0,
+            if (int irc = issue_batch_wave(ctx, Bt, P, npaths, npix_total, max_spp, max_b, kmax_any, S0, proc,
                                            adj ? &A : nullptr, smem))
                 return irc;
         }
