@@ -285,7 +285,9 @@ struct DScene {
     float sdf_eps;
     uint32_t frac_iters;         // fractal leaves: DE iterations, default power, epsilon growth per step
     float frac_power, frac_eps_scale;
-    uint32_t sdf_proc;           // 1: evaluate the procedural ops 5-9 (else they read as empty)
+    uint32_t sdf_proc;           // 1, 2: evaluate the procedural ops 5-9 (0: they read as empty);
+                                 // 2: normals by forward-mode AD unless sdf_nmode says central
+    uint32_t sdf_nmode;          // r_sdf_normal_mode: 0 forward-mode AD, 1 central differences
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs
@@ -555,8 +557,9 @@ __device__ __forceinline__ float sdf_hash3(uint32_t x, uint32_t y, uint32_t z) {
 __device__ __forceinline__ uint32_t sdf_cell(float x) {
     return uint32_t(int(fminf(fmaxf(x, -2147483648.0f), 2147483520.0f)));
 }
-// sdfValueNoise3 (value only): quintic-smoothstep trilinear mix of hashed lattice values
-__device__ float sdf_value_noise(V3 p) {
+// sdfValueNoise3: quintic-smoothstep trilinear mix of hashed lattice values, and
+// (grad non-null) its analytic gradient
+__device__ __forceinline__ float sdf_value_noise(V3 p, V3* grad = nullptr) {
     const V3 ip = v3(floorf(p.x), floorf(p.y), floorf(p.z));
     const V3 f = p - ip;
     const uint32_t ix = sdf_cell(ip.x), iy = sdf_cell(ip.y), iz = sdf_cell(ip.z);
@@ -570,19 +573,29 @@ __device__ float sdf_value_noise(V3 p) {
     const float k5 = n000 - n010 - n001 + n011;
     const float k6 = n000 - n100 - n001 + n101;
     const float k7 = -n000 + n100 + n010 + n001 - n110 - n011 - n101 + n111;
+    if (grad) {
+        const V3 du = 30.0f * f * f * (f * (f - v3(2.0f, 2.0f, 2.0f)) + v3(1.0f, 1.0f, 1.0f));
+        *grad = v3(du.x * (k1 + k4 * u.y + k6 * u.z + k7 * u.y * u.z), du.y * (k2 + k4 * u.x + k5 * u.z + k7 * u.x * u.z),
+                   du.z * (k3 + k5 * u.y + k6 * u.x + k7 * u.x * u.y));
+    }
     return k0 + k1 * u.x + k2 * u.y + k3 * u.z + k4 * u.x * u.y + k5 * u.y * u.z + k6 * u.z * u.x +
            k7 * u.x * u.y * u.z;
 }
-// sdfFbm3 (value only): at most 6 octaves, each re-centred to [-1, 1]
-__device__ float sdf_fbm(V3 p, uint32_t octaves) {
+// sdfFbm3: at most 6 octaves, each re-centred to [-1, 1]; (grad non-null) the
+// gradient summed through the octaves
+__device__ __forceinline__ float sdf_fbm(V3 p, uint32_t octaves, V3* grad = nullptr) {
     float v = 0.0f, amp = 1.0f, frq = 1.0f;
+    V3 g = v3(0.0f, 0.0f, 0.0f);
     const uint32_t o = min(octaves, 6u);
     for (uint32_t i = 0; i < o; ++i) {
-        const float vn = sdf_value_noise(p * frq);
+        V3 gn;
+        const float vn = sdf_value_noise(p * frq, grad ? &gn : nullptr);
         v += amp * (2.0f * vn - 1.0f);
+        if (grad) g = g + amp * 2.0f * gn * frq;
         amp *= 0.5f;
         frq *= 2.0f;
     }
+    if (grad) *grad = g;
     return v;
 }
 // sdfClusterDistProcN: the phase-1 walker over nodes [0, nc) plus the fBm
@@ -672,7 +685,7 @@ __device__ __forceinline__ bool sdf_has_proc(const float4* C, uint32_t count) {
 }
 // sdfClusterNormalCentral: 6-tap central differences of step h (the taps in
 // a loop, so that the walker is compiled once)
-__device__ V3 sdf_normal_central(const float4* C, uint32_t count, V3 p, float h) {
+__device__ __noinline__ V3 sdf_normal_central(const float4* C, uint32_t count, V3 p, float h) {
     float d[6];
 #pragma unroll 1
     for (int k = 0; k < 6; ++k) {
@@ -680,6 +693,107 @@ __device__ V3 sdf_normal_central(const float4* C, uint32_t count, V3 p, float h)
         d[k] = sdf_dist_warped(C, count, (k & 1) ? p - e : p + e);
     }
     const V3 g = v3(d[0] - d[1], d[2] - d[3], d[4] - d[5]);
+    const float l = length(g);
+    return l > 1e-12f ? g / l : v3(0.0f, 1.0f, 0.0f);
+}
+
+// sdfClusterDistDN: the forward-mode AD walker over nodes [0, nc), value and
+// gradient per node (smooth ops blend the children's gradients unnormalised)
+__device__ V3 sdf_dual_proc(const float4* C, uint32_t nc, V3 p) {
+    float vv[kSdfMaxNodes];
+    V3 vg[kSdfMaxNodes];
+    for (uint32_t i = 0; i < kSdfMaxNodes; ++i) {
+        if (i >= nc) break;
+        const SdfNodeD n = sdf_node(C, i);
+        float rv;
+        V3 rg;
+        if (n.op == 0u) {
+            const V3 pl = p - n.c;
+            rv = sd_leaf(pl, n.shape, n.q);
+            rg = sd_leaf_normal(pl, n.shape, n.q);
+        } else if (n.op >= 1u && n.op <= 5u) {
+            const uint32_t ia = min(n.a, i - 1u), ib = min(n.b, i - 1u);
+            const float av = vv[ia], bv = vv[ib], k = n.q.x;
+            const V3 ag = vg[ia], bg = vg[ib];
+            if (n.op == 1u) {
+                if (k <= 0.0f) {
+                    rv = (av < bv) ? av : bv;
+                    rg = (av < bv) ? ag : bg;
+                } else {
+                    const float h = clampf(0.5f + 0.5f * (bv - av) / k, 0.0f, 1.0f);
+                    rv = lerpf_(bv, av, h) - k * h * (1.0f - h);
+                    rg = lerp3(bg, ag, h);
+                }
+            } else if (n.op == 2u) {
+                if (k <= 0.0f) {
+                    rv = fmaxf(av, -bv);
+                    rg = (av > -bv) ? ag : -bg;
+                } else {
+                    const float h = clampf(0.5f - 0.5f * (bv + av) / k, 0.0f, 1.0f);
+                    rv = lerpf_(av, -bv, h) + k * h * (1.0f - h);
+                    rg = lerp3(ag, -bg, h);
+                }
+            } else if (n.op == 3u) {
+                if (k <= 0.0f) {
+                    rv = (av > bv) ? av : bv;
+                    rg = (av > bv) ? ag : bg;
+                } else {
+                    const float h = clampf(0.5f - 0.5f * (bv - av) / k, 0.0f, 1.0f);
+                    rv = lerpf_(bv, av, h) + k * h * (1.0f - h);
+                    rg = lerp3(bg, ag, h);
+                }
+            } else if (n.op == 4u) {
+                rv = av + k;
+                rg = ag;
+            } else {   // sdfDisplaceNoiseBand: amp fBm(freq p), gradient amp freq fBm'
+                V3 fg;
+                const float fv = sdf_fbm(p * n.q.y, __float_as_uint(n.q.z), &fg);
+                rv = av + k * fv;
+                rg = ag + k * n.q.y * fg;
+            }
+        } else {
+            rv = 1e30f;
+            rg = v3(0.0f, 1.0f, 0.0f);
+        }
+        vv[i] = rv;
+        vg[i] = rg;
+    }
+    return nc > 0u ? vg[nc - 1u] : v3(0.0f, 1.0f, 0.0f);
+}
+// sdfClusterNormalForwardAD: the AD gradient at the warped point, mapped back
+// through the root warp's Jacobian (transposed), normalised
+__device__ __noinline__ V3 sdf_normal_ad(const float4* C, uint32_t count, V3 p) {
+    const SdfNodeD r = sdf_node(C, count > 0u ? count - 1u : 0u);
+    const uint32_t nc = (r.op >= 6u && r.op <= 9u) ? min(r.a + 1u, kSdfMaxNodes) : count;
+    const float rate = r.q.x;
+    V3 g;
+    if (r.op == 6u) {   // twist: q = (c x - s z, y, s x + c z), c, s of rate y
+        const float c = f_cos(rate * p.y), s = f_sin(rate * p.y);
+        const V3 d = sdf_dual_proc(C, nc, v3(c * p.x - s * p.z, p.y, s * p.x + c * p.z));
+        g = v3(c * d.x + s * d.z, -rate * (s * p.x + c * p.z) * d.x + d.y + rate * (c * p.x - s * p.z) * d.z,
+               -s * d.x + c * d.z);
+    } else if (r.op == 7u) {   // bend: q = (x, c y - s z, s y + c z), c, s of rate x
+        const float c = f_cos(rate * p.x), s = f_sin(rate * p.x);
+        const V3 d = sdf_dual_proc(C, nc, v3(p.x, c * p.y - s * p.z, s * p.y + c * p.z));
+        g = v3(d.x + (-rate * (s * p.y + c * p.z)) * d.y + (rate * (c * p.y - s * p.z)) * d.z, c * d.y + s * d.z,
+               -s * d.y + c * d.z);
+    } else if (r.op == 8u || r.op == 9u) {   // repetition: identity Jacobian between cell edges
+        const uint32_t pk = __float_as_uint(r.q.w);
+        const float per[3] = {r.q.x, r.q.y, r.q.z};
+        const float lim[3] = {float(pk & 0x3FFu), float((pk >> 10) & 0x3FFu), float((pk >> 20) & 0x3FFu)};
+        float w[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            if (per[j] > 1e-6f) {
+                float idx = roundf(w[j] / per[j]);
+                if (r.op == 9u) idx = clampf(idx, -lim[j], lim[j]);
+                w[j] = w[j] - per[j] * idx;
+            }
+        }
+        g = sdf_dual_proc(C, nc, v3(w[0], w[1], w[2]));
+    } else {
+        g = sdf_dual_proc(C, nc, p);
+    }
     const float l = length(g);
     return l > 1e-12f ? g / l : v3(0.0f, 1.0f, 0.0f);
 }
@@ -712,7 +826,7 @@ __device__ bool sdf_trace(const DScene& S, const float4* C, V3 ro, V3 rd, float 
     return false;
 }
 
-__device__ __forceinline__ bool sdf_trace_proc(const DScene& S, const float4* C, V3 ro, V3 rd, float t_min,
+__device__ __noinline__ bool sdf_trace_proc(const DScene& S, const float4* C, V3 ro, V3 rd, float t_min,
                                                float t_max, float& out_t) {
     return sdf_trace<true>(S, C, ro, rd, t_min, t_max, out_t);
 }
@@ -1231,7 +1345,10 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
             const float hh = fmaxf(eps_i * 8.0f, S.sdf_eps * 4.0f);
             s.normal = fractal_normal((ro + rd * h.t) - n.c, n.shape, n.q, S.frac_power, S.frac_iters, hh);
         } else if (Proc && S.sdf_proc != 0u && sdf_has_proc(C, __float_as_uint(h0.w))) {
-            s.normal = sdf_normal_central(C, __float_as_uint(h0.w), ro + rd * h.t, S.sdf_eps);
+            if (S.sdf_proc == 2u && S.sdf_nmode == 0u)
+                s.normal = sdf_normal_ad(C, __float_as_uint(h0.w), ro + rd * h.t);
+            else
+                s.normal = sdf_normal_central(C, __float_as_uint(h0.w), ro + rd * h.t, S.sdf_eps);
         } else {
             s.normal = normalize(sdf_normal(C, __float_as_uint(h0.w), ro + rd * h.t));
         }

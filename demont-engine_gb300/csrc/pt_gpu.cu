@@ -1548,7 +1548,8 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
         S.frac_iters = prm->sdf_params[3];
         S.frac_power = prm->sdf_params_f[1];
         S.frac_eps_scale = prm->sdf_params_f[2];
-        S.sdf_proc = prm->sdf_procedural_ops ? 1u : 0u;
+        S.sdf_proc = min(prm->sdf_procedural_ops, 2u);
+        S.sdf_nmode = prm->sdf_params_f[3] != 0.0f ? 1u : 0u;
     }
     return S;
 }
@@ -2862,7 +2863,8 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             if (seen[views[i].scene] && (d.sdf_count != q.sdf_params[0] || d.sdf_iters != q.sdf_params[1] ||
                                          d.sdf_eps != q.sdf_params_f[0] || d.frac_iters != q.sdf_params[3] ||
                                          d.frac_power != q.sdf_params_f[1] || d.frac_eps_scale != q.sdf_params_f[2] ||
-                                         d.sdf_proc != (q.sdf_procedural_ops ? 1u : 0u)))
+                                         d.sdf_proc != std::min(q.sdf_procedural_ops, 2u) ||
+                                         d.sdf_nmode != (q.sdf_params_f[3] != 0.0f ? 1u : 0u)))
                 return set_err(ctx, PT_ERR_INVALID, "batch: views of one scene disagree on the SDF settings");
             d.sdf_count = q.sdf_params[0];
             d.sdf_iters = q.sdf_params[1];
@@ -2870,7 +2872,8 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
             d.frac_iters = q.sdf_params[3];
             d.frac_power = q.sdf_params_f[1];
             d.frac_eps_scale = q.sdf_params_f[2];
-            d.sdf_proc = q.sdf_procedural_ops ? 1u : 0u;
+            d.sdf_proc = std::min(q.sdf_procedural_ops, 2u);
+            d.sdf_nmode = q.sdf_params_f[3] != 0.0f ? 1u : 0u;
             seen[views[i].scene] = 1;
         }
     }

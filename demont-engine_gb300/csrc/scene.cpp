@@ -1662,7 +1662,7 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
         params->sdf_params_f[1] = power;
         params->sdf_params_f[2] = de_sc;
         params->sdf_params_f[3] = float(nm);
-        params->sdf_procedural_ops = s->cvar("r_sdf_procedural_ops") != 0.0 ? 1u : 0u;
+        params->sdf_procedural_ops = uint32_t(std::min(std::max(int(s->cvar("r_sdf_procedural_ops")), 0), 2));
     }
     return PT_OK;
 }

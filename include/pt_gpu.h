@@ -80,10 +80,11 @@ typedef struct PtPathParams {
     float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 1 env map, 2 procedural,
                                        3 Hosek-Wilkie, not built) */
     uint32_t stars;                 /* exposure_pad.y/z: procedural-sky stars (must be 0: not built) */
-    uint32_t sdf_procedural_ops;    /* 1: SDF ops 5-9 (fBm displace, twist, bend, repeat, limited repeat)
-                                       are evaluated, with central-difference normals, as in the reference
-                                       built with PT_SDF_PROCEDURAL_OPS=1 (shaders/SdfPrimitives.slang:56-58,
-                                       504-1245); 0: they read as empty, as in its default build */
+    uint32_t sdf_procedural_ops;    /* SDF ops 5-9 (fBm displace, twist, bend, repeat, limited repeat):
+                                       0 read as empty (the reference's default build); 1 evaluated, with
+                                       central-difference normals (built with PT_SDF_PROCEDURAL_OPS=1);
+                                       2 evaluated, with forward-mode AD normals where sdf_params_f[3] is 0
+                                       (also PT_SDF_AUTODIFF=1); shaders/SdfPrimitives.slang:56-68, 504-1245 */
     uint32_t reserved[2];
     /* gradient sky (no env map): the moon and the sun-disc shape
        (shaders/PathTrace.slang:766, 1222-1241; engine fill src/engine/Engine.cpp:8324-8410) */
@@ -93,7 +94,8 @@ typedef struct PtPathParams {
     float    sun_extra2[4];         /* sun disc brightness, -, -, - */
     /* SDF clusters (shaders/PathTrace.slang:859-885; engine fill src/engine/Engine.cpp:7940-7981) */
     uint32_t sdf_params[4];         /* cluster count (= uploaded), march step budget, -, fractal DE iterations */
-    float    sdf_params_f[4];       /* hit epsilon, fractal default power, fractal epsilon growth per step, - */
+    float    sdf_params_f[4];       /* hit epsilon, fractal default power, fractal epsilon growth per step,
+                                       r_sdf_normal_mode (0 forward-mode AD, 1 central differences) */
 } PtPathParams;
 
 /* 32-byte BVH node, identical to the reference's BvhNode / TriBvhNode

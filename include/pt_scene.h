@@ -98,7 +98,8 @@ int pt_scene_set_camera(pt_scene* s, float x, float y, float z, float yaw, float
  * r_moon_size 1, r_moon_disc_brightness 0.7; output step: r_exposure 1.5, r_tonemap_op 0 (aces);
  * SDF: r_sdf_max_iters 128, r_sdf_epsilon 1e-4, r_sdf_fractal_power 8, r_sdf_fractal_iters 12,
  * r_sdf_de_eps_scale 1, r_sdf_normal_mode 0, r_sdf_displace_octaves 4; r_sdf_procedural_ops 0
- * stands in for the reference's PT_SDF_PROCEDURAL_OPS build flag (1: ops 5-9 are evaluated).
+ * stands in for the reference's build flags (1: PT_SDF_PROCEDURAL_OPS, ops 5-9 evaluated with
+ * central-difference normals; 2: also PT_SDF_AUTODIFF, forward-mode AD normals by r_sdf_normal_mode).
  * Returns PT_ERR_INVALID for unknown names. */
 int pt_scene_set_cvar(pt_scene* s, const char* name, double value);
 int pt_scene_get_cvar(const pt_scene* s, const char* name, double* value);

@@ -574,7 +574,7 @@ template <class R> struct Tracer {
         const R c = mn(mx(x, R(-2147483648.0)), R(2147483520.0));
         return uint32_t(int32_t(c));
     }
-    static R sdf_value_noise(V3<R> p) {   // sdfValueNoise3, value only
+    static R sdf_value_noise(V3<R> p, V3<R>* grad = nullptr) {   // sdfValueNoise3 (+ gradient)
         const V3<R> ip{std::floor(p.x), std::floor(p.y), std::floor(p.z)};
         const V3<R> f = p - ip;
         const uint32_t ix = sdf_cell(ip.x), iy = sdf_cell(ip.y), iz = sdf_cell(ip.z);
@@ -589,18 +589,28 @@ template <class R> struct Tracer {
         const R k5 = n000 - n010 - n001 + n011;
         const R k6 = n000 - n100 - n001 + n101;
         const R k7 = -n000 + n100 + n010 + n001 - n110 - n011 - n101 + n111;
+        if (grad) {
+            const V3<R> c2{R(2), R(2), R(2)}, c1{R(1), R(1), R(1)};
+            const V3<R> du = R(30) * f * f * (f * (f - c2) + c1);
+            *grad = {du.x * (k1 + k4 * u.y + k6 * u.z + k7 * u.y * u.z), du.y * (k2 + k4 * u.x + k5 * u.z + k7 * u.x * u.z),
+                     du.z * (k3 + k5 * u.y + k6 * u.x + k7 * u.x * u.y)};
+        }
         return k0 + k1 * u.x + k2 * u.y + k3 * u.z + k4 * u.x * u.y + k5 * u.y * u.z + k6 * u.z * u.x +
                k7 * u.x * u.y * u.z;
     }
-    static R sdf_fbm(V3<R> p, uint32_t octaves) {   // sdfFbm3, value only
+    static R sdf_fbm(V3<R> p, uint32_t octaves, V3<R>* grad = nullptr) {   // sdfFbm3 (+ gradient)
         R v = R(0), amp = R(1), frq = R(1);
+        V3<R> g{R(0), R(0), R(0)};
         const uint32_t o = std::min(octaves, 6u);
         for (uint32_t i = 0; i < o; ++i) {
-            const R vn = sdf_value_noise(p * frq);
+            V3<R> gn{R(0), R(0), R(0)};
+            const R vn = sdf_value_noise(p * frq, grad ? &gn : nullptr);
             v += amp * (R(2) * vn - R(1));
+            if (grad) g = g + amp * R(2) * gn * frq;
             amp *= R(0.5);
             frq *= R(2);
         }
+        if (grad) *grad = g;
         return v;
     }
     // sdfClusterDistProcN: nodes [0, nc), with the noise band; warps below the root read as 1e30
@@ -692,6 +702,108 @@ template <class R> struct Tracer {
         const R dzp = sdf_dist_warped(C, count, p + V3<R>{R(0), R(0), h});
         const R dzn = sdf_dist_warped(C, count, p - V3<R>{R(0), R(0), h});
         const V3<R> g{dxp - dxn, dyp - dyn, dzp - dzn};
+        const R l = length(g);
+        return l > R(1e-12) ? g / l : V3<R>{R(0), R(1), R(0)};
+    }
+    static uint32_t bits_of(R x) {
+        const float f = float(x);
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return u;
+    }
+    // sdfClusterDistDN: forward-mode AD over nodes [0, nc), gradient of the last node
+    V3<R> sdf_dual_proc(const float* C, uint32_t nc, V3<R> p) const {
+        R vv[8];
+        V3<R> vg[8];
+        const V3<R> up{R(0), R(1), R(0)};
+        for (uint32_t i = 0; i < 8 && i < nc; ++i) {
+            const SdfN n = sdf_node(C, i);
+            R rv;
+            V3<R> rg;
+            if (n.op == 0u) {
+                const V3<R> pl = p - n.c;
+                rv = sd_leaf(pl, n.shape, n.q);
+                rg = sd_leaf_normal(pl, n.shape, n.q);
+            } else if (n.op >= 1u && n.op <= 5u) {
+                const R av = vv[n.a], bv = vv[n.b], k = n.q[0];
+                const V3<R> ag = vg[n.a], bg = vg[n.b];
+                if (n.op == 1u) {
+                    if (k <= R(0)) {
+                        rv = (av < bv) ? av : bv;
+                        rg = (av < bv) ? ag : bg;
+                    } else {
+                        const R h = clampv(R(0.5) + R(0.5) * (bv - av) / k, R(0), R(1));
+                        rv = lerp(bv, av, h) - k * h * (R(1) - h);
+                        rg = lerp(bg, ag, h);
+                    }
+                } else if (n.op == 2u) {
+                    if (k <= R(0)) {
+                        rv = mx(av, -bv);
+                        rg = (av > -bv) ? ag : -bg;
+                    } else {
+                        const R h = clampv(R(0.5) - R(0.5) * (bv + av) / k, R(0), R(1));
+                        rv = lerp(av, -bv, h) + k * h * (R(1) - h);
+                        rg = lerp(ag, -bg, h);
+                    }
+                } else if (n.op == 3u) {
+                    if (k <= R(0)) {
+                        rv = (av > bv) ? av : bv;
+                        rg = (av > bv) ? ag : bg;
+                    } else {
+                        const R h = clampv(R(0.5) - R(0.5) * (bv - av) / k, R(0), R(1));
+                        rv = lerp(bv, av, h) + k * h * (R(1) - h);
+                        rg = lerp(bg, ag, h);
+                    }
+                } else if (n.op == 4u) {
+                    rv = av + k;
+                    rg = ag;
+                } else {   // sdfDisplaceNoiseBand: amp fBm(freq p), gradient amp freq fBm'
+                    V3<R> fg;
+                    const R fv = sdf_fbm(p * n.q[1], bits_of(n.q[2]), &fg);
+                    rv = av + k * fv;
+                    rg = ag + k * n.q[1] * fg;
+                }
+            } else {
+                rv = R(1e30);
+                rg = up;
+            }
+            vv[i] = rv;
+            vg[i] = rg;
+        }
+        return nc > 0u ? vg[std::min(nc, 8u) - 1u] : up;
+    }
+    // sdfClusterNormalForwardAD: the root warp's transposed Jacobian applied to the AD gradient
+    V3<R> sdf_normal_ad(const float* C, uint32_t count, V3<R> p) const {
+        const SdfN r = sdf_node(C, count > 0u ? count - 1u : 0u);
+        const uint32_t nc = (r.op >= 6u && r.op <= 9u) ? std::min(r.a + 1u, 8u) : count;
+        const R rate = r.q[0];
+        V3<R> g;
+        if (r.op == 6u) {
+            const R c = M<R>::cos(rate * p.y), s = M<R>::sin(rate * p.y);
+            const V3<R> d = sdf_dual_proc(C, nc, V3<R>{c * p.x - s * p.z, p.y, s * p.x + c * p.z});
+            g = {c * d.x + s * d.z, -rate * (s * p.x + c * p.z) * d.x + d.y + rate * (c * p.x - s * p.z) * d.z,
+                 -s * d.x + c * d.z};
+        } else if (r.op == 7u) {
+            const R c = M<R>::cos(rate * p.x), s = M<R>::sin(rate * p.x);
+            const V3<R> d = sdf_dual_proc(C, nc, V3<R>{p.x, c * p.y - s * p.z, s * p.y + c * p.z});
+            g = {d.x + (-rate * (s * p.y + c * p.z)) * d.y + (rate * (c * p.y - s * p.z)) * d.z, c * d.y + s * d.z,
+                 -s * d.y + c * d.z};
+        } else if (r.op == 8u || r.op == 9u) {
+            const uint32_t pk = bits_of(r.q[3]);
+            const R lim[3] = {R(pk & 0x3FFu), R((pk >> 10) & 0x3FFu), R((pk >> 20) & 0x3FFu)};
+            R w[3] = {p.x, p.y, p.z};
+            for (int j = 0; j < 3; ++j) {
+                const R per = r.q[j];
+                if (per > R(1e-6f)) {
+                    R idx = std::round(w[j] / per);
+                    if (r.op == 9u) idx = clampv(idx, -lim[j], lim[j]);
+                    w[j] = w[j] - per * idx;
+                }
+            }
+            g = sdf_dual_proc(C, nc, V3<R>{w[0], w[1], w[2]});
+        } else {
+            g = sdf_dual_proc(C, nc, p);
+        }
         const R l = length(g);
         return l > R(1e-12) ? g / l : V3<R>{R(0), R(1), R(0)};
     }
@@ -851,7 +963,10 @@ template <class R> struct Tracer {
                 const uint32_t count = u_at(C + 3);
                 h.hit = true;
                 if (Q.sdf_procedural_ops != 0u && sdf_has_proc(C, count)) {
-                    h.normal = sdf_normal_central(C, count, ro + rd * t, R(Q.sdf_params_f[0]));
+                    if (Q.sdf_procedural_ops >= 2u && Q.sdf_params_f[3] == 0.0f)   // PT_SDF_AUTODIFF build
+                        h.normal = sdf_normal_ad(C, count, ro + rd * t);
+                    else
+                        h.normal = sdf_normal_central(C, count, ro + rd * t, R(Q.sdf_params_f[0]));
                 } else {
                     V3<R> g;
                     sdf_dist(C, count, ro + rd * t, &g);

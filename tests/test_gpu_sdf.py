@@ -193,11 +193,12 @@ light_point 1 -2 4 3 20 20 20
 
 
 @pytest.mark.parametrize("mode", [0, 1])
-@pytest.mark.parametrize("on", [1, 0])
+@pytest.mark.parametrize("on", [1, 0, 2])
 def test_sdf_procedural_render_bit_exact(pt, orc, dev, mode, on):
     """Procedural ops 5-9 (fBm displace, twist, bend, limited and unbounded
     repetition; a dielectric bent capsule in the shadow rays) render bit for bit
-    as the oracle does, with the ops on, and off (where they read as empty)."""
+    as the oracle does: on with central-difference normals (1), off, where they
+    read as empty (0), and on with forward-mode AD normals (2)."""
     s = pt.Scene()
     rep, n = s.exec_cfg(PROC_SCENE + "r_sdf_procedural_ops %d\n" % on)
     assert n == 0, rep
