@@ -383,7 +383,9 @@ int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathP
  * uploaded buffer; (1u << 30 | tri) = original triangle index; (1u << 31 | c) = SDF
  * cluster c (fractal clusters also carry the accepted step << 20), sphere-traced
  * with the reference's defaults (128 steps, epsilon 1e-4, fractal: 12 DE
- * iterations, power 8, epsilon growth 1).
+ * iterations, power 8, epsilon growth 1) and the procedural ops 5-9 off, as in the
+ * reference's default build (clusters holding them are never hit here; renders
+ * evaluate them under PtPathParams.sdf_procedural_ops).
  * t out: hit distance.
  * on_device != 0: all four pointers are device pointers. */
 int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d,
