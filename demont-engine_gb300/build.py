@@ -5,8 +5,9 @@ sm_103a + the C++ host scene builder) next to this file, under _build/.
 
 nvcc compiles the .cu with -fmad=false (no FMA contraction: every float
 expression rounds as written) and g++ compiles the host C++ with
--ffp-contract=off for the same reason.  One -gencode, two translation units,
-compiled in parallel.
+-ffp-contract=off for the same reason.  The host scene builder is C++23; the
+CUDA translation unit is C++20, the newest dialect nvcc 13 accepts.  One
+-gencode, two translation units, compiled in parallel.
 """
 import os
 import subprocess
@@ -39,7 +40,7 @@ def build(verbose=False):
         [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++20", "-fmad=false", "-prec-div=true",
          "-prec-sqrt=true", "-Xcompiler", "-fPIC,-ffp-contract=off", *inc, "-c",
          os.path.join(SRC, "pt_gpu.cu"), "-o", cu_obj],
-        [CXX, "-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", *inc, "-c",
+        [CXX, "-std=c++23", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", *inc, "-c",
          os.path.join(SRC, "scene.cpp"), "-o", cpp_obj],
     ]
     with ThreadPoolExecutor(2) as ex:

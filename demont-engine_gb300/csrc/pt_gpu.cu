@@ -3250,7 +3250,12 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     const int gtr = ctx->sm_count * kTransmitBlocks;
     const uint32_t fpw = std::max<uint32_t>(1u, std::min<uint32_t>(frames, kNoAllocMaxPixels / F.npix));
     float4* accum = reinterpret_cast<float4*>(accum_device);
+    const bool proc = S.sdf_proc != 0u && ctx->sdf_proc_any;   // procedural SDF walker needed
 
+    // work a failed earlier pt_gpu_render left on the side stream (it writes
+    // the error word) finishes before this call clears it
+    CK(cudaEventRecord(ctx->ev_join, ctx->side));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaMemsetAsync(P.stat, 0, 32, ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     ctx->stats = PtStats{};
@@ -3272,19 +3277,20 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                 CK(cudaMemsetAsync(P.cnt + 2, 0, 4, ctx->stream));
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_closest<false><<<gpers, kThreads, 0, ctx->stream>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o,
-                                                                          P.ray_d, P.hit_t, P.hit_id, P.cnt + 3,
-                                                                          P.stat);
+                    (proc ? k_closest<false, true> : k_closest<false, false>)<<<gpers, kThreads, 0, ctx->stream>>>(
+                        S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id, P.cnt + 3, P.stat);
                 } else if (S.use_wide) {
                     k_extend<true><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
                 } else {
                     k_extend<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
                 }
-                k_shade<false, false><<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
-                                                                                              qs, b);
+                (proc ? k_shade<false, false, true> : k_shade<false, false, false>)
+                    <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                                                                                              Adj{}, qs, b);
                 if (persistent) {
                     CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
-                    k_transmit<false, false><<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                    (proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
+                        <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
                 } else {

@@ -74,7 +74,9 @@ typedef struct PtPathParams {
     uint32_t bvh_params[4];         /* linear_prim_count, analytic BVH node count,
                                        triangle count (0 = no mesh), triangle BVH node count */
     uint32_t light_count;
-    uint32_t light_tree_enabled;    /* must be 0 (uniform pick); the tree is not built here */
+    uint32_t light_tree_enabled;    /* 1: pick lights through the tree uploaded with
+                                       pt_gpu_upload_light_tree (r_light_tree, the reference's
+                                       default); 0: uniform pick (one random number) */
     uint32_t light_tree_node_count;
     uint32_t rr_start;              /* Russian roulette starts at bounce b >= rr_start; reference: 2 */
     float    sun_and_mode[4];       /* sun dir xyz, sky mode in w (0 gradient, 1 env map, 2 procedural,

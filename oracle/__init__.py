@@ -22,7 +22,26 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_builders.so")
-REF_TREE = os.environ.get("PT_REFERENCE_TREE", "/root/reference")
+
+
+def _reference_tree():
+    """The reference source tree: PT_REFERENCE_TREE when set, else the REF
+    default of oracle/Makefile (the recipe that compiles the reference's
+    builders from their sources).  None when no such tree exists here: the
+    tests that read it skip, and the GPU host never has it."""
+    env = os.environ.get("PT_REFERENCE_TREE")
+    if env:
+        return env
+    try:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"],
+                           capture_output=True, text=True, timeout=30)
+        path = r.stdout.strip()
+    except Exception:
+        return None
+    return path if path and os.path.isdir(os.path.join(path, "src", "renderer")) else None
+
+
+REF_TREE = _reference_tree()
 
 u32 = ctypes.c_uint32
 f32 = ctypes.c_float
@@ -40,10 +59,11 @@ def build(ref: bool | None = None):
     """make -C oracle (and the reference builders when the reference tree exists)."""
     targets = ["all"]
     if ref is None:
-        ref = os.path.isdir(os.path.join(REF_TREE, "src", "renderer"))
-    if ref:
+        ref = REF_TREE is not None
+    if ref and REF_TREE:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_TREE}", *targets], check=True)
+    extra = [f"REF={REF_TREE}"] if REF_TREE else []
+    subprocess.run(["make", "-s", "-C", HERE, *extra, *targets], check=True)
 
 
 _lib = None
@@ -90,6 +110,25 @@ def render(packed, head, prm, W, H, frames=1, accum=None, crop=None, fp64=False,
     if rc != 0:
         raise RuntimeError(f"oracle_render failed: {rc}")
     return accum, c
+
+
+def capture_rays(packed, head, prm, W, H, bounce, crop=None, threads=0):
+    """The extension rays bounce `bounce` of frame head.frame_index traces, for
+    every sample of the pixels in crop = (x0, y0, x1, y1): (ro4, rd4) float32
+    arrays of shape (n, 4), only the samples whose path reached that bounce."""
+    lib = load()
+    x0, y0, x1, y1 = crop if crop is not None else (0, 0, W, H)
+    spp = max(int(head.spp), 1)
+    n = (x1 - x0) * (y1 - y0) * spp
+    ro = np.zeros((n, 4), np.float32)
+    rd = np.zeros((n, 4), np.float32)
+    rc = lib.oracle_capture_rays(ctypes.byref(packed), ctypes.byref(head), ctypes.byref(prm), u32(W), u32(H),
+                                 u32(bounce), u32(x0), u32(y0), u32(x1), u32(y1), ro.ctypes.data_as(P(f32)),
+                                 rd.ctypes.data_as(P(f32)), ctypes.c_int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_capture_rays failed: {rc}")
+    live = np.any(rd[:, :3] != 0.0, axis=1)
+    return ro[live], rd[live]
 
 
 def software_preview(packed, head, prm, W, H, accum=None, threads=0):

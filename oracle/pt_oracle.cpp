@@ -337,6 +337,14 @@ struct AdjSink {
 
 template <class R> struct Tracer {
     AdjSink* adj = nullptr;
+    // ray capture (test hook): the extension ray a sample traces at bounce
+    // cap_bounce is written to cap_o / cap_d at float4 slot cap_slot; the path
+    // continues, so later samples of the pixel draw from the same seed state as
+    // in a render
+    float* cap_o = nullptr;
+    float* cap_d = nullptr;
+    uint32_t cap_bounce = 0;
+    size_t cap_slot = 0;
     const PtPackedScene& S;
     const PtPushHead& P;
     const PtPathParams& Q;
@@ -1590,6 +1598,12 @@ template <class R> struct Tracer {
             if (adj) adj->contrib(c, shadow);
         };
         for (uint32_t b = 0; b < maxb; ++b) {
+            if (cap_o && b == cap_bounce) {
+                float* o = cap_o + 4 * cap_slot;
+                float* d = cap_d + 4 * cap_slot;
+                o[0] = float(ro.x); o[1] = float(ro.y); o[2] = float(ro.z); o[3] = 0.0f;
+                d[0] = float(rd.x); d[1] = float(rd.y); d[2] = float(rd.z); d[3] = 0.0f;
+            }
             cnt.ext++;
             const uint64_t n0 = cnt.nodes, t0 = cnt.tris, p0 = cnt.prims;
             Hit<R> h = trace(ro, rd);
@@ -1826,6 +1840,43 @@ void render(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, 
             }
 }
 
+// The extension rays of bounce `bounce` of every sample of one frame over the
+// pixels of [x0,x1) x [y0,y1), fp32 instance (the rays the GPU render traces,
+// bit for bit): slot ((y - y0) * (x1 - x0) + (x - x0)) * spp + s.  Samples whose
+// path ended before that bounce keep a zero direction.
+void capture_rays(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, uint32_t W, uint32_t H,
+                  uint32_t bounce, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, float* out_o,
+                  float* out_d, int threads) {
+    const uint32_t spp = (P.spp == 0u) ? 1u : P.spp;
+    const uint32_t cw = x1 - x0, rows = y1 - y0;
+    std::fill(out_o, out_o + size_t(cw) * rows * spp * 4, 0.0f);
+    std::fill(out_d, out_d + size_t(cw) * rows * spp * 4, 0.0f);
+    int nt = threads > 0 ? threads : int(std::thread::hardware_concurrency());
+    if (nt < 1) nt = 1;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        Tracer<float> tr(S, P, Q, W, H);
+        tr.cap_o = out_o;
+        tr.cap_d = out_d;
+        tr.cap_bounce = bounce;
+        for (;;) {
+            const uint32_t r = next.fetch_add(1);
+            if (r >= rows) break;
+            const uint32_t y = y0 + r;
+            for (uint32_t x = x0; x < x1; ++x) {
+                uint32_t seed = pcg_hash(x * 1973u + y * 9277u + P.frame_index * 26699u);
+                for (uint32_t s = 0; s < spp; ++s) {
+                    tr.cap_slot = (size_t(r) * cw + (x - x0)) * spp + s;
+                    (void)tr.sample_path(x, y, s, seed);
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < nt; ++i) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+}
+
 // adjoint oracle: fp32 paths (the GPU's, bit for bit), derivatives in double
 void adjoint(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q, uint32_t W, uint32_t H,
              uint32_t frames, const float* dldi, int threads, double* g_alb, double* g_em) {
@@ -2002,6 +2053,16 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
     else
         orc::render<float>(*scene, *head, *params, W, H, frames, accum_rgba, x0, y0, x1, y1, threads, c);
     orc::export_counters(c, counters);
+    return 0;
+}
+
+int oracle_capture_rays(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                        uint32_t W, uint32_t H, uint32_t bounce, uint32_t x0, uint32_t y0, uint32_t x1,
+                        uint32_t y1, float* ray_o, float* ray_d, int threads) {
+    if (!scene || !head || !params || !ray_o || !ray_d || W == 0 || H == 0) return -1;
+    if (x1 > W || y1 > H || x0 > x1 || y0 > y1) return -1;
+    if (head->tlas_present) return -6;
+    orc::capture_rays(*scene, *head, *params, W, H, bounce, x0, y0, x1, y1, ray_o, ray_d, threads);
     return 0;
 }
 

@@ -53,12 +53,15 @@ int oracle_render(const PtPackedScene* scene, const PtPushHead* head, const PtPa
                   uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
                   int fp64, int threads, OracleCounters* counters);
 
-/* Adjoint oracle: dLoss/d(albedo) and dLoss/d(emission) per material-table
- * row (3 doubles a row each) of a render of `frames` frames from reset, for
- * dLoss/dImage = dl_di_rgba (W*H*4 floats, .a ignored).  The paths are the
- * fp32 instance's (the GPU's paths bit for bit); each sample's contributions
- * are differentiated term by term in double (no suffix sums), with the
- * Russian-roulette probabilities held fixed.  -7: firefly clamp enabled. */
+/* The extension rays that bounce `bounce` of frame head->frame_index traces
+ * (fp32 instance: the rays the GPU render traces, bit for bit), for every
+ * sample of every pixel of [x0,x1) x [y0,y1): float4 slot
+ * ((y - y0) * (x1 - x0) + (x - x0)) * spp + s of ray_o / ray_d (w = 0).
+ * Samples whose path ended earlier keep a zero direction. */
+int oracle_capture_rays(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
+                        uint32_t W, uint32_t H, uint32_t bounce, uint32_t x0, uint32_t y0, uint32_t x1,
+                        uint32_t y1, float* ray_o, float* ray_d, int threads);
+
 /* The reference's Software-backend preview estimator (primary hit, sky-lit
  * ambient, one sun shadow ray, emission; running mean), for a timed CPU
  * baseline only: one frame into accum_rgba (H x W x 4). */
@@ -68,6 +71,12 @@ int oracle_software_preview(const PtPackedScene* scene, const PtPushHead* head, 
  * directions (x, y, z, 0), their pdf as sampled, and pdfEnvMapDir of each. */
 int oracle_env_sample(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params, uint32_t n,
                       const float* xu, const float* xv, float* dir4, float* pdf, float* pdf_of_dir);
+/* Adjoint oracle: dLoss/d(albedo) and dLoss/d(emission) per material-table
+ * row (3 doubles a row each) of a render of `frames` frames from reset, for
+ * dLoss/dImage = dl_di_rgba (W*H*4 floats, .a ignored).  The paths are the
+ * fp32 instance's (the GPU's paths bit for bit); each sample's contributions
+ * are differentiated term by term in double (no suffix sums), with the
+ * Russian-roulette probabilities held fixed.  -7: firefly clamp enabled. */
 int oracle_adjoint(const PtPackedScene* scene, const PtPushHead* head, const PtPathParams* params,
                    uint32_t W, uint32_t H, uint32_t frames, const float* dl_di_rgba, int threads,
                    double* grad_albedo, double* grad_emission);
