@@ -123,22 +123,6 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def extend_traffic_per_ray():
-    """DRAM bytes per extension segment of the closest-hit kernel from the
-    committed ncu summary (profiles/k_closest_c1.md, line
-    `dram_bytes_per_extension_segment: X`)."""
-    p = os.path.join(ROOT, "profiles", "k_closest_c1.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.strip().startswith("dram_bytes_per_extension_segment:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
-
-
 def shade_bytes_per_vertex(scene):
     """Algorithmic bytes the shading stage reads per path vertex of this
     workload, on the reference's data layouts: a material row (3 float4, 48 B);
@@ -159,25 +143,36 @@ def shade_bytes_per_vertex(scene):
                      f"miss: 4 bilinear texels 64 + pdf texel 16"}
 
 
-def closest_hit_alu_share():
-    """ALU-pipe utilisation of the closest-hit kernel at bounce 0 from the
-    committed ncu summary (profiles/k_closest_c1.md, the
-    `sm__inst_executed_pipe_alu` row), as a fraction; None if absent."""
-    p = os.path.join(ROOT, "profiles", "k_closest_c1.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("| sm__inst_executed_pipe_alu"):
-            try:
-                return float(line.split("|")[2].strip().rstrip("%")) / 100.0
-            except (IndexError, ValueError):
-                return None
-    return None
+# bytes one closest-hit query moves on the structures it walks (the 4-wide
+# trees): queue entry 4 + ray origin and direction 2 x 16 in, hit t and id 2 x 4
+# out; per wide node tested its six box planes and four child codes (7 x 16, the
+# last 16 bytes of the 128-byte node are not loaded); per triangle 3 x 16; per
+# analytic primitive in a leaf 16 (geometry) + 16 (id, type, tie key); per plane
+# record tested linearly 16 + 4; per traversal-stack push or pop 8.
+RAY_IO_BYTES = 4 + 32 + 8
+NODE_BYTES, TRI_BYTES, APRIM_BYTES, LINEAR_BYTES, STACK_BYTES = 112, 48, 32, 20, 8
+
+
+def traversed_bytes(t, kind):
+    """Bytes per segment on the traversed structures from the counting pass's
+    PtTraversalStats: (total, terms)."""
+    g = lambda f: getattr(t, f"{kind}_{f}")
+    n = max(g("segments"), 1)
+    terms = {"ray_and_hit": float(RAY_IO_BYTES),
+             "nodes": NODE_BYTES * g("nodes") / n,
+             "triangles": TRI_BYTES * g("tris") / n,
+             "analytic_prims": APRIM_BYTES * g("aprims") / n + LINEAR_BYTES * g("linear") / n,
+             "stack": STACK_BYTES * (g("push") + g("pop")) / n}
+    per = {"nodes": g("nodes") / n, "triangles": g("tris") / n, "analytic_prims": g("aprims") / n,
+           "linear_prims": g("linear") / n, "stack_push": g("push") / n, "stack_pop": g("pop") / n}
+    return sum(terms.values()), terms, per
 
 
 def algorithmic_bytes(pt, orc, scene, head, prm):
-    """B_seg = 32 (ray) + 16 (hit) + 32 N_node + 52 N_tri + 112 N_prim per extension
-    segment, N from the oracle walking the reference binary BVH on a crop of frame 0."""
+    """Bytes per extension segment on the REFERENCE's binary structures (for
+    comparison with the trees actually walked): 32 (ray) + 16 (hit) + 32 N_node
+    + 52 N_tri + 112 N_prim, N from the oracle walking the reference BVHs on a
+    crop of frame 0."""
     _, c = orc.render(scene.packed(), head, prm, W_FULL, H_FULL, 1, crop=(704, 396, 1216, 684))
     n = max(c.ext_rays, 1)
     nn, nt, npr = c.ext_nodes / n, c.ext_tris / n, c.ext_prims / n
@@ -218,6 +213,47 @@ def cpu_baseline(pt, orc, scene, head, prm, budget_s=12.0):
         "sample": f"{sw_frames} frames 1920x1080 of the reference's Software-backend preview estimator "
                   f"(1 primary + <=1 sun shadow ray per pixel), {sw_segs} segments in {sw_t:.1f} s"}
     return out
+
+
+def c0_bench(pt, orc, frames=64, steps=3, cpu_budget_s=6.0):
+    """The plain analytic configuration: 256x256, 16 spp, depth 8, roulette from
+    bounce 3; 64 spheres, 4 boxes (12 triangles each), one 1x1 quad light of
+    radiance 15, black environment.  One step = `frames` frames accumulated.
+    Beside it the fp32 oracle on all host cores over whole frames of the same
+    workload (about `cpu_budget_s` of CPU work)."""
+    s = pt.Scene().synth(0, seed=0)
+    W = H = 256
+    dev = pt.Device(0)
+    try:
+        dev.upload(s)
+        dev.set_target(W, H)
+        head, prm = s.push(W, H, frame_index=0, reset=1)
+        for _ in range(3):
+            dev.render(head, prm, frames)
+        t_ms, segs = 0.0, 0
+        for _ in range(steps):
+            dev.render(head, prm, frames)
+            st = dev.stats()
+            t_ms += st.gpu_ms
+            segs += st.extension_rays + st.shadow_rays
+    finally:
+        dev.close()
+    cores = os.cpu_count() or 1
+    acc = np.zeros((H, W, 4), np.float32)
+    c_segs, c_t, f = 0, 0.0, 0
+    while c_t < cpu_budget_s and f < frames:
+        h0, p0 = s.push(W, H, frame_index=f, reset=int(f == 0))
+        t0 = time.perf_counter()
+        _, c = orc.render(s.packed(), h0, p0, W, H, 1, accum=acc, threads=cores)
+        c_t += time.perf_counter() - t0
+        c_segs += c.ext_rays + c.shadow_rays
+        f += 1
+    return {"workload": f"plain analytic 256x256, {head.spp} spp x {frames} frames, depth {head.max_bounces}, "
+                        f"roulette from bounce {prm.rr_start}, 64 spheres + 4 boxes, 1 quad light",
+            "mrays_s": segs / (t_ms / 1e3) / 1e6, "ms_per_step": t_ms / steps,
+            "segments_per_step": segs // steps,
+            "cpu_baseline": {"value": c_segs / c_t / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": f"{f} whole frames (256x256, 16 spp each), {c_segs} segments in {c_t:.1f} s"}}
 
 
 def _tris_at_scale(sc):
@@ -591,6 +627,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c0", action="store_true", help="skip the plain analytic (256x256, 16 spp) leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-views leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-render leg")
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse-rendering leg")
@@ -662,6 +699,12 @@ def main():
         ext_launch += st.extend_launches
         t_serial += st.gpu_ms / 1e3
     barrier()
+    # what the traversal touched: one step with the counting kernel variants
+    # (same images; the counting costs time, so kernel times come from mode 2)
+    dev.set_profiling(3)
+    dev.render(head, prm, args.frames)
+    tstat = dev.traversal_stats()
+    barrier()
 
     # end to end through the C-ABI with host buffers (pinned when torch can pin)
     dev.set_profiling(False)
@@ -691,35 +734,38 @@ def main():
 
     import oracle as orc
     orc.load()
-    bseg, nbar = algorithmic_bytes(pt, orc, scene, head, prm)
+    ref_bseg, ref_nbar = algorithmic_bytes(pt, orc, scene, head, prm)
     peak, peak_kind = measured_peak()
-    ext_s = ext_ms / 1e3
-    achieved = (ext * bseg / ext_s / 1e9) if ext_s > 0 else None
-    tpr = extend_traffic_per_ray()
-    per_launch_rays = ext / max(ext_launch, 1)
-    roofline = {"bound": "hbm", "kernel": "k_closest (persistent closest hit, 4-wide SAH trees)", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                "traffic": (tpr * per_launch_rays) if tpr else None,
-                "algorithmic_bytes_per_launch": bseg * per_launch_rays,
-                "avg_launch_ms": ext_ms / max(ext_launch, 1), "launches": ext_launch,
-                "B_seg": bseg, "N_per_segment": nbar, "peak_kind": peak_kind,
-                "dram_achieved_GBs": (tpr * per_launch_rays / (ext_ms / max(ext_launch, 1)) / 1e6)
-                if (tpr and ext_ms > 0) else None,
-                "dram_frac": (tpr * per_launch_rays / (ext_ms / max(ext_launch, 1)) / 1e6 / peak)
-                if (tpr and ext_ms > 0) else None,
-                "alu_pipe_frac_ncu": closest_hit_alu_share(),
-                "shade_bytes_per_vertex": shade_bytes_per_vertex(scene),
-                "compulsory_bytes_per_segment": 48,
-                "note": "achieved = algorithmic bytes of the reference binary structures per segment "
-                        "(B_seg) x segments / k_closest time; those bytes are mostly served by L1/L2, so "
-                        "frac can exceed 1; dram_frac is the measured DRAM traffic (ncu, "
-                        "profiles/k_closest_c1.md) over the same time; the kernel's limiter is its ALU pipe "
-                        "(alu_pipe_frac_ncu, same summary).  Kernel times: CUDA events around "
-                        "each launch in a second pass of the same K steps with the stages serial (in the "
-                        "timed schedule the next bounce's k_closest overlaps this bounce's k_transmit)",
-                "step_share": {"k_closest": ext_ms / max(1e3 * t_serial, 1e-9),
-                               "k_transmit": sh_ms / max(1e3 * t_serial, 1e-9),
-                               "serial_ms_per_step": 1e3 * t_serial / args.steps}}
+    roofline = None
+    if tstat.ext_segments:
+        launch_ms = ext_ms / max(ext_launch, 1)
+        per_launch = ext / max(ext_launch, 1)
+        bseg, terms, per = traversed_bytes(tstat, "ext")
+        achieved = bseg * per_launch / (launch_ms * 1e-3) / 1e9
+        sh_bseg, sh_terms, sh_per = traversed_bytes(tstat, "shadow")
+        roofline = {
+            "bound": "hbm", "kernel": "k_closest (persistent closest hit, 4-wide SAH trees)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": bseg * per_launch, "avg_launch_ms": launch_ms, "launches": ext_launch,
+            "bytes_per_segment": bseg, "bytes_per_segment_terms": terms, "per_segment": per,
+            "dram_compulsory_frac": RAY_IO_BYTES * per_launch / (launch_ms * 1e-3) / 1e9 / peak,
+            "ref_structure_bytes_per_segment": ref_bseg, "ref_structure_N_per_segment": ref_nbar,
+            "shadow_kernel": {"kernel": "k_transmit", "bytes_per_segment": sh_bseg, "bytes_per_segment_terms": sh_terms,
+                              "per_segment": sh_per,
+                              "achieved_GBs": sh_bseg * tstat.shadow_segments
+                              / max(sh_ms / args.steps * 1e-3, 1e-12) / 1e9},
+            "shade_bytes_per_vertex": shade_bytes_per_vertex(scene),
+            "note": "achieved = bytes the closest-hit kernel moves per segment on the trees it walks (device "
+                    "counters of a counting pass: wide nodes, triangles, leaf and plane records, 8-byte stack "
+                    "pushes and pops, ray in and hit out) x extension segments per launch / average launch "
+                    "time (CUDA events, stages serial).  Most of these bytes are L1/L2 hits: ray in and hit "
+                    "out (dram_compulsory_frac) are the only bytes that must reach DRAM; the scene (~350 MB) "
+                    "exceeds L2, so part of the node and triangle traffic does too (ncu DRAM bytes per "
+                    "launch: DESIGN.md).  traffic is null: no ncu capture runs inside the bench.",
+            "step_share": {"k_closest": ext_ms / max(1e3 * t_serial, 1e-9),
+                           "k_transmit": sh_ms / max(1e3 * t_serial, 1e-9),
+                           "serial_ms_per_step": 1e3 * t_serial / args.steps}}
     line = {"metric": METRIC, "value": segs / t_dev / 1e6, "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
             "wall_ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -742,6 +788,8 @@ def main():
             "clocks": clk}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pt, orc, scene, head, prm)
+    if world == 1 and not args.no_c0:
+        line["c0"] = c0_bench(pt, orc)
     if world == 1 and not args.no_batched:
         dev.close()
         line["batched"] = batched_bench(pt)

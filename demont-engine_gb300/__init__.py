@@ -88,6 +88,11 @@ class PtLightInput(ctypes.Structure):
                 ("cos_outer", f32), ("u_vec", f32 * 3), ("v_half", f32)]
 
 
+class PtTraversalStats(ctypes.Structure):
+    _fields_ = [(f"{k}_{f}", ctypes.c_uint64) for k in ("ext", "shadow")
+                for f in ("segments", "nodes", "tris", "aprims", "linear", "push", "pop")]
+
+
 class PtDiffStats(ctypes.Structure):
     _fields_ = [("max_delta", ctypes.c_double), ("mean_delta", ctypes.c_double), ("rms_delta", ctypes.c_double),
                 ("bad_percent", ctypes.c_double), ("total_pixels", ctypes.c_uint64), ("bad_pixels", ctypes.c_uint64)]
@@ -138,6 +143,8 @@ SIGNATURES = {
     "pt_gpu_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_set_wave_frames": (ctypes.c_int, [ctypes.c_void_p, u32]),
     "pt_gpu_set_traversal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pt_gpu_get_traversal_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtTraversalStats)]),
+    "pt_gpu_set_debug_limits": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
     "pt_gpu_get_accel_info": (ctypes.c_int, [ctypes.c_void_p, P(PtAccelInfo)]),
     "pt_gpu_batch_render": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p), u32, P(PtBatchView), u32, u32]),
     "pt_gpu_batch_read_accum": (ctypes.c_int, [ctypes.c_void_p, u32, P(f32)]),
@@ -563,8 +570,19 @@ class Device:
 
     def set_profiling(self, on=True):
         """True/1: events on the overlapped schedule; 2: stages serial (each
-        kernel timed alone); False/0: off."""
+        kernel timed alone); 3: as 2 with the counting traversal variants
+        (traversal_stats); False/0: off."""
         self._check(self.lib.pt_gpu_set_profiling(self.h, int(on)))
+
+    def set_debug_limits(self, traverse_cap=0, stack_entries=0):
+        """Lower the traversal iteration cap / stack (failure-path tests); 0 = default."""
+        self._check(self.lib.pt_gpu_set_debug_limits(self.h, traverse_cap, stack_entries))
+
+    def traversal_stats(self) -> PtTraversalStats:
+        """Traversal work of the last render in profiling mode 3."""
+        t = PtTraversalStats()
+        self._check(self.lib.pt_gpu_get_traversal_stats(self.h, ctypes.byref(t)))
+        return t
 
     def set_traversal(self, mode):
         self._check(self.lib.pt_gpu_set_traversal(self.h, mode))

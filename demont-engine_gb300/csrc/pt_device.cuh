@@ -289,15 +289,39 @@ struct DScene {
                                  // 2: normals by forward-mode AD unless sdf_nmode says central
     uint32_t sdf_nmode;          // r_sdf_normal_mode: 0 forward-mode AD, 1 central differences
     uint32_t* err;               // error word: bit 0 traversal cap, bit 1 stack overflow
+    uint32_t trav_cap;           // loop iterations allowed per query (default kTraverseCap)
+    int stack_cap;               // wide-tree traversal stack entries allowed (default and maximum 64)
     // 4-wide SAH trees (128-byte nodes: child boxes SoA, child, count)
     uint32_t use_wide;           // traversal mode: 1 wide SAH trees, 0 the reference BVHs
     uint32_t a_wide, t_wide;     // 1: walk the wide tree for that part
+    uint32_t wide_linear;        // records the wide-tree kernels test linearly: the planes when the
+                                 // dispatch walks an analytic BVH, else every record (the reference
+                                 // scans them all in order when bvh_params.y == 0)
     const float4* a4;            // analytic wide nodes (8 float4 each)
     const float4* a4_geo;        // finite analytic prims in wide-leaf order
     const uint4* a4_meta;        // (record slot, type, tie key, 0)
     const float4* t4;            // mesh wide nodes
     const float4* tri4;          // triangles in wide-leaf order: (v0, orig id) (e1, material) (e2, tie rank)
+    // traversal counters of the counting kernel variants (profiling mode 3), or null:
+    // [0..7] extension segments, [8..15] shadow segments, each (segments, wide nodes
+    // tested, triangles tested, analytic prims tested in wide leaves, linear prims
+    // tested, stack pushes, stack pops, -)
+    unsigned long long* tcount;
 };
+
+// Per-lane traversal counters of the counting variants.
+struct TravCount {
+    uint32_t seg = 0, nodes = 0, tris = 0, aprims = 0, linear = 0, push = 0, pop = 0;
+};
+__device__ __forceinline__ void tcount_flush(unsigned long long* out, const TravCount& c) {
+    const uint32_t v[7] = {c.seg, c.nodes, c.tris, c.aprims, c.linear, c.push, c.pop};
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        unsigned long long x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + k, x);
+    }
+}
 
 struct HitRec {
     float t;
@@ -982,7 +1006,7 @@ __device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, floa
         int sp = 0;
         stack[sp++] = 0u;
         while (sp > 0) {
-            if (++iters > kTraverseCap) { atomicOr(S.err, 1u); break; }
+            if (++iters > S.trav_cap) { atomicOr(S.err, 1u); break; }
             const uint32_t idx = stack[--sp];
             const float4 lo = __ldg(S.bvh + 2u * idx), hi = __ldg(S.bvh + 2u * idx + 1u);
             if (!slab(ro, inv, lo, hi, h.t)) continue;
@@ -1006,7 +1030,7 @@ __device__ __noinline__ HitRec trace_closest(const DScene& S, V3 ro, V3 rd, floa
         int sp = 0;
         stack[sp++] = 0u;
         while (sp > 0) {
-            if (++iters > kTraverseCap) { atomicOr(S.err, 1u); break; }
+            if (++iters > S.trav_cap) { atomicOr(S.err, 1u); break; }
             const uint32_t idx = stack[--sp];
             const float4 lo = __ldg(S.tri_bvh + 2u * idx), hi = __ldg(S.tri_bvh + 2u * idx + 1u);
             if (!slab(ro, inv, lo, hi, t_mesh)) continue;
@@ -1224,7 +1248,7 @@ __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, 
     uint32_t leaf = 0u;   // postponed leaf (0 = none; leaf codes always carry kLeafBit)
     while (sp > 0 || leaf) {
         while (sp > 0 && !leaf) {
-            if (++iters > kTraverseCap) { atomicOr(S.err, 1u); return; }
+            if (++iters > S.trav_cap) { atomicOr(S.err, 1u); return; }
             --sp;
             const uint32_t code = st_code[sp];
             if (st_t[sp] > b.t) continue;
@@ -1235,7 +1259,7 @@ __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, 
             float dk[4];
             uint32_t ck[4];
             const int nh = wide_children(nodes, code, inv, nx, ny, nz, b.t, dk, ck);
-            if (sp + nh > kWideStackDev) { atomicOr(S.err, 2u); return; }
+            if (sp + nh > S.stack_cap) { atomicOr(S.err, 2u); return; }
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 if (k < nh) {
@@ -1256,7 +1280,7 @@ __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, 
 // when its wide tree is not built).
 __device__ __noinline__ HitRec trace_wide(const DScene& S, V3 ro, V3 rd, float t_init) {
     Best b{t_init, 0u, kMiss};
-    const uint32_t linear = S.linear_count;
+    const uint32_t linear = S.wide_linear;
     for (uint32_t i = 0; i < linear; ++i) {
         const float t = isect_geo(__ldg(S.prim_type + i), __ldg(S.prim_geo + i), ro, rd);
         if (t > 1e-3f && better(t, i, b)) {
@@ -1495,7 +1519,7 @@ struct ItemScenes {
     const uint32_t* path_scene; // scene index per path
 };
 
-template <bool kShadow, bool kBatch, bool kMats = false, bool kProc = true>
+template <bool kShadow, bool kBatch, bool kMats = false, bool kProc = true, bool kCount = false>
 __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes isc, const uint32_t* queue,
                                                    uint32_t n, const float4* ray_o, const float4* ray_d,
                                                    float* out_t, uint32_t* out_id, uint32_t* fetch_ctr,
@@ -1517,6 +1541,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     float t_max = 0.0f;
     int seg = 0;
     uint32_t xm[4] = {kNoMat, kNoMat, kNoMat, kNoMat};   // dielectric rows crossed (adjoint)
+    TravCount tc;   // counting variants only
 
     // SDF clusters, once the analytic part of the best hit is final
     auto sdf_pass = [&]() {
@@ -1535,9 +1560,13 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         ny = -ro.y * inv.y;
         nz = -ro.z * inv.z;
         b = Best{kShadow ? fminf(t_max, 1e30f) : 1e30f, 0u, kMiss};   // shadow: bounded as in transmittance_from
-        const uint32_t linear = Sp->linear_count;
+        const uint32_t linear = Sp->wide_linear;
         const float4* pg = Sp->prim_geo;
         const uint32_t* pty = Sp->prim_type;
+        if (kCount) {
+            tc.seg += 1;
+            tc.linear += linear;
+        }
         for (uint32_t i = 0; i < linear; ++i) {
             const float t = isect_geo(__ldg(pty + i), __ldg(pg + i), ro, rd);
             if (t > 1e-3f && better(t, i, b)) {
@@ -1617,7 +1646,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 if (__popc(idle) >= kRefillLanes) break;
             }
             if (!want) continue;
-            if (++iters > kTraverseCap) {
+            if (++iters > Sp->trav_cap) {
                 atomicOr(Sp->err, 1u);
                 sp = 0;
                 continue;
@@ -1625,6 +1654,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
             --sp;
             const uint2 top = st[sp];
             const uint32_t code = top.x;
+            if (kCount) tc.pop += 1;
             if (__uint_as_float(top.y) > b.t) continue;
             if (code & kLeafBit) {
                 leaf = code;
@@ -1633,7 +1663,11 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
             float dk[4];
             uint32_t ck[4];
             const int nh = wide_children(nodes, code, inv, nx, ny, nz, b.t, dk, ck);
-            if (sp + nh > kPStack) {
+            if (kCount) {
+                tc.nodes += 1;
+                tc.push += uint32_t(nh);
+            }
+            if (sp + nh > Sp->stack_cap) {
                 atomicOr(Sp->err, 2u);
                 sp = 0;
                 continue;
@@ -1645,6 +1679,11 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         }
         // leaf phase
         if (active && leaf != 0u) {
+            if (kCount) {
+                const uint32_t cnt = ((leaf >> 28) & 7u) + 1u;
+                if (phase == 1) tc.aprims += cnt;
+                else tc.tris += cnt;
+            }
             if (phase == 1) wide_leaf<false>(*Sp, leaf, ro, rd, b, 0u);
             else wide_leaf<true>(*Sp, leaf, ro, rd, b, 0x80000000u);
             leaf = 0u;
@@ -1701,6 +1740,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
             }
         }
     }
+    if (kCount && S0->tcount) tcount_flush(S0->tcount + (kShadow ? 8 : 0), tc);
 }
 
 }  // namespace ptd

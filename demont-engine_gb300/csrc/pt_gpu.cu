@@ -31,6 +31,8 @@
 #include "pt_device.cuh"
 #include "bvh_build.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
@@ -1098,26 +1100,28 @@ __global__ void __launch_bounds__(kThreads, 4) k_shadow(DScene S, DPaths P, int 
 // persistent closest hit for a queue of rays (extension rays or first shadow segments)
 // (kProc false: the procedural SDF walker compiled out, for launches whose scenes
 // hold no procedural cluster in use; it keeps the hot traversal loop lean)
-template <bool kB, bool kProc = true>
+// (kCount: the counting variant of profiling mode 3, which also tallies nodes,
+// primitives and stack operations into S.tcount)
+template <bool kB, bool kProc = true, bool kCount = false>
 __global__ void __launch_bounds__(kThreads, 4) k_closest(const __grid_constant__ DScene S, Batch B,
                                                          const uint32_t* queue, const uint32_t* count,
                                                          const float4* ray_o, const float4* ray_d, float* out_t,
                                                          uint32_t* out_id, uint32_t* fetch_ctr,
                                                          unsigned long long* stat) {
     uint32_t done = 0;
-    persistent_closest<false, kB, false, kProc>(&S, ItemScenes{B.scenes, B.path_scene}, queue, *count, ray_o, ray_d, out_t,
+    persistent_closest<false, kB, false, kProc, kCount>(&S, ItemScenes{B.scenes, B.path_scene}, queue, *count, ray_o, ray_d, out_t,
                                   out_id, fetch_ctr, done, ShadowIO{});
     warp_add(stat, done);
 }
 
 // persistent transmittance: whole dielectric chains per lane (every segment
 // counted as a shadow segment)
-template <bool kB, bool kMats, bool kProc = true>
+template <bool kB, bool kMats, bool kProc = true, bool kCount = false>
 __global__ void __launch_bounds__(kThreads, kTransmitBlocks) k_transmit(const __grid_constant__ DScene S, Batch B, DPaths P,
                                                           int kmax, uint4* sh_mats) {
     uint32_t done = 0;
     const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax, sh_mats};
-    persistent_closest<true, kB, kMats, kProc>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
+    persistent_closest<true, kB, kMats, kProc, kCount>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
                                  nullptr, P.cnt + 3, done, io);
     warp_add(P.stat + 1, done);
 }
@@ -1374,6 +1378,7 @@ struct pt_gpu_ctx {
     uint32_t sdf_count = 0;
     bool sdf_proc_any = false;   // some cluster holds a procedural op (5-9)
     DBuf<uint32_t> err_word;
+    uint32_t dbg_trav_cap = 0, dbg_stack_cap = 0;   // pt_gpu_set_debug_limits (0 = defaults)
     // target
     uint32_t W = 0, H = 0;
     DBuf<float4> accum;
@@ -1383,6 +1388,7 @@ struct pt_gpu_ctx {
     DBuf<uint32_t> seed, state, hit_id, shmask, q0, q1, sq, cnt;
     DBuf<float> hit_t;
     DBuf<unsigned long long> stat;
+    DBuf<unsigned long long> tcount;   // traversal counters (profiling mode 3), 16 entries
     uint32_t wave_frames_override = 0;
     // wide SAH trees built on the device at upload
     int traversal = 0;   // 0 wide (default), 1 reference BVHs
@@ -1417,7 +1423,8 @@ struct pt_gpu_ctx {
     pt_gpu_ctx* d_batch_scene = nullptr;
     std::vector<PtBatchView> d_batch_views;
     PtStats stats{};
-    int profile = 0;            // 0 off, 1 events on the overlapped schedule, 2 events, stages serial
+    int profile = 0;            // 0 off, 1 events on the overlapped schedule, 2 events, stages serial,
+                                // 3 as 2 with the counting traversal variants
     std::vector<cudaEvent_t> ev_pool;
 };
 
@@ -1426,6 +1433,31 @@ namespace {
 int set_err(pt_gpu_ctx* c, int code, const std::string& m) {
     if (c) c->err = m;
     return code;
+}
+
+// NVTX range over a scope: a render's waves, samples, bounces and stages show
+// up as named ranges in Nsight tools (ncu --nvtx --nvtx-include "bounce 0/"
+// selects one bounce's kernels); without a tool attached a push or pop is a
+// no-op call.
+struct Nvtx {
+    explicit Nvtx(const char* name) { nvtxRangePushA(name); }
+    Nvtx(const char* fmt, uint32_t a) {
+        char b[48];
+        std::snprintf(b, sizeof(b), fmt, a);
+        nvtxRangePushA(b);
+    }
+    ~Nvtx() { nvtxRangePop(); }
+    Nvtx(const Nvtx&) = delete;
+    Nvtx& operator=(const Nvtx&) = delete;
+};
+
+// Message for a traversal error word (bit 0: a query ran into the iteration
+// cap; bit 1: a wide-tree walk needed more stack entries than allowed).
+std::string traversal_error(uint32_t w) {
+    std::string m;
+    if (w & 1u) m += "traversal iteration cap reached (malformed BVH?)";
+    if (w & 2u) m += std::string(m.empty() ? "" : "; ") + "traversal stack overflow (tree deeper than the stack)";
+    return m.empty() ? "traversal error" : m;
 }
 
 #define CK(call)                                                                          \
@@ -1524,6 +1556,9 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     S.moon_w = c->moon_w;
     S.moon_h = c->moon_h;
     S.err = c->err_word.p;
+    S.trav_cap = c->dbg_trav_cap ? c->dbg_trav_cap : kTraverseCap;
+    S.stack_cap = c->dbg_stack_cap ? int(c->dbg_stack_cap) : kPStack;
+    S.tcount = c->tcount.p;
     S.use_wide = (c->traversal == 0) ? 1u : 0u;
     S.a_wide = (S.use_wide && c->a_wide) ? 1u : 0u;
     S.t_wide = (S.use_wide && c->t_wide) ? 1u : 0u;
@@ -1533,9 +1568,6 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     S.t4 = c->t4.p;
     S.tri4 = c->tri4.p;
     if (prm) {
-        // a linear-scan request over prims uploaded with a BVH changes the
-        // reference test order: use the reference walk for that dispatch
-        if (prm->bvh_params[1] == 0u && c->bvh_nodes != 0u) S.a_wide = 0u;
         // the push tail decides what the kernel walks (bvh_params), as in the reference
         S.linear_count = prm->bvh_params[0];
         S.bvh_nodes = prm->bvh_params[1];
@@ -1551,6 +1583,12 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
         S.sdf_proc = min(prm->sdf_procedural_ops, 2u);
         S.sdf_nmode = prm->sdf_params_f[3] != 0.0f ? 1u : 0u;
     }
+    // Without an analytic BVH in the dispatch the reference tests every record
+    // linearly, in record order, with no box in front of it; far from a sphere
+    // its float intersection cancels badly and can report hits that a box test
+    // would cull, so the wide-tree kernels then scan the records too.
+    if (S.bvh_nodes == 0u) S.a_wide = 0u;
+    S.wide_linear = (S.bvh_nodes == 0u) ? S.prim_count : S.linear_count;
     return S;
 }
 
@@ -1797,7 +1835,7 @@ int build_wide_prims(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref
     ctx->a_wide = false;
     ctx->a4_count = 0;
     const uint32_t nf = ctx->prim_count - ctx->linear_count;
-    if (nf == 0) return PT_OK;
+    if (nf == 0 || n_ref == 0) return PT_OK;   // no reference BVH: the records are scanned linearly
     std::vector<uint32_t> rank;
     if (!ptb::ref_ranks(ref_nodes, n_ref, nf, 32, rank)) return PT_OK;
     DBuf<float4> blo, bhi;
@@ -1867,6 +1905,8 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->stat, 4);
     if (rc) { *out = ctx; return rc; }
+    rc = dalloc(ctx, ctx->tcount, 16);
+    if (rc) { *out = ctx; return rc; }
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     *out = ctx;
@@ -1895,6 +1935,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     dfree(ctx->a4_meta);
     dfree(ctx->hit_t);
     dfree(ctx->stat);
+    dfree(ctx->tcount);
     if (ctx->b_graph) cudaGraphExecDestroy(ctx->b_graph);
     dfree(ctx->b_views);
     dfree(ctx->b_scenes);
@@ -2250,7 +2291,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
     P.q[0] = ctx->q0.p; P.q[1] = ctx->q1.p; P.sq = ctx->sq.p; P.cnt = ctx->cnt.p; P.stat = ctx->stat.p;
     // persistent wide-tree kernels need both wide trees (or no such part)
-    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
+    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.wide_linear) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
     const int gpers = ctx->sm_count * 4;
     const int gtr = ctx->sm_count * kTransmitBlocks;
@@ -2290,7 +2331,8 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     // The next bounce's closest-hit pass overlaps this bounce's shadow rays
     // (profiling mode 2 keeps the stages serial).  Profiling records an event
     // pair around every closest-hit and shadow launch on the stream it runs on.
-    const bool overlap = ctx->profile != 2;
+    const bool overlap = ctx->profile < 2;
+    const bool counting = ctx->profile == 3 && !proc && !adj;   // counting traversal variants
     const int ge = grid_for(ctx, size_t(fpw) * F.npix, 8);
     std::vector<std::pair<size_t, size_t>> ext_ev, sh_ev;
     size_t ev_i = 0;
@@ -2302,8 +2344,9 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         }
         if (persistent) {
             CK(cudaMemsetAsync(fetch, 0, 4, st));
-            (proc ? k_closest<false, true> : k_closest<false, false>)<<<gpers, kThreads, 0, st>>>(
-                S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id, fetch, P.stat);
+            (counting ? k_closest<false, false, true> : proc ? k_closest<false, true> : k_closest<false, false>)
+                <<<gpers, kThreads, 0, st>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id,
+                                             fetch, P.stat);
         } else if (S.use_wide) {
             k_extend<true><<<ge, kThreads, 0, st>>>(S, P, qs);
         } else {
@@ -2318,9 +2361,12 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
+    if (counting) CK(cudaMemsetAsync(ctx->tcount.p, 0, 16 * sizeof(unsigned long long), ctx->stream));
     ctx->stats = PtStats{};
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    const Nvtx nv_render(adj ? "pt_gpu adjoint replay" : "pt_gpu_render");
     for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
+        const Nvtx nv_wave("wave from frame %u", f0);
         const uint32_t nf = std::min(fpw, frames - f0);
         const uint32_t npaths = nf * F.npix;
         F.nframes = nf;
@@ -2329,11 +2375,13 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
         ctx->stats.kernel_launches += adj ? 1 : 2;   // init (+ accumulate)
         for (uint32_t s = 0; s < F.spp; ++s) {
+            const Nvtx nv_sample("sample %u", s);
             const size_t srec = size_t(s) * total_paths + size_t(f0) * F.npix;
             A.srec_base = srec;
             k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
+                const Nvtx nv_bounce("bounce %u", b);
                 const int qs = int(b & 1u);
                 if (b == 0u || !overlap) {
                     CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
@@ -2373,7 +2421,8 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                             <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
                                                                                      ctx->d_sh_mats.p);
                     else
-                        (proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
+                        (counting ? k_transmit<false, false, false, true>
+                                  : proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
                             <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
                 } else if (S.use_wide) {
                     k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
@@ -2425,7 +2474,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
     ctx->stats.extension_rays = st[0];
     ctx->stats.shadow_rays = st[1];
-    if (errw) return set_err(ctx, PT_ERR_KERNEL, "render: traversal iteration cap reached (malformed BVH?)");
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "render: " + traversal_error(errw));
     return PT_OK;
 }
 
@@ -2559,8 +2608,34 @@ int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out) {
 
 int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on) {
     if (!ctx) return PT_ERR_INVALID;
-    if (on < 0 || on > 2) return set_err(ctx, PT_ERR_INVALID, "set_profiling: on must be 0, 1 or 2");
+    if (on < 0 || on > 3) return set_err(ctx, PT_ERR_INVALID, "set_profiling: on must be 0, 1, 2 or 3");
     ctx->profile = on;
+    return PT_OK;
+}
+
+int pt_gpu_set_debug_limits(pt_gpu_ctx* ctx, uint32_t traverse_cap, uint32_t stack_entries) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (stack_entries > uint32_t(kPStack))
+        return set_err(ctx, PT_ERR_INVALID, "set_debug_limits: at most " + std::to_string(kPStack) +
+                                                " stack entries");
+    if (stack_entries != 0u && stack_entries < 4u)
+        return set_err(ctx, PT_ERR_INVALID, "set_debug_limits: at least 4 stack entries (one node's children)");
+    ctx->dbg_trav_cap = traverse_cap;
+    ctx->dbg_stack_cap = stack_entries;
+    return PT_OK;
+}
+
+int pt_gpu_get_traversal_stats(pt_gpu_ctx* ctx, PtTraversalStats* out) {
+    if (!ctx || !out) return PT_ERR_INVALID;
+    unsigned long long c[16];
+    CK(cudaMemcpy(c, ctx->tcount.p, sizeof(c), cudaMemcpyDeviceToHost));
+    *out = PtTraversalStats{};
+    uint64_t* ext = &out->ext_segments;
+    uint64_t* sh = &out->shadow_segments;
+    for (int k = 0; k < 7; ++k) {
+        ext[k] = c[k];
+        sh[k] = c[8 + k];
+    }
     return PT_OK;
 }
 
@@ -2613,7 +2688,7 @@ int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d
     if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("trace_closest: ") + cudaGetErrorString(e));
     uint32_t errw = 0;
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
-    if (errw) return set_err(ctx, PT_ERR_KERNEL, "trace_closest: traversal iteration cap reached");
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "trace_closest: " + traversal_error(errw));
     return PT_OK;
 }
 
@@ -2641,7 +2716,7 @@ int validate_view(pt_gpu_ctx* ctx, pt_gpu_ctx* sc, const PtBatchView& v, uint32_
         (prm->bvh_params[2] != 0u && prm->bvh_params[3] != sc->tri_nodes))
         return set_err(ctx, PT_ERR_INVALID, w + "mesh bvh_params disagree with its scene");
     if (prm->light_count != sc->light_count) return set_err(ctx, PT_ERR_INVALID, w + "light_count disagrees");
-    if (!sc->a_wide && sc->prim_count > sc->linear_count)
+    if (!sc->a_wide && sc->prim_count > sc->linear_count && sc->bvh_nodes != 0u)
         return set_err(ctx, PT_ERR_UNSUPPORTED, w + "scene has no wide analytic tree");
     if (!sc->t_wide && sc->tri_nodes > 0u)
         return set_err(ctx, PT_ERR_UNSUPPORTED, w + "scene has no wide mesh tree");
@@ -2987,7 +3062,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     ctx->stats.shadow_rays = tot_sh;
     uint32_t errw = 0;
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
-    if (errw) return set_err(ctx, PT_ERR_KERNEL, "batch: traversal iteration cap reached");
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "batch: " + traversal_error(errw));
     return PT_OK;
 }
 
@@ -3244,7 +3319,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     F.light_count = prm->light_count;
     sky_of(F, prm);
     const DScene S = make_scene(ctx, prm);
-    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.linear_count) &&
+    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.wide_linear) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
     const int gpers = ctx->sm_count * 4;
     const int gtr = ctx->sm_count * kTransmitBlocks;
@@ -3320,6 +3395,6 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
     ctx->stats.extension_rays = st[0];
     ctx->stats.shadow_rays = st[1];
-    if (errw) return set_err(ctx, PT_ERR_KERNEL, "render_noalloc: traversal iteration cap reached");
+    if (errw) return set_err(ctx, PT_ERR_KERNEL, "render_noalloc: " + traversal_error(errw));
     return PT_OK;
 }

@@ -253,14 +253,40 @@ int pt_gpu_tonemap(pt_gpu_ctx* ctx, float exposure, uint32_t op, int srgb_oetf, 
  *            run (the two event spans overlap, so each kernel's span includes
  *            time shared with the other);
  *   on == 2: the stages run one after another on one stream, so each span is
- *            the kernel's own device time (for per-kernel timing). */
+ *            the kernel's own device time (for per-kernel timing);
+ *   on == 3: as 2, with traversal kernels compiled to also count what they
+ *            touch (read with pt_gpu_get_traversal_stats; plain renders with
+ *            the wide trees and no procedural SDF cluster; results unchanged,
+ *            the counting itself costs time, so take kernel times from mode 2). */
 int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on);
+
+/* Traversal work of the last render in profiling mode 3, summed over its
+ * closest-hit (ext_*) and transmittance (shadow_*) launches on the 4-wide
+ * trees: segments traced, wide nodes whose four child boxes were tested,
+ * triangles and analytic primitives tested in leaves, linear (plane) records
+ * tested, and traversal-stack pushes and pops (8-byte entries). */
+typedef struct PtTraversalStats {
+    uint64_t ext_segments, ext_nodes, ext_tris, ext_aprims, ext_linear, ext_push, ext_pop;
+    uint64_t shadow_segments, shadow_nodes, shadow_tris, shadow_aprims, shadow_linear, shadow_push,
+             shadow_pop;
+} PtTraversalStats;
+int pt_gpu_get_traversal_stats(pt_gpu_ctx* ctx, PtTraversalStats* out);
 
 /* Traversal structure: 0 (default) = 4-wide SAH trees built on the device at
  * upload from the same primitives (hit ids and distances still follow the
  * reference's first-tested-wins order exactly, via per-primitive reference
  * ranks); 1 = walk the uploaded reference BVHs in the reference's own order. */
 int pt_gpu_set_traversal(pt_gpu_ctx* ctx, int mode);
+
+/* Failure-path testing: lower the per-query traversal iteration cap (default
+ * 4,194,304 loop iterations) and the wide-tree traversal stack (default and
+ * maximum 64 entries, minimum 4) so that a normal scene exceeds them.  A query
+ * that runs into either limit ends with the best hit found so far and sets the
+ * context's error word; the call then returns PT_ERR_KERNEL naming the limit,
+ * and the context stays usable.  0 restores a default.  The reference-order
+ * walk keeps the reference's own stack rule (children are dropped when its
+ * 32 / 64-entry stack is full, with no error). */
+int pt_gpu_set_debug_limits(pt_gpu_ctx* ctx, uint32_t traverse_cap, uint32_t stack_entries);
 
 typedef struct PtAccelInfo {
     uint32_t traversal;          /* current mode */

@@ -95,22 +95,31 @@ def test_accumulation_resumed_in_uneven_calls(pt, orc, dev):
 
 def test_stage_schedules_and_profiling_modes_give_the_same_image(pt, dev):
     """The overlapped schedule (next bounce's closest hits beside this bounce's
-    shadow rays), the same with events, and the serial schedule agree bit for
-    bit; the event modes report kernel times; other modes are refused."""
+    shadow rays), the same with events, the serial schedule and the serial
+    schedule with the counting traversal variants agree bit for bit; the event
+    modes report kernel times; the counting mode's segment counts equal the
+    render's own; other modes are refused."""
     s = pt.Scene().synth(1, seed=2, scale=0.02)
     W, H = 64, 40
     head, prm = s.push(W, H, frame_index=3, reset=1)
+    dev.set_traversal(0)
     dev.upload(s)
     dev.set_target(W, H)
     out = []
-    for mode in (0, 1, 2):
+    for mode in (0, 1, 2, 3):
         dev.set_profiling(mode)
         dev.render(head, prm, 3)
         out.append(dev.read_accum().copy())
         st = dev.stats()
         assert (st.extend_ms > 0 and st.shadow_ms > 0) == (mode != 0)
+    t = dev.traversal_stats()
     dev.set_profiling(0)
-    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
-    assert np.array_equal(out[0].view(np.uint32), out[2].view(np.uint32))
+    for k in (1, 2, 3):
+        assert np.array_equal(out[0].view(np.uint32), out[k].view(np.uint32))
+    assert t.ext_segments == st.extension_rays and t.shadow_segments == st.shadow_rays
+    assert t.ext_nodes > t.ext_segments and t.ext_tris > 0 and t.ext_aprims > 0
+    # every node tested was popped; every entry pushed (plus each walk's root) is popped once
+    assert t.ext_pop >= t.ext_nodes and t.ext_push <= t.ext_pop
+    assert t.shadow_nodes > 0 and t.shadow_pop >= t.shadow_nodes
     with pytest.raises(pt.PtError):
-        dev.set_profiling(3)
+        dev.set_profiling(4)

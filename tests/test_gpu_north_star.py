@@ -64,7 +64,9 @@ def test_converged_image_matches_the_fp64_oracle(pt, orc, dev, config, seed, W, 
 
 
 def render_rays(orc, s, W, H, bounce, n, crop=None):
-    """The first n rays bounce `bounce` traces, over consecutive frames."""
+    """n of the rays bounce `bounce` traces over consecutive frames (as many
+    frames as it takes to reach n), evenly spaced over them so that they cover
+    the whole image."""
     ros, rds, got, f = [], [], 0, 0
     while got < n:
         head, prm = s.push(W, H, frame_index=f, reset=1)
@@ -73,7 +75,8 @@ def render_rays(orc, s, W, H, bounce, n, crop=None):
         rds.append(rd)
         got += len(ro)
         f += 1
-    return np.concatenate(ros)[:n], np.concatenate(rds)[:n], head, prm
+    pick = np.linspace(0, got - 1, n).round().astype(np.int64)
+    return np.concatenate(ros)[pick], np.concatenate(rds)[pick], head, prm
 
 
 @pytest.fixture(scope="module")

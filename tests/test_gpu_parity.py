@@ -328,3 +328,46 @@ def test_batch_autotune_keeps_results(pt, dev):
     devs[k].set_target(w, h)
     devs[k].render(head, prm, 1)
     np.testing.assert_array_equal(batch.batch_read(1, w, h), devs[k].read_accum())
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_records_without_a_bvh_are_scanned_linearly_far_away(pt, orc, dev, mode):
+    """With fewer finite records than r_analytic_bvh_threshold there is no
+    analytic BVH and the reference tests every record linearly, in record order,
+    with no bounding box in front of it (shaders/PathTrace.slang:2402-2434).
+    From ~10^4 units away a sphere's float intersection cancels badly
+    (b^2 - (|oc|^2 - r^2) with |oc|^2 ~ 10^8) and reports hits for rays that
+    pass a few units outside it; a box test would cull those rays.  Both
+    traversal modes must return the oracle's hits bit for bit, these far hits
+    included (shadow rays from far ground points toward lights beside a sphere
+    meet exactly this case)."""
+    s = pt.Scene()
+    s.env(np.full((4, 8, 3), 0.1, np.float32))
+    s.plane(1, (0.0, 1.0, 0.0), 0.0, 0, (0.7, 0.7, 0.7))
+    s.sphere(10, 0.0, 1.0, 0.0, 1.0, 0, (0.85, 0.85, 0.85))
+    s.sphere(11, 3.0, 1.5, -2.0, 0.5, 1, (0.9, 0.9, 0.9))
+    head, prm = s.push(8, 8)
+    assert prm.bvh_params[1] == 0
+    rng = np.random.default_rng(17)
+    n = 1 << 14
+    ang = rng.uniform(0, 2 * np.pi, n)
+    dist = 10 ** rng.uniform(3, 4.3, n)
+    o = np.stack([dist * np.cos(ang), rng.uniform(1e-3, 0.05, n), dist * np.sin(ang)], 1)
+    tgt = np.array([0.0, 1.0, 0.0]) + rng.uniform(-6, 6, (n, 3)) * [1, 0.3, 1]
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    ro = np.zeros((n, 4), np.float32)
+    rd = np.zeros((n, 4), np.float32)
+    ro[:, :3], rd[:, :3] = o, d
+    o_hit, o_t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+    dev.set_traversal(mode)
+    dev.upload(s)
+    g_hit, g_t = dev.trace(ro, rd)
+    np.testing.assert_array_equal(g_hit, o_hit)
+    np.testing.assert_array_equal(g_t, o_t)
+    # some of these hits are the far-field artefact: the ray's true distance
+    # from the sphere centre exceeds the radius
+    c = np.array([0.0, 1.0, 0.0])
+    oc = c - ro[:, :3].astype(np.float64)
+    miss_dist = np.linalg.norm(oc - (oc * rd[:, :3]).sum(1, keepdims=True) * rd[:, :3], axis=1)
+    assert ((o_hit == 1) & (miss_dist > 1.05)).any()
