@@ -20,7 +20,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libdemont_pt.so")
+# the in-tree build; DEMONT_PT_LIB names another build of the same library
+LIB_PATH = os.environ.get("DEMONT_PT_LIB") or os.path.join(HERE, "_build", "libdemont_pt.so")
 
 PT_OK = 0
 ERRORS = {-1: "PT_ERR_INVALID", -2: "PT_ERR_CUDA", -3: "PT_ERR_OOM", -4: "PT_ERR_STATE",
@@ -75,7 +76,7 @@ class PtBatchView(ctypes.Structure):
 
 class PtBatchTuning(ctypes.Structure):
     _fields_ = [("persistent_blocks_per_sm", u32), ("stream_blocks_per_sm", u32), ("use_graph", u32),
-                ("reserved", u32)]
+                ("shade_threads", u32), ("camera_tile_w", u32), ("octant_grouping", u32), ("reserved", u32 * 2)]
 
 
 class PtLightTreeNode(ctypes.Structure):
@@ -145,6 +146,8 @@ SIGNATURES = {
     "pt_gpu_set_traversal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_get_traversal_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtTraversalStats)]),
     "pt_gpu_set_debug_limits": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
+    "pt_gpu_set_roulette_freeze": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pt_gpu_batch_tuning_gain": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_double), P(ctypes.c_double)]),
     "pt_gpu_get_accel_info": (ctypes.c_int, [ctypes.c_void_p, P(PtAccelInfo)]),
     "pt_gpu_batch_render": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p), u32, P(PtBatchView), u32, u32]),
     "pt_gpu_batch_read_accum": (ctypes.c_int, [ctypes.c_void_p, u32, P(f32)]),
@@ -574,6 +577,12 @@ class Device:
         (traversal_stats); False/0: off."""
         self._check(self.lib.pt_gpu_set_profiling(self.h, int(on)))
 
+    def set_roulette_freeze(self, mode):
+        """1: the next render records its roulette survival probabilities; 2:
+        later renders of the same shape reuse them; 0: off (finite differences
+        under roulette)."""
+        self._check(self.lib.pt_gpu_set_roulette_freeze(self.h, int(mode)))
+
     def set_debug_limits(self, traverse_cap=0, stack_entries=0):
         """Lower the traversal iteration cap / stack (failure-path tests); 0 = default."""
         self._check(self.lib.pt_gpu_set_debug_limits(self.h, traverse_cap, stack_entries))
@@ -616,9 +625,17 @@ class Device:
         self._check(self.lib.pt_gpu_batch_autotune(self.h, arr, len(scene_devs), va, len(views), ctypes.byref(t)))
         return t
 
-    def batch_set_tuning(self, persistent_blocks_per_sm=4, stream_blocks_per_sm=8, use_graph=1):
-        t = PtBatchTuning(persistent_blocks_per_sm, stream_blocks_per_sm, use_graph, 0)
+    def batch_set_tuning(self, persistent_blocks_per_sm=4, stream_blocks_per_sm=8, use_graph=1, shade_threads=512,
+                         camera_tile_w=8, octant_grouping=1):
+        t = PtBatchTuning(persistent_blocks_per_sm, stream_blocks_per_sm, use_graph, shade_threads, camera_tile_w,
+                          octant_grouping)
         self._check(self.lib.pt_gpu_batch_set_tuning(self.h, ctypes.byref(t)))
+
+    def batch_tuning_gain(self):
+        """(default ms, tuned ms) per frame from the last batch_autotune."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.pt_gpu_batch_tuning_gain(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     # ---- differentiable renders ----
     def materials(self, mats12):

@@ -1559,7 +1559,9 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         nx = -ro.x * inv.x;
         ny = -ro.y * inv.y;
         nz = -ro.z * inv.z;
-        b = Best{kShadow ? fminf(t_max, 1e30f) : 1e30f, 0u, kMiss};   // shadow: bounded as in transmittance_from
+        // shadow: bounded as in transmittance_from; extension rays: ray_d.w > 0
+        // is an initial closest distance (the trace probe's; renders write 0)
+        b = Best{kShadow ? fminf(t_max, 1e30f) : (t_max > 0.0f ? t_max : 1e30f), 0u, kMiss};
         const uint32_t linear = Sp->wide_linear;
         const float4* pg = Sp->prim_geo;
         const uint32_t* pty = Sp->prim_type;
@@ -1615,6 +1617,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                     const float4 o = ray_o[item], d = ray_d[item];
                     ro = v3(o);
                     rd = v3(d);
+                    if (!kShadow) t_max = d.w;
                     if (kShadow) {
                         t_max = o.w;
                         trans = v3(1.0f, 1.0f, 1.0f);

@@ -34,6 +34,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <initializer_list>
 #include <cstdio>
 #include <mutex>
 #include <cstring>
@@ -85,6 +86,9 @@ struct DFrame {
     float4 moon;
     float4 moon_extra;
     float4 sun_extra;
+    // launch-shape knobs (batched renders; results do not depend on them)
+    uint32_t tile_lw;        // camera tile width log2, one warp of 32 pixels per tile (0: 3, 8 x 4)
+    uint32_t octant_off;     // 1: the shading kernel's queue compaction does not group by ray octant
 };
 
 // Adjoint replay state (differentiable renders)
@@ -132,6 +136,11 @@ struct DPaths {
     float4* amb;       // gradient sky: skylight ambient of the bounce, added after its NEE terms
     float4* srad;      // differentiable renders: radiance of every sample [s * npaths + p], or null
     unsigned long long* stat;   // [0] extension rays, [1] shadow segments
+    // roulette survival probabilities held fixed (pt_gpu_set_roulette_freeze):
+    // [p * max_bounces + b] for this sample and wave, recorded (rr_mode 1) or
+    // read back (rr_mode 2); null when off
+    float* rr_frozen;
+    uint32_t rr_mode;
 };
 
 // ---------------------------------------------------------------------------
@@ -681,15 +690,19 @@ __global__ void kb_init_bins(uint32_t* bins, uint32_t nwords) {
     bins[i] = (w == 0u) ? 0u : ((w <= 3u || (w >= 7u && w <= 9u)) ? 0xFFFFFFFFu : 0u);
 }
 
-// Path slot -> pixel: slots run through 8x4 pixel tiles (one warp per tile)
-// in row-major tile order, so a warp's primary rays are spatially coherent.
-// Frames whose size is not a multiple of the tile fall back to row order.
+// Path slot -> pixel: slots run through tiles of 32 pixels (one warp per
+// tile; 8 x 4 unless the frame's tile_lw says otherwise) in row-major tile
+// order, so a warp's primary rays are spatially coherent.  Frames whose size is
+// not a multiple of the tile fall back to row order.  Each pixel's seed depends
+// only on its coordinates, so the mapping changes no result.
 __device__ __forceinline__ void slot_pixel(const DFrame& F, uint32_t pix, uint32_t& x, uint32_t& y) {
-    if ((F.W & 7u) == 0u && (F.H & 3u) == 0u) {
+    const uint32_t lw = F.tile_lw ? F.tile_lw : 3u;
+    const uint32_t tw_px = 1u << lw, th_px = 32u >> lw;
+    if ((F.W & (tw_px - 1u)) == 0u && (F.H % th_px) == 0u) {
         const uint32_t tile = pix >> 5, in = pix & 31u;
-        const uint32_t tw = F.W >> 3;
-        x = (tile % tw) * 8u + (in & 7u);
-        y = (tile / tw) * 4u + (in >> 3);
+        const uint32_t tw = F.W >> lw;
+        x = (tile % tw) * tw_px + (in & (tw_px - 1u));
+        y = (tile / tw) * th_px + (in >> lw);
     } else {
         x = pix % F.W;
         y = pix / F.W;
@@ -848,8 +861,8 @@ __device__ __forceinline__ V3 safe_div(V3 a, V3 b) {
     return v3(b.x > 0.0f ? a.x / b.x : 0.0f, b.y > 0.0f ? a.y / b.y : 0.0f, b.z > 0.0f ? a.z / b.z : 0.0f);
 }
 
-template <bool kB, bool kAdj, bool kProc = true>
-__global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__ DScene S0,
+template <bool kB, bool kAdj, bool kProc = true, int kSB = kShadeThreads>
+__global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0,
                                                      const __grid_constant__ DFrame F0, DPaths P, Batch B,
                                                      const __grid_constant__ Adj A, int qsel, uint32_t b) {
     const uint32_t n = P.cnt[qsel];
@@ -1035,6 +1048,11 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__
                 if (b >= F.rr_start) {
                     float pr = fmaxf(thr.x, fmaxf(thr.y, thr.z));
                     pr = clampf(pr, 0.05f, 1.0f);
+                    if (!kB && P.rr_frozen) {
+                        float* slot = P.rr_frozen + size_t(p) * F.maxb + b;
+                        if (P.rr_mode == 1u) *slot = pr;
+                        else pr = *slot;
+                    }
                     if (randf(seed) > pr) ended = true;
                     else thr = thr / pr;
                 }
@@ -1044,7 +1062,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(const __grid_constant__
             if (!ended) {
                 P.ray_o[p] = f4(ro, 0.0f);
                 P.ray_d[p] = f4(rd, 0.0f);
-                oct = (rd.x < 0.0f ? 1u : 0u) | (rd.y < 0.0f ? 2u : 0u) | (rd.z < 0.0f ? 4u : 0u);
+                oct = F.octant_off ? 0u : ((rd.x < 0.0f ? 1u : 0u) | (rd.y < 0.0f ? 2u : 0u) | (rd.z < 0.0f ? 4u : 0u));
             }
             P.thr[p] = f4(thr, prev_pdf);
             P.rad[p] = f4(rad, 0.0f);
@@ -1324,6 +1342,28 @@ __global__ void k_tonemap(const float4* accum, uint32_t n, float exposure, uint3
     out[i] = make_uchar4(uint8_t(unorm8(ldr.x)), uint8_t(unorm8(ldr.y)), uint8_t(unorm8(ldr.z)), 255);
 }
 
+// identity queue for the trace probe through the persistent kernel: q[i] = i,
+// then the count n and a zeroed fetch counter
+__global__ void k_probe_queue(uint32_t* q, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = i;
+    if (i == 0) {
+        q[n] = n;
+        q[n + 1] = 0u;
+    }
+}
+
+// triangle hits of the persistent kernel name the wide-leaf slot: report the
+// original triangle index (stored in the slot's first float4 .w)
+__global__ void k_probe_ids(DScene S, uint32_t n, uint32_t* hit, float* t) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t id = hit[i];
+    if (id != kMiss && (id & kTriBit) && !(id & kSdfBit)) id = kTriBit | __float_as_uint(S.tri4[3u * (id & ~kTriBit)].w);
+    hit[i] = id;
+    if (id == kMiss) t[i] = 0.0f;
+}
+
 __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint32_t n, uint32_t* hit,
                               float* t) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1408,9 +1448,13 @@ struct pt_gpu_ctx {
     std::vector<DFrame> b_views_h;
     cudaGraphExec_t b_graph = nullptr;
     std::vector<uint64_t> b_sig;
-    PtBatchTuning b_tune{4u, 8u, 1u, 0u};
+    PtBatchTuning b_tune{4u, 8u, 1u, 512u, 8u, 1u, 0u, 0u};
+    double b_tune_default_ms = 0.0, b_tune_best_ms = 0.0;   // last pt_gpu_batch_autotune
     // differentiable renders: the recorded forward and the replay's buffers
     DBuf<float4> d_srad, d_dldi;
+    int rr_freeze = 0;           // pt_gpu_set_roulette_freeze: 0 off, 1 record, 2 replay
+    DBuf<float> rr_buf;          // survival probabilities [sample][path][bounce]
+    uint32_t rr_meta[5] = {};    // W, H, frames, spp, max_bounces of the recording
     DBuf<double> d_grad;
     DBuf<uint4> d_sh_mats;
     bool d_valid = false;
@@ -1936,6 +1980,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     dfree(ctx->hit_t);
     dfree(ctx->stat);
     dfree(ctx->tcount);
+    dfree(ctx->rr_buf);
     if (ctx->b_graph) cudaGraphExecDestroy(ctx->b_graph);
     dfree(ctx->b_views);
     dfree(ctx->b_scenes);
@@ -2318,6 +2363,22 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         CK(cudaFuncSetAttribute(k_resolve<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     }
     P.srad = (dr.mode == RunMode::kRecord) ? ctx->d_srad.p : nullptr;
+    // fixed roulette probabilities: recorded by one plain render, read back by
+    // later ones of the same shape
+    const bool rr_fix = ctx->rr_freeze != 0 && dr.mode == RunMode::kRender && F.rr_start < F.maxb;
+    if (rr_fix) {
+        const uint32_t meta[5] = {F.W, F.H, frames, F.spp, F.maxb};
+        if (ctx->rr_freeze == 1) {
+            rc = dalloc(ctx, ctx->rr_buf, size_t(F.spp) * total_paths * F.maxb);
+            if (rc) return rc;
+            std::memcpy(ctx->rr_meta, meta, sizeof(meta));
+        } else if (std::memcmp(ctx->rr_meta, meta, sizeof(meta)) != 0 || !ctx->rr_buf.p) {
+            return set_err(ctx, PT_ERR_STATE,
+                           "render: the recorded roulette probabilities are for another size, frame count, "
+                           "spp or depth");
+        }
+    }
+    P.rr_mode = uint32_t(ctx->rr_freeze);
     Adj A{};
     if (adj) {
         A.srad = ctx->d_srad.p;
@@ -2378,6 +2439,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
             const Nvtx nv_sample("sample %u", s);
             const size_t srec = size_t(s) * total_paths + size_t(f0) * F.npix;
             A.srec_base = srec;
+            P.rr_frozen = rr_fix ? ctx->rr_buf.p + srec * F.maxb : nullptr;
             k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
@@ -2613,6 +2675,19 @@ int pt_gpu_set_profiling(pt_gpu_ctx* ctx, int on) {
     return PT_OK;
 }
 
+int pt_gpu_set_roulette_freeze(pt_gpu_ctx* ctx, int mode) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (mode < 0 || mode > 2) return set_err(ctx, PT_ERR_INVALID, "set_roulette_freeze: mode must be 0, 1 or 2");
+    if (mode == 2 && !ctx->rr_buf.p)
+        return set_err(ctx, PT_ERR_STATE, "set_roulette_freeze: nothing recorded (render once in mode 1)");
+    ctx->rr_freeze = mode;
+    if (mode == 0) {
+        dfree(ctx->rr_buf);
+        std::memset(ctx->rr_meta, 0, sizeof(ctx->rr_meta));
+    }
+    return PT_OK;
+}
+
 int pt_gpu_set_debug_limits(pt_gpu_ctx* ctx, uint32_t traverse_cap, uint32_t stack_entries) {
     if (!ctx) return PT_ERR_INVALID;
     if (stack_entries > uint32_t(kPStack))
@@ -2677,14 +2752,31 @@ int pt_gpu_trace_closest(pt_gpu_ctx* ctx, const float* ray_o, const float* ray_d
         }
         dro = bo.p; drd = bd.p; dh = bh.p; dt = bt.p;
     }
-    k_trace_probe<<<(n + 127) / 128, 128, 0, ctx->stream>>>(S, dro, drd, n, dh, dt);
+    // With the wide trees the probe runs the renders' own closest-hit kernel
+    // (persistent, dynamic ray fetch) over an identity queue; otherwise the
+    // per-ray walk of the chosen traversal.
+    const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.wide_linear) &&
+                            (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
+    DBuf<uint32_t> bq;
+    if (persistent) {
+        if (int rc = dalloc(ctx, bq, size_t(n) + 2)) {
+            dfree(bo); dfree(bd); dfree(bh); dfree(bt);
+            return rc;
+        }
+        k_probe_queue<<<(n + 255) / 256, 256, 0, ctx->stream>>>(bq.p, n);
+        k_closest<false, false><<<ctx->sm_count * 4, kThreads, 0, ctx->stream>>>(S, Batch{}, bq.p, bq.p + n, dro, drd,
+                                                                                 dt, dh, bq.p + n + 1, ctx->stat.p);
+        k_probe_ids<<<(n + 255) / 256, 256, 0, ctx->stream>>>(S, n, dh, dt);
+    } else {
+        k_trace_probe<<<(n + 127) / 128, 128, 0, ctx->stream>>>(S, dro, drd, n, dh, dt);
+    }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && !on_device) {
         e = cudaMemcpyAsync(hit_id, dh, size_t(n) * 4, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(t, dt, size_t(n) * 4, cudaMemcpyDeviceToHost, ctx->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    dfree(bo); dfree(bd); dfree(bh); dfree(bt);
+    dfree(bo); dfree(bd); dfree(bh); dfree(bt); dfree(bq);
     if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("trace_closest: ") + cudaGetErrorString(e));
     uint32_t errw = 0;
     CK(cudaMemcpy(&errw, ctx->err_word.p, 4, cudaMemcpyDeviceToHost));
@@ -2794,8 +2886,13 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
                 (proc ? k_shade<true, true, true> : k_shade<true, true, false>)
                     <<<ctx->sm_count * 2, kShadeThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs, b);
             } else {
-                (proc ? k_shade<true, false, true> : k_shade<true, false, false>)
-                    <<<(gstream + 1) / 2, kShadeThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+                // shading block: 512 threads (default) or 256 (autotuner); same grid in threads
+                if (ctx->b_tune.shade_threads == 256u)
+                    (proc ? k_shade<true, false, true, 256> : k_shade<true, false, false, 256>)
+                        <<<gstream, 256, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+                else
+                    (proc ? k_shade<true, false, true> : k_shade<true, false, false>)
+                        <<<(gstream + 1) / 2, kShadeThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
             }
             if (b + 1u < max_b) {
                 // fork: the next bounce's closest hits overlap this bounce's shadow rays
@@ -2830,8 +2927,11 @@ extern "C" {
 
 int pt_gpu_batch_set_tuning(pt_gpu_ctx* ctx, const PtBatchTuning* t) {
     if (!ctx || !t || t->persistent_blocks_per_sm < 1 || t->persistent_blocks_per_sm > 4 ||
-        t->stream_blocks_per_sm < 1 || t->stream_blocks_per_sm > 64)
-        return PT_ERR_INVALID;
+        t->stream_blocks_per_sm < 1 || t->stream_blocks_per_sm > 64 ||
+        (t->shade_threads != 256u && t->shade_threads != 512u) ||
+        (t->camera_tile_w != 4u && t->camera_tile_w != 8u && t->camera_tile_w != 16u && t->camera_tile_w != 32u) ||
+        t->octant_grouping > 1u || t->use_graph > 1u)
+        return ctx ? set_err(ctx, PT_ERR_INVALID, "batch_set_tuning: a knob is out of range") : PT_ERR_INVALID;
     ctx->b_tune = *t;
     if (ctx->b_graph) {
         cudaGraphExecDestroy(ctx->b_graph);
@@ -2957,6 +3057,8 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     uint32_t base_slot = 0;
     for (uint32_t i = 0; i < n_views; ++i) {
         ctx->b_views_h[i] = frame_of(views[i]);
+        ctx->b_views_h[i].tile_lw = uint32_t(__builtin_ctz(ctx->b_tune.camera_tile_w));
+        ctx->b_views_h[i].octant_off = ctx->b_tune.octant_grouping ? 0u : 1u;
         ctx->b_views_h[i].slot_base = base_slot;
         ctx->b_views_h[i].accum_base = ctx->b_accum_off[i];
         base_slot += fpw(i) * views[i].width * views[i].height;
@@ -3148,21 +3250,54 @@ int pt_gpu_batch_read_accum(pt_gpu_ctx* ctx, uint32_t view, float* host_rgba) {
 int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, const PtBatchView* views,
                           uint32_t n_views, PtBatchTuning* chosen) {
     if (!ctx) return PT_ERR_INVALID;
-    const PtBatchTuning cands[] = {{4u, 8u, 1u, 0u}, {3u, 8u, 1u, 0u}, {2u, 8u, 1u, 0u},
-                                   {4u, 4u, 1u, 0u}, {4u, 16u, 1u, 0u}};
-    double best = 1e30;
-    PtBatchTuning pick = cands[0];
-    for (const auto& c : cands) {
+    // one frame of the batch per candidate: a render that builds (captures) the
+    // wave, then a timed one; the best time wins
+    auto time_of = [&](const PtBatchTuning& c, double& ms) -> int {
         if (int rc = pt_gpu_batch_set_tuning(ctx, &c)) return rc;
-        if (int rc = pt_gpu_batch_render(ctx, scenes, n_scenes, views, n_views, 1)) return rc;   // capture
-        if (int rc = pt_gpu_batch_render(ctx, scenes, n_scenes, views, n_views, 1)) return rc;   // timed
-        if (ctx->stats.gpu_ms < best) {
-            best = ctx->stats.gpu_ms;
-            pick = c;
+        if (int rc = pt_gpu_batch_render(ctx, scenes, n_scenes, views, n_views, 1)) return rc;
+        if (int rc = pt_gpu_batch_render(ctx, scenes, n_scenes, views, n_views, 1)) return rc;
+        ms = ctx->stats.gpu_ms;
+        return PT_OK;
+    };
+    // coordinate descent from the default, one knob at a time: persistent
+    // grid, streaming grid, shading block, camera tile, octant grouping, graph
+    PtBatchTuning best{4u, 8u, 1u, 512u, 8u, 1u, 0u, 0u};
+    double best_ms = 0.0;
+    if (int rc = time_of(best, best_ms)) return rc;
+    const double default_ms = best_ms;
+    auto sweep = [&](uint32_t PtBatchTuning::*knob, std::initializer_list<uint32_t> values) -> int {
+        const PtBatchTuning base = best;
+        for (uint32_t v : values) {
+            if (base.*knob == v) continue;
+            PtBatchTuning c = base;
+            c.*knob = v;
+            double ms = 0.0;
+            if (int rc = time_of(c, ms)) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
         }
-    }
-    if (int rc = pt_gpu_batch_set_tuning(ctx, &pick)) return rc;
-    if (chosen) *chosen = pick;
+        return PT_OK;
+    };
+    int rc = 0;
+    if ((rc = sweep(&PtBatchTuning::persistent_blocks_per_sm, {3u, 2u})) ||
+        (rc = sweep(&PtBatchTuning::stream_blocks_per_sm, {4u, 16u})) ||
+        (rc = sweep(&PtBatchTuning::shade_threads, {256u})) ||
+        (rc = sweep(&PtBatchTuning::camera_tile_w, {4u, 16u, 32u})) ||
+        (rc = sweep(&PtBatchTuning::octant_grouping, {0u})) || (rc = sweep(&PtBatchTuning::use_graph, {0u})))
+        return rc;
+    if ((rc = pt_gpu_batch_set_tuning(ctx, &best))) return rc;
+    ctx->b_tune_default_ms = default_ms;
+    ctx->b_tune_best_ms = best_ms;
+    if (chosen) *chosen = best;
+    return PT_OK;
+}
+
+int pt_gpu_batch_tuning_gain(pt_gpu_ctx* ctx, double* default_ms, double* tuned_ms) {
+    if (!ctx || !default_ms || !tuned_ms) return PT_ERR_INVALID;
+    *default_ms = ctx->b_tune_default_ms;
+    *tuned_ms = ctx->b_tune_best_ms;
     return PT_OK;
 }
 

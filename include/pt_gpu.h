@@ -325,11 +325,16 @@ typedef struct PtBatchView {
     PtPathParams params;
 } PtBatchView;
 
+/* Launch shape of batched renders; no knob changes a result. */
 typedef struct PtBatchTuning {
     uint32_t persistent_blocks_per_sm;   /* grid of the persistent traversal kernels (1..4) */
-    uint32_t stream_blocks_per_sm;       /* grid cap of the streaming kernels (shade/resolve) */
-    uint32_t use_graph;                  /* 1: replay the captured wave graph */
-    uint32_t reserved;
+    uint32_t stream_blocks_per_sm;       /* grid cap of the streaming kernels (shade/resolve, 1..64) */
+    uint32_t use_graph;                  /* 1: replay the captured wave graph; 0: launch the wave directly */
+    uint32_t shade_threads;              /* shading-kernel block: 512 (default) or 256 threads */
+    uint32_t camera_tile_w;              /* pixels of a 32-pixel camera tile along x: 4, 8 (default), 16, 32 */
+    uint32_t octant_grouping;            /* 1: the shading kernel groups each block's next-bounce queue
+                                            entries by ray direction octant (default); 0: plain compaction */
+    uint32_t reserved[2];
 } PtBatchTuning;
 
 int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes,
@@ -337,11 +342,16 @@ int pt_gpu_batch_render(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_s
 int pt_gpu_batch_read_accum(pt_gpu_ctx* ctx, uint32_t view, float* host_rgba);
 int pt_gpu_batch_set_tuning(pt_gpu_ctx* ctx, const PtBatchTuning* tuning);
 int pt_gpu_batch_get_tuning(pt_gpu_ctx* ctx, PtBatchTuning* tuning);
-/* Times each candidate launch shape on one frame of this batch (the views'
- * accumulation is reset afterwards by the next render with reset_accum) and
- * keeps the fastest.  Writes the choice to *chosen (nullable). */
+/* Tunes every PtBatchTuning knob on this batch by coordinate descent from the
+ * default: one knob at a time (persistent grid, streaming grid, shading block,
+ * camera tile, octant grouping, graph replay), each candidate timed on one
+ * frame of the batch, the fastest kept.  The views' accumulation is reset
+ * afterwards by the next render with reset_accum.  Writes the choice to *chosen
+ * (nullable); pt_gpu_batch_tuning_gain reports the default's and the chosen
+ * shape's frame times from that search. */
 int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes,
                           const PtBatchView* views, uint32_t n_views, PtBatchTuning* chosen);
+int pt_gpu_batch_tuning_gain(pt_gpu_ctx* ctx, double* default_ms, double* tuned_ms);
 
 /* ---- differentiable render (extension: path-replay adjoint) ----
  * The reference has no derivative path; these two calls are shaped like the
@@ -382,6 +392,22 @@ int pt_gpu_batch_diff_backward(pt_gpu_ctx* ctx, const float* dl_di_rgba, int on_
                                double* grad_albedo, double* grad_emission);
 /* PtStats of the last backward replay (pt_gpu_get_stats keeps the forward's). */
 int pt_gpu_diff_get_backward_stats(pt_gpu_ctx* ctx, PtStats* out);
+
+/* Finite-difference checks under Russian roulette.  With common random numbers
+ * alone, a roulette decision u > p(theta) flips for a few samples when a
+ * material parameter moves by eps, and each flip changes its sample by O(1/p):
+ * the per-sample finite difference is noise.  mode 1 makes the next
+ * pt_gpu_render store every survival probability it draws against (per
+ * sample, path vertex); mode 2 makes later pt_gpu_render calls of the same
+ * width, height, frame count, spp and depth use those stored probabilities
+ * instead of computing them, so that renders at theta +- eps follow the same
+ * paths and each sample is a smooth function of the parameters -- the
+ * estimator whose gradient pt_gpu_diff_backward computes (it holds the
+ * probabilities fixed too).  The image of the recording render is unchanged.
+ * mode 0 (default) stops and frees the record.  Memory: 4 bytes per sample
+ * and bounce.  PT_ERR_STATE: mode 2 with nothing recorded, or a replaying
+ * render of another shape. */
+int pt_gpu_set_roulette_freeze(pt_gpu_ctx* ctx, int mode);
 
 /* ---- allocation-free render (no counterpart in the reference) ----
  * For callers that must not allocate device memory while rendering: an engine

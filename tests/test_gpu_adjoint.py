@@ -83,6 +83,80 @@ def test_adjoint_matches_central_differences(pt, dev):
     assert np.median(errs) < 2e-3
 
 
+def test_adjoint_matches_central_differences_under_roulette(pt, dev):
+    """Roulette from bounce 3, the differentiable configuration's estimator.
+    With common random numbers alone its per-sample finite differences are
+    flip noise (a decision u > p(theta) changes for a few samples).  The
+    nominal render records every survival probability and the renders at
+    theta +- eps reuse them (pt_gpu_set_roulette_freeze): the paths are then the
+    same and each sample is a smooth function of the parameters, whose gradient
+    is what the replay computes (it holds the probabilities fixed too)."""
+    W, H, F = 128, 96, 1
+    s, head, prm, pk, mats = _scene(pt, 0.5, 8, 3, W, H)
+    assert prm.rr_start == 3 and head.max_bounces > 3
+    dev.upload(s)
+    dev.set_target(W, H)
+    rng = np.random.default_rng(12)
+    target = rng.uniform(0.0, 0.3, (H, W, 3)).astype(np.float32)
+    dev.diff_forward(head, prm, F)
+    img = dev.read_accum()[..., :3].astype(np.float64)
+    ga, ge = dev.diff_backward((2.0 * (img - target)).astype(np.float32), mats.shape[0])
+    dev.render(head, prm, F)
+    plain = dev.read_accum().copy()
+    dev.set_roulette_freeze(1)
+    try:
+        dev.render(head, prm, F)                                 # records; the image is unchanged
+        assert np.array_equal(dev.read_accum().view(np.uint32), plain.view(np.uint32))
+        dev.set_roulette_freeze(2)
+        dev.render(head, prm, F)                                 # replays the same probabilities
+        assert np.array_equal(dev.read_accum().view(np.uint32), plain.view(np.uint32))
+
+        def loss(m):
+            dev.materials(m)
+            dev.render(head, prm, F)
+            return float(((dev.read_accum()[..., :3].astype(np.float64) - target) ** 2).sum())
+
+        eps = 1e-3
+        picks = [("a", int(k)) for k in np.argsort(-np.abs(ga).ravel())[:24]]
+        picks += [("e", int(k)) for k in np.argsort(-np.abs(ge).ravel())[:8]]
+        errs = []
+        for kind, k in picks:
+            r, c = divmod(k, 3)
+            col = c if kind == "a" else 4 + c
+            mp, mm = mats.copy(), mats.copy()
+            mp[r, col] += eps
+            mm[r, col] -= eps
+            fd = (loss(mp) - loss(mm)) / (2 * eps)
+            g = ga[r, c] if kind == "a" else ge[r, c]
+            errs.append(abs(g - fd) / max(abs(fd), 1e-12))
+            assert abs(g - fd) <= 0.02 * abs(fd), (kind, r, c, g, fd)
+        assert np.median(errs) < 2e-3
+    finally:
+        dev.set_roulette_freeze(0)
+        dev.materials(mats)
+
+
+def test_roulette_freeze_state_errors(pt, dev):
+    W, H = 32, 24
+    s, head, prm, pk, mats = _scene(pt, 0.1, 2, 3, W, H)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.set_roulette_freeze(0)
+    with pytest.raises(pt.PtError):               # nothing recorded
+        dev.set_roulette_freeze(2)
+    with pytest.raises(pt.PtError):
+        dev.set_roulette_freeze(3)
+    try:
+        dev.set_roulette_freeze(1)
+        dev.render(head, prm, 1)
+        dev.set_roulette_freeze(2)
+        with pytest.raises(pt.PtError):           # another frame count than recorded
+            dev.render(head, prm, 2)
+        dev.render(head, prm, 1)
+    finally:
+        dev.set_roulette_freeze(0)
+
+
 def test_adjoint_state_and_argument_errors(pt, dev):
     W, H = 32, 32
     s, head, prm, pk, mats = _scene(pt, 0.1, 1, 3, W, H)

@@ -322,12 +322,33 @@ def test_batch_autotune_keeps_results(pt, dev):
     scenes, devs, views = _batch_setup(pt)
     batch = pt.Device(0)
     t = batch.batch_autotune(devs, views)
-    assert 1 <= t.persistent_blocks_per_sm <= 4
+    assert 1 <= t.persistent_blocks_per_sm <= 4 and t.shade_threads in (256, 512)
+    assert t.camera_tile_w in (4, 8, 16, 32) and t.octant_grouping in (0, 1) and t.use_graph in (0, 1)
+    d_ms, t_ms = batch.batch_tuning_gain()
+    assert 0 < t_ms <= d_ms
     batch.batch_render(devs, views, frames=1)
     k, w, h, head, prm = views[1]
     devs[k].set_target(w, h)
     devs[k].render(head, prm, 1)
     np.testing.assert_array_equal(batch.batch_read(1, w, h), devs[k].read_accum())
+
+
+@pytest.mark.parametrize("tile,octants,shade", [(4, 1, 512), (16, 0, 256), (32, 1, 256)])
+def test_batch_launch_shapes_keep_results(pt, dev, tile, octants, shade):
+    """Every launch-shape knob the autotuner searches (camera tile, octant
+    grouping of the queue, shading block) leaves each view bit-identical to its
+    plain render."""
+    scenes, devs, views = _batch_setup(pt)
+    batch = pt.Device(0)
+    batch.batch_set_tuning(3, 4, 1, shade, tile, octants)
+    batch.batch_render(devs, views, frames=1)
+    for i, (k, w, h, head, prm) in enumerate(views):
+        devs[k].set_target(w, h)
+        devs[k].render(head, prm, 1)
+        np.testing.assert_array_equal(batch.batch_read(i, w, h), devs[k].read_accum(), err_msg=f"view {i}")
+    with pytest.raises(pt.PtError):
+        batch.batch_set_tuning(4, 8, 1, 384, 8, 1)
+    batch.close()
 
 
 @pytest.mark.parametrize("mode", MODES)
