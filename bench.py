@@ -350,7 +350,7 @@ def batched_bench(pt, steps=3):
                       "stream_blocks_per_sm": tune.stream_blocks_per_sm, "cuda_graph": bool(tune.use_graph),
                       "shade_threads": tune.shade_threads, "camera_tile": f"{tune.camera_tile_w}x{32 // tune.camera_tile_w}",
                       "octant_grouping": bool(tune.octant_grouping),
-                      "search": "coordinate descent from the default (4, 8, graph, 512, 8x4, grouping), "
+                      "search": "coordinate descent from the default (4, 8, graph, 512, 4x8, no grouping), "
                                 "one frame of the batch per candidate",
                       "default_ms_per_frame": default_ms, "tuned_ms_per_frame": tuned_ms,
                       "tuned_over_default": default_ms / tuned_ms if tuned_ms > 0 else None},

@@ -626,7 +626,7 @@ class Device:
         return t
 
     def batch_set_tuning(self, persistent_blocks_per_sm=4, stream_blocks_per_sm=8, use_graph=1, shade_threads=512,
-                         camera_tile_w=8, octant_grouping=1):
+                         camera_tile_w=4, octant_grouping=0):
         t = PtBatchTuning(persistent_blocks_per_sm, stream_blocks_per_sm, use_graph, shade_threads, camera_tile_w,
                           octant_grouping)
         self._check(self.lib.pt_gpu_batch_set_tuning(self.h, ctypes.byref(t)))

@@ -20,9 +20,9 @@
 // Extend and shadow are persistent closest-hit kernels over 4-wide SAH trees
 // (pt_device.cuh).  Once shade has written bounce b's next rays, extend of
 // bounce b+1 runs on a second stream beside shadow and resolve of bounce b.
-// Shade writes the next queue grouped by ray-direction octant within each
-// block, so the next extend's warps are more coherent.  A wave holds up to
-// ~64 M paths.
+// Shade writes the next queue in each block's path order (grouped by
+// ray-direction octant when a batch tuning asks for it); camera rays run in
+// 4 x 8 pixel tiles, one warp each.  A wave holds up to ~64 M paths.
 //
 // All float math is compiled with -fmad=false and follows the shader's
 // operation order, so the result equals a scalar restatement bit for bit.
@@ -53,9 +53,8 @@ constexpr int kThreads = 256;
 // 3 blocks of 256 per SM it needs no register spills (at 4 it spilled 230 bytes
 // per thread and ran 2% slower on the 1080p triangle scene).
 constexpr int kTransmitBlocks = 3;
-// k_shade runs blocks of 512: its queue compaction groups each block's survivors
-// by ray-direction octant, and larger groups give the next closest-hit pass more
-// coherent warps (+0.8% on the 1080p triangle scene against 256).
+// k_shade runs blocks of 512 (+0.8% on the 1080p triangle scene against 256
+// when its queue compaction grouped by octant; batched renders can pick 256).
 constexpr int kShadeThreads = 512;
 
 struct DFrame {
@@ -86,9 +85,9 @@ struct DFrame {
     float4 moon;
     float4 moon_extra;
     float4 sun_extra;
-    // launch-shape knobs (batched renders; results do not depend on them)
-    uint32_t tile_lw;        // camera tile width log2, one warp of 32 pixels per tile (0: 3, 8 x 4)
-    uint32_t octant_off;     // 1: the shading kernel's queue compaction does not group by ray octant
+    // launch-shape knobs (results do not depend on them; zero = the defaults)
+    uint32_t tile_lw;        // camera tile width log2, one warp of 32 pixels per tile (0: 2, 4 x 8)
+    uint32_t octant_on;      // 1: the shading kernel's queue compaction groups by ray octant
 };
 
 // Adjoint replay state (differentiable renders)
@@ -691,12 +690,13 @@ __global__ void kb_init_bins(uint32_t* bins, uint32_t nwords) {
 }
 
 // Path slot -> pixel: slots run through tiles of 32 pixels (one warp per
-// tile; 8 x 4 unless the frame's tile_lw says otherwise) in row-major tile
-// order, so a warp's primary rays are spatially coherent.  Frames whose size is
-// not a multiple of the tile fall back to row order.  Each pixel's seed depends
-// only on its coordinates, so the mapping changes no result.
+// tile; 4 x 8 unless the frame's tile_lw says otherwise: +0.6% on the 1080p
+// triangle scene against 8 x 4) in row-major tile order, so a warp's primary
+// rays are spatially coherent.  Frames whose size is not a multiple of the
+// tile fall back to row order.  Each pixel's seed depends only on its
+// coordinates, so the mapping changes no result.
 __device__ __forceinline__ void slot_pixel(const DFrame& F, uint32_t pix, uint32_t& x, uint32_t& y) {
-    const uint32_t lw = F.tile_lw ? F.tile_lw : 3u;
+    const uint32_t lw = F.tile_lw ? F.tile_lw : 2u;
     const uint32_t tw_px = 1u << lw, th_px = 32u >> lw;
     if ((F.W & (tw_px - 1u)) == 0u && (F.H % th_px) == 0u) {
         const uint32_t tile = pix >> 5, in = pix & 31u;
@@ -1062,7 +1062,7 @@ __global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0
             if (!ended) {
                 P.ray_o[p] = f4(ro, 0.0f);
                 P.ray_d[p] = f4(rd, 0.0f);
-                oct = F.octant_off ? 0u : ((rd.x < 0.0f ? 1u : 0u) | (rd.y < 0.0f ? 2u : 0u) | (rd.z < 0.0f ? 4u : 0u));
+                oct = F.octant_on ? ((rd.x < 0.0f ? 1u : 0u) | (rd.y < 0.0f ? 2u : 0u) | (rd.z < 0.0f ? 4u : 0u)) : 0u;
             }
             P.thr[p] = f4(thr, prev_pdf);
             P.rad[p] = f4(rad, 0.0f);
@@ -1072,12 +1072,16 @@ __global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0
             cont = !ended;
             }
         }
-        // compaction: survivors to the next queue grouped by the direction octant
-        // of their next ray within the block (a counting sort in shared memory),
-        // so that the closest-hit kernel's warps, which take consecutive queue
-        // slots, mostly hold rays of one octant; shadow rays to the shadow queue
-        // (two histograms used in turn: iteration it counts into s_hist[it & 1]
-        // and clears the other one for the next iteration, two barriers each)
+        // compaction: survivors to the next queue in the block's path order (a
+        // counting sort in shared memory; keeping that order makes the next
+        // kernels' path-record accesses more contiguous than per-warp atomic
+        // appends, which measured -3.3% on the 1080p triangle scene).  With
+        // octant grouping on (a batch tuning knob) the entries are grouped by the
+        // direction octant of their next ray, so that a closest-hit warp mostly
+        // holds rays of one octant; it measured +2.4% with the 8 x 4 camera tiles
+        // and -0.7% with the current build.  Shadow rays go to the shadow queue.
+        // (Two histograms used in turn: iteration it counts into s_hist[it & 1]
+        // and clears the other one for the next iteration, two barriers each.)
         const uint32_t hb = it & 1u;
         const uint32_t rank = cont ? atomicAdd(&s_hist[hb][oct], 1u) : 0u;
         __syncthreads();
@@ -1448,7 +1452,7 @@ struct pt_gpu_ctx {
     std::vector<DFrame> b_views_h;
     cudaGraphExec_t b_graph = nullptr;
     std::vector<uint64_t> b_sig;
-    PtBatchTuning b_tune{4u, 8u, 1u, 512u, 8u, 1u, 0u, 0u};
+    PtBatchTuning b_tune{4u, 8u, 1u, 512u, 4u, 0u, 0u, 0u};
     double b_tune_default_ms = 0.0, b_tune_best_ms = 0.0;   // last pt_gpu_batch_autotune
     // differentiable renders: the recorded forward and the replay's buffers
     DBuf<float4> d_srad, d_dldi;
@@ -3058,7 +3062,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     for (uint32_t i = 0; i < n_views; ++i) {
         ctx->b_views_h[i] = frame_of(views[i]);
         ctx->b_views_h[i].tile_lw = uint32_t(__builtin_ctz(ctx->b_tune.camera_tile_w));
-        ctx->b_views_h[i].octant_off = ctx->b_tune.octant_grouping ? 0u : 1u;
+        ctx->b_views_h[i].octant_on = ctx->b_tune.octant_grouping ? 1u : 0u;
         ctx->b_views_h[i].slot_base = base_slot;
         ctx->b_views_h[i].accum_base = ctx->b_accum_off[i];
         base_slot += fpw(i) * views[i].width * views[i].height;
@@ -3261,7 +3265,7 @@ int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n
     };
     // coordinate descent from the default, one knob at a time: persistent
     // grid, streaming grid, shading block, camera tile, octant grouping, graph
-    PtBatchTuning best{4u, 8u, 1u, 512u, 8u, 1u, 0u, 0u};
+    PtBatchTuning best{4u, 8u, 1u, 512u, 4u, 0u, 0u, 0u};
     double best_ms = 0.0;
     if (int rc = time_of(best, best_ms)) return rc;
     const double default_ms = best_ms;
@@ -3284,8 +3288,8 @@ int pt_gpu_batch_autotune(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n
     if ((rc = sweep(&PtBatchTuning::persistent_blocks_per_sm, {3u, 2u})) ||
         (rc = sweep(&PtBatchTuning::stream_blocks_per_sm, {4u, 16u})) ||
         (rc = sweep(&PtBatchTuning::shade_threads, {256u})) ||
-        (rc = sweep(&PtBatchTuning::camera_tile_w, {4u, 16u, 32u})) ||
-        (rc = sweep(&PtBatchTuning::octant_grouping, {0u})) || (rc = sweep(&PtBatchTuning::use_graph, {0u})))
+        (rc = sweep(&PtBatchTuning::camera_tile_w, {8u, 16u, 32u})) ||
+        (rc = sweep(&PtBatchTuning::octant_grouping, {1u})) || (rc = sweep(&PtBatchTuning::use_graph, {0u})))
         return rc;
     if ((rc = pt_gpu_batch_set_tuning(ctx, &best))) return rc;
     ctx->b_tune_default_ms = default_ms;

@@ -331,9 +331,9 @@ typedef struct PtBatchTuning {
     uint32_t stream_blocks_per_sm;       /* grid cap of the streaming kernels (shade/resolve, 1..64) */
     uint32_t use_graph;                  /* 1: replay the captured wave graph; 0: launch the wave directly */
     uint32_t shade_threads;              /* shading-kernel block: 512 (default) or 256 threads */
-    uint32_t camera_tile_w;              /* pixels of a 32-pixel camera tile along x: 4, 8 (default), 16, 32 */
+    uint32_t camera_tile_w;              /* pixels of a 32-pixel camera tile along x: 4 (default), 8, 16, 32 */
     uint32_t octant_grouping;            /* 1: the shading kernel groups each block's next-bounce queue
-                                            entries by ray direction octant (default); 0: plain compaction */
+                                            entries by ray direction octant; 0: path order (default) */
     uint32_t reserved[2];
 } PtBatchTuning;
 
