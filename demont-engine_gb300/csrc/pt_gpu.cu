@@ -87,6 +87,7 @@ struct DFrame {
     float4 sun_extra;
     // launch-shape knobs (results do not depend on them; zero = the defaults)
     uint32_t tile_lw;        // camera tile width log2, one warp of 32 pixels per tile (0: 2, 4 x 8)
+    uint32_t call_fi0;       // frame index of the call's first frame (it takes the push's jitter)
     uint32_t octant_on;      // 1: the shading kernel's queue compaction groups by ray octant
 };
 
@@ -749,6 +750,23 @@ __global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B,
     P.fsum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// The engine's sub-pixel jitter with the denoiser on: Halton bases 2 and 3 at
+// index frame_index % 16 + 1, minus 0.5 (src/engine/Engine.cpp:8241-8252).
+__device__ __forceinline__ float halton_ri(uint32_t i, uint32_t base) {
+    float f = 1.0f, r = 0.0f;
+    while (i > 0u) {
+        f /= float(base);
+        r += f * float(i % base);
+        i /= base;
+    }
+    return r;
+}
+__device__ __forceinline__ void halton_jitter(uint32_t frame_index, float& jx, float& jy) {
+    const uint32_t hi = (frame_index % 16u) + 1u;
+    jx = halton_ri(hi, 2u) - 0.5f;
+    jy = halton_ri(hi, 3u) - 0.5f;
+}
+
 // primary rays (shaders/PathTrace.slang:5722-5778)
 template <bool kB>
 __global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths, uint32_t s) {
@@ -773,8 +791,23 @@ __global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, ui
     uint32_t seed = P.seed[p];
     float jx, jy;
     if (V.denoiser != 0u && s == 0u) {
-        jx = V.jx;
-        jy = V.jy;
+        // sample 0 with the denoiser on: the push's sub-pixel jitter for the
+        // call's first frame; later frames take the engine's jitter of their
+        // own frame index, as back-to-back dispatches would
+        uint32_t f = 0;
+        if (kB) {
+            uint32_t xx, yy;
+            view_pixel(V, p, xx, yy, f);
+        } else {
+            f = p / F.npix;
+        }
+        const uint32_t fi = V.frame_index0 + f;
+        if (fi == V.call_fi0) {
+            jx = V.jx;
+            jy = V.jy;
+        } else {
+            halton_jitter(fi, jx, jy);
+        }
     } else {
         const float a = randf(seed);
         const float b = randf(seed);
@@ -2436,6 +2469,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         const uint32_t npaths = nf * F.npix;
         F.nframes = nf;
         F.frame_index0 = head->frame_index + f0;
+        F.call_fi0 = head->frame_index;
         const int gp = (npaths + 255) / 256;
         k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
         ctx->stats.kernel_launches += adj ? 1 : 2;   // init (+ accumulate)
@@ -2834,6 +2868,7 @@ DFrame frame_of(const PtBatchView& v) {
     F.npix = v.width * v.height;
     F.nframes = v.frames_per_wave == 0u ? 1u : v.frames_per_wave;
     F.frame_index0 = head->frame_index;
+    F.call_fi0 = head->frame_index;
     F.spp = head->spp == 0u ? 1u : head->spp;
     F.maxb = head->max_bounces;
     F.denoiser = head->denoiser_enabled;
@@ -3479,6 +3514,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         const uint32_t npaths = nf * F.npix;
         F.nframes = nf;
         F.frame_index0 = head->frame_index + f0;
+        F.call_fi0 = head->frame_index;
         const int gp = (npaths + 255) / 256;
         k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
         ctx->stats.kernel_launches += 2;

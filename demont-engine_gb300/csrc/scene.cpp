@@ -1573,6 +1573,22 @@ int pt_scene_fill_push(pt_scene* s, uint32_t width, uint32_t height, uint32_t fr
         head->spp = uint32_t(n);
     }
     head->denoiser_enabled = s->cvar("r_denoiser") != 0.0 ? 1u : 0u;
+    if (head->denoiser_enabled) {
+        // the engine's sub-pixel jitter: Halton bases 2 and 3 at index
+        // frame_index % 16 + 1, minus 0.5 (src/engine/Engine.cpp:8241-8252)
+        auto radical_inverse = [](uint32_t i, uint32_t base) {
+            float f = 1.0f, r = 0.0f;
+            while (i > 0u) {
+                f /= float(base);
+                r += f * float(i % base);
+                i /= base;
+            }
+            return r;
+        };
+        const uint32_t hi = (frame_index % 16u) + 1u;
+        head->halton_jitter[0] = radical_inverse(hi, 2u) - 0.5f;
+        head->halton_jitter[1] = radical_inverse(hi, 3u) - 0.5f;
+    }
     head->env_map_present = s->env_present ? 1u : 0u;
     head->env_intensity = float(s->cvar("r_env_intensity"));
     head->env_total_luminance = float(s->env_total);

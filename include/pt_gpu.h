@@ -54,7 +54,9 @@ typedef struct PtPushHead {
     uint32_t tlas_present;    /* must be 0: the hardware-RT branch has no CUDA counterpart */
     uint32_t prim_count;
     uint32_t spp;             /* samples per pixel per frame (0 is treated as 1) */
-    uint32_t denoiser_enabled;/* only its RNG effect is honoured: sample 0 uses halton_jitter */
+    uint32_t denoiser_enabled;/* only its RNG effect is honoured: sample 0 uses halton_jitter (a
+                                 multi-frame call gives its later frames the engine's jitter of
+                                 their frame index, Halton(2,3) of frame_index % 16 + 1 minus 0.5) */
     uint32_t env_map_present;
     float    halton_jitter[2];
     float    env_intensity;

@@ -345,6 +345,30 @@ template <class R> struct Tracer {
     float* cap_d = nullptr;
     uint32_t cap_bounce = 0;
     size_t cap_slot = 0;
+    // sub-pixel jitter of the current frame's sample 0 when the denoiser is on:
+    // the push's for the call's first frame, the engine's Halton(2,3) jitter of
+    // its own frame index for later ones (set_frame)
+    float frame_jx = 0.0f, frame_jy = 0.0f;
+    void set_frame(uint32_t frame_index) {
+        if (frame_index == P.frame_index) {
+            frame_jx = P.halton_jitter[0];
+            frame_jy = P.halton_jitter[1];
+            return;
+        }
+        // src/engine/Engine.cpp:8241-8252
+        auto radical_inverse = [](uint32_t i, uint32_t base) {
+            float f = 1.0f, r = 0.0f;
+            while (i > 0u) {
+                f /= float(base);
+                r += f * float(i % base);
+                i /= base;
+            }
+            return r;
+        };
+        const uint32_t hi = (frame_index % 16u) + 1u;
+        frame_jx = radical_inverse(hi, 2u) - 0.5f;
+        frame_jy = radical_inverse(hi, 3u) - 0.5f;
+    }
     const PtPackedScene& S;
     const PtPushHead& P;
     const PtPathParams& Q;
@@ -1571,8 +1595,8 @@ template <class R> struct Tracer {
     V3<R> sample_path(uint32_t px, uint32_t py, uint32_t s, uint32_t& seed) {
         R jx, jy;
         if (P.denoiser_enabled != 0u && s == 0u) {
-            jx = R(P.halton_jitter[0]);
-            jy = R(P.halton_jitter[1]);
+            jx = R(frame_jx);
+            jy = R(frame_jy);
         } else {
             const R a = randf<R>(seed);
             const R b = randf<R>(seed);
@@ -1770,6 +1794,7 @@ template <class R> struct Tracer {
 
     // frame radiance of one pixel: average of spp samples, sanitised (PathTrace.slang:7707-7734)
     V3<R> pixel(uint32_t px, uint32_t py, uint32_t frame_index) {
+        set_frame(frame_index);
         uint32_t seed = pcg_hash(px * 1973u + py * 9277u + frame_index * 26699u);
         const uint32_t n = (P.spp == 0u) ? 1u : P.spp;
         V3<R> fr{R(0), R(0), R(0)};
@@ -1864,6 +1889,7 @@ void capture_rays(const PtPackedScene& S, const PtPushHead& P, const PtPathParam
             if (r >= rows) break;
             const uint32_t y = y0 + r;
             for (uint32_t x = x0; x < x1; ++x) {
+                tr.set_frame(P.frame_index);
                 uint32_t seed = pcg_hash(x * 1973u + y * 9277u + P.frame_index * 26699u);
                 for (uint32_t s = 0; s < spp; ++s) {
                     tr.cap_slot = (size_t(r) * cw + (x - x0)) * spp + s;
@@ -1902,6 +1928,7 @@ void adjoint(const PtPackedScene& S, const PtPushHead& P, const PtPathParams& Q,
                 if (d[0] == 0.0f && d[1] == 0.0f && d[2] == 0.0f) continue;
                 for (int c = 0; c < 3; ++c) a.w[c] = double(d[c]) * scale;
                 for (uint32_t f = 0; f < frames; ++f) {
+                    tr.set_frame(P.frame_index + f);
                     uint32_t seed = pcg_hash(x * 1973u + y * 9277u + (P.frame_index + f) * 26699u);
                     for (uint32_t s = 0; s < spp; ++s) (void)tr.sample_path(x, y, s, seed);
                 }

@@ -172,3 +172,36 @@ def test_hdri_extraction_keeps_the_sun(pt):
     c = a["env_conditional"]
     assert (c[21, 41] <= c[21, 40])   # masked pixel adds no CDF mass
     assert c[50, 100] > c[50, 99]     # the dropped cluster stays in the CDF
+
+
+def _halton_jitter(frame_index):
+    """The engine's sub-pixel jitter with the denoiser on, in float32 as it
+    computes it (src/engine/Engine.cpp:8241-8252)."""
+    f32 = np.float32
+
+    def ri(i, base):
+        f, r = f32(1.0), f32(0.0)
+        while i > 0:
+            f = f32(f / f32(base))
+            r = f32(r + f32(f * f32(i % base)))
+            i //= base
+        return r
+
+    hi = frame_index % 16 + 1
+    return f32(ri(hi, 2) - f32(0.5)), f32(ri(hi, 3) - f32(0.5))
+
+
+def test_push_fills_the_engine_jitter_when_the_denoiser_is_on(pt):
+    s = pt.Scene().synth(0, seed=1)
+    head, _ = s.push(32, 32, frame_index=7)
+    assert head.denoiser_enabled == 0 and tuple(head.halton_jitter) == (0.0, 0.0)
+    s.set_cvar("r_denoiser", 1)
+    for fi in (0, 5, 15, 16, 1000):
+        head, _ = s.push(32, 32, frame_index=fi)
+        assert head.denoiser_enabled == 1
+        jx, jy = _halton_jitter(fi)
+        assert np.float32(head.halton_jitter[0]) == jx and np.float32(head.halton_jitter[1]) == jy
+    head, _ = s.push(32, 32, frame_index=0)
+    # frame 0 -> Halton index 1: 1/2 - 1/2 = 0 and float(1/3) - 1/2
+    assert np.float32(head.halton_jitter[0]) == np.float32(0.0)
+    assert np.float32(head.halton_jitter[1]) == np.float32(np.float32(1.0 / 3.0) - np.float32(0.5))

@@ -123,3 +123,37 @@ def test_stage_schedules_and_profiling_modes_give_the_same_image(pt, dev):
     assert t.shadow_nodes > 0 and t.shadow_pop >= t.shadow_nodes
     with pytest.raises(pt.PtError):
         dev.set_profiling(4)
+
+
+def test_denoiser_jitter_on_sample_zero(pt, orc, dev):
+    """With the denoiser on, sample 0 of a frame takes the push's sub-pixel
+    jitter instead of two random numbers (shaders/PathTrace.slang:5729-5736);
+    the engine pushes Halton(2,3) of frame_index % 16 + 1, minus 0.5, each
+    frame.  A three-frame call equals three single-frame calls with the
+    engine's pushes and the oracle, bit for bit, and a caller's own jitter is
+    honoured for a single frame."""
+    s = pt.Scene().synth(0, seed=7)
+    s.set_cvar("r_denoiser", 1)
+    s.set_cvar("r_spp", 2)
+    W, H = 40, 24
+    head, prm = s.push(W, H, frame_index=5, reset=1)
+    assert head.denoiser_enabled == 1 and head.halton_jitter[0] != 0.0
+    dev.set_traversal(0)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.render(head, prm, 3)
+    g = dev.read_accum().copy()
+    o, _ = orc.render(s.packed(), head, prm, W, H, 3)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+    for k in range(3):
+        h, p = s.push(W, H, frame_index=5 + k, reset=int(k == 0))
+        dev.render(h, p, 1)
+    assert np.array_equal(dev.read_accum().view(np.uint32), g.view(np.uint32))
+    mine = type(head).from_buffer_copy(head)
+    mine.halton_jitter[0], mine.halton_jitter[1] = 0.25, -0.125
+    dev.render(mine, prm, 1)
+    g1 = dev.read_accum().copy()
+    o1, _ = orc.render(s.packed(), mine, prm, W, H, 1)
+    assert np.array_equal(g1.view(np.uint32), o1.view(np.uint32))
+    dev.render(head, prm, 1)
+    assert not np.array_equal(g1, dev.read_accum())
