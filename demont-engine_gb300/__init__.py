@@ -66,7 +66,7 @@ class PtStats(ctypes.Structure):
 class PtAccelInfo(ctypes.Structure):
     _fields_ = [("traversal", u32), ("mesh_wide", u32), ("prims_wide", u32), ("mesh_wide_nodes", u32),
                 ("mesh_wide_depth", u32), ("mesh_binary_nodes", u32), ("prims_wide_nodes", u32),
-                ("reserved", u32), ("mesh_build_ms", ctypes.c_double)]
+                ("merged_wide_nodes", u32), ("mesh_build_ms", ctypes.c_double)]
 
 
 class PtBatchView(ctypes.Structure):

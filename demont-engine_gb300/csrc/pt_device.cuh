@@ -247,6 +247,7 @@ __device__ __forceinline__ V3 quat_rotate(float4 q, V3 v) {
 constexpr uint32_t kMatLambert = 0u, kMatMetal = 1u, kMatDielectric = 2u;
 constexpr uint32_t kMiss = 0xFFFFFFFFu;
 constexpr uint32_t kTriBit = 1u << 30;
+constexpr uint32_t kMergedTri = 1u << 29;   // with kTriBit: the slot is in the merged tree's triangle order
 constexpr uint32_t kTraverseCap = 1u << 22;   // loop-iteration cap per query (error word if hit)
 
 struct DScene {
@@ -302,6 +303,14 @@ struct DScene {
     const uint4* a4_meta;        // (record slot, type, tie key, 0)
     const float4* t4;            // mesh wide nodes
     const float4* tri4;          // triangles in wide-leaf order: (v0, orig id) (e1, material) (e2, tie rank)
+    // merged 4-wide tree over the triangles and the finite analytic records
+    // (record leaves flagged by bit 27 of the first-item field), with its own
+    // item orders; walked instead of the two trees when m_wide is set
+    uint32_t m_wide;
+    const float4* m4;
+    const float4* mtri4;
+    const float4* ma4_geo;
+    const uint4* ma4_meta;
     // traversal counters of the counting kernel variants (profiling mode 3), or null:
     // [0..7] extension segments, [8..15] shadow segments, each (segments, wide nodes
     // tested, triangles tested, analytic prims tested in wide leaves, linear prims
@@ -1114,17 +1123,22 @@ __device__ __forceinline__ float isect_geo(uint32_t type, float4 g, V3 ro, V3 rd
     return -1.0f;
 }
 
+// One leaf of a wide tree: triangles of `tri4` (kTri) or analytic records of
+// ageo / ameta.  first_mask selects the first-item field of the leaf code
+// (the merged tree keeps its record-leaf flag above it); triangle hits are
+// reported as kTriBit | id_tag | slot.
 template <bool kTri>
-__device__ __forceinline__ void wide_leaf(const DScene& S, uint32_t code, V3 ro, V3 rd, Best& b,
-                                          uint32_t key_base) {
-    const uint32_t first = code & 0x0FFFFFFFu;
+__device__ __forceinline__ void wide_leaf(const float4* tri4, const float4* ageo, const uint4* ameta, uint32_t code,
+                                          V3 ro, V3 rd, Best& b, uint32_t key_base,
+                                          uint32_t first_mask = 0x0FFFFFFFu, uint32_t id_tag = 0u) {
+    const uint32_t first = code & first_mask;
     const uint32_t cnt = ((code >> 28) & 7u) + 1u;
     for (uint32_t k = 0; k < cnt; ++k) {
         const uint32_t p = first + k;
         if (kTri) {
-            const float4 a = __ldg(S.tri4 + 3u * p);
-            const float4 bb = __ldg(S.tri4 + 3u * p + 1u);
-            const float4 c = __ldg(S.tri4 + 3u * p + 2u);
+            const float4 a = __ldg(tri4 + 3u * p);
+            const float4 bb = __ldg(tri4 + 3u * p + 1u);
+            const float4 c = __ldg(tri4 + 3u * p + 2u);
             const V3 v0 = v3(a), e1 = v3(bb), e2 = v3(c);
             const V3 pv = cross(rd, e2);
             const float det = dot(e1, pv);
@@ -1141,11 +1155,11 @@ __device__ __forceinline__ void wide_leaf(const DScene& S, uint32_t code, V3 ro,
             if (tt > 1e-3f && better(tt, key, b)) {
                 b.t = tt;
                 b.key = key;
-                b.id = kTriBit | p;
+                b.id = kTriBit | id_tag | p;
             }
         } else {
-            const float4 g = __ldg(S.a4_geo + p);
-            const uint4 m = __ldg(S.a4_meta + p);
+            const float4 g = __ldg(ageo + p);
+            const uint4 m = __ldg(ameta + p);
             const float t = isect_geo(m.y, g, ro, rd);
             if (t > 1e-3f && better(t, m.z, b)) {
                 b.t = t;
@@ -1270,7 +1284,7 @@ __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, 
             if (!__any_sync(__activemask(), leaf == 0u && sp > 0)) break;
         }
         if (leaf) {
-            wide_leaf<kTri>(S, leaf, ro, rd, b, key_base);
+            wide_leaf<kTri>(S.tri4, S.a4_geo, S.a4_meta, leaf, ro, rd, b, key_base);
             leaf = 0u;
         }
     }
@@ -1383,8 +1397,8 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
         s.emission = v3(0.0f, 0.0f, 0.0f);
         s.mid = kNoMat;
     } else if (h.id & kTriBit) {
-        const uint32_t slot = h.id & ~kTriBit;
-        const float4* T = S.t_wide ? S.tri4 : S.tri;
+        const uint32_t slot = h.id & ~(kTriBit | kMergedTri);
+        const float4* T = (h.id & kMergedTri) ? S.mtri4 : (S.t_wide ? S.tri4 : S.tri);
         const float4 b = __ldg(T + 3u * slot + 1u);
         const float4 c = __ldg(T + 3u * slot + 2u);
         s.normal = normalize(cross(v3(b), v3(c)));
@@ -1527,7 +1541,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     const uint32_t FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const DScene* Sp = S0;
-    bool has_a = false, has_t = false;
+    bool has_a = false, has_t = false, has_m = false;
     bool active = false, exhausted = false;
     uint32_t item = 0, leaf = 0u, iters = 0;
     int phase = 0, sp = 0;
@@ -1580,7 +1594,13 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         sp = 0;
         leaf = 0u;
         iters = 0;
-        if (has_a) {
+        if (has_m) {
+            // one walk over the merged tree (no SDF cluster in the dispatch)
+            phase = 5;
+            nodes = Sp->m4;
+            st[0] = make_uint2(0u, __float_as_uint(-3.0e38f));
+            sp = 1;
+        } else if (has_a) {
             phase = 1;
             nodes = Sp->a4;
             st[0] = make_uint2(0u, __float_as_uint(-3.0e38f));
@@ -1614,6 +1634,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                     if (kBatch) Sp = isc.table + isc.path_scene[kShadow ? item / 3u : item];
                     has_a = Sp->a_wide && Sp->prim_count > Sp->linear_count;
                     has_t = Sp->t_wide && Sp->tri_enabled != 0u && Sp->tri_nodes > 0u;
+                    has_m = Sp->m_wide && has_a && has_t;
                     const float4 o = ray_o[item], d = ray_d[item];
                     ro = v3(o);
                     rd = v3(d);
@@ -1682,13 +1703,21 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         }
         // leaf phase
         if (active && leaf != 0u) {
+            const bool rec_leaf = (phase == 1) || (phase == 5 && (leaf & 0x08000000u));
             if (kCount) {
                 const uint32_t cnt = ((leaf >> 28) & 7u) + 1u;
-                if (phase == 1) tc.aprims += cnt;
+                if (rec_leaf) tc.aprims += cnt;
                 else tc.tris += cnt;
             }
-            if (phase == 1) wide_leaf<false>(*Sp, leaf, ro, rd, b, 0u);
-            else wide_leaf<true>(*Sp, leaf, ro, rd, b, 0x80000000u);
+            if (phase == 5) {
+                if (rec_leaf) wide_leaf<false>(Sp->mtri4, Sp->ma4_geo, Sp->ma4_meta, leaf, ro, rd, b, 0u, 0x07FFFFFFu);
+                else wide_leaf<true>(Sp->mtri4, Sp->ma4_geo, Sp->ma4_meta, leaf, ro, rd, b, 0x80000000u, 0x07FFFFFFu,
+                                     kMergedTri);
+            } else if (phase == 1) {
+                wide_leaf<false>(Sp->tri4, Sp->a4_geo, Sp->a4_meta, leaf, ro, rd, b, 0u);
+            } else {
+                wide_leaf<true>(Sp->tri4, Sp->a4_geo, Sp->a4_meta, leaf, ro, rd, b, 0x80000000u);
+            }
             leaf = 0u;
         }
         // end of a tree

@@ -298,7 +298,8 @@ typedef struct PtAccelInfo {
     uint32_t mesh_wide_depth;
     uint32_t mesh_binary_nodes;  /* SAH binary nodes before the 4-wide collapse */
     uint32_t prims_wide_nodes;
-    uint32_t reserved;
+    uint32_t merged_wide_nodes;  /* nodes of the merged tree over triangles and analytic records (0: none);
+                                    renders walk it when both parts are present and no SDF cluster is */
     double   mesh_build_ms;      /* device build time of the mesh wide tree */
 } PtAccelInfo;
 int pt_gpu_get_accel_info(pt_gpu_ctx* ctx, PtAccelInfo* out);
