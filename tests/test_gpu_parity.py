@@ -392,3 +392,52 @@ def test_records_without_a_bvh_are_scanned_linearly_far_away(pt, orc, dev, mode)
     oc = c - ro[:, :3].astype(np.float64)
     miss_dist = np.linalg.norm(oc - (oc * rd[:, :3]).sum(1, keepdims=True) * rd[:, :3], axis=1)
     assert ((o_hit == 1) & (miss_dist > 1.05)).any()
+
+
+def _mixed_scene(pt, n=400, seed=31, with_sdf=False):
+    """Small spheres and small triangles interleaved in the same places, so that
+    the merged tree's SAH build makes leaves holding both kinds, which it splits
+    into a triangle leaf and a record leaf.  A plane is tested linearly."""
+    rng = np.random.default_rng(seed)
+    s = pt.Scene()
+    s.env(np.full((4, 8, 3), 0.3, np.float32))
+    s.plane(1, (0.0, 1.0, 0.0), 9.0, 0, (0.6, 0.6, 0.6))
+    c = rng.uniform(-8.0, 8.0, (n, 3))
+    for i in range(n):
+        s.sphere(100 + i, *c[i], float(rng.uniform(0.05, 0.3)), i % 3, (0.7, 0.5, 0.3))
+    pos = (c[:, None, :] + rng.uniform(-0.4, 0.4, (n, 1, 3)) + rng.uniform(-0.9, 0.9, (n, 3, 3))).reshape(-1, 3)
+    idx = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+    s.mesh(pos.astype(np.float32), idx)
+    if with_sdf:
+        s.sdf_leaf(500, 0, (0.8,), (0.0, 0.0, 0.0), 0, (0.8, 0.8, 0.8))
+    s.camera((0.0, 2.0, 24.0), 0.0, 0.0, 50.0)
+    return s
+
+
+@pytest.mark.parametrize("with_sdf", [False, True])
+def test_merged_tree_matches_the_reference(pt, orc, dev, with_sdf):
+    """Spheres in a BVH plus a mesh, no SDF cluster: the wide-tree kernels walk
+    one merged tree over both.  Its hits are the reference walk's (each item
+    keeps its reference tie rank), on rays and in renders; with an SDF cluster
+    the dispatch keeps the two trees (the cluster sits between them in the
+    reference's order) and is bit-exact as well."""
+    s = _mixed_scene(pt, with_sdf=with_sdf)
+    dev.set_traversal(0)
+    dev.upload(s)
+    info = dev.accel_info()
+    assert info.mesh_wide and info.prims_wide and info.merged_wide_nodes > 0
+    ro, rd = random_rays(1 << 14, -12.0, 12.0, 41)
+    head, prm = s.push(8, 8)
+    o_hit, o_t, _ = orc.trace(s.packed(), head, prm, ro, rd)
+    g_hit, g_t = dev.trace(ro, rd)
+    agree = g_hit == o_hit
+    assert agree.mean() >= 0.9999, agree.mean()
+    assert np.array_equal(g_t[agree], o_t[agree])
+    hit = o_hit != 0xFFFFFFFF
+    assert (hit & ((o_hit & (1 << 30)) != 0)).sum() > 100 and (hit & ((o_hit & (1 << 30)) == 0)).sum() > 100
+    W, H = 64, 48
+    dev.set_target(W, H)
+    head, prm = s.push(W, H, frame_index=3, reset=1)
+    dev.render(head, prm, 2)
+    o, _ = orc.render(s.packed(), head, prm, W, H, 2)
+    assert np.array_equal(dev.read_accum().view(np.uint32), o.view(np.uint32))
