@@ -60,7 +60,7 @@ class PtStats(ctypes.Structure):
                 ("paths", ctypes.c_uint64), ("frames", u32), ("waves", u32), ("gpu_ms", ctypes.c_double),
                 ("extend_ms", ctypes.c_double), ("shadow_ms", ctypes.c_double),
                 ("extend_launches", u32), ("shadow_launches", u32), ("kernel_launches", u32),
-                ("reserved", u32)]
+                ("graph_replays", u32)]
 
 
 class PtAccelInfo(ctypes.Structure):
@@ -147,6 +147,7 @@ SIGNATURES = {
     "pt_gpu_get_traversal_stats": (ctypes.c_int, [ctypes.c_void_p, P(PtTraversalStats)]),
     "pt_gpu_set_debug_limits": (ctypes.c_int, [ctypes.c_void_p, u32, u32]),
     "pt_gpu_set_roulette_freeze": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pt_gpu_set_render_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pt_gpu_batch_tuning_gain": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_double), P(ctypes.c_double)]),
     "pt_gpu_get_accel_info": (ctypes.c_int, [ctypes.c_void_p, P(PtAccelInfo)]),
     "pt_gpu_batch_render": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p), u32, P(PtBatchView), u32, u32]),
@@ -582,6 +583,11 @@ class Device:
         later renders of the same shape reuse them; 0: off (finite differences
         under roulette)."""
         self._check(self.lib.pt_gpu_set_roulette_freeze(self.h, int(mode)))
+
+    def set_render_graphs(self, on=True):
+        """Replay each render wave as a cached CUDA graph, or launch every
+        kernel directly (default); the images are the same bit for bit."""
+        self._check(self.lib.pt_gpu_set_render_graphs(self.h, int(bool(on))))
 
     def set_debug_limits(self, traverse_cap=0, stack_entries=0):
         """Lower the traversal iteration cap / stack (failure-path tests); 0 = default."""

@@ -34,6 +34,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <array>
 #include <initializer_list>
 #include <cstdio>
 #include <mutex>
@@ -141,6 +142,11 @@ struct DPaths {
     // read back (rr_mode 2); null when off
     float* rr_frozen;
     uint32_t rr_mode;
+    // single-view renders: [0] frame index of the wave's first frame, [1] of
+    // the call's first frame, [2] reset the accumulation at the wave's first
+    // frame; written by k_set_wave ahead of each wave, so that the wave's other
+    // launches (and a CUDA graph of them) do not depend on the frame index
+    const uint32_t* wave;
 };
 
 // ---------------------------------------------------------------------------
@@ -728,8 +734,14 @@ __device__ __forceinline__ void view_pixel(const DFrame& V, uint32_t p, uint32_t
     slot_pixel(V, local - f * V.npix, x, y);
 }
 
+__global__ void k_set_wave(uint32_t* wave, uint32_t frame0, uint32_t call_frame0, uint32_t reset) {
+    wave[0] = frame0;
+    wave[1] = call_frame0;
+    wave[2] = reset;
+}
+
 template <bool kB>
-__global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths, uint32_t frame0) {
+__global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npaths) return;
     uint32_t x, y, fidx;
@@ -744,7 +756,7 @@ __global__ void k_init_wave(const __grid_constant__ DFrame F, DPaths P, Batch B,
     } else {
         const uint32_t f = p / F.npix, pix = p - f * F.npix;
         slot_pixel(F, pix, x, y);
-        fidx = frame0 + f;
+        fidx = P.wave[0] + f;
     }
     P.seed[p] = pcg_hash(x * 1973u + y * 9277u + fidx * 26699u);
     P.fsum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -794,15 +806,17 @@ __global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, ui
         // sample 0 with the denoiser on: the push's sub-pixel jitter for the
         // call's first frame; later frames take the engine's jitter of their
         // own frame index, as back-to-back dispatches would
-        uint32_t f = 0;
+        uint32_t fi, call_fi;
         if (kB) {
-            uint32_t xx, yy;
+            uint32_t xx, yy, f;
             view_pixel(V, p, xx, yy, f);
+            fi = V.frame_index0 + f;
+            call_fi = V.call_fi0;
         } else {
-            f = p / F.npix;
+            fi = P.wave[0] + p / F.npix;
+            call_fi = P.wave[1];
         }
-        const uint32_t fi = V.frame_index0 + f;
-        if (fi == V.call_fi0) {
+        if (fi == call_fi) {
             jx = V.jx;
             jy = V.jy;
         } else {
@@ -1256,10 +1270,10 @@ __device__ __forceinline__ float4 accum_update(float4 a, float4 fs, float nspp, 
     return f4(avg, n_new);
 }
 
-__global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes, bool reset_first,
-                             float ema_in) {
+__global__ void k_accumulate(DFrame F, DPaths P, float4* accum, uint32_t nframes, float ema_in) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;   // path slot within a frame
     if (pix >= F.npix) return;
+    const bool reset_first = P.wave[2] != 0u;
     uint32_t x, y;
     slot_pixel(F, pix, x, y);
     const size_t out = size_t(y) * F.W + x;
@@ -1430,6 +1444,14 @@ template <class T> struct DBuf {
 
 }  // namespace
 
+// a cached CUDA graph of one plain-render wave (launch_wave_graph)
+struct WaveGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> key;   // the launch parameters it was captured with
+    std::array<uint32_t, 4> topo{};   // what fixes its node list
+    uint64_t used = 0;                // last use, for replacement
+};
+
 struct pt_gpu_ctx {
     int device = 0;
     int sm_count = 152;
@@ -1458,6 +1480,7 @@ struct pt_gpu_ctx {
     uint32_t sdf_count = 0;
     bool sdf_proc_any = false;   // some cluster holds a procedural op (5-9)
     DBuf<uint32_t> err_word;
+    DBuf<uint32_t> wave_vars;   // DPaths::wave
     // reference tie ranks of the wide trees' items (kept for the merged tree)
     DBuf<uint32_t> t_rank, a_rank;
     // merged 4-wide tree over the triangles and the finite analytic records
@@ -1494,6 +1517,10 @@ struct pt_gpu_ctx {
     std::vector<uint32_t> b_w, b_h;
     std::vector<DFrame> b_views_h;
     cudaGraphExec_t b_graph = nullptr;
+    // plain renders: cached wave graphs (launch_wave_graph)
+    int render_graphs = 0;
+    uint64_t graph_clock = 0;
+    WaveGraph wave_graphs[8];
     std::vector<uint64_t> b_sig;
     PtBatchTuning b_tune{4u, 8u, 1u, 512u, 4u, 0u, 0u, 0u};
     double b_tune_default_ms = 0.0, b_tune_best_ms = 0.0;   // last pt_gpu_batch_autotune
@@ -2092,6 +2119,8 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->cnt, 8);
     if (rc) { *out = ctx; return rc; }
+    rc = dalloc(ctx, ctx->wave_vars, 4);
+    if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->stat, 4);
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->tcount, 16);
@@ -2116,7 +2145,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     dfree(ctx->ldr);
     dfree(ctx->prim_mat);
     for (auto* b : {&ctx->prim_type, &ctx->seed, &ctx->state, &ctx->hit_id, &ctx->shmask, &ctx->q0,
-                    &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word})
+                    &ctx->q1, &ctx->sq, &ctx->cnt, &ctx->err_word, &ctx->wave_vars})
         dfree(*b);
     dfree(ctx->marg);
     dfree(ctx->cond);
@@ -2131,6 +2160,8 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     dfree(ctx->tcount);
     dfree(ctx->rr_buf);
     if (ctx->b_graph) cudaGraphExecDestroy(ctx->b_graph);
+    for (auto& gs : ctx->wave_graphs)
+        if (gs.exec) cudaGraphExecDestroy(gs.exec);
     dfree(ctx->b_views);
     dfree(ctx->b_scenes);
     dfree(ctx->b_view_base);
@@ -2419,6 +2450,88 @@ struct DiffRun {
     uint32_t nmat = 0;
 };
 
+// Replay of a plain render's wave as a CUDA graph (see render_waves).  The key
+// is every byte the wave's launches depend on; the structure (the node list)
+// depends on fewer fields, and a graph of the same structure is updated in
+// place with cudaGraphExecUpdate when the key differs.
+template <class Issue>
+int launch_wave_graph(pt_gpu_ctx* ctx, Issue& issue_wave, uint32_t f0, uint32_t nf, const DFrame& F, const DScene& S,
+                      DPaths P, float ema, bool rr_fix, bool proc, bool persistent, bool overlap) {
+    std::vector<unsigned char> key;
+    auto put = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), b, b + n);
+    };
+    // f0 fixes the roulette records' offset; the frame indices and the reset
+    // flag are read from P.wave at run time
+    const uint32_t flags[8] = {f0, nf, 0u, uint32_t(rr_fix), uint32_t(proc), uint32_t(persistent),
+                               uint32_t(overlap), uint32_t(ctx->sm_count)};
+    P.rr_frozen = nullptr;   // set per sample inside the wave
+    put(&F, sizeof(F));
+    put(&S, sizeof(S));
+    put(&P, sizeof(P));
+    put(flags, sizeof(flags));
+    put(&ema, sizeof(ema));
+    const void* ptrs[4] = {ctx->accum.p, ctx->rr_buf.p, ctx->wave_vars.p, ctx->err_word.p};
+    put(ptrs, sizeof(ptrs));
+    // the node list depends on the sample and bounce counts and the kernel
+    // variants; f0 keeps the waves of one call in graphs of their own (they
+    // would otherwise update each other in place on every call)
+    const std::array<uint32_t, 4> topo = {F.spp, F.maxb, f0,
+                                          uint32_t(proc) | uint32_t(persistent) << 1 | uint32_t(overlap) << 2 |
+                                              uint32_t(S.use_wide) << 3};
+    ++ctx->graph_clock;
+    for (auto& gs : ctx->wave_graphs)
+        if (gs.exec && gs.key == key) {
+            gs.used = ctx->graph_clock;
+            CK(cudaGraphLaunch(gs.exec, ctx->stream));
+            ctx->stats.graph_replays++;
+            return PT_OK;
+        }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int irc = issue_wave(f0, nf);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (irc) {
+        if (g) cudaGraphDestroy(g);
+        return irc;
+    }
+    if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("render capture: ") + cudaGetErrorString(e));
+    // a cached graph of the same structure: update it in place; else replace the
+    // least recently used slot
+    WaveGraph* slot = nullptr;
+    bool updated = false;
+    for (auto& gs : ctx->wave_graphs)
+        if (gs.exec && gs.topo == topo) {
+            slot = &gs;
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(gs.exec, g, &info) == cudaSuccess;
+            if (!updated) cudaGetLastError();
+            break;
+        }
+    if (!updated) {
+        if (!slot) {
+            slot = &ctx->wave_graphs[0];
+            for (auto& gs : ctx->wave_graphs)
+                if (gs.used < slot->used) slot = &gs;
+        }
+        if (slot->exec) cudaGraphExecDestroy(slot->exec);
+        slot->exec = nullptr;
+        e = cudaGraphInstantiate(&slot->exec, g, 0);
+        if (e != cudaSuccess) {
+            slot->exec = nullptr;
+            cudaGraphDestroy(g);
+            return set_err(ctx, PT_ERR_CUDA, std::string("render graph: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaGraphDestroy(g);
+    slot->key = std::move(key);
+    slot->topo = topo;
+    slot->used = ctx->graph_clock;
+    CK(cudaGraphLaunch(slot->exec, ctx->stream));
+    return PT_OK;
+}
+
 int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* prm, uint32_t frames,
                  const DiffRun& dr) {
     if (!ctx || !head || !prm) return PT_ERR_INVALID;
@@ -2486,6 +2599,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     P.hit_id = ctx->hit_id.p; P.shmask = ctx->shmask.p; P.sh_o = ctx->sh_o.p; P.sh_d = ctx->sh_d.p;
     P.sh_pre = ctx->sh_pre.p; P.sh_brdf = ctx->sh_brdf.p; P.sh_tr = ctx->sh_tr.p;
     P.q[0] = ctx->q0.p; P.q[1] = ctx->q1.p; P.sq = ctx->sq.p; P.cnt = ctx->cnt.p; P.stat = ctx->stat.p;
+    P.wave = ctx->wave_vars.p;
     // persistent wide-tree kernels need both wide trees (or no such part)
     const bool persistent = S.use_wide && (S.a_wide || S.prim_count == S.wide_linear) &&
                             (S.t_wide || S.tri_enabled == 0u || S.tri_nodes == 0u);
@@ -2577,23 +2691,17 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     ctx->stats = PtStats{};
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     const Nvtx nv_render(adj ? "pt_gpu adjoint replay" : "pt_gpu_render");
-    for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
-        const Nvtx nv_wave("wave from frame %u", f0);
-        const uint32_t nf = std::min(fpw, frames - f0);
+    // one wave's launches, on ctx->stream (the next bounce's closest hits forked to ctx->side)
+    auto issue_wave = [&](uint32_t f0, uint32_t nf) -> int {
         const uint32_t npaths = nf * F.npix;
-        F.nframes = nf;
-        F.frame_index0 = head->frame_index + f0;
-        F.call_fi0 = head->frame_index;
         const int gp = (npaths + 255) / 256;
-        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
-        ctx->stats.kernel_launches += adj ? 1 : 2;   // init (+ accumulate)
+        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths);
         for (uint32_t s = 0; s < F.spp; ++s) {
             const Nvtx nv_sample("sample %u", s);
             const size_t srec = size_t(s) * total_paths + size_t(f0) * F.npix;
             A.srec_base = srec;
             P.rr_frozen = rr_fix ? ctx->rr_buf.p + srec * F.maxb : nullptr;
             k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
-            ctx->stats.kernel_launches += 1 + 4 * F.maxb;   // camera + (extend, shade, shadow, resolve) per bounce
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const Nvtx nv_bounce("bounce %u", b);
                 const int qs = int(b & 1u);
@@ -2649,14 +2757,35 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                 else
                     k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{},
                                                                                                     Adj{}, qs, srec);
-                ctx->stats.extend_launches++;
-                ctx->stats.shadow_launches++;
             }
         }
         if (!adj)
-            k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf,
-                                                                       f0 == 0 && head->reset_accum != 0u,
-                                                                       prm->accum_ema_alpha);
+            k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf, prm->accum_ema_alpha);
+        return PT_OK;
+    };
+    // With render graphs on, plain renders replay each wave as a CUDA graph: a
+    // call that repeats an earlier one's launch parameters (every byte of them)
+    // replays its graph as it is; otherwise the wave is captured and the cached
+    // graph of the same structure is updated in place (or a new one
+    // instantiated).
+    const bool use_graph = ctx->render_graphs && ctx->profile == 0 && dr.mode == RunMode::kRender;
+    for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
+        const Nvtx nv_wave("wave from frame %u", f0);
+        const uint32_t nf = std::min(fpw, frames - f0);
+        const uint32_t npaths = nf * F.npix;
+        F.nframes = nf;
+        k_set_wave<<<1, 1, 0, ctx->stream>>>(ctx->wave_vars.p, head->frame_index + f0, head->frame_index,
+                                             f0 == 0 && head->reset_accum != 0u);
+        if (use_graph) {
+            if (int rc = launch_wave_graph(ctx, issue_wave, f0, nf, F, S, P, prm->accum_ema_alpha, rr_fix, proc,
+                                           persistent, overlap))
+                return rc;
+        } else if (int rc = issue_wave(f0, nf)) {
+            return rc;
+        }
+        ctx->stats.kernel_launches += (adj ? 2u : 3u) + F.spp * (1u + 4u * F.maxb);
+        ctx->stats.extend_launches += F.spp * F.maxb;
+        ctx->stats.shadow_launches += F.spp * F.maxb;
         ctx->stats.waves++;
         ctx->stats.paths += uint64_t(npaths) * F.spp;
     }
@@ -2853,6 +2982,12 @@ int pt_gpu_set_debug_limits(pt_gpu_ctx* ctx, uint32_t traverse_cap, uint32_t sta
     return PT_OK;
 }
 
+int pt_gpu_set_render_graphs(pt_gpu_ctx* ctx, int on) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->render_graphs = on != 0;
+    return PT_OK;
+}
+
 int pt_gpu_get_traversal_stats(pt_gpu_ctx* ctx, PtTraversalStats* out) {
     if (!ctx || !out) return PT_ERR_INVALID;
     unsigned long long c[16];
@@ -3015,7 +3150,7 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
     const int gstream = int(std::max<size_t>(1, std::min<size_t>((npaths + kThreads - 1) / kThreads,
                                                                  size_t(ctx->sm_count) * ctx->b_tune.stream_blocks_per_sm)));
     CK(cudaMemsetAsync(P.stat, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    k_init_wave<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths, 0u);
+    k_init_wave<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths);
     for (uint32_t s = 0; s < max_spp; ++s) {
         CK(cudaMemsetAsync(P.cnt, 0, 4, ctx->stream));
         k_camera<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths, s);
@@ -3581,6 +3716,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     P.sq = reinterpret_cast<uint32_t*>(take(4 * 3 * kNA_P));
     P.cnt = reinterpret_cast<uint32_t*>(take(32));
     P.stat = reinterpret_cast<unsigned long long*>(take(32));
+    P.wave = ctx->wave_vars.p;
     if (off > kNoAllocBytes) return set_err(ctx, PT_ERR_KERNEL, "render_noalloc: scratch layout overflow");
 
     DFrame F{};
@@ -3628,11 +3764,11 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         const uint32_t nf = std::min(fpw, frames - f0);
         const uint32_t npaths = nf * F.npix;
         F.nframes = nf;
-        F.frame_index0 = head->frame_index + f0;
-        F.call_fi0 = head->frame_index;
         const int gp = (npaths + 255) / 256;
-        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, head->frame_index + f0);
-        ctx->stats.kernel_launches += 2;
+        k_set_wave<<<1, 1, 0, ctx->stream>>>(ctx->wave_vars.p, head->frame_index + f0, head->frame_index,
+                                             f0 == 0 && head->reset_accum != 0u);
+        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths);
+        ctx->stats.kernel_launches += 3;
         for (uint32_t s = 0; s < F.spp; ++s) {
             k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;
@@ -3667,8 +3803,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                 ctx->stats.shadow_launches++;
             }
         }
-        k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, accum, nf,
-                                                                   f0 == 0 && head->reset_accum != 0u, prm->accum_ema_alpha);
+        k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, accum, nf, prm->accum_ema_alpha);
         ctx->stats.waves++;
         ctx->stats.paths += uint64_t(npaths) * F.spp;
     }

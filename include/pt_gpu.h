@@ -124,7 +124,8 @@ typedef struct PtStats {
     uint32_t extend_launches;
     uint32_t shadow_launches;
     uint32_t kernel_launches; /* every kernel this render call launched */
-    uint32_t reserved;
+    uint32_t graph_replays;   /* waves replayed from a cached CUDA graph unchanged
+                                 (pt_gpu_set_render_graphs); 0 when launched directly */
 } PtStats;
 
 /* ---- lifecycle (replaces Device::Create(BackendType), src/rhi/Device.cpp:20-48) ---- */
@@ -289,6 +290,19 @@ int pt_gpu_set_traversal(pt_gpu_ctx* ctx, int mode);
  * walk keeps the reference's own stack rule (children are dropped when its
  * 32 / 64-entry stack is full, with no error). */
 int pt_gpu_set_debug_limits(pt_gpu_ctx* ctx, uint32_t traverse_cap, uint32_t stack_entries);
+
+/* CUDA-graph replay of pt_gpu_render's waves (no counterpart in the
+ * reference; default off).  With it on and profiling off, each wave's launches
+ * are captured once into a CUDA graph and replayed by later calls with the same
+ * scene, view, size, sample and bounce counts; the frame index and the
+ * accumulation reset are read on the device, so a frame loop that advances
+ * frame_index replays the same graph.  A call that changes the launch
+ * parameters updates the cached graph in place.  Up to 8 graphs are cached per
+ * context.  The images are the same bit for bit either way.  Measured on the
+ * 256 x 256, 16 spp analytic scene: +5% at one frame per call, -2.4% at 64
+ * frames per call (the time between a wave's launches is the slowest rays'
+ * latency, not launch overhead), so direct launches stay the default. */
+int pt_gpu_set_render_graphs(pt_gpu_ctx* ctx, int on);
 
 typedef struct PtAccelInfo {
     uint32_t traversal;          /* current mode */
