@@ -133,7 +133,18 @@ struct DPaths {
     float4* sh_tr;     // transmittance result
     uint32_t* q[2];
     uint32_t* sq;
-    uint32_t* cnt;     // [0],[1] path queues, [2] shadow queue, [3] fetch counter
+    // Queue counters: a ring of 4 blocks of 4 words, block b & 3 for bounce b:
+    // [0] rays queued for the bounce (q[b & 1]), [1] shadow rays (sq), [2] the
+    // closest-hit kernel's fetch counter, [3] the transmittance kernel's.  A
+    // bounce's launches get cnt = its block, cnt_next = the next bounce's
+    // (k_shade appends the survivors there) and cnt_clear = block (b + 2) & 3,
+    // which k_shade zeroes for bounce b + 2: every launch of bounce b - 2 has
+    // finished by then and none that may run beside k_shade uses it.  k_camera
+    // (single-view renders) sets up block 0 and zeroes the rest, so a sample
+    // needs no memset of its own.
+    uint32_t* cnt;
+    uint32_t* cnt_next;
+    uint32_t* cnt_clear;
     float4* amb;       // gradient sky: skylight ambient of the bounce, added after its NEE terms
     float4* srad;      // differentiable renders: radiance of every sample [s * npaths + p], or null
     unsigned long long* stat;   // [0] extension rays, [1] shadow segments
@@ -783,7 +794,7 @@ __device__ __forceinline__ void halton_jitter(uint32_t frame_index, float& jx, f
 template <bool kB>
 __global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, uint32_t npaths, uint32_t s) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!kB && p == 0) P.cnt[0] = npaths;
+    if (!kB && p < 16u) P.cnt[p] = (p == 0u) ? npaths : 0u;   // the counter ring (P.cnt: block 0)
     bool live = p < npaths;
     const DFrame& V = (kB && live) ? B.views[B.path_view[p]] : F;
     if (kB && live && s >= V.spp) live = false;   // this view has fewer samples
@@ -843,7 +854,7 @@ __global__ void k_camera(const __grid_constant__ DFrame F, DPaths P, Batch B, ui
 
 template <bool kWide>
 __global__ void __launch_bounds__(kThreads) k_extend(DScene S, DPaths P, int qsel) {
-    const uint32_t n = P.cnt[qsel];
+    const uint32_t n = P.cnt[0];
     const uint32_t* q = P.q[qsel];
     uint32_t done = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -912,9 +923,10 @@ template <bool kB, bool kAdj, bool kProc = true, int kSB = kShadeThreads>
 __global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0,
                                                      const __grid_constant__ DFrame F0, DPaths P, Batch B,
                                                      const __grid_constant__ Adj A, int qsel, uint32_t b) {
-    const uint32_t n = P.cnt[qsel];
+    const uint32_t n = P.cnt[0];
     const uint32_t* q = P.q[qsel];
     uint32_t* qn = P.q[qsel ^ 1];
+    if (blockIdx.x == 0u && threadIdx.x < 4u) P.cnt_clear[threadIdx.x] = 0u;
     const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
     if (kAdj) adj_begin(A);
     __shared__ uint32_t s_hist[2][8], s_base[8], s_block;
@@ -1139,13 +1151,13 @@ __global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0
                 s_base[o] = tot;
                 tot += s_hist[hb][o];
             }
-            s_block = tot ? atomicAdd(P.cnt + (qsel ^ 1), tot) : 0u;
+            s_block = tot ? atomicAdd(P.cnt_next, tot) : 0u;
         }
         __syncthreads();
         if (cont) qn[s_block + s_base[oct] + rank] = p;
         for (int k = 0; k < 3; ++k) {
             const bool has = (shadow_mask >> k) & 1u;
-            const uint32_t ss = warp_push(P.cnt + 2, has);
+            const uint32_t ss = warp_push(P.cnt + 1, has);
             if (has) P.sq[ss] = 3u * p + uint32_t(k);
         }
     }
@@ -1154,7 +1166,7 @@ __global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0
 
 template <bool kWide>
 __global__ void __launch_bounds__(kThreads, 4) k_shadow(DScene S, DPaths P, int kmax) {
-    const uint32_t n = P.cnt[2];
+    const uint32_t n = P.cnt[1];
     uint32_t segs = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t e = P.sq[i];
@@ -1190,7 +1202,7 @@ __global__ void __launch_bounds__(kThreads, kTransmitBlocks) k_transmit(const __
                                                           int kmax, uint4* sh_mats) {
     uint32_t done = 0;
     const ShadowIO io{P.sh_o, P.sh_d, P.sh_tr, kmax, sh_mats};
-    persistent_closest<true, kB, kMats, kProc, kCount>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[2], P.sh_o, P.sh_d, nullptr,
+    persistent_closest<true, kB, kMats, kProc, kCount>(&S, ItemScenes{B.scenes, B.path_scene}, P.sq, P.cnt[1], P.sh_o, P.sh_d, nullptr,
                                  nullptr, P.cnt + 3, done, io);
     warp_add(P.stat + 1, done);
 }
@@ -1200,7 +1212,7 @@ __global__ void __launch_bounds__(kThreads, kTransmitBlocks) k_transmit(const __
 template <bool kB, bool kAdj>
 __global__ void k_resolve(const __grid_constant__ DScene S0, const __grid_constant__ DFrame F0, DPaths P, Batch B,
                           const __grid_constant__ Adj A, int qsel, size_t srec_base) {
-    const uint32_t n = P.cnt[qsel];
+    const uint32_t n = P.cnt[0];
     const uint32_t* q = P.q[qsel];
     const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
     if (kAdj) adj_begin(A);
@@ -2117,7 +2129,7 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
     CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     int rc = dalloc(ctx, ctx->err_word, 1);
     if (rc) { *out = ctx; return rc; }
-    rc = dalloc(ctx, ctx->cnt, 8);
+    rc = dalloc(ctx, ctx->cnt, 16);   // the counter ring (DPaths::cnt)
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->wave_vars, 4);
     if (rc) { *out = ctx; return rc; }
@@ -2450,6 +2462,15 @@ struct DiffRun {
     uint32_t nmat = 0;
 };
 
+// The path state with bounce b's queue counters (DPaths::cnt).
+DPaths bounce_paths(const DPaths& P, uint32_t b) {
+    DPaths Q = P;
+    Q.cnt = P.cnt + 4u * (b & 3u);
+    Q.cnt_next = P.cnt + 4u * ((b + 1u) & 3u);
+    Q.cnt_clear = P.cnt + 4u * ((b + 2u) & 3u);
+    return Q;
+}
+
 // Replay of a plain render's wave as a CUDA graph (see render_waves).  The key
 // is every byte the wave's launches depend on; the structure (the node list)
 // depends on fewer fields, and a graph of the same structure is updated in
@@ -2662,21 +2683,22 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     const int ge = grid_for(ctx, size_t(fpw) * F.npix, 8);
     std::vector<std::pair<size_t, size_t>> ext_ev, sh_ev;
     size_t ev_i = 0;
-    auto launch_extend = [&](cudaStream_t st, int qs, uint32_t* fetch) -> int {
+    auto launch_extend = [&](cudaStream_t st, uint32_t b) -> int {
         if (ctx->profile) {
             ext_ev.emplace_back(ev_i, ev_i + 1);
             CK(cudaEventRecord(pool_event(ctx, ev_i++), st));
             ++ev_i;
         }
+        const int qs = int(b & 1u);
+        const DPaths Pb = bounce_paths(P, b);
         if (persistent) {
-            CK(cudaMemsetAsync(fetch, 0, 4, st));
             (counting ? k_closest<false, false, true> : proc ? k_closest<false, true> : k_closest<false, false>)
-                <<<gpers, kThreads, 0, st>>>(S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id,
-                                             fetch, P.stat);
+                <<<gpers, kThreads, 0, st>>>(S, Batch{}, P.q[qs], Pb.cnt, P.ray_o, P.ray_d, P.hit_t, P.hit_id,
+                                             Pb.cnt + 2, P.stat);
         } else if (S.use_wide) {
-            k_extend<true><<<ge, kThreads, 0, st>>>(S, P, qs);
+            k_extend<true><<<ge, kThreads, 0, st>>>(S, Pb, qs);
         } else {
-            k_extend<false><<<ge, kThreads, 0, st>>>(S, P, qs);
+            k_extend<false><<<ge, kThreads, 0, st>>>(S, Pb, qs);
         }
         if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, ext_ev.back().second), st));
         return PT_OK;
@@ -2705,22 +2727,19 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const Nvtx nv_bounce("bounce %u", b);
                 const int qs = int(b & 1u);
+                const DPaths Pb = bounce_paths(P, b);
                 if (b == 0u || !overlap) {
-                    CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
-                    CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
-                    if (int rc = launch_extend(ctx->stream, qs, ctx->cnt.p + 3)) return rc;
+                    if (int rc = launch_extend(ctx->stream, b)) return rc;
                 } else {
                     // this bounce's closest hits were traced on the side stream
                     CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-                    CK(cudaMemsetAsync(ctx->cnt.p + (qs ^ 1), 0, 4, ctx->stream));
-                    CK(cudaMemsetAsync(ctx->cnt.p + 2, 0, 4, ctx->stream));
                 }
                 if (adj)
                     (proc ? k_shade<false, true, true> : k_shade<false, true, false>)
-                        <<<gadj / 2, kShadeThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, b);
+                        <<<gadj / 2, kShadeThreads, smem, ctx->stream>>>(S, F, Pb, Batch{}, A, qs, b);
                 else
                     (proc ? k_shade<false, false, true> : k_shade<false, false, false>)
-                        <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                        <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, Pb, Batch{},
                                                                                                   Adj{}, qs, b);
                 if (overlap && b + 1u < F.maxb) {
                     // fork: the next bounce's rays (written by k_shade) are traced
@@ -2728,7 +2747,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                     // neither the rays nor the hits
                     CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
                     CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-                    if (int rc = launch_extend(ctx->side, qs ^ 1, ctx->cnt.p + 4)) return rc;
+                    if (int rc = launch_extend(ctx->side, b + 1u)) return rc;
                     CK(cudaEventRecord(ctx->ev_join, ctx->side));
                 }
                 if (ctx->profile) {
@@ -2737,25 +2756,24 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                     ev_i += 2;
                 }
                 if (persistent) {
-                    CK(cudaMemsetAsync(ctx->cnt.p + 3, 0, 4, ctx->stream));
                     if (adj)
                         (proc ? k_transmit<false, true, true> : k_transmit<false, true, false>)
-                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax,
+                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, Pb, F.kmax,
                                                                                      ctx->d_sh_mats.p);
                     else
                         (counting ? k_transmit<false, false, false, true>
                                   : proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
-                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, Pb, F.kmax, nullptr);
                 } else if (S.use_wide) {
-                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
                 } else {
-                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
                 }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, sh_ev.back().second), ctx->stream));
                 if (adj)
-                    k_resolve<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, qs, srec);
+                    k_resolve<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, Pb, Batch{}, A, qs, srec);
                 else
-                    k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                    k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, Pb, Batch{},
                                                                                                     Adj{}, qs, srec);
             }
         }
@@ -3152,20 +3170,18 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
     CK(cudaMemsetAsync(P.stat, 0, 4 * sizeof(unsigned long long), ctx->stream));
     k_init_wave<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths);
     for (uint32_t s = 0; s < max_spp; ++s) {
-        CK(cudaMemsetAsync(P.cnt, 0, 4, ctx->stream));
+        // the counter ring (DPaths::cnt); k_camera appends the compacted queue to block 0
+        CK(cudaMemsetAsync(P.cnt, 0, 16 * sizeof(uint32_t), ctx->stream));
         k_camera<true><<<gp, 256, 0, ctx->stream>>>(F0, P, Bt, npaths, s);
         for (uint32_t b = 0; b < max_b; ++b) {
             const int qs = int(b & 1u);
+            const DPaths Pb = bounce_paths(P, b);
             if (b == 0u) {
-                CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
-                CK(cudaMemsetAsync(P.cnt + 2, 0, 8, ctx->stream));   // shadow queue + fetch counter
                 (proc ? k_closest<true, true> : k_closest<true, false>)<<<gpers, kThreads, 0, ctx->stream>>>(
-                    S0, Bt, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                    S0, Bt, P.q[qs], Pb.cnt, P.ray_o, P.ray_d, P.hit_t, P.hit_id, Pb.cnt + 2, P.stat);
             } else {
                 // this bounce's closest hits were traced on the side stream
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-                CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
-                CK(cudaMemsetAsync(P.cnt + 2, 0, 4, ctx->stream));
             }
             const size_t srec = size_t(s) * npaths;
             Adj A{};
@@ -3173,37 +3189,36 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
                 A = *adj;
                 A.srec_base = srec;
                 (proc ? k_shade<true, true, true> : k_shade<true, true, false>)
-                    <<<ctx->sm_count * 2, kShadeThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs, b);
+                    <<<ctx->sm_count * 2, kShadeThreads, smem, ctx->stream>>>(S0, F0, Pb, Bt, A, qs, b);
             } else {
                 // shading block: 512 threads (default) or 256 (autotuner); same grid in threads
                 if (ctx->b_tune.shade_threads == 256u)
                     (proc ? k_shade<true, false, true, 256> : k_shade<true, false, false, 256>)
-                        <<<gstream, 256, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+                        <<<gstream, 256, 0, ctx->stream>>>(S0, F0, Pb, Bt, Adj{}, qs, b);
                 else
                     (proc ? k_shade<true, false, true> : k_shade<true, false, false>)
-                        <<<(gstream + 1) / 2, kShadeThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, b);
+                        <<<(gstream + 1) / 2, kShadeThreads, 0, ctx->stream>>>(S0, F0, Pb, Bt, Adj{}, qs, b);
             }
             if (b + 1u < max_b) {
                 // fork: the next bounce's closest hits overlap this bounce's shadow rays
+                const DPaths Pn = bounce_paths(P, b + 1u);
                 CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
                 CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-                CK(cudaMemsetAsync(P.cnt + 4, 0, 4, ctx->side));
                 (proc ? k_closest<true, true> : k_closest<true, false>)<<<gpers, kThreads, 0, ctx->side>>>(
-                    S0, Bt, P.q[qs ^ 1], P.cnt + (qs ^ 1), P.ray_o, P.ray_d, P.hit_t, P.hit_id, P.cnt + 4, P.stat);
+                    S0, Bt, P.q[qs ^ 1], Pn.cnt, P.ray_o, P.ray_d, P.hit_t, P.hit_id, Pn.cnt + 2, P.stat);
                 CK(cudaEventRecord(ctx->ev_join, ctx->side));
             }
-            CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
             if (adj)
                 (proc ? k_transmit<true, true, true> : k_transmit<true, true, false>)
-                    <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, ctx->d_sh_mats.p);
+                    <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, Pb, kmax_any, ctx->d_sh_mats.p);
             else
                 (proc ? k_transmit<true, false, true> : k_transmit<true, false, false>)
-                    <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, P, kmax_any, nullptr);
+                    <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, Pb, kmax_any, nullptr);
             if (adj)
-                k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, qs,
+                k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, Pb, Bt, A, qs,
                                                                                           srec);
             else
-                k_resolve<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, qs, srec);
+                k_resolve<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, Pb, Bt, Adj{}, qs, srec);
         }
     }
     if (!adj) k_accumulate_batch<<<(npix_total + 255) / 256, 256, 0, ctx->stream>>>(P, Bt, npix_total);
@@ -3626,9 +3641,9 @@ constexpr size_t kNoAllocAlign = 256;
 constexpr size_t align_up(size_t v) { return (v + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
 constexpr size_t kNA_P = kNoAllocMaxPixels;
 // 6 float4 path arrays, 5 float4 x 3 shadow slots, 7 u32 path arrays, 1 u32 x 3 shadow queue,
-// 8 u32 counters, 4 u64 statistics
+// the 16 u32 queue counters (the ring of DPaths::cnt), 4 u64 statistics
 constexpr size_t kNoAllocBytes = 6 * align_up(16 * kNA_P) + 5 * align_up(16 * 3 * kNA_P) +
-                                 7 * align_up(4 * kNA_P) + align_up(4 * 3 * kNA_P) + align_up(32) +
+                                 7 * align_up(4 * kNA_P) + align_up(4 * 3 * kNA_P) + align_up(64) +
                                  align_up(32);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
@@ -3714,7 +3729,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
     P.q[0] = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
     P.q[1] = reinterpret_cast<uint32_t*>(take(4 * kNA_P));
     P.sq = reinterpret_cast<uint32_t*>(take(4 * 3 * kNA_P));
-    P.cnt = reinterpret_cast<uint32_t*>(take(32));
+    P.cnt = reinterpret_cast<uint32_t*>(take(64));   // the counter ring
     P.stat = reinterpret_cast<unsigned long long*>(take(32));
     P.wave = ctx->wave_vars.p;
     if (off > kNoAllocBytes) return set_err(ctx, PT_ERR_KERNEL, "render_noalloc: scratch layout overflow");
@@ -3774,30 +3789,27 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
             ctx->stats.kernel_launches += 1 + 4 * F.maxb;
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const int qs = int(b & 1u);
-                CK(cudaMemsetAsync(P.cnt + (qs ^ 1), 0, 4, ctx->stream));
-                CK(cudaMemsetAsync(P.cnt + 2, 0, 4, ctx->stream));
+                const DPaths Pb = bounce_paths(P, b);
                 if (persistent) {
-                    CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
                     (proc ? k_closest<false, true> : k_closest<false, false>)<<<gpers, kThreads, 0, ctx->stream>>>(
-                        S, Batch{}, P.q[qs], P.cnt + qs, P.ray_o, P.ray_d, P.hit_t, P.hit_id, P.cnt + 3, P.stat);
+                        S, Batch{}, P.q[qs], Pb.cnt, P.ray_o, P.ray_d, P.hit_t, P.hit_id, Pb.cnt + 2, P.stat);
                 } else if (S.use_wide) {
-                    k_extend<true><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
+                    k_extend<true><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, Pb, qs);
                 } else {
-                    k_extend<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, P, qs);
+                    k_extend<false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, Pb, qs);
                 }
                 (proc ? k_shade<false, false, true> : k_shade<false, false, false>)
-                    <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, P, Batch{},
+                    <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, Pb, Batch{},
                                                                                               Adj{}, qs, b);
                 if (persistent) {
-                    CK(cudaMemsetAsync(P.cnt + 3, 0, 4, ctx->stream));
                     (proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
-                        <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, P, F.kmax, nullptr);
+                        <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, Pb, F.kmax, nullptr);
                 } else if (S.use_wide) {
-                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
                 } else {
-                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, P, F.kmax);
+                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
                 }
-                k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
+                k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, Pb, Batch{}, Adj{},
                                                                                                 qs, 0);
                 ctx->stats.extend_launches++;
                 ctx->stats.shadow_launches++;
