@@ -273,6 +273,10 @@ struct DScene {
     const float4* env;           // W*H texels
     const float* marg;
     const float* cond;
+    // guide tables of the CDFs (kCdfGuide + 1 entries per array: the marginal,
+    // then row by row), or null: cdf_search's bracket for u in [k/K, (k+1)/K)
+    const uint32_t* marg_guide;
+    const uint32_t* cond_guide;
     uint32_t env_w, env_h;
     uint32_t hdri_count;
     float4 hdri_dir[8];

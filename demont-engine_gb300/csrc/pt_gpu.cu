@@ -50,6 +50,7 @@ constexpr uint32_t kEnded = 4u, kSkipSky = 1u, kPrevLambert = 2u;
 constexpr uint32_t kAmbBit = 1u << 8;   // shadow mask: the path has a skylight ambient term (P.amb)
 static_assert(ptb::kWideLeafBit == ptd::kLeafBit, "wide-node leaf codes must match the traversal's");
 constexpr int kThreads = 256;
+constexpr uint32_t kCdfGuide = 256;   // guide-table buckets per CDF (cdf_search)
 // k_transmit carries the dielectric-chain state besides the traversal state: at
 // 3 blocks of 256 per SM it needs no register spills (at 4 it spilled 230 bytes
 // per thread and ran 2% slower on the 1080p triangle scene).
@@ -388,8 +389,24 @@ __device__ V3 sky_env(const DScene& S, const DFrame& F, V3 rd) {
     return sky * F.env_intensity;
 }
 
-__device__ __forceinline__ uint32_t cdf_search(const float* cdf, uint32_t count, float u) {
+// The smallest i with cdf[i] >= u (count - 1 if none): a binary search over
+// the whole array, or, with a guide table g (g[k] = that index for u = k / K,
+// g[K] = count, K = kCdfGuide; built only for non-decreasing arrays), over
+// [g[k], g[k + 1]] for u in [k/K, (k+1)/K).  The index sought lies in that
+// bracket (the search is monotone in u), and the same comparisons inside it
+// give the same index, so the guide only removes dependent loads: about 3
+// steps on a 2048-texel row instead of 11 (Chen and Asau's guide-table
+// method).  u * K is exact (K is a power of two); negative or NaN u takes the
+// full search.
+__device__ __forceinline__ uint32_t cdf_search(const float* cdf, uint32_t count, float u,
+                                               const uint32_t* g = nullptr) {
     uint32_t lo = 0, hi = count;
+    const float uk = u * float(kCdfGuide);
+    if (g && uk >= 0.0f) {
+        const uint32_t k = uint32_t(fminf(uk, float(kCdfGuide - 1u)));
+        lo = __ldg(g + k);
+        hi = __ldg(g + k + 1u);
+    }
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (__ldg(cdf + mid) < u) lo = mid + 1;
@@ -408,8 +425,9 @@ __device__ void sample_env(const DScene& S, const DFrame& F, float xu, float xv,
     pdf = 0.0f;
     if (F.env_present == 0u || !(F.env_total > 0.0f)) return;
     const uint32_t w = S.env_w, hh = S.env_h;
-    const uint32_t vi = cdf_search(S.marg, hh, xv);
-    const uint32_t ui = cdf_search(S.cond + size_t(vi) * w, w, xu);
+    const uint32_t vi = cdf_search(S.marg, hh, xv, S.marg_guide);
+    const uint32_t ui = cdf_search(S.cond + size_t(vi) * w, w, xu,
+                                   S.cond_guide ? S.cond_guide + size_t(vi) * (kCdfGuide + 1u) : nullptr);
     const float u = (float(ui) + 0.5f) / float(w);
     const float v = (float(vi) + 0.5f) / float(hh);
     const float theta = v * kPi;
@@ -1479,6 +1497,8 @@ struct pt_gpu_ctx {
     DBuf<uint32_t> prim_type, prim_mat;
     bool has_prim_mat = false;
     DBuf<float> marg, cond;
+    DBuf<uint32_t> marg_guide, cond_guide;   // DScene::marg_guide / cond_guide
+    bool env_guided = false;
     uint32_t prim_count = 0, linear_count = 0, bvh_nodes = 0, tri_slots = 0, tri_nodes = 0, tri_count = 0;
     uint32_t mat_count = 0, light_count = 0, env_w = 0, env_h = 0, hdri_count = 0;
     bool mesh_has_mat = false;
@@ -1664,6 +1684,8 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     S.env = c->env.p;
     S.marg = c->marg.p;
     S.cond = c->cond.p;
+    S.marg_guide = c->env_guided ? c->marg_guide.p : nullptr;
+    S.cond_guide = c->env_guided ? c->cond_guide.p : nullptr;
     S.env_w = c->env_w;
     S.env_h = c->env_h;
     S.hdri_count = c->hdri_count;
@@ -1779,6 +1801,23 @@ int grid_for(pt_gpu_ctx* c, size_t work, int per_sm, int threads = kThreads) {
 }
 
 constexpr size_t kWavePaths = size_t(1) << 26;
+
+// cdf_search's guide table of one CDF of n values: g[k] = the smallest i with
+// cdf[i] >= k / kCdfGuide (n if none), g[kCdfGuide] = n.  False (no table) when
+// the array is not non-decreasing or holds a NaN: the bracket argument needs a
+// sorted array.
+bool build_cdf_guide(const float* cdf, uint32_t n, uint32_t* g) {
+    for (uint32_t i = 0; i < n; ++i)
+        if (!(cdf[i] == cdf[i]) || (i + 1u < n && !(cdf[i] <= cdf[i + 1u]))) return false;
+    uint32_t i = 0;
+    for (uint32_t k = 0; k < kCdfGuide; ++k) {
+        const float u = float(k) / float(kCdfGuide);
+        while (i < n && cdf[i] < u) ++i;
+        g[k] = i;
+    }
+    g[kCdfGuide] = n;
+    return true;
+}
 
 int ensure_wave(pt_gpu_ctx* ctx, size_t npaths) {
     if (ctx->cap >= npaths) return PT_OK;
@@ -2161,6 +2200,8 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
         dfree(*b);
     dfree(ctx->marg);
     dfree(ctx->cond);
+    dfree(ctx->marg_guide);
+    dfree(ctx->cond_guide);
     for (auto* b : {&ctx->a4, &ctx->a4_geo, &ctx->t4, &ctx->tri4, &ctx->tri_lo, &ctx->tri_hi}) dfree(*b);
     dfree(ctx->a4_meta);
     for (auto* b : {&ctx->m4, &ctx->mtri4, &ctx->ma4_geo}) dfree(*b);
@@ -2329,6 +2370,21 @@ int pt_gpu_upload_env(pt_gpu_ctx* ctx, const float* rgba, uint32_t W, uint32_t H
     if ((rc = dupload(ctx, ctx->env, rgba, size_t(W) * H)) || (rc = dupload(ctx, ctx->marg, marginal, H)) ||
         (rc = dupload(ctx, ctx->cond, conditional, size_t(W) * H)))
         return rc;
+    // guide tables for the env-sampling searches (cdf_search), when every CDF
+    // is non-decreasing (BuildEnvCdf's always are)
+    ctx->env_guided = false;
+    if (W && H) {
+        std::vector<uint32_t> mg(kCdfGuide + 1u), cg(size_t(H) * (kCdfGuide + 1u));
+        bool ok = build_cdf_guide(marginal, H, mg.data());
+        for (uint32_t v = 0; ok && v < H; ++v)
+            ok = build_cdf_guide(conditional + size_t(v) * W, W, cg.data() + size_t(v) * (kCdfGuide + 1u));
+        if (ok) {
+            if ((rc = dupload(ctx, ctx->marg_guide, mg.data(), mg.size())) ||
+                (rc = dupload(ctx, ctx->cond_guide, cg.data(), cg.size())))
+                return rc;
+            ctx->env_guided = true;
+        }
+    }
     ctx->env_w = W;
     ctx->env_h = H;
     ctx->hdri_count = n_hdri;

@@ -157,3 +157,53 @@ def test_denoiser_jitter_on_sample_zero(pt, orc, dev):
     assert np.array_equal(g1.view(np.uint32), o1.view(np.uint32))
     dev.render(head, prm, 1)
     assert not np.array_equal(g1, dev.read_accum())
+
+
+def _env_scene(pt):
+    """The plain analytic scene under a 64 x 32 environment with a dark band
+    (flat stretches in every row's CDF) and a small bright patch (a jump)."""
+    s = pt.Scene().synth(0, seed=2)
+    rng = np.random.default_rng(7)
+    env = rng.uniform(0.0, 0.4, (32, 64, 3)).astype(np.float32)
+    env[:, 20:30] = 0.0
+    env[5:7, 40:42] = 500.0
+    s.env(env)
+    return s
+
+
+def test_env_sampling_with_guide_tables(pt, orc, dev):
+    """Env samples through the CDF guide tables pick the texels the full binary
+    search picks: the render equals the oracle's bit for bit."""
+    s = _env_scene(pt)
+    g, o = _render_both(dev, orc, s, 48, 40, frames=3, frame_index=11)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_env_sampling_of_an_unsorted_cdf_takes_the_full_search(pt, orc, dev):
+    """A conditional row that is not non-decreasing gets no guide table; the
+    full binary search then gives the oracle's texels on the same arrays."""
+    import ctypes
+    s = _env_scene(pt)
+    W, H = 48, 40
+    head, prm = s.push(W, H, frame_index=3, reset=1)
+    p = s.packed()
+    ew, eh = p.env_w, p.env_h
+    rgba = np.ctypeslib.as_array(p.env_rgba, (eh * ew * 4,)).copy()
+    marg = np.ctypeslib.as_array(p.env_marginal, (eh,)).copy()
+    cond = np.ctypeslib.as_array(p.env_conditional, (eh * ew,)).copy().reshape(eh, ew)
+    row = int(np.argmax(np.diff(marg, prepend=0.0)))   # the likeliest row
+    cond[row, 10], cond[row, 40] = cond[row, 40], cond[row, 10]
+    assert (np.diff(cond[row]) < 0).any()
+    cond = np.ascontiguousarray(cond.ravel())
+    hd = np.ctypeslib.as_array(p.hdri_dir_pmf, (32,)).copy()
+    hc = np.ctypeslib.as_array(p.hdri_col, (32,)).copy()
+    fp = pt.fptr
+    dev.upload(s)
+    assert dev.lib.pt_gpu_upload_env(dev.h, fp(rgba), ew, eh, fp(marg), fp(cond), fp(hd), fp(hc),
+                                     p.hdri_count) == 0
+    dev.set_target(W, H)
+    dev.render(head, prm, 2)
+    g = dev.read_accum()
+    p.env_conditional = cond.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    o, _ = orc.render(p, head, prm, W, H, 2)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
