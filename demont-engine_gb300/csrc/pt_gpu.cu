@@ -937,8 +937,43 @@ __device__ __forceinline__ V3 safe_div(V3 a, V3 b) {
     return v3(b.x > 0.0f ? a.x / b.x : 0.0f, b.y > 0.0f ? a.y / b.y : 0.0f, b.z > 0.0f ? a.z / b.z : 0.0f);
 }
 
+// The NEE terms of a path's last vertex, once its shadow rays are traced: in
+// the reference order (light, env, HDRI; shaders/PathTrace.slang:6341-6520),
+// each ((((pre * T) * brdf) * s1) * s2) / pdf, clamped where the slot says so,
+// then the skylight ambient.  Run by k_shade for the paths of its queue (the
+// previous bounce's terms, before the vertex is shaded) and by k_finish for the
+// paths that ended.
+template <bool kB, bool kAdj>
+__device__ __forceinline__ V3 resolve_nee(const DScene& S0, const DFrame& F, const DPaths& P, const Batch& B,
+                                          const Adj& A, uint32_t p, uint32_t mask, V3 rad) {
+    for (int k = 0; k < 3; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const uint32_t e = 3u * p + uint32_t(k);
+        const V3 tr = v3(P.sh_tr[e]);
+        if (!any_pos(tr)) continue;
+        const float4 pre = P.sh_pre[e], br = P.sh_brdf[e];
+        const float s1 = P.sh_d[e].w;
+        const V3 c = v3(pre) * tr * v3(br) * s1 * pre.w / br.w;
+        rad = rad + (((mask >> (4 + k)) & 1u) ? clamp_ind(c, F.firefly) : c);
+        if (kAdj) {   // each dielectric the shadow ray crossed multiplied c by its albedo
+            const DScene& S = kB ? B.scenes[F.scene] : S0;
+            const uint4 xm = A.sh_mats[e];
+            const uint32_t ms[4] = {xm.x, xm.y, xm.z, xm.w};
+            const V3 g = adj_weight<kB>(A, F, p);
+            for (int j = 0; j < 4; ++j) {
+                if (ms[j] == kNoMat || S.mat_count == 0u) continue;
+                const uint32_t m = min(ms[j], S.mat_count - 1u);
+                adj_add(A, 0, m, g * safe_div(c, v3(__ldg(S.mats + 3u * m))));
+            }
+        }
+    }
+    if (mask & kAmbBit) rad = rad + v3(P.amb[p]);
+    return rad;
+}
+
+// (512-thread blocks are held to 64 registers: two blocks per SM)
 template <bool kB, bool kAdj, bool kProc = true, int kSB = kShadeThreads>
-__global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0,
+__global__ void __launch_bounds__(kSB, kSB == 512 ? 2 : 1) k_shade(const __grid_constant__ DScene S0,
                                                      const __grid_constant__ DFrame F0, DPaths P, Batch B,
                                                      const __grid_constant__ Adj A, int qsel, uint32_t b) {
     const uint32_t n = P.cnt[0];
@@ -967,6 +1002,12 @@ __global__ void __launch_bounds__(kSB) k_shade(const __grid_constant__ DScene S0
             uint32_t st = P.state[p];
             uint32_t seed = P.seed[p];
             const HitRec h{P.hit_t[p], P.hit_id[p]};
+            // the previous vertex's NEE terms (its shadow rays were traced by
+            // the last transmittance launch) before this vertex adds its own
+            if (b > 0u) {
+                const uint32_t pmask = P.shmask[p];
+                if (pmask) rad = resolve_nee<kB, kAdj>(S0, F, P, B, A, p, pmask, rad);
+            }
             bool ended = false;
             if (h.id == kMiss) {
                 if (F.mis != 0u && (st & kPrevLambert)) {
@@ -1225,53 +1266,27 @@ __global__ void __launch_bounds__(kThreads, kTransmitBlocks) k_transmit(const __
     warp_add(P.stat + 1, done);
 }
 
-// NEE terms in the reference order (light, env, HDRI), then the sample's
-// radiance for paths that ended (shaders/PathTrace.slang:6341-6520, 7701).
+// End of a sample: the paths that ended (at any bounce) get their last
+// vertex's NEE terms and add the sample's radiance to the frame sum
+// (shaders/PathTrace.slang:7701); differentiable records keep it per sample.
+// An ended path's shadow slots and mask are its own and no later launch of the
+// sample writes them, so resolving here gives the values the path had when it
+// ended.  One thread per path slot of the wave; batched views with fewer
+// samples than this one (their paths were not restarted) are skipped.
 template <bool kB, bool kAdj>
-__global__ void k_resolve(const __grid_constant__ DScene S0, const __grid_constant__ DFrame F0, DPaths P, Batch B,
-                          const __grid_constant__ Adj A, int qsel, size_t srec_base) {
-    const uint32_t n = P.cnt[0];
-    const uint32_t* q = P.q[qsel];
-    const uint32_t n_iter = (n + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
+__global__ void k_finish(const __grid_constant__ DScene S0, const __grid_constant__ DFrame F0, DPaths P, Batch B,
+                         const __grid_constant__ Adj A, uint32_t npaths, uint32_t s, size_t srec_base) {
     if (kAdj) adj_begin(A);
-    for (uint32_t it = 0; it < n_iter; ++it) {
-        const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        if (i >= n) continue;
-        const uint32_t p = q[i];
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npaths; p += gridDim.x * blockDim.x) {
         const DFrame& F = kB ? B.views[B.path_view[p]] : F0;
+        if (kB && s >= F.spp) continue;
+        if (!(P.state[p] & kEnded)) continue;
         const uint32_t mask = P.shmask[p];
-        const uint32_t st = P.state[p];
-        if (mask == 0u && !(st & kEnded)) continue;
-        float4 r4 = P.rad[p];
-        V3 rad = v3(r4);
-        for (int k = 0; k < 3; ++k) {
-            if (!((mask >> k) & 1u)) continue;
-            const uint32_t e = 3u * p + uint32_t(k);
-            const V3 tr = v3(P.sh_tr[e]);
-            if (!any_pos(tr)) continue;
-            const float4 pre = P.sh_pre[e], br = P.sh_brdf[e];
-            const float s1 = P.sh_d[e].w;
-            const V3 c = v3(pre) * tr * v3(br) * s1 * pre.w / br.w;
-            rad = rad + (((mask >> (4 + k)) & 1u) ? clamp_ind(c, F.firefly) : c);
-            if (kAdj) {   // each dielectric the shadow ray crossed multiplied c by its albedo
-                const DScene& S = kB ? B.scenes[F.scene] : S0;
-                const uint4 xm = A.sh_mats[e];
-                const uint32_t ms[4] = {xm.x, xm.y, xm.z, xm.w};
-                const V3 g = adj_weight<kB>(A, F, p);
-                for (int j = 0; j < 4; ++j) {
-                    if (ms[j] == kNoMat || S.mat_count == 0u) continue;
-                    const uint32_t m = min(ms[j], S.mat_count - 1u);
-                    adj_add(A, 0, m, g * safe_div(c, v3(__ldg(S.mats + 3u * m))));
-                }
-            }
-        }
-        if (mask & kAmbBit) rad = rad + v3(P.amb[p]);
-        if (mask) P.rad[p] = f4(rad, 0.0f);
-        if (st & kEnded) {
-            const float4 fs = P.fsum[p];
-            P.fsum[p] = make_float4(fs.x + rad.x, fs.y + rad.y, fs.z + rad.z, 0.0f);
-            if (P.srad) P.srad[srec_base + p] = f4(rad, 0.0f);
-        }
+        V3 rad = v3(P.rad[p]);
+        if (mask) rad = resolve_nee<kB, kAdj>(S0, F, P, B, A, p, mask, rad);
+        const float4 fs = P.fsum[p];
+        P.fsum[p] = make_float4(fs.x + rad.x, fs.y + rad.y, fs.z + rad.z, 0.0f);
+        if (P.srad) P.srad[srec_base + p] = f4(rad, 0.0f);
     }
     if (kAdj) adj_end(A);
 }
@@ -2702,7 +2717,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         // counting sort), and the 48 KB default bounds static + dynamic together
         CK(cudaFuncSetAttribute(k_shade<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         CK(cudaFuncSetAttribute(k_shade<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        CK(cudaFuncSetAttribute(k_resolve<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_finish<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     }
     P.srad = (dr.mode == RunMode::kRecord) ? ctx->d_srad.p : nullptr;
     // fixed roulette probabilities: recorded by one plain render, read back by
@@ -2799,8 +2814,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                                                                                                   Adj{}, qs, b);
                 if (overlap && b + 1u < F.maxb) {
                     // fork: the next bounce's rays (written by k_shade) are traced
-                    // while this bounce's shadow rays are; k_resolve touches
-                    // neither the rays nor the hits
+                    // while this bounce's shadow rays are
                     CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
                     CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
                     if (int rc = launch_extend(ctx->side, b + 1u)) return rc;
@@ -2826,12 +2840,14 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
                 }
                 if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, sh_ev.back().second), ctx->stream));
-                if (adj)
-                    k_resolve<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, Pb, Batch{}, A, qs, srec);
-                else
-                    k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, Pb, Batch{},
-                                                                                                    Adj{}, qs, srec);
             }
+            // the paths' last NEE terms and the sample's radiance (the next
+            // bounce's k_shade resolved those of the paths that went on)
+            if (adj)
+                k_finish<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, npaths, s, srec);
+            else
+                k_finish<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
+                                                                                               npaths, s, srec);
         }
         if (!adj)
             k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf, prm->accum_ema_alpha);
@@ -2857,7 +2873,7 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         } else if (int rc = issue_wave(f0, nf)) {
             return rc;
         }
-        ctx->stats.kernel_launches += (adj ? 2u : 3u) + F.spp * (1u + 4u * F.maxb);
+        ctx->stats.kernel_launches += (adj ? 2u : 3u) + F.spp * (2u + 3u * F.maxb);
         ctx->stats.extend_launches += F.spp * F.maxb;
         ctx->stats.shadow_launches += F.spp * F.maxb;
         ctx->stats.waves++;
@@ -3270,11 +3286,16 @@ int issue_batch_wave(pt_gpu_ctx* ctx, const Batch& Bt, const DPaths& P, uint32_t
             else
                 (proc ? k_transmit<true, false, true> : k_transmit<true, false, false>)
                     <<<gtr, kThreads, 0, ctx->stream>>>(S0, Bt, Pb, kmax_any, nullptr);
-            if (adj)
-                k_resolve<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, Pb, Bt, A, qs,
-                                                                                          srec);
-            else
-                k_resolve<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, Pb, Bt, Adj{}, qs, srec);
+        }
+        // the paths' last NEE terms and the sample's radiance
+        const size_t srec = size_t(s) * npaths;
+        if (adj) {
+            Adj A = *adj;
+            A.srec_base = srec;
+            k_finish<true, true><<<ctx->sm_count * 4, kThreads, smem, ctx->stream>>>(S0, F0, P, Bt, A, npaths, s,
+                                                                                     srec);
+        } else {
+            k_finish<true, false><<<gstream, kThreads, 0, ctx->stream>>>(S0, F0, P, Bt, Adj{}, npaths, s, srec);
         }
     }
     if (!adj) k_accumulate_batch<<<(npix_total + 255) / 256, 256, 0, ctx->stream>>>(P, Bt, npix_total);
@@ -3456,7 +3477,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
         // counting sort), and the 48 KB default bounds static + dynamic together
         CK(cudaFuncSetAttribute(k_shade<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         CK(cudaFuncSetAttribute(k_shade<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        CK(cudaFuncSetAttribute(k_resolve<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        CK(cudaFuncSetAttribute(k_finish<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         A.srad = ctx->d_srad.p;
         A.dldi = dr.dldi;
         A.grad = ctx->d_grad.p;
@@ -3472,7 +3493,7 @@ int batch_waves(pt_gpu_ctx* ctx, pt_gpu_ctx* const* scenes, uint32_t n_scenes, c
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     ctx->stats = PtStats{};
     unsigned long long tot_ext = 0, tot_sh = 0;
-    const uint32_t launches_per_wave = 2 + max_spp * (1 + 4 * max_b);
+    const uint32_t launches_per_wave = 2 + max_spp * (2 + 3 * max_b);
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     for (uint32_t f = 0; f < frames; ++f) {
         for (uint32_t i = 0; i < n_views; ++i) {
@@ -3842,7 +3863,7 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
         ctx->stats.kernel_launches += 3;
         for (uint32_t s = 0; s < F.spp; ++s) {
             k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
-            ctx->stats.kernel_launches += 1 + 4 * F.maxb;
+            ctx->stats.kernel_launches += 2 + 3 * F.maxb;
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const int qs = int(b & 1u);
                 const DPaths Pb = bounce_paths(P, b);
@@ -3865,11 +3886,11 @@ extern "C" int pt_gpu_render_noalloc(pt_gpu_ctx* ctx, const PtPushHead* head, co
                 } else {
                     k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
                 }
-                k_resolve<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, Pb, Batch{}, Adj{},
-                                                                                                qs, 0);
                 ctx->stats.extend_launches++;
                 ctx->stats.shadow_launches++;
             }
+            k_finish<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
+                                                                                           npaths, s, 0);
         }
         k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, accum, nf, prm->accum_ema_alpha);
         ctx->stats.waves++;
