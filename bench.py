@@ -130,15 +130,18 @@ def shade_bytes_per_vertex(scene):
     step of the two CDF binary searches) and the HDRI-cluster pick (a direction
     + pmf and a colour float4, 32 B); at a miss, the bilinear sky lookup (four
     16-B texels) and the MIS pdf texel (16 B).  No analytic lights in this
-    workload."""
+    workload.  cdf_search_guided_B: what the two searches read with this
+    library's CDF guide tables (an 8-B bracket per search, then about
+    log2(n / 256) + 1 steps)."""
     import math
     a = scene.arrays()
     h, w = a["env_conditional"].shape
     search = 4 * (math.ceil(math.log2(h)) + math.ceil(math.log2(w)))
+    guided = sum(8 + 4 * (math.ceil(math.log2(max(n / 256, 1))) + 1) for n in (h, w))
     lambert = 48 + 16 + search + (32 if a["hdri_count"] else 0)
     miss = 4 * 16 + 16
     hdri = " + HDRI pick 32" if a["hdri_count"] else ""
-    return {"lambert_hit": lambert, "miss": miss, "unit": "B",
+    return {"lambert_hit": lambert, "miss": miss, "unit": "B", "cdf_search_guided_B": guided,
             "terms": f"material 48 + env texel 16 + CDF searches {search}{hdri}; "
                      f"miss: 4 bilinear texels 64 + pdf texel 16"}
 
