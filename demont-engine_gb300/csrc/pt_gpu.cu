@@ -1518,6 +1518,10 @@ struct pt_gpu_ctx {
     // shadow rays of the current bounce run on `stream` (fork/join by events)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // small waves run as two halves at once: the second half on its own pair of
+    // streams (stream2 + side2, the same fork/join), started and joined by events
+    cudaStream_t stream2 = nullptr, side2 = nullptr;
+    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr, ev_split = nullptr, ev_half = nullptr;
     // scene
     DBuf<float4> prim_rec, prim_geo, bvh, tri, tri_bvh, mats, lights, env;
     DBuf<uint32_t> prim_type, prim_mat;
@@ -1827,6 +1831,8 @@ int grid_for(pt_gpu_ctx* c, size_t work, int per_sm, int threads = kThreads) {
 }
 
 constexpr size_t kWavePaths = size_t(1) << 26;
+// waves of at most this many paths run as two concurrent halves (render_waves)
+constexpr size_t kSplitWavePaths = size_t(1) << 23;
 
 // cdf_search's guide table of one CDF of n values: g[k] = the smallest i with
 // cdf[i] >= k / kCdfGuide (n if none), g[kCdfGuide] = n.  False (no table) when
@@ -2188,15 +2194,19 @@ int pt_gpu_create(pt_gpu_ctx** out, int device_ordinal) {
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device_ordinal);
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->side2, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ctx->ev_fork2, &ctx->ev_join2, &ctx->ev_split, &ctx->ev_half})
+        CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     CK(cudaEventCreate(&ctx->ev0));
     CK(cudaEventCreate(&ctx->ev1));
     CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     int rc = dalloc(ctx, ctx->err_word, 1);
     if (rc) { *out = ctx; return rc; }
-    rc = dalloc(ctx, ctx->cnt, 16);   // the counter ring (DPaths::cnt)
+    rc = dalloc(ctx, ctx->cnt, 32);   // the counter rings (DPaths::cnt) of the two half-waves
     if (rc) { *out = ctx; return rc; }
-    rc = dalloc(ctx, ctx->wave_vars, 4);
+    rc = dalloc(ctx, ctx->wave_vars, 8);   // DPaths::wave of the two half-waves
     if (rc) { *out = ctx; return rc; }
     rc = dalloc(ctx, ctx->stat, 4);
     if (rc) { *out = ctx; return rc; }
@@ -2212,6 +2222,8 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     if (!ctx) return PT_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+    if (ctx->side2) cudaStreamSynchronize(ctx->side2);
     for (auto* b : {&ctx->prim_rec, &ctx->prim_geo, &ctx->bvh, &ctx->tri, &ctx->tri_bvh, &ctx->mats,
                     &ctx->lights, &ctx->env, &ctx->accum, &ctx->ray_o, &ctx->ray_d, &ctx->thr,
                     &ctx->rad, &ctx->fsum, &ctx->amb, &ctx->sh_o, &ctx->sh_d, &ctx->sh_pre, &ctx->sh_brdf,
@@ -2252,6 +2264,10 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    for (cudaEvent_t e : {ctx->ev_fork2, ctx->ev_join2, ctx->ev_split, ctx->ev_half})
+        if (e) cudaEventDestroy(e);
+    if (ctx->side2) cudaStreamDestroy(ctx->side2);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -2765,18 +2781,18 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     const int ge = grid_for(ctx, size_t(fpw) * F.npix, 8);
     std::vector<std::pair<size_t, size_t>> ext_ev, sh_ev;
     size_t ev_i = 0;
-    auto launch_extend = [&](cudaStream_t st, uint32_t b) -> int {
+    auto launch_extend = [&](const DPaths& PP, cudaStream_t st, uint32_t b) -> int {
         if (ctx->profile) {
             ext_ev.emplace_back(ev_i, ev_i + 1);
             CK(cudaEventRecord(pool_event(ctx, ev_i++), st));
             ++ev_i;
         }
         const int qs = int(b & 1u);
-        const DPaths Pb = bounce_paths(P, b);
+        const DPaths Pb = bounce_paths(PP, b);
         if (persistent) {
             (counting ? k_closest<false, false, true> : proc ? k_closest<false, true> : k_closest<false, false>)
-                <<<gpers, kThreads, 0, st>>>(S, Batch{}, P.q[qs], Pb.cnt, P.ray_o, P.ray_d, P.hit_t, P.hit_id,
-                                             Pb.cnt + 2, P.stat);
+                <<<gpers, kThreads, 0, st>>>(S, Batch{}, PP.q[qs], Pb.cnt, PP.ray_o, PP.ray_d, PP.hit_t, PP.hit_id,
+                                             Pb.cnt + 2, PP.stat);
         } else if (S.use_wide) {
             k_extend<true><<<ge, kThreads, 0, st>>>(S, Pb, qs);
         } else {
@@ -2786,82 +2802,85 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         return PT_OK;
     };
 
-    // work a failed earlier call left on the side stream finishes first
-    CK(cudaEventRecord(ctx->ev_join, ctx->side));
-    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+    // work a failed earlier call left on the side streams finishes first
+    for (cudaStream_t st : {ctx->side, ctx->stream2, ctx->side2}) {
+        CK(cudaEventRecord(ctx->ev_join, st));
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+    }
     CK(cudaMemsetAsync(ctx->stat.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->err_word.p, 0, 4, ctx->stream));
     if (counting) CK(cudaMemsetAsync(ctx->tcount.p, 0, 16 * sizeof(unsigned long long), ctx->stream));
     ctx->stats = PtStats{};
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     const Nvtx nv_render(adj ? "pt_gpu adjoint replay" : "pt_gpu_render");
-    // one wave's launches, on ctx->stream (the next bounce's closest hits forked to ctx->side)
-    auto issue_wave = [&](uint32_t f0, uint32_t nf) -> int {
+    // The samples and bounces of nf frames whose path state is PP, on stream st
+    // (the next bounce's closest hits forked to sd through the events evf / evj).
+    // PP's per-path arrays start at the first of those frames.
+    auto issue_paths = [&](const DPaths& PP, cudaStream_t st, cudaStream_t sd, cudaEvent_t evf, cudaEvent_t evj,
+                           uint32_t f0, uint32_t nf) -> int {
         const uint32_t npaths = nf * F.npix;
         const int gp = (npaths + 255) / 256;
-        k_init_wave<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths);
+        DPaths Pw = PP;
+        k_init_wave<false><<<gp, 256, 0, st>>>(F, Pw, Batch{}, npaths);
         for (uint32_t s = 0; s < F.spp; ++s) {
             const Nvtx nv_sample("sample %u", s);
             const size_t srec = size_t(s) * total_paths + size_t(f0) * F.npix;
             A.srec_base = srec;
-            P.rr_frozen = rr_fix ? ctx->rr_buf.p + srec * F.maxb : nullptr;
-            k_camera<false><<<gp, 256, 0, ctx->stream>>>(F, P, Batch{}, npaths, s);
+            Pw.rr_frozen = rr_fix ? ctx->rr_buf.p + srec * F.maxb : nullptr;
+            k_camera<false><<<gp, 256, 0, st>>>(F, Pw, Batch{}, npaths, s);
             for (uint32_t b = 0; b < F.maxb; ++b) {
                 const Nvtx nv_bounce("bounce %u", b);
                 const int qs = int(b & 1u);
-                const DPaths Pb = bounce_paths(P, b);
+                const DPaths Pb = bounce_paths(Pw, b);
                 if (b == 0u || !overlap) {
-                    if (int rc = launch_extend(ctx->stream, b)) return rc;
+                    if (int rc = launch_extend(Pw, st, b)) return rc;
                 } else {
                     // this bounce's closest hits were traced on the side stream
-                    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+                    CK(cudaStreamWaitEvent(st, evj, 0));
                 }
                 if (adj)
                     (proc ? k_shade<false, true, true> : k_shade<false, true, false>)
-                        <<<gadj / 2, kShadeThreads, smem, ctx->stream>>>(S, F, Pb, Batch{}, A, qs, b);
+                        <<<gadj / 2, kShadeThreads, smem, st>>>(S, F, Pb, Batch{}, A, qs, b);
                 else
                     (proc ? k_shade<false, false, true> : k_shade<false, false, false>)
-                        <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, ctx->stream>>>(S, F, Pb, Batch{},
-                                                                                                  Adj{}, qs, b);
+                        <<<grid_for(ctx, npaths, 4, kShadeThreads), kShadeThreads, 0, st>>>(S, F, Pb, Batch{},
+                                                                                            Adj{}, qs, b);
                 if (overlap && b + 1u < F.maxb) {
                     // fork: the next bounce's rays (written by k_shade) are traced
                     // while this bounce's shadow rays are
-                    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
-                    CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-                    if (int rc = launch_extend(ctx->side, b + 1u)) return rc;
-                    CK(cudaEventRecord(ctx->ev_join, ctx->side));
+                    CK(cudaEventRecord(evf, st));
+                    CK(cudaStreamWaitEvent(sd, evf, 0));
+                    if (int rc = launch_extend(Pw, sd, b + 1u)) return rc;
+                    CK(cudaEventRecord(evj, sd));
                 }
                 if (ctx->profile) {
                     sh_ev.emplace_back(ev_i, ev_i + 1);
-                    CK(cudaEventRecord(pool_event(ctx, ev_i), ctx->stream));
+                    CK(cudaEventRecord(pool_event(ctx, ev_i), st));
                     ev_i += 2;
                 }
                 if (persistent) {
                     if (adj)
                         (proc ? k_transmit<false, true, true> : k_transmit<false, true, false>)
-                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, Pb, F.kmax,
-                                                                                     ctx->d_sh_mats.p);
+                            <<<gtr, kThreads, 0, st>>>(S, Batch{}, Pb, F.kmax, ctx->d_sh_mats.p);
                     else
                         (counting ? k_transmit<false, false, false, true>
                                   : proc ? k_transmit<false, false, true> : k_transmit<false, false, false>)
-                            <<<gtr, kThreads, 0, ctx->stream>>>(S, Batch{}, Pb, F.kmax, nullptr);
+                            <<<gtr, kThreads, 0, st>>>(S, Batch{}, Pb, F.kmax, nullptr);
                 } else if (S.use_wide) {
-                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
+                    k_shadow<true><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, st>>>(S, Pb, F.kmax);
                 } else {
-                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, ctx->stream>>>(S, Pb, F.kmax);
+                    k_shadow<false><<<grid_for(ctx, 3 * size_t(npaths), 8), kThreads, 0, st>>>(S, Pb, F.kmax);
                 }
-                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, sh_ev.back().second), ctx->stream));
+                if (ctx->profile) CK(cudaEventRecord(pool_event(ctx, sh_ev.back().second), st));
             }
             // the paths' last NEE terms and the sample's radiance (the next
             // bounce's k_shade resolved those of the paths that went on)
             if (adj)
-                k_finish<false, true><<<gadj, kThreads, smem, ctx->stream>>>(S, F, P, Batch{}, A, npaths, s, srec);
+                k_finish<false, true><<<gadj, kThreads, smem, st>>>(S, F, Pw, Batch{}, A, npaths, s, srec);
             else
-                k_finish<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, ctx->stream>>>(S, F, P, Batch{}, Adj{},
-                                                                                               npaths, s, srec);
+                k_finish<false, false><<<grid_for(ctx, npaths, 8), kThreads, 0, st>>>(S, F, Pw, Batch{}, Adj{},
+                                                                                       npaths, s, srec);
         }
-        if (!adj)
-            k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf, prm->accum_ema_alpha);
         return PT_OK;
     };
     // With render graphs on, plain renders replay each wave as a CUDA graph: a
@@ -2870,13 +2889,55 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
     // graph of the same structure is updated in place (or a new one
     // instantiated).
     const bool use_graph = ctx->render_graphs && ctx->profile == 0 && dr.mode == RunMode::kRender;
+    // A small wave (C0's 256 x 256 frames: 4 M paths) spends a large share of
+    // each sample-bounce step in the ramp and drain of its four dependent
+    // launches.  It runs as two halves of its frames at once, the second half on
+    // the second stream pair with its own queues, counters and frame index, so
+    // that one half's launches fill the SMs the other's tails leave idle.  The
+    // halves touch disjoint path slots and frames; the running mean is applied
+    // after both, in frame order, so the image is the same bit for bit.
+    auto split_wave = [&](uint32_t nf) {
+        return dr.mode == RunMode::kRender && !rr_fix && ctx->profile == 0 && !use_graph && overlap && persistent &&
+               nf >= 2u && size_t(nf) * F.npix <= kSplitWavePaths;
+    };
+    // one wave's launches, on ctx->stream (and, split, on ctx->stream2)
+    auto issue_wave = [&](uint32_t f0, uint32_t nf) -> int {
+        if (!split_wave(nf)) {
+            if (int rc = issue_paths(P, ctx->stream, ctx->side, ctx->ev_fork, ctx->ev_join, f0, nf)) return rc;
+        } else {
+            const uint32_t na = (nf + 1u) / 2u;
+            const size_t off = size_t(na) * F.npix;
+            DPaths P2 = P;
+            for (float4** a : {&P2.ray_o, &P2.ray_d, &P2.thr, &P2.rad, &P2.fsum, &P2.amb}) *a += off;
+            for (uint32_t** a : {&P2.seed, &P2.state, &P2.hit_id, &P2.shmask, &P2.q[0], &P2.q[1]}) *a += off;
+            P2.hit_t += off;
+            for (float4** a : {&P2.sh_o, &P2.sh_d, &P2.sh_pre, &P2.sh_brdf, &P2.sh_tr}) *a += 3 * off;
+            P2.sq += 3 * off;
+            P2.cnt = ctx->cnt.p + 16;
+            P2.wave = ctx->wave_vars.p + 4;
+            CK(cudaEventRecord(ctx->ev_split, ctx->stream));
+            CK(cudaStreamWaitEvent(ctx->stream2, ctx->ev_split, 0));
+            if (int rc = issue_paths(P, ctx->stream, ctx->side, ctx->ev_fork, ctx->ev_join, f0, na)) return rc;
+            if (int rc = issue_paths(P2, ctx->stream2, ctx->side2, ctx->ev_fork2, ctx->ev_join2, f0 + na, nf - na))
+                return rc;
+            CK(cudaEventRecord(ctx->ev_half, ctx->stream2));
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_half, 0));
+        }
+        if (!adj)
+            k_accumulate<<<(F.npix + 255) / 256, 256, 0, ctx->stream>>>(F, P, ctx->accum.p, nf, prm->accum_ema_alpha);
+        return PT_OK;
+    };
     for (uint32_t f0 = 0; f0 < frames; f0 += fpw) {
         const Nvtx nv_wave("wave from frame %u", f0);
         const uint32_t nf = std::min(fpw, frames - f0);
         const uint32_t npaths = nf * F.npix;
+        const bool split = split_wave(nf);
         F.nframes = nf;
         k_set_wave<<<1, 1, 0, ctx->stream>>>(ctx->wave_vars.p, head->frame_index + f0, head->frame_index,
                                              f0 == 0 && head->reset_accum != 0u);
+        if (split)   // the second half's frame index (its reset flag is not read)
+            k_set_wave<<<1, 1, 0, ctx->stream>>>(ctx->wave_vars.p + 4, head->frame_index + f0 + (nf + 1u) / 2u,
+                                                 head->frame_index, 0u);
         if (use_graph) {
             if (int rc = launch_wave_graph(ctx, issue_wave, f0, nf, F, S, P, prm->accum_ema_alpha, rr_fix, proc,
                                            persistent, overlap))
@@ -2884,9 +2945,10 @@ int render_waves(pt_gpu_ctx* ctx, const PtPushHead* head, const PtPathParams* pr
         } else if (int rc = issue_wave(f0, nf)) {
             return rc;
         }
-        ctx->stats.kernel_launches += (adj ? 2u : 3u) + F.spp * (2u + 3u * F.maxb);
-        ctx->stats.extend_launches += F.spp * F.maxb;
-        ctx->stats.shadow_launches += F.spp * F.maxb;
+        const uint32_t halves = split ? 2u : 1u;
+        ctx->stats.kernel_launches += (adj ? 1u : 2u) + (split ? 1u : 0u) + halves * (1u + F.spp * (2u + 3u * F.maxb));
+        ctx->stats.extend_launches += halves * F.spp * F.maxb;
+        ctx->stats.shadow_launches += halves * F.spp * F.maxb;
         ctx->stats.waves++;
         ctx->stats.paths += uint64_t(npaths) * F.spp;
     }
