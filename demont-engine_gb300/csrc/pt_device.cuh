@@ -248,6 +248,7 @@ constexpr uint32_t kMatLambert = 0u, kMatMetal = 1u, kMatDielectric = 2u;
 constexpr uint32_t kMiss = 0xFFFFFFFFu;
 constexpr uint32_t kTriBit = 1u << 30;
 constexpr uint32_t kMergedTri = 1u << 29;   // with kTriBit: the slot is in the merged tree's triangle order
+constexpr uint32_t kRefTri = 1u << 28;      // with kTriBit: the slot is in the reference BVH's order (S.tri)
 constexpr uint32_t kTraverseCap = 1u << 22;   // loop-iteration cap per query (error word if hit)
 
 struct DScene {
@@ -315,6 +316,13 @@ struct DScene {
     const float4* mtri4;
     const float4* ma4_geo;
     const uint4* ma4_meta;
+    // the reference BVH leaf (node index) that holds each item, or kMiss for an
+    // item no reference leaf holds: triangles in wide-leaf order (t_leaf) and in
+    // the merged tree's order (m_leaf), analytic records by record index minus
+    // linear_count (a_leaf); null when not built
+    const uint32_t* t_leaf;
+    const uint32_t* m_leaf;
+    const uint32_t* a_leaf;
     // traversal counters of the counting kernel variants (profiling mode 3), or null:
     // [0..7] extension segments, [8..15] shadow segments, each (segments, wide nodes
     // tested, triangles tested, analytic prims tested in wide leaves, linear prims
@@ -1127,14 +1135,103 @@ __device__ __forceinline__ float isect_geo(uint32_t type, float4 g, V3 ro, V3 rd
     return -1.0f;
 }
 
+// The reference walk tests an item only when the slab test of the reference
+// BVH leaf that holds it passes (shaders/PathTrace.slang:2321-2329, 2408-2433,
+// 2592-2636); the leaf's ancestors then pass too, because their boxes contain
+// the leaf's and the slab arithmetic is monotonic in the planes.  The wide
+// trees' boxes are padded outward, so they can reach an item whose unpadded
+// reference leaf the ray only grazes and the reference's rounding rejects (on
+// the 256 x 256 analytic scene: one primary ray in about a million, at a box's
+// outer edge).  Such a hit is not the reference's.  The persistent kernels then
+// trace the segment again with every candidate checked here before it is
+// accepted, which finds the closest item the reference walk reaches: the
+// reference's answer; trace_wide asks the reference walk itself (reference_hit).
+//
+// Rounding can empty the slab interval only where the ray's exact passage
+// through the leaf box is within rounding of empty: the hit point then lies
+// within rounding of a face of the leaf box in an axis where the box is not
+// flat, and since the leaf box contains the item's own box, within rounding of
+// a face of the item's own box too (the flat axes of the item, a triangle lying
+// in a plane of constant x, y or z, are flat or interior for the leaf as well).
+// So the leaf is fetched only when the hit point lies within eps of a face of
+// the item's own box, eps = 2^-16 (|ro| + |p| + t) per axis, far above the few
+// ulps the slab test can lose; everywhere else the hit is the reference's.
+// The slab test of the reference leaf that holds item `id` (no pre-filter):
+// the check of every candidate while a segment is traced again.
+__device__ __forceinline__ bool ref_leaf_slab(const DScene& S, uint32_t id, V3 ro, V3 inv) {
+    uint32_t leaf = kMiss;
+    const float4* nodes;
+    if (id & kTriBit) {
+        leaf = __ldg(((id & kMergedTri) ? S.m_leaf : S.t_leaf) + (id & ~(kTriBit | kMergedTri)));
+        nodes = S.tri_bvh;
+    } else {
+        if (S.bvh_nodes == 0u || id < S.linear_count) return true;
+        leaf = __ldg(S.a_leaf + (id - S.linear_count));
+        nodes = S.bvh;
+    }
+    if (leaf == kMiss) return false;
+    return slab(ro, inv, __ldg(nodes + 2u * leaf), __ldg(nodes + 2u * leaf + 1u), __uint_as_float(0x7F800000u));
+}
+__device__ __forceinline__ bool near_own_face(float pv, float lo, float hi, float eps) {
+    return hi > lo && (pv - lo <= eps || hi - pv <= eps);
+}
+__device__ __forceinline__ bool ref_leaf_accepts(const DScene& S, uint32_t id, float t, V3 ro, V3 rd, V3 inv) {
+    if (id == kMiss || (id & kSdfBit)) return true;
+    uint32_t leaf;
+    const float4* nodes;
+    if (id & kTriBit) {
+        // reference-order slots come from the reference walk itself
+        if ((id & kRefTri) || S.tri_bvh == nullptr || !(S.t_wide || (id & kMergedTri))) return true;
+        const uint32_t p = id & ~(kTriBit | kMergedTri);
+        const uint32_t* L = (id & kMergedTri) ? S.m_leaf : S.t_leaf;
+        if (L == nullptr) return true;
+        // one axis at a time, the next one read only when this one is clear:
+        // few registers are live where the traversal state still is
+        const float* T = reinterpret_cast<const float*>(((id & kMergedTri) ? S.mtri4 : S.tri4) + 3u * p);
+        const float k = 1.52587890625e-5f;   // 2^-16
+        bool near = false;
+#pragma unroll 1
+        for (int a = 0; a < 3 && !near; ++a) {
+            const float o = (a == 0) ? ro.x : ((a == 1) ? ro.y : ro.z);
+            const float d = (a == 0) ? rd.x : ((a == 1) ? rd.y : rd.z);
+            const float v0 = __ldg(T + a), v1 = v0 + __ldg(T + 4 + a), v2 = v0 + __ldg(T + 8 + a);
+            const float hp = o + d * t;
+            near = near_own_face(hp, fminf(fminf(v0, v1), v2), fmaxf(fmaxf(v0, v1), v2), k * (fabsf(o) + fabsf(hp) + t));
+        }
+        if (!near) return true;
+        leaf = __ldg(L + p);
+        nodes = S.tri_bvh;
+    } else {
+        if (!S.a_wide || S.bvh_nodes == 0u || id < S.linear_count || S.a_leaf == nullptr) return true;
+        const float4 g = __ldg(S.prim_geo + id);
+        if (__ldg(S.prim_type + id) == 0u) {   // sphere: centre +- radius
+            const V3 hp = ro + rd * t;
+            const float k = 1.52587890625e-5f;
+            const V3 c = v3(g);
+            if (!near_own_face(hp.x, c.x - g.w, c.x + g.w, k * (fabsf(ro.x) + fabsf(hp.x) + t)) &&
+                !near_own_face(hp.y, c.y - g.w, c.y + g.w, k * (fabsf(ro.y) + fabsf(hp.y) + t)) &&
+                !near_own_face(hp.z, c.z - g.w, c.z + g.w, k * (fabsf(ro.z) + fabsf(hp.z) + t)))
+                return true;
+        }
+        leaf = __ldg(S.a_leaf + (id - S.linear_count));
+        nodes = S.bvh;
+    }
+    if (leaf == kMiss) return false;
+    return slab(ro, inv, __ldg(nodes + 2u * leaf), __ldg(nodes + 2u * leaf + 1u), __uint_as_float(0x7F800000u));
+}
 // One leaf of a wide tree: triangles of `tri4` (kTri) or analytic records of
 // ageo / ameta.  first_mask selects the first-item field of the leaf code
 // (the merged tree keeps its record-leaf flag above it); triangle hits are
 // reported as kTriBit | id_tag | slot.
+// With refS set (a segment traced again because its first walk ended on a hit
+// the reference walk does not reach), a candidate is accepted only when the
+// slab test of its reference leaf passes (ref_leaf_slab; inv is the ray's
+// safe_inv); with refS null, inv is not read.
 template <bool kTri>
 __device__ __forceinline__ void wide_leaf(const float4* tri4, const float4* ageo, const uint4* ameta, uint32_t code,
                                           V3 ro, V3 rd, Best& b, uint32_t key_base,
-                                          uint32_t first_mask = 0x0FFFFFFFu, uint32_t id_tag = 0u) {
+                                          uint32_t first_mask = 0x0FFFFFFFu, uint32_t id_tag = 0u,
+                                          const DScene* refS = nullptr, V3 inv = V3{0.0f, 0.0f, 0.0f}) {
     const uint32_t first = code & first_mask;
     const uint32_t cnt = ((code >> 28) & 7u) + 1u;
     for (uint32_t k = 0; k < cnt; ++k) {
@@ -1156,7 +1253,8 @@ __device__ __forceinline__ void wide_leaf(const float4* tri4, const float4* ageo
             if (v < 0.0f || u + v > 1.0f) continue;
             const float tt = dot(e2, qv) * inv_det;
             const uint32_t key = key_base | __float_as_uint(c.w);
-            if (tt > 1e-3f && better(tt, key, b)) {
+            if (tt > 1e-3f && better(tt, key, b) &&
+                (refS == nullptr || ref_leaf_slab(*refS, kTriBit | id_tag | p, ro, inv))) {
                 b.t = tt;
                 b.key = key;
                 b.id = kTriBit | id_tag | p;
@@ -1165,7 +1263,8 @@ __device__ __forceinline__ void wide_leaf(const float4* tri4, const float4* ageo
             const float4 g = __ldg(ageo + p);
             const uint4 m = __ldg(ameta + p);
             const float t = isect_geo(m.y, g, ro, rd);
-            if (t > 1e-3f && better(t, m.z, b)) {
+            if (t > 1e-3f && better(t, m.z, b) &&
+                (refS == nullptr || ref_leaf_slab(*refS, m.x, ro, inv))) {
                 b.t = t;
                 b.key = m.z;
                 b.id = m.x;
@@ -1294,6 +1393,13 @@ __device__ __forceinline__ void wide_walk(const DScene& S, const float4* nodes, 
     }
 }
 
+// the reference walk's hit, triangle slots flagged as reference order
+__device__ __noinline__ HitRec reference_hit(const DScene& S, V3 ro, V3 rd, float t_init) {
+    HitRec h = trace_closest(S, ro, rd, t_init, 7u);
+    if (h.id != kMiss && !(h.id & kSdfBit) && (h.id & kTriBit)) h.id |= kRefTri;
+    return h;
+}
+
 // traceScene on the wide trees (analytic part falls back to the reference walk
 // when its wide tree is not built).
 __device__ __noinline__ HitRec trace_wide(const DScene& S, V3 ro, V3 rd, float t_init) {
@@ -1343,6 +1449,7 @@ __device__ __noinline__ HitRec trace_wide(const DScene& S, V3 ro, V3 rd, float t
             }
         }
     }
+    if (!ref_leaf_accepts(S, b.id, b.t, ro, rd, inv)) return reference_hit(S, ro, rd, t_init);
     return HitRec{b.t, b.id};
 }
 
@@ -1401,8 +1508,8 @@ __device__ __forceinline__ Surface surface_at(const DScene& S, V3 ro, V3 rd, Hit
         s.emission = v3(0.0f, 0.0f, 0.0f);
         s.mid = kNoMat;
     } else if (h.id & kTriBit) {
-        const uint32_t slot = h.id & ~(kTriBit | kMergedTri);
-        const float4* T = (h.id & kMergedTri) ? S.mtri4 : (S.t_wide ? S.tri4 : S.tri);
+        const uint32_t slot = h.id & ~(kTriBit | kMergedTri | kRefTri);
+        const float4* T = (h.id & kMergedTri) ? S.mtri4 : ((S.t_wide && !(h.id & kRefTri)) ? S.tri4 : S.tri);
         const float4 b = __ldg(T + 3u * slot + 1u);
         const float4 c = __ldg(T + 3u * slot + 2u);
         s.normal = normalize(cross(v3(b), v3(c)));
@@ -1560,6 +1667,11 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
     int seg = 0;
     uint32_t xm[4] = {kNoMat, kNoMat, kNoMat, kNoMat};   // dielectric rows crossed (adjoint)
     TravCount tc;   // counting variants only
+    // the segment is being traced again with every candidate checked against
+    // its reference leaf (ref_leaf_accepts): its first walk ended on a hit the
+    // reference walk does not reach
+    bool refmode = false;
+    bool redo = false;   // extension rays: the fetch step starts this lane's ray again, in refmode
 
     // SDF clusters, once the analytic part of the best hit is final
     auto sdf_pass = [&]() {
@@ -1572,7 +1684,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
             b.id = id;
         }
     };
-    auto start_segment = [&]() {
+    auto start_segment = [&](bool count) {
         inv = safe_inv(rd);
         nx = -ro.x * inv.x;
         ny = -ro.y * inv.y;
@@ -1583,7 +1695,7 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
         const uint32_t linear = Sp->wide_linear;
         const float4* pg = Sp->prim_geo;
         const uint32_t* pty = Sp->prim_type;
-        if (kCount) {
+        if (kCount && count) {
             tc.seg += 1;
             tc.linear += linear;
         }
@@ -1618,23 +1730,26 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 sp = 1;
             }
         }
-        ++done;
+        if (count) ++done;
     };
 
     for (;;) {
-        const bool need = !active && !exhausted;
+        const bool need = !active && !exhausted && !redo;
         const uint32_t m = __ballot_sync(FULL, need);
+        uint32_t base = 0;
         if (m) {
             const int leader = __ffs(m) - 1;
-            uint32_t base = 0;
             if (lane == leader) base = atomicAdd(fetch_ctr, uint32_t(__popc(m)));
             base = __shfl_sync(FULL, base, leader);
-            if (need) {
-                const uint32_t slot = base + uint32_t(__popc(m & ((1u << lane) - 1u)));
-                if (slot >= n) {
+        }
+        if (need || redo) {
+            {
+                const uint32_t slot = need ? base + uint32_t(__popc(m & ((1u << lane) - 1u))) : 0u;
+                if (need && slot >= n) {
                     exhausted = true;
                 } else {
-                    item = queue[slot];
+                    // a new ray, or (redo) this lane's own ray again
+                    if (need) item = queue[slot];
                     if (kBatch) Sp = isc.table + isc.path_scene[kShadow ? item / 3u : item];
                     has_a = Sp->a_wide && Sp->prim_count > Sp->linear_count;
                     has_t = Sp->t_wide && Sp->tri_enabled != 0u && Sp->tri_nodes > 0u;
@@ -1649,7 +1764,9 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                         seg = 0;
                         if (kMats) xm[0] = xm[1] = xm[2] = xm[3] = kNoMat;
                     }
-                    start_segment();
+                    refmode = redo;
+                    start_segment(!redo);
+                    redo = false;
                     active = true;
                 }
             }
@@ -1713,21 +1830,41 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                 if (rec_leaf) tc.aprims += cnt;
                 else tc.tris += cnt;
             }
+            const DScene* refS = refmode ? Sp : nullptr;
             if (phase == 5) {
-                if (rec_leaf) wide_leaf<false>(Sp->mtri4, Sp->ma4_geo, Sp->ma4_meta, leaf, ro, rd, b, 0u, 0x07FFFFFFu);
-                else wide_leaf<true>(Sp->mtri4, Sp->ma4_geo, Sp->ma4_meta, leaf, ro, rd, b, 0x80000000u, 0x07FFFFFFu,
-                                     kMergedTri);
+                if (rec_leaf)
+                    wide_leaf<false>(Sp->mtri4, Sp->ma4_geo, Sp->ma4_meta, leaf, ro, rd, b, 0u, 0x07FFFFFFu, 0u, refS,
+                                     inv);
+                else
+                    wide_leaf<true>(Sp->mtri4, Sp->ma4_geo, Sp->ma4_meta, leaf, ro, rd, b, 0x80000000u, 0x07FFFFFFu,
+                                    kMergedTri, refS, inv);
             } else if (phase == 1) {
-                wide_leaf<false>(Sp->tri4, Sp->a4_geo, Sp->a4_meta, leaf, ro, rd, b, 0u);
+                wide_leaf<false>(Sp->tri4, Sp->a4_geo, Sp->a4_meta, leaf, ro, rd, b, 0u, 0x0FFFFFFFu, 0u, refS, inv);
             } else {
-                wide_leaf<true>(Sp->tri4, Sp->a4_geo, Sp->a4_meta, leaf, ro, rd, b, 0x80000000u);
+                wide_leaf<true>(Sp->tri4, Sp->a4_geo, Sp->a4_meta, leaf, ro, rd, b, 0x80000000u, 0x0FFFFFFFu, 0u, refS,
+                                inv);
             }
             leaf = 0u;
         }
         // end of a tree
         if (active && leaf == 0u && sp == 0) {
             if (phase == 1 && Sp->sdf_count) sdf_pass();
-            if (phase == 1 && has_t) {
+            const bool last_tree = !(phase == 1 && has_t);
+            if (last_tree && !refmode && !ref_leaf_accepts(*Sp, b.id, b.t, ro, rd, inv)) {
+                // a hit the reference walk does not reach: the same segment
+                // again, each candidate checked before it is accepted (the
+                // segment is not counted twice).  Shadow segments restart in
+                // place (their chain state stays in registers); an extension
+                // ray is restarted by the fetch step, whose segment set-up it
+                // shares, which keeps this kernel's registers as they were.
+                if (kShadow) {
+                    refmode = true;
+                    start_segment(false);
+                } else {
+                    redo = true;
+                    active = false;
+                }
+            } else if (!last_tree) {
                 phase = 2;
                 nodes = Sp->t4;
                 st[0] = make_uint2(0u, __float_as_uint(-3.0e38f));
@@ -1762,7 +1899,8 @@ __device__ __forceinline__ void persistent_closest(const DScene* S0, ItemScenes 
                             rd = normalize(refr);
                             t_max = fmaxf(t_max - adv, 0.0f);
                             ++seg;
-                            start_segment();
+                            refmode = false;
+                            start_segment(true);
                             finished = false;
                         }
                     }

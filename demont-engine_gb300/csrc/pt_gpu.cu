@@ -713,6 +713,11 @@ __global__ void k_gather_prims(const float4* geo, const uint32_t* type, const ui
     m4[p] = make_uint4(slot, type[slot], linear + rank[k], 0u);
 }
 
+__global__ void k_gather_u32(const uint32_t* src, const uint32_t* order, uint32_t n, uint32_t* dst) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) dst[p] = src[order[p]];
+}
+
 __global__ void k_iota(uint32_t* a, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = i;
@@ -1467,8 +1472,8 @@ __global__ void k_probe_ids(DScene S, uint32_t n, uint32_t* hit, float* t) {
     if (i >= n) return;
     uint32_t id = hit[i];
     if (id != kMiss && (id & kTriBit) && !(id & kSdfBit)) {
-        const float4* T = (id & kMergedTri) ? S.mtri4 : S.tri4;
-        id = kTriBit | __float_as_uint(T[3u * (id & ~(kTriBit | kMergedTri))].w);
+        const float4* T = (id & kMergedTri) ? S.mtri4 : ((id & kRefTri) ? S.tri : S.tri4);
+        id = kTriBit | __float_as_uint(T[3u * (id & ~(kTriBit | kMergedTri | kRefTri))].w);
     }
     hit[i] = id;
     if (id == kMiss) t[i] = 0.0f;
@@ -1482,8 +1487,9 @@ __global__ void k_trace_probe(DScene S, const float4* ro, const float4* rd, uint
     const float tinit = (d.w > 0.0f) ? d.w : 1e30f;
     const HitRec h = trace_any_mode(S, v3(o), v3(d), tinit, S.use_wide != 0u);
     uint32_t id = h.id;
-    if (id != kMiss && (id & kTriBit)) {
-        const float4 a = (S.use_wide && S.t_wide) ? S.tri4[3u * (id & ~kTriBit)] : S.tri[3u * (id & ~kTriBit)];
+    if (id != kMiss && (id & kTriBit) && !(id & kSdfBit)) {
+        const uint32_t slot = id & ~(kTriBit | kRefTri);
+        const float4 a = (S.use_wide && S.t_wide && !(id & kRefTri)) ? S.tri4[3u * slot] : S.tri[3u * slot];
         id = kTriBit | __float_as_uint(a.w);
     }
     hit[i] = id;
@@ -1545,6 +1551,9 @@ struct pt_gpu_ctx {
     DBuf<uint32_t> wave_vars;   // DPaths::wave
     // reference tie ranks of the wide trees' items (kept for the merged tree)
     DBuf<uint32_t> t_rank, a_rank;
+    // the reference BVH leaf of each item (DScene::t_leaf / m_leaf / a_leaf);
+    // tslot_leaf: per triangle slot of the reference order, gathered into the wide orders
+    DBuf<uint32_t> t_leaf, m_leaf, a_leaf, tslot_leaf;
     // merged 4-wide tree over the triangles and the finite analytic records
     bool m_wide = false;
     DBuf<float4> m4, mtri4, ma4_geo;
@@ -1753,6 +1762,9 @@ DScene make_scene(pt_gpu_ctx* c, const PtPathParams* prm) {
     S.mtri4 = c->mtri4.p;
     S.ma4_geo = c->ma4_geo.p;
     S.ma4_meta = c->ma4_meta.p;
+    S.t_leaf = c->t_leaf.p;
+    S.m_leaf = c->m_leaf.p;
+    S.a_leaf = c->a_leaf.p;
     if (prm) {
         // the push tail decides what the kernel walks (bvh_params), as in the reference
         S.linear_count = prm->bvh_params[0];
@@ -2007,6 +2019,20 @@ int gpu_build_tree(pt_gpu_ctx* ctx, const float4* lo, const float4* hi, uint32_t
     return PT_OK;
 }
 
+// The reference BVH leaf (node index) holding each of n_items items (leaf
+// ranges left_first .. left_first + count - 1); kMiss for an item no leaf holds.
+std::vector<uint32_t> ref_item_leaf(const PtBvhNode* nodes, uint32_t n_nodes, uint32_t n_items) {
+    std::vector<uint32_t> leaf(n_items, kMiss);
+    for (uint32_t i = 0; i < n_nodes; ++i) {
+        if (nodes[i].count == 0u) continue;
+        for (uint32_t k = 0; k < nodes[i].count; ++k) {
+            const uint64_t it = uint64_t(nodes[i].left_first) + k;
+            if (it < n_items) leaf[size_t(it)] = i;
+        }
+    }
+    return leaf;
+}
+
 // Wide tree over the triangle slots of the uploaded (reference) mesh BVH.
 int build_wide_mesh(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref, uint32_t n_slots) {
     ctx->t_wide = false;
@@ -2023,13 +2049,16 @@ int build_wide_mesh(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref,
     const int depth = ptb::collapse4(bin, wide);
     ctx->t4_bin_nodes = uint32_t(bin.size());
     if (depth < 0 || 3 * depth + 1 > kWideStackDev) { dfree(order); return PT_OK; }
+    const std::vector<uint32_t> sleaf = ref_item_leaf(ref_nodes, n_ref, n_slots);
     if ((rc = dupload(ctx, ctx->t_rank, rank.data(), n_slots)) || (rc = dalloc(ctx, ctx->tri4, 3 * size_t(n_slots))) ||
-        (rc = dupload(ctx, ctx->t4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
+        (rc = dupload(ctx, ctx->t4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8)) ||
+        (rc = dupload(ctx, ctx->tslot_leaf, sleaf.data(), n_slots)) || (rc = dalloc(ctx, ctx->t_leaf, n_slots))) {
         dfree(order);
         return rc;
     }
     k_gather_tris<<<(n_slots + 255) / 256, 256, 0, ctx->stream>>>(ctx->tri.p, order.p, ctx->t_rank.p, n_slots,
                                                                  ctx->tri4.p);
+    k_gather_u32<<<(n_slots + 255) / 256, 256, 0, ctx->stream>>>(ctx->tslot_leaf.p, order.p, n_slots, ctx->t_leaf.p);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     dfree(order);
     if (e != cudaSuccess) return set_err(ctx, PT_ERR_CUDA, std::string("gather tris: ") + cudaGetErrorString(e));
@@ -2061,8 +2090,9 @@ int build_wide_prims(pt_gpu_ctx* ctx, const PtBvhNode* ref_nodes, uint32_t n_ref
     std::vector<ptb::Wide4> wide;
     const int depth = ptb::collapse4(bin, wide);
     if (depth < 0 || 3 * depth + 1 > kWideStackDev) { cleanup(); return PT_OK; }
+    const std::vector<uint32_t> aleaf = ref_item_leaf(ref_nodes, n_ref, nf);
     if ((rc = dupload(ctx, drank, rank.data(), nf)) || (rc = dalloc(ctx, ctx->a4_geo, nf)) ||
-        (rc = dalloc(ctx, ctx->a4_meta, nf)) ||
+        (rc = dalloc(ctx, ctx->a4_meta, nf)) || (rc = dupload(ctx, ctx->a_leaf, aleaf.data(), nf)) ||
         (rc = dupload(ctx, ctx->a4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
         cleanup();
         return rc;
@@ -2092,7 +2122,7 @@ constexpr uint32_t kPrimLeafFlag = 1u << 27;
 int build_wide_merged(pt_gpu_ctx* ctx) {
     ctx->m_wide = false;
     ctx->m4_count = 0;
-    if (!ctx->t_wide || !ctx->a_wide || !ctx->t_rank.p || !ctx->a_rank.p) return PT_OK;
+    if (!ctx->t_wide || !ctx->a_wide || !ctx->t_rank.p || !ctx->a_rank.p || !ctx->tslot_leaf.p) return PT_OK;
     const uint32_t n_t = ctx->tri_slots, n_a = ctx->prim_count - ctx->linear_count;
     if (n_t == 0 || n_a == 0 || n_t >= kPrimLeafFlag || n_a >= kPrimLeafFlag) return PT_OK;
     const uint32_t n = n_t + n_a;
@@ -2148,12 +2178,14 @@ int build_wide_merged(pt_gpu_ctx* ctx) {
     if (depth < 0 || 3 * depth + 1 > kWideStackDev) { cleanup(); return PT_OK; }
     if ((rc = dupload(ctx, tperm, tp.data(), n_t)) || (rc = dupload(ctx, pperm, pp.data(), n_a)) ||
         (rc = dalloc(ctx, ctx->mtri4, 3 * size_t(n_t))) || (rc = dalloc(ctx, ctx->ma4_geo, n_a)) ||
+        (rc = dalloc(ctx, ctx->m_leaf, n_t)) ||
         (rc = dalloc(ctx, ctx->ma4_meta, n_a)) ||
         (rc = dupload(ctx, ctx->m4, reinterpret_cast<const float4*>(wide.data()), wide.size() * 8))) {
         cleanup();
         return rc;
     }
     k_gather_tris<<<(n_t + 255) / 256, 256, 0, ctx->stream>>>(ctx->tri.p, tperm.p, ctx->t_rank.p, n_t, ctx->mtri4.p);
+    k_gather_u32<<<(n_t + 255) / 256, 256, 0, ctx->stream>>>(ctx->tslot_leaf.p, tperm.p, n_t, ctx->m_leaf.p);
     k_gather_prims<<<(n_a + 255) / 256, 256, 0, ctx->stream>>>(ctx->prim_geo.p, ctx->prim_type.p, pperm.p,
                                                              ctx->a_rank.p, ctx->linear_count, n_a, ctx->ma4_geo.p,
                                                              ctx->ma4_meta.p);
@@ -2246,6 +2278,7 @@ int pt_gpu_destroy(pt_gpu_ctx* ctx) {
     dfree(ctx->ma4_meta);
     dfree(ctx->t_rank);
     dfree(ctx->a_rank);
+    for (auto* b : {&ctx->t_leaf, &ctx->m_leaf, &ctx->a_leaf, &ctx->tslot_leaf}) dfree(*b);
     dfree(ctx->hit_t);
     dfree(ctx->stat);
     dfree(ctx->tcount);

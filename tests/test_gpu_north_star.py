@@ -15,12 +15,18 @@ C-ABI.
 2. Closest-hit ids on the rays a render really traces.  The fp32 oracle
    records the extension rays of bounce 0 and bounce 1 of every sample of
    whole frames (oracle_capture_rays; these are the GPU render's own rays, bit
-   for bit), 2^20 rays per case.  The reference-order walk of the reference BVHs
-   (traversal mode 1) must return the oracle's hit ids and distances exactly;
-   the 4-wide SAH trees (mode 0, the default) must agree on >= 99.99% of hit
-   ids, with t within 1e-5 relative where they agree.  The two modes differ
-   only where the reference's unpadded slab test rounds tmax below tmin at a
-   box corner and drops a true hit (the wide boxes are padded)."""
+   for bit), 2^20 rays per case.  Both the reference-order walk of the reference
+   BVHs (traversal mode 1) and the 4-wide SAH trees (mode 0, the default) must
+   return the oracle's hit ids and distances exactly (the bar is 99.99%).  The
+   wide trees' boxes are padded, so they reach hits that the reference's
+   unpadded slab test rounds away where a ray grazes a box's edge; the wide
+   kernels re-trace such a segment with the reference walk.
+
+3. The whole 256 x 256 analytic workload: 64 frames of 16 spp in one call
+   (4.2 M paths, 116 M segments), in the default mode, against the fp32 oracle
+   over the same frames: the same segment counts and the same image bit for
+   bit.  Two of its primary rays graze box 2's outer edge and are pinned on
+   their own."""
 import numpy as np
 import pytest
 
@@ -105,10 +111,49 @@ def test_hit_ids_on_the_rays_a_render_traces(pt, orc, dev, scenes, config, W, H,
     dev.upload(s)
     w_hit, w_t = dev.trace(ro, rd)
     agree = w_hit == o_hit
-    hit = agree & (o_hit != 0xFFFFFFFF)
-    rel = np.abs(w_t[hit].astype(np.float64) - o_t[hit]) / np.maximum(np.abs(o_t[hit]), 1e-30)
     print(f"config {config} bounce {bounce}: {N_RAYS} rays, {int((o_hit != 0xFFFFFFFF).sum())} hits, "
-          f"wide-tree hit-id agreement {agree.mean():.7f} ({int((~agree).sum())} differ), "
-          f"max t rel diff {rel.max() if rel.size else 0.0:.3g}")
-    assert agree.mean() >= 0.9999, f"hit-id agreement {agree.mean():.7f}"
-    assert rel.size == 0 or rel.max() <= 1e-5
+          f"wide-tree hit-id agreement {agree.mean():.7f} ({int((~agree).sum())} differ)")
+    np.testing.assert_array_equal(w_hit, o_hit)
+    np.testing.assert_array_equal(w_t, o_t)
+
+
+# Primary rays of the 256 x 256 analytic scene (seed 0; frames 1 and 58, from
+# the camera at (0, 0, 28)) that pass within rounding of box 2's outer edge
+# y = -7.6174984: triangle 25 reports a hit (u + v = 1 - 6e-8 and 1 - 2.4e-7),
+# but the reference's slab test of the leaf holding it rounds the ray out, so
+# the reference walk, and the oracle, report a miss
+EDGE_RAYS = np.array([[-0.289293110370636, -0.25726765394210815, -0.9220210909843445, 0.0],
+                      [-0.16045163571834564, -0.26527756452560425, -0.9507277011871338, 0.0]], np.float32)
+
+
+def test_rays_grazing_a_reference_leaf_edge(pt, orc, dev):
+    s = pt.Scene().synth(0, seed=0)
+    head, prm = s.push(256, 256, frame_index=0, reset=1)
+    ro = np.tile(np.array([[0.0, 0.0, 28.0, 0.0]], np.float32), (len(EDGE_RAYS), 1))
+    o_hit, o_t, _ = orc.trace(s.packed(), head, prm, ro, EDGE_RAYS)
+    assert (o_hit == 0xFFFFFFFF).all()
+    for mode in (0, 1):
+        dev.set_traversal(mode)
+        dev.upload(s)
+        hit, t = dev.trace(ro, EDGE_RAYS)
+        np.testing.assert_array_equal(hit, o_hit)
+        np.testing.assert_array_equal(t, o_t)
+    dev.set_traversal(0)
+
+
+def test_whole_analytic_workload_matches_the_oracle(pt, orc, dev):
+    s = pt.Scene().synth(0, seed=0)
+    W = H = 256
+    frames = 64
+    head, prm = s.push(W, H, frame_index=0, reset=1)
+    dev.set_traversal(0)
+    dev.upload(s)
+    dev.set_target(W, H)
+    dev.render(head, prm, frames)
+    st = dev.stats()
+    gpu = dev.read_accum()
+    want, c = orc.render(s.packed(), head, prm, W, H, frames)
+    print(f"256 x 256 x {head.spp} spp x {frames} frames: GPU {st.extension_rays} + {st.shadow_rays} segments, "
+          f"oracle {c.ext_rays} + {c.shadow_rays}")
+    assert (st.extension_rays, st.shadow_rays) == (c.ext_rays, c.shadow_rays)
+    np.testing.assert_array_equal(gpu, want)

@@ -99,27 +99,27 @@ def test_trace_shared_vertex_ties_reference_walk_is_bit_exact(pt, orc, dev):
 
 
 def test_trace_shared_vertex_ties_wide_tree(pt, orc, dev):
-    """Equal distances on several triangles are resolved by the reference rank:
-    the wide tree returns exactly the reference's first-tested-wins result over
-    every triangle the reference intersector accepts.  (The reference walk itself
-    can additionally lose a triangle whose box the ray only touches at a corner,
-    where its unpadded slab test rounds tmax below tmin; the wide tree's padded
-    boxes never cull a true hit, so those rays legitimately differ from the
-    reference walk and the test compares against the brute-force rule.)"""
+    """Equal distances on several triangles are resolved by the reference rank,
+    and a triangle whose reference leaf box the ray only touches at a corner
+    (these rays aim at grid vertices, so about one in five does),
+    where the reference's unpadded slab test rounds tmax below tmin and the
+    reference walk never tests it, is dropped as the reference drops it: the
+    wide tree returns the reference walk's (the oracle's) hits exactly.  Against
+    the brute-force first-tested-wins rule over every triangle the intersector
+    accepts, the rays that differ are exactly those corner cases, where the
+    brute force keeps a hit the reference walk does not."""
     s, xs = grid_mesh_scene(pt)
     ro, rd = vertex_rays(xs, 1500, 9)
-    dev.set_traversal(0)
-    dev.upload(s)
-    g_hit, g_t = dev.trace(ro, rd)
-    want_hit, want_t = first_tested_wins(s.arrays(), ro, rd)
-    np.testing.assert_array_equal(g_hit, want_hit)
-    np.testing.assert_array_equal(g_t, want_t)
+    o_hit = check_trace(pt, orc, dev, s, ro, rd, mode=0)
+    want_hit, _ = first_tested_wins(s.arrays(), ro, rd)
+    corner = np.flatnonzero(o_hit != want_hit)
+    print(f"{corner.size} of {len(ro)} rays lose a corner-touched triangle in the reference walk")
+    assert (want_hit[corner] != 0xFFFFFFFF).all()
 
 
 def test_trace_full_c1_rays_agreement(pt, orc, dev):
-    """2^17 camera + 2^17 random rays of the full 2.46 M-triangle scene: the
-    reference walk is bit-exact, the wide tree agrees on >= 99.99 % of hit ids
-    with t within 1e-5 relative."""
+    """2^17 camera + 2^17 random rays of the full 2.46 M-triangle scene: both
+    the reference walk and the wide tree return the oracle's hits bit for bit."""
     s = pt.Scene().synth(1, seed=0)
     W, H = 1920, 1080
     head, prm = s.push(W, H)
@@ -142,10 +142,8 @@ def test_trace_full_c1_rays_agreement(pt, orc, dev):
     dev.set_traversal(0)
     dev.upload(s)
     g_hit, g_t = dev.trace(ro, rd)
-    agree = g_hit == o_hit
-    assert agree.mean() >= 0.9999, f"hit-id agreement {agree.mean():.6f}"
-    hit = agree & (o_hit != 0xFFFFFFFF)
-    np.testing.assert_allclose(g_t[hit], o_t[hit], rtol=1e-5)
+    np.testing.assert_array_equal(g_hit, o_hit)
+    np.testing.assert_array_equal(g_t, o_t)
 
 
 def render_both(pt, orc, dev, s, W, H, frames, mode=0):
