@@ -278,7 +278,9 @@ int pt_gpu_get_traversal_stats(pt_gpu_ctx* ctx, PtTraversalStats* out);
 /* Traversal structure: 0 (default) = 4-wide SAH trees built on the device at
  * upload from the same primitives (hit ids and distances still follow the
  * reference's first-tested-wins order exactly, via per-primitive reference
- * ranks); 1 = walk the uploaded reference BVHs in the reference's own order. */
+ * ranks, and a hit is kept only where the slab test of its reference BVH leaf
+ * passes, as the reference walk requires before it tests the primitive);
+ * 1 = walk the uploaded reference BVHs in the reference's own order. */
 int pt_gpu_set_traversal(pt_gpu_ctx* ctx, int mode);
 
 /* Failure-path testing: lower the per-query traversal iteration cap (default
