@@ -781,8 +781,8 @@ def main():
                     "pushes and pops, ray in and hit out) x extension segments per launch / average launch "
                     "time (CUDA events, stages serial).  Most of these bytes are L1/L2 hits: ray in and hit "
                     "out (dram_compulsory_frac) are the only bytes that must reach DRAM; the scene (~350 MB) "
-                    "exceeds L2, so part of the node and triangle traffic does too (ncu DRAM bytes per "
-                    "launch: DESIGN.md).  traffic is null: no ncu capture runs inside the bench.",
+                    "exceeds L2, so part of the node and triangle traffic does too (an ncu capture of one "
+                    "launch measures it).  traffic is null: no ncu capture runs inside the bench.",
             "step_share": {"k_closest": ext_ms / max(1e3 * t_serial, 1e-9),
                            "k_transmit": sh_ms / max(1e3 * t_serial, 1e-9),
                            "serial_ms_per_step": 1e3 * t_serial / args.steps}}
